@@ -1,0 +1,224 @@
+/*
+ * gbblas.h -- C ABI of libgbblas, a GB300 (sm_103a) implementation of
+ * OpenBLAS's level-3 BLAS and blocked-LAPACK hot path.
+ *
+ * Part 1 declares the drop-in entry points with exactly the prototypes of
+ * OpenBLAS's cblas.h and Fortran-77 interface (column-major, transpose and
+ * leading-dimension semantics, xerbla error reporting, LAPACK `info`).  Each
+ * declaration names the reference interface it replaces (paths relative to
+ * the OpenBLAS source tree).  These entry points take HOST pointers, copy
+ * operands to the GPU, compute there and copy results back before returning
+ * (blocking BLAS semantics).  Pointers that are already device memory are
+ * detected and used in place.
+ *
+ * Part 2 declares device-pointer variants (gb_*_dev) that only enqueue work
+ * on the library stream, plus control functions (stream, precision mode,
+ * error state).  No entry point takes framework-specific types: plain
+ * pointers, 32/64-bit integers and an opaque stream handle.
+ */
+#ifndef GBBLAS_H
+#define GBBLAS_H
+
+#include <stdint.h>
+
+#if defined(__GNUC__)
+#pragma GCC visibility push(default)
+#endif
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int blasint; /* common.h:270-277 (32-bit unless INTERFACE64) */
+
+/* cblas.h:62-66 */
+enum CBLAS_ORDER { CblasRowMajor = 101, CblasColMajor = 102 };
+enum CBLAS_TRANSPOSE { CblasNoTrans = 111, CblasTrans = 112, CblasConjTrans = 113,
+                       CblasConjNoTrans = 114 };
+enum CBLAS_UPLO { CblasUpper = 121, CblasLower = 122 };
+enum CBLAS_DIAG { CblasNonUnit = 131, CblasUnit = 132 };
+enum CBLAS_SIDE { CblasLeft = 141, CblasRight = 142 };
+typedef enum CBLAS_ORDER CBLAS_ORDER;
+typedef enum CBLAS_TRANSPOSE CBLAS_TRANSPOSE;
+typedef enum CBLAS_UPLO CBLAS_UPLO;
+typedef enum CBLAS_DIAG CBLAS_DIAG;
+typedef enum CBLAS_SIDE CBLAS_SIDE;
+
+/* ======================================================================= */
+/* Part 1: drop-in entry points (host pointers, blocking)                   */
+/* ======================================================================= */
+
+/* replaces cblas_dgemm, interface/gemm.c:294-651 (cblas.h:300-301) */
+void cblas_dgemm(enum CBLAS_ORDER Order, enum CBLAS_TRANSPOSE TransA,
+                 enum CBLAS_TRANSPOSE TransB, blasint M, blasint N, blasint K,
+                 double alpha, const double *A, blasint lda, const double *B,
+                 blasint ldb, double beta, double *C, blasint ldc);
+/* replaces cblas_sgemm, interface/gemm.c (FP32 build; cblas.h:298-299) */
+void cblas_sgemm(enum CBLAS_ORDER Order, enum CBLAS_TRANSPOSE TransA,
+                 enum CBLAS_TRANSPOSE TransB, blasint M, blasint N, blasint K,
+                 float alpha, const float *A, blasint lda, const float *B,
+                 blasint ldb, float beta, float *C, blasint ldc);
+/* replaces cblas_dtrsm, interface/trsm.c:213-412 (cblas.h:358-359) */
+void cblas_dtrsm(enum CBLAS_ORDER Order, enum CBLAS_SIDE Side,
+                 enum CBLAS_UPLO Uplo, enum CBLAS_TRANSPOSE TransA,
+                 enum CBLAS_DIAG Diag, blasint M, blasint N, double alpha,
+                 const double *A, blasint lda, double *B, blasint ldb);
+/* replaces cblas_dsyrk, interface/syrk.c:195-402 (cblas.h:331-332) */
+void cblas_dsyrk(enum CBLAS_ORDER Order, enum CBLAS_UPLO Uplo,
+                 enum CBLAS_TRANSPOSE Trans, blasint N, blasint K, double alpha,
+                 const double *A, blasint lda, double beta, double *C,
+                 blasint ldc);
+/* replaces cblas_dgemm_batch, interface/gemm_batch.c:117-372 (cblas.h:422-423) */
+void cblas_dgemm_batch(enum CBLAS_ORDER Order,
+                       const enum CBLAS_TRANSPOSE *TransA_array,
+                       const enum CBLAS_TRANSPOSE *TransB_array,
+                       const blasint *M_array, const blasint *N_array,
+                       const blasint *K_array, const double *alpha_array,
+                       const double **A_array, const blasint *lda_array,
+                       const double **B_array, const blasint *ldb_array,
+                       const double *beta_array, double **C_array,
+                       const blasint *ldc_array, blasint group_count,
+                       const blasint *group_size);
+
+/* replaces dgemm_, interface/gemm.c:181-290 (common_interface.h) */
+void dgemm_(const char *TRANSA, const char *TRANSB, const blasint *M,
+            const blasint *N, const blasint *K, const double *alpha,
+            const double *A, const blasint *ldA, const double *B,
+            const blasint *ldB, const double *beta, double *C,
+            const blasint *ldC);
+/* replaces sgemm_, interface/gemm.c:181-290 (FP32 build) */
+void sgemm_(const char *TRANSA, const char *TRANSB, const blasint *M,
+            const blasint *N, const blasint *K, const float *alpha,
+            const float *A, const blasint *ldA, const float *B,
+            const blasint *ldB, const float *beta, float *C,
+            const blasint *ldC);
+/* replaces dtrsm_, interface/trsm.c:114-209 */
+void dtrsm_(const char *SIDE, const char *UPLO, const char *TRANSA,
+            const char *DIAG, const blasint *M, const blasint *N,
+            const double *alpha, const double *A, const blasint *ldA,
+            double *B, const blasint *ldB);
+/* replaces dsyrk_, interface/syrk.c:96-191 */
+void dsyrk_(const char *UPLO, const char *TRANS, const blasint *N,
+            const blasint *K, const double *alpha, const double *A,
+            const blasint *ldA, const double *beta, double *C,
+            const blasint *ldC);
+
+/* replaces dgetrf_, interface/lapack/getrf.c:53-133 */
+int dgetrf_(const blasint *M, const blasint *N, double *A, const blasint *ldA,
+            blasint *ipiv, blasint *Info);
+/* replaces dgetrs_, interface/lapack/getrs.c:63-152 */
+int dgetrs_(const char *TRANS, const blasint *N, const blasint *NRHS,
+            const double *A, const blasint *ldA, const blasint *ipiv,
+            double *B, const blasint *ldB, blasint *Info);
+/* replaces dgesv_, interface/lapack/gesv.c:63-161 */
+int dgesv_(const blasint *N, const blasint *NRHS, double *A, const blasint *ldA,
+           blasint *ipiv, double *B, const blasint *ldB, blasint *Info);
+/* replaces dpotrf_, interface/lapack/potrf.c:63-150 */
+int dpotrf_(const char *UPLO, const blasint *N, double *A, const blasint *ldA,
+            blasint *Info);
+/* replaces dlaswp_, interface/lapack/laswp.c:55-110 */
+int dlaswp_(const blasint *N, double *A, const blasint *LDA, const blasint *K1,
+            const blasint *K2, const blasint *ipiv, const blasint *INCX);
+/* replaces dsgesv_ (netlib, compiled into OpenBLAS),
+ * lapack-netlib/SRC/dsgesv.f:193-430.  SWORK/WORK are accepted for ABI
+ * compatibility; the GPU path keeps its own workspace. */
+int dsgesv_(const blasint *N, const blasint *NRHS, double *A, const blasint *ldA,
+            blasint *ipiv, const double *B, const blasint *ldB, double *X,
+            const blasint *ldX, double *WORK, float *SWORK, blasint *ITER,
+            blasint *Info);
+
+/* replaces xerbla_, driver/others/xerbla.c:56-64.  Weak: an application may
+ * define its own.  Prints " ** On entry to %6s parameter number %2d had an
+ * illegal value" and returns. */
+int xerbla_(const char *name, const blasint *info, blasint len);
+
+/* ======================================================================= */
+/* Part 2: GB300-native API (device pointers, stream-ordered)               */
+/* ======================================================================= */
+
+/* status codes returned by gb_* functions */
+#define GB_SUCCESS 0
+#define GB_ERR_INVALID_VALUE 1 /* argument error (xerbla also called) */
+#define GB_ERR_CUDA 2          /* a CUDA runtime/driver call failed */
+#define GB_ERR_NO_DEVICE 3     /* no usable CUDA device */
+#define GB_ERR_ALLOC 4         /* device or pinned allocation failed */
+#define GB_ERR_KERNEL 5        /* a kernel reported an error (e.g. bounded wait expired) */
+#define GB_ERR_UNSUPPORTED 6   /* shape/option outside what the kernels support */
+
+/* DGEMM precision modes */
+#define GB_DGEMM_NATIVE 0   /* FP64 FMA units */
+#define GB_DGEMM_EMULATED 1 /* Ozaki split into 7-bit slices on bf16 tensor cores */
+#define GB_DGEMM_AUTO 2     /* emulated when the shape is large enough to win */
+
+/* Stream used by every entry point of the calling thread (NULL = the
+ * library's own non-blocking stream).  The handle is a cudaStream_t. */
+int gb_set_stream(void *stream);
+void *gb_get_stream(void);
+/* Block until all work queued by this thread's entry points is done and
+ * report any kernel-side error. */
+int gb_synchronize(void);
+/* Status and message of the calling thread's last error (message may be NULL). */
+int gb_last_error(char *msg, int len);
+void gb_clear_error(void);
+/* Last argument error seen by xerbla on this thread: routine name (up to 8
+ * chars + NUL) and parameter position; returns that position or 0. */
+int gb_last_xerbla(char *name, int len);
+/* Precision of the FP64 GEMM behind cblas_dgemm/dgemm_ and the LAPACK
+ * trailing updates' caller-facing DGEMM (default from GB_DGEMM_MODE). */
+int gb_set_dgemm_mode(int mode);
+int gb_get_dgemm_mode(void);
+/* Slice count of the emulated DGEMM (0 = chosen from K and accuracy target). */
+int gb_set_ozaki_slices(int slices);
+/* Library version string. */
+const char *gb_version(void);
+
+/* C <- alpha*op(A)*op(B) + beta*C, all device pointers, column-major,
+ * trans 'N'/'T'/'C'.  Uses the current DGEMM mode. */
+int gb_dgemm_dev(char transa, char transb, int64_t m, int64_t n, int64_t k,
+                 double alpha, const double *A, int64_t lda, const double *B,
+                 int64_t ldb, double beta, double *C, int64_t ldc);
+/* Native FP64 GEMM regardless of mode. */
+int gb_dgemm_native_dev(char transa, char transb, int64_t m, int64_t n,
+                        int64_t k, double alpha, const double *A, int64_t lda,
+                        const double *B, int64_t ldb, double beta, double *C,
+                        int64_t ldc);
+/* Emulated FP64 GEMM with `slices` 7-bit slices per operand (0 = auto). */
+int gb_dgemm_emulated_dev(char transa, char transb, int64_t m, int64_t n,
+                          int64_t k, double alpha, const double *A, int64_t lda,
+                          const double *B, int64_t ldb, double beta, double *C,
+                          int64_t ldc, int slices);
+int gb_sgemm_dev(char transa, char transb, int64_t m, int64_t n, int64_t k,
+                 float alpha, const float *A, int64_t lda, const float *B,
+                 int64_t ldb, float beta, float *C, int64_t ldc);
+int gb_dtrsm_dev(char side, char uplo, char transa, char diag, int64_t m,
+                 int64_t n, double alpha, const double *A, int64_t lda,
+                 double *B, int64_t ldb);
+int gb_dsyrk_dev(char uplo, char trans, int64_t n, int64_t k, double alpha,
+                 const double *A, int64_t lda, double beta, double *C,
+                 int64_t ldc);
+/* LU with partial pivoting; ipiv (int32, 1-based, min(m,n) entries) and
+ * info (one int32) are device pointers written by the GPU. */
+int gb_dgetrf_dev(int64_t m, int64_t n, double *A, int64_t lda, int *ipiv,
+                  int *info);
+int gb_dgetrs_dev(char trans, int64_t n, int64_t nrhs, const double *A,
+                  int64_t lda, const int *ipiv, double *B, int64_t ldb);
+/* Row interchanges k1..k2 (1-based) of an n-column device matrix using a
+ * device ipiv vector with increment incx (+1 or -1 for the fast path). */
+int gb_dlaswp_dev(int64_t n, double *A, int64_t lda, int64_t k1, int64_t k2,
+                  const int *ipiv, int64_t incx);
+int gb_dpotrf_dev(char uplo, int64_t n, double *A, int64_t lda, int *info);
+/* Mixed-precision solve (FP32 LU on the GPU + FP64 refinement, GMRES-IR
+ * when plain refinement stalls, FP64 LU fallback).  Device pointers except
+ * iter/info, which are host outputs (this call synchronises).  iter follows
+ * dsgesv (>= 0 refinement steps, < 0 fallback reason); GMRES-IR steps are
+ * reported as 100 + steps. */
+int gb_dsgesv_dev(int64_t n, int64_t nrhs, const double *A, int64_t lda,
+                  int *ipiv, const double *B, int64_t ldb, double *X,
+                  int64_t ldx, int *iter, int *info);
+
+#ifdef __cplusplus
+}
+#endif
+#if defined(__GNUC__)
+#pragma GCC visibility pop
+#endif
+#endif /* GBBLAS_H */

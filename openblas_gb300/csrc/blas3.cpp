@@ -1,0 +1,548 @@
+// Level-3 BLAS entry points of libgbblas: dgemm_/cblas_dgemm, sgemm_/
+// cblas_sgemm, dtrsm_/cblas_dtrsm, dsyrk_/cblas_dsyrk, cblas_dgemm_batch,
+// and their device-pointer variants.
+//
+// Argument decoding, the order of the checks (so the same parameter
+// position reaches xerbla), the row-major -> column-major operand swap and
+// the quick returns restate interface/gemm.c:181-476, interface/trsm.c:114-
+// 351 and interface/syrk.c:96-340.  Instead of the reference's thread-count
+// decision and scratch buffer, the call is dispatched to the GPU stream.
+#include <stdio.h>
+#include <string.h>
+
+#include <vector>
+
+#include "gb_internal.h"
+#include "operand.h"
+
+extern "C" int gb_get_ozaki_slices_internal(void);
+
+namespace gb {
+
+void call_xerbla(const char *name, int info) {
+  record_xerbla(name, info);
+  blasint i = info;
+  xerbla_(name, &i, (blasint)strlen(name));
+}
+
+int finish_blocking(cudaStream_t s) {
+  cudaError_t e = cudaStreamSynchronize(s);
+  if (e != cudaSuccess) return check_cuda(e, "cudaStreamSynchronize");
+  int h = 0;
+  e = cudaMemcpy(&h, ctx().d_status, sizeof(int), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return check_cuda(e, "cudaMemcpy(status)");
+  if (h) {
+    int site[4] = {0, 0, 0, 0};
+    cudaMemcpy(site, ctx().d_status, sizeof(site), cudaMemcpyDeviceToHost);
+    cudaMemset(ctx().d_status, 0, sizeof(site));
+    return set_error(GB_ERR_KERNEL, "kernel reported error code %d (site %d)", site[0], site[1]);
+  }
+  return GB_SUCCESS;
+}
+
+// transa/transb code: 0 = N, 1 = T, -1 = invalid (interface/gemm.c:243-262;
+// for real types 'R' means N and 'C' means T)
+static inline int trans_code(char t) {
+  t = upch(t);
+  if (t == 'N' || t == 'R') return 0;
+  if (t == 'T' || t == 'C') return 1;
+  return -1;
+}
+static inline int cblas_trans_code(int t) {
+  if (t == CblasNoTrans || t == CblasConjNoTrans) return 0;
+  if (t == CblasTrans || t == CblasConjTrans) return 1;
+  return -1;
+}
+
+// C <- alpha*op(A)op(B) + beta*C on device pointers, native FP64.
+static int dgemm_native(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
+                        const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
+                        double *C, int64_t ldc, cudaStream_t s) {
+  if (m == 0 || n == 0) return GB_SUCCESS;
+  if (k == 0 || alpha == 0.0) {
+    launch_dgemm_beta(m, n, beta, C, ldc, s);
+  } else {
+    launch_dgemm_fp64(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s);
+  }
+  return check_cuda(cudaGetLastError(), "dgemm launch");
+}
+
+int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
+                   const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
+                   double *C, int64_t ldc, int slices, cudaStream_t s);
+
+// Selected by the DGEMM mode: emulated when requested, or in auto mode when
+// the product is large enough for the split/recombine passes to pay off.
+static int dgemm_dispatch(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
+                          const double *A, int64_t lda, const double *B, int64_t ldb,
+                          double beta, double *C, int64_t ldc, cudaStream_t s) {
+  int mode = gb_get_dgemm_mode();
+  bool emu = mode == GB_DGEMM_EMULATED ||
+             (mode == GB_DGEMM_AUTO && (double)m * n * k >= 256.0 * 256.0 * 256.0 && k >= 64);
+  if (emu && k > 0 && alpha != 0.0)
+    return dgemm_emulated(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
+                          gb_get_ozaki_slices_internal(), s);
+  return dgemm_native(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s);
+}
+
+// Blocking host-pointer DGEMM after argument checks (column-major form).
+static void dgemm_blocking(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
+                           const double *A, int64_t lda, const double *B, int64_t ldb,
+                           double beta, double *C, int64_t ldc) {
+  if (m == 0 || n == 0) return;  // interface/gemm.c:494
+  if (ensure_init()) return;
+  cudaStream_t s = stream();
+  bool need_ab = k > 0 && alpha != 0.0;
+  Operand a(A, ta ? k : m, ta ? m : k, lda, 8), b(B, tb ? n : k, tb ? k : n, ldb, 8);
+  Operand c(C, m, n, ldc, 8);
+  if (need_ab && (a.bind(true, s) || b.bind(true, s))) return;
+  if (c.bind(beta != 0.0, s)) return;
+  if (dgemm_dispatch(ta, tb, m, n, k, alpha, a.d<double>(), a.dld, b.d<double>(), b.dld, beta,
+                     c.d<double>(), c.dld, s))
+    return;
+  c.unbind(s);
+  finish_blocking(s);
+}
+
+static void sgemm_blocking(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha,
+                           const float *A, int64_t lda, const float *B, int64_t ldb, float beta,
+                           float *C, int64_t ldc) {
+  if (m == 0 || n == 0) return;
+  if (ensure_init()) return;
+  cudaStream_t s = stream();
+  bool need_ab = k > 0 && alpha != 0.0f;
+  Operand a(A, ta ? k : m, ta ? m : k, lda, 4), b(B, tb ? n : k, tb ? k : n, ldb, 4);
+  Operand c(C, m, n, ldc, 4);
+  if (need_ab && (a.bind(true, s) || b.bind(true, s))) return;
+  if (c.bind(beta != 0.0f, s)) return;
+  if (!need_ab)
+    launch_sgemm_beta(m, n, beta, c.d<float>(), c.dld, s);
+  else
+    launch_sgemm_fp32(ta, tb, m, n, k, alpha, a.d<float>(), a.dld, b.d<float>(), b.dld, beta,
+                      c.d<float>(), c.dld, s);
+  if (check_cuda(cudaGetLastError(), "sgemm launch")) return;
+  c.unbind(s);
+  finish_blocking(s);
+}
+
+// GEMM argument check shared by the Fortran and CBLAS forms
+// (interface/gemm.c:264-278, 409-418).  Returns the xerbla position or 0.
+static int gemm_check(int transa, int transb, int64_t m, int64_t n, int64_t k, int64_t lda,
+                      int64_t ldb, int64_t ldc) {
+  int64_t nrowa = (transa & 1) ? k : m;
+  int64_t nrowb = (transb & 1) ? n : k;
+  int info = 0;
+  if (ldc < m) info = 13;
+  if (ldb < nrowb) info = 10;
+  if (lda < nrowa) info = 8;
+  if (k < 0) info = 5;
+  if (n < 0) info = 4;
+  if (m < 0) info = 3;
+  if (transb < 0) info = 2;
+  if (transa < 0) info = 1;
+  return info;
+}
+
+int dtrsm_device(int side, int uplo, int trans, int unit, int64_t m, int64_t n, double alpha,
+                 const double *A, int64_t lda, double *B, int64_t ldb, cudaStream_t s);
+int dsyrk_device(int uplo, int trans, int64_t n, int64_t k, double alpha, const double *A,
+                 int64_t lda, double beta, double *C, int64_t ldc, cudaStream_t s);
+int gb_dgemm_batch_grouped(int order, const int *ta, const int *tb, const blasint *m,
+                           const blasint *n, const blasint *k, const double *alpha,
+                           const double **A, const blasint *lda, const double **B,
+                           const blasint *ldb, const double *beta, double **C,
+                           const blasint *ldc, blasint group_count, const blasint *group_size);
+
+static void dtrsm_blocking(int side, int uplo, int trans, int unit, int64_t m, int64_t n,
+                           double alpha, const double *A, int64_t lda, double *B, int64_t ldb) {
+  if (m == 0 || n == 0) return;  // interface/trsm.c:355
+  if (ensure_init()) return;
+  cudaStream_t s = stream();
+  int64_t na = side ? n : m;
+  Operand a(A, na, na, lda, 8), b(B, m, n, ldb, 8);
+  if (alpha != 0.0 && a.bind(true, s)) return;
+  if (b.bind(alpha != 0.0, s)) return;
+  if (dtrsm_device(side, uplo, trans, unit, m, n, alpha, a.d<double>(), a.dld, b.d<double>(),
+                   b.dld, s))
+    return;
+  b.unbind(s);
+  finish_blocking(s);
+}
+
+static void dsyrk_blocking(int uplo, int trans, int64_t n, int64_t k, double alpha,
+                           const double *A, int64_t lda, double beta, double *C, int64_t ldc) {
+  if (n == 0) return;  // interface/syrk.c:344
+  if (ensure_init()) return;
+  cudaStream_t s = stream();
+  Operand a(A, trans ? k : n, trans ? n : k, lda, 8), c(C, n, n, ldc, 8);
+  if (k > 0 && alpha != 0.0 && a.bind(true, s)) return;
+  // the untouched triangle must survive the round trip, so C is always staged in
+  if (c.bind(true, s)) return;
+  if (dsyrk_device(uplo, trans, n, k, alpha, a.d<double>(), a.dld, beta, c.d<double>(), c.dld,
+                   s))
+    return;
+  c.unbind(s);
+  finish_blocking(s);
+}
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+// ---------------------------------------------------------------------------
+// GEMM
+// ---------------------------------------------------------------------------
+void dgemm_(const char *TRANSA, const char *TRANSB, const blasint *M, const blasint *N,
+            const blasint *K, const double *alpha, const double *A, const blasint *ldA,
+            const double *B, const blasint *ldB, const double *beta, double *C,
+            const blasint *ldC) {
+  int ta = trans_code(*TRANSA), tb = trans_code(*TRANSB);
+  int info = gemm_check(ta, tb, *M, *N, *K, *ldA, *ldB, *ldC);
+  if (info) {
+    call_xerbla("DGEMM ", info);
+    return;
+  }
+  dgemm_blocking(ta, tb, *M, *N, *K, *alpha, A, *ldA, B, *ldB, *beta, C, *ldC);
+}
+
+void sgemm_(const char *TRANSA, const char *TRANSB, const blasint *M, const blasint *N,
+            const blasint *K, const float *alpha, const float *A, const blasint *ldA,
+            const float *B, const blasint *ldB, const float *beta, float *C,
+            const blasint *ldC) {
+  int ta = trans_code(*TRANSA), tb = trans_code(*TRANSB);
+  int info = gemm_check(ta, tb, *M, *N, *K, *ldA, *ldB, *ldC);
+  if (info) {
+    call_xerbla("SGEMM ", info);
+    return;
+  }
+  sgemm_blocking(ta, tb, *M, *N, *K, *alpha, A, *ldA, B, *ldB, *beta, C, *ldC);
+}
+
+void cblas_dgemm(enum CBLAS_ORDER order, enum CBLAS_TRANSPOSE TransA,
+                 enum CBLAS_TRANSPOSE TransB, blasint m, blasint n, blasint k, double alpha,
+                 const double *a, blasint lda, const double *b, blasint ldb, double beta,
+                 double *c, blasint ldc) {
+  // interface/gemm.c:374-471: row-major is the column-major product of the
+  // transposes, so A<->B, m<->n and transa<->transb swap.
+  int info = -1, ta = -1, tb = -1;
+  int64_t M = m, N = n;
+  const double *pa = a, *pb = b;
+  int64_t la = lda, lb = ldb;
+  if (order == CblasColMajor) {
+    ta = cblas_trans_code(TransA);
+    tb = cblas_trans_code(TransB);
+  } else if (order == CblasRowMajor) {
+    M = n;
+    N = m;
+    pa = b;
+    pb = a;
+    la = ldb;
+    lb = lda;
+    ta = cblas_trans_code(TransB);
+    tb = cblas_trans_code(TransA);
+  }
+  if (order == CblasColMajor || order == CblasRowMajor) {
+    info = gemm_check(ta, tb, M, N, k, la, lb, ldc);
+    if (info == 0) info = -1;
+  }
+  if (info >= 0) {
+    call_xerbla("DGEMM ", info);
+    return;
+  }
+  dgemm_blocking(ta, tb, M, N, k, alpha, pa, la, pb, lb, beta, c, ldc);
+}
+
+void cblas_sgemm(enum CBLAS_ORDER order, enum CBLAS_TRANSPOSE TransA,
+                 enum CBLAS_TRANSPOSE TransB, blasint m, blasint n, blasint k, float alpha,
+                 const float *a, blasint lda, const float *b, blasint ldb, float beta, float *c,
+                 blasint ldc) {
+  int info = -1, ta = -1, tb = -1;
+  int64_t M = m, N = n;
+  const float *pa = a, *pb = b;
+  int64_t la = lda, lb = ldb;
+  if (order == CblasColMajor) {
+    ta = cblas_trans_code(TransA);
+    tb = cblas_trans_code(TransB);
+  } else if (order == CblasRowMajor) {
+    M = n;
+    N = m;
+    pa = b;
+    pb = a;
+    la = ldb;
+    lb = lda;
+    ta = cblas_trans_code(TransB);
+    tb = cblas_trans_code(TransA);
+  }
+  if (order == CblasColMajor || order == CblasRowMajor) {
+    info = gemm_check(ta, tb, M, N, k, la, lb, ldc);
+    if (info == 0) info = -1;
+  }
+  if (info >= 0) {
+    call_xerbla("SGEMM ", info);
+    return;
+  }
+  sgemm_blocking(ta, tb, M, N, k, alpha, pa, la, pb, lb, beta, c, ldc);
+}
+
+// ---------------------------------------------------------------------------
+// TRSM (interface/trsm.c)
+// ---------------------------------------------------------------------------
+static int trsm_check(int side, int uplo, int trans, int unit, int64_t m, int64_t n, int64_t lda,
+                      int64_t ldb) {
+  int64_t nrowa = (side & 1) ? n : m;
+  int info = 0;
+  if (ldb < (m > 1 ? m : 1)) info = 11;
+  if (lda < (nrowa > 1 ? nrowa : 1)) info = 9;
+  if (n < 0) info = 6;
+  if (m < 0) info = 5;
+  if (unit < 0) info = 4;
+  if (trans < 0) info = 3;
+  if (uplo < 0) info = 2;
+  if (side < 0) info = 1;
+  return info;
+}
+
+void dtrsm_(const char *SIDE, const char *UPLO, const char *TRANSA, const char *DIAG,
+            const blasint *M, const blasint *N, const double *alpha, const double *A,
+            const blasint *ldA, double *B, const blasint *ldB) {
+  char sd = upch(SIDE), up = upch(UPLO), tr = upch(TRANSA), dg = upch(DIAG);
+  int side = sd == 'L' ? 0 : sd == 'R' ? 1 : -1;
+  int uplo = up == 'U' ? 0 : up == 'L' ? 1 : -1;
+  int trans = (tr == 'N' || tr == 'R') ? 0 : (tr == 'T' || tr == 'C') ? 1 : -1;
+  int unit = dg == 'U' ? 0 : dg == 'N' ? 1 : -1;
+  int info = trsm_check(side, uplo, trans, unit, *M, *N, *ldA, *ldB);
+  if (info) {
+    call_xerbla("DTRSM ", info);
+    return;
+  }
+  dtrsm_blocking(side, uplo, trans, unit, *M, *N, *alpha, A, *ldA, B, *ldB);
+}
+
+void cblas_dtrsm(enum CBLAS_ORDER order, enum CBLAS_SIDE Side, enum CBLAS_UPLO Uplo,
+                 enum CBLAS_TRANSPOSE Trans, enum CBLAS_DIAG Diag, blasint m, blasint n,
+                 double alpha, const double *a, blasint lda, double *b, blasint ldb) {
+  // interface/trsm.c:276-351: row-major swaps m<->n, Left<->Right, Upper<->Lower
+  int side = -1, uplo = -1, trans = -1, unit = -1, info = -1;
+  int64_t M = m, N = n;
+  if (order == CblasColMajor) {
+    side = Side == CblasLeft ? 0 : Side == CblasRight ? 1 : -1;
+    uplo = Uplo == CblasUpper ? 0 : Uplo == CblasLower ? 1 : -1;
+  } else if (order == CblasRowMajor) {
+    M = n;
+    N = m;
+    side = Side == CblasLeft ? 1 : Side == CblasRight ? 0 : -1;
+    uplo = Uplo == CblasUpper ? 1 : Uplo == CblasLower ? 0 : -1;
+  }
+  trans = cblas_trans_code(Trans);
+  unit = Diag == CblasUnit ? 0 : Diag == CblasNonUnit ? 1 : -1;
+  if (order == CblasColMajor || order == CblasRowMajor) {
+    info = trsm_check(side, uplo, trans, unit, M, N, lda, ldb);
+    if (info == 0) info = -1;
+  }
+  if (info >= 0) {
+    call_xerbla("DTRSM ", info);
+    return;
+  }
+  dtrsm_blocking(side, uplo, trans, unit, M, N, alpha, a, lda, b, ldb);
+}
+
+// ---------------------------------------------------------------------------
+// SYRK (interface/syrk.c)
+// ---------------------------------------------------------------------------
+static int syrk_check(int uplo, int trans, int64_t n, int64_t k, int64_t lda, int64_t ldc) {
+  int64_t nrowa = (trans & 1) ? k : n;
+  int info = 0;
+  if (ldc < (n > 1 ? n : 1)) info = 10;
+  if (lda < (nrowa > 1 ? nrowa : 1)) info = 7;
+  if (k < 0) info = 4;
+  if (n < 0) info = 3;
+  if (trans < 0) info = 2;
+  if (uplo < 0) info = 1;
+  return info;
+}
+
+void dsyrk_(const char *UPLO, const char *TRANS, const blasint *N, const blasint *K,
+            const double *alpha, const double *A, const blasint *ldA, const double *beta,
+            double *C, const blasint *ldC) {
+  char up = upch(UPLO), tr = upch(TRANS);
+  int uplo = up == 'U' ? 0 : up == 'L' ? 1 : -1;
+  int trans = tr == 'N' ? 0 : (tr == 'T' || tr == 'C') ? 1 : -1;
+  int info = syrk_check(uplo, trans, *N, *K, *ldA, *ldC);
+  if (info) {
+    call_xerbla("DSYRK ", info);
+    return;
+  }
+  dsyrk_blocking(uplo, trans, *N, *K, *alpha, A, *ldA, *beta, C, *ldC);
+}
+
+void cblas_dsyrk(enum CBLAS_ORDER order, enum CBLAS_UPLO Uplo, enum CBLAS_TRANSPOSE Trans,
+                 blasint n, blasint k, double alpha, const double *a, blasint lda, double beta,
+                 double *c, blasint ldc) {
+  // interface/syrk.c:291-335: row-major flips uplo and trans
+  int uplo = -1, trans = -1, info = -1;
+  if (order == CblasColMajor) {
+    uplo = Uplo == CblasUpper ? 0 : Uplo == CblasLower ? 1 : -1;
+    trans = cblas_trans_code(Trans);
+  } else if (order == CblasRowMajor) {
+    uplo = Uplo == CblasUpper ? 1 : Uplo == CblasLower ? 0 : -1;
+    int t = cblas_trans_code(Trans);
+    trans = t < 0 ? -1 : 1 - t;
+  }
+  if (order == CblasColMajor || order == CblasRowMajor) {
+    info = syrk_check(uplo, trans, n, k, lda, ldc);
+    if (info == 0) info = -1;
+  }
+  if (info >= 0) {
+    call_xerbla("DSYRK ", info);
+    return;
+  }
+  dsyrk_blocking(uplo, trans, n, k, alpha, a, lda, beta, c, ldc);
+}
+
+// ---------------------------------------------------------------------------
+// grouped batch (interface/gemm_batch.c:117-372)
+// ---------------------------------------------------------------------------
+
+void cblas_dgemm_batch(enum CBLAS_ORDER order, const enum CBLAS_TRANSPOSE *transa_array,
+                       const enum CBLAS_TRANSPOSE *transb_array, const blasint *m_array,
+                       const blasint *n_array, const blasint *k_array,
+                       const double *alpha_array, const double **a_array,
+                       const blasint *lda_array, const double **b_array,
+                       const blasint *ldb_array, const double *beta_array, double **c_array,
+                       const blasint *ldc_array, blasint group_count,
+                       const blasint *group_size) {
+  // validate every group first, exactly as the reference does before it
+  // runs anything (gemm_batch.c:195-283)
+  std::vector<int> ta(group_count > 0 ? group_count : 1), tb(ta.size());
+  for (blasint g = 0; g < group_count; ++g) {
+    int64_t M, N, la, lb;
+    int a_code, b_code;
+    if (order == CblasColMajor) {
+      M = m_array[g];
+      N = n_array[g];
+      la = lda_array[g];
+      lb = ldb_array[g];
+      a_code = cblas_trans_code(transa_array[g]);
+      b_code = cblas_trans_code(transb_array[g]);
+    } else if (order == CblasRowMajor) {
+      M = n_array[g];
+      N = m_array[g];
+      la = ldb_array[g];
+      lb = lda_array[g];
+      a_code = cblas_trans_code(transb_array[g]);
+      b_code = cblas_trans_code(transa_array[g]);
+    } else {
+      call_xerbla("DGEMM ", 0);
+      return;
+    }
+    int info = gemm_check(a_code, b_code, M, N, k_array[g], la, lb, ldc_array[g]);
+    if (info) {
+      call_xerbla("DGEMM ", info);
+      return;
+    }
+    ta[g] = a_code;
+    tb[g] = b_code;
+  }
+  gb_dgemm_batch_grouped(order, ta.data(), tb.data(), m_array, n_array, k_array, alpha_array,
+                         a_array, lda_array, b_array, ldb_array, beta_array, c_array, ldc_array,
+                         group_count, group_size);
+}
+
+// ---------------------------------------------------------------------------
+// device-pointer API
+// ---------------------------------------------------------------------------
+static int dev_gemm_args(char transa, char transb, int64_t m, int64_t n, int64_t k, int64_t lda,
+                         int64_t ldb, int64_t ldc, int *ta, int *tb, const char *name) {
+  *ta = trans_code(transa);
+  *tb = trans_code(transb);
+  int info = gemm_check(*ta, *tb, m, n, k, lda, ldb, ldc);
+  if (info) {
+    call_xerbla(name, info);
+    return GB_ERR_INVALID_VALUE;
+  }
+  return ensure_init();
+}
+
+int gb_dgemm_dev(char transa, char transb, int64_t m, int64_t n, int64_t k, double alpha,
+                 const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
+                 double *C, int64_t ldc) {
+  int ta, tb;
+  int st = dev_gemm_args(transa, transb, m, n, k, lda, ldb, ldc, &ta, &tb, "DGEMM ");
+  if (st) return st;
+  return dgemm_dispatch(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, stream());
+}
+
+int gb_dgemm_native_dev(char transa, char transb, int64_t m, int64_t n, int64_t k, double alpha,
+                        const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
+                        double *C, int64_t ldc) {
+  int ta, tb;
+  int st = dev_gemm_args(transa, transb, m, n, k, lda, ldb, ldc, &ta, &tb, "DGEMM ");
+  if (st) return st;
+  return dgemm_native(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, stream());
+}
+
+int gb_dgemm_emulated_dev(char transa, char transb, int64_t m, int64_t n, int64_t k,
+                          double alpha, const double *A, int64_t lda, const double *B,
+                          int64_t ldb, double beta, double *C, int64_t ldc, int slices) {
+  int ta, tb;
+  int st = dev_gemm_args(transa, transb, m, n, k, lda, ldb, ldc, &ta, &tb, "DGEMM ");
+  if (st) return st;
+  if (m == 0 || n == 0) return GB_SUCCESS;
+  if (k == 0 || alpha == 0.0) {
+    launch_dgemm_beta(m, n, beta, C, ldc, stream());
+    return check_cuda(cudaGetLastError(), "dgemm_beta launch");
+  }
+  return dgemm_emulated(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, slices, stream());
+}
+
+int gb_sgemm_dev(char transa, char transb, int64_t m, int64_t n, int64_t k, float alpha,
+                 const float *A, int64_t lda, const float *B, int64_t ldb, float beta, float *C,
+                 int64_t ldc) {
+  int ta, tb;
+  int st = dev_gemm_args(transa, transb, m, n, k, lda, ldb, ldc, &ta, &tb, "SGEMM ");
+  if (st) return st;
+  if (m == 0 || n == 0) return GB_SUCCESS;
+  if (k == 0 || alpha == 0.0f)
+    launch_sgemm_beta(m, n, beta, C, ldc, stream());
+  else
+    launch_sgemm_fp32(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, stream());
+  return check_cuda(cudaGetLastError(), "sgemm launch");
+}
+
+int gb_dtrsm_dev(char side, char uplo, char transa, char diag, int64_t m, int64_t n,
+                 double alpha, const double *A, int64_t lda, double *B, int64_t ldb) {
+  char sd = upch(side), up = upch(uplo), tr = upch(transa), dg = upch(diag);
+  int is = sd == 'L' ? 0 : sd == 'R' ? 1 : -1;
+  int iu = up == 'U' ? 0 : up == 'L' ? 1 : -1;
+  int it = (tr == 'N' || tr == 'R') ? 0 : (tr == 'T' || tr == 'C') ? 1 : -1;
+  int id = dg == 'U' ? 0 : dg == 'N' ? 1 : -1;
+  int info = trsm_check(is, iu, it, id, m, n, lda, ldb);
+  if (info) {
+    call_xerbla("DTRSM ", info);
+    return GB_ERR_INVALID_VALUE;
+  }
+  int st = ensure_init();
+  if (st) return st;
+  if (m == 0 || n == 0) return GB_SUCCESS;
+  return dtrsm_device(is, iu, it, id, m, n, alpha, A, lda, B, ldb, stream());
+}
+
+int gb_dsyrk_dev(char uplo, char trans, int64_t n, int64_t k, double alpha, const double *A,
+                 int64_t lda, double beta, double *C, int64_t ldc) {
+  char up = upch(uplo), tr = upch(trans);
+  int iu = up == 'U' ? 0 : up == 'L' ? 1 : -1;
+  int it = tr == 'N' ? 0 : (tr == 'T' || tr == 'C') ? 1 : -1;
+  int info = syrk_check(iu, it, n, k, lda, ldc);
+  if (info) {
+    call_xerbla("DSYRK ", info);
+    return GB_ERR_INVALID_VALUE;
+  }
+  int st = ensure_init();
+  if (st) return st;
+  if (n == 0) return GB_SUCCESS;
+  return dsyrk_device(iu, it, n, k, alpha, A, lda, beta, C, ldc, stream());
+}
+
+}  // extern "C"

@@ -1,0 +1,262 @@
+// Per-thread execution context, error state, scratch memory, host<->device
+// staging and the xerbla error hook of libgbblas.
+//
+// The reference keeps a process-wide thread server and a scratch pool
+// (driver/others/blas_server.c, driver/others/memory.c:1161).  On the GPU
+// the equivalent state is one CUDA stream per calling host thread plus a
+// stream-ordered memory pool: concurrent callers never share a stream, and
+// scratch comes from cudaMallocAsync on that stream, cached by the pool.
+#include <cuda_runtime.h>
+#include <stdarg.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <mutex>
+
+#include "gb_internal.h"
+
+namespace gb {
+
+namespace {
+struct ErrorState {
+  int status = GB_SUCCESS;
+  char msg[512] = {0};
+  char xerbla_name[16] = {0};
+  int xerbla_info = 0;
+};
+thread_local ErrorState t_err;
+thread_local Context t_ctx;
+std::once_flag g_cfg_once;
+Config g_cfg;
+std::mutex g_pool_mu;
+bool g_pool_ready[64] = {false};
+}  // namespace
+
+int set_error(int status, const char *fmt, ...) {
+  t_err.status = status;
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(t_err.msg, sizeof(t_err.msg), fmt, ap);
+  va_end(ap);
+  if (config().verbose || status != GB_ERR_INVALID_VALUE)
+    fprintf(stderr, "libgbblas: %s\n", t_err.msg);
+  return status;
+}
+
+int check_cuda(cudaError_t e, const char *what) {
+  if (e == cudaSuccess) return GB_SUCCESS;
+  int st = (e == cudaErrorMemoryAllocation) ? GB_ERR_ALLOC
+           : (e == cudaErrorNoDevice || e == cudaErrorInsufficientDriver) ? GB_ERR_NO_DEVICE
+                                                                          : GB_ERR_CUDA;
+  return set_error(st, "%s failed: %s", what, cudaGetErrorString(e));
+}
+
+const Config &config() {
+  std::call_once(g_cfg_once, [] {
+    const char *m = getenv("GB_DGEMM_MODE");
+    if (m) {
+      if (!strcmp(m, "emulated") || !strcmp(m, "ozaki")) g_cfg.dgemm_mode = GB_DGEMM_EMULATED;
+      else if (!strcmp(m, "auto")) g_cfg.dgemm_mode = GB_DGEMM_AUTO;
+      else g_cfg.dgemm_mode = GB_DGEMM_NATIVE;
+    }
+    const char *s = getenv("GB_OZAKI_SLICES");
+    if (s) g_cfg.ozaki_slices = atoi(s);
+    const char *v = getenv("GB_VERBOSE");
+    if (v) g_cfg.verbose = atoi(v);
+  });
+  return g_cfg;
+}
+
+Context &ctx() { return t_ctx; }
+
+int ensure_init() {
+  Context &c = t_ctx;
+  if (c.stream && c.d_status) return GB_SUCCESS;
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return check_cuda(e, "cudaGetDevice");
+  int ndev = 0;
+  e = cudaGetDeviceCount(&ndev);
+  if (e != cudaSuccess || ndev == 0) return check_cuda(e == cudaSuccess ? cudaErrorNoDevice : e,
+                                                       "cudaGetDeviceCount");
+  c.device = dev;
+  if (!c.stream) {
+    GB_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
+  }
+  if (!c.d_status) {
+    GB_CUDA(cudaMalloc(&c.d_status, sizeof(int) * 4));
+    GB_CUDA(cudaMemsetAsync(c.d_status, 0, sizeof(int) * 4, c.stream));
+  }
+  {
+    std::lock_guard<std::mutex> lk(g_pool_mu);
+    if (dev < 64 && !g_pool_ready[dev]) {
+      cudaMemPool_t pool;
+      if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;  // keep freed scratch cached in the pool
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+      }
+      g_pool_ready[dev] = true;
+    }
+  }
+  return GB_SUCCESS;
+}
+
+cudaStream_t stream() { return t_ctx.stream; }
+
+void *scratch_alloc(size_t bytes, cudaStream_t s) {
+  if (bytes == 0) bytes = 256;
+  void *p = nullptr;
+  cudaError_t e = cudaMallocAsync(&p, bytes, s);
+  if (e != cudaSuccess) {
+    check_cuda(e, "cudaMallocAsync(scratch)");
+    return nullptr;
+  }
+  return p;
+}
+
+void scratch_free(void *p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
+}
+
+bool is_device_pointer(const void *p) {
+  if (!p) return false;
+  cudaPointerAttributes at;
+  cudaError_t e = cudaPointerGetAttributes(&at, p);
+  if (e != cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
+  return at.type == cudaMemoryTypeDevice || at.type == cudaMemoryTypeManaged;
+}
+
+int stage_in(void *dst_dev, const void *src_host, size_t ld, size_t m, size_t n, size_t esize,
+             cudaStream_t s) {
+  if (m == 0 || n == 0) return GB_SUCCESS;
+  GB_CUDA(cudaMemcpy2DAsync(dst_dev, m * esize, src_host, ld * esize, m * esize, n,
+                            cudaMemcpyHostToDevice, s));
+  return GB_SUCCESS;
+}
+
+int stage_out(void *dst_host, const void *src_dev, size_t ld, size_t m, size_t n, size_t esize,
+              cudaStream_t s) {
+  if (m == 0 || n == 0) return GB_SUCCESS;
+  GB_CUDA(cudaMemcpy2DAsync(dst_host, ld * esize, src_dev, m * esize, m * esize, n,
+                            cudaMemcpyDeviceToHost, s));
+  return GB_SUCCESS;
+}
+
+// Called from the xerbla_ entry point (also when the application overrides
+// xerbla_, the library records the argument error before calling it).
+void record_xerbla(const char *name, int info) {
+  size_t n = strnlen(name, 8);
+  memcpy(t_err.xerbla_name, name, n);
+  t_err.xerbla_name[n] = 0;
+  t_err.xerbla_info = info;
+  t_err.status = GB_ERR_INVALID_VALUE;
+  snprintf(t_err.msg, sizeof(t_err.msg), "%s: parameter %d had an illegal value",
+           t_err.xerbla_name, info);
+}
+
+}  // namespace gb
+
+// ---------------------------------------------------------------------------
+// public control API
+// ---------------------------------------------------------------------------
+extern "C" {
+
+__attribute__((weak)) int xerbla_(const char *name, const blasint *info, blasint len) {
+  (void)len;
+  char buf[16];
+  size_t n = strnlen(name, 6);
+  memcpy(buf, name, n);
+  buf[n] = 0;
+  printf(" ** On entry to %6s parameter number %2d had an illegal value\n", buf, *info);
+  fflush(stdout);
+  return 0;
+}
+
+int gb_set_stream(void *s) {
+  int st = gb::ensure_init();
+  if (st) return st;
+  gb::Context &c = gb::ctx();
+  if (s) {
+    c.stream = (cudaStream_t)s;
+    c.user_stream = true;
+  } else if (c.user_stream) {
+    c.user_stream = false;
+    c.stream = nullptr;
+    return gb::ensure_init();
+  }
+  return GB_SUCCESS;
+}
+
+void *gb_get_stream(void) {
+  if (gb::ensure_init()) return nullptr;
+  return (void *)gb::stream();
+}
+
+int gb_synchronize(void) {
+  int st = gb::ensure_init();
+  if (st) return st;
+  GB_CUDA(cudaStreamSynchronize(gb::stream()));
+  int h[4] = {0, 0, 0, 0};
+  GB_CUDA(cudaMemcpy(h, gb::ctx().d_status, sizeof(h), cudaMemcpyDeviceToHost));
+  if (h[0]) {
+    cudaMemset(gb::ctx().d_status, 0, sizeof(h));
+    return gb::set_error(GB_ERR_KERNEL, "kernel reported error code %d (site %d)", h[0], h[1]);
+  }
+  return GB_SUCCESS;
+}
+
+int gb_last_error(char *msg, int len) {
+  if (msg && len > 0) {
+    strncpy(msg, gb::t_err.msg, (size_t)len - 1);
+    msg[len - 1] = 0;
+  }
+  return gb::t_err.status;
+}
+
+void gb_clear_error(void) {
+  gb::t_err.status = GB_SUCCESS;
+  gb::t_err.msg[0] = 0;
+  gb::t_err.xerbla_info = 0;
+  gb::t_err.xerbla_name[0] = 0;
+}
+
+int gb_last_xerbla(char *name, int len) {
+  if (name && len > 0) {
+    strncpy(name, gb::t_err.xerbla_name, (size_t)len - 1);
+    name[len - 1] = 0;
+  }
+  return gb::t_err.xerbla_info;
+}
+
+static thread_local int t_dgemm_mode = -1;
+static thread_local int t_ozaki_slices = -1;
+
+int gb_set_dgemm_mode(int mode) {
+  if (mode < GB_DGEMM_NATIVE || mode > GB_DGEMM_AUTO)
+    return gb::set_error(GB_ERR_INVALID_VALUE, "gb_set_dgemm_mode: bad mode %d", mode);
+  t_dgemm_mode = mode;
+  return GB_SUCCESS;
+}
+
+int gb_get_dgemm_mode(void) {
+  return t_dgemm_mode >= 0 ? t_dgemm_mode : gb::config().dgemm_mode;
+}
+
+int gb_set_ozaki_slices(int slices) {
+  if (slices < 0 || slices > 12)
+    return gb::set_error(GB_ERR_INVALID_VALUE, "gb_set_ozaki_slices: %d not in [0,12]", slices);
+  t_ozaki_slices = slices;
+  return GB_SUCCESS;
+}
+
+int gb_get_ozaki_slices_internal(void) {
+  return t_ozaki_slices >= 0 ? t_ozaki_slices : gb::config().ozaki_slices;
+}
+
+const char *gb_version(void) { return "libgbblas 0.1 (sm_103a)"; }
+
+}  // extern "C"

@@ -1,0 +1,105 @@
+// Internal declarations shared by the host dispatcher and the CUDA kernels
+// of libgbblas.  Nothing here is part of the public ABI (include/gbblas.h).
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stddef.h>
+#include <stdint.h>
+
+#include "../../include/gbblas.h"
+
+namespace gb {
+
+// ---------------------------------------------------------------------------
+// error reporting
+// ---------------------------------------------------------------------------
+// Records a library error (status code + message) for the calling thread and
+// prints it once to stderr.  Never aborts the process.
+int set_error(int status, const char *fmt, ...);
+int check_cuda(cudaError_t e, const char *what);
+#define GB_CUDA(call)                                                         \
+  do {                                                                        \
+    cudaError_t _e = (call);                                                  \
+    if (_e != cudaSuccess) return gb::check_cuda(_e, #call);                  \
+  } while (0)
+
+// ---------------------------------------------------------------------------
+// per-thread execution context
+// ---------------------------------------------------------------------------
+struct Context {
+  int device = -1;
+  cudaStream_t stream = nullptr;     // library stream (or user stream)
+  bool user_stream = false;
+  int *d_status = nullptr;           // device status word for kernel errors
+};
+Context &ctx();
+// Lazily initialise CUDA for this thread; returns GB_SUCCESS or an error.
+int ensure_init();
+cudaStream_t stream();
+
+// Stream-ordered device scratch (cudaMallocAsync from a pool that keeps its
+// memory cached between calls, so repeated calls do not hit the driver).
+void *scratch_alloc(size_t bytes, cudaStream_t s);
+void scratch_free(void *p, cudaStream_t s);
+
+// RAII holder of a scratch allocation.
+struct Scratch {
+  void *p = nullptr;
+  cudaStream_t s = nullptr;
+  Scratch() = default;
+  Scratch(size_t bytes, cudaStream_t st) : p(scratch_alloc(bytes, st)), s(st) {}
+  ~Scratch() {
+    if (p) scratch_free(p, s);
+  }
+  Scratch(const Scratch &) = delete;
+  Scratch &operator=(const Scratch &) = delete;
+  template <class T>
+  T *as() const { return reinterpret_cast<T *>(p); }
+};
+
+// True when `p` is device-accessible memory owned by CUDA (device or managed).
+bool is_device_pointer(const void *p);
+
+// Host<->device staging of a column-major m x n block with leading
+// dimension ld (elements of `esize` bytes).  Device copies are packed with
+// the same ld so kernels see the caller's layout.
+int stage_in(void *dst_dev, const void *src_host, size_t ld, size_t m, size_t n,
+             size_t esize, cudaStream_t s);
+int stage_out(void *dst_host, const void *src_dev, size_t ld, size_t m, size_t n,
+              size_t esize, cudaStream_t s);
+
+// Library configuration read from the environment once.
+struct Config {
+  int dgemm_mode = GB_DGEMM_NATIVE;   // GB_DGEMM_MODE=native|emulated|auto
+  int ozaki_slices = 0;               // GB_OZAKI_SLICES (0 = auto)
+  int verbose = 0;                    // GB_VERBOSE
+};
+const Config &config();
+
+// ---------------------------------------------------------------------------
+// kernels (device pointers, stream-ordered)
+// ---------------------------------------------------------------------------
+// C <- beta*C (beta==0 stores zeros).  kernel/generic/gemm_beta.c:41-94
+void launch_dgemm_beta(int64_t m, int64_t n, double beta, double *C, int64_t ldc,
+                       cudaStream_t s);
+void launch_sgemm_beta(int64_t m, int64_t n, float beta, float *C, int64_t ldc,
+                       cudaStream_t s);
+// Native FP64 GEMM (DFMA).  Assumes m,n,k > 0 and alpha != 0.
+void launch_dgemm_fp64(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
+                       const double *A, int64_t lda, const double *B, int64_t ldb,
+                       double beta, double *C, int64_t ldc, cudaStream_t s);
+// Same, writing only one triangle of C: tri 0 full, 1 lower (i>=j), 2 upper.
+void launch_dgemm_fp64_tri(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
+                           const double *A, int64_t lda, const double *B, int64_t ldb,
+                           double beta, double *C, int64_t ldc, int tri, cudaStream_t s,
+                           const int *skip = nullptr);
+// Triangular beta scaling of an n x n C (tri as above).
+void launch_dbeta_tri(int64_t n, double beta, double *C, int64_t ldc, int tri, cudaStream_t s);
+// Number of SMs of the current device.
+int sm_count();
+// Native FP32 GEMM (FFMA).
+void launch_sgemm_fp32(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha,
+                       const float *A, int64_t lda, const float *B, int64_t ldb,
+                       float beta, float *C, int64_t ldc, cudaStream_t s);
+
+}  // namespace gb

@@ -1,0 +1,45 @@
+// Internal interfaces of the LAPACK drivers (LU, Cholesky, solves).
+#pragma once
+
+#include "gb_internal.h"
+
+namespace gb {
+
+// Width of a panel factored by the cooperative panel kernel; also the
+// diagonal-block size of the triangular solves that follow it.
+constexpr int PANEL_NB = 32;
+
+// Kernel error codes written to the context status word.
+constexpr int GB_KERR_BARRIER_TIMEOUT = 1;
+constexpr int GB_KERR_MBARRIER_TIMEOUT = 2;
+
+// LU with partial pivoting of an m x n matrix (device pointers).  ipiv gets
+// min(m,n) 1-based global row indices, *info the first zero pivot (1-based)
+// or 0.  Semantics of lapack/getrf/getrf_single.c + getf2_k.c.
+template <typename T>
+int getrf_device(int64_t m, int64_t n, T *A, int64_t lda, int *ipiv, int *info, cudaStream_t s);
+// Solve op(A) X = B with an LU from getrf_device (lapack/getrs/getrs_single.c).
+template <typename T>
+int getrs_device(int trans, int64_t n, int64_t nrhs, const T *A, int64_t lda, const int *ipiv,
+                 T *B, int64_t ldb, cudaStream_t s);
+// Row interchanges k1..k2 (1-based) over n columns (lapack/laswp/generic).
+template <typename T>
+int laswp_device(int64_t n, T *A, int64_t lda, int64_t k1, int64_t k2, const int *ipiv,
+                 int64_t incx, cudaStream_t s);
+// Cholesky (lapack/potrf/potrf_{L,U}_single.c); *info_host receives info.
+int potrf_device(int uplo, int64_t n, double *A, int64_t lda, int *info_dev, cudaStream_t s);
+
+int dtrsm_device(int side, int uplo, int trans, int unit, int64_t m, int64_t n, double alpha,
+                 const double *A, int64_t lda, double *B, int64_t ldb, cudaStream_t s);
+int strsm_device(int side, int uplo, int trans, int unit, int64_t m, int64_t n, float alpha,
+                 const float *A, int64_t lda, float *B, int64_t ldb, cudaStream_t s);
+int dtrsm_device_skip(int side, int uplo, int trans, int unit, int64_t m, int64_t n,
+                      double alpha, const double *A, int64_t lda, double *B, int64_t ldb,
+                      cudaStream_t s, const int *skip);
+int dsyrk_device_skip(int uplo, int trans, int64_t n, int64_t k, double alpha, const double *A,
+                      int64_t lda, double beta, double *C, int64_t ldc, cudaStream_t s,
+                      const int *skip);
+int dsyrk_device(int uplo, int trans, int64_t n, int64_t k, double alpha, const double *A,
+                 int64_t lda, double beta, double *C, int64_t ldc, cudaStream_t s);
+
+}  // namespace gb

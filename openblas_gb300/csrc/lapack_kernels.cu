@@ -1,0 +1,556 @@
+// LU / Cholesky building blocks on the GPU: the partial-pivot panel
+// factorisation, row interchanges (LASWP) and the diagonal-block Cholesky.
+//
+// Panel LU (lapack/getf2/getf2_k.c:46-125 semantics).  The m x nb panel is
+// factored by one cooperative launch: every thread owns up to R rows of the
+// panel and keeps them in registers for the whole panel.  Per column j:
+//   1. each block finds its first-maximum |a_ij| row (IAMAX rule: largest
+//      magnitude, smallest index on ties) and publishes the value, the row
+//      index and the full row to a parity-buffered slot; the owner of row j
+//      also publishes row j;
+//   2. one grid barrier;
+//   3. every block reduces the candidates to the same pivot p, then each
+//      thread updates only its own rows: row j takes the old row p, row p
+//      takes the old row j, multipliers l_i = a_ij * (1/pivot) (only when
+//      |pivot| >= DBL_MIN, as in getf2_k.c:105-116, where the swap is also
+//      skipped), and the rank-1 update a_ic -= l_i * u_c for c > j.
+// Because each thread writes only rows it owns and reads the published rows
+// from the slot buffers, one barrier per column suffices.  The barrier is a
+// bounded spin: if it does not complete within its iteration limit the
+// kernel records an error status and returns.
+#include <cuda_runtime.h>
+#include <float.h>
+#include <stdint.h>
+
+#include "gb_internal.h"
+#include "lapack_internal.h"
+
+namespace gb {
+
+namespace {
+
+constexpr int PANEL_THREADS = 256;
+constexpr unsigned BARRIER_SPIN_LIMIT = 1u << 24;
+
+// Bounded grid-wide barrier for a cooperatively launched grid.  bar[0] is
+// the arrival counter, bar[1] the generation.  Returns false (and sets the
+// status word) when the wait limit expires.
+__device__ bool grid_barrier(unsigned *bar, unsigned nblocks, int *status, int site) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile unsigned *vgen = bar + 1;
+    unsigned gen = *vgen;
+    __threadfence();
+    unsigned arrived = atomicAdd(bar, 1u);
+    if (arrived == nblocks - 1) {
+      atomicExch(bar, 0u);
+      __threadfence();
+      atomicAdd(bar + 1, 1u);
+    } else {
+      unsigned spins = 0;
+      while (*vgen == gen) {
+        if (++spins > BARRIER_SPIN_LIMIT) {
+          ok = 0;
+          atomicCAS(status, 0, GB_KERR_BARRIER_TIMEOUT);
+          atomicExch(status + 1, site);
+          break;
+        }
+        if (spins > 64) __nanosleep(64);
+      }
+    }
+    __threadfence();
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+template <typename T>
+__device__ inline T tiny_pivot();
+template <>
+__device__ inline double tiny_pivot<double>() { return DBL_MIN; }
+template <>
+__device__ inline float tiny_pivot<float>() { return FLT_MIN; }
+
+template <typename T, int R>
+__global__ void __launch_bounds__(PANEL_THREADS)
+getf2_panel_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__restrict__ ipiv,
+                   int64_t row_off, int *__restrict__ info, T *__restrict__ slots,
+                   unsigned *__restrict__ bar, int *__restrict__ status) {
+  // slots layout: [2][nblocks][PANEL_NB + 2] for candidate rows (value, index
+  // stored in the two extra entries) + [2][PANEL_NB] for row j.
+  const unsigned nblocks = gridDim.x;
+  const int64_t nthreads = (int64_t)nblocks * PANEL_THREADS;
+  const int64_t gtid = (int64_t)blockIdx.x * PANEL_THREADS + threadIdx.x;
+  constexpr int W = PANEL_NB + 2;
+  T *cand = slots;                                    // [2][nblocks][W]
+  T *rowj_buf = slots + 2 * (int64_t)nblocks * W;     // [2][PANEL_NB]
+
+  T v[R][PANEL_NB];
+  int64_t rows[R];
+#pragma unroll
+  for (int r = 0; r < R; ++r) {
+    rows[r] = gtid + r * nthreads;
+#pragma unroll
+    for (int c = 0; c < PANEL_NB; ++c)
+      v[r][c] = (rows[r] < m && c < nb) ? A[rows[r] + c * lda] : T(0);
+  }
+
+  __shared__ T s_val[PANEL_THREADS / 32];
+  __shared__ int64_t s_idx[PANEL_THREADS / 32];
+  __shared__ int64_t s_best;
+  __shared__ T s_u[PANEL_NB];     // new row j (old row p)
+  __shared__ T s_oldj[PANEL_NB];  // old row j
+  __shared__ int64_t s_p;
+
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int j = 0; j < nb && j < m; ++j) {
+    const int par = j & 1;
+    // ---- 1. block-local first-max over rows >= j
+    T best = T(-1);
+    int64_t bidx = INT64_MAX;
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      if (rows[r] < m && rows[r] >= j) {
+        T a = v[r][0];
+#pragma unroll
+        for (int c = 1; c < PANEL_NB; ++c)
+          if (c == j) a = v[r][c];
+        a = a < T(0) ? -a : a;
+        if (a > best || (a == best && rows[r] < bidx)) {
+          best = a;
+          bidx = rows[r];
+        }
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      T ob = __shfl_down_sync(0xffffffffu, best, off);
+      int64_t oi = __shfl_down_sync(0xffffffffu, bidx, off);
+      if (ob > best || (ob == best && oi < bidx)) {
+        best = ob;
+        bidx = oi;
+      }
+    }
+    if (lane == 0) {
+      s_val[warp] = best;
+      s_idx[warp] = bidx;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      T bb = s_val[0];
+      int64_t bi = s_idx[0];
+      for (int w = 1; w < PANEL_THREADS / 32; ++w)
+        if (s_val[w] > bb || (s_val[w] == bb && s_idx[w] < bi)) {
+          bb = s_val[w];
+          bi = s_idx[w];
+        }
+      s_best = bi;
+      T *slot = cand + ((int64_t)par * nblocks + blockIdx.x) * W;
+      slot[PANEL_NB] = bb;
+      slot[PANEL_NB + 1] = (T)(double)(bi == INT64_MAX ? -1 : bi);
+    }
+    __syncthreads();
+    // the owner thread of the block's best row publishes the row
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      if (rows[r] == s_best) {
+        T *slot = cand + ((int64_t)par * nblocks + blockIdx.x) * W;
+#pragma unroll
+        for (int c = 0; c < PANEL_NB; ++c) slot[c] = v[r][c];
+      }
+      if (rows[r] == j) {
+        T *rb = rowj_buf + (int64_t)par * PANEL_NB;
+#pragma unroll
+        for (int c = 0; c < PANEL_NB; ++c) rb[c] = v[r][c];
+      }
+    }
+    // ---- 2. grid barrier
+    if (!grid_barrier(bar, nblocks, status, 100 + j)) return;
+    // ---- 3. global pivot (same in every block)
+    if (threadIdx.x < 32) {
+      T bb = T(-1);
+      int64_t bi = INT64_MAX;
+      for (unsigned b = lane; b < nblocks; b += 32) {
+        const T *slot = cand + ((int64_t)par * nblocks + b) * W;
+        T val = __ldcg(slot + PANEL_NB);
+        int64_t idx = (int64_t)__ldcg(slot + PANEL_NB + 1);
+        if (idx >= 0 && (val > bb || (val == bb && idx < bi))) {
+          bb = val;
+          bi = idx;
+        }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        T ob = __shfl_down_sync(0xffffffffu, bb, off);
+        int64_t oi = __shfl_down_sync(0xffffffffu, bi, off);
+        if (ob > bb || (ob == bb && oi < bi)) {
+          bb = ob;
+          bi = oi;
+        }
+      }
+      if (lane == 0) s_p = bi;
+    }
+    __syncthreads();
+    const int64_t p = s_p;
+    const unsigned owner = (unsigned)((p % nthreads) / PANEL_THREADS);
+    if (threadIdx.x < PANEL_NB) {
+      s_u[threadIdx.x] = __ldcg(cand + ((int64_t)par * nblocks + owner) * W + threadIdx.x);
+      s_oldj[threadIdx.x] = __ldcg(rowj_buf + (int64_t)par * PANEL_NB + threadIdx.x);
+    }
+    __syncthreads();
+    T piv = s_u[0];
+#pragma unroll
+    for (int c = 1; c < PANEL_NB; ++c)
+      if (c == j) piv = s_u[c];
+    const T apiv = piv < T(0) ? -piv : piv;
+    const bool nonzero = piv != T(0);
+    // getf2_k.c:103-116: scale (and swap the processed columns) only when
+    // |pivot| >= DBL_MIN.  Columns after j always see the interchange, as the
+    // reference applies the recorded pivots lazily to later columns.
+    const bool scaled = nonzero && apiv >= tiny_pivot<T>();
+    const bool swap = p != j;
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+      ipiv[j] = (int)(p + row_off + 1);
+      if (!nonzero && *info == 0) *info = (int)(j + row_off + 1);
+    }
+    const T rcp = scaled ? T(1) / piv : T(1);
+    // ---- 4. interchange and update the rows this thread owns
+#pragma unroll
+    for (int r = 0; r < R; ++r) {
+      const int64_t i = rows[r];
+      if (i >= m || i < j) continue;
+      if (swap && i == j) {
+#pragma unroll
+        for (int c = 0; c < PANEL_NB; ++c)
+          if (scaled || c > j) v[r][c] = s_u[c];
+        continue;  // the pivot row is final
+      }
+      if (swap && i == p) {
+#pragma unroll
+        for (int c = 0; c < PANEL_NB; ++c)
+          if (scaled || c > j) v[r][c] = s_oldj[c];
+      }
+      if (i == j) continue;
+      T l = v[r][0];
+#pragma unroll
+      for (int c = 1; c < PANEL_NB; ++c)
+        if (c == j) l = v[r][c];
+      if (scaled) l *= rcp;
+#pragma unroll
+      for (int c = 0; c < PANEL_NB; ++c) {
+        if (c == j) v[r][c] = l;
+        if (c > j) v[r][c] = fma(-l, s_u[c], v[r][c]);
+      }
+    }
+  }
+#pragma unroll
+  for (int r = 0; r < R; ++r)
+    if (rows[r] < m)
+#pragma unroll
+      for (int c = 0; c < PANEL_NB; ++c)
+        if (c < nb) A[rows[r] + c * lda] = v[r][c];
+}
+
+
+// Row interchanges (lapack/laswp/generic/laswp_k_1.c semantics): rows
+// k1..k2 (1-based) in order for incx > 0, in reverse for incx < 0; the pivot
+// of row i is ipiv[(k1-1) + (i-k1)*|incx|].  One thread per column applies the
+// interchanges in sequence (each column is independent).
+template <typename T>
+__global__ void laswp_kernel(int64_t n, T *__restrict__ A, int64_t lda, int64_t k1, int64_t k2,
+                             const int *__restrict__ ipiv, int64_t incx) {
+  const int64_t col = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (col >= n) return;
+  T *a = A + col * lda;
+  const int64_t cnt = k2 - k1 + 1;
+  const int64_t ainc = incx < 0 ? -incx : incx;
+  for (int64_t t = 0; t < cnt; ++t) {
+    const int64_t i = incx > 0 ? k1 + t : k2 - t;
+    const int64_t ip = ipiv[(k1 - 1) + (i - k1) * ainc];
+    if (ip != i) {
+      T tmp = a[i - 1];
+      a[i - 1] = a[ip - 1];
+      a[ip - 1] = tmp;
+    }
+  }
+}
+
+// Final permutation of a pivot sequence: row i of P*B is row perm[i] of B.
+// One thread replays the interchanges on an index vector (only used for
+// the solve step, where it replaces many sequential column sweeps).
+__global__ void pivots_to_perm_kernel(int64_t n, const int *__restrict__ ipiv,
+                                      int *__restrict__ perm) {
+  if (blockIdx.x != 0 || threadIdx.x != 0) return;
+  for (int64_t i = 0; i < n; ++i) perm[i] = (int)i;
+  for (int64_t i = 0; i < n; ++i) {
+    const int64_t ip = ipiv[i] - 1;
+    if (ip != i) {
+      int t = perm[i];
+      perm[i] = perm[ip];
+      perm[ip] = t;
+    }
+  }
+}
+
+template <typename T>
+__global__ void permute_rows_kernel(int64_t n, int64_t ncol, const int *__restrict__ perm,
+                                    const T *__restrict__ src, int64_t lds, T *__restrict__ dst,
+                                    int64_t ldd, int inverse) {
+  const int64_t total = n * ncol;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = e / n, i = e - c * n;
+    if (!inverse)
+      dst[i + c * ldd] = src[perm[i] + c * lds];
+    else
+      dst[perm[i] + c * ldd] = src[i + c * lds];
+  }
+}
+
+// Unblocked Cholesky of an nb x nb diagonal block (nb <= PANEL_NB) in
+// shared memory, lapack/potf2/potf2_L.c:50-97 (upper: potf2_U.c, handled by
+// transposing into the lower form).  On the first pivot <= 0 the pivot value
+// is written back and info = row_off + j + 1; later calls see info != 0 and
+// return at once.
+template <typename T>
+__global__ void __launch_bounds__(256)
+potf2_kernel(int upper, int nb, T *__restrict__ A, int64_t lda, int *__restrict__ info,
+             int64_t row_off) {
+  if (*info) return;
+  __shared__ T S[PANEL_NB][PANEL_NB + 1];  // lower-triangular working copy
+  __shared__ int s_fail;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < nb * nb; e += blockDim.x) {
+    int r = e % nb, c = e / nb;
+    if (r >= c) S[r][c] = upper ? A[c + (int64_t)r * lda] : A[r + (int64_t)c * lda];
+  }
+  if (tid == 0) s_fail = -1;
+  __syncthreads();
+  for (int j = 0; j < nb; ++j) {
+    if (tid < 32) {
+      T acc = T(0);
+      for (int p = tid; p < j; p += 32) acc = fma(S[j][p], S[j][p], acc);
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
+      if (tid == 0) {
+        T ajj = S[j][j] - acc;
+        if (ajj <= T(0)) {
+          S[j][j] = ajj;
+          s_fail = j;
+        } else {
+          S[j][j] = sqrt(ajj);
+        }
+      }
+    }
+    __syncthreads();
+    if (s_fail >= 0) break;
+    const T r = T(1) / S[j][j];
+    for (int i = j + 1 + tid; i < nb; i += blockDim.x) {
+      T t = T(0);
+      for (int p = 0; p < j; ++p) t = fma(S[i][p], S[j][p], t);
+      S[i][j] = (S[i][j] - t) * r;
+    }
+    __syncthreads();
+  }
+  const int ncols = s_fail >= 0 ? s_fail + 1 : nb;
+  for (int e = tid; e < nb * nb; e += blockDim.x) {
+    int r = e % nb, c = e / nb;
+    if (r < c || c >= ncols) continue;
+    if (s_fail >= 0 && c == s_fail && r != c) continue;  // column stops at the failing pivot
+    if (upper)
+      A[c + (int64_t)r * lda] = S[r][c];
+    else
+      A[r + (int64_t)c * lda] = S[r][c];
+  }
+  if (tid == 0 && s_fail >= 0) *info = (int)(row_off + s_fail + 1);
+}
+
+template <typename T, int R>
+int launch_panel(int64_t rows, int nb, T *A, int64_t lda, int *ipiv, int64_t row_off, int *info,
+                 T *slots, unsigned *bar, int *status, unsigned nblocks, cudaStream_t s) {
+  void *args[] = {&rows, &nb, &A, &lda, &ipiv, &row_off, &info, &slots, &bar, &status};
+  return check_cuda(cudaLaunchCooperativeKernel((const void *)getf2_panel_kernel<T, R>,
+                                                dim3(nblocks), dim3(PANEL_THREADS), args, 0, s),
+                    "panel factorisation launch");
+}
+
+template <typename T, int R>
+int coop_limit() {
+  static int lim = 0;
+  if (!lim) {
+    int per_sm = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, getf2_panel_kernel<T, R>,
+                                                  PANEL_THREADS, 0);
+    lim = per_sm * sm_count();
+    if (lim <= 0) lim = 1;
+  }
+  return lim;
+}
+
+template <typename T>
+void gemm_minus(int64_t m, int64_t n, int64_t k, const T *A, int64_t lda, const T *B,
+                int64_t ldb, T *C, int64_t ldc, cudaStream_t s);
+template <>
+void gemm_minus<double>(int64_t m, int64_t n, int64_t k, const double *A, int64_t lda,
+                        const double *B, int64_t ldb, double *C, int64_t ldc, cudaStream_t s) {
+  launch_dgemm_fp64(0, 0, m, n, k, -1.0, A, lda, B, ldb, 1.0, C, ldc, s);
+}
+template <>
+void gemm_minus<float>(int64_t m, int64_t n, int64_t k, const float *A, int64_t lda,
+                       const float *B, int64_t ldb, float *C, int64_t ldc, cudaStream_t s) {
+  launch_sgemm_fp32(0, 0, m, n, k, -1.0f, A, lda, B, ldb, 1.0f, C, ldc, s);
+}
+
+template <typename T>
+int trsm_any(int side, int uplo, int trans, int unit, int64_t m, int64_t n, const T *A,
+             int64_t lda, T *B, int64_t ldb, cudaStream_t s);
+template <>
+int trsm_any<double>(int side, int uplo, int trans, int unit, int64_t m, int64_t n,
+                     const double *A, int64_t lda, double *B, int64_t ldb, cudaStream_t s) {
+  return dtrsm_device(side, uplo, trans, unit, m, n, 1.0, A, lda, B, ldb, s);
+}
+template <>
+int trsm_any<float>(int side, int uplo, int trans, int unit, int64_t m, int64_t n,
+                    const float *A, int64_t lda, float *B, int64_t ldb, cudaStream_t s) {
+  return strsm_device(side, uplo, trans, unit, m, n, 1.0f, A, lda, B, ldb, s);
+}
+
+}  // namespace
+
+template <typename T>
+int laswp_device(int64_t n, T *A, int64_t lda, int64_t k1, int64_t k2, const int *ipiv,
+                 int64_t incx, cudaStream_t s) {
+  if (n <= 0 || incx == 0 || k2 < k1) return GB_SUCCESS;
+  laswp_kernel<T><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(n, A, lda, k1, k2, ipiv, incx);
+  return check_cuda(cudaGetLastError(), "laswp launch");
+}
+
+// Right-looking blocked LU (lapack/getrf/getrf_single.c:47-180 with the
+// recursion flattened to PANEL_NB-wide panels): factor the panel, apply its
+// interchanges to the trailing columns, solve with the unit-lower diagonal
+// block, GEMM-update the trailing matrix, and apply the interchanges to the
+// columns left of the panel.
+template <typename T>
+int getrf_device(int64_t m, int64_t n, T *A, int64_t lda, int *ipiv, int *info,
+                 cudaStream_t s) {
+  GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
+  const int64_t mn = m < n ? m : n;
+  if (mn <= 0) return GB_SUCCESS;
+  const int lim1 = coop_limit<T, 1>(), lim2 = coop_limit<T, 2>();
+  const int64_t maxblk = lim1 > lim2 ? lim1 : lim2;
+  const size_t slot_elems = 2 * (size_t)maxblk * (PANEL_NB + 2) + 2 * PANEL_NB;
+  Scratch ws(slot_elems * sizeof(T) + 256, s);
+  if (!ws.p) return GB_ERR_ALLOC;
+  T *slots = ws.as<T>();
+  unsigned *bar = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(ws.p) +
+                                               ((slot_elems * sizeof(T) + 127) & ~size_t(127)));
+  int *status = ctx().d_status;
+  for (int64_t j0 = 0; j0 < mn; j0 += PANEL_NB) {
+    const int jb = (int)((mn - j0) < PANEL_NB ? (mn - j0) : PANEL_NB);
+    const int64_t rows = m - j0;
+    GB_CUDA(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), s));
+    T *P = A + j0 + j0 * lda;
+    int st;
+    const int64_t b1 = (rows + PANEL_THREADS - 1) / PANEL_THREADS;
+    const int64_t b2 = (rows + 2 * PANEL_THREADS - 1) / (2 * PANEL_THREADS);
+    if (b1 <= lim1)
+      st = launch_panel<T, 1>(rows, jb, P, lda, ipiv + j0, j0, info, slots, bar, status,
+                              (unsigned)b1, s);
+    else if (b2 <= lim2)
+      st = launch_panel<T, 2>(rows, jb, P, lda, ipiv + j0, j0, info, slots, bar, status,
+                              (unsigned)b2, s);
+    else
+      return set_error(GB_ERR_UNSUPPORTED, "getrf: %lld rows exceed the panel kernel limit",
+                       (long long)rows);
+    if (st) return st;
+    if (j0 + jb < n) {
+      const int64_t nr = n - j0 - jb;
+      T *A12 = A + j0 + (j0 + jb) * lda;
+      if ((st = laswp_device<T>(nr, A + (j0 + jb) * lda, lda, j0 + 1, j0 + jb, ipiv, 1, s)))
+        return st;
+      if ((st = trsm_any<T>(0, 1, 0, 0, jb, nr, P, lda, A12, lda, s))) return st;
+      if (j0 + jb < m)
+        gemm_minus<T>(m - j0 - jb, nr, jb, P + jb, lda, A12, lda, A12 + jb, lda, s);
+    }
+    if (j0 > 0) {
+      if ((st = laswp_device<T>(j0, A, lda, j0 + 1, j0 + jb, ipiv, 1, s))) return st;
+    }
+  }
+  return check_cuda(cudaGetLastError(), "getrf");
+}
+
+// lapack/getrs/getrs_single.c:42-68.  The interchanges of the solve are
+// applied as one gather through the final permutation.
+template <typename T>
+int getrs_device(int trans, int64_t n, int64_t nrhs, const T *A, int64_t lda, const int *ipiv,
+                 T *B, int64_t ldb, cudaStream_t s) {
+  if (n <= 0 || nrhs <= 0) return GB_SUCCESS;
+  Scratch ws(n * sizeof(int) + (size_t)n * nrhs * sizeof(T) + 256, s);
+  if (!ws.p) return GB_ERR_ALLOC;
+  int *perm = ws.as<int>();
+  T *tmp = reinterpret_cast<T *>(reinterpret_cast<char *>(ws.p) +
+                                 ((n * sizeof(int) + 127) & ~size_t(127)));
+  pivots_to_perm_kernel<<<1, 1, 0, s>>>(n, ipiv, perm);
+  const int64_t total = n * nrhs;
+  const unsigned grid = (unsigned)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
+  int st;
+  if (!trans) {
+    permute_rows_kernel<T><<<grid, 256, 0, s>>>(n, nrhs, perm, B, ldb, tmp, n, 0);
+    GB_CUDA(cudaMemcpy2DAsync(B, ldb * sizeof(T), tmp, n * sizeof(T), n * sizeof(T), nrhs,
+                              cudaMemcpyDeviceToDevice, s));
+    if ((st = trsm_any<T>(0, 1, 0, 0, n, nrhs, A, lda, B, ldb, s))) return st;
+    if ((st = trsm_any<T>(0, 0, 0, 1, n, nrhs, A, lda, B, ldb, s))) return st;
+  } else {
+    if ((st = trsm_any<T>(0, 0, 1, 1, n, nrhs, A, lda, B, ldb, s))) return st;
+    if ((st = trsm_any<T>(0, 1, 1, 0, n, nrhs, A, lda, B, ldb, s))) return st;
+    permute_rows_kernel<T><<<grid, 256, 0, s>>>(n, nrhs, perm, B, ldb, tmp, n, 1);
+    GB_CUDA(cudaMemcpy2DAsync(B, ldb * sizeof(T), tmp, n * sizeof(T), n * sizeof(T), nrhs,
+                              cudaMemcpyDeviceToDevice, s));
+  }
+  return check_cuda(cudaGetLastError(), "getrs");
+}
+
+// Right-looking blocked Cholesky (lapack/potrf/potrf_L_single.c:81-236,
+// potrf_U_single.c:79-193): potf2 on the diagonal block, TRSM of the panel,
+// SYRK of the trailing matrix.  Every kernel after a failed potf2 sees info
+// != 0 and does nothing, so the matrix is left as at the failure point.
+int potrf_device(int uplo, int64_t n, double *A, int64_t lda, int *info, cudaStream_t s) {
+  GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
+  const bool upper = uplo == 0;
+  for (int64_t j0 = 0; j0 < n; j0 += PANEL_NB) {
+    const int jb = (int)((n - j0) < PANEL_NB ? (n - j0) : PANEL_NB);
+    double *D = A + j0 + j0 * lda;
+    potf2_kernel<double><<<1, 256, 0, s>>>(upper ? 1 : 0, jb, D, lda, info, j0);
+    const int64_t rest = n - j0 - jb;
+    if (rest <= 0) continue;
+    int st;
+    if (!upper) {
+      double *P = A + (j0 + jb) + j0 * lda;
+      if ((st = dtrsm_device_skip(1, 1, 1, 1, rest, jb, 1.0, D, lda, P, lda, s, info))) return st;
+      if ((st = dsyrk_device_skip(1, 0, rest, jb, -1.0, P, lda, 1.0, P + jb * lda, lda, s, info)))
+        return st;
+    } else {
+      double *P = A + j0 + (j0 + jb) * lda;
+      if ((st = dtrsm_device_skip(0, 0, 1, 1, jb, rest, 1.0, D, lda, P, lda, s, info))) return st;
+      if ((st = dsyrk_device_skip(0, 1, rest, jb, -1.0, P, lda, 1.0, P + jb, lda, s, info)))
+        return st;
+    }
+  }
+  return check_cuda(cudaGetLastError(), "potrf");
+}
+
+template int getrf_device<double>(int64_t, int64_t, double *, int64_t, int *, int *,
+                                  cudaStream_t);
+template int getrf_device<float>(int64_t, int64_t, float *, int64_t, int *, int *, cudaStream_t);
+template int getrs_device<double>(int, int64_t, int64_t, const double *, int64_t, const int *,
+                                  double *, int64_t, cudaStream_t);
+template int getrs_device<float>(int, int64_t, int64_t, const float *, int64_t, const int *,
+                                 float *, int64_t, cudaStream_t);
+template int laswp_device<double>(int64_t, double *, int64_t, int64_t, int64_t, const int *,
+                                  int64_t, cudaStream_t);
+template int laswp_device<float>(int64_t, float *, int64_t, int64_t, int64_t, const int *,
+                                 int64_t, cudaStream_t);
+
+}  // namespace gb

@@ -1,0 +1,166 @@
+"""C-ABI boundary checks that need no GPU: every symbol declared in
+include/*.h is exported, argument errors reach xerbla with the reference's
+parameter positions (interface/*.c), LAPACK routines set Info = -position,
+and quick returns do not touch the device."""
+from __future__ import annotations
+
+import ctypes as C
+import glob
+import os
+import re
+
+import numpy as np
+import pytest
+
+import openblas_gb300 as gb
+from openblas_gb300 import abi
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_functions():
+    names = set()
+    for h in glob.glob(os.path.join(ROOT, "include", "*.h")):
+        src = open(h).read()
+        src = re.sub(r"/\*.*?\*/", "", src, flags=re.S)
+        for m in re.finditer(r"\b([A-Za-z_][A-Za-z0-9_]*)\s*\(", src):
+            name = m.group(1)
+            start = src.rfind("\n", 0, m.start())
+            line = src[start:m.start()]
+            if re.search(r"\b(void|int|const char \*|void \*|double|float)\s*\**\s*$", line):
+                names.add(name)
+    return sorted(names)
+
+
+def test_exports_every_declared_symbol(gblib):
+    names = declared_functions()
+    assert len(names) >= 30
+    missing = [n for n in names if not hasattr(gblib, n)]
+    assert not missing, missing
+
+
+def test_version(gblib):
+    assert b"sm_103a" in gblib.gb_version()
+
+
+def _xerbla(gblib):
+    return gb.last_xerbla(gblib)
+
+
+@pytest.mark.parametrize("args,pos", [
+    (("X", "N", 4, 4, 4, 4, 4, 4), 1),
+    (("N", "X", 4, 4, 4, 4, 4, 4), 2),
+    (("N", "N", -1, 4, 4, 4, 4, 4), 3),
+    (("N", "N", 4, -1, 4, 4, 4, 4), 4),
+    (("N", "N", 4, 4, -1, 4, 4, 4), 5),
+    (("N", "N", 4, 4, 4, 3, 4, 4), 8),
+    (("T", "N", 4, 4, 5, 4, 5, 4), 8),
+    (("N", "N", 4, 4, 4, 4, 3, 4), 10),
+    (("N", "T", 4, 5, 4, 4, 4, 4), 10),
+    (("N", "N", 4, 4, 4, 4, 4, 3), 13),
+])
+def test_dgemm_argument_errors(gblib, F, args, pos):
+    ta, tb, m, n, k, lda, ldb, ldc = args
+    buf = np.zeros((64, 64), order="F")
+    gblib.gb_clear_error()
+    F.dgemm(ta, tb, m, n, k, 1.0, buf, lda, buf, ldb, 0.0, buf, ldc)
+    name, info = _xerbla(gblib)
+    assert name.strip() == "DGEMM" and info == pos
+
+
+def test_cblas_rowmajor_positions(gblib):
+    ns = gb.cblas()
+    buf = np.zeros(256)
+    gblib.gb_clear_error()
+    # row-major A is m x k with lda >= k; the operand swap reports it as B (10)
+    ns.cblas_dgemm(abi.CblasRowMajor, abi.CblasNoTrans, abi.CblasNoTrans, 4, 3, 5, 1.0,
+                   buf.ctypes.data, 4, buf.ctypes.data, 3, 0.0, buf.ctypes.data, 3)
+    assert _xerbla(gblib) == ("DGEMM ", 10)
+    gblib.gb_clear_error()
+    ns.cblas_dgemm(77, abi.CblasNoTrans, abi.CblasNoTrans, 4, 3, 5, 1.0, buf.ctypes.data, 4,
+                   buf.ctypes.data, 5, 0.0, buf.ctypes.data, 4)
+    assert _xerbla(gblib)[1] == 0  # invalid order: xerbla with position 0
+    gblib.gb_clear_error()
+    ns.cblas_dtrsm(abi.CblasColMajor, 99, abi.CblasLower, abi.CblasNoTrans, abi.CblasNonUnit, 4,
+                   4, 1.0, buf.ctypes.data, 4, buf.ctypes.data, 4)
+    assert _xerbla(gblib) == ("DTRSM ", 1)
+    gblib.gb_clear_error()
+    ns.cblas_dsyrk(abi.CblasColMajor, abi.CblasLower, abi.CblasNoTrans, 5, 2, 1.0,
+                   buf.ctypes.data, 4, 0.0, buf.ctypes.data, 5)
+    assert _xerbla(gblib) == ("DSYRK ", 7)
+
+
+@pytest.mark.parametrize("args,pos", [
+    (("X", "L", "N", "N", 4, 4, 4, 4), 1),
+    (("L", "X", "N", "N", 4, 4, 4, 4), 2),
+    (("L", "L", "X", "N", 4, 4, 4, 4), 3),
+    (("L", "L", "N", "X", 4, 4, 4, 4), 4),
+    (("L", "L", "N", "N", -1, 4, 4, 4), 5),
+    (("L", "L", "N", "N", 4, -1, 4, 4), 6),
+    (("L", "L", "N", "N", 4, 4, 3, 4), 9),
+    (("R", "L", "N", "N", 4, 5, 4, 4), 9),
+    (("L", "L", "N", "N", 4, 4, 4, 3), 11),
+])
+def test_dtrsm_argument_errors(gblib, F, args, pos):
+    side, uplo, ta, diag, m, n, lda, ldb = args
+    buf = np.zeros((64, 64), order="F")
+    gblib.gb_clear_error()
+    F.dtrsm(side, uplo, ta, diag, m, n, 1.0, buf, lda, buf, ldb)
+    assert _xerbla(gblib) == ("DTRSM ", pos)
+
+
+def test_dsyrk_argument_errors(gblib, F):
+    buf = np.zeros((64, 64), order="F")
+    for args, pos in [(("X", "N", 4, 4, 4, 4), 1), (("L", "X", 4, 4, 4, 4), 2),
+                      (("L", "N", -1, 4, 4, 4), 3), (("L", "N", 4, -1, 4, 4), 4),
+                      (("L", "N", 4, 4, 3, 4), 7), (("L", "T", 4, 5, 4, 4), 7),
+                      (("L", "N", 4, 4, 4, 3), 10)]:
+        uplo, tr, n, k, lda, ldc = args
+        gblib.gb_clear_error()
+        F.dsyrk(uplo, tr, n, k, 1.0, buf, lda, 0.0, buf, ldc)
+        assert _xerbla(gblib) == ("DSYRK ", pos), args
+
+
+def test_lapack_argument_errors(gblib, F):
+    buf = np.zeros((64, 64), order="F")
+    piv = np.zeros(64, np.int32)
+    assert F.dgetrf(-1, 4, buf, 4, piv) == -1
+    assert F.dgetrf(4, -1, buf, 4, piv) == -2
+    assert F.dgetrf(4, 4, buf, 3, piv) == -4
+    assert _xerbla(gblib) == ("DGETRF", 4)
+    assert F.dpotrf("X", 4, buf, 4) == -1
+    assert F.dpotrf("L", -2, buf, 4) == -2
+    assert F.dpotrf("U", 4, buf, 3) == -4
+    assert F.dgesv(-1, 1, buf, 4, piv, buf, 4) == -1
+    assert F.dgesv(4, -1, buf, 4, piv, buf, 4) == -2
+    assert F.dgesv(4, 1, buf, 3, piv, buf, 4) == -4
+    assert F.dgesv(4, 1, buf, 4, piv, buf, 3) == -7
+    gblib.gb_clear_error()
+    F.dgetrs("X", 4, 1, buf, 4, piv, buf, 4)
+    assert _xerbla(gblib) == ("DGETRS", 1)
+    F.dgetrs("N", 4, 1, buf, 4, piv, buf, 3)
+    assert _xerbla(gblib) == ("DGETRS", 8)
+
+
+def test_quick_returns_do_not_touch_device(gblib, F):
+    """m==0/n==0 quick returns happen before any CUDA call, so they succeed on
+    a machine without a GPU (interface/gemm.c:494, getrf.c:83, potrf.c:104)."""
+    buf = np.zeros((4, 4), order="F")
+    piv = np.zeros(4, np.int32)
+    gblib.gb_clear_error()
+    F.dgemm("N", "N", 0, 4, 4, 1.0, buf, 4, buf, 4, 0.0, buf, 4)
+    F.dtrsm("L", "L", "N", "N", 4, 0, 1.0, buf, 4, buf, 4)
+    F.dsyrk("L", "N", 0, 4, 1.0, buf, 4, 0.0, buf, 4)
+    assert F.dgetrf(0, 4, buf, 4, piv) == 0
+    assert F.dpotrf("L", 0, buf, 4) == 0
+    assert F.dgesv(0, 1, buf, 4, piv, buf, 4) == 0
+    F.dlaswp(4, buf, 4, 1, 4, piv, 0)
+    assert gb.last_error(gblib)[0] == 0
+
+
+def test_xerbla_message_format(gblib, capfd):
+    """driver/others/xerbla.c:58: ' ** On entry to %6s parameter number %2d ...'"""
+    info = C.c_int(3)
+    gblib.xerbla_(b"DGEMM ", C.byref(info), 6)
+    out = capfd.readouterr().out
+    assert " ** On entry to DGEMM  parameter number  3 had an illegal value" in out

@@ -1,0 +1,234 @@
+"""GPU parity of the level-3 BLAS entry points against the oracle and the
+OpenBLAS golden vectors.  GEMM/TRSM/SYRK use the DMMCH-style bound of
+ctest/c_dblat3c.c:2956: |C - Cref| <= c * eps * (|alpha||A||B| + |beta||C|),
+with c = 2(k+2) (both results carry <= (k+2) eps rounding)."""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import EPS, dmmch_ratio
+
+sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+import gen_golden as GG  # noqa: E402
+
+import openblas_gb300 as gb  # noqa: E402
+from openblas_gb300 import abi  # noqa: E402
+from openblas_gb300 import workloads as W  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def test_dgemm_golden_cases(golden, orc, F, gb_clean):
+    idx = 0
+    for (m, n, k) in GG.GEMM_SHAPES:
+        for (alpha, beta) in GG.GEMM_AB:
+            for ta in "NT":
+                for tb in "NT":
+                    A, B, Cm = W.gemm_operands(GG.gemm_case_seed(idx), m, n, k, ta, tb, pad=3)
+                    C0 = Cm.copy(order="F")
+                    if beta == 0.0:
+                        Cm[:m, :n] = np.nan
+                    F.dgemm(ta, tb, m, n, k, alpha, A, A.shape[0], B, B.shape[0], beta, Cm,
+                            Cm.shape[0])
+                    G = orc.dgemm_absbound(ta, tb, m, n, k, alpha, A, A.shape[0], B, B.shape[0],
+                                           beta, C0, C0.shape[0])
+                    assert not np.isnan(Cm[:m, :n]).any(), idx
+                    r = dmmch_ratio(Cm[:m, :n], golden[f"dgemm_{idx}"], G, k)
+                    assert r <= 2 * (k + 2), (idx, m, n, k, ta, tb, alpha, beta, r)
+                    assert np.array_equal(Cm[m:, :], C0[m:, :])  # padding untouched
+                    idx += 1
+
+
+def test_dgemm_c1_1024(golden, F, gb_clean):
+    """1024^3 NN alpha=1.5 beta=0.5 -- the reference's CPU-runnable case."""
+    A, B, Cm = W.gemm_operands(42, 1024, 1024, 1024)
+    F.dgemm("N", "N", 1024, 1024, 1024, 1.5, A, 1024, B, 1024, 0.5, Cm, 1024)
+    G = 1.5 * np.abs(A) @ np.abs(B) + 0.5 * np.abs(W.gemm_operands(42, 1024, 1024, 1024)[2])
+    assert np.allclose(Cm.sum(axis=0), golden["dgemm_c1_colsum"], rtol=0,
+                       atol=2 * 1026 * EPS * G.sum(axis=0).max())
+    r = dmmch_ratio(Cm[::37, ::41], golden["dgemm_c1_sample"], G[::37, ::41], 1024)
+    assert r <= 2 * 1026
+
+
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("N", "T"), ("T", "N"), ("T", "T")])
+def test_dgemm_padded_lda_vs_oracle(orc, F, gb_clean, ta, tb):
+    m, n, k = 1000, 777, 613
+    A, B, Cm = W.gemm_operands(91, m, n, k, ta, tb, pad=8)
+    C0, Co = Cm.copy(order="F"), Cm.copy(order="F")
+    F.dgemm(ta, tb, m, n, k, -0.75, A, A.shape[0], B, B.shape[0], 1.25, Cm, Cm.shape[0])
+    orc.dgemm(ta, tb, m, n, k, -0.75, A, A.shape[0], B, B.shape[0], 1.25, Co, Co.shape[0])
+    G = orc.dgemm_absbound(ta, tb, m, n, k, -0.75, A, A.shape[0], B, B.shape[0], 1.25, C0,
+                           C0.shape[0])
+    assert dmmch_ratio(Cm[:m], Co[:m], G, k) <= 2 * (k + 2)
+    assert np.array_equal(Cm[m:], C0[m:])
+
+
+def test_dgemm_rowmajor_cblas(gb_clean):
+    ns = gb.cblas()
+    m, n, k = 37, 29, 41
+    A = np.ascontiguousarray(W.uniform(5, (m, k)))   # row-major m x k
+    B = np.ascontiguousarray(W.uniform(6, (k, n)))
+    C = np.ascontiguousarray(W.uniform(7, (m, n)))
+    ref = 0.5 * A @ B + 2.0 * C
+    ns.cblas_dgemm(abi.CblasRowMajor, abi.CblasNoTrans, abi.CblasNoTrans, m, n, k, 0.5,
+                   A.ctypes.data, k, B.ctypes.data, n, 2.0, C.ctypes.data, n)
+    assert np.max(np.abs(C - ref)) <= 4 * (k + 2) * EPS * (np.abs(A) @ np.abs(B) + 2).max()
+
+
+def test_dgemm_device_pointers(orc, gblib, gb_clean):
+    torch = pytest.importorskip("torch")
+    m, n, k = 300, 257, 190
+    A, B, Cm = W.gemm_operands(13, m, n, k, "T", "N", pad=8)
+    dA = torch.from_numpy(A.T.copy()).cuda()  # row-major copy of the column-major buffer
+    dB = torch.from_numpy(B.T.copy()).cuda()
+    dC = torch.from_numpy(Cm.T.copy()).cuda()
+    st = gblib.gb_dgemm_native_dev(b"T", b"N", m, n, k, 0.5, dA.data_ptr(), A.shape[0],
+                                   dB.data_ptr(), B.shape[0], -1.0, dC.data_ptr(), Cm.shape[0])
+    assert st == 0
+    assert gblib.gb_synchronize() == 0
+    got = dC.cpu().numpy().T
+    Co = Cm.copy(order="F")
+    orc.dgemm("T", "N", m, n, k, 0.5, A, A.shape[0], B, B.shape[0], -1.0, Co, Co.shape[0])
+    G = orc.dgemm_absbound("T", "N", m, n, k, 0.5, A, A.shape[0], B, B.shape[0], -1.0, Cm,
+                           Cm.shape[0])
+    assert dmmch_ratio(got[:m], Co[:m], G, k) <= 2 * (k + 2)
+
+
+def test_sgemm(golden, F, gb_clean):
+    A, B, Cm = W.gemm_operands(77, 35, 33, 64, "N", "T", dtype=np.float32)
+    C0 = Cm.copy(order="F")
+    F.sgemm("N", "T", 35, 33, 64, 0.7, A, 35, B, 33, 1.3, Cm, 35)
+    G = 0.7 * np.abs(A.astype(np.float64)) @ np.abs(B.astype(np.float64)).T + 1.3 * np.abs(C0)
+    feps = np.finfo(np.float32).eps
+    assert np.max(np.abs(Cm - golden["sgemm_0"]) / (feps * G)) <= 2 * 66
+
+
+def test_sgemm_large(F, gb_clean):
+    m, n, k = 1536, 1100, 700
+    A, B, Cm = W.gemm_operands(78, m, n, k, "T", "N", dtype=np.float32)
+    ref = 1.0 * A.astype(np.float64).T @ B.astype(np.float64) + 0.5 * Cm.astype(np.float64)
+    G = np.abs(A.astype(np.float64)).T @ np.abs(B.astype(np.float64)) + 0.5 * np.abs(Cm)
+    F.sgemm("T", "N", m, n, k, 1.0, A, k, B, k, 0.5, Cm, m)
+    feps = np.finfo(np.float32).eps
+    assert np.max(np.abs(Cm - ref) / (feps * G)) <= (k + 2)
+
+
+def test_dtrsm_golden_cases(golden, F, gb_clean):
+    idx = 0
+    for (m, n) in GG.TRSM_SHAPES:
+        for side in "LR":
+            for uplo in "UL":
+                for ta in "NT":
+                    for diag in "UN":
+                        for alpha in GG.TRSM_ALPHA:
+                            na = m if side == "L" else n
+                            A = W.trsm_lower(3000 + idx, na)
+                            if uplo == "U":
+                                A = np.asfortranarray(A.T)
+                            B = W.uniform(4000 + idx, (m, n))
+                            F.dtrsm(side, uplo, ta, diag, m, n, alpha, A, na, B, m)
+                            ref = golden[f"dtrsm_{idx}"]
+                            scale = max(1.0, np.abs(ref).max())
+                            assert np.max(np.abs(B - ref)) <= 64 * na * EPS * scale, (
+                                idx, side, uplo, ta, diag, alpha)
+                            idx += 1
+
+
+@pytest.mark.parametrize("side,uplo,ta,diag", [
+    (s, u, t, d) for s in "LR" for u in "UL" for t in "NT" for d in "UN"])
+def test_dtrsm_blocked_vs_oracle(orc, F, gb_clean, side, uplo, ta, diag):
+    """Sizes that cross several 32-wide diagonal blocks (GEMM updates active)."""
+    m, n = 203, 150
+    na = m if side == "L" else n
+    A = W.trsm_lower(31, na)
+    if uplo == "U":
+        A = np.asfortranarray(A.T)
+    if diag == "U":
+        # unit-diagonal solves of a random triangle grow quickly; keep it tame
+        A = np.asfortranarray(np.where(np.eye(na) == 1, A, A / na))
+    B = W.uniform(32, (m, n))
+    Bo = B.copy(order="F")
+    F.dtrsm(side, uplo, ta, diag, m, n, 0.7, A, na, B, m)
+    orc.dtrsm(side, uplo, ta, diag, m, n, 0.7, A, na, Bo, m)
+    assert np.max(np.abs(B - Bo)) <= 1e3 * na * EPS * max(1.0, np.abs(Bo).max())
+
+
+def test_dtrsm_config_8192_rows_property(F, gb_clean):
+    """Left/Lower/NoTrans/NonUnit with diag n+U(0,1) (the level-3 sweep's TRSM
+    operand) on a tall problem: the residual L*X - alpha*B is at rounding level."""
+    m, n = 2048, 64
+    L = W.trsm_lower(55, m)
+    B = W.uniform(56, (m, n))
+    X = B.copy(order="F")
+    F.dtrsm("L", "L", "N", "N", m, n, 1.0, L, m, X, m)
+    res = np.abs(L @ X - B).max() / (np.abs(L).sum(axis=1).max() * np.abs(X).max())
+    assert res <= 4 * m * EPS
+
+
+def test_dsyrk_golden_cases(golden, F, gb_clean):
+    idx = 0
+    for (n, k) in GG.SYRK_SHAPES:
+        for uplo in "UL":
+            for tr in "NT":
+                for (alpha, beta) in GG.SYRK_AB:
+                    ra, ca = (n, k) if tr == "N" else (k, n)
+                    A = W.uniform(5000 + idx, (ra, ca))
+                    Cm = W.uniform(6000 + idx, (n, n))
+                    C0 = Cm.copy(order="F")
+                    F.dsyrk(uplo, tr, n, k, alpha, A, ra, beta, Cm, n)
+                    ref = golden[f"dsyrk_{idx}"]
+                    assert np.max(np.abs(Cm - ref)) <= 4 * (k + 2) * EPS * 3, idx
+                    other = np.triu(C0, 1) if uplo == "L" else np.tril(C0, -1)
+                    got_other = np.triu(Cm, 1) if uplo == "L" else np.tril(Cm, -1)
+                    assert np.array_equal(other, got_other), idx
+                    idx += 1
+
+
+def test_dsyrk_large(orc, F, gb_clean):
+    n, k = 700, 333
+    for uplo in "UL":
+        for tr in "NT":
+            ra, ca = (n, k) if tr == "N" else (k, n)
+            A = W.uniform(60, (ra, ca))
+            Cm = W.uniform(61, (n, n))
+            Co = Cm.copy(order="F")
+            F.dsyrk(uplo, tr, n, k, -1.0, A, ra, 0.5, Cm, n)
+            orc.dsyrk(uplo, tr, n, k, -1.0, A, ra, 0.5, Co, n)
+            assert np.max(np.abs(Cm - Co)) <= 4 * (k + 2) * EPS * k
+
+
+def test_dgemm_batch_grouped(orc, gb_clean):
+    ns = gb.cblas()
+    import ctypes as C
+    groups = [(17, 9, 33, "N", "T", 1.0, 0.0, 3), (40, 41, 8, "T", "N", -0.5, 2.0, 2)]
+    ta, tb, ms, ns_, ks, al, be, lda, ldb, ldc, gs = ([] for _ in range(11))
+    Aps, Bps, Cps, keep, refs = [], [], [], [], []
+    seed = 900
+    for (m, n, k, a, b, alpha, beta, cnt) in groups:
+        ta.append(abi.CblasNoTrans if a == "N" else abi.CblasTrans)
+        tb.append(abi.CblasNoTrans if b == "N" else abi.CblasTrans)
+        ms.append(m); ns_.append(n); ks.append(k); al.append(alpha); be.append(beta)
+        gs.append(cnt)
+        for _ in range(cnt):
+            A, B, Cm = W.gemm_operands(seed, m, n, k, a, b, pad=1)
+            seed += 3
+            Co = Cm.copy(order="F")
+            orc.dgemm(a, b, m, n, k, alpha, A, A.shape[0], B, B.shape[0], beta, Co, Co.shape[0])
+            keep += [A, B, Cm]
+            refs.append((Cm, Co, k))
+            Aps.append(A.ctypes.data); Bps.append(B.ctypes.data); Cps.append(Cm.ctypes.data)
+        lda.append(A.shape[0]); ldb.append(B.shape[0]); ldc.append(Cm.shape[0])
+
+    def iarr(v):
+        return (C.c_int * len(v))(*v)
+
+    ns.cblas_dgemm_batch(abi.CblasColMajor, iarr(ta), iarr(tb), iarr(ms), iarr(ns_), iarr(ks),
+                         (C.c_double * 2)(*al), (C.c_void_p * len(Aps))(*Aps), iarr(lda),
+                         (C.c_void_p * len(Bps))(*Bps), iarr(ldb), (C.c_double * 2)(*be),
+                         (C.c_void_p * len(Cps))(*Cps), iarr(ldc), 2, iarr(gs))
+    for (Cm, Co, k) in refs:
+        assert np.max(np.abs(Cm - Co)) <= 4 * (k + 2) * EPS * k * 4

@@ -1,0 +1,173 @@
+"""GPU parity of the LAPACK entry points: pivots identical to OpenBLAS's,
+scaled residuals ||PA-LU||/(n eps ||A||) <= 10, Cholesky and solve residuals,
+info codes on singular / non-SPD inputs."""
+from __future__ import annotations
+
+import os
+import sys
+
+import numpy as np
+import pytest
+
+from conftest import EPS
+
+sys.path.insert(0, os.path.join(os.path.dirname(__file__), "golden"))
+import gen_golden as GG  # noqa: E402
+
+from openblas_gb300 import workloads as W  # noqa: E402
+
+pytestmark = pytest.mark.gpu
+
+
+def lu_residual(A0, LU, ipiv):
+    m, n = A0.shape
+    mn = min(m, n)
+    L = np.tril(LU[:, :mn], -1) + np.eye(m, mn)
+    U = np.triu(LU[:mn, :])
+    PA = A0.copy(order="F")
+    for i in range(mn):
+        p = ipiv[i] - 1
+        if p != i:
+            PA[[i, p], :] = PA[[p, i], :]
+    nrm = np.abs(A0).sum(axis=0).max()
+    return np.abs(PA - L @ U).sum(axis=0).max() / (max(m, n) * EPS * nrm)
+
+
+def test_dgetrf_golden(golden, F, gb_clean):
+    for idx, (m, n) in enumerate(GG.GETRF_SHAPES):
+        A0 = W.uniform(7000 + idx, (m, n))
+        A = A0.copy(order="F")
+        ipiv = np.zeros(min(m, n), np.int32)
+        info = F.dgetrf(m, n, A, m, ipiv)
+        assert info == int(golden[f"dgetrf_{idx}_info"])
+        assert np.array_equal(ipiv, golden[f"dgetrf_{idx}_ipiv"]), (m, n)
+        if f"dgetrf_{idx}_lu" in golden:
+            assert np.max(np.abs(A - golden[f"dgetrf_{idx}_lu"])) < 1e-11
+        assert lu_residual(A0, A, ipiv) <= 10
+    for n in GG.GETRF_PIV_ONLY:
+        A0 = W.uniform(7100 + n, (n, n))
+        A = A0.copy(order="F")
+        ipiv = np.zeros(n, np.int32)
+        assert F.dgetrf(n, n, A, n, ipiv) == 0
+        assert np.array_equal(ipiv, golden[f"dgetrf_piv{n}"])
+        assert lu_residual(A0, A, ipiv) <= 10
+
+
+def test_dgetrf_singular(golden, F, gb_clean):
+    A = W.uniform(7200, (9, 9))
+    A[:, 3] = 0.0
+    ipiv = np.zeros(9, np.int32)
+    assert F.dgetrf(9, 9, A, 9, ipiv) == 4
+    assert np.array_equal(ipiv, golden["dgetrf_sing_ipiv"])
+    assert np.max(np.abs(A - golden["dgetrf_sing_lu"])) < 1e-12
+
+
+@pytest.mark.parametrize("m,n", [(3000, 3000), (2500, 1800), (1200, 2100)])
+def test_dgetrf_vs_oracle(orc, F, gb_clean, m, n):
+    A0 = W.uniform(7600 + m, (m, n))
+    A, Ao = A0.copy(order="F"), A0.copy(order="F")
+    p, po = np.zeros(min(m, n), np.int32), np.zeros(min(m, n), np.int32)
+    assert F.dgetrf(m, n, A, m, p) == orc.dgetrf(m, n, Ao, m, po) == 0
+    assert np.array_equal(p, po)
+    assert np.max(np.abs(A - Ao)) <= 1e-9 * np.abs(Ao).max()
+    assert lu_residual(A0, A, p) <= 10
+
+
+def test_dgetrf_tiny_pivot_rule(orc, F, gb_clean):
+    """A subnormal pivot is recorded but neither swapped nor divided by
+    (getf2_k.c:103-116); the GPU panel follows the same rule."""
+    n = 40
+    A0 = W.uniform(77, (n, n)) * 1e-310
+    A0[:, 5:] = W.uniform(78, (n, n - 5))
+    A, Ao = A0.copy(order="F"), A0.copy(order="F")
+    p, po = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    assert F.dgetrf(n, n, A, n, p) == orc.dgetrf(n, n, Ao, n, po)
+    assert np.array_equal(p, po)
+    assert np.max(np.abs(A - Ao)) <= 1e-9 * np.abs(Ao).max()
+
+
+def test_dgetrs_dgesv(golden, F, gb_clean):
+    for t, trans in enumerate("NT"):
+        for nrhs in (1, 5):
+            n = 64
+            A = W.uniform(7300 + t, (n, n))
+            ipiv = np.zeros(n, np.int32)
+            F.dgetrf(n, n, A, n, ipiv)
+            B = W.uniform(7400 + nrhs, (n, nrhs))
+            assert F.dgetrs(trans, n, nrhs, A, n, ipiv, B, n) == 0
+            ref = golden[f"dgetrs_{trans}_{nrhs}"]
+            assert np.max(np.abs(B - ref)) <= 1e-10 * max(1, np.abs(ref).max())
+    A = W.uniform(7500, (100, 100))
+    B = W.uniform(7501, (100, 3))
+    ipiv = np.zeros(100, np.int32)
+    assert F.dgesv(100, 3, A, 100, ipiv, B, 100) == 0
+    assert np.array_equal(ipiv, golden["dgesv_ipiv"])
+    assert np.max(np.abs(B - golden["dgesv_x"])) <= 1e-10 * np.abs(B).max()
+
+
+@pytest.mark.parametrize("nrhs", [1, 64])
+def test_dgesv_residual(F, gb_clean, nrhs):
+    n = 2000
+    A0 = W.uniform(3, (n, n))
+    B0 = W.uniform(4, (n, nrhs))
+    A, X = A0.copy(order="F"), B0.copy(order="F")
+    ipiv = np.zeros(n, np.int32)
+    assert F.dgesv(n, nrhs, A, n, ipiv, X, n) == 0
+    r = np.abs(B0 - A0 @ X).sum(axis=0).max()
+    scaled = r / (np.abs(A0).sum(axis=0).max() * np.abs(X).sum(axis=0).max() * EPS * n)
+    assert scaled <= 10
+
+
+def test_dgesv_singular_skips_solve(F, gb_clean):
+    n = 10
+    A = W.uniform(9, (n, n))
+    A[:, 6] = 0.0
+    B = W.uniform(10, (n, 2))
+    B0 = B.copy(order="F")
+    ipiv = np.zeros(n, np.int32)
+    assert F.dgesv(n, 2, A, n, ipiv, B, n) == 7
+    assert np.array_equal(B, B0)  # gesv.c:131: getrs only when info == 0
+
+
+def test_dpotrf_golden(golden, F, gb_clean):
+    for n in GG.POTRF_N:
+        for uplo in "LU":
+            A0 = W.spd(8000 + n, n)
+            A = A0.copy(order="F")
+            assert F.dpotrf(uplo, n, A, n) == 0
+            tri = np.tril if uplo == "L" else np.triu
+            assert np.max(np.abs(tri(A) - tri(golden[f"dpotrf_{uplo}_{n}"]))) < 1e-12
+            other = (lambda X: np.triu(X, 1)) if uplo == "L" else (lambda X: np.tril(X, -1))
+            assert np.array_equal(other(A), other(A0))
+
+
+def test_dpotrf_not_positive_definite(golden, F, gb_clean):
+    A = W.spd(8100, 20)
+    A[11, 11] = -1.0
+    assert F.dpotrf("L", 20, A, 20) == 12
+    ref = golden["dpotrf_npd"]
+    assert np.max(np.abs(np.tril(A)[:, :12] - np.tril(ref)[:, :12])) < 1e-12
+    n = 300  # failure inside a later diagonal block
+    A = W.spd(8101, n)
+    A[200, 200] = -5.0
+    assert F.dpotrf("U", n, A, n) == 201
+
+
+@pytest.mark.parametrize("uplo", ["L", "U"])
+def test_dpotrf_residual(F, gb_clean, uplo):
+    n = 1500
+    A0 = W.spd(8200, n)
+    A = A0.copy(order="F")
+    assert F.dpotrf(uplo, n, A, n) == 0
+    Lf = np.tril(A) if uplo == "L" else np.triu(A).T
+    r = np.abs(A0 - Lf @ Lf.T).sum(axis=0).max() / (n * EPS * np.abs(A0).sum(axis=0).max())
+    assert r <= 10
+
+
+def test_dlaswp_golden(golden, F, gb_clean):
+    for idx, (n, k1, k2, incx) in enumerate(GG.LASWP_CASES):
+        rows = 12
+        A = W.uniform(8200 + idx, (rows, n))
+        ipiv = golden[f"dlaswp_{idx}_ipiv"].astype(np.int32)
+        F.dlaswp(n, A, rows, k1, k2, ipiv, incx)
+        assert np.array_equal(A, golden[f"dlaswp_{idx}"]), (n, k1, k2, incx)
