@@ -1,8 +1,566 @@
-// Emulated FP64 GEMM (placeholder until the tensor-core path lands).
+// Emulated FP64 GEMM on the bf16 tensor cores (Ozaki splitting).
+//
+// C = alpha*op(A)*op(B) + beta*C is computed from fixed-point slices:
+//   1. split: every row i of op(A) is scaled by 2^-e_i (e_i = exponent of
+//      the row's max |a|), truncated to S*7 bits and cut into S signed 7-bit
+//      digits A_1..A_S (|digit| <= 127, exactly representable in bf16);
+//      columns of op(B) likewise with exponents f_j.  Slices are stored
+//      K-contiguous and zero-padded to the tile grid, whatever the caller's
+//      transpose and leading dimension.
+//   2. slice GEMM (tcgen05, kind::f16): for each output tile and each level
+//      L = s+t (2..S+1, the Ozaki triangle), the products A_s*B_t^T are
+//      accumulated in TMEM in FP32 over K-chunks of 1024.  With |digit| <=
+//      127, every partial sum of a chunk is an integer below 2^24, so the
+//      FP32 accumulation is exact; each chunk is drained to int32 registers
+//      (exact conversion) and summed per level.  A level sum of up to S
+//      products over K <= 16384 stays below 2^31.  Level sums are written as
+//      int32 planes.
+//   3. recombine (FP64): C_ij = alpha * 2^(e_i+f_j) * sum_L P_L,ij 2^(-7L)
+//      + beta*C_ij.  Rows/columns holding Inf/NaN fall back to a direct FP64
+//      dot product so IEEE special values propagate.
+//
+// The slice GEMM is a persistent warp-specialised kernel, one CTA per SM:
+// warp 0 issues TMA loads of 128x64 (A) and 256x64 (B) bf16 tiles into a
+// 4-stage shared-memory ring, warp 1 issues tcgen05.mma (M=128, N=256,
+// K=16) into one of two 256-column TMEM accumulators, and warps 2..9 drain
+// the other accumulator (tcgen05.ld), so MMA and drain overlap.  All waits
+// are bounded: a role that times out raises an abort flag and the kernel
+// winds down, reporting an error status instead of hanging.
+#include <cuda.h>
+#include <cuda_bf16.h>
+#include <cuda_runtime.h>
+#include <math.h>
+#include <stdint.h>
+
 #include "gb_internal.h"
+#include "lapack_internal.h"
+#include "sm100_primitives.cuh"
+
 namespace gb {
-int dgemm_emulated(int, int, int64_t, int64_t, int64_t, double, const double *, int64_t,
-                   const double *, int64_t, double, double *, int64_t, int, cudaStream_t) {
-  return set_error(GB_ERR_UNSUPPORTED, "emulated DGEMM not built");
+
+namespace oz {
+
+constexpr int BM = 128, BN = 256, BK = 64;
+constexpr int STAGES = 4;
+constexpr int KC_BLOCKS = 16;  // K chunk of one exact FP32 accumulation: 1024
+constexpr int A_BYTES = BM * BK * 2;
+constexpr int B_BYTES = BN * BK * 2;
+constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
+constexpr int NUM_THREADS = 320;
+constexpr int TMEM_COLS = 512;
+constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
+constexpr int MAX_SLICES = 8;
+constexpr int64_t MAX_K_SEGMENT = 16384;  // keeps a level sum below 2^31
+constexpr uint64_t WAIT_LIMIT_NS = 4000000000ull;
+constexpr int NONFINITE = -100000;  // exponent marker of a row/column with Inf/NaN
+
+struct GemmParams {
+  int S;
+  int m_tiles, n_tiles;
+  int kblocks;
+  int m_pad, n_pad;
+  int64_t plane_stride;
+  int *planes;
+  int *status;
+};
+
+__global__ void __launch_bounds__(NUM_THREADS, 1)
+slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                  const GemmParams p) {
+  using namespace sm100;
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t *smem = reinterpret_cast<uint8_t *>(
+      (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
+  uint8_t *sA = smem;
+  uint8_t *sB = smem + STAGES * A_BYTES;
+  uint64_t *full = reinterpret_cast<uint64_t *>(smem + STAGES * STAGE_BYTES);
+  uint64_t *empty = full + STAGES;
+  uint64_t *tfull = empty + STAGES;
+  uint64_t *tempty = tfull + 2;
+  uint64_t *mma_done = tempty + 2;
+  uint32_t *tmem_slot = reinterpret_cast<uint32_t *>(mma_done + 1);
+  volatile int *abort_flag = reinterpret_cast<volatile int *>(tmem_slot + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < STAGES; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&empty[i], 1);
+    }
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&tfull[i], 1);
+      mbar_init(&tempty[i], 8);
+    }
+    mbar_init(mma_done, 1);
+    *abort_flag = 0;
+    fence_mbar_init();
+  }
+  if (warp == 0) {
+    tmem_alloc(tmem_slot, TMEM_COLS);
+    tmem_relinquish();
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem_base = *tmem_slot;
+
+  const int S = p.S;
+  const int ntiles = p.m_tiles * p.n_tiles;
+  const int nkc = (p.kblocks + KC_BLOCKS - 1) / KC_BLOCKS;
+  auto fail = [&](int site) {
+    *abort_flag = 1;
+    atomicCAS(p.status, 0, GB_KERR_MBARRIER_TIMEOUT);
+    atomicExch(p.status + 1, site);
+  };
+
+  if (warp == 0) {
+    // ------------------------------------------------ TMA producer
+    if (lane == 0) {
+      tma_prefetch_desc(&tmA);
+      tma_prefetch_desc(&tmB);
+      int stage = 0;
+      uint32_t phase = 0;
+      uint32_t issued_phase[STAGES];
+      bool issued[STAGES];
+      for (int i = 0; i < STAGES; ++i) issued[i] = false;
+      bool ok = true;
+      for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+        const int mt = tile % p.m_tiles, nt = tile / p.m_tiles;
+        for (int L = 2; ok && L <= S + 1; ++L) {
+          const int s_lo = L - S > 1 ? L - S : 1, s_hi = L - 1 < S ? L - 1 : S;
+          for (int s = s_lo; ok && s <= s_hi; ++s) {
+            const int t = L - s;
+            const int rowA = (s - 1) * p.m_pad + mt * BM;
+            const int rowB = (t - 1) * p.n_pad + nt * BN;
+            for (int kc = 0; ok && kc < nkc; ++kc) {
+              const int kb1 = min(p.kblocks, (kc + 1) * KC_BLOCKS);
+              for (int kb = kc * KC_BLOCKS; kb < kb1; ++kb) {
+                if (!mbar_wait(&empty[stage], phase ^ 1u, abort_flag, WAIT_LIMIT_NS)) {
+                  fail(1);
+                  ok = false;
+                  break;
+                }
+                mbar_arrive_expect_tx(&full[stage], STAGE_BYTES);
+                tma_load_2d(sA + stage * A_BYTES, &tmA, &full[stage], kb * BK, rowA);
+                tma_load_2d(sB + stage * B_BYTES, &tmB, &full[stage], kb * BK, rowB);
+                issued[stage] = true;
+                issued_phase[stage] = phase;
+                if (++stage == STAGES) {
+                  stage = 0;
+                  phase ^= 1u;
+                }
+              }
+            }
+          }
+        }
+      }
+      // never leave with TMA writes still landing in shared memory
+      volatile int no_abort = 0;
+      for (int i = 0; i < STAGES; ++i)
+        if (issued[i]) mbar_wait(&full[i], issued_phase[i], &no_abort, WAIT_LIMIT_NS);
+    }
+  } else if (warp == 1) {
+    // ------------------------------------------------ MMA issuer
+    if (lane == 0) {
+      constexpr uint32_t IDESC = idesc_bf16_f32(BM, BN);
+      int stage = 0;
+      uint32_t phase = 0;
+      int acc = 0;
+      uint32_t acc_phase = 0;
+      bool ok = true;
+      for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+        for (int L = 2; ok && L <= S + 1; ++L) {
+          const int s_lo = L - S > 1 ? L - S : 1, s_hi = L - 1 < S ? L - 1 : S;
+          for (int s = s_lo; ok && s <= s_hi; ++s) {
+            for (int kc = 0; ok && kc < nkc; ++kc) {
+              if (!mbar_wait(&tempty[acc], acc_phase ^ 1u, abort_flag, WAIT_LIMIT_NS)) {
+                fail(2);
+                ok = false;
+                break;
+              }
+              tc_fence_after();
+              const uint32_t d_tmem = tmem_base + (uint32_t)(acc * BN);
+              const int kb0 = kc * KC_BLOCKS, kb1 = min(p.kblocks, kb0 + KC_BLOCKS);
+              for (int kb = kb0; kb < kb1; ++kb) {
+                if (!mbar_wait(&full[stage], phase, abort_flag, WAIT_LIMIT_NS)) {
+                  fail(3);
+                  ok = false;
+                  break;
+                }
+                tc_fence_after();
+                const uint64_t adesc = sdesc_kmajor_sw128(smem_u32(sA + stage * A_BYTES));
+                const uint64_t bdesc = sdesc_kmajor_sw128(smem_u32(sB + stage * B_BYTES));
+#pragma unroll
+                for (int k = 0; k < BK / 16; ++k) {
+                  // advance 16 bf16 (32 bytes) along K inside the swizzle atom
+                  mma_bf16(d_tmem, adesc + (uint64_t)(2 * k), bdesc + (uint64_t)(2 * k), IDESC,
+                           (kb > kb0 || k > 0) ? 1u : 0u);
+                }
+                mma_commit(&empty[stage]);
+                if (++stage == STAGES) {
+                  stage = 0;
+                  phase ^= 1u;
+                }
+              }
+              if (!ok) break;
+              mma_commit(&tfull[acc]);
+              acc ^= 1;
+              if (acc == 0) acc_phase ^= 1u;
+            }
+          }
+        }
+      }
+      // TMEM is freed at exit: wait until every issued MMA has completed
+      mma_commit(mma_done);
+      volatile int no_abort = 0;
+      mbar_wait(mma_done, 0, &no_abort, WAIT_LIMIT_NS);
+    }
+  } else {
+    // ------------------------------------------------ epilogue (8 warps)
+    const int q = warp & 3;             // TMEM lane quadrant this warp may access
+    const int half = (warp - 2) >> 2;   // column half of the 256-wide tile
+    const int row = q * 32 + lane;      // tile row owned by this thread
+    int acc = 0;
+    uint32_t acc_phase = 0;
+    bool ok = true;
+    int32_t sum[128];
+    for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+      for (int L = 2; ok && L <= S + 1; ++L) {
+#pragma unroll
+        for (int c = 0; c < 128; ++c) sum[c] = 0;
+        const int s_lo = L - S > 1 ? L - S : 1, s_hi = L - 1 < S ? L - 1 : S;
+        for (int s = s_lo; ok && s <= s_hi; ++s) {
+          for (int kc = 0; kc < nkc; ++kc) {
+            const bool got = mbar_wait(&tfull[acc], acc_phase, abort_flag, WAIT_LIMIT_NS);
+            // the warp-wide tcgen05.ld below needs a converged warp: agree first
+            if (!__all_sync(0xffffffffu, got)) {
+              if (lane == 0) fail(4);
+              ok = false;
+              break;
+            }
+            tc_fence_after();
+            const uint32_t taddr =
+                tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + half * 128);
+#pragma unroll
+            for (int c = 0; c < 4; ++c) {
+              uint32_t r[32];
+              tmem_ld_32x32b_x32(taddr + c * 32, r);
+              tmem_ld_wait();
+#pragma unroll
+              for (int j = 0; j < 32; ++j) sum[c * 32 + j] += __float2int_rn(__uint_as_float(r[j]));
+            }
+            tc_fence_before();
+            __syncwarp();
+            if (lane == 0) mbar_arrive(&tempty[acc]);
+            acc ^= 1;
+            if (acc == 0) acc_phase ^= 1u;
+          }
+        }
+        if (!ok) break;
+        // level plane, tile-blocked and column-major inside the tile so a
+        // warp's store of one column is 128 contiguous bytes
+        int *dst = p.planes + (int64_t)(L - 2) * p.plane_stride + (int64_t)tile * (BM * BN) +
+                   (int64_t)(half * 128) * BM + row;
+#pragma unroll
+        for (int c = 0; c < 128; ++c) dst[c * BM] = sum[c];
+      }
+    }
+  }
+
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 0) {
+    __syncwarp();
+    tc_fence_after();
+    tmem_dealloc(tmem_base, TMEM_COLS);
+  }
 }
+
+// ------------------------------------------------------------------ split
+// Max |x| over each row of the op-view R x K (src(r,p)).  Bits of
+// non-negative doubles order like the values, so atomicMax on the bit
+// pattern is a max; any NaN wins as the largest pattern.
+__global__ void rowmax_kcontig_kernel(int64_t R, int64_t K, const double *__restrict__ X,
+                                      int64_t ld, unsigned long long *__restrict__ out) {
+  const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= R) return;
+  const double *x = X + r * ld;
+  unsigned long long best = 0;
+  for (int64_t pp = lane; pp < K; pp += 32) {
+    unsigned long long b = __double_as_longlong(fabs(x[pp]));
+    best = b > best ? b : best;
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    unsigned long long o = __shfl_down_sync(0xffffffffu, best, off);
+    best = o > best ? o : best;
+  }
+  if (lane == 0) atomicMax(out + r, best);
+}
+
+__global__ void rowmax_mcontig_kernel(int64_t R, int64_t K, const double *__restrict__ X,
+                                      int64_t ld, int64_t kspan,
+                                      unsigned long long *__restrict__ out) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= R) return;
+  const int64_t p0 = (int64_t)blockIdx.y * kspan;
+  const int64_t p1 = p0 + kspan < K ? p0 + kspan : K;
+  unsigned long long best = 0;
+  for (int64_t pp = p0; pp < p1; ++pp) {
+    unsigned long long b = __double_as_longlong(fabs(X[r + pp * ld]));
+    best = b > best ? b : best;
+  }
+  atomicMax(out + r, best);
+}
+
+__global__ void exponent_kernel(int64_t Rpad, int64_t R, const unsigned long long *__restrict__ mx,
+                                int *__restrict__ expo) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= Rpad) return;
+  int e = 0;
+  if (r < R) {
+    double v = __longlong_as_double((long long)mx[r]);
+    if (!isfinite(v)) {
+      e = NONFINITE;
+    } else if (v > 0.0) {
+      frexp(v, &e);  // v = f * 2^e with f in [0.5, 1): |x| < 2^e on the row
+    }
+  }
+  expo[r] = e;
+}
+
+// Digits of a 32-row x 64-K tile.  The tile is staged through shared memory
+// so both the read (in the caller's layout) and the write (K-contiguous
+// slices) are coalesced.
+template <bool KCONTIG>
+__global__ void __launch_bounds__(256)
+split_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
+             const int *__restrict__ expo, int S, int64_t Rpad, int64_t Kpad,
+             __nv_bfloat16 *__restrict__ slices) {
+  __shared__ double tile[32][65];
+  const int64_t r0 = (int64_t)blockIdx.y * 32, p0 = (int64_t)blockIdx.x * 64;
+  const int tid = threadIdx.x;
+  for (int e = tid; e < 32 * 64; e += 256) {
+    int rr, pp;
+    if (KCONTIG) {
+      rr = e / 64;
+      pp = e % 64;
+    } else {
+      rr = e % 32;
+      pp = e / 32;
+    }
+    const int64_t r = r0 + rr, pk = p0 + pp;
+    double v = 0.0;
+    if (r < R && pk < K) v = KCONTIG ? X[pk + r * ld] : X[r + pk * ld];
+    tile[rr][pp] = v;
+  }
+  __syncthreads();
+  // each thread: row rr = tid / 8, 8 consecutive k values
+  const int rr = tid >> 3, pc = (tid & 7) * 8;
+  const int64_t r = r0 + rr;
+  const int e = (r < R) ? expo[r] : 0;
+  const int shift = 7 * S - e;
+  unsigned long long mag[8];
+  bool neg[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    double v = tile[rr][pc + j];
+    neg[j] = v < 0.0;
+    double sv = (e == NONFINITE) ? 0.0 : ldexp(fabs(v), shift);  // < 2^(7S), exact scaling
+    mag[j] = (unsigned long long)sv;                             // truncation toward zero
+  }
+  for (int s = 1; s <= S; ++s) {
+    const int sh = 7 * (S - s);
+    __align__(16) __nv_bfloat16 out[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      int d = (int)((mag[j] >> sh) & 127ull);
+      out[j] = __float2bfloat16_rn((float)(neg[j] ? -d : d));
+    }
+    __nv_bfloat16 *dst = slices + ((int64_t)(s - 1) * Rpad + r) * Kpad + p0 + pc;
+    *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<const uint4 *>(out);
+  }
+}
+
+// ------------------------------------------------------------------ recombine
+__global__ void recombine_kernel(int64_t m, int64_t n, int S, int m_tiles, int64_t plane_stride,
+                                 const int *__restrict__ planes, const int *__restrict__ ea,
+                                 const int *__restrict__ eb, double alpha, double beta,
+                                 double *__restrict__ C, int64_t ldc, int ta, int tb, int64_t k,
+                                 const double *__restrict__ A, int64_t lda,
+                                 const double *__restrict__ B, int64_t ldb) {
+  const int64_t total = m * n;
+  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
+       idx += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t j = idx / m, i = idx - j * m;
+    const int ei = ea[i], fj = eb[j];
+    double v;
+    if (ei == NONFINITE || fj == NONFINITE) {
+      // Inf/NaN in row i of op(A) or column j of op(B): direct FP64 dot
+      double s = 0.0;
+      for (int64_t pp = 0; pp < k; ++pp) {
+        double a = ta ? A[pp + i * lda] : A[i + pp * lda];
+        double b = tb ? B[j + pp * ldb] : B[pp + j * ldb];
+        s = fma(a, b, s);
+      }
+      v = alpha * s;
+    } else {
+      const int64_t tile = (j / 256) * m_tiles + (i / 128);
+      const int64_t off = tile * (128 * 256) + (j % 256) * 128 + (i % 128);
+      double acc = (double)planes[(int64_t)(S - 1) * plane_stride + off];
+      for (int L = S; L >= 2; --L)
+        acc = fma(acc, 0.0078125 /* 2^-7 */, (double)planes[(int64_t)(L - 2) * plane_stride + off]);
+      // acc * 2^(ei + fj - 14), scaled in two steps against over/underflow
+      v = alpha * ldexp(ldexp(acc, ei - 14), fj);
+    }
+    double *c = C + i + j * ldc;
+    *c = (beta == 0.0) ? v : fma(beta, *c, v);
+  }
+}
+
+// ------------------------------------------------------------------ host
+typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
+                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
+                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void *p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<EncodeTiledFn>(p);
+  }
+  return fn;
+}
+
+// 2-D tensor map over `rows` x `kpad` bf16 (K innermost), box 64 x box_rows.
+int make_map(CUtensorMap *map, void *base, int64_t rows, int64_t kpad, int box_rows) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return set_error(GB_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
+  cuuint64_t dims[2] = {(cuuint64_t)kpad, (cuuint64_t)rows};
+  cuuint64_t strides[1] = {(cuuint64_t)kpad * 2};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) return set_error(GB_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
+  return GB_SUCCESS;
+}
+
+inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
+inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+// Split an R x K op-view operand into S K-contiguous bf16 slices + exponents.
+void split_operand(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld, int S,
+                   int64_t Rpad, int64_t Kpad, unsigned long long *mx, int *expo,
+                   __nv_bfloat16 *slices, cudaStream_t s) {
+  cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * Rpad, s);
+  if (kcontig) {
+    rowmax_kcontig_kernel<<<(unsigned)((R + 7) / 8), 256, 0, s>>>(R, K, X, ld, mx);
+  } else {
+    const int64_t kspan = 256;
+    dim3 g((unsigned)((R + 255) / 256), (unsigned)((K + kspan - 1) / kspan));
+    rowmax_mcontig_kernel<<<g, 256, 0, s>>>(R, K, X, ld, kspan, mx);
+  }
+  exponent_kernel<<<(unsigned)((Rpad + 255) / 256), 256, 0, s>>>(Rpad, R, mx, expo);
+  dim3 g2((unsigned)(Kpad / 64), (unsigned)(Rpad / 32));
+  if (kcontig)
+    split_kernel<true><<<g2, 256, 0, s>>>(R, K, X, ld, expo, S, Rpad, Kpad, slices);
+  else
+    split_kernel<false><<<g2, 256, 0, s>>>(R, K, X, ld, expo, S, Rpad, Kpad, slices);
+}
+
+// One pass over a K segment (k <= MAX_K_SEGMENT).
+int emulated_segment(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
+                     const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
+                     double *C, int64_t ldc, int S, cudaStream_t s) {
+  const int64_t m_pad = round_up(m, BM), n_pad = round_up(n, BN), k_pad = round_up(k, BK);
+  const size_t bytes_sa = align256((size_t)S * m_pad * k_pad * 2);
+  const size_t bytes_sb = align256((size_t)S * n_pad * k_pad * 2);
+  const size_t bytes_mx = align256((size_t)(m_pad + n_pad) * 8);
+  const size_t bytes_e = align256((size_t)(m_pad + n_pad) * 4);
+  const int64_t plane_stride = m_pad * n_pad;
+  const size_t bytes_pl = align256((size_t)S * plane_stride * 4);
+  Scratch ws(bytes_sa + bytes_sb + bytes_mx + bytes_e + bytes_pl, s);
+  if (!ws.p) return GB_ERR_ALLOC;
+  char *base = ws.as<char>();
+  __nv_bfloat16 *sla = reinterpret_cast<__nv_bfloat16 *>(base);
+  __nv_bfloat16 *slb = reinterpret_cast<__nv_bfloat16 *>(base + bytes_sa);
+  unsigned long long *mx = reinterpret_cast<unsigned long long *>(base + bytes_sa + bytes_sb);
+  int *ea = reinterpret_cast<int *>(base + bytes_sa + bytes_sb + bytes_mx);
+  int *eb = ea + m_pad;
+  int *planes = reinterpret_cast<int *>(base + bytes_sa + bytes_sb + bytes_mx + bytes_e);
+
+  // op(A) rows: K-contiguous when A is transposed; op(B) columns: K-contiguous when B is not
+  split_operand(ta != 0, m, k, A, lda, S, m_pad, k_pad, mx, ea, sla, s);
+  split_operand(tb == 0, n, k, B, ldb, S, n_pad, k_pad, mx + m_pad, eb, slb, s);
+
+  CUtensorMap mapA, mapB;
+  int st = make_map(&mapA, sla, (int64_t)S * m_pad, k_pad, BM);
+  if (st) return st;
+  if ((st = make_map(&mapB, slb, (int64_t)S * n_pad, k_pad, BN))) return st;
+
+  static bool attr_set = false;
+  if (!attr_set) {
+    GB_CUDA(cudaFuncSetAttribute(slice_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 SMEM_BYTES));
+    attr_set = true;
+  }
+  GemmParams gp;
+  gp.S = S;
+  gp.m_tiles = (int)(m_pad / BM);
+  gp.n_tiles = (int)(n_pad / BN);
+  gp.kblocks = (int)(k_pad / BK);
+  gp.m_pad = (int)m_pad;
+  gp.n_pad = (int)n_pad;
+  gp.plane_stride = plane_stride;
+  gp.planes = planes;
+  gp.status = ctx().d_status;
+  const int ntiles = gp.m_tiles * gp.n_tiles;
+  const int grid = ntiles < sm_count() ? ntiles : sm_count();
+  slice_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, gp);
+  GB_CUDA(cudaGetLastError());
+
+  const int64_t total = m * n;
+  int64_t blocks = (total + 255) / 256;
+  const int64_t cap = (int64_t)sm_count() * 32;
+  recombine_kernel<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(
+      m, n, S, gp.m_tiles, plane_stride, planes, ea, eb, alpha, beta, C, ldc, ta, tb, k, A, lda,
+      B, ldb);
+  return check_cuda(cudaGetLastError(), "emulated dgemm");
+}
+
+}  // namespace oz
+
+// Slice count used when the caller passes 0: 8 slices (56 bits) reach FP64
+// accuracy for operands whose rows/columns span a moderate exponent range.
+int ozaki_default_slices() { return oz::MAX_SLICES; }
+
+int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
+                   const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
+                   double *C, int64_t ldc, int slices, cudaStream_t s) {
+  int S = slices > 0 ? slices : ozaki_default_slices();
+  if (S > oz::MAX_SLICES) S = oz::MAX_SLICES;
+  if (m <= 0 || n <= 0) return GB_SUCCESS;
+  if (m > (int64_t)1 << 22 || n > (int64_t)1 << 22)
+    return set_error(GB_ERR_UNSUPPORTED, "emulated dgemm: dimension too large");
+  // K segments keep every int32 level sum exact; later segments accumulate.
+  double b = beta;
+  for (int64_t k0 = 0; k0 < k; k0 += oz::MAX_K_SEGMENT) {
+    const int64_t kk = (k - k0) < oz::MAX_K_SEGMENT ? (k - k0) : oz::MAX_K_SEGMENT;
+    const double *Ak = ta ? A + k0 : A + k0 * lda;
+    const double *Bk = tb ? B + k0 * ldb : B + k0;
+    int st = oz::emulated_segment(ta, tb, m, n, kk, alpha, Ak, lda, Bk, ldb, b, C, ldc, S, s);
+    if (st) return st;
+    b = 1.0;
+  }
+  return GB_SUCCESS;
+}
+
 }  // namespace gb

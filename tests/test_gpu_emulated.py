@@ -1,0 +1,156 @@
+"""Emulated FP64 GEMM (Ozaki slices on bf16 tensor cores) parity.
+
+1. Exactness: integer operands are represented exactly by their slices, so
+   the result must equal the exact integer product bit for bit -- including
+   the worst case where every digit is +-127 and each 1024-deep FP32
+   accumulation reaches its largest value (1024*127^2 < 2^24).
+2. Accuracy against a double-double reference on uniform(-1,1) and
+   exponent-spread operands U*2^E: normwise error
+   ||C - Cref||_max / ||G||_max, G = |alpha||A||B| + |beta||C| (the DMMCH
+   denominator), bounded by 8*eps for 8 slices on e = 0 operands.
+3. The DGEMM contract: transposes, padded leading dimensions, alpha/beta,
+   beta = 0 overwriting NaN, and Inf/NaN inputs propagating.
+"""
+from __future__ import annotations
+
+import numpy as np
+import pytest
+
+from conftest import EPS, dmmch_ratio
+
+from openblas_gb300 import workloads as W
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture
+def emulated(gblib):
+    gblib.gb_set_dgemm_mode(1)
+    yield gblib
+    gblib.gb_set_dgemm_mode(0)
+
+
+def _int_matrix(seed, shape, lo=-127, hi=127):
+    return np.asfortranarray(W.randint(seed, shape, lo, hi).astype(np.float64))
+
+
+@pytest.mark.parametrize("m,n,k", [(64, 48, 1000), (300, 520, 2100), (128, 256, 5000)])
+def test_integer_operands_exact(F, emulated, m, n, k):
+    A = _int_matrix(1, (m, k))
+    B = _int_matrix(2, (k, n))
+    C = np.zeros((m, n), order="F")
+    F.dgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, C, m)
+    exact = (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64)
+    assert np.array_equal(C, exact)
+
+
+def test_worst_case_digits_exact(F, emulated):
+    """All digits +-127 with aligned signs: every chunk sum is 1024*16129."""
+    m, n, k = 130, 260, 4096
+    A = np.full((m, k), 127.0, order="F")
+    B = np.full((k, n), 127.0, order="F")
+    A[::2] = -127.0
+    C = np.zeros((m, n), order="F")
+    F.dgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, C, m)
+    exact = np.where(np.arange(m)[:, None] % 2 == 0, -1.0, 1.0) * (k * 127.0 * 127.0)
+    assert np.array_equal(C, np.broadcast_to(exact, (m, n)))
+
+
+def test_multi_digit_exact(F, emulated):
+    """Operands with several nonzero 7-bit digits (integers below 2^40 with a
+    common row scale) are still represented exactly by 8 slices."""
+    m, n, k = 96, 96, 300
+    A = _int_matrix(3, (m, k), -(2 ** 20), 2 ** 20)
+    B = _int_matrix(4, (k, n), -(2 ** 20), 2 ** 20)
+    A[:, 0] = 2.0 ** 40  # every row max -> exponent 41; digits span 41 bits
+    C = np.zeros((m, n), order="F")
+    F.dgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, C, m)
+    exact = A.astype(object) @ B.astype(object)
+    err = max(abs(float(C[i, j] - exact[i, j])) for i in range(0, m, 7) for j in range(0, n, 5))
+    ref_scale = float(np.abs(A).max() * np.abs(B).max() * k)
+    assert err <= 2 * EPS * ref_scale
+
+
+def _normwise(Cg, Cref, G):
+    return np.abs(Cg - Cref).max() / G.max()
+
+
+@pytest.mark.parametrize("e,slices,bound", [(0, 8, 8), (0, 7, 200), (8, 8, 32), (16, 8, 256)])
+def test_accuracy_vs_double_double(orc, F, emulated, gblib, e, slices, bound):
+    m = n = k = 384
+    A = W.exponent_spread(10 + e, (m, k), e)
+    B = W.exponent_spread(20 + e, (k, n), e)
+    C = W.uniform(30, (m, n))
+    gblib.gb_set_ozaki_slices(slices)
+    try:
+        Cg = C.copy(order="F")
+        F.dgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, Cg, m)
+    finally:
+        gblib.gb_set_ozaki_slices(0)
+    Cref = C.copy(order="F")
+    orc.dgemm_dd("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, Cref, m)
+    G = orc.dgemm_absbound("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, C, m)
+    # normwise error against ||G||: FP64 level (the native FP64 GEMM has up to k*eps)
+    assert _normwise(Cg, Cref, G) <= bound * EPS, _normwise(Cg, Cref, G) / EPS
+
+
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("N", "T"), ("T", "N"), ("T", "T")])
+def test_transposes_padding_alpha_beta(orc, F, emulated, ta, tb):
+    m, n, k = 333, 290, 1111
+    A, B, C = W.gemm_operands(70, m, n, k, ta, tb, pad=8)
+    C0 = C.copy(order="F")
+    F.dgemm(ta, tb, m, n, k, -1.5, A, A.shape[0], B, B.shape[0], 0.5, C, C.shape[0])
+    Cref = C0.copy(order="F")
+    orc.dgemm_dd(ta, tb, m, n, k, -1.5, A, A.shape[0], B, B.shape[0], 0.5, Cref, C0.shape[0])
+    G = orc.dgemm_absbound(ta, tb, m, n, k, -1.5, A, A.shape[0], B, B.shape[0], 0.5, C0,
+                           C0.shape[0])
+    assert dmmch_ratio(C[:m], Cref[:m], G, k) <= 16
+    assert np.array_equal(C[m:], C0[m:])
+
+
+def test_beta_zero_and_special_values(F, emulated):
+    m, n, k = 70, 90, 200
+    A = W.uniform(1, (m, k))
+    B = W.uniform(2, (k, n))
+    C = np.full((m, n), np.nan, order="F")
+    F.dgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, C, m)
+    assert np.isfinite(C).all()
+    A2 = A.copy(order="F")
+    A2[5, 17] = np.inf
+    A2[9, 3] = np.nan
+    C2 = np.zeros((m, n), order="F")
+    F.dgemm("N", "N", m, n, k, 1.0, A2, m, B, k, 0.0, C2, m)
+    ref = A2 @ B
+    assert np.array_equal(np.isnan(C2), np.isnan(ref))
+    assert np.array_equal(np.isinf(C2), np.isinf(ref))
+    fin = np.isfinite(ref)
+    assert np.abs(C2[fin] - ref[fin]).max() <= 1e-12
+
+
+def test_large_k_segments(orc, F, emulated):
+    """K beyond one 16384 segment: segments accumulate into C."""
+    m, n, k = 64, 40, 20000
+    A = W.uniform(5, (m, k))
+    B = W.uniform(6, (k, n))
+    C = W.uniform(7, (m, n))
+    Cg, Cref = C.copy(order="F"), C.copy(order="F")
+    F.dgemm("N", "N", m, n, k, 1.0, A, m, B, k, 1.0, Cg, m)
+    orc.dgemm_dd("N", "N", m, n, k, 1.0, A, m, B, k, 1.0, Cref, m)
+    G = orc.dgemm_absbound("N", "N", m, n, k, 1.0, A, m, B, k, 1.0, C, m)
+    assert dmmch_ratio(Cg, Cref, G, k) <= 16
+
+
+def test_device_entry_point(orc, gblib):
+    torch = pytest.importorskip("torch")
+    m, n, k = 256, 256, 1024
+    A, B, C = W.gemm_operands(80, m, n, k, "N", "N")
+    dA, dB = torch.from_numpy(A.T.copy()).cuda(), torch.from_numpy(B.T.copy()).cuda()
+    dC = torch.from_numpy(C.T.copy()).cuda()
+    assert gblib.gb_dgemm_emulated_dev(b"N", b"N", m, n, k, 2.0, dA.data_ptr(), m, dB.data_ptr(),
+                                       k, -1.0, dC.data_ptr(), m, 8) == 0
+    assert gblib.gb_synchronize() == 0
+    got = dC.cpu().numpy().T
+    Cref = C.copy(order="F")
+    orc.dgemm_dd("N", "N", m, n, k, 2.0, A, m, B, k, -1.0, Cref, m)
+    G = orc.dgemm_absbound("N", "N", m, n, k, 2.0, A, m, B, k, -1.0, C, m)
+    assert dmmch_ratio(got, Cref, G, k) <= 16
