@@ -171,6 +171,16 @@ int gb_set_ozaki_slices(int slices);
 /* Library version string. */
 const char *gb_version(void);
 
+/* Instrumentation.  gb_kernel_launches: number of CUDA kernels this library
+ * has launched (all threads) since it was loaded.  gb_profile_enable(1)
+ * brackets the dominant kernel of each call (e.g. "slice_gemm") with CUDA
+ * events on the launching stream; gb_profile_kernel_ms synchronises, returns
+ * the summed duration of the named kernel and its launch count, and resets
+ * the record when `reset` is non-zero. */
+int64_t gb_kernel_launches(void);
+int gb_profile_enable(int on);
+double gb_profile_kernel_ms(const char *name, int *launches, int reset);
+
 /* C <- alpha*op(A)*op(B) + beta*C, all device pointers, column-major,
  * trans 'N'/'T'/'C'.  Uses the current DGEMM mode. */
 int gb_dgemm_dev(char transa, char transb, int64_t m, int64_t n, int64_t k,
@@ -201,6 +211,12 @@ int gb_dgetrf_dev(int64_t m, int64_t n, double *A, int64_t lda, int *ipiv,
                   int *info);
 int gb_dgetrs_dev(char trans, int64_t n, int64_t nrhs, const double *A,
                   int64_t lda, const int *ipiv, double *B, int64_t ldb);
+/* FP32 LU and solve (the factorisation behind the mixed solver; sgetrf_ /
+ * sgetrs_ semantics, interface/lapack/getrf.c, getrs.c, single precision). */
+int gb_sgetrf_dev(int64_t m, int64_t n, float *A, int64_t lda, int *ipiv,
+                  int *info);
+int gb_sgetrs_dev(char trans, int64_t n, int64_t nrhs, const float *A,
+                  int64_t lda, const int *ipiv, float *B, int64_t ldb);
 /* Row interchanges k1..k2 (1-based) of an n-column device matrix using a
  * device ipiv vector with increment incx (+1 or -1 for the fast path). */
 int gb_dlaswp_dev(int64_t n, double *A, int64_t lda, int64_t k1, int64_t k2,
@@ -208,12 +224,13 @@ int gb_dlaswp_dev(int64_t n, double *A, int64_t lda, int64_t k1, int64_t k2,
 int gb_dpotrf_dev(char uplo, int64_t n, double *A, int64_t lda, int *info);
 /* Mixed-precision solve (FP32 LU on the GPU + FP64 refinement, GMRES-IR
  * when plain refinement stalls, FP64 LU fallback).  Device pointers except
- * iter/info, which are host outputs (this call synchronises).  iter follows
- * dsgesv (>= 0 refinement steps, < 0 fallback reason); GMRES-IR steps are
- * reported as 100 + steps. */
-int gb_dsgesv_dev(int64_t n, int64_t nrhs, const double *A, int64_t lda,
-                  int *ipiv, const double *B, int64_t ldb, double *X,
-                  int64_t ldx, int *iter, int *info);
+ * iter/info, which are host outputs (this call synchronises).  A is only
+ * overwritten (with its FP64 LU) when the solve falls back to FP64, as in
+ * dsgesv.  iter follows dsgesv (>= 0 refinement steps, < 0 fallback reason);
+ * a solve finished by GMRES-IR reports 100 + GMRES iterations. */
+int gb_dsgesv_dev(int64_t n, int64_t nrhs, double *A, int64_t lda, int *ipiv,
+                  const double *B, int64_t ldb, double *X, int64_t ldx,
+                  int *iter, int *info);
 
 #ifdef __cplusplus
 }

@@ -27,6 +27,9 @@ DEV_SIGS = {
     "gb_get_dgemm_mode": (_i, []),
     "gb_set_ozaki_slices": (_i, [_i]),
     "gb_version": (C.c_char_p, []),
+    "gb_kernel_launches": (C.c_int64, []),
+    "gb_profile_enable": (_i, [_i]),
+    "gb_profile_kernel_ms": (_d, [C.c_char_p, C.POINTER(_i), _i]),
     "gb_dgemm_dev": (_i, [_c, _c, _i64, _i64, _i64, _d, _vp, _i64, _vp, _i64, _d, _vp, _i64]),
     "gb_dgemm_native_dev": (_i, [_c, _c, _i64, _i64, _i64, _d, _vp, _i64, _vp, _i64, _d, _vp,
                                  _i64]),
@@ -37,6 +40,8 @@ DEV_SIGS = {
     "gb_dsyrk_dev": (_i, [_c, _c, _i64, _i64, _d, _vp, _i64, _d, _vp, _i64]),
     "gb_dgetrf_dev": (_i, [_i64, _i64, _vp, _i64, _vp, _vp]),
     "gb_dgetrs_dev": (_i, [_c, _i64, _i64, _vp, _i64, _vp, _vp, _i64]),
+    "gb_sgetrf_dev": (_i, [_i64, _i64, _vp, _i64, _vp, _vp]),
+    "gb_sgetrs_dev": (_i, [_c, _i64, _i64, _vp, _i64, _vp, _vp, _i64]),
     "gb_dlaswp_dev": (_i, [_i64, _vp, _i64, _i64, _i64, _vp, _i64]),
     "gb_dpotrf_dev": (_i, [_c, _i64, _vp, _i64, _vp]),
     "gb_dsgesv_dev": (_i, [_i64, _i64, _vp, _i64, _vp, _vp, _i64, _vp, _i64, C.POINTER(_i),

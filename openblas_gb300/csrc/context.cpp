@@ -12,7 +12,10 @@
 #include <stdlib.h>
 #include <string.h>
 
+#include <atomic>
 #include <mutex>
+#include <string>
+#include <vector>
 
 #include "gb_internal.h"
 
@@ -158,6 +161,38 @@ void record_xerbla(const char *name, int info) {
            t_err.xerbla_name, info);
 }
 
+// ---------------------------------------------------------------------------
+// instrumentation
+// ---------------------------------------------------------------------------
+namespace {
+std::atomic<int64_t> g_launches{0};
+struct ProfileRec {
+  std::string name;
+  cudaEvent_t e0, e1;
+};
+thread_local bool t_prof_on = false;
+thread_local std::vector<ProfileRec> t_prof;
+}  // namespace
+
+void count_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+ProfileScope::ProfileScope(const char *nm, cudaStream_t st) : name(nm), s(st) {
+  if (!t_prof_on) return;
+  if (cudaEventCreate(&e0) != cudaSuccess) {
+    e0 = nullptr;
+    return;
+  }
+  cudaEventRecord(e0, s);
+}
+
+ProfileScope::~ProfileScope() {
+  if (!e0) return;
+  cudaEvent_t e1;
+  if (cudaEventCreate(&e1) != cudaSuccess) return;
+  cudaEventRecord(e1, s);
+  t_prof.push_back({name, e0, e1});
+}
+
 }  // namespace gb
 
 // ---------------------------------------------------------------------------
@@ -258,5 +293,33 @@ int gb_get_ozaki_slices_internal(void) {
 }
 
 const char *gb_version(void) { return "libgbblas 0.1 (sm_103a)"; }
+
+int64_t gb_kernel_launches(void) { return gb::g_launches.load(); }
+
+int gb_profile_enable(int on) {
+  gb::t_prof_on = on != 0;
+  return GB_SUCCESS;
+}
+
+double gb_profile_kernel_ms(const char *name, int *launches, int reset) {
+  double total = 0.0;
+  int cnt = 0;
+  for (auto &r : gb::t_prof) {
+    if (name && r.name != name) continue;
+    cudaEventSynchronize(r.e1);
+    float ms = 0.f;
+    if (cudaEventElapsedTime(&ms, r.e0, r.e1) == cudaSuccess) total += ms;
+    ++cnt;
+  }
+  if (launches) *launches = cnt;
+  if (reset) {
+    for (auto &r : gb::t_prof) {
+      cudaEventDestroy(r.e0);
+      cudaEventDestroy(r.e1);
+    }
+    gb::t_prof.clear();
+  }
+  return total;
+}
 
 }  // extern "C"

@@ -68,6 +68,17 @@ int stage_in(void *dst_dev, const void *src_host, size_t ld, size_t m, size_t n,
 int stage_out(void *dst_host, const void *src_dev, size_t ld, size_t m, size_t n,
               size_t esize, cudaStream_t s);
 
+// Kernel-launch accounting (every launch site calls count_launch) and the
+// optional event bracketing of a named kernel on its stream.
+void count_launch(int n = 1);
+struct ProfileScope {
+  const char *name;
+  cudaStream_t s;
+  cudaEvent_t e0 = nullptr;
+  ProfileScope(const char *nm, cudaStream_t st);
+  ~ProfileScope();
+};
+
 // Library configuration read from the environment once.
 struct Config {
   int dgemm_mode = GB_DGEMM_NATIVE;   // GB_DGEMM_MODE=native|emulated|auto

@@ -168,8 +168,8 @@ void launch_dgemm_beta(int64_t m, int64_t n, double beta, double *C, int64_t ldc
   if (m <= 0 || n <= 0 || beta == 1.0) return;
   int64_t blocks = (m * n + 255) / 256;
   int64_t cap = (int64_t)sm_count() * 16;
-  gemm_beta_kernel<double><<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(m, n, beta,
-                                                                                  C, ldc, 0);
+  { gemm_beta_kernel<double><<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(m, n, beta,
+                                                                                  C, ldc, 0); count_launch(); }
 }
 
 void launch_sgemm_beta(int64_t m, int64_t n, float beta, float *C, int64_t ldc,
@@ -177,23 +177,24 @@ void launch_sgemm_beta(int64_t m, int64_t n, float beta, float *C, int64_t ldc,
   if (m <= 0 || n <= 0 || beta == 1.0f) return;
   int64_t blocks = (m * n + 255) / 256;
   int64_t cap = (int64_t)sm_count() * 16;
-  gemm_beta_kernel<float><<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(m, n, beta, C,
-                                                                                 ldc, 0);
+  { gemm_beta_kernel<float><<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(m, n, beta, C,
+                                                                                 ldc, 0); count_launch(); }
 }
 
 void launch_dgemm_fp64_tri(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
                            const double *A, int64_t lda, const double *B, int64_t ldb,
                            double beta, double *C, int64_t ldc, int tri, cudaStream_t s,
                            const int *skip) {
+  ProfileScope prof("dgemm_fp64", s);
   const int64_t tiles64 = ((m + 63) / 64) * ((n + 63) / 64);
   if (tiles64 >= (int64_t)sm_count() * 8) {
     dim3 grid((unsigned)((m + 63) / 64), (unsigned)((n + 63) / 64));
-    gemm_simt_kernel<double, 64, 64, 16, 4, 4><<<grid, 256, 0, s>>>(
-        ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, skip);
+    { gemm_simt_kernel<double, 64, 64, 16, 4, 4><<<grid, 256, 0, s>>>(
+        ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, skip); count_launch(); }
   } else {
     dim3 grid((unsigned)((m + 31) / 32), (unsigned)((n + 31) / 32));
-    gemm_simt_kernel<double, 32, 32, 16, 2, 2><<<grid, 256, 0, s>>>(
-        ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, skip);
+    { gemm_simt_kernel<double, 32, 32, 16, 2, 2><<<grid, 256, 0, s>>>(
+        ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, skip); count_launch(); }
   }
 }
 
@@ -207,8 +208,8 @@ void launch_dbeta_tri(int64_t n, double beta, double *C, int64_t ldc, int tri, c
   if (n <= 0 || beta == 1.0) return;
   int64_t blocks = (n * n + 255) / 256;
   int64_t cap = (int64_t)sm_count() * 16;
-  gemm_beta_kernel<double><<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(n, n, beta,
-                                                                                  C, ldc, tri);
+  { gemm_beta_kernel<double><<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(n, n, beta,
+                                                                                  C, ldc, tri); count_launch(); }
 }
 
 void launch_sgemm_fp32(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha,
@@ -217,12 +218,12 @@ void launch_sgemm_fp32(int ta, int tb, int64_t m, int64_t n, int64_t k, float al
   const int64_t tiles128 = ((m + 127) / 128) * ((n + 127) / 128);
   if (tiles128 >= (int64_t)sm_count() * 2) {
     dim3 grid((unsigned)((m + 127) / 128), (unsigned)((n + 127) / 128));
-    gemm_simt_kernel<float, 128, 128, 8, 8, 8><<<grid, 256, 0, s>>>(
-        ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, 0, nullptr);
+    { gemm_simt_kernel<float, 128, 128, 8, 8, 8><<<grid, 256, 0, s>>>(
+        ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, 0, nullptr); count_launch(); }
   } else {
     dim3 grid((unsigned)((m + 63) / 64), (unsigned)((n + 63) / 64));
-    gemm_simt_kernel<float, 64, 64, 16, 4, 4><<<grid, 256, 0, s>>>(
-        ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, 0, nullptr);
+    { gemm_simt_kernel<float, 64, 64, 16, 4, 4><<<grid, 256, 0, s>>>(
+        ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, 0, nullptr); count_launch(); }
   }
 }
 

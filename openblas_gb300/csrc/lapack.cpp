@@ -69,7 +69,9 @@ int getrf_blocking(int64_t m, int64_t n, double *A, int64_t lda, int *ipiv, int 
   if ((st = a.bind(true, s)) || (st = p.bind(false, s))) return st;
   DevInfo di(s);
   if (!di.buf.p) return GB_ERR_ALLOC;
-  if ((st = getrf_device<double>(m, n, a.d<double>(), a.dld, p.dev, di.d(), s))) return st;
+  const int mode = gb_get_dgemm_mode() == GB_DGEMM_NATIVE ? 0 : 1;
+  if ((st = getrf_device_mode<double>(m, n, a.d<double>(), a.dld, p.dev, di.d(), mode, s)))
+    return st;
   if ((st = a.unbind(s)) || (st = p.unbind(s))) return st;
   return di.read(s, info);
 }
@@ -150,7 +152,8 @@ int dgesv_(const blasint *N, const blasint *NRHS, double *a, const blasint *ldA,
   if (A.bind(true, s) || B.bind(true, s) || p.bind(false, s)) return 0;
   DevInfo di(s);
   if (!di.buf.p) return 0;
-  if (getrf_device<double>(n, n, A.d<double>(), A.dld, p.dev, di.d(), s)) return 0;
+  const int mode = gb_get_dgemm_mode() == GB_DGEMM_NATIVE ? 0 : 1;
+  if (getrf_device_mode<double>(n, n, A.d<double>(), A.dld, p.dev, di.d(), mode, s)) return 0;
   int h = 0;
   if (di.read(s, &h)) return 0;
   // interface/lapack/gesv.c:131-135: solve only when the factorisation is regular
@@ -238,7 +241,8 @@ int gb_dgetrf_dev(int64_t m, int64_t n, double *A, int64_t lda, int *ipiv, int *
     GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), stream()));
     return GB_SUCCESS;
   }
-  return getrf_device<double>(m, n, A, lda, ipiv, info, stream());
+  const int mode = gb_get_dgemm_mode() == GB_DGEMM_NATIVE ? 0 : 1;
+  return getrf_device_mode<double>(m, n, A, lda, ipiv, info, mode, stream());
 }
 
 int gb_dgetrs_dev(char trans, int64_t n, int64_t nrhs, const double *A, int64_t lda,
@@ -258,6 +262,43 @@ int gb_dgetrs_dev(char trans, int64_t n, int64_t nrhs, const double *A, int64_t 
   int st = ensure_init();
   if (st) return st;
   return getrs_device<double>(tr, n, nrhs, A, lda, ipiv, B, ldb, stream());
+}
+
+int gb_sgetrf_dev(int64_t m, int64_t n, float *A, int64_t lda, int *ipiv, int *info) {
+  int code = 0;
+  if (lda < (m > 1 ? m : 1)) code = 4;
+  if (n < 0) code = 2;
+  if (m < 0) code = 1;
+  if (code) {
+    call_xerbla("SGETRF", code);
+    return GB_ERR_INVALID_VALUE;
+  }
+  int st = ensure_init();
+  if (st) return st;
+  if (m == 0 || n == 0) {
+    GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), stream()));
+    return GB_SUCCESS;
+  }
+  return getrf_device<float>(m, n, A, lda, ipiv, info, stream());
+}
+
+int gb_sgetrs_dev(char trans, int64_t n, int64_t nrhs, const float *A, int64_t lda,
+                  const int *ipiv, float *B, int64_t ldb) {
+  char t = upch(trans);
+  int tr = (t == 'N' || t == 'R') ? 0 : (t == 'T' || t == 'C') ? 1 : -1;
+  int code = 0;
+  if (ldb < (n > 1 ? n : 1)) code = 8;
+  if (lda < (n > 1 ? n : 1)) code = 5;
+  if (nrhs < 0) code = 3;
+  if (n < 0) code = 2;
+  if (tr < 0) code = 1;
+  if (code) {
+    call_xerbla("SGETRS", code);
+    return GB_ERR_INVALID_VALUE;
+  }
+  int st = ensure_init();
+  if (st) return st;
+  return getrs_device<float>(tr, n, nrhs, A, lda, ipiv, B, ldb, stream());
 }
 
 int gb_dlaswp_dev(int64_t n, double *A, int64_t lda, int64_t k1, int64_t k2, const int *ipiv,

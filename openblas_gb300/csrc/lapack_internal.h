@@ -18,6 +18,11 @@ constexpr int GB_KERR_MBARRIER_TIMEOUT = 2;
 // or 0.  Semantics of lapack/getrf/getrf_single.c + getf2_k.c.
 template <typename T>
 int getrf_device(int64_t m, int64_t n, T *A, int64_t lda, int *ipiv, int *info, cudaStream_t s);
+// gemm_mode 1 (double only): the trailing updates run on the emulated-FP64
+// GEMM (FP64-accurate, tensor cores); 0: native FP64 / FP32 SIMT GEMM.
+template <typename T>
+int getrf_device_mode(int64_t m, int64_t n, T *A, int64_t lda, int *ipiv, int *info,
+                      int gemm_mode, cudaStream_t s);
 // Solve op(A) X = B with an LU from getrf_device (lapack/getrs/getrs_single.c).
 template <typename T>
 int getrs_device(int trans, int64_t n, int64_t nrhs, const T *A, int64_t lda, const int *ipiv,

@@ -371,6 +371,7 @@ template <typename T, int R>
 int launch_panel(int64_t rows, int nb, T *A, int64_t lda, int *ipiv, int64_t row_off, int *info,
                  T *slots, unsigned *bar, int *status, unsigned nblocks, cudaStream_t s) {
   void *args[] = {&rows, &nb, &A, &lda, &ipiv, &row_off, &info, &slots, &bar, &status};
+  count_launch();
   return check_cuda(cudaLaunchCooperativeKernel((const void *)getf2_panel_kernel<T, R>,
                                                 dim3(nblocks), dim3(PANEL_THREADS), args, 0, s),
                     "panel factorisation launch");
@@ -423,63 +424,136 @@ template <typename T>
 int laswp_device(int64_t n, T *A, int64_t lda, int64_t k1, int64_t k2, const int *ipiv,
                  int64_t incx, cudaStream_t s) {
   if (n <= 0 || incx == 0 || k2 < k1) return GB_SUCCESS;
-  laswp_kernel<T><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(n, A, lda, k1, k2, ipiv, incx);
+  { laswp_kernel<T><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(n, A, lda, k1, k2, ipiv, incx); count_launch(); }
   return check_cuda(cudaGetLastError(), "laswp launch");
 }
 
-// Right-looking blocked LU (lapack/getrf/getrf_single.c:47-180 with the
-// recursion flattened to PANEL_NB-wide panels): factor the panel, apply its
-// interchanges to the trailing columns, solve with the unit-lower diagonal
-// block, GEMM-update the trailing matrix, and apply the interchanges to the
-// columns left of the panel.
+// Recursive LU (lapack/getrf/getrf_single.c:47-180 splits the columns in
+// halves in the same way): factor the left half, apply its interchanges to
+// the right half, solve for U12 with the unit-lower L11, update A22 with one
+// GEMM of rank n1, factor A22 recursively and apply its interchanges back to
+// the left half.  Leaves of PANEL_NB columns go to the cooperative panel
+// kernel.  Compared with a flat right-looking sweep, every trailing element
+// is rounded O(log n) instead of O(n / PANEL_NB) times and the GEMMs are
+// large, which matters most for the FP32 factorisation of the mixed solver.
 template <typename T>
-int getrf_device(int64_t m, int64_t n, T *A, int64_t lda, int *ipiv, int *info,
-                 cudaStream_t s) {
+struct LuCtx {
+  T *A;
+  int64_t lda;
+  int *ipiv;
+  int *info;
+  T *slots;
+  unsigned *bar;
+  int *status;
+  int lim1, lim2;
+  int gemm_mode;  // double only: 0 native FP64 updates, 1 emulated-FP64 updates
+  cudaStream_t s;
+};
+
+int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
+                   const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
+                   double *C, int64_t ldc, int slices, cudaStream_t s);
+
+template <typename T>
+int lu_update(LuCtx<T> &c, int64_t m, int64_t n, int64_t k, const T *A21, const T *A12, T *A22);
+template <>
+int lu_update<double>(LuCtx<double> &c, int64_t m, int64_t n, int64_t k, const double *A21,
+                      const double *A12, double *A22) {
+  if (c.gemm_mode == 1 && m >= 256 && n >= 256 && k >= 64)
+    return dgemm_emulated(0, 0, m, n, k, -1.0, A21, c.lda, A12, c.lda, 1.0, A22, c.lda, 0, c.s);
+  gemm_minus<double>(m, n, k, A21, c.lda, A12, c.lda, A22, c.lda, c.s);
+  return GB_SUCCESS;
+}
+template <>
+int lu_update<float>(LuCtx<float> &c, int64_t m, int64_t n, int64_t k, const float *A21,
+                     const float *A12, float *A22) {
+  gemm_minus<float>(m, n, k, A21, c.lda, A12, c.lda, A22, c.lda, c.s);
+  return GB_SUCCESS;
+}
+
+template <typename T>
+int lu_panel(LuCtx<T> &c, int64_t r0, int64_t m, int n) {
+  GB_CUDA(cudaMemsetAsync(c.bar, 0, 2 * sizeof(unsigned), c.s));
+  T *P = c.A + r0 + r0 * c.lda;
+  const int64_t b1 = (m + PANEL_THREADS - 1) / PANEL_THREADS;
+  const int64_t b2 = (m + 2 * PANEL_THREADS - 1) / (2 * PANEL_THREADS);
+  if (b1 <= c.lim1)
+    return launch_panel<T, 1>(m, n, P, c.lda, c.ipiv + r0, r0, c.info, c.slots, c.bar, c.status,
+                              (unsigned)b1, c.s);
+  if (b2 <= c.lim2)
+    return launch_panel<T, 2>(m, n, P, c.lda, c.ipiv + r0, r0, c.info, c.slots, c.bar, c.status,
+                              (unsigned)b2, c.s);
+  return set_error(GB_ERR_UNSUPPORTED, "getrf: %lld rows exceed the panel kernel limit",
+                   (long long)m);
+}
+
+// Factor the m x n block whose top-left corner is the diagonal entry (r0, r0); n <= m.
+template <typename T>
+int lu_rec(LuCtx<T> &c, int64_t r0, int64_t m, int64_t n) {
+  if (n <= PANEL_NB) return lu_panel<T>(c, r0, m, (int)n);
+  int64_t n1 = (n / 2) / PANEL_NB * PANEL_NB;
+  if (n1 < PANEL_NB) n1 = PANEL_NB;
+  const int64_t lda = c.lda;
+  int st;
+  if ((st = lu_rec<T>(c, r0, m, n1))) return st;
+  T *L11 = c.A + r0 + r0 * lda;
+  T *A12 = c.A + r0 + (r0 + n1) * lda;
+  if ((st = laswp_device<T>(n - n1, c.A + (r0 + n1) * lda, lda, r0 + 1, r0 + n1, c.ipiv, 1,
+                            c.s)))
+    return st;
+  if ((st = trsm_any<T>(0, 1, 0, 0, n1, n - n1, L11, lda, A12, lda, c.s))) return st;
+  if (m > n1) {
+    if ((st = lu_update<T>(c, m - n1, n - n1, n1, L11 + n1, A12, A12 + n1))) return st;
+    if ((st = lu_rec<T>(c, r0 + n1, m - n1, n - n1))) return st;
+    const int64_t kend = r0 + (m < n ? m : n);
+    if ((st = laswp_device<T>(n1, c.A + r0 * lda, lda, r0 + n1 + 1, kend, c.ipiv, 1, c.s)))
+      return st;
+  }
+  return GB_SUCCESS;
+}
+
+template <typename T>
+int getrf_device_mode(int64_t m, int64_t n, T *A, int64_t lda, int *ipiv, int *info,
+                      int gemm_mode, cudaStream_t s) {
   GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
   const int64_t mn = m < n ? m : n;
   if (mn <= 0) return GB_SUCCESS;
-  const int lim1 = coop_limit<T, 1>(), lim2 = coop_limit<T, 2>();
-  const int64_t maxblk = lim1 > lim2 ? lim1 : lim2;
+  LuCtx<T> c;
+  c.lim1 = coop_limit<T, 1>();
+  c.lim2 = coop_limit<T, 2>();
+  const int64_t maxblk = c.lim1 > c.lim2 ? c.lim1 : c.lim2;
   const size_t slot_elems = 2 * (size_t)maxblk * (PANEL_NB + 2) + 2 * PANEL_NB;
   Scratch ws(slot_elems * sizeof(T) + 256, s);
   if (!ws.p) return GB_ERR_ALLOC;
-  T *slots = ws.as<T>();
-  unsigned *bar = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(ws.p) +
-                                               ((slot_elems * sizeof(T) + 127) & ~size_t(127)));
-  int *status = ctx().d_status;
-  for (int64_t j0 = 0; j0 < mn; j0 += PANEL_NB) {
-    const int jb = (int)((mn - j0) < PANEL_NB ? (mn - j0) : PANEL_NB);
-    const int64_t rows = m - j0;
-    GB_CUDA(cudaMemsetAsync(bar, 0, 2 * sizeof(unsigned), s));
-    T *P = A + j0 + j0 * lda;
-    int st;
-    const int64_t b1 = (rows + PANEL_THREADS - 1) / PANEL_THREADS;
-    const int64_t b2 = (rows + 2 * PANEL_THREADS - 1) / (2 * PANEL_THREADS);
-    if (b1 <= lim1)
-      st = launch_panel<T, 1>(rows, jb, P, lda, ipiv + j0, j0, info, slots, bar, status,
-                              (unsigned)b1, s);
-    else if (b2 <= lim2)
-      st = launch_panel<T, 2>(rows, jb, P, lda, ipiv + j0, j0, info, slots, bar, status,
-                              (unsigned)b2, s);
-    else
-      return set_error(GB_ERR_UNSUPPORTED, "getrf: %lld rows exceed the panel kernel limit",
-                       (long long)rows);
-    if (st) return st;
-    if (j0 + jb < n) {
-      const int64_t nr = n - j0 - jb;
-      T *A12 = A + j0 + (j0 + jb) * lda;
-      if ((st = laswp_device<T>(nr, A + (j0 + jb) * lda, lda, j0 + 1, j0 + jb, ipiv, 1, s)))
-        return st;
-      if ((st = trsm_any<T>(0, 1, 0, 0, jb, nr, P, lda, A12, lda, s))) return st;
-      if (j0 + jb < m)
-        gemm_minus<T>(m - j0 - jb, nr, jb, P + jb, lda, A12, lda, A12 + jb, lda, s);
-    }
-    if (j0 > 0) {
-      if ((st = laswp_device<T>(j0, A, lda, j0 + 1, j0 + jb, ipiv, 1, s))) return st;
-    }
+  c.A = A;
+  c.lda = lda;
+  c.ipiv = ipiv;
+  c.info = info;
+  c.slots = ws.as<T>();
+  c.bar = reinterpret_cast<unsigned *>(reinterpret_cast<char *>(ws.p) +
+                                       ((slot_elems * sizeof(T) + 127) & ~size_t(127)));
+  c.status = ctx().d_status;
+  c.gemm_mode = gemm_mode;
+  c.s = s;
+  int st = lu_rec<T>(c, 0, m, mn);
+  if (st) return st;
+  if (n > mn) {
+    // wide matrix: the remaining columns get the interchanges and L11^-1
+    T *R = A + mn * lda;
+    if ((st = laswp_device<T>(n - mn, R, lda, 1, mn, ipiv, 1, s))) return st;
+    if ((st = trsm_any<T>(0, 1, 0, 0, mn, n - mn, A, lda, R, lda, s))) return st;
   }
   return check_cuda(cudaGetLastError(), "getrf");
 }
+
+template <typename T>
+int getrf_device(int64_t m, int64_t n, T *A, int64_t lda, int *ipiv, int *info,
+                 cudaStream_t s) {
+  return getrf_device_mode<T>(m, n, A, lda, ipiv, info, 0, s);
+}
+
+template int getrf_device_mode<double>(int64_t, int64_t, double *, int64_t, int *, int *, int,
+                                       cudaStream_t);
 
 // lapack/getrs/getrs_single.c:42-68.  The interchanges of the solve are
 // applied as one gather through the final permutation.
@@ -492,12 +566,12 @@ int getrs_device(int trans, int64_t n, int64_t nrhs, const T *A, int64_t lda, co
   int *perm = ws.as<int>();
   T *tmp = reinterpret_cast<T *>(reinterpret_cast<char *>(ws.p) +
                                  ((n * sizeof(int) + 127) & ~size_t(127)));
-  pivots_to_perm_kernel<<<1, 1, 0, s>>>(n, ipiv, perm);
+  { pivots_to_perm_kernel<<<1, 1, 0, s>>>(n, ipiv, perm); count_launch(); }
   const int64_t total = n * nrhs;
   const unsigned grid = (unsigned)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
   int st;
   if (!trans) {
-    permute_rows_kernel<T><<<grid, 256, 0, s>>>(n, nrhs, perm, B, ldb, tmp, n, 0);
+    { permute_rows_kernel<T><<<grid, 256, 0, s>>>(n, nrhs, perm, B, ldb, tmp, n, 0); count_launch(); }
     GB_CUDA(cudaMemcpy2DAsync(B, ldb * sizeof(T), tmp, n * sizeof(T), n * sizeof(T), nrhs,
                               cudaMemcpyDeviceToDevice, s));
     if ((st = trsm_any<T>(0, 1, 0, 0, n, nrhs, A, lda, B, ldb, s))) return st;
@@ -505,7 +579,7 @@ int getrs_device(int trans, int64_t n, int64_t nrhs, const T *A, int64_t lda, co
   } else {
     if ((st = trsm_any<T>(0, 0, 1, 1, n, nrhs, A, lda, B, ldb, s))) return st;
     if ((st = trsm_any<T>(0, 1, 1, 0, n, nrhs, A, lda, B, ldb, s))) return st;
-    permute_rows_kernel<T><<<grid, 256, 0, s>>>(n, nrhs, perm, B, ldb, tmp, n, 1);
+    { permute_rows_kernel<T><<<grid, 256, 0, s>>>(n, nrhs, perm, B, ldb, tmp, n, 1); count_launch(); }
     GB_CUDA(cudaMemcpy2DAsync(B, ldb * sizeof(T), tmp, n * sizeof(T), n * sizeof(T), nrhs,
                               cudaMemcpyDeviceToDevice, s));
   }
@@ -522,7 +596,7 @@ int potrf_device(int uplo, int64_t n, double *A, int64_t lda, int *info, cudaStr
   for (int64_t j0 = 0; j0 < n; j0 += PANEL_NB) {
     const int jb = (int)((n - j0) < PANEL_NB ? (n - j0) : PANEL_NB);
     double *D = A + j0 + j0 * lda;
-    potf2_kernel<double><<<1, 256, 0, s>>>(upper ? 1 : 0, jb, D, lda, info, j0);
+    { potf2_kernel<double><<<1, 256, 0, s>>>(upper ? 1 : 0, jb, D, lda, info, j0); count_launch(); }
     const int64_t rest = n - j0 - jb;
     if (rest <= 0) continue;
     int st;

@@ -94,14 +94,14 @@ void launch_trsm_diag(bool left, bool forward, int trans, int unit, int ib, int6
                       const int *skip) {
   const unsigned grid = (unsigned)((nvec + 127) / 128);
   if (left && forward)
-    trsm_diag_kernel<T, true, true><<<grid, 128, 0, s>>>(trans, unit, ib, nvec, A, lda, B, ldb, skip);
+    { trsm_diag_kernel<T, true, true><<<grid, 128, 0, s>>>(trans, unit, ib, nvec, A, lda, B, ldb, skip); count_launch(); }
   else if (left)
-    trsm_diag_kernel<T, true, false><<<grid, 128, 0, s>>>(trans, unit, ib, nvec, A, lda, B, ldb, skip);
+    { trsm_diag_kernel<T, true, false><<<grid, 128, 0, s>>>(trans, unit, ib, nvec, A, lda, B, ldb, skip); count_launch(); }
   else if (forward)
-    trsm_diag_kernel<T, false, true><<<grid, 128, 0, s>>>(trans, unit, ib, nvec, A, lda, B, ldb, skip);
+    { trsm_diag_kernel<T, false, true><<<grid, 128, 0, s>>>(trans, unit, ib, nvec, A, lda, B, ldb, skip); count_launch(); }
   else
-    trsm_diag_kernel<T, false, false><<<grid, 128, 0, s>>>(trans, unit, ib, nvec, A, lda, B,
-                                                           ldb, skip);
+    { trsm_diag_kernel<T, false, false><<<grid, 128, 0, s>>>(trans, unit, ib, nvec, A, lda, B,
+                                                           ldb, skip); count_launch(); }
 }
 
 template <typename T>

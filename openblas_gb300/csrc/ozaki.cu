@@ -321,10 +321,14 @@ __global__ void exponent_kernel(int64_t Rpad, int64_t R, const unsigned long lon
   int e = 0;
   if (r < R) {
     double v = __longlong_as_double((long long)mx[r]);
-    if (!isfinite(v)) {
+    const unsigned long long b = mx[r];
+    const int E = (int)((b >> 52) & 0x7ff);
+    if (E == 0x7ff) {
       e = NONFINITE;
-    } else if (v > 0.0) {
-      frexp(v, &e);  // v = f * 2^e with f in [0.5, 1): |x| < 2^e on the row
+    } else if (E > 0) {
+      e = E - 1022;  // max = 1.f * 2^(E-1023) < 2^(E-1022): |x| < 2^e on the row
+    } else if (b != 0) {
+      frexp(v, &e);  // subnormal maximum
     }
   }
   expo[r] = e;
@@ -356,19 +360,35 @@ split_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
     tile[rr][pp] = v;
   }
   __syncthreads();
-  // each thread: row rr = tid / 8, 8 consecutive k values
+  // each thread: row rr = tid / 8, 8 consecutive k values.  The fixed-point
+  // value trunc(|x| * 2^(7S - e)) is taken straight from the IEEE bits
+  // (mantissa shifted by the exponent difference): integer work only, as
+  // FP64 arithmetic is the scarcest unit on this part.
   const int rr = tid >> 3, pc = (tid & 7) * 8;
   const int64_t r = r0 + rr;
   const int e = (r < R) ? expo[r] : 0;
-  const int shift = 7 * S - e;
   unsigned long long mag[8];
   bool neg[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    double v = tile[rr][pc + j];
-    neg[j] = v < 0.0;
-    double sv = (e == NONFINITE) ? 0.0 : ldexp(fabs(v), shift);  // < 2^(7S), exact scaling
-    mag[j] = (unsigned long long)sv;                             // truncation toward zero
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(tile[rr][pc + j]);
+    neg[j] = (bits >> 63) != 0;
+    const int E = (int)((bits >> 52) & 0x7ff);
+    unsigned long long M = bits & 0xFFFFFFFFFFFFFull;
+    int sh;  // |x| = M * 2^(sh0) with sh0 = E - 1075 (normal) or -1074 (subnormal)
+    if (E == 0) {
+      sh = -1074;
+    } else {
+      M |= 1ull << 52;
+      sh = E - 1075;
+    }
+    sh += 7 * S - e;
+    unsigned long long t;
+    if (e == NONFINITE || M == 0) t = 0;
+    else if (sh >= 0) t = M << sh;       // |x| < 2^e keeps t < 2^(7S)
+    else if (sh > -64) t = M >> (-sh);   // truncation toward zero
+    else t = 0;
+    mag[j] = t;
   }
   for (int s = 1; s <= S; ++s) {
     const int sh = 7 * (S - s);
@@ -406,13 +426,34 @@ __global__ void recombine_kernel(int64_t m, int64_t n, int S, int m_tiles, int64
       }
       v = alpha * s;
     } else {
+      // exact integer sum of the levels: sum_L P_L * 2^(7(S+1-L)) (< 2^81)
       const int64_t tile = (j / 256) * m_tiles + (i / 128);
       const int64_t off = tile * (128 * 256) + (j % 256) * 128 + (i % 128);
-      double acc = (double)planes[(int64_t)(S - 1) * plane_stride + off];
-      for (int L = S; L >= 2; --L)
-        acc = fma(acc, 0.0078125 /* 2^-7 */, (double)planes[(int64_t)(L - 2) * plane_stride + off]);
-      // acc * 2^(ei + fj - 14), scaled in two steps against over/underflow
-      v = alpha * ldexp(ldexp(acc, ei - 14), fj);
+      __int128 acc = 0;
+      for (int L = 2; L <= S + 1; ++L)
+        acc += (__int128)planes[(int64_t)(L - 2) * plane_stride + off] << (7 * (S + 1 - L));
+      v = 0.0;
+      if (acc != 0) {
+        const bool neg = acc < 0;
+        unsigned __int128 u = neg ? (unsigned __int128)(-acc) : (unsigned __int128)acc;
+        const unsigned long long hi = (unsigned long long)(u >> 64);
+        const int msb = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)(unsigned long long)u);
+        int sh = msb > 63 ? msb - 63 : 0;
+        unsigned long long top = (unsigned long long)(u >> sh);
+        if (sh && (u & (((unsigned __int128)1 << sh) - 1)) != 0) top |= 1ull;  // sticky bit
+        // one correctly rounded conversion, then an exact power-of-two scaling
+        // folded into alpha: value = top * 2^(sh - 7(S+1) + e_i + f_j)
+        const double t = __ull2double_rn(top);
+        const int x = sh - 7 * (S + 1) + ei + fj;
+        const long long ab = __double_as_longlong(alpha);
+        const int ea = (int)((ab >> 52) & 0x7ff);
+        double scale;
+        if (ea > 0 && ea < 0x7ff && ea + x > 0 && ea + x < 0x7ff)
+          scale = __longlong_as_double(ab + ((long long)x << 52));
+        else
+          scale = alpha * ldexp(1.0, x);
+        v = (neg ? -t : t) * scale;
+      }
     }
     double *c = C + i + j * ldc;
     *c = (beta == 0.0) ? v : fma(beta, *c, v);
@@ -462,18 +503,18 @@ void split_operand(bool kcontig, int64_t R, int64_t K, const double *X, int64_t 
                    __nv_bfloat16 *slices, cudaStream_t s) {
   cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * Rpad, s);
   if (kcontig) {
-    rowmax_kcontig_kernel<<<(unsigned)((R + 7) / 8), 256, 0, s>>>(R, K, X, ld, mx);
+    { rowmax_kcontig_kernel<<<(unsigned)((R + 7) / 8), 256, 0, s>>>(R, K, X, ld, mx); count_launch(); }
   } else {
     const int64_t kspan = 256;
     dim3 g((unsigned)((R + 255) / 256), (unsigned)((K + kspan - 1) / kspan));
-    rowmax_mcontig_kernel<<<g, 256, 0, s>>>(R, K, X, ld, kspan, mx);
+    { rowmax_mcontig_kernel<<<g, 256, 0, s>>>(R, K, X, ld, kspan, mx); count_launch(); }
   }
-  exponent_kernel<<<(unsigned)((Rpad + 255) / 256), 256, 0, s>>>(Rpad, R, mx, expo);
+  { exponent_kernel<<<(unsigned)((Rpad + 255) / 256), 256, 0, s>>>(Rpad, R, mx, expo); count_launch(); }
   dim3 g2((unsigned)(Kpad / 64), (unsigned)(Rpad / 32));
   if (kcontig)
-    split_kernel<true><<<g2, 256, 0, s>>>(R, K, X, ld, expo, S, Rpad, Kpad, slices);
+    { split_kernel<true><<<g2, 256, 0, s>>>(R, K, X, ld, expo, S, Rpad, Kpad, slices); count_launch(); }
   else
-    split_kernel<false><<<g2, 256, 0, s>>>(R, K, X, ld, expo, S, Rpad, Kpad, slices);
+    { split_kernel<false><<<g2, 256, 0, s>>>(R, K, X, ld, expo, S, Rpad, Kpad, slices); count_launch(); }
 }
 
 // One pass over a K segment (k <= MAX_K_SEGMENT).
@@ -524,15 +565,19 @@ int emulated_segment(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
   gp.status = ctx().d_status;
   const int ntiles = gp.m_tiles * gp.n_tiles;
   const int grid = ntiles < sm_count() ? ntiles : sm_count();
-  slice_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, gp);
+  {
+    ProfileScope prof("slice_gemm", s);
+    slice_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, gp);
+    count_launch();
+  }
   GB_CUDA(cudaGetLastError());
 
   const int64_t total = m * n;
   int64_t blocks = (total + 255) / 256;
   const int64_t cap = (int64_t)sm_count() * 32;
-  recombine_kernel<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(
+  { recombine_kernel<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(
       m, n, S, gp.m_tiles, plane_stride, planes, ea, eb, alpha, beta, C, ldc, ta, tb, k, A, lda,
-      B, ldb);
+      B, ldb); count_launch(); }
   return check_cuda(cudaGetLastError(), "emulated dgemm");
 }
 

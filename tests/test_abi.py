@@ -142,6 +142,20 @@ def test_lapack_argument_errors(gblib, F):
     assert _xerbla(gblib) == ("DGETRS", 8)
 
 
+def test_dsgesv_argument_errors(gblib, F):
+    buf = np.zeros((64, 64), order="F")
+    piv = np.zeros(64, np.int32)
+    w = np.zeros(64 * 64)
+    sw = np.zeros(64 * 64, np.float32)
+    # lapack-netlib/SRC/dsgesv.f:236-249
+    for args, pos in [((-1, 1, 4, 4, 4), 1), ((4, -1, 4, 4, 4), 2), ((4, 1, 3, 4, 4), 4),
+                      ((4, 1, 4, 3, 4), 7), ((4, 1, 4, 4, 3), 9)]:
+        n, nrhs, lda, ldb, ldx = args
+        info, it = F.dsgesv(n, nrhs, buf, lda, piv, buf, ldb, buf, ldx, w, sw)
+        assert info == -pos and it == 0
+        assert _xerbla(gblib) == ("DSGESV", pos)
+
+
 def test_quick_returns_do_not_touch_device(gblib, F):
     """m==0/n==0 quick returns happen before any CUDA call, so they succeed on
     a machine without a GPU (interface/gemm.c:494, getrf.c:83, potrf.c:104)."""

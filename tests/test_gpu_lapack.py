@@ -73,6 +73,23 @@ def test_dgetrf_vs_oracle(orc, F, gb_clean, m, n):
     assert lu_residual(A0, A, p) <= 10
 
 
+@pytest.mark.parametrize("n", [700, 2600])
+def test_dgetrf_emulated_updates(orc, F, gblib, gb_clean, n):
+    """DGETRF whose trailing updates run on the emulated-FP64 GEMM (DGEMM
+    mode 'emulated'): same pivots as the oracle, FP64-level scaled residual."""
+    A0 = W.uniform(7700 + n, (n, n))
+    A, Ao = A0.copy(order="F"), A0.copy(order="F")
+    p, po = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    gblib.gb_set_dgemm_mode(1)
+    try:
+        assert F.dgetrf(n, n, A, n, p) == 0
+    finally:
+        gblib.gb_set_dgemm_mode(0)
+    assert orc.dgetrf(n, n, Ao, n, po) == 0
+    assert np.array_equal(p, po)
+    assert lu_residual(A0, A, p) <= 10
+
+
 def test_dgetrf_tiny_pivot_rule(orc, F, gb_clean):
     """A subnormal pivot is recorded but neither swapped nor divided by
     (getf2_k.c:103-116); the GPU panel follows the same rule."""
@@ -171,3 +188,42 @@ def test_dlaswp_golden(golden, F, gb_clean):
         ipiv = golden[f"dlaswp_{idx}_ipiv"].astype(np.int32)
         F.dlaswp(n, A, rows, k1, k2, ipiv, incx)
         assert np.array_equal(A, golden[f"dlaswp_{idx}"]), (n, k1, k2, incx)
+
+
+def _sgetrf_dev(gblib, A32):
+    torch = pytest.importorskip("torch")
+    m, n = A32.shape
+    dA = torch.from_numpy(np.ascontiguousarray(A32.T)).cuda()
+    dp = torch.zeros(min(m, n), dtype=torch.int32, device="cuda")
+    di = torch.zeros(1, dtype=torch.int32, device="cuda")
+    assert gblib.gb_sgetrf_dev(m, n, dA.data_ptr(), m, dp.data_ptr(), di.data_ptr()) == 0
+    assert gblib.gb_synchronize() == 0
+    return dA.cpu().numpy().T.copy(order="F"), dp.cpu().numpy(), int(di.item())
+
+
+@pytest.mark.parametrize("n", [256, 1500])
+def test_sgetrf_vs_oracle(orc, gblib, gb_clean, n):
+    """The FP32 factorisation behind the mixed solver: pivots identical to the
+    oracle's sgetrf and FP32-level scaled residual."""
+    A0 = np.asfortranarray(W.uniform(8700 + n, (n, n)).astype(np.float32))
+    LU, piv, info = _sgetrf_dev(gblib, A0)
+    Ao = A0.copy(order="F")
+    po = np.zeros(n, np.int32)
+    assert info == orc.sgetrf(n, n, Ao, n, po) == 0
+    assert np.array_equal(piv, po)
+    feps = float(np.finfo(np.float32).eps)
+    L = np.tril(LU.astype(np.float64), -1) + np.eye(n)
+    U = np.triu(LU.astype(np.float64))
+    PA = _apply_piv(A0, piv)
+    r = np.abs(PA - L @ U).sum(axis=0).max() / (n * feps * np.abs(A0).sum(axis=0).max())
+    assert r <= 10, r
+    rel = np.abs(LU - Ao).max() / np.abs(Ao).max()
+    assert rel <= 1e-3, rel
+
+
+def _apply_piv(A, piv):
+    P = A.astype(np.float64).copy(order="F")
+    for i, p in enumerate(piv):
+        if p - 1 != i:
+            P[[i, p - 1], :] = P[[p - 1, i], :]
+    return P
