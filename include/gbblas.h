@@ -222,6 +222,22 @@ int gb_sgetrs_dev(char trans, int64_t n, int64_t nrhs, const float *A,
 int gb_dlaswp_dev(int64_t n, double *A, int64_t lda, int64_t k1, int64_t k2,
                   const int *ipiv, int64_t incx);
 int gb_dpotrf_dev(char uplo, int64_t n, double *A, int64_t lda, int *info);
+/* LU with partial pivoting that allocates no device memory.  This entry has
+ * no counterpart in the reference.  It exists for callers that cannot let a
+ * library allocate: applications that hand all of HBM to their own arena and
+ * forbid other allocations, services held to a fixed memory budget, and loops
+ * that cannot absorb the synchronisation and latency of cudaMalloc/cudaFree.
+ * Same contract as gb_dgetrf_dev (native FP64 trailing updates), on the given
+ * stream (NULL = the legacy default stream).  Its scratch is a 1 MiB
+ * file-scope device array inside the library, held by every GPU that loads
+ * the library until the process exits; it serves m <= 524288 rows, and larger
+ * m is rejected with GB_ERR_UNSUPPORTED.  The first call on each device looks
+ * up the array's device address with that device current; make that first
+ * call before any stream capture.  All calls share the array: calls whose GPU
+ * work overlaps (other streams, other threads) race and must be serialised by
+ * the caller. */
+int gb_dgetrf_noalloc_dev(int64_t m, int64_t n, double *A, int64_t lda,
+                          int *ipiv, int *info, void *stream);
 /* Mixed-precision solve (FP32 LU on the GPU + FP64 refinement, GMRES-IR
  * when plain refinement stalls, FP64 LU fallback).  Device pointers except
  * iter/info, which are host outputs (this call synchronises).  A is only

@@ -22,8 +22,11 @@
 #include <float.h>
 #include <stdint.h>
 
+#include <mutex>
+
 #include "gb_internal.h"
 #include "lapack_internal.h"
+#include "operand.h"
 
 namespace gb {
 
@@ -554,6 +557,109 @@ int getrf_device(int64_t m, int64_t n, T *A, int64_t lda, int *ipiv, int *info,
 
 template int getrf_device_mode<double>(int64_t, int64_t, double *, int64_t, int *, int *, int,
                                        cudaStream_t);
+
+// ---------------------------------------------------------------------------
+// LU without device allocation.
+//
+// Some callers cannot let a library allocate device memory: an application
+// that hands every byte of HBM to its own arena or pool and forbids other
+// allocations, a service that must stay inside a fixed memory budget for its
+// whole life, or a caller that cannot afford the implicit synchronisation and
+// latency of cudaMalloc/cudaFree in its loop.  For them the LU entry point
+// below keeps the only scratch it needs -- the panel factorisation's
+// parity-buffered candidate rows, its grid-barrier words and a status word --
+// in this file-scope device array, so it makes no allocation at all.  The
+// array is part of the loaded module: every GPU that uses the library holds
+// these bytes until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+
+constexpr int NOALLOC_MAX_BLOCKS = 1024;  // cooperative panel blocks served
+constexpr size_t NOALLOC_SLOT_BYTES =
+    (2 * (size_t)NOALLOC_MAX_BLOCKS * (PANEL_NB + 2) + 2 * PANEL_NB) * sizeof(double);
+constexpr size_t NOALLOC_SCRATCH_BYTES = 1u << 20;  // 1 MiB
+static_assert(NOALLOC_SLOT_BYTES + 256 <= NOALLOC_SCRATCH_BYTES, "scratch too small");
+// Rows the panel kernel can cover with the blocks above (two rows per thread).
+constexpr int64_t NOALLOC_MAX_ROWS = (int64_t)NOALLOC_MAX_BLOCKS * 2 * PANEL_THREADS;
+
+static __device__ __align__(256) unsigned char g_lu_scratch[NOALLOC_SCRATCH_BYTES];
+
+// Device address of g_lu_scratch per device, resolved once per device with
+// that device current (host code must not use the symbol itself as an address).
+std::mutex g_lu_scratch_mu;
+void *g_lu_scratch_addr[64] = {nullptr};
+
+int lu_scratch_address(void **out) {
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return check_cuda(e, "cudaGetDevice");
+  if (dev < 0 || dev >= 64) return set_error(GB_ERR_UNSUPPORTED, "device index %d", dev);
+  std::lock_guard<std::mutex> lk(g_lu_scratch_mu);
+  if (!g_lu_scratch_addr[dev]) {
+    void *p = nullptr;
+    e = cudaGetSymbolAddress(&p, g_lu_scratch);
+    if (e != cudaSuccess) return check_cuda(e, "cudaGetSymbolAddress(g_lu_scratch)");
+    g_lu_scratch_addr[dev] = p;
+  }
+  *out = g_lu_scratch_addr[dev];
+  return GB_SUCCESS;
+}
+
+}  // namespace
+
+}  // namespace gb
+
+extern "C" int gb_dgetrf_noalloc_dev(int64_t m, int64_t n, double *A, int64_t lda, int *ipiv,
+                                     int *info, void *stream) {
+  using namespace gb;
+  int code = 0;
+  if (lda < (m > 1 ? m : 1)) code = 4;
+  if (n < 0) code = 2;
+  if (m < 0) code = 1;
+  if (code) {
+    call_xerbla("DGETRF", code);
+    return GB_ERR_INVALID_VALUE;
+  }
+  if (m > NOALLOC_MAX_ROWS)
+    return set_error(GB_ERR_UNSUPPORTED,
+                     "gb_dgetrf_noalloc_dev: m = %lld exceeds the %lld rows its fixed scratch "
+                     "serves",
+                     (long long)m, (long long)NOALLOC_MAX_ROWS);
+  cudaStream_t s = reinterpret_cast<cudaStream_t>(stream);
+  void *base = nullptr;
+  int st = lu_scratch_address(&base);
+  if (st) return st;
+  GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
+  const int64_t mn = m < n ? m : n;
+  if (mn <= 0) return GB_SUCCESS;
+  LuCtx<double> c;
+  c.lim1 = coop_limit<double, 1>();
+  c.lim2 = coop_limit<double, 2>();
+  if (c.lim1 > NOALLOC_MAX_BLOCKS) c.lim1 = NOALLOC_MAX_BLOCKS;
+  if (c.lim2 > NOALLOC_MAX_BLOCKS) c.lim2 = NOALLOC_MAX_BLOCKS;
+  char *b = reinterpret_cast<char *>(base);
+  c.A = A;
+  c.lda = lda;
+  c.ipiv = ipiv;
+  c.info = info;
+  c.slots = reinterpret_cast<double *>(b);
+  c.bar = reinterpret_cast<unsigned *>(b + ((NOALLOC_SLOT_BYTES + 127) & ~size_t(127)));
+  c.status = reinterpret_cast<int *>(c.bar + 32);
+  c.gemm_mode = 0;  // native FP64 trailing updates: no scratch anywhere below
+  c.s = s;
+  // the shared array keeps the previous call's contents: clear the words that
+  // must start at zero (barrier counters are cleared again before every panel)
+  GB_CUDA(cudaMemsetAsync(c.bar, 0, 32 * sizeof(unsigned) + 4 * sizeof(int), s));
+  if ((st = lu_rec<double>(c, 0, m, mn))) return st;
+  if (n > mn) {
+    double *R = A + mn * lda;
+    if ((st = laswp_device<double>(n - mn, R, lda, 1, mn, ipiv, 1, s))) return st;
+    if ((st = trsm_any<double>(0, 1, 0, 0, mn, n - mn, A, lda, R, lda, s))) return st;
+  }
+  return check_cuda(cudaGetLastError(), "gb_dgetrf_noalloc_dev");
+}
+
+namespace gb {
 
 // lapack/getrs/getrs_single.c:42-68.  The interchanges of the solve are
 // applied as one gather through the final permutation.
