@@ -31,6 +31,21 @@ int getrs_device(int trans, int64_t n, int64_t nrhs, const T *A, int64_t lda, co
 template <typename T>
 int laswp_device(int64_t n, T *A, int64_t lda, int64_t k1, int64_t k2, const int *ipiv,
                  int64_t incx, cudaStream_t s);
+// Inverses of the 64x64 diagonal blocks of the unit-lower L and of U of an
+// LU factorisation (each n/64 * 64*64 entries), and the blocked solve that
+// uses them (interchanges applied beforehand).
+template <typename T>
+int lu_block_inverses(int64_t n, const T *A, int64_t lda, T *Linv, T *Uinv, cudaStream_t s);
+template <typename T>
+int lu_block_solve(int64_t n, int64_t nrhs, const T *A, int64_t lda, const T *Linv,
+                   const T *Uinv, T *B, int64_t ldb, cudaStream_t s);
+// Final permutation of the interchanges ipiv[0..n): row i of P*B is row
+// perm[i] of B; and the gather dst = P*src.
+int pivots_to_perm(int64_t n, const int *ipiv, int *perm, cudaStream_t s);
+template <typename T>
+int apply_perm(int64_t n, int64_t ncol, const int *perm, const T *src, int64_t lds, T *dst,
+               int64_t ldd, cudaStream_t s);
+
 // Cholesky (lapack/potrf/potrf_{L,U}_single.c); *info_host receives info.
 int potrf_device(int uplo, int64_t n, double *A, int64_t lda, int *info_dev, cudaStream_t s);
 

@@ -21,6 +21,9 @@
 #include <cuda_runtime.h>
 #include <float.h>
 #include <stdint.h>
+#include <stdio.h>
+
+#include <cooperative_groups.h>
 
 #include <mutex>
 
@@ -370,6 +373,277 @@ potf2_kernel(int upper, int nb, T *__restrict__ A, int64_t lda, int *__restrict_
   if (tid == 0 && s_fail >= 0) *info = (int)(row_off + s_fail + 1);
 }
 
+// Panel LU on one thread-block cluster (up to 16 CTAs of 512 threads).
+// Same algorithm and pivot rules as getf2_panel_kernel, but the panel rows
+// live in shared memory, the per-column exchange of candidate rows goes
+// through distributed shared memory and the per-column synchronisation is the
+// hardware cluster barrier -- no global-memory round trips on the critical
+// path.  Rows per thread: L (<= 3 for float, 1 for double).
+constexpr int CPANEL_THREADS = 512;
+constexpr int CPANEL_WARPS = CPANEL_THREADS / 32;
+constexpr int CPANEL_LD = PANEL_NB + 1;  // padded row stride in shared memory
+
+template <typename T>
+__host__ __device__ constexpr size_t cpanel_smem_bytes(int L) {
+  return (size_t)L * CPANEL_THREADS * CPANEL_LD * sizeof(T)  // rows
+         + 6 * PANEL_NB * sizeof(T)                            // cand rows, row j, u, old j
+         + 2 * sizeof(T) + 2 * sizeof(long long)               // cand (value, index) x2
+         + CPANEL_WARPS * (sizeof(T) + sizeof(long long)) + 64;
+}
+
+template <typename T>
+__global__ void __launch_bounds__(CPANEL_THREADS, 1)
+getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__restrict__ ipiv,
+                     int64_t row_off, int *__restrict__ info, int L) {
+  namespace cg = cooperative_groups;
+  cg::cluster_group cluster = cg::this_cluster();
+  const int CS = (int)cluster.num_blocks();
+  const int rank = (int)cluster.block_rank();
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  T *rows = reinterpret_cast<T *>(smem_raw);
+  T *cand_row = rows + (size_t)L * CPANEL_THREADS * CPANEL_LD;  // [2][NB]
+  T *rowj = cand_row + 2 * PANEL_NB;                             // [2][NB]
+  T *s_u = rowj + 2 * PANEL_NB;                                  // [NB]
+  T *s_oldj = s_u + PANEL_NB;                                    // [NB]
+  T *cand_val = s_oldj + PANEL_NB;                               // [2]
+  long long *cand_idx = reinterpret_cast<long long *>(
+      (reinterpret_cast<uintptr_t>(cand_val + 2) + 7) & ~uintptr_t(7));  // [2]
+  T *red_val = reinterpret_cast<T *>(cand_idx + 2);                    // [WARPS]
+  long long *red_idx = reinterpret_cast<long long *>(
+      (reinterpret_cast<uintptr_t>(red_val + CPANEL_WARPS) + 7) & ~uintptr_t(7));
+  __shared__ long long s_best, s_p;
+
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t nthr = (int64_t)CS * CPANEL_THREADS;
+  const int64_t g = (int64_t)rank * CPANEL_THREADS + tid;
+  auto row_ptr = [&](int q) { return rows + ((size_t)q * CPANEL_THREADS + tid) * CPANEL_LD; };
+
+  for (int q = 0; q < L; ++q) {
+    const int64_t r = g + q * nthr;
+    T *v = row_ptr(q);
+    for (int c = 0; c < PANEL_NB; ++c) v[c] = (r < m && c < nb) ? A[r + c * lda] : T(0);
+  }
+  cluster.sync();
+
+  const int ncol = (int)(nb < m ? nb : m);
+  for (int j = 0; j < ncol; ++j) {
+    const int par = j & 1;
+    // ---- local first maximum of |a_ij| over this thread's rows >= j
+    T best = T(-1);
+    long long bidx = LLONG_MAX;
+    for (int q = 0; q < L; ++q) {
+      const int64_t r = g + q * nthr;
+      if (r < m && r >= j) {
+        T a = row_ptr(q)[j];
+        a = a < T(0) ? -a : a;
+        if (a > best || (a == best && r < bidx)) {
+          best = a;
+          bidx = r;
+        }
+      }
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      T ob = __shfl_down_sync(0xffffffffu, best, off);
+      long long oi = __shfl_down_sync(0xffffffffu, bidx, off);
+      if (ob > best || (ob == best && oi < bidx)) {
+        best = ob;
+        bidx = oi;
+      }
+    }
+    if (lane == 0) {
+      red_val[warp] = best;
+      red_idx[warp] = bidx;
+    }
+    __syncthreads();
+    if (warp == 0) {
+      T bb = lane < CPANEL_WARPS ? red_val[lane] : T(-1);
+      long long bi = lane < CPANEL_WARPS ? red_idx[lane] : LLONG_MAX;
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        T ob = __shfl_down_sync(0xffffffffu, bb, off);
+        long long oi = __shfl_down_sync(0xffffffffu, bi, off);
+        if (ob > bb || (ob == bb && oi < bi)) {
+          bb = ob;
+          bi = oi;
+        }
+      }
+      if (lane == 0) {
+        cand_val[par] = bb;
+        cand_idx[par] = (bi == LLONG_MAX) ? -1 : bi;
+        s_best = bi;
+      }
+    }
+    __syncthreads();
+    // publish the CTA's best row and (if held here) row j, one column per thread
+    if (tid < PANEL_NB) {
+      const long long b = s_best;
+      if (b != LLONG_MAX) {
+        const int64_t gt = b % nthr, q = b / nthr;
+        const int lt = (int)(gt - (int64_t)rank * CPANEL_THREADS);
+        cand_row[par * PANEL_NB + tid] = rows[((size_t)q * CPANEL_THREADS + lt) * CPANEL_LD + tid];
+      }
+      const int64_t gj = (int64_t)j % nthr, qj = (int64_t)j / nthr;
+      if (gj / CPANEL_THREADS == rank) {
+        const int lt = (int)(gj - (int64_t)rank * CPANEL_THREADS);
+        rowj[par * PANEL_NB + tid] = rows[((size_t)qj * CPANEL_THREADS + lt) * CPANEL_LD + tid];
+      }
+    }
+    cluster.sync();  // candidates of column j visible cluster-wide
+    // ---- global pivot (identical in every CTA): first maximum over the CTAs
+    if (warp == 0) {
+      T bb = T(-1);
+      long long bi = LLONG_MAX;
+      if (lane < CS) {
+        const T val = *cluster.map_shared_rank(cand_val + par, lane);
+        const long long idx = *cluster.map_shared_rank(cand_idx + par, lane);
+        if (idx >= 0) {
+          bb = val;
+          bi = idx;
+        }
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        T ob = __shfl_down_sync(0xffffffffu, bb, off);
+        long long oi = __shfl_down_sync(0xffffffffu, bi, off);
+        if (ob > bb || (ob == bb && oi < bi)) {
+          bb = ob;
+          bi = oi;
+        }
+      }
+      if (lane == 0) s_p = bi;
+    }
+    __syncthreads();
+    const int64_t p = s_p;
+    if (tid < PANEL_NB) {
+      const int owner = (int)((p % nthr) / CPANEL_THREADS);
+      const int jowner = (int)(((int64_t)j % nthr) / CPANEL_THREADS);
+      s_u[tid] = *cluster.map_shared_rank(cand_row + par * PANEL_NB + tid, owner);
+      s_oldj[tid] = *cluster.map_shared_rank(rowj + par * PANEL_NB + tid, jowner);
+    }
+    __syncthreads();
+    const T piv = s_u[j];
+    const T apiv = piv < T(0) ? -piv : piv;
+    const bool nonzero = piv != T(0);
+    const bool scaled = nonzero && apiv >= tiny_pivot<T>();  // getf2_k.c:103-116
+    const bool swap = p != j;
+    if (rank == 0 && tid == 0) {
+      ipiv[j] = (int)(p + row_off + 1);
+      if (!nonzero && *info == 0) *info = (int)(j + row_off + 1);
+    }
+    const T rcp = scaled ? T(1) / piv : T(1);
+    for (int q = 0; q < L; ++q) {
+      const int64_t i = g + q * nthr;
+      if (i >= m || i < j) continue;
+      T *v = row_ptr(q);
+      if (swap && i == j) {
+        for (int c = 0; c < PANEL_NB; ++c)
+          if (scaled || c > j) v[c] = s_u[c];
+        continue;  // the pivot row is final
+      }
+      if (swap && i == p) {
+        for (int c = 0; c < PANEL_NB; ++c)
+          if (scaled || c > j) v[c] = s_oldj[c];
+      }
+      if (i == j) continue;
+      T l = v[j];
+      if (scaled) l *= rcp;
+      v[j] = l;
+      for (int c = j + 1; c < PANEL_NB; ++c) v[c] = fma(-l, s_u[c], v[c]);
+    }
+  }
+  for (int q = 0; q < L; ++q) {
+    const int64_t r = g + q * nthr;
+    if (r >= m) continue;
+    const T *v = row_ptr(q);
+    for (int c = 0; c < nb; ++c) A[r + c * lda] = v[c];
+  }
+  cluster.sync();  // no CTA leaves while another may still read its shared memory
+}
+
+template <typename T>
+struct ClusterPanel {
+  int max_cs = 0;  // largest launchable cluster size (0: unavailable)
+  int lmax = 0;
+};
+
+template <typename T>
+const ClusterPanel<T> &cluster_panel_caps() {
+  static ClusterPanel<T> caps;
+  static bool done = false;
+  if (done) return caps;
+  done = true;
+  const int lmax = sizeof(T) == 4 ? 3 : 1;
+  const size_t smem = cpanel_smem_bytes<T>(lmax);
+  if (cudaFuncSetAttribute(getf2_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)smem) != cudaSuccess ||
+      cudaFuncSetAttribute(getf2_cluster_kernel<T>,
+                           cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+    cudaGetLastError();
+    return caps;
+  }
+  for (int cs = 16; cs >= 2; cs /= 2) {
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(cs);
+    cfg.blockDim = dim3(CPANEL_THREADS);
+    cfg.dynamicSmemBytes = smem;
+    cudaLaunchAttribute at[1];
+    at[0].id = cudaLaunchAttributeClusterDimension;
+    at[0].val.clusterDim.x = cs;
+    at[0].val.clusterDim.y = 1;
+    at[0].val.clusterDim.z = 1;
+    cfg.attrs = at;
+    cfg.numAttrs = 1;
+    int nclusters = 0;
+    if (cudaOccupancyMaxActiveClusters(&nclusters, getf2_cluster_kernel<T>, &cfg) ==
+            cudaSuccess &&
+        nclusters >= 1) {
+      caps.max_cs = cs;
+      caps.lmax = lmax;
+      break;
+    }
+    cudaGetLastError();
+  }
+  if (config().verbose)
+    fprintf(stderr, "libgbblas: cluster panel (%s): max cluster %d CTAs, %d rows/thread\n",
+            sizeof(T) == 4 ? "fp32" : "fp64", caps.max_cs, caps.lmax);
+  return caps;
+}
+
+// Launch the cluster panel when the panel fits one cluster; returns 1 when
+// it does not (the caller then uses the grid-wide kernel).
+template <typename T>
+int launch_cluster_panel(int64_t rows, int nb, T *A, int64_t lda, int *ipiv, int64_t row_off,
+                         int *info, cudaStream_t s) {
+  const ClusterPanel<T> &caps = cluster_panel_caps<T>();
+  if (caps.max_cs < 2) return 1;
+  int64_t cs = (rows + CPANEL_THREADS - 1) / CPANEL_THREADS;
+  if (cs < 2) cs = 2;
+  if (cs > caps.max_cs) cs = caps.max_cs;
+  const int64_t L = (rows + cs * CPANEL_THREADS - 1) / (cs * CPANEL_THREADS);
+  if (L > caps.lmax) return 1;
+  // cluster sizes must divide the grid; use a power of two
+  int csp = 2;
+  while (csp < cs) csp *= 2;
+  if (csp > caps.max_cs) return 1;
+  cudaLaunchConfig_t cfg = {};
+  cfg.gridDim = dim3((unsigned)csp);
+  cfg.blockDim = dim3(CPANEL_THREADS);
+  cfg.dynamicSmemBytes = cpanel_smem_bytes<T>((int)L);
+  cfg.stream = s;
+  cudaLaunchAttribute at[1];
+  at[0].id = cudaLaunchAttributeClusterDimension;
+  at[0].val.clusterDim.x = (unsigned)csp;
+  at[0].val.clusterDim.y = 1;
+  at[0].val.clusterDim.z = 1;
+  cfg.attrs = at;
+  cfg.numAttrs = 1;
+  count_launch();
+  return check_cuda(cudaLaunchKernelEx(&cfg, getf2_cluster_kernel<T>, rows, nb, A, lda, ipiv,
+                                       row_off, info, (int)L),
+                    "cluster panel launch");
+}
+
 template <typename T, int R>
 int launch_panel(int64_t rows, int nb, T *A, int64_t lda, int *ipiv, int64_t row_off, int *info,
                  T *slots, unsigned *bar, int *status, unsigned nblocks, cudaStream_t s) {
@@ -423,6 +697,105 @@ int trsm_any<float>(int side, int uplo, int trans, int unit, int64_t m, int64_t 
 
 }  // namespace
 
+// Parallel form of a long interchange sequence (incx = 1): one block replays
+// the interchanges on an index vector in shared memory, giving the final
+// permutation of the touched rows, and the moved rows are then gathered and
+// scattered by all SMs.  The per-column sequential kernel above costs one
+// memory round trip per interchange; this form costs one for the whole
+// sequence.  rows = number of rows of the matrix (pivots are < rows).
+__global__ void __launch_bounds__(1024)
+laswp_plan_kernel(int64_t k1, int64_t k2, const int *__restrict__ ipiv, int64_t range,
+                  int *__restrict__ dst, int *__restrict__ src, int *__restrict__ count) {
+  extern __shared__ int pos[];
+  for (int64_t p = threadIdx.x; p < range; p += blockDim.x) pos[p] = (int)p;
+  if (threadIdx.x == 0) *count = 0;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    const int64_t base = k1 - 1;
+    for (int64_t i = k1 - 1; i < k2; ++i) {
+      const int64_t li = i - base, lp = (int64_t)ipiv[i] - 1 - base;
+      if (lp != li) {
+        const int t = pos[li];
+        pos[li] = pos[lp];
+        pos[lp] = t;
+      }
+    }
+  }
+  __syncthreads();
+  for (int64_t p = threadIdx.x; p < range; p += blockDim.x) {
+    if (pos[p] != (int)p) {
+      const int slot = atomicAdd(count, 1);
+      dst[slot] = (int)(p + k1 - 1);
+      src[slot] = pos[p] + (int)(k1 - 1);
+    }
+  }
+}
+
+template <typename T>
+__global__ void laswp_gather_kernel(int64_t ncols, const T *__restrict__ A, int64_t lda,
+                                    const int *__restrict__ src, const int *__restrict__ count,
+                                    int64_t cap, T *__restrict__ tmp) {
+  const int64_t nm = *count;
+  const int64_t total = nm * ncols;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = e / nm, t = e - c * nm;
+    tmp[t + c * cap] = A[src[t] + c * lda];
+  }
+}
+
+template <typename T>
+__global__ void laswp_scatter_kernel(int64_t ncols, T *__restrict__ A, int64_t lda,
+                                     const int *__restrict__ dst, const int *__restrict__ count,
+                                     int64_t cap, const T *__restrict__ tmp) {
+  const int64_t nm = *count;
+  const int64_t total = nm * ncols;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = e / nm, t = e - c * nm;
+    A[dst[t] + c * lda] = tmp[t + c * cap];
+  }
+}
+
+constexpr int64_t LASWP_SEQ_MAX = 64;          // short sequences: per-column kernel
+constexpr int64_t LASWP_PLAN_SMEM_ROWS = 50000;  // index vector must fit in shared memory
+
+template <typename T>
+int laswp_device_rows(int64_t n, T *A, int64_t lda, int64_t k1, int64_t k2, const int *ipiv,
+                      int64_t incx, int64_t rows, cudaStream_t s) {
+  if (n <= 0 || incx == 0 || k2 < k1) return GB_SUCCESS;
+  const int64_t cnt = k2 - k1 + 1;
+  const int64_t range = rows - (k1 - 1);
+  if (incx != 1 || cnt <= LASWP_SEQ_MAX || rows <= 0 || range > LASWP_PLAN_SMEM_ROWS ||
+      n < 4) {
+    { laswp_kernel<T><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(n, A, lda, k1, k2, ipiv, incx); count_launch(); }
+    return check_cuda(cudaGetLastError(), "laswp launch");
+  }
+  const int64_t cap = 2 * cnt < range ? 2 * cnt : range;  // at most 2 rows move per interchange
+  Scratch ws((size_t)(2 * cap + 32) * sizeof(int) + (size_t)cap * n * sizeof(T) + 512, s);
+  if (!ws.p) return GB_ERR_ALLOC;
+  int *dst = ws.as<int>();
+  int *src = dst + cap;
+  int *count = src + cap;
+  T *tmp = reinterpret_cast<T *>(reinterpret_cast<char *>(ws.p) +
+                                 (((2 * cap + 32) * sizeof(int) + 255) & ~size_t(255)));
+  const size_t smem = (size_t)range * sizeof(int);
+  static bool attr = false;
+  if (!attr) {
+    cudaFuncSetAttribute(laswp_plan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(LASWP_PLAN_SMEM_ROWS * sizeof(int)));
+    attr = true;
+  }
+  { laswp_plan_kernel<<<1, 1024, smem, s>>>(k1, k2, ipiv, range, dst, src, count); count_launch(); }
+  const int64_t total = cap * n;
+  int64_t blocks = (total + 255) / 256;
+  const int64_t lim = (int64_t)sm_count() * 16;
+  const unsigned g = (unsigned)(blocks < lim ? blocks : lim);
+  { laswp_gather_kernel<T><<<g, 256, 0, s>>>(n, A, lda, src, count, cap, tmp); count_launch(); }
+  { laswp_scatter_kernel<T><<<g, 256, 0, s>>>(n, A, lda, dst, count, cap, tmp); count_launch(); }
+  return check_cuda(cudaGetLastError(), "laswp (planned)");
+}
+
 template <typename T>
 int laswp_device(int64_t n, T *A, int64_t lda, int64_t k1, int64_t k2, const int *ipiv,
                  int64_t incx, cudaStream_t s) {
@@ -450,6 +823,8 @@ struct LuCtx {
   int *status;
   int lim1, lim2;
   int gemm_mode;  // double only: 0 native FP64 updates, 1 emulated-FP64 updates
+  int64_t rows;   // rows of the whole matrix (interchange targets are below it)
+  bool use_cluster = true;  // panel on one thread-block cluster when it fits
   cudaStream_t s;
 };
 
@@ -476,8 +851,13 @@ int lu_update<float>(LuCtx<float> &c, int64_t m, int64_t n, int64_t k, const flo
 
 template <typename T>
 int lu_panel(LuCtx<T> &c, int64_t r0, int64_t m, int n) {
-  GB_CUDA(cudaMemsetAsync(c.bar, 0, 2 * sizeof(unsigned), c.s));
+  ProfileScope prof("lu_panel", c.s);
   T *P = c.A + r0 + r0 * c.lda;
+  if (c.use_cluster) {
+    const int st = launch_cluster_panel<T>(m, n, P, c.lda, c.ipiv + r0, r0, c.info, c.s);
+    if (st != 1) return st;
+  }
+  GB_CUDA(cudaMemsetAsync(c.bar, 0, 2 * sizeof(unsigned), c.s));
   const int64_t b1 = (m + PANEL_THREADS - 1) / PANEL_THREADS;
   const int64_t b2 = (m + 2 * PANEL_THREADS - 1) / (2 * PANEL_THREADS);
   if (b1 <= c.lim1)
@@ -501,16 +881,68 @@ int lu_rec(LuCtx<T> &c, int64_t r0, int64_t m, int64_t n) {
   if ((st = lu_rec<T>(c, r0, m, n1))) return st;
   T *L11 = c.A + r0 + r0 * lda;
   T *A12 = c.A + r0 + (r0 + n1) * lda;
-  if ((st = laswp_device<T>(n - n1, c.A + (r0 + n1) * lda, lda, r0 + 1, r0 + n1, c.ipiv, 1,
-                            c.s)))
-    return st;
-  if ((st = trsm_any<T>(0, 1, 0, 0, n1, n - n1, L11, lda, A12, lda, c.s))) return st;
+  {
+    ProfileScope prof("lu_laswp", c.s);
+    if ((st = laswp_device_rows<T>(n - n1, c.A + (r0 + n1) * lda, lda, r0 + 1, r0 + n1, c.ipiv,
+                                   1, c.rows, c.s)))
+      return st;
+  }
+  {
+    ProfileScope prof("lu_trsm", c.s);
+    if ((st = trsm_any<T>(0, 1, 0, 0, n1, n - n1, L11, lda, A12, lda, c.s))) return st;
+  }
   if (m > n1) {
-    if ((st = lu_update<T>(c, m - n1, n - n1, n1, L11 + n1, A12, A12 + n1))) return st;
+    {
+      ProfileScope prof("lu_gemm", c.s);
+      if ((st = lu_update<T>(c, m - n1, n - n1, n1, L11 + n1, A12, A12 + n1))) return st;
+    }
     if ((st = lu_rec<T>(c, r0 + n1, m - n1, n - n1))) return st;
     const int64_t kend = r0 + (m < n ? m : n);
-    if ((st = laswp_device<T>(n1, c.A + r0 * lda, lda, r0 + n1 + 1, kend, c.ipiv, 1, c.s)))
+    ProfileScope prof("lu_laswp", c.s);
+    if ((st = laswp_device_rows<T>(n1, c.A + r0 * lda, lda, r0 + n1 + 1, kend, c.ipiv, 1, c.rows,
+                                   c.s)))
       return st;
+  }
+  return GB_SUCCESS;
+}
+
+// Outer right-looking loop over LU_OUTER_NB-wide block columns, each block
+// factored recursively -- the structure of getrf_single.c:80-177 (blocking =
+// min(mn/2, GEMM_Q), recursive call on the panel, LASWP + TRSM + GEMM on the
+// trailing columns, later interchanges applied to the columns on the left).
+constexpr int64_t LU_OUTER_NB = 256;
+
+template <typename T>
+int lu_blocked(LuCtx<T> &c, int64_t m, int64_t mn, int64_t n) {
+  const int64_t lda = c.lda;
+  int st;
+  for (int64_t j0 = 0; j0 < mn; j0 += LU_OUTER_NB) {
+    const int64_t jb = (mn - j0) < LU_OUTER_NB ? (mn - j0) : LU_OUTER_NB;
+    if ((st = lu_rec<T>(c, j0, m - j0, jb))) return st;
+    T *L11 = c.A + j0 + j0 * lda;
+    if (j0 + jb < n) {
+      T *A12 = c.A + j0 + (j0 + jb) * lda;
+      {
+        ProfileScope prof("lu_laswp", c.s);
+        if ((st = laswp_device_rows<T>(n - j0 - jb, c.A + (j0 + jb) * lda, lda, j0 + 1, j0 + jb,
+                                       c.ipiv, 1, c.rows, c.s)))
+          return st;
+      }
+      {
+        ProfileScope prof("lu_trsm", c.s);
+        if ((st = trsm_any<T>(0, 1, 0, 0, jb, n - j0 - jb, L11, lda, A12, lda, c.s))) return st;
+      }
+      if (j0 + jb < m) {
+        ProfileScope prof("lu_gemm", c.s);
+        if ((st = lu_update<T>(c, m - j0 - jb, n - j0 - jb, jb, L11 + jb, A12, A12 + jb)))
+          return st;
+      }
+    }
+    if (j0 > 0) {
+      ProfileScope prof("lu_laswp", c.s);
+      if ((st = laswp_device_rows<T>(j0, c.A, lda, j0 + 1, j0 + jb, c.ipiv, 1, c.rows, c.s)))
+        return st;
+    }
   }
   return GB_SUCCESS;
 }
@@ -537,15 +969,11 @@ int getrf_device_mode(int64_t m, int64_t n, T *A, int64_t lda, int *ipiv, int *i
                                        ((slot_elems * sizeof(T) + 127) & ~size_t(127)));
   c.status = ctx().d_status;
   c.gemm_mode = gemm_mode;
+  c.rows = m;
   c.s = s;
-  int st = lu_rec<T>(c, 0, m, mn);
+  // the outer loop already covers the columns right of the square part
+  int st = lu_blocked<T>(c, m, mn, n);
   if (st) return st;
-  if (n > mn) {
-    // wide matrix: the remaining columns get the interchanges and L11^-1
-    T *R = A + mn * lda;
-    if ((st = laswp_device<T>(n - mn, R, lda, 1, mn, ipiv, 1, s))) return st;
-    if ((st = trsm_any<T>(0, 1, 0, 0, mn, n - mn, A, lda, R, lda, s))) return st;
-  }
   return check_cuda(cudaGetLastError(), "getrf");
 }
 
@@ -646,16 +1074,12 @@ extern "C" int gb_dgetrf_noalloc_dev(int64_t m, int64_t n, double *A, int64_t ld
   c.bar = reinterpret_cast<unsigned *>(b + ((NOALLOC_SLOT_BYTES + 127) & ~size_t(127)));
   c.status = reinterpret_cast<int *>(c.bar + 32);
   c.gemm_mode = 0;  // native FP64 trailing updates: no scratch anywhere below
+  c.rows = 0;       // 0 selects the per-column interchange kernel, which needs no scratch
   c.s = s;
   // the shared array keeps the previous call's contents: clear the words that
   // must start at zero (barrier counters are cleared again before every panel)
   GB_CUDA(cudaMemsetAsync(c.bar, 0, 32 * sizeof(unsigned) + 4 * sizeof(int), s));
-  if ((st = lu_rec<double>(c, 0, m, mn))) return st;
-  if (n > mn) {
-    double *R = A + mn * lda;
-    if ((st = laswp_device<double>(n - mn, R, lda, 1, mn, ipiv, 1, s))) return st;
-    if ((st = trsm_any<double>(0, 1, 0, 0, mn, n - mn, A, lda, R, lda, s))) return st;
-  }
+  if ((st = lu_blocked<double>(c, m, mn, n))) return st;
   return check_cuda(cudaGetLastError(), "gb_dgetrf_noalloc_dev");
 }
 
@@ -720,6 +1144,24 @@ int potrf_device(int uplo, int64_t n, double *A, int64_t lda, int *info, cudaStr
   }
   return check_cuda(cudaGetLastError(), "potrf");
 }
+
+int pivots_to_perm(int64_t n, const int *ipiv, int *perm, cudaStream_t s) {
+  { pivots_to_perm_kernel<<<1, 1, 0, s>>>(n, ipiv, perm); count_launch(); }
+  return check_cuda(cudaGetLastError(), "pivots_to_perm");
+}
+
+template <typename T>
+int apply_perm(int64_t n, int64_t ncol, const int *perm, const T *src, int64_t lds, T *dst,
+               int64_t ldd, cudaStream_t s) {
+  const int64_t total = n * ncol;
+  const unsigned grid = (unsigned)((total + 255) / 256 < 4096 ? (total + 255) / 256 : 4096);
+  { permute_rows_kernel<T><<<grid, 256, 0, s>>>(n, ncol, perm, src, lds, dst, ldd, 0); count_launch(); }
+  return check_cuda(cudaGetLastError(), "apply_perm");
+}
+template int apply_perm<float>(int64_t, int64_t, const int *, const float *, int64_t, float *,
+                               int64_t, cudaStream_t);
+template int apply_perm<double>(int64_t, int64_t, const int *, const double *, int64_t,
+                                double *, int64_t, cudaStream_t);
 
 template int getrf_device<double>(int64_t, int64_t, double *, int64_t, int *, int *,
                                   cudaStream_t);

@@ -22,6 +22,7 @@
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
+#include <stdlib.h>
 #include <string.h>
 
 #include <vector>
@@ -31,6 +32,10 @@
 #include "operand.h"
 
 namespace gb {
+
+int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
+                   const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
+                   double *C, int64_t ldc, int slices, cudaStream_t s);
 
 namespace {
 
@@ -222,9 +227,24 @@ struct Mixed {
   int *dflag = nullptr;
   Host *hx = nullptr;       // pinned host scratch
   double *LU64 = nullptr;   // FP64 copy of the FP32 factors (GMRES-IR stage)
+  float *SX2 = nullptr;     // n x nrhs FP32 work (permuted right-hand sides)
+  int *perm = nullptr;      // final row permutation of the FP32 LU
+  float *Linv = nullptr, *Uinv = nullptr;  // inverted 64x64 diagonal blocks of L, U
+
+  // X32 = (LU)^-1 P * X32 (in place through SX2): the FP32 solve of the refinement
+  int solve32(float *V, int64_t k) {
+    static const bool trsm_solve = getenv("GB_MIXED_SOLVE") && !strcmp(getenv("GB_MIXED_SOLVE"), "trsm");
+    if (trsm_solve) return getrs_device<float>(0, n, k, SA, n, ipiv, V, n, s);
+    int st = apply_perm<float>(n, k, perm, V, n, SX2, n, s);
+    if (st) return st;
+    if ((st = lu_block_solve<float>(n, k, SA, n, Linv, Uinv, SX2, n, s))) return st;
+    GB_CUDA(cudaMemcpyAsync(V, SX2, (size_t)n * k * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    return GB_SUCCESS;
+  }
 
   // R = B - A X (FP64)
   int residual() {
+    ProfileScope prof("mixed_residual", s);
     if (nrhs <= 8) {
       for (int64_t j = 0; j < nrhs; ++j) {
         dim3 g((unsigned)((n + 255) / 256), (unsigned)nchunks);
@@ -232,8 +252,11 @@ struct Mixed {
         { gemv_combine_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, nchunks, part, -1.0, B + j * ldb, 1.0, R + j * n); count_launch(); }
       }
     } else {
+      // many right-hand sides: the product runs on the emulated-FP64 GEMM, whose
+      // error (a few eps * |A||X|) is the same scale as a native FP64 product's
       GB_CUDA(cudaMemcpy2DAsync(R, n * 8, B, ldb * 8, n * 8, nrhs, cudaMemcpyDeviceToDevice, s));
-      launch_dgemm_fp64(0, 0, n, nrhs, n, -1.0, A, lda, X, ldx, 1.0, R, n, s);
+      int st = dgemm_emulated(0, 0, n, nrhs, n, -1.0, A, lda, X, ldx, 1.0, R, n, 0, s);
+      if (st) return st;
     }
     return check_cuda(cudaGetLastError(), "residual");
   }
@@ -263,7 +286,11 @@ struct Mixed {
   int precond(double *V, int64_t ldv, int64_t k, bool *overflow) {
     GB_CUDA(cudaMemsetAsync(dflag, 0, sizeof(int), s));
     { lag2s_kernel<<<grid_for(n * k), 256, 0, s>>>(n, k, V, ldv, SX, n, dflag); count_launch(); }
-    int st = getrs_device<float>(0, n, k, SA, n, ipiv, SX, n, s);
+    int st;
+    {
+      ProfileScope prof("mixed_getrs", s);
+      st = solve32(SX, k);
+    }
     if (st) return st;
     { lag2d_kernel<<<grid_for(n * k), 256, 0, s>>>(n, k, SX, n, V, ldv, 0); count_launch(); }
     int h = 0;
@@ -400,6 +427,15 @@ int dsgesv_device(int64_t n, int64_t nrhs, double *A, int64_t lda, int *ipiv, co
   const size_t bytes_sx = ((size_t)n * nrhs * 4 + 255) & ~size_t(255);
   const size_t bytes_r = ((size_t)n * nrhs * 8 + 255) & ~size_t(255);
   const size_t bytes_p = ((size_t)n * (M.nchunks > 64 ? M.nchunks : 64) * 8 + 255) & ~size_t(255);
+  const int64_t nblk64 = (n + 63) / 64;
+  const size_t bytes_inv = ((size_t)nblk64 * 64 * 64 * 4 + 255) & ~size_t(255);
+  const size_t bytes_perm = ((size_t)n * 4 + 255) & ~size_t(255);
+  Scratch ws2(bytes_sx + 2 * bytes_inv + bytes_perm, s);
+  if (!ws2.p) return GB_ERR_ALLOC;
+  M.SX2 = ws2.as<float>();
+  M.Linv = reinterpret_cast<float *>(ws2.as<char>() + bytes_sx);
+  M.Uinv = reinterpret_cast<float *>(ws2.as<char>() + bytes_sx + bytes_inv);
+  M.perm = reinterpret_cast<int *>(ws2.as<char>() + bytes_sx + 2 * bytes_inv);
   Scratch ws(bytes_sa + bytes_sx + bytes_r + bytes_p + 1024 + (size_t)nrhs * 32, s);
   if (!ws.p) return GB_ERR_ALLOC;
   char *base = ws.as<char>();
@@ -442,7 +478,10 @@ int dsgesv_device(int64_t n, int64_t nrhs, double *A, int64_t lda, int *ipiv, co
   }
   if (!fallback) {
     // sgetrf (dsgesv.f:310): a singular FP32 factor sends the solve to FP64
-    if ((st = getrf_device<float>(n, n, M.SA, n, ipiv, dinfo, s))) return st;
+    {
+      ProfileScope prof("mixed_sgetrf", s);
+      if ((st = getrf_device<float>(n, n, M.SA, n, ipiv, dinfo, s))) return st;
+    }
     GB_CUDA(cudaMemcpyAsync(hx.p, dinfo, sizeof(int), cudaMemcpyDeviceToHost, s));
     if ((st = finish_blocking(s))) return st;
     int sinfo;
@@ -453,7 +492,13 @@ int dsgesv_device(int64_t n, int64_t nrhs, double *A, int64_t lda, int *ipiv, co
     }
   }
   if (!fallback) {
-    if ((st = getrs_device<float>(0, n, nrhs, M.SA, n, ipiv, M.SX, n, s))) return st;
+    // once per factorisation: the final permutation and the inverted diagonal blocks
+    if ((st = pivots_to_perm(n, ipiv, M.perm, s))) return st;
+    if ((st = lu_block_inverses<float>(n, M.SA, n, M.Linv, M.Uinv, s))) return st;
+    {
+      ProfileScope prof("mixed_getrs", s);
+      if ((st = M.solve32(M.SX, nrhs))) return st;
+    }
     { lag2d_kernel<<<grid_for(n * nrhs), 256, 0, s>>>(n, nrhs, M.SX, n, X, ldx, 0); count_launch(); }
     double prev = INFINITY, best = INFINITY;
     int stalls = 0;
