@@ -229,6 +229,59 @@ def cpu_baseline_sample():
                       f"of the reference's GEMM with OpenMP over {cores} host threads"}
 
 
+def dgesv_compare(lib, torch, gb, world, n=8192, nrhs=1, reps=3):
+    g = torch.Generator(device="cuda")
+    g.manual_seed(77)
+    A = torch.rand((n, n), dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    B = torch.rand((nrhs, n), dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    X = torch.zeros_like(B)
+    ipiv = torch.zeros(n, dtype=torch.int32, device="cuda")
+    it, info = C.c_int(0), C.c_int(0)
+
+    def mixed():
+        st = lib.gb_dsgesv_dev(n, nrhs, A.data_ptr(), n, ipiv.data_ptr(), B.data_ptr(), n,
+                               X.data_ptr(), n, C.byref(it), C.byref(info))
+        if st != 0:
+            raise RuntimeError(gb.last_error(lib))
+
+    mixed()
+    torch.cuda.synchronize()
+    times = []
+    for _ in range(reps):
+        t0 = time.perf_counter()
+        mixed()
+        torch.cuda.synchronize()
+        times.append(time.perf_counter() - t0)
+    t_mixed = allreduce_max(statistics.median(times), world)
+    # backward error ||b - A x||_inf / (||A||_inf ||x||_inf + ||b||_inf), FP64 on the GPU
+    R = B.clone()
+    lib.gb_dgemm_native_dev(b"N", b"N", n, nrhs, n, -1.0, A.data_ptr(), n, X.data_ptr(), n, 1.0,
+                            R.data_ptr(), n)
+    torch.cuda.synchronize()
+    anorm = float(A.abs().sum(dim=0).max())  # rows of A are columns of the torch tensor
+    berr = float(R.abs().max() / (anorm * X.abs().max() + B.abs().max()))
+    iters = it.value
+    # native FP64 getrf + getrs (one timed call, ~0.4 s)
+    Af = torch.empty_like(A)
+    Xn = torch.empty_like(B)
+    dinfo = torch.zeros(1, dtype=torch.int32, device="cuda")
+    Af.copy_(A)
+    Xn.copy_(B)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lib.gb_dgetrf_dev(n, n, Af.data_ptr(), n, ipiv.data_ptr(), dinfo.data_ptr())
+    lib.gb_dgetrs_dev(b"N", n, nrhs, Af.data_ptr(), n, ipiv.data_ptr(), Xn.data_ptr(), n)
+    torch.cuda.synchronize()
+    t_native = allreduce_max(time.perf_counter() - t0, world)
+    flops = 2.0 / 3.0 * n ** 3 + 2.0 * n * n * nrhs
+    return {"workload": f"DGESV N={n} NRHS={nrhs}, A,B uniform(-1,1) seeded", "unit": UNIT,
+            "mixed": {"value": world * flops / t_mixed / 1e12, "ms": t_mixed * 1e3,
+                      "iter": iters, "backward_error_eps": berr / 2.220446049250313e-16,
+                      "bound_n_eps": n},
+            "native_fp64": {"value": world * flops / t_native / 1e12, "ms": t_native * 1e3},
+            "speedup_mixed_over_native": t_native / t_mixed}
+
+
 # --------------------------------------------------------------------------
 # main arm
 # --------------------------------------------------------------------------
@@ -347,6 +400,10 @@ def main():
     if st not in (0,):
         raise RuntimeError(msg)
 
+    # DGESV N=8192, NRHS=1: mixed precision (FP32 LU on the GPU + FP64
+    # refinement) against native FP64 getrf+getrs, both on the same operands
+    dgesv = dgesv_compare(lib, torch, gb, world)
+
     peaks, src = measured_peaks()
     slice_flops = S * (S + 1) / 2 * flops
     achieved = slice_flops / (kern_ms * 1e-3) / 1e12
@@ -371,6 +428,7 @@ def main():
                      "peak_source": f"{src} bf16_tflops_sustained",
                      "kernel_ms_per_launch": kern_ms,
                      "algorithmic_flops_per_launch": slice_flops},
+        "dgesv": dgesv,
         "gpu_launches": int(launches),
         "clocks": clk,
     }

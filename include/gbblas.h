@@ -222,6 +222,41 @@ int gb_sgetrs_dev(char trans, int64_t n, int64_t nrhs, const float *A,
 int gb_dlaswp_dev(int64_t n, double *A, int64_t lda, int64_t k1, int64_t k2,
                   const int *ipiv, int64_t incx);
 int gb_dpotrf_dev(char uplo, int64_t n, double *A, int64_t lda, int *info);
+/* Grouped batches of small, uneven problems in one persistent launch (the
+ * reference's cblas_dgemm_batch, interface/gemm_batch.c, extended to LU solves
+ * and Cholesky).  All pointers are device pointers.  type selects:
+ *   GB_BATCH_DGEMM : C = alpha*op(A)*op(B) + beta*C (m, n, k, transa/transb)
+ *   GB_BATCH_DGESV : A (n x n) overwritten by its LU, B (n x k right-hand
+ *                    sides) by the solution, C = int ipiv[n], *info
+ *   GB_BATCH_DPOTRF: Cholesky of A (n x n, uplo 'L'/'U'), *info
+ * A plan uploads the table, orders it by cost and captures the launch in a
+ * CUDA graph; gb_batch_execute replays it on the thread's stream.
+ * GB_BATCH_MIXED solves the DGESV problems with an FP32 LU and FP64
+ * refinement (FP64 fallback per problem).  gb_batch_plan_tune times the
+ * candidate CTA sizes on the batch itself (it executes the batch, so inputs
+ * must be re-initialised afterwards) and caches the winner for batches with
+ * the same size histogram.  gb_batch_execute_loop runs the same per-problem
+ * code with one launch per problem (the comparison baseline). */
+#define GB_BATCH_DGEMM 0
+#define GB_BATCH_DGESV 1
+#define GB_BATCH_DPOTRF 2
+#define GB_BATCH_MIXED 1
+typedef struct gb_batch_problem {
+  int type;
+  int m, n, k;
+  char transa, transb, uplo, pad;
+  double alpha, beta;
+  void *A, *B, *C;
+  int lda, ldb, ldc;
+  int *info;
+} gb_batch_problem;
+void *gb_batch_plan_create(const gb_batch_problem *problems, int count, int flags);
+int gb_batch_plan_tune(void *plan);
+int gb_batch_plan_threads(void *plan);
+int gb_batch_execute(void *plan);
+int gb_batch_execute_loop(void *plan);
+void gb_batch_plan_destroy(void *plan);
+
 /* LU with partial pivoting that allocates no device memory.  This entry has
  * no counterpart in the reference.  It exists for callers that cannot let a
  * library allocate: applications that hand all of HBM to their own arena and

@@ -1,0 +1,850 @@
+// Grouped batches of small uneven problems in one persistent launch.
+//
+// The reference runs cblas_dgemm_batch (interface/gemm_batch.c:117-372,
+// driver/level3/gemm_batch_thread.c:79-156) by looping over the problems or
+// handing chunks of them to its threads; it has no batched LU/Cholesky.  Here
+// a device-side problem table (DGEMM, DGESV = DGETRF+DGETRS, DPOTRF) is
+// processed by one persistent kernel: every CTA takes the next problem from
+// an atomic counter over a list sorted by decreasing cost, so uneven sizes
+// balance across the SMs.  A plan uploads the table once, autotunes the CTA
+// size on the actual batch (the choice is cached under a key made of the
+// problem-size histogram), and captures the launch in a CUDA graph that is
+// replayed for every execution.
+//
+// Per-problem algorithms (one CTA each, operands in global memory where they
+// stay resident in L2; FP64 throughput bounds these sizes on this part):
+//   DGEMM   C = alpha op(A) op(B) + beta C, 64x64 register-tiled CTA loop;
+//           beta == 0 overwrites C (gemm_beta.c:41-94).
+//   DGESV   right-looking LU with the getf2_k.c pivot rules (first maximum
+//           |a|, swap and reciprocal scaling only when |pivot| >= DBL_MIN,
+//           info = first zero pivot), then forward/back substitution of the
+//           right-hand sides when info == 0 (gesv.c:131-135).
+//           Mixed variant: the LU runs in FP32 on a scratch copy, the solution
+//           is refined in FP64 with the dsgesv.f stopping test; problems that
+//           do not converge in 30 steps are redone in FP64 by the same CTA.
+//   DPOTRF  right-looking Cholesky (potf2_L.c / potf2_U.c contract: info =
+//           first non-positive pivot, whose value is written back).
+#include <cuda_runtime.h>
+#include <float.h>
+#include <math.h>
+#include <stdint.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "gb_internal.h"
+#include "operand.h"
+
+namespace gb {
+
+namespace {
+
+struct DevProblem {
+  int type, m, n, k;
+  int ta, tb, uplo, pad;
+  double alpha, beta;
+  void *A, *B, *C;
+  int lda, ldb, ldc, pad2;
+  int *info;
+  float *work;  // FP32 scratch for the mixed DGESV variant (n*n + 2n floats)
+};
+
+// ---------------------------------------------------------------- DGEMM
+template <int NT>
+__device__ void cta_dgemm(const DevProblem &p) {
+  constexpr int BM = 64, BN = 64, BK = 16;
+  constexpr int TX = 16, TY = NT / 16;  // thread grid over the tile
+  constexpr int RM = BM / TX, RN = BN / TY;
+  __shared__ double As[BK][BM];
+  __shared__ double Bs[BK][BN];
+  const double *A = (const double *)p.A, *B = (const double *)p.B;
+  double *C = (double *)p.C;
+  const int m = p.m, n = p.n, k = p.k;
+  const int tid = threadIdx.x, tx = tid % TX, ty = tid / TX;
+  for (int m0 = 0; m0 < m; m0 += BM)
+    for (int n0 = 0; n0 < n; n0 += BN) {
+      double acc[RM][RN];
+#pragma unroll
+      for (int i = 0; i < RM; ++i)
+#pragma unroll
+        for (int j = 0; j < RN; ++j) acc[i][j] = 0.0;
+      if (p.alpha != 0.0)
+        for (int k0 = 0; k0 < k; k0 += BK) {
+          __syncthreads();
+          for (int e = tid; e < BM * BK; e += NT) {
+            int i, kk;
+            if (!p.ta) { i = e % BM; kk = e / BM; } else { kk = e % BK; i = e / BK; }
+            const int gi = m0 + i, gk = k0 + kk;
+            double v = 0.0;
+            if (gi < m && gk < k) v = p.ta ? A[gk + (int64_t)gi * p.lda] : A[gi + (int64_t)gk * p.lda];
+            As[kk][i] = v;
+          }
+          for (int e = tid; e < BN * BK; e += NT) {
+            int j, kk;
+            if (!p.tb) { kk = e % BK; j = e / BK; } else { j = e % BN; kk = e / BN; }
+            const int gj = n0 + j, gk = k0 + kk;
+            double v = 0.0;
+            if (gj < n && gk < k) v = p.tb ? B[gj + (int64_t)gk * p.ldb] : B[gk + (int64_t)gj * p.ldb];
+            Bs[kk][j] = v;
+          }
+          __syncthreads();
+#pragma unroll
+          for (int kk = 0; kk < BK; ++kk) {
+            double a[RM], b[RN];
+#pragma unroll
+            for (int i = 0; i < RM; ++i) a[i] = As[kk][tx + i * TX];
+#pragma unroll
+            for (int j = 0; j < RN; ++j) b[j] = Bs[kk][ty + j * TY];
+#pragma unroll
+            for (int i = 0; i < RM; ++i)
+#pragma unroll
+              for (int j = 0; j < RN; ++j) acc[i][j] = fma(a[i], b[j], acc[i][j]);
+          }
+        }
+#pragma unroll
+      for (int j = 0; j < RN; ++j) {
+        const int gj = n0 + ty + j * TY;
+        if (gj >= n) continue;
+#pragma unroll
+        for (int i = 0; i < RM; ++i) {
+          const int gi = m0 + tx + i * TX;
+          if (gi >= m) continue;
+          double *c = C + gi + (int64_t)gj * p.ldc;
+          double v = p.alpha * acc[i][j];
+          *c = (p.beta == 0.0) ? v : fma(p.beta, *c, v);
+        }
+      }
+    }
+}
+
+// ---------------------------------------------------------------- reductions
+template <typename T, int NT>
+__device__ void cta_argmax(T val, int idx, T *sv, int *si, T *bv, int *bi) {
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    T ov = __shfl_down_sync(0xffffffffu, val, off);
+    int oi = __shfl_down_sync(0xffffffffu, idx, off);
+    if (ov > val || (ov == val && oi < idx)) {
+      val = ov;
+      idx = oi;
+    }
+  }
+  if (lane == 0) {
+    sv[warp] = val;
+    si[warp] = idx;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    T v = sv[0];
+    int i = si[0];
+    for (int w = 1; w < NT / 32; ++w)
+      if (sv[w] > v || (sv[w] == v && si[w] < i)) {
+        v = sv[w];
+        i = si[w];
+      }
+    *bv = v;
+    *bi = i;
+  }
+  __syncthreads();
+}
+
+// ---------------------------------------------------------------- LU (one CTA)
+// Right-looking LU of an n x n matrix at M (leading dimension ld) with the
+// getf2_k.c rules.  ipiv 1-based.  Returns info.
+template <typename T, int NT>
+__device__ int cta_getrf(int n, T *M, int ld, int *ipiv) {
+  __shared__ T sv[NT / 32];
+  __shared__ int si[NT / 32];
+  __shared__ T s_piv;
+  __shared__ int s_p;
+  const T tiny = sizeof(T) == 8 ? (T)DBL_MIN : (T)FLT_MIN;
+  int info = 0;
+  for (int j = 0; j < n; ++j) {
+    T best = T(-1);
+    int bidx = 1 << 30;
+    for (int i = j + threadIdx.x; i < n; i += NT) {
+      T a = M[i + (int64_t)j * ld];
+      a = a < T(0) ? -a : a;
+      if (a > best) {  // rows visited in increasing order: first maximum per thread
+        best = a;
+        bidx = i;
+      }
+    }
+    cta_argmax<T, NT>(best, bidx, sv, si, &s_piv, &s_p);
+    const int p = s_p;
+    const T piv = M[p + (int64_t)j * ld];
+    __syncthreads();  // every thread has the pivot before any row moves
+    const T apiv = piv < T(0) ? -piv : piv;
+    const bool nonzero = piv != T(0);
+    const bool scaled = nonzero && apiv >= tiny;
+    if (threadIdx.x == 0) ipiv[j] = p + 1;
+    if (!nonzero && info == 0) info = j + 1;
+    // interchange rows j and p: all columns when scaled, columns > j otherwise
+    if (p != j)
+      for (int c = threadIdx.x; c < n; c += NT)
+        if (scaled || c > j) {
+          T t = M[j + (int64_t)c * ld];
+          M[j + (int64_t)c * ld] = M[p + (int64_t)c * ld];
+          M[p + (int64_t)c * ld] = t;
+        }
+    __syncthreads();
+    if (scaled) {
+      const T r = T(1) / piv;
+      for (int i = j + 1 + threadIdx.x; i < n; i += NT) M[i + (int64_t)j * ld] *= r;
+    }
+    __syncthreads();
+    const int rows = n - j - 1;
+    const int64_t total = (int64_t)rows * rows;
+    for (int64_t e = threadIdx.x; e < total; e += NT) {
+      const int i = j + 1 + (int)(e % rows), c = j + 1 + (int)(e / rows);
+      M[i + (int64_t)c * ld] = fma(-M[i + (int64_t)j * ld], M[j + (int64_t)c * ld],
+                                   M[i + (int64_t)c * ld]);
+    }
+    __syncthreads();
+  }
+  return info;
+}
+
+// Solve (LU) X = P B for nrhs columns (B overwritten), forward/back substitution.
+template <typename TM, typename TB_, int NT>
+__device__ void cta_getrs(int n, int nrhs, const TM *LU, int ld, const int *ipiv, TB_ *B,
+                          int ldb) {
+  for (int r = 0; r < nrhs; ++r) {
+    TB_ *b = B + (int64_t)r * ldb;
+    if (threadIdx.x == 0)
+      for (int i = 0; i < n; ++i) {
+        const int p = ipiv[i] - 1;
+        if (p != i) {
+          TB_ t = b[i];
+          b[i] = b[p];
+          b[p] = t;
+        }
+      }
+    __syncthreads();
+    for (int j = 0; j < n; ++j) {  // L y = b (unit diagonal)
+      const TB_ xj = b[j];
+      for (int i = j + 1 + threadIdx.x; i < n; i += NT)
+        b[i] = fma(-(TB_)LU[i + (int64_t)j * ld], xj, b[i]);
+      __syncthreads();
+    }
+    for (int j = n - 1; j >= 0; --j) {  // U x = y
+      if (threadIdx.x == 0) b[j] = b[j] / (TB_)LU[j + (int64_t)j * ld];
+      __syncthreads();
+      const TB_ xj = b[j];
+      for (int i = threadIdx.x; i < j; i += NT) b[i] = fma(-(TB_)LU[i + (int64_t)j * ld], xj, b[i]);
+      __syncthreads();
+    }
+  }
+}
+
+// ---------------------------------------------------------------- POTRF
+template <int NT>
+__device__ int cta_potrf(int n, double *M, int ld, bool upper) {
+  __shared__ double s_d;
+  __shared__ int s_fail;
+  auto at = [&](int i, int c) -> double & {  // element (i, c) of the lower view
+    return upper ? M[c + (int64_t)i * ld] : M[i + (int64_t)c * ld];
+  };
+  for (int j = 0; j < n; ++j) {
+    if (threadIdx.x == 0) {
+      const double ajj = at(j, j);
+      s_fail = 0;
+      if (ajj <= 0.0) {
+        s_fail = 1;  // potf2_L.c:67-71: write the pivot back, info = j + 1
+      } else {
+        at(j, j) = sqrt(ajj);
+      }
+      s_d = at(j, j);
+    }
+    __syncthreads();
+    if (s_fail) return j + 1;
+    const double r = 1.0 / s_d;
+    for (int i = j + 1 + threadIdx.x; i < n; i += NT) at(i, j) *= r;
+    __syncthreads();
+    const int rows = n - j - 1;
+    const int64_t total = (int64_t)rows * rows;
+    for (int64_t e = threadIdx.x; e < total; e += NT) {
+      const int i = j + 1 + (int)(e % rows), c = j + 1 + (int)(e / rows);
+      if (i >= c) at(i, c) = fma(-at(i, j), at(c, j), at(i, c));
+    }
+    __syncthreads();
+  }
+  return 0;
+}
+
+// ---------------------------------------------------------------- mixed DGESV
+template <int NT>
+__device__ int cta_dsgesv(const DevProblem &p) {
+  const int n = p.n, nrhs = p.k;
+  double *A = (double *)p.A;
+  double *B = (double *)p.B;
+  int *ipiv = (int *)p.C;
+  float *S = p.work;            // n x n FP32 factors
+  float *sr = S + (int64_t)n * n;  // FP32 correction (n)
+  double *x = (double *)(sr + n);  // FP64 iterate (n); n*n + n floats keep 8-byte alignment
+  __shared__ double red[NT / 32];
+  __shared__ int s_ok;
+  __shared__ double s_anrm;
+  // ||A||_inf and the FP32 copy of A
+  {
+    double best = 0.0;
+    for (int i = threadIdx.x; i < n; i += NT) {
+      double s = 0.0;
+      for (int c = 0; c < n; ++c) s += fabs(A[i + (int64_t)c * p.lda]);
+      best = s > best ? s : best;
+    }
+    for (int off = 16; off > 0; off >>= 1) best = fmax(best, __shfl_down_sync(0xffffffffu, best, off));
+    if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = best;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double b = 0.0;
+      for (int w = 0; w < NT / 32; ++w) b = fmax(b, red[w]);
+      s_anrm = b;
+    }
+    for (int64_t e = threadIdx.x; e < (int64_t)n * n; e += NT) {
+      const int i = (int)(e % n), c = (int)(e / n);
+      S[e] = (float)A[i + (int64_t)c * p.lda];
+    }
+    __syncthreads();
+  }
+  const double cte = s_anrm * (DBL_EPSILON * 0.5) * sqrt((double)n);
+  int sinfo = cta_getrf<float, NT>(n, S, n, ipiv);
+  __syncthreads();
+  bool ok = sinfo == 0;
+  int r = 0;  // columns < r hold converged solutions
+  for (; r < nrhs && ok; ++r) {
+    double *b = B + (int64_t)r * p.ldb;
+    // x0 = fp64(LU32 \ fp32(b))
+    for (int i = threadIdx.x; i < n; i += NT) sr[i] = (float)b[i];
+    __syncthreads();
+    cta_getrs<float, float, NT>(n, 1, S, n, ipiv, sr, n);
+    for (int i = threadIdx.x; i < n; i += NT) x[i] = (double)sr[i];
+    __syncthreads();
+    bool conv = false;
+    for (int it = 0; it <= 30; ++it) {
+      // r = b - A x (FP64), max|r| and max|x|
+      double rmax = 0.0, xmax = 0.0;
+      for (int i = threadIdx.x; i < n; i += NT) {
+        double s = b[i];
+        for (int c = 0; c < n; ++c) s = fma(-A[i + (int64_t)c * p.lda], x[c], s);
+        sr[i] = (float)s;
+        rmax = fmax(rmax, fabs(s));
+        xmax = fmax(xmax, fabs(x[i]));
+      }
+      for (int off = 16; off > 0; off >>= 1) {
+        rmax = fmax(rmax, __shfl_down_sync(0xffffffffu, rmax, off));
+        xmax = fmax(xmax, __shfl_down_sync(0xffffffffu, xmax, off));
+      }
+      __syncthreads();
+      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = rmax;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double b2 = 0.0;
+        for (int w = 0; w < NT / 32; ++w) b2 = fmax(b2, red[w]);
+        s_anrm = b2;  // reuse as max|r|
+      }
+      __syncthreads();
+      const double rm = s_anrm;
+      __syncthreads();
+      if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = xmax;
+      __syncthreads();
+      if (threadIdx.x == 0) {
+        double b2 = 0.0;
+        for (int w = 0; w < NT / 32; ++w) b2 = fmax(b2, red[w]);
+        s_ok = rm <= b2 * cte;
+      }
+      __syncthreads();
+      if (s_ok) {
+        conv = true;
+        break;
+      }
+      cta_getrs<float, float, NT>(n, 1, S, n, ipiv, sr, n);
+      for (int i = threadIdx.x; i < n; i += NT) x[i] += (double)sr[i];
+      __syncthreads();
+    }
+    if (!conv) {
+      ok = false;
+      break;
+    }
+    for (int i = threadIdx.x; i < n; i += NT) b[i] = x[i];
+    __syncthreads();
+  }
+  if (ok) return 0;
+  // FP64 fallback (dsgesv.f:410-425): factor A in place and solve the
+  // right-hand sides that have no converged solution yet
+  const int info = cta_getrf<double, NT>(n, A, p.lda, ipiv);
+  __syncthreads();
+  if (info == 0)
+    cta_getrs<double, double, NT>(n, nrhs - r, A, p.lda, ipiv, B + (int64_t)r * p.ldb, p.ldb);
+  return info;
+}
+
+// ---------------------------------------------------------------- kernel
+template <int NT>
+__global__ void __launch_bounds__(NT)
+grouped_kernel(const DevProblem *__restrict__ probs, const int *__restrict__ order, int count,
+               int *__restrict__ next, int mixed) {
+  __shared__ int s_idx;
+  for (;;) {
+    if (threadIdx.x == 0) s_idx = atomicAdd(next, 1);
+    __syncthreads();
+    const int q = s_idx;
+    __syncthreads();
+    if (q >= count) break;
+    const DevProblem p = probs[order[q]];
+    if (p.type == GB_BATCH_DGEMM) {
+      cta_dgemm<NT>(p);
+    } else if (p.type == GB_BATCH_DGESV) {
+      int info;
+      if (mixed) {
+        info = cta_dsgesv<NT>(p);
+      } else {
+        info = cta_getrf<double, NT>(p.n, (double *)p.A, p.lda, (int *)p.C);
+        __syncthreads();
+        if (info == 0)
+          cta_getrs<double, double, NT>(p.n, p.k, (const double *)p.A, p.lda, (const int *)p.C,
+                                        (double *)p.B, p.ldb);
+      }
+      if (threadIdx.x == 0 && p.info) *p.info = info;
+    } else if (p.type == GB_BATCH_DPOTRF) {
+      const int info = cta_potrf<NT>(p.n, (double *)p.A, p.lda, p.uplo == 0);
+      if (threadIdx.x == 0 && p.info) *p.info = info;
+    }
+    __syncthreads();
+  }
+}
+
+double problem_cost(const gb_batch_problem &p) {
+  const double n = p.n, m = p.m, k = p.k;
+  if (p.type == GB_BATCH_DGEMM) return 2.0 * m * n * k;
+  if (p.type == GB_BATCH_DGESV) return 2.0 / 3.0 * n * n * n + 2.0 * n * n * k;
+  return n * n * n / 3.0;
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ plan
+struct BatchPlan {
+  std::string key;
+  int count = 0;
+  int mixed = 0;
+  int threads = 256;
+  DevProblem *d_probs = nullptr;
+  int *d_order = nullptr;
+  int *d_next = nullptr;
+  int *d_loopnext = nullptr;
+  float *d_work = nullptr;
+  cudaStream_t stream = nullptr;
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+  int grid = 0;
+};
+
+namespace {
+
+std::mutex g_tune_mu;
+std::map<std::string, int> g_tuned;  // histogram key -> threads per CTA
+
+int launch_grouped(BatchPlan *pl, int threads, cudaStream_t s) {
+  GB_CUDA(cudaMemsetAsync(pl->d_next, 0, sizeof(int), s));
+  if (threads == 128)
+    grouped_kernel<128><<<pl->grid, 128, 0, s>>>(pl->d_probs, pl->d_order, pl->count, pl->d_next,
+                                                 pl->mixed);
+  else if (threads == 512)
+    grouped_kernel<512><<<pl->grid, 512, 0, s>>>(pl->d_probs, pl->d_order, pl->count, pl->d_next,
+                                                 pl->mixed);
+  else
+    grouped_kernel<256><<<pl->grid, 256, 0, s>>>(pl->d_probs, pl->d_order, pl->count, pl->d_next,
+                                                 pl->mixed);
+  count_launch();
+  return check_cuda(cudaGetLastError(), "grouped batch launch");
+}
+
+// Key of the autotuner: type counts and a log2 histogram of the dominant size.
+std::string histogram_key(const std::vector<gb_batch_problem> &v, int mixed) {
+  int hist[3][10] = {{0}};
+  for (const auto &p : v) {
+    const int sz = p.type == GB_BATCH_DGEMM ? std::max(p.m, std::max(p.n, p.k)) : p.n;
+    int b = 0;
+    while (b < 9 && (1 << (b + 3)) < sz) ++b;
+    const int t = p.type < 0 ? 0 : (p.type > 2 ? 2 : p.type);
+    hist[t][b]++;
+  }
+  std::string key = "fp64:" + std::to_string(mixed) + ":";
+  for (int t = 0; t < 3; ++t)
+    for (int b = 0; b < 10; ++b) {
+      // coarse (log2) counts keep similar batches on the same entry
+      int c = hist[t][b], lg = 0;
+      while (c > 0) {
+        c >>= 1;
+        ++lg;
+      }
+      key += std::to_string(lg) + ",";
+    }
+  return key;
+}
+
+}  // namespace
+
+}  // namespace gb
+
+using namespace gb;
+
+extern "C" {
+
+void *gb_batch_plan_create(const gb_batch_problem *problems, int count, int flags) {
+  if (count < 0 || (count > 0 && !problems)) {
+    set_error(GB_ERR_INVALID_VALUE, "gb_batch_plan_create: bad problem list");
+    return nullptr;
+  }
+  for (int i = 0; i < count; ++i) {
+    const gb_batch_problem &p = problems[i];
+    const bool bad = p.type < GB_BATCH_DGEMM || p.type > GB_BATCH_DPOTRF || p.n < 0 ||
+                     (p.type == GB_BATCH_DGEMM && (p.m < 0 || p.k < 0 || p.ldc < (p.m > 1 ? p.m : 1))) ||
+                     (p.type != GB_BATCH_DGEMM && p.lda < (p.n > 1 ? p.n : 1)) ||
+                     (p.type == GB_BATCH_DGESV && (p.k < 0 || p.ldb < (p.n > 1 ? p.n : 1)));
+    if (bad) {
+      set_error(GB_ERR_INVALID_VALUE, "gb_batch_plan_create: problem %d is invalid", i);
+      return nullptr;
+    }
+  }
+  if (ensure_init()) return nullptr;
+  cudaStream_t s = stream();
+  BatchPlan *pl = new BatchPlan();
+  pl->count = count;
+  pl->mixed = (flags & GB_BATCH_MIXED) ? 1 : 0;
+  pl->stream = s;
+  std::vector<gb_batch_problem> v(problems, problems + count);
+  // FP32 scratch for the mixed DGESV variant
+  size_t work_floats = 0;
+  std::vector<size_t> work_off(count, 0);
+  if (pl->mixed)
+    for (int i = 0; i < count; ++i)
+      if (v[i].type == GB_BATCH_DGESV) {
+        work_off[i] = work_floats;
+        const size_t nn = (size_t)v[i].n;
+        work_floats += nn * nn + 4 * nn + 8;  // factors, correction, FP64 iterate (2 words/entry)
+        work_floats = (work_floats + 63) & ~size_t(63);
+      }
+  std::vector<DevProblem> d(count);
+  for (int i = 0; i < count; ++i) {
+    const gb_batch_problem &p = v[i];
+    DevProblem &q = d[i];
+    memset(&q, 0, sizeof(q));
+    q.type = p.type;
+    q.m = p.m;
+    q.n = p.n;
+    q.k = p.k;
+    q.ta = (upch(p.transa) == 'T' || upch(p.transa) == 'C') ? 1 : 0;
+    q.tb = (upch(p.transb) == 'T' || upch(p.transb) == 'C') ? 1 : 0;
+    q.uplo = upch(p.uplo) == 'U' ? 0 : 1;
+    q.alpha = p.alpha;
+    q.beta = p.beta;
+    q.A = p.A;
+    q.B = p.B;
+    q.C = p.C;
+    q.lda = p.lda;
+    q.ldb = p.ldb;
+    q.ldc = p.ldc;
+    q.info = p.info;
+  }
+  // order: decreasing cost (longest-processing-time first)
+  std::vector<int> order(count);
+  for (int i = 0; i < count; ++i) order[i] = i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    return problem_cost(v[a]) > problem_cost(v[b]);
+  });
+  const size_t bytes = sizeof(DevProblem) * (size_t)(count > 0 ? count : 1);
+  if (cudaMalloc(&pl->d_probs, bytes) != cudaSuccess ||
+      cudaMalloc(&pl->d_order, sizeof(int) * (size_t)(count > 0 ? count : 1)) != cudaSuccess ||
+      cudaMalloc(&pl->d_next, sizeof(int) * 4) != cudaSuccess ||
+      (work_floats && cudaMalloc(&pl->d_work, work_floats * sizeof(float)) != cudaSuccess)) {
+    check_cuda(cudaErrorMemoryAllocation, "gb_batch_plan_create");
+    gb_batch_plan_destroy(pl);
+    return nullptr;
+  }
+  for (int i = 0; i < count; ++i)
+    if (pl->mixed && v[i].type == GB_BATCH_DGESV) d[i].work = pl->d_work + work_off[i];
+  if (count) {
+    cudaMemcpy(pl->d_probs, d.data(), bytes, cudaMemcpyHostToDevice);
+    cudaMemcpy(pl->d_order, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice);
+  }
+  pl->grid = sm_count() * 2;
+  // CTA size from the autotuner cache (keyed by the problem-size histogram)
+  const std::string key = histogram_key(v, pl->mixed);
+  pl->key = key;
+  int best_t = 0;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) best_t = it->second;
+  }
+  if (!best_t) best_t = 256;  // untuned default; gb_batch_plan_tune refines and caches
+  pl->threads = best_t;
+  // capture the launch in a CUDA graph on a private capture stream
+  cudaStream_t cap;
+  if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) == cudaSuccess) {
+    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      launch_grouped(pl, pl->threads, cap);
+      if (cudaStreamEndCapture(cap, &pl->graph) == cudaSuccess &&
+          cudaGraphInstantiate(&pl->exec, pl->graph, 0) == cudaSuccess) {
+        // ready
+      } else {
+        cudaGetLastError();
+        pl->exec = nullptr;
+      }
+    }
+    cudaStreamDestroy(cap);
+  }
+  return pl;
+}
+
+int gb_batch_plan_tune(void *plan) {
+  BatchPlan *pl = reinterpret_cast<BatchPlan *>(plan);
+  if (!pl) return set_error(GB_ERR_INVALID_VALUE, "gb_batch_plan_tune: null plan");
+  if (pl->count == 0) return GB_SUCCESS;
+  int st = ensure_init();
+  if (st) return st;
+  cudaStream_t s = stream();
+  const int cands[3] = {128, 256, 512};
+  float best_ms = 1e30f;
+  int best_t = pl->threads;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  for (int t : cands) {
+    cudaEventRecord(e0, s);
+    if ((st = launch_grouped(pl, t, s))) break;
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    if (ms < best_ms) {
+      best_ms = ms;
+      best_t = t;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (st) return st;
+  pl->threads = best_t;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[pl->key] = best_t;
+  }
+  if (pl->exec) {
+    cudaGraphExecDestroy(pl->exec);
+    pl->exec = nullptr;
+  }
+  if (pl->graph) {
+    cudaGraphDestroy(pl->graph);
+    pl->graph = nullptr;
+  }
+  cudaStream_t cap;
+  if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) == cudaSuccess) {
+    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+      launch_grouped(pl, pl->threads, cap);
+      if (cudaStreamEndCapture(cap, &pl->graph) != cudaSuccess ||
+          cudaGraphInstantiate(&pl->exec, pl->graph, 0) != cudaSuccess) {
+        cudaGetLastError();
+        pl->exec = nullptr;
+      }
+    }
+    cudaStreamDestroy(cap);
+  }
+  return finish_blocking(s);
+}
+
+int gb_batch_plan_threads(void *plan) {
+  BatchPlan *pl = reinterpret_cast<BatchPlan *>(plan);
+  return pl ? pl->threads : 0;
+}
+
+int gb_batch_execute(void *plan) {
+  BatchPlan *pl = reinterpret_cast<BatchPlan *>(plan);
+  if (!pl) return set_error(GB_ERR_INVALID_VALUE, "gb_batch_execute: null plan");
+  int st = ensure_init();
+  if (st) return st;
+  if (pl->count == 0) return GB_SUCCESS;
+  cudaStream_t s = stream();
+  if (pl->exec) {
+    count_launch();
+    return check_cuda(cudaGraphLaunch(pl->exec, s), "cudaGraphLaunch(batch)");
+  }
+  return launch_grouped(pl, pl->threads, s);
+}
+
+int gb_batch_execute_loop(void *plan) {
+  BatchPlan *pl = reinterpret_cast<BatchPlan *>(plan);
+  if (!pl) return set_error(GB_ERR_INVALID_VALUE, "gb_batch_execute_loop: null plan");
+  int st = ensure_init();
+  if (st) return st;
+  if (pl->count == 0) return GB_SUCCESS;
+  cudaStream_t s = stream();
+  if (!pl->d_loopnext) {
+    if (cudaMalloc(&pl->d_loopnext, sizeof(int) * (size_t)pl->count) != cudaSuccess)
+      return check_cuda(cudaErrorMemoryAllocation, "gb_batch_execute_loop");
+  }
+  GB_CUDA(cudaMemsetAsync(pl->d_loopnext, 0, sizeof(int) * (size_t)pl->count, s));
+  // one launch of the same per-problem code for every problem, in table order
+  for (int q = 0; q < pl->count; ++q) {
+    if (pl->threads == 128)
+      grouped_kernel<128><<<1, 128, 0, s>>>(pl->d_probs, pl->d_order + q, 1, pl->d_loopnext + q, pl->mixed);
+    else if (pl->threads == 512)
+      grouped_kernel<512><<<1, 512, 0, s>>>(pl->d_probs, pl->d_order + q, 1, pl->d_loopnext + q, pl->mixed);
+    else
+      grouped_kernel<256><<<1, 256, 0, s>>>(pl->d_probs, pl->d_order + q, 1, pl->d_loopnext + q, pl->mixed);
+    count_launch();
+  }
+  return check_cuda(cudaGetLastError(), "batch loop");
+}
+
+}  // extern "C"
+
+namespace gb {
+
+// cblas_dgemm_batch after argument checks: all problems go to one grouped
+// launch.  Host operands are packed into one pinned buffer, copied with one
+// transfer each way and unpacked; device operands are used in place.
+int gb_dgemm_batch_grouped(int order, const int *ta, const int *tb, const blasint *m,
+                           const blasint *n, const blasint *k, const double *alpha,
+                           const double **A, const blasint *lda, const double **B,
+                           const blasint *ldb, const double *beta, double **C,
+                           const blasint *ldc, blasint group_count, const blasint *group_size) {
+  int st = ensure_init();
+  if (st) return st;
+  cudaStream_t s = stream();
+  const bool row = order == CblasRowMajor;
+  int64_t total = 0;
+  for (blasint g = 0; g < group_count; ++g) total += group_size[g];
+  if (total == 0) return GB_SUCCESS;
+  // device or host operands (decided on the first problem, applied to all)
+  const double *firstA = nullptr;
+  for (blasint g = 0, idx = 0; g < group_count && !firstA; idx += group_size[g], ++g)
+    if (group_size[g] > 0) firstA = C[idx];
+  const bool on_device = firstA && is_device_pointer(firstA);
+  std::vector<gb_batch_problem> probs;
+  probs.reserve((size_t)total);
+  // host staging: offsets of every packed operand
+  struct Pack {
+    const double *src;
+    double *dst_host;
+    int64_t rows, cols, ld;
+    size_t off;
+    bool out;
+  };
+  std::vector<Pack> packs;
+  size_t elems = 0;
+  auto add = [&](const double *src, int64_t rows, int64_t cols, int64_t ld, bool out) {
+    Pack pk{src, const_cast<double *>(src), rows, cols, ld, elems, out};
+    packs.push_back(pk);
+    elems += (size_t)rows * cols;
+    return packs.size() - 1;
+  };
+  std::vector<size_t> pa, pb, pc;
+  int64_t idx = 0;
+  for (blasint g = 0; g < group_count; ++g) {
+    const int64_t M = row ? n[g] : m[g], N = row ? m[g] : n[g], K = k[g];
+    for (blasint t = 0; t < group_size[g]; ++t, ++idx) {
+      gb_batch_problem p;
+      memset(&p, 0, sizeof(p));
+      p.type = GB_BATCH_DGEMM;
+      p.m = (int)M;
+      p.n = (int)N;
+      p.k = (int)K;
+      p.transa = ta[g] ? 'T' : 'N';
+      p.transb = tb[g] ? 'T' : 'N';
+      p.alpha = alpha[g];
+      p.beta = beta[g];
+      const double *pa_ = row ? B[idx] : A[idx];
+      const double *pb_ = row ? A[idx] : B[idx];
+      p.lda = (int)(row ? ldb[g] : lda[g]);
+      p.ldb = (int)(row ? lda[g] : ldb[g]);
+      p.ldc = (int)ldc[g];
+      p.A = const_cast<double *>(pa_);
+      p.B = const_cast<double *>(pb_);
+      p.C = C[idx];
+      if (M == 0 || N == 0) continue;
+      if (!on_device) {
+        const bool need_ab = K > 0 && alpha[g] != 0.0;
+        const int64_t ra = ta[g] ? K : M, ca = ta[g] ? M : K;
+        const int64_t rb = tb[g] ? N : K, cb = tb[g] ? K : N;
+        pa.push_back(need_ab ? add(pa_, ra, ca, p.lda, false) : (size_t)-1);
+        pb.push_back(need_ab ? add(pb_, rb, cb, p.ldb, false) : (size_t)-1);
+        pc.push_back(add(C[idx], M, N, p.ldc, true));
+      }
+      probs.push_back(p);
+    }
+  }
+  Scratch dev(on_device ? 0 : elems * sizeof(double), s);
+  double *hbuf = nullptr;
+  if (!on_device) {
+    if (!dev.p) return GB_ERR_ALLOC;
+    GB_CUDA(cudaMallocHost((void **)&hbuf, elems * sizeof(double)));
+    for (const Pack &pk : packs)
+      for (int64_t c = 0; c < pk.cols; ++c)
+        memcpy(hbuf + pk.off + c * pk.rows, pk.src + c * pk.ld, pk.rows * sizeof(double));
+    GB_CUDA(cudaMemcpyAsync(dev.p, hbuf, elems * sizeof(double), cudaMemcpyHostToDevice, s));
+    double *d = dev.as<double>();
+    for (size_t i = 0; i < probs.size(); ++i) {
+      gb_batch_problem &p = probs[i];
+      if (pa[i] != (size_t)-1) {
+        p.A = d + packs[pa[i]].off;
+        p.lda = (int)packs[pa[i]].rows;
+        p.B = d + packs[pb[i]].off;
+        p.ldb = (int)packs[pb[i]].rows;
+      }
+      p.C = d + packs[pc[i]].off;
+      p.ldc = (int)packs[pc[i]].rows;
+      if (p.ldc < 1) p.ldc = 1;
+      if (p.lda < 1) p.lda = 1;
+      if (p.ldb < 1) p.ldb = 1;
+    }
+  }
+  void *plan = gb_batch_plan_create(probs.data(), (int)probs.size(), 0);
+  if (!plan) {
+    if (hbuf) cudaFreeHost(hbuf);
+    return GB_ERR_CUDA;
+  }
+  st = gb_batch_execute(plan);
+  if (!st && !on_device) {
+    GB_CUDA(cudaMemcpyAsync(hbuf, dev.p, elems * sizeof(double), cudaMemcpyDeviceToHost, s));
+    st = finish_blocking(s);
+    if (!st)
+      for (const Pack &pk : packs)
+        if (pk.out)
+          for (int64_t c = 0; c < pk.cols; ++c)
+            memcpy(pk.dst_host + c * pk.ld, hbuf + pk.off + c * pk.rows, pk.rows * sizeof(double));
+  } else if (!st) {
+    st = finish_blocking(s);
+  }
+  gb_batch_plan_destroy(plan);
+  if (hbuf) cudaFreeHost(hbuf);
+  return st;
+}
+
+}  // namespace gb
+
+extern "C" {
+
+void gb_batch_plan_destroy(void *plan) {
+  BatchPlan *pl = reinterpret_cast<BatchPlan *>(plan);
+  if (!pl) return;
+  if (pl->exec) cudaGraphExecDestroy(pl->exec);
+  if (pl->graph) cudaGraphDestroy(pl->graph);
+  cudaFree(pl->d_probs);
+  cudaFree(pl->d_order);
+  cudaFree(pl->d_next);
+  cudaFree(pl->d_work);
+  cudaFree(pl->d_loopnext);
+  delete pl;
+}
+
+}  // extern "C"
