@@ -43,6 +43,8 @@ def parse_args():
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=8192)
     ap.add_argument("--slices", type=int, default=8)
+    ap.add_argument("--no-extras", action="store_true",
+                    help="skip the DGESV and batched legs (profiling runs)")
     return ap.parse_args()
 
 
@@ -153,19 +155,26 @@ def measured_peaks():
 
 
 def profiled_traffic(n):
-    """DRAM bytes per slice-GEMM launch from the committed ncu summary, scaled
-    from the captured size to n (traffic grows as n^3 for this kernel: every
-    tile re-reads its K-panel of slices for each product)."""
+    """DRAM bytes per slice-GEMM launch from the committed ncu summary
+    (dram__bytes_read.sum + dram__bytes_write.sum, one-pass capture).  A
+    capture at exactly n is used as is; otherwise the nearest captured size
+    is scaled by n^3 (every tile re-reads its K-panel of slices for each
+    product) and the result says so."""
     path = os.path.join(ROOT, "profiles", "slice_gemm_ncu.txt")
+    caps = {}
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch"):
                 _, size, val = line.split()
-                size, val = int(size), float(val)
-                return val * (n / size) ** 3
+                caps[int(size)] = float(val)
     except Exception:
-        pass
-    return None
+        return None, None
+    if not caps:
+        return None, None
+    if n in caps:
+        return caps[n], f"ncu one-pass capture at n={n}"
+    size = min(caps, key=lambda c: abs(c - n))
+    return caps[size] * (n / size) ** 3, f"ncu capture at n={size} scaled by n^3"
 
 
 # --------------------------------------------------------------------------
@@ -280,6 +289,102 @@ def dgesv_compare(lib, torch, gb, world, n=8192, nrhs=1, reps=3):
                       "bound_n_eps": n},
             "native_fp64": {"value": world * flops / t_native / 1e12, "ms": t_native * 1e3},
             "speedup_mixed_over_native": t_native / t_mixed}
+
+
+def batched_compare(lib, torch, gb, count=20000, loop_sample=1000):
+    """20,000 uneven problems (n uniform in [8,256]; 40% DGEMM, 40% DGESV with
+    one right-hand side, 20% DPOTRF), FP64, one grouped persistent launch
+    replayed from a CUDA graph; the per-problem loop of the same kernel is
+    timed on the first `loop_sample` problems of the table and scaled."""
+    from openblas_gb300 import batch as BT
+    import numpy as np
+    BT.bind(lib)
+    rng = np.random.default_rng(1)
+    sizes = rng.integers(8, 257, size=(count, 3))
+    kinds = rng.choice(3, size=count, p=[0.4, 0.4, 0.2])
+    ta = tb = tc = tp = 0
+    for i in range(count):
+        m, n, k = (int(x) for x in sizes[i])
+        if kinds[i] == 0:
+            ta, tb, tc = ta + m * k, tb + k * n, tc + m * n
+        else:
+            ta, tb, tp = ta + n * n, tb + n, tp + n
+    bufA = torch.empty(ta, dtype=torch.float64, device="cuda")
+    bufB = torch.empty(tb, dtype=torch.float64, device="cuda")
+    bufC = torch.empty(max(tc, 1), dtype=torch.float64, device="cuda")
+    piv = torch.zeros(tp + 1, dtype=torch.int32, device="cuda")
+    info = torch.zeros(count, dtype=torch.int32, device="cuda")
+    table = (BT.Problem * count)()
+    oa = ob = oc = op = 0
+    flops = np.zeros(count)
+    spd = []
+    for i in range(count):
+        m, n, k = (int(x) for x in sizes[i])
+        q = table[i]
+        if kinds[i] == 0:
+            q.type, q.m, q.n, q.k = 0, m, n, k
+            q.transa, q.transb, q.alpha, q.beta = b"N", b"N", 1.0, 0.0
+            q.A, q.lda = bufA.data_ptr() + 8 * oa, m
+            q.B, q.ldb = bufB.data_ptr() + 8 * ob, k
+            q.C, q.ldc = bufC.data_ptr() + 8 * oc, m
+            oa, ob, oc = oa + m * k, ob + k * n, oc + m * n
+            flops[i] = 2.0 * m * n * k
+        else:
+            q.type, q.n = int(kinds[i]), n
+            q.A, q.lda = bufA.data_ptr() + 8 * oa, n
+            q.info = info.data_ptr() + 4 * i
+            if kinds[i] == 1:
+                q.k, q.B, q.ldb, q.C = 1, bufB.data_ptr() + 8 * ob, n, piv.data_ptr() + 4 * op
+                ob, op = ob + n, op + n
+                flops[i] = 2.0 / 3.0 * n ** 3 + 2.0 * n * n
+            else:
+                q.uplo = b"L"
+                spd.append((oa, n))
+                flops[i] = n ** 3 / 3.0
+            oa += n * n
+    g = torch.Generator(device="cuda")
+
+    def init():
+        g.manual_seed(3)
+        bufA.uniform_(-1, 1, generator=g)
+        bufB.uniform_(-1, 1, generator=g)
+        for (o, n) in spd:  # B + B^T + n I: symmetric positive definite
+            blk = bufA[o:o + n * n].view(n, n)
+            blk.add_(blk.T.clone()).add_(torch.eye(n, dtype=torch.float64, device="cuda") * n)
+
+    out = {"workload": f"{count} problems, n uniform in [8,256]: 40% DGEMM (m,n,k independent), "
+                       "40% DGETRF+DGETRS (1 RHS), 20% DPOTRF; FP64", "unit": UNIT}
+    total = float(flops.sum())
+    for flags, name in ((0, "grouped_graph_fp64"), (BT.GB_BATCH_MIXED, "grouped_graph_mixed")):
+        init()
+        plan = lib.gb_batch_plan_create(table, count, flags)
+        lib.gb_batch_plan_tune(plan)
+        init()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        lib.gb_batch_execute(plan)
+        torch.cuda.synchronize()
+        dt = time.perf_counter() - t0
+        out[name] = {"value": total / dt / 1e12, "ms": dt * 1e3,
+                     "threads_per_cta": lib.gb_batch_plan_threads(plan),
+                     "nonzero_info": int((info != 0).sum().item())}
+        lib.gb_batch_plan_destroy(plan)
+    # per-problem loop of the same kernel on a sample of the table
+    sub = (BT.Problem * loop_sample)(*[table[i] for i in range(loop_sample)])
+    init()
+    plan = lib.gb_batch_plan_create(sub, loop_sample, 0)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    lib.gb_batch_execute_loop(plan)
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t0
+    lib.gb_batch_plan_destroy(plan)
+    sflops = float(flops[:loop_sample].sum())
+    out["per_problem_loop_fp64"] = {"value": sflops / dt / 1e12, "ms_sample": dt * 1e3,
+                                    "sample": f"first {loop_sample} problems of the table"}
+    out["speedup_grouped_over_loop"] = out["grouped_graph_fp64"]["value"] / \
+        out["per_problem_loop_fp64"]["value"]
+    return out
 
 
 # --------------------------------------------------------------------------
@@ -402,13 +507,16 @@ def main():
 
     # DGESV N=8192, NRHS=1: mixed precision (FP32 LU on the GPU + FP64
     # refinement) against native FP64 getrf+getrs, both on the same operands
-    dgesv = dgesv_compare(lib, torch, gb, world)
+    dgesv = batched = None
+    if not args.no_extras:
+        dgesv = dgesv_compare(lib, torch, gb, world)
+        batched = batched_compare(lib, torch, gb)
 
     peaks, src = measured_peaks()
     slice_flops = S * (S + 1) / 2 * flops
     achieved = slice_flops / (kern_ms * 1e-3) / 1e12
     peak = float(peaks.get("bf16_tflops_sustained", 1700.0))
-    traffic = profiled_traffic(n)
+    traffic, traffic_src = profiled_traffic(n)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
@@ -424,11 +532,12 @@ def main():
                 "api": "cblas_dgemm (host pointers, pinned), GB_DGEMM_MODE=emulated"},
         "roofline": {"bound": "tensor", "kernel": "slice_gemm_kernel (tcgen05 kind::f16)",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
-                     "frac": achieved / peak, "traffic": traffic,
+                     "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
                      "peak_source": f"{src} bf16_tflops_sustained",
                      "kernel_ms_per_launch": kern_ms,
                      "algorithmic_flops_per_launch": slice_flops},
         "dgesv": dgesv,
+        "batched": batched,
         "gpu_launches": int(launches),
         "clocks": clk,
     }

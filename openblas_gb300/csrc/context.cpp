@@ -67,6 +67,8 @@ const Config &config() {
     if (s) g_cfg.ozaki_slices = atoi(s);
     const char *v = getenv("GB_VERBOSE");
     if (v) g_cfg.verbose = atoi(v);
+    const char *g = getenv("GB_OZAKI_GROUP_M");
+    if (g && atoi(g) > 0) g_cfg.ozaki_group_m = atoi(g);
   });
   return g_cfg;
 }

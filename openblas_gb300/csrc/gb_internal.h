@@ -84,6 +84,7 @@ struct Config {
   int dgemm_mode = GB_DGEMM_NATIVE;   // GB_DGEMM_MODE=native|emulated|auto
   int ozaki_slices = 0;               // GB_OZAKI_SLICES (0 = auto)
   int verbose = 0;                    // GB_VERBOSE
+  int ozaki_group_m = 8;              // GB_OZAKI_GROUP_M: m-tiles per slice-GEMM tile group
 };
 const Config &config();
 

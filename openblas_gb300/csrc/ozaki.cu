@@ -57,12 +57,27 @@ constexpr int NONFINITE = -100000;  // exponent marker of a row/column with Inf/
 struct GemmParams {
   int S;
   int m_tiles, n_tiles;
+  int group_m;  // m-tiles per group of the tile order
   int kblocks;
   int m_pad, n_pad;
   int64_t plane_stride;
   int *planes;
   int *status;
 };
+
+// Tile order: groups of group_m m-tiles, walked column by column inside a
+// group, so the tiles resident at one time cover a near-square block of C
+// and their A and B panels are shared through L2 (a plain m-fastest order
+// puts every m-tile of a few columns in flight and re-reads A from HBM).
+__device__ __forceinline__ void tile_coords(int tile, const GemmParams &p, int &mt, int &nt) {
+  const int span = p.group_m * p.n_tiles;
+  const int first_m = (tile / span) * p.group_m;
+  const int rem = p.m_tiles - first_m;
+  const int gm = rem < p.group_m ? rem : p.group_m;
+  const int in = tile % span;
+  mt = first_m + in % gm;
+  nt = in / gm;
+}
 
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
@@ -125,7 +140,8 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       for (int i = 0; i < STAGES; ++i) issued[i] = false;
       bool ok = true;
       for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
-        const int mt = tile % p.m_tiles, nt = tile / p.m_tiles;
+        int mt, nt;
+        tile_coords(tile, p, mt, nt);
         for (int L = 2; ok && L <= S + 1; ++L) {
           const int s_lo = L - S > 1 ? L - S : 1, s_hi = L - 1 < S ? L - 1 : S;
           for (int s = s_lo; ok && s <= s_hi; ++s) {
@@ -225,6 +241,9 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     bool ok = true;
     int32_t sum[128];
     for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+      int mt, nt;
+      tile_coords(tile, p, mt, nt);
+      const int64_t plane_tile = (int64_t)nt * p.m_tiles + mt;
       for (int L = 2; ok && L <= S + 1; ++L) {
 #pragma unroll
         for (int c = 0; c < 128; ++c) sum[c] = 0;
@@ -259,7 +278,7 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         if (!ok) break;
         // level plane, tile-blocked and column-major inside the tile so a
         // warp's store of one column is 128 contiguous bytes
-        int *dst = p.planes + (int64_t)(L - 2) * p.plane_stride + (int64_t)tile * (BM * BN) +
+        int *dst = p.planes + (int64_t)(L - 2) * p.plane_stride + plane_tile * (BM * BN) +
                    (int64_t)(half * 128) * BM + row;
 #pragma unroll
         for (int c = 0; c < 128; ++c) dst[c * BM] = sum[c];
@@ -557,6 +576,7 @@ int emulated_segment(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
   gp.S = S;
   gp.m_tiles = (int)(m_pad / BM);
   gp.n_tiles = (int)(n_pad / BN);
+  gp.group_m = config().ozaki_group_m;
   gp.kblocks = (int)(k_pad / BK);
   gp.m_pad = (int)m_pad;
   gp.n_pad = (int)n_pad;

@@ -34,7 +34,9 @@ def _int_matrix(seed, shape, lo=-127, hi=127):
     return np.asfortranarray(W.randint(seed, shape, lo, hi).astype(np.float64))
 
 
-@pytest.mark.parametrize("m,n,k", [(64, 48, 1000), (300, 520, 2100), (128, 256, 5000)])
+# (2200, 3000, 200): 18 m-tiles, so the tile order's last group is a ragged 2
+@pytest.mark.parametrize("m,n,k", [(64, 48, 1000), (300, 520, 2100), (128, 256, 5000),
+                                   (2200, 3000, 200)])
 def test_integer_operands_exact(F, emulated, m, n, k):
     A = _int_matrix(1, (m, k))
     B = _int_matrix(2, (k, n))
