@@ -12,6 +12,7 @@ constexpr int PANEL_NB = 32;
 // Kernel error codes written to the context status word.
 constexpr int GB_KERR_BARRIER_TIMEOUT = 1;
 constexpr int GB_KERR_MBARRIER_TIMEOUT = 2;
+constexpr int GB_KERR_CHAIN_TIMEOUT = 3;  // a solve block waited too long for its predecessor
 
 // LU with partial pivoting of an m x n matrix (device pointers).  ipiv gets
 // min(m,n) 1-based global row indices, *info the first zero pivot (1-based)
@@ -32,8 +33,9 @@ template <typename T>
 int laswp_device(int64_t n, T *A, int64_t lda, int64_t k1, int64_t k2, const int *ipiv,
                  int64_t incx, cudaStream_t s);
 // Inverses of the 64x64 diagonal blocks of the unit-lower L and of U of an
-// LU factorisation (each n/64 * 64*64 entries), and the blocked solve that
-// uses them (interchanges applied beforehand).
+// LU factorisation (each n/64 * 64*64 entries), and the solve that uses them
+// (interchanges applied beforehand): one launch per triangle, 64-row blocks
+// chained through release/acquire flags.
 template <typename T>
 int lu_block_inverses(int64_t n, const T *A, int64_t lda, T *Linv, T *Uinv, cudaStream_t s);
 template <typename T>

@@ -1,13 +1,18 @@
-// LU solve for a few right-hand sides with inverted diagonal blocks.
+// LU solve with inverted diagonal blocks, one launch per triangle.
 //
 // getrs (lapack/getrs/getrs_single.c:42-68) applies the interchanges and two
 // triangular solves; for one right-hand side the reference switches to TRSV
 // (driver/level2/trsv_L.c, trsv_U.c), a latency-bound sweep.  Here the
 // diagonal blocks (TB x TB) of the unit-lower L and of U are inverted once
-// per factorisation; each solve step i is then one kernel in which every CTA
-// recomputes x_i = inv(D_ii) * b_i (a small dense product, no inter-CTA
-// dependency) and updates its share of the remaining rows,
-// b_r -= A_{r,i} x_i.  A solve is n/TB launches that read the triangle once.
+// per factorisation.  A solve is then one kernel per triangle in which each
+// CTA owns one 64-row block of the solution for a group of right-hand
+// sides: it takes a ticket from an atomic counter (block order = ticket
+// order, so every block it waits for belongs to a CTA that is already
+// running), accumulates A(i, j) x_j over the finished blocks j as their
+// release flags appear, and finishes with x_i = inv(D_ii) (b_i - sum).  The
+// triangle is read once, by all CTAs in parallel; only the short dependency
+// tail of each block is serial.  Every wait is bounded: on timeout the
+// kernel records GB_KERR_CHAIN_TIMEOUT in the status word and returns.
 // Used by the mixed-precision solver's refinement steps, where the factors
 // are reused many times.
 #include <cuda_runtime.h>
@@ -21,9 +26,9 @@ namespace gb {
 namespace {
 
 constexpr int TB = 64;           // diagonal block size
-// right-hand sides per solve pass (static shared memory stays within 48 KB)
+// right-hand sides per chain (accumulators per thread)
 template <typename T>
-constexpr int maxr() { return sizeof(T) == 4 ? 32 : 16; }
+constexpr int maxr() { return sizeof(T) == 4 ? 8 : 4; }
 
 // Inverse of the diagonal block of L (unit lower, lower = 1) or U (upper,
 // lower = 0).  One CTA per block, thread c computes column c of the inverse
@@ -71,66 +76,162 @@ diag_inverse_kernel(int64_t n, const T *__restrict__ A, int64_t lda, int lower,
   for (int r = 0; r < TB; ++r) out[r + c * TB] = x[r];
 }
 
-// One step of the blocked solve: x_i = inv_i * w_i (every CTA computes it
-// from the working buffer W, whose block i no step of this pass writes),
-// CTA 0 stores x_i into the output buffer X, and rows [u0, u1) of W get
-// w_r -= A(r, block i) x_i.
-template <typename T, int R>
+__device__ __forceinline__ int ld_acquire(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+
+__device__ __forceinline__ void st_release(int *p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ uint64_t now_ns() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+constexpr uint64_t CHAIN_WAIT_NS = 2000000000ull;
+
+// One triangle of the solve.  lower = 1: L y = b (blocks in ascending
+// order, inverses of L); lower = 0: U x = y (descending, inverses of U).
+// Bin is read only; Xout receives the solution blocks, which other CTAs of
+// the same launch read back (through L2) once the block's flag is set.
+// flags[grp * nblk + i] = 1 when block i of right-hand-side group grp is
+// final.  Thread (r, g4) owns row r of the block and columns g4*16..+16 of
+// each 64-column tile of A; U tiles are in flight per step.
+template <typename T, int R, int U>
 __global__ void __launch_bounds__(256)
-block_solve_step_kernel(int nrhs, const T *__restrict__ A, int64_t lda,
-                        const T *__restrict__ inv, int64_t r0, int nb, T *__restrict__ W,
-                        int64_t ldw, T *__restrict__ X, int64_t ldx, int64_t u0, int64_t u1) {
-  __shared__ T Iv[TB * TB];  // inverted diagonal block, column-major
-  __shared__ T bi[R][TB];
-  __shared__ T xi[R][TB];
-  const int tid = threadIdx.x;
-  const T *src = inv + (r0 / TB) * (TB * TB);
-  for (int e = tid; e < TB * TB; e += 256) Iv[e] = src[e];
-  for (int e = tid; e < R * TB; e += 256) {
-    const int k = e / TB, r = e % TB;
-    bi[k][r] = (k < nrhs && r < nb) ? W[(r0 + r) + k * ldw] : T(0);
-  }
+chain_solve_kernel(int64_t n, int nrhs, const T *__restrict__ A, int64_t lda,
+                   const T *__restrict__ inv, int lower, const T *__restrict__ Bin, int64_t ldb,
+                   T *Xout, int64_t ldx, int *flags, int *ticket, int nblk, int ngroups,
+                   int *status) {
+  __shared__ T xs[U][R][TB];
+  __shared__ T red[4][R][TB];
+  __shared__ int s_val;
+  const int tid = threadIdx.x, r = tid & (TB - 1), g4 = tid >> 6;
+  if (tid == 0) s_val = atomicAdd(ticket, 1);
   __syncthreads();
-  for (int e = tid; e < R * TB; e += 256) {
-    const int k = e / TB, r = e % TB;
-    T s = T(0);
-    if (k < nrhs) {
-#pragma unroll 16
-      for (int c = 0; c < TB; ++c) s = fma(Iv[r + c * TB], bi[k][c], s);
-    }
-    xi[k][r] = s;
+  const int t = s_val;
+  const int idx = t / ngroups, grp = t - idx * ngroups;
+  const int i = lower ? idx : nblk - 1 - idx;
+  const int64_t r0 = (int64_t)i * TB;
+  const int nb = (int)((n - r0) < TB ? (n - r0) : TB);
+  const int k0 = grp * R;
+  const int kk = (nrhs - k0) < R ? (nrhs - k0) : R;
+  int *fl = flags + (int64_t)grp * nblk;
+  auto chain = [&](int jj) { return lower ? jj : nblk - 1 - jj; };
+
+  T iv[16];
+  {
+    const T *ivb = inv + (int64_t)i * (TB * TB);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) iv[c] = ivb[r + (g4 * 16 + c) * TB];
   }
-  __syncthreads();
-  if (blockIdx.x == 0)
-    for (int e = tid; e < nrhs * TB; e += 256) {
-      const int k = e / TB, r = e % TB;
-      if (r < nb) X[(r0 + r) + k * ldx] = xi[k][r];
-    }
-  const int64_t rows = u1 - u0;
-  for (int64_t rr = (int64_t)blockIdx.x * 256 + tid; rr < rows; rr += (int64_t)gridDim.x * 256) {
-    const int64_t r = u0 + rr;
-    const T *a = A + r + r0 * lda;
-    T acc[R];
+  T acc[R];
 #pragma unroll
-    for (int k = 0; k < R; ++k) acc[k] = T(0);
-    if (nb == TB) {
-#pragma unroll 8
-      for (int c = 0; c < TB; ++c) {
-        const T av = a[c * lda];
+  for (int k = 0; k < R; ++k) acc[k] = T(0);
+  const T *Arow = A + r0 + r;
+  const bool row_ok = r < nb;
+
+  int ready = -1;  // dependencies 0..ready (in chain order) are final
+  int jj = 0;
+  while (jj < idx) {
+    const int jmax = (idx - jj) < U ? (idx - jj) : U;
+    // the A tiles do not depend on the solution: issue them before waiting
+    T a[U][16];
 #pragma unroll
-        for (int k = 0; k < R; ++k) acc[k] = fma(av, xi[k][c], acc[k]);
-      }
-    } else {
-      for (int c = 0; c < nb; ++c) {
-        const T av = a[c * lda];
+    for (int u = 0; u < U; ++u) {
+      if (u < jmax) {
+        const int64_t c0 = (int64_t)chain(jj + u) * TB + g4 * 16;
 #pragma unroll
-        for (int k = 0; k < R; ++k) acc[k] = fma(av, xi[k][c], acc[k]);
+        for (int c = 0; c < 16; ++c)
+          a[u][c] = (row_ok && c0 + c < n) ? Arow[(c0 + c) * lda] : T(0);
       }
     }
+    if (jj > ready) {
+      __syncthreads();  // every thread has read s_val
+      if (tid == 0) {
+        int rd = -2;
+        if (ld_acquire(&fl[chain(idx - 1)])) {
+          rd = idx - 1;  // a flag implies all earlier flags of the chain
+        } else {
+          const uint64_t t0 = now_ns();
+          for (;;) {
+            if (ld_acquire(&fl[chain(jj)])) {
+              rd = jj;
+              break;
+            }
+            if (*(volatile int *)status) break;  // another block gave up
+            if (now_ns() - t0 > CHAIN_WAIT_NS) {
+              atomicCAS(status, 0, GB_KERR_CHAIN_TIMEOUT);
+              atomicExch(status + 1, 100 + lower);
+              break;
+            }
+            __nanosleep(100);
+          }
+          if (rd >= 0)
+            while (rd + 1 < idx && rd + 1 < jj + U && ld_acquire(&fl[chain(rd + 1)])) ++rd;
+        }
+        s_val = rd;
+      }
+      __syncthreads();
+      ready = s_val;
+      if (ready < 0) return;  // uniform: every thread read the same value
+    }
+    const int jn = (ready - jj + 1) < jmax ? (ready - jj + 1) : jmax;
+    for (int e = tid; e < jn * R * TB; e += 256) {
+      const int u = e / (R * TB), k = (e / TB) % R, c = e % TB;
+      const int64_t col = (int64_t)chain(jj + u) * TB + c;
+      xs[u][k][c] = (k < kk && col < n) ? __ldcg(&Xout[col + (int64_t)(k0 + k) * ldx]) : T(0);
+    }
+    __syncthreads();
 #pragma unroll
-    for (int k = 0; k < R; ++k)
-      if (k < nrhs) W[r + k * ldw] -= acc[k];
+    for (int u = 0; u < U; ++u) {
+      if (u < jn) {
+#pragma unroll
+        for (int c = 0; c < 16; ++c)
+#pragma unroll
+          for (int k = 0; k < R; ++k) acc[k] = fma(a[u][c], xs[u][k][g4 * 16 + c], acc[k]);
+      }
+    }
+    __syncthreads();
+    jj += jn;
   }
+
+  // v = b_i - sum_j A(i, j) x_j, then x_i = inv(D_ii) v
+#pragma unroll
+  for (int k = 0; k < R; ++k) red[g4][k][r] = acc[k];
+  __syncthreads();
+  for (int e = tid; e < R * TB; e += 256) {
+    const int k = e / TB, rr = e % TB;
+    T v = T(0);
+    if (k < kk && rr < nb)
+      v = Bin[(r0 + rr) + (int64_t)(k0 + k) * ldb] -
+          ((red[0][k][rr] + red[1][k][rr]) + (red[2][k][rr] + red[3][k][rr]));
+    xs[0][k][rr] = v;
+  }
+  __syncthreads();
+  T p[R];
+#pragma unroll
+  for (int k = 0; k < R; ++k) {
+    p[k] = T(0);
+#pragma unroll
+    for (int c = 0; c < 16; ++c) p[k] = fma(iv[c], xs[0][k][g4 * 16 + c], p[k]);
+  }
+#pragma unroll
+  for (int k = 0; k < R; ++k) red[g4][k][r] = p[k];
+  __syncthreads();
+  for (int e = tid; e < R * TB; e += 256) {
+    const int k = e / TB, rr = e % TB;
+    if (k < kk && rr < nb)
+      Xout[(r0 + rr) + (int64_t)(k0 + k) * ldx] =
+          (red[0][k][rr] + red[1][k][rr]) + (red[2][k][rr] + red[3][k][rr]);
+  }
+  __threadfence();
+  __syncthreads();
+  if (tid == 0) st_release(&fl[i], 1);
 }
 
 }  // namespace
@@ -143,45 +244,55 @@ int lu_block_inverses(int64_t n, const T *A, int64_t lda, T *Linv, T *Uinv, cuda
   return check_cuda(cudaGetLastError(), "diag_inverse");
 }
 
-// Solve L U X = B in place (interchanges already applied), in passes of
-// MAXR columns.  The forward pass works in B and writes y to the scratch Y;
-// the backward pass works in Y and writes x back into B.
+template <typename T, int R>
+static void launch_chain(unsigned grid, int64_t n, int nrhs, const T *A, int64_t lda,
+                         const T *inv, int lower, const T *Bin, int64_t ldb, T *Xout, int64_t ldx,
+                         int *flags, int *ticket, int nblk, int ngroups, cudaStream_t s) {
+  constexpr int U = sizeof(T) == 4 ? 4 : 2;
+  chain_solve_kernel<T, R, U><<<grid, 256, 0, s>>>(n, nrhs, A, lda, inv, lower, Bin, ldb, Xout,
+                                                   ldx, flags, ticket, nblk, ngroups,
+                                                   ctx().d_status);
+  count_launch();
+}
+
+// Solve L U X = B in place (interchanges already applied): the forward
+// triangle reads B and writes y to scratch, the backward triangle reads y
+// and writes x back into B.  Right-hand sides are solved in groups of R
+// columns, each group an independent chain of blocks.
 template <typename T>
 int lu_block_solve(int64_t n, int64_t nrhs, const T *A, int64_t lda, const T *Linv,
                    const T *Uinv, T *B, int64_t ldb, cudaStream_t s) {
-  const int64_t nblk = (n + TB - 1) / TB;
-  constexpr int MAXR = maxr<T>();
-  Scratch ws((size_t)n * MAXR * sizeof(T), s);
+  if (n <= 0 || nrhs <= 0) return GB_SUCCESS;
+  const int nblk = (int)((n + TB - 1) / TB);
+  const int R = nrhs == 1 ? 1 : (nrhs <= 4 ? 4 : maxr<T>());
+  const int ngroups = (int)((nrhs + R - 1) / R);
+  const size_t ybytes = (((size_t)n * nrhs * sizeof(T)) + 255) & ~size_t(255);
+  const size_t nflags = 2 * (size_t)ngroups * nblk + 2;
+  Scratch ws(ybytes + nflags * sizeof(int), s);
   if (!ws.p) return GB_ERR_ALLOC;
   T *Y = ws.as<T>();
-  auto grid = [&](int64_t rows) {
-    int64_t g = (rows + 255) / 256;
-    if (g < 1) g = 1;
-    if (g > (int64_t)sm_count() * 4) g = (int64_t)sm_count() * 4;
-    return (unsigned)g;
-  };
-  for (int64_t k0 = 0; k0 < nrhs; k0 += MAXR) {
-    const int kk = (int)((nrhs - k0) < MAXR ? (nrhs - k0) : MAXR);
-    T *Bk = B + k0 * ldb;
-    auto step = [&](const T *inv, int64_t r0, int nb, T *Wb, int64_t ldw, T *Xb, int64_t ldx,
-                    int64_t u0, int64_t u1) {
-      const unsigned g = grid(u1 - u0);
-      if (kk <= 4)
-        block_solve_step_kernel<T, 4><<<g, 256, 0, s>>>(kk, A, lda, inv, r0, nb, Wb, ldw, Xb, ldx, u0, u1);
-      else
-        block_solve_step_kernel<T, MAXR><<<g, 256, 0, s>>>(kk, A, lda, inv, r0, nb, Wb, ldw, Xb, ldx, u0, u1);
-      count_launch();
-    };
-    for (int64_t i = 0; i < nblk; ++i) {  // forward: L y = b
-      const int64_t r0 = i * TB;
-      const int nb = (int)((n - r0) < TB ? (n - r0) : TB);
-      step(Linv, r0, nb, Bk, ldb, Y, n, r0 + nb, n);
-    }
-    for (int64_t i = nblk - 1; i >= 0; --i) {  // backward: U x = y
-      const int64_t r0 = i * TB;
-      const int nb = (int)((n - r0) < TB ? (n - r0) : TB);
-      step(Uinv, r0, nb, Y, n, Bk, ldb, 0, r0);
-    }
+  int *flags = reinterpret_cast<int *>(static_cast<char *>(ws.p) + ybytes);
+  int *tickets = flags + 2 * (size_t)ngroups * nblk;
+  GB_CUDA(cudaMemsetAsync(flags, 0, nflags * sizeof(int), s));
+  const unsigned grid = (unsigned)nblk * (unsigned)ngroups;
+  const int k = (int)nrhs;
+  for (int pass = 0; pass < 2; ++pass) {
+    const int lower = pass == 0;
+    const T *inv = lower ? Linv : Uinv;
+    const T *Bin = lower ? B : Y;
+    const int64_t lbin = lower ? ldb : n;
+    T *Xo = lower ? Y : B;
+    const int64_t lxo = lower ? n : ldb;
+    int *fl = flags + (size_t)pass * ngroups * nblk;
+    if (R == 1)
+      launch_chain<T, 1>(grid, n, k, A, lda, inv, lower, Bin, lbin, Xo, lxo, fl, tickets + pass,
+                         nblk, ngroups, s);
+    else if (R == 4)
+      launch_chain<T, 4>(grid, n, k, A, lda, inv, lower, Bin, lbin, Xo, lxo, fl, tickets + pass,
+                         nblk, ngroups, s);
+    else
+      launch_chain<T, maxr<T>()>(grid, n, k, A, lda, inv, lower, Bin, lbin, Xo, lxo, fl,
+                                 tickets + pass, nblk, ngroups, s);
   }
   return check_cuda(cudaGetLastError(), "lu_block_solve");
 }

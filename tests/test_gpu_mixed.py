@@ -83,7 +83,7 @@ def test_dsgesv_singular(F, gb_clean):
     assert info == 12 and it == -3
 
 
-@pytest.mark.parametrize("n,nrhs", [(2000, 1), (2000, 64), (3000, 3)])
+@pytest.mark.parametrize("n,nrhs", [(2000, 1), (2000, 64), (3000, 3), (1537, 11)])
 def test_dsgesv_uniform(F, gb_clean, n, nrhs):
     A = W.uniform(11, (n, n))
     B = W.uniform(12, (n, nrhs))
