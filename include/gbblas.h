@@ -166,6 +166,15 @@ int gb_last_xerbla(char *name, int len);
  * trailing updates' caller-facing DGEMM (default from GB_DGEMM_MODE). */
 int gb_set_dgemm_mode(int mode);
 int gb_get_dgemm_mode(void);
+/* FP32 GEMM behind sgemm_/cblas_sgemm and the FP32 LU of the mixed solver
+ * (default from GB_SGEMM_MODE=auto|simt|tensor).  The tensor form splits
+ * each operand into three bf16 terms and runs six products on the tensor
+ * cores with FP32 accumulation (FP32-level accuracy). */
+#define GB_SGEMM_AUTO 0   /* tensor cores when the shape fills the GPU */
+#define GB_SGEMM_SIMT 1   /* FP32 FMA units */
+#define GB_SGEMM_TENSOR 2 /* always the bf16x3 tensor-core form */
+int gb_set_sgemm_mode(int mode);
+int gb_get_sgemm_mode(void);
 /* Slice count of the emulated DGEMM (0 = chosen from K and accuracy target). */
 int gb_set_ozaki_slices(int slices);
 /* Library version string. */

@@ -25,6 +25,8 @@ DEV_SIGS = {
     "gb_last_xerbla": (_i, [C.c_char_p, _i]),
     "gb_set_dgemm_mode": (_i, [_i]),
     "gb_get_dgemm_mode": (_i, []),
+    "gb_set_sgemm_mode": (_i, [_i]),
+    "gb_get_sgemm_mode": (_i, []),
     "gb_set_ozaki_slices": (_i, [_i]),
     "gb_version": (C.c_char_p, []),
     "gb_kernel_launches": (C.c_int64, []),

@@ -115,12 +115,13 @@ static void sgemm_blocking(int ta, int tb, int64_t m, int64_t n, int64_t k, floa
   Operand c(C, m, n, ldc, 4);
   if (need_ab && (a.bind(true, s) || b.bind(true, s))) return;
   if (c.bind(beta != 0.0f, s)) return;
-  if (!need_ab)
+  if (!need_ab) {
     launch_sgemm_beta(m, n, beta, c.d<float>(), c.dld, s);
-  else
-    launch_sgemm_fp32(ta, tb, m, n, k, alpha, a.d<float>(), a.dld, b.d<float>(), b.dld, beta,
-                      c.d<float>(), c.dld, s);
-  if (check_cuda(cudaGetLastError(), "sgemm launch")) return;
+    if (check_cuda(cudaGetLastError(), "sgemm launch")) return;
+  } else if (sgemm_dispatch(ta, tb, m, n, k, alpha, a.d<float>(), a.dld, b.d<float>(), b.dld,
+                            beta, c.d<float>(), c.dld, s)) {
+    return;
+  }
   c.unbind(s);
   finish_blocking(s);
 }
@@ -504,11 +505,11 @@ int gb_sgemm_dev(char transa, char transb, int64_t m, int64_t n, int64_t k, floa
   int st = dev_gemm_args(transa, transb, m, n, k, lda, ldb, ldc, &ta, &tb, "SGEMM ");
   if (st) return st;
   if (m == 0 || n == 0) return GB_SUCCESS;
-  if (k == 0 || alpha == 0.0f)
+  if (k == 0 || alpha == 0.0f) {
     launch_sgemm_beta(m, n, beta, C, ldc, stream());
-  else
-    launch_sgemm_fp32(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, stream());
-  return check_cuda(cudaGetLastError(), "sgemm launch");
+    return check_cuda(cudaGetLastError(), "sgemm launch");
+  }
+  return sgemm_dispatch(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, stream());
 }
 
 int gb_dtrsm_dev(char side, char uplo, char transa, char diag, int64_t m, int64_t n,

@@ -67,6 +67,8 @@ const Config &config() {
     if (s) g_cfg.ozaki_slices = atoi(s);
     const char *v = getenv("GB_VERBOSE");
     if (v) g_cfg.verbose = atoi(v);
+    const char *sm = getenv("GB_SGEMM_MODE");
+    if (sm) g_cfg.sgemm_mode = !strcmp(sm, "simt") ? 1 : !strcmp(sm, "tensor") ? 2 : 0;
     const char *g = getenv("GB_OZAKI_GROUP_M");
     if (g && atoi(g) > 0) g_cfg.ozaki_group_m = atoi(g);
   });
@@ -271,6 +273,18 @@ int gb_last_xerbla(char *name, int len) {
 
 static thread_local int t_dgemm_mode = -1;
 static thread_local int t_ozaki_slices = -1;
+static thread_local int t_sgemm_mode = -1;
+
+int gb_set_sgemm_mode(int mode) {
+  if (mode < GB_SGEMM_AUTO || mode > GB_SGEMM_TENSOR)
+    return gb::set_error(GB_ERR_INVALID_VALUE, "gb_set_sgemm_mode: bad mode %d", mode);
+  t_sgemm_mode = mode;
+  return GB_SUCCESS;
+}
+
+int gb_get_sgemm_mode(void) {
+  return t_sgemm_mode >= 0 ? t_sgemm_mode : gb::config().sgemm_mode;
+}
 
 int gb_set_dgemm_mode(int mode) {
   if (mode < GB_DGEMM_NATIVE || mode > GB_DGEMM_AUTO)

@@ -84,6 +84,7 @@ struct Config {
   int dgemm_mode = GB_DGEMM_NATIVE;   // GB_DGEMM_MODE=native|emulated|auto
   int ozaki_slices = 0;               // GB_OZAKI_SLICES (0 = auto)
   int verbose = 0;                    // GB_VERBOSE
+  int sgemm_mode = 0;                 // GB_SGEMM_MODE: 0 auto, 1 simt, 2 tensor
   int ozaki_group_m = 8;              // GB_OZAKI_GROUP_M: m-tiles per slice-GEMM tile group
 };
 const Config &config();
@@ -113,5 +114,16 @@ int sm_count();
 void launch_sgemm_fp32(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha,
                        const float *A, int64_t lda, const float *B, int64_t ldb,
                        float beta, float *C, int64_t ldc, cudaStream_t s);
+// FP32 GEMM on the bf16 tensor cores (three-term split, FP32 accuracy).
+// Assumes m, n, k > 0.
+int sgemm_tc(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha, const float *A,
+             int64_t lda, const float *B, int64_t ldb, float beta, float *C, int64_t ldc,
+             cudaStream_t s);
+// FP32 GEMM behind sgemm_/cblas_sgemm and the FP32 LU: the tensor-core form
+// for shapes large enough to fill the GPU (GB_SGEMM_MODE=auto, default), or
+// always SIMT / always tensor (GB_SGEMM_MODE=simt|tensor).
+int sgemm_dispatch(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha, const float *A,
+                   int64_t lda, const float *B, int64_t ldb, float beta, float *C, int64_t ldc,
+                   cudaStream_t s);
 
 }  // namespace gb

@@ -196,14 +196,22 @@ getf2_panel_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__res
           bi = oi;
         }
       }
-      if (lane == 0) s_p = bi;
+      if (lane == 0) {
+        // IAMAX starts from |a_jj| and only a larger value moves it: a NaN at
+        // row j (or no comparable entry at all) keeps row j (-1 below)
+        const T ajj = __ldcg(rowj_buf + (int64_t)par * PANEL_NB + j);
+        s_p = (bi == INT64_MAX || ajj != ajj) ? -1 : bi;
+      }
     }
     __syncthreads();
-    const int64_t p = s_p;
+    const bool none = s_p < 0;
+    const int64_t p = none ? (int64_t)j : s_p;  // keep row j, as a first-index IAMAX does
     const unsigned owner = (unsigned)((p % nthreads) / PANEL_THREADS);
     if (threadIdx.x < PANEL_NB) {
-      s_u[threadIdx.x] = __ldcg(cand + ((int64_t)par * nblocks + owner) * W + threadIdx.x);
-      s_oldj[threadIdx.x] = __ldcg(rowj_buf + (int64_t)par * PANEL_NB + threadIdx.x);
+      const T oj = __ldcg(rowj_buf + (int64_t)par * PANEL_NB + threadIdx.x);
+      s_u[threadIdx.x] =
+          none ? oj : __ldcg(cand + ((int64_t)par * nblocks + owner) * W + threadIdx.x);
+      s_oldj[threadIdx.x] = oj;
     }
     __syncthreads();
     T piv = s_u[0];
@@ -373,55 +381,102 @@ potf2_kernel(int upper, int nb, T *__restrict__ A, int64_t lda, int *__restrict_
   if (tid == 0 && s_fail >= 0) *info = (int)(row_off + s_fail + 1);
 }
 
-// Panel LU on one thread-block cluster (up to 16 CTAs of 512 threads).
-// Same algorithm and pivot rules as getf2_panel_kernel, but the panel rows
-// live in shared memory, the per-column exchange of candidate rows goes
-// through distributed shared memory and the per-column synchronisation is the
-// hardware cluster barrier -- no global-memory round trips on the critical
-// path.  Rows per thread: L (<= 3 for float, 1 for double).
 constexpr int CPANEL_THREADS = 512;
 constexpr int CPANEL_WARPS = CPANEL_THREADS / 32;
 constexpr int CPANEL_LD = PANEL_NB + 1;  // padded row stride in shared memory
 
 template <typename T>
 __host__ __device__ constexpr size_t cpanel_smem_bytes(int L) {
-  return (size_t)L * CPANEL_THREADS * CPANEL_LD * sizeof(T)  // rows
-         + 6 * PANEL_NB * sizeof(T)                            // cand rows, row j, u, old j
-         + 2 * sizeof(T) + 2 * sizeof(long long)               // cand (value, index) x2
-         + CPANEL_WARPS * (sizeof(T) + sizeof(long long)) + 64;
+  return (size_t)L * CPANEL_THREADS * CPANEL_LD * sizeof(T)             // rows
+         + (size_t)(4 + 2 * CPANEL_WARPS) * PANEL_NB * sizeof(T)        // exchanged rows
+         + (size_t)(2 + 2 * CPANEL_WARPS) * sizeof(T)                   // values
+         + 8 + (size_t)(2 + 2 * CPANEL_WARPS) * sizeof(long long)       // indices
+         + 64;
 }
 
+// First maximum of (value, row) pairs over a warp: the largest value, the
+// lowest row among equal values (IAMAX order).  An empty entry is (-1,
+// LLONG_MAX).  Every lane receives the result.
+template <typename T>
+__device__ __forceinline__ void warp_argmax(T &v, long long &i) {
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const T ov = __shfl_xor_sync(0xffffffffu, v, off);
+    const long long oi = __shfl_xor_sync(0xffffffffu, i, off);
+    if (ov > v || (ov == v && oi < i)) {
+      v = ov;
+      i = oi;
+    }
+  }
+}
+// FP32: the bits of a non-negative float order like the value, so the
+// maximum is one integer reduction and the first row among the maxima a
+// second (rows < 2^31).
+template <>
+__device__ __forceinline__ void warp_argmax<float>(float &v, long long &i) {
+  const unsigned key = v < 0.f ? 0u : __float_as_uint(v) + 1u;
+  const unsigned kmax = __reduce_max_sync(0xffffffffu, key);
+  const unsigned ik = key == kmax ? (unsigned)i : 0xffffffffu;
+  const unsigned imin = __reduce_min_sync(0xffffffffu, ik);
+  v = kmax == 0u ? -1.f : __uint_as_float(kmax - 1u);
+  i = imin == 0xffffffffu ? LLONG_MAX : (long long)imin;
+}
+
+// Panel LU on one thread-block cluster (up to 16 CTAs of 512 threads).
+// Same algorithm and pivot rules as getf2_panel_kernel, but the panel rows
+// live in shared memory and the per-column exchange goes through distributed
+// shared memory.  Per column there is one CTA barrier and one cluster
+// barrier; everything else is done by each warp on its own: it reduces the
+// warps' candidates to the CTA's first maximum, the warp holding that row
+// (or row j) publishes it, and after the cluster barrier every warp fetches
+// the CTAs' candidates, picks the pivot and copies the pivot row and old row
+// j into a private buffer (lane c holds column c; the panel is one warp
+// wide).  Published data and reduction slots alternate between two buffers
+// by column parity: a buffer is rewritten two columns later, after the
+// barrier that every reader of the earlier column has passed.  Rows per
+// thread: L (<= 3 for float, 1 for double).
 template <typename T>
 __global__ void __launch_bounds__(CPANEL_THREADS, 1)
 getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__restrict__ ipiv,
                      int64_t row_off, int *__restrict__ info, int L) {
+  static_assert(PANEL_NB == 32, "one lane per panel column");
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   const int CS = (int)cluster.num_blocks();
   const int rank = (int)cluster.block_rank();
   extern __shared__ __align__(16) unsigned char smem_raw[];
   T *rows = reinterpret_cast<T *>(smem_raw);
-  T *cand_row = rows + (size_t)L * CPANEL_THREADS * CPANEL_LD;  // [2][NB]
-  T *rowj = cand_row + 2 * PANEL_NB;                             // [2][NB]
-  T *s_u = rowj + 2 * PANEL_NB;                                  // [NB]
-  T *s_oldj = s_u + PANEL_NB;                                    // [NB]
-  T *cand_val = s_oldj + PANEL_NB;                               // [2]
+  T *cand_row = rows + (size_t)L * CPANEL_THREADS * CPANEL_LD;  // [2][NB] published
+  T *rowj = cand_row + 2 * PANEL_NB;                             // [2][NB] published
+  T *wu = rowj + 2 * PANEL_NB;                                   // [WARPS][NB] pivot row
+  T *woj = wu + CPANEL_WARPS * PANEL_NB;                         // [WARPS][NB] old row j
+  T *cand_val = woj + CPANEL_WARPS * PANEL_NB;                   // [2] published
+  T *red_val = cand_val + 2;                                     // [2][WARPS]
   long long *cand_idx = reinterpret_cast<long long *>(
-      (reinterpret_cast<uintptr_t>(cand_val + 2) + 7) & ~uintptr_t(7));  // [2]
-  T *red_val = reinterpret_cast<T *>(cand_idx + 2);                    // [WARPS]
-  long long *red_idx = reinterpret_cast<long long *>(
-      (reinterpret_cast<uintptr_t>(red_val + CPANEL_WARPS) + 7) & ~uintptr_t(7));
-  __shared__ long long s_best, s_p;
+      (reinterpret_cast<uintptr_t>(red_val + 2 * CPANEL_WARPS) + 7) & ~uintptr_t(7));  // [2]
+  long long *red_idx = cand_idx + 2;  // [2][WARPS]
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  // rows are dealt to the cluster's threads round robin: row r sits with
+  // thread (r mod nthr), slot (r div nthr).  nthr is a power of two (the
+  // cluster size is), so both are a mask and a shift -- no 64-bit division
+  // on the per-column path
   const int64_t nthr = (int64_t)CS * CPANEL_THREADS;
+  const int lg_nthr = __ffsll(nthr) - 1;
+  const int64_t nmask = nthr - 1;
   const int64_t g = (int64_t)rank * CPANEL_THREADS + tid;
   auto row_ptr = [&](int q) { return rows + ((size_t)q * CPANEL_THREADS + tid) * CPANEL_LD; };
+  T *my_u = wu + warp * PANEL_NB;
+  T *my_oj = woj + warp * PANEL_NB;
 
   for (int q = 0; q < L; ++q) {
     const int64_t r = g + q * nthr;
     T *v = row_ptr(q);
-    for (int c = 0; c < PANEL_NB; ++c) v[c] = (r < m && c < nb) ? A[r + c * lda] : T(0);
+    T tmp[PANEL_NB];  // all loads of the row in flight before the shared stores
+#pragma unroll
+    for (int c = 0; c < PANEL_NB; ++c) tmp[c] = (r < m && c < nb) ? A[r + c * lda] : T(0);
+#pragma unroll
+    for (int c = 0; c < PANEL_NB; ++c) v[c] = tmp[c];
   }
   cluster.sync();
 
@@ -442,87 +497,59 @@ getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__r
         }
       }
     }
-#pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      T ob = __shfl_down_sync(0xffffffffu, best, off);
-      long long oi = __shfl_down_sync(0xffffffffu, bidx, off);
-      if (ob > best || (ob == best && oi < bidx)) {
-        best = ob;
-        bidx = oi;
-      }
-    }
+    warp_argmax<T>(best, bidx);
     if (lane == 0) {
-      red_val[warp] = best;
-      red_idx[warp] = bidx;
+      red_val[par * CPANEL_WARPS + warp] = best;
+      red_idx[par * CPANEL_WARPS + warp] = bidx;
     }
     __syncthreads();
-    if (warp == 0) {
-      T bb = lane < CPANEL_WARPS ? red_val[lane] : T(-1);
-      long long bi = lane < CPANEL_WARPS ? red_idx[lane] : LLONG_MAX;
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        T ob = __shfl_down_sync(0xffffffffu, bb, off);
-        long long oi = __shfl_down_sync(0xffffffffu, bi, off);
-        if (ob > bb || (ob == bb && oi < bi)) {
-          bb = ob;
-          bi = oi;
-        }
-      }
-      if (lane == 0) {
-        cand_val[par] = bb;
-        cand_idx[par] = (bi == LLONG_MAX) ? -1 : bi;
-        s_best = bi;
-      }
+    // ---- every warp: the CTA's candidate; its holder and row j's holder publish
+    T cb = lane < CPANEL_WARPS ? red_val[par * CPANEL_WARPS + lane] : T(-1);
+    long long ci = lane < CPANEL_WARPS ? red_idx[par * CPANEL_WARPS + lane] : LLONG_MAX;
+    warp_argmax<T>(cb, ci);
+    if (ci != LLONG_MAX) {
+      const int lt = (int)((ci & nmask) - (int64_t)rank * CPANEL_THREADS);
+      if ((lt >> 5) == warp)
+        cand_row[par * PANEL_NB + lane] =
+            rows[((size_t)(ci >> lg_nthr) * CPANEL_THREADS + lt) * CPANEL_LD + lane];
     }
-    __syncthreads();
-    // publish the CTA's best row and (if held here) row j, one column per thread
-    if (tid < PANEL_NB) {
-      const long long b = s_best;
-      if (b != LLONG_MAX) {
-        const int64_t gt = b % nthr, q = b / nthr;
-        const int lt = (int)(gt - (int64_t)rank * CPANEL_THREADS);
-        cand_row[par * PANEL_NB + tid] = rows[((size_t)q * CPANEL_THREADS + lt) * CPANEL_LD + tid];
-      }
-      const int64_t gj = (int64_t)j % nthr, qj = (int64_t)j / nthr;
-      if (gj / CPANEL_THREADS == rank) {
-        const int lt = (int)(gj - (int64_t)rank * CPANEL_THREADS);
-        rowj[par * PANEL_NB + tid] = rows[((size_t)qj * CPANEL_THREADS + lt) * CPANEL_LD + tid];
-      }
+    if (warp == 0 && lane == 0) {
+      cand_val[par] = cb;
+      cand_idx[par] = (ci == LLONG_MAX) ? -1 : ci;
+    }
+    const int64_t gj = (int64_t)j & nmask, qj = (int64_t)j >> lg_nthr;
+    const int jowner = (int)(gj / CPANEL_THREADS);
+    if (jowner == rank) {
+      const int lt = (int)(gj - (int64_t)rank * CPANEL_THREADS);
+      if ((lt >> 5) == warp)
+        rowj[par * PANEL_NB + lane] = rows[((size_t)qj * CPANEL_THREADS + lt) * CPANEL_LD + lane];
     }
     cluster.sync();  // candidates of column j visible cluster-wide
-    // ---- global pivot (identical in every CTA): first maximum over the CTAs
-    if (warp == 0) {
-      T bb = T(-1);
-      long long bi = LLONG_MAX;
-      if (lane < CS) {
-        const T val = *cluster.map_shared_rank(cand_val + par, lane);
-        const long long idx = *cluster.map_shared_rank(cand_idx + par, lane);
-        if (idx >= 0) {
-          bb = val;
-          bi = idx;
-        }
+    // ---- every warp: global pivot (identical everywhere), pivot row, old row j
+    const T oj = *cluster.map_shared_rank(rowj + par * PANEL_NB + lane, jowner);
+    T gb = T(-1);
+    long long gi = LLONG_MAX;
+    if (lane < CS) {
+      const long long idx = *cluster.map_shared_rank(cand_idx + par, lane);
+      const T val = *cluster.map_shared_rank(cand_val + par, lane);
+      if (idx >= 0) {
+        gb = val;
+        gi = idx;
       }
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) {
-        T ob = __shfl_down_sync(0xffffffffu, bb, off);
-        long long oi = __shfl_down_sync(0xffffffffu, bi, off);
-        if (ob > bb || (ob == bb && oi < bi)) {
-          bb = ob;
-          bi = oi;
-        }
-      }
-      if (lane == 0) s_p = bi;
     }
-    __syncthreads();
-    const int64_t p = s_p;
-    if (tid < PANEL_NB) {
-      const int owner = (int)((p % nthr) / CPANEL_THREADS);
-      const int jowner = (int)(((int64_t)j % nthr) / CPANEL_THREADS);
-      s_u[tid] = *cluster.map_shared_rank(cand_row + par * PANEL_NB + tid, owner);
-      s_oldj[tid] = *cluster.map_shared_rank(rowj + par * PANEL_NB + tid, jowner);
-    }
-    __syncthreads();
-    const T piv = s_u[j];
+    warp_argmax<T>(gb, gi);
+    // IAMAX starts from |a_jj| and only a larger value moves it: a NaN at row
+    // j (or no comparable entry at all) keeps row j
+    const T ajj = __shfl_sync(0xffffffffu, oj, j);
+    const bool keep = gi == LLONG_MAX || ajj != ajj;
+    const int64_t p = keep ? (int64_t)j : gi;
+    const T u = keep ? oj
+                     : *cluster.map_shared_rank(cand_row + par * PANEL_NB + lane,
+                                                (int)((gi & nmask) / CPANEL_THREADS));
+    my_u[lane] = u;
+    my_oj[lane] = oj;
+    __syncwarp();
+    const T piv = __shfl_sync(0xffffffffu, u, j);
     const T apiv = piv < T(0) ? -piv : piv;
     const bool nonzero = piv != T(0);
     const bool scaled = nonzero && apiv >= tiny_pivot<T>();  // getf2_k.c:103-116
@@ -538,18 +565,18 @@ getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__r
       T *v = row_ptr(q);
       if (swap && i == j) {
         for (int c = 0; c < PANEL_NB; ++c)
-          if (scaled || c > j) v[c] = s_u[c];
+          if (scaled || c > j) v[c] = my_u[c];
         continue;  // the pivot row is final
       }
       if (swap && i == p) {
         for (int c = 0; c < PANEL_NB; ++c)
-          if (scaled || c > j) v[c] = s_oldj[c];
+          if (scaled || c > j) v[c] = my_oj[c];
       }
       if (i == j) continue;
       T l = v[j];
       if (scaled) l *= rcp;
       v[j] = l;
-      for (int c = j + 1; c < PANEL_NB; ++c) v[c] = fma(-l, s_u[c], v[c]);
+      for (int c = j + 1; c < PANEL_NB; ++c) v[c] = fma(-l, my_u[c], v[c]);
     }
   }
   for (int q = 0; q < L; ++q) {
@@ -757,6 +784,120 @@ __global__ void laswp_scatter_kernel(int64_t ncols, T *__restrict__ A, int64_t l
   }
 }
 
+// Interchange sequences of up to LASWP_FUSED_MAX steps in one launch, any
+// incx.  Every CTA replays the sequence on slot indices in shared memory
+// (slot s < cnt is row k1-1+s of the window; slot cnt+t stands for the pivot
+// row of step t outside the window, deduplicated to its first step), which
+// gives the final source of every touched row; the CTA then gathers the
+// moved rows of its columns into shared memory and writes them back.  The
+// result equals applying the interchanges one after another
+// (lapack/laswp/generic/laswp_k_1.c), at the cost of two memory round trips
+// instead of one per interchange.
+constexpr int LASWP_FUSED_MAX = 256;
+constexpr int LASWP_FUSED_ELEMS = 4096;
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+laswp_fused_kernel(int64_t n, T *__restrict__ A, int64_t lda, int64_t k1, int64_t k2,
+                   const int *__restrict__ ipiv, int64_t incx, int cols_per_cta) {
+  __shared__ int prow[LASWP_FUSED_MAX];
+  __shared__ int slotp[LASWP_FUSED_MAX];
+  __shared__ int pos[2 * LASWP_FUSED_MAX];
+  __shared__ int moved[2 * LASWP_FUSED_MAX];
+  __shared__ int nmoved;
+  __shared__ T vals[LASWP_FUSED_ELEMS];
+  const int cnt = (int)(k2 - k1 + 1);
+  const int64_t w0 = k1 - 1;
+  const int64_t ainc = incx < 0 ? -incx : incx;
+  const int tid = threadIdx.x;
+  for (int t = tid; t < cnt; t += blockDim.x) {
+    const int64_t i = incx > 0 ? k1 + t : k2 - t;  // 1-based row of step t
+    prow[t] = ipiv[(k1 - 1) + (i - k1) * ainc] - 1;
+  }
+  for (int sl = tid; sl < 2 * cnt; sl += blockDim.x) pos[sl] = sl;
+  if (tid == 0) nmoved = 0;
+  __syncthreads();
+  for (int t = tid; t < cnt; t += blockDim.x) {
+    const int p = prow[t];
+    int sp;
+    if (p >= w0 && p < w0 + cnt) {
+      sp = (int)(p - w0);
+    } else {
+      int c = t;
+      for (int u = 0; u < t; ++u)
+        if (prow[u] == p) {
+          c = u;
+          break;
+        }
+      sp = cnt + c;
+    }
+    slotp[t] = sp;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    // pos[s] = slot whose original row ends up in slot s
+    for (int t = 0; t < cnt; ++t) {
+      const int si = incx > 0 ? t : cnt - 1 - t;
+      const int sp = slotp[t];
+      if (sp != si) {
+        const int a = pos[si];
+        pos[si] = pos[sp];
+        pos[sp] = a;
+      }
+    }
+  }
+  __syncthreads();
+  for (int sl = tid; sl < 2 * cnt; sl += blockDim.x) {
+    const bool active = sl < cnt || slotp[sl - cnt] == sl;
+    if (active && pos[sl] != sl) moved[atomicAdd(&nmoved, 1)] = sl;
+  }
+  __syncthreads();
+  const int nm = nmoved;
+  if (nm == 0) return;
+  auto row_of = [&](int sl) -> int64_t { return sl < cnt ? w0 + sl : (int64_t)prow[sl - cnt]; };
+  // the plan is reused for every column chunk this CTA visits; within a
+  // chunk each thread keeps 8 loads in flight before it stores to shared
+  const int64_t nchunks = (n + cols_per_cta - 1) / cols_per_cta;
+  for (int64_t ch = blockIdx.x; ch < nchunks; ch += gridDim.x) {
+    const int64_t c0 = ch * cols_per_cta;
+    const int nc = (int)((n - c0) < cols_per_cta ? (n - c0) : cols_per_cta);
+    const int total = nm * nc;
+    for (int e0 = tid; e0 < total; e0 += 8 * 256) {
+      T v[8];
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int e = e0 + u * 256;
+        if (e < total) {
+          const int c = e / nm, q = e - c * nm;
+          v[u] = A[row_of(pos[moved[q]]) + (c0 + c) * lda];
+        }
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u)
+        if (e0 + u * 256 < total) vals[e0 + u * 256] = v[u];
+    }
+    __syncthreads();
+    for (int e = tid; e < total; e += 256) {
+      const int c = e / nm, q = e - c * nm;
+      A[row_of(moved[q]) + (c0 + c) * lda] = vals[e];
+    }
+    __syncthreads();
+  }
+}
+
+template <typename T>
+int launch_laswp_fused(int64_t n, T *A, int64_t lda, int64_t k1, int64_t k2, const int *ipiv,
+                       int64_t incx, cudaStream_t s) {
+  const int64_t cnt = k2 - k1 + 1;
+  int cols = (int)(LASWP_FUSED_ELEMS / (2 * cnt));
+  if (cols < 1) cols = 1;
+  int64_t grid = (n + cols - 1) / cols;
+  const int64_t cap = (int64_t)sm_count() * 2;
+  if (grid > cap) grid = cap;
+  { laswp_fused_kernel<T><<<(unsigned)grid, 256, 0, s>>>(n, A, lda, k1, k2, ipiv, incx, cols); count_launch(); }
+  return check_cuda(cudaGetLastError(), "laswp launch");
+}
+
 constexpr int64_t LASWP_SEQ_MAX = 64;          // short sequences: per-column kernel
 constexpr int64_t LASWP_PLAN_SMEM_ROWS = 50000;  // index vector must fit in shared memory
 
@@ -765,6 +906,7 @@ int laswp_device_rows(int64_t n, T *A, int64_t lda, int64_t k1, int64_t k2, cons
                       int64_t incx, int64_t rows, cudaStream_t s) {
   if (n <= 0 || incx == 0 || k2 < k1) return GB_SUCCESS;
   const int64_t cnt = k2 - k1 + 1;
+  if (cnt <= LASWP_FUSED_MAX) return launch_laswp_fused<T>(n, A, lda, k1, k2, ipiv, incx, s);
   const int64_t range = rows - (k1 - 1);
   if (incx != 1 || cnt <= LASWP_SEQ_MAX || rows <= 0 || range > LASWP_PLAN_SMEM_ROWS ||
       n < 4) {
@@ -800,6 +942,7 @@ template <typename T>
 int laswp_device(int64_t n, T *A, int64_t lda, int64_t k1, int64_t k2, const int *ipiv,
                  int64_t incx, cudaStream_t s) {
   if (n <= 0 || incx == 0 || k2 < k1) return GB_SUCCESS;
+  if (k2 - k1 + 1 <= LASWP_FUSED_MAX) return launch_laswp_fused<T>(n, A, lda, k1, k2, ipiv, incx, s);
   { laswp_kernel<T><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(n, A, lda, k1, k2, ipiv, incx); count_launch(); }
   return check_cuda(cudaGetLastError(), "laswp launch");
 }
@@ -845,8 +988,7 @@ int lu_update<double>(LuCtx<double> &c, int64_t m, int64_t n, int64_t k, const d
 template <>
 int lu_update<float>(LuCtx<float> &c, int64_t m, int64_t n, int64_t k, const float *A21,
                      const float *A12, float *A22) {
-  gemm_minus<float>(m, n, k, A21, c.lda, A12, c.lda, A22, c.lda, c.s);
-  return GB_SUCCESS;
+  return sgemm_dispatch(0, 0, m, n, k, -1.0f, A21, c.lda, A12, c.lda, 1.0f, A22, c.lda, c.s);
 }
 
 template <typename T>

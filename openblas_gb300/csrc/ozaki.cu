@@ -35,6 +35,7 @@
 #include "gb_internal.h"
 #include "lapack_internal.h"
 #include "sm100_primitives.cuh"
+#include "tma_host.h"
 
 namespace gb {
 
@@ -480,37 +481,9 @@ __global__ void recombine_kernel(int64_t m, int64_t n, int S, int m_tiles, int64
 }
 
 // ------------------------------------------------------------------ host
-typedef CUresult (*EncodeTiledFn)(CUtensorMap *, CUtensorMapDataType, cuuint32_t, void *,
-                                  const cuuint64_t *, const cuuint64_t *, const cuuint32_t *,
-                                  const cuuint32_t *, CUtensorMapInterleave, CUtensorMapSwizzle,
-                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
-
-EncodeTiledFn encode_fn() {
-  static EncodeTiledFn fn = nullptr;
-  if (!fn) {
-    void *p = nullptr;
-    cudaDriverEntryPointQueryResult q;
-    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
-                                         &q) == cudaSuccess &&
-        q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<EncodeTiledFn>(p);
-  }
-  return fn;
-}
-
 // 2-D tensor map over `rows` x `kpad` bf16 (K innermost), box 64 x box_rows.
 int make_map(CUtensorMap *map, void *base, int64_t rows, int64_t kpad, int box_rows) {
-  EncodeTiledFn fn = encode_fn();
-  if (!fn) return set_error(GB_ERR_CUDA, "cuTensorMapEncodeTiled unavailable");
-  cuuint64_t dims[2] = {(cuuint64_t)kpad, (cuuint64_t)rows};
-  cuuint64_t strides[1] = {(cuuint64_t)kpad * 2};
-  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
-  cuuint32_t estr[2] = {1, 1};
-  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, base, dims, strides, box, estr,
-                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
-                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
-  if (r != CUDA_SUCCESS) return set_error(GB_ERR_CUDA, "cuTensorMapEncodeTiled failed (%d)", (int)r);
-  return GB_SUCCESS;
+  return make_bf16_kmajor_map(map, base, rows, kpad, BK, box_rows);
 }
 
 inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }

@@ -117,6 +117,59 @@ def test_sgemm_large(F, gb_clean):
     assert np.max(np.abs(Cm - ref) / (feps * G)) <= (k + 2)
 
 
+@pytest.fixture
+def sgemm_tensor(gblib):
+    gblib.gb_set_sgemm_mode(2)   # GB_SGEMM_TENSOR
+    yield
+    gblib.gb_set_sgemm_mode(0)
+
+
+def _sgemm_ref(ta, tb, alpha, A, B, beta, C0, m, n, k):
+    a = A.astype(np.float64)[:m if ta == "N" else k, :k if ta == "N" else m]
+    b = B.astype(np.float64)[:k if tb == "N" else n, :n if tb == "N" else k]
+    oa = a if ta == "N" else a.T
+    ob = b if tb == "N" else b.T
+    c0 = C0.astype(np.float64)[:m, :n]
+    ref = alpha * oa @ ob + beta * c0
+    G = abs(alpha) * np.abs(oa) @ np.abs(ob) + abs(beta) * np.abs(c0)
+    return ref, G
+
+
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("N", "T"), ("T", "N"), ("T", "T")])
+def test_sgemm_tensor_cores(F, gb_clean, sgemm_tensor, ta, tb):
+    """FP32 GEMM through the bf16x3 tensor-core form: ragged tiles (m, n, k not
+    multiples of 128, 256, 64), padded leading dimensions, alpha/beta; the
+    DMMCH-style ratio stays within the FP32 GEMM bound k + 2."""
+    m, n, k = 1100, 1300, 333
+    A, B, Cm = W.gemm_operands(79, m, n, k, ta, tb, pad=5, dtype=np.float32)
+    C0 = Cm.copy(order="F")
+    F.sgemm(ta, tb, m, n, k, -0.75, A, A.shape[0], B, B.shape[0], 1.25, Cm, Cm.shape[0])
+    ref, G = _sgemm_ref(ta, tb, -0.75, A, B, 1.25, C0, m, n, k)
+    feps = np.finfo(np.float32).eps
+    assert np.max(np.abs(Cm[:m, :n] - ref) / (feps * G)) <= k + 2
+    assert np.array_equal(Cm[m:], C0[m:])          # padding rows untouched
+
+
+def test_sgemm_tensor_beta_zero_and_specials(F, gb_clean, sgemm_tensor):
+    """beta = 0 overwrites C without reading it (NaN in C is not propagated);
+    Inf in A propagates as in an FP32 product."""
+    m, n, k = 700, 520, 130
+    A, B, Cm = W.gemm_operands(80, m, n, k, dtype=np.float32)
+    Cm[:] = np.nan
+    A[3, 7] = np.inf
+    F.sgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, Cm, m)
+    with np.errstate(invalid="ignore"):
+        ref = A.astype(np.float64) @ B.astype(np.float64)
+    fin = np.isfinite(ref)
+    assert np.array_equal(np.isposinf(Cm), np.isposinf(ref))
+    assert np.array_equal(np.isneginf(Cm), np.isneginf(ref))
+    G = np.abs(A[np.isfinite(A).all(axis=1)].astype(np.float64)) @ np.abs(B.astype(np.float64))
+    rows = np.isfinite(A).all(axis=1)
+    feps = np.finfo(np.float32).eps
+    assert np.max(np.abs(Cm[rows] - ref[rows]) / (feps * G)) <= k + 2
+    assert fin[rows].all()
+
+
 def test_dtrsm_golden_cases(golden, F, gb_clean):
     idx = 0
     for (m, n) in GG.TRSM_SHAPES:

@@ -103,6 +103,30 @@ def test_dgetrf_tiny_pivot_rule(orc, F, gb_clean):
     assert np.max(np.abs(A - Ao)) <= 1e-9 * np.abs(Ao).max()
 
 
+@pytest.mark.parametrize("m,n,where", [
+    (300, 300, "column"),   # column 5 all NaN: every later pivot search sees NaN at row j
+    (300, 300, "entry"),    # one NaN below the diagonal: skipped, then met at its own step
+    (9000, 40, "entry"),    # taller than one cluster: grid-wide panel kernel
+])
+def test_dgetrf_nan_pivot_rule(orc, F, gb_clean, m, n, where):
+    """IAMAX order with NaN (getf2_k.c pivot search): the running maximum starts
+    at |a_jj| and only a larger value replaces it, so a NaN elsewhere never wins
+    and a NaN at row j keeps row j.  Pivots stay in range and match the oracle."""
+    A0 = W.uniform(7900 + m, (m, n))
+    if where == "column":
+        A0[:, 5] = np.nan
+    else:
+        A0[11, 3] = np.nan
+    A, Ao = A0.copy(order="F"), A0.copy(order="F")
+    p, po = np.zeros(min(m, n), np.int32), np.zeros(min(m, n), np.int32)
+    assert F.dgetrf(m, n, A, m, p) == orc.dgetrf(m, n, Ao, m, po)
+    assert p.min() >= 1 and p.max() <= m
+    assert np.array_equal(p, po)
+    fin = np.isfinite(Ao)
+    assert np.array_equal(fin, np.isfinite(A))
+    assert np.max(np.abs(A[fin] - Ao[fin]), initial=0.0) <= 1e-9 * np.abs(Ao[fin]).max()
+
+
 def test_dgetrs_dgesv(golden, F, gb_clean):
     for t, trans in enumerate("NT"):
         for nrhs in (1, 5):
@@ -188,6 +212,24 @@ def test_dlaswp_golden(golden, F, gb_clean):
         ipiv = golden[f"dlaswp_{idx}_ipiv"].astype(np.int32)
         F.dlaswp(n, A, rows, k1, k2, ipiv, incx)
         assert np.array_equal(A, golden[f"dlaswp_{idx}"]), (n, k1, k2, incx)
+
+
+@pytest.mark.parametrize("rows,n,k1,k2,incx", [
+    (3000, 500, 5, 260, 1),      # 256 interchanges: one fused launch
+    (3000, 300, 100, 300, -1),   # reverse order
+    (1000, 64, 1, 100, 3),       # strided pivots
+    (3000, 200, 1, 700, 1),      # long sequence: planned gather/scatter path
+    (3000, 40, 1, 700, -2),      # long sequence, reverse strided: per-column path
+])
+def test_dlaswp_random_pivots(orc, F, gb_clean, rows, n, k1, k2, incx):
+    """Random pivot rows above, inside and below the window, with repeats."""
+    A = W.uniform(8600 + k2, (rows, n))
+    npiv = k1 - 1 + (k2 - k1 + 1) * abs(incx)
+    ipiv = W.randint(8700 + k2, (npiv,), 1, rows).astype(np.int32)  # inclusive
+    ref = A.copy(order="F")
+    orc.dlaswp(n, ref, rows, k1, k2, ipiv, incx)
+    F.dlaswp(n, A, rows, k1, k2, ipiv, incx)
+    assert np.array_equal(A, ref)
 
 
 def _sgetrf_dev(gblib, A32):
