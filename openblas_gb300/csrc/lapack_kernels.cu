@@ -384,14 +384,16 @@ potf2_kernel(int upper, int nb, T *__restrict__ A, int64_t lda, int *__restrict_
 constexpr int CPANEL_THREADS = 512;
 constexpr int CPANEL_WARPS = CPANEL_THREADS / 32;
 constexpr int CPANEL_LD = PANEL_NB + 1;  // padded row stride in shared memory
+constexpr int CPANEL_MAX_CS = 16;       // one pushing warp per destination CTA
 
+// Shared memory of the cluster panel kernel: candidate inboxes (rows,
+// values, indices), per-warp candidate rows and row j, by column parity.
 template <typename T>
-__host__ __device__ constexpr size_t cpanel_smem_bytes(int L) {
-  return (size_t)L * CPANEL_THREADS * CPANEL_LD * sizeof(T)             // rows
-         + (size_t)(4 + 2 * CPANEL_WARPS) * PANEL_NB * sizeof(T)        // exchanged rows
-         + (size_t)(2 + 2 * CPANEL_WARPS) * sizeof(T)                   // values
-         + 8 + (size_t)(2 + 2 * CPANEL_WARPS) * sizeof(long long)       // indices
-         + 64;
+__host__ __device__ constexpr size_t cpanel_smem_bytes() {
+  return (size_t)2 * (2 * CPANEL_MAX_CS + 2) * PANEL_NB * sizeof(T)  // inbox + warp rows, row j x2
+         + (size_t)2 * (CPANEL_MAX_CS + CPANEL_WARPS) * sizeof(T)     // inbox/warp values
+         + (size_t)2 * CPANEL_MAX_CS * sizeof(int) + 8                // inbox row indices
+         + (size_t)2 * CPANEL_WARPS * sizeof(long long) + 64;         // warp row indices
 }
 
 // First maximum of (value, row) pairs over a warp: the largest value, the
@@ -423,62 +425,73 @@ __device__ __forceinline__ void warp_argmax<float>(float &v, long long &i) {
 }
 
 // Panel LU on one thread-block cluster (up to 16 CTAs of 512 threads).
-// Same algorithm and pivot rules as getf2_panel_kernel, but the panel rows
-// live in shared memory and the per-column exchange goes through distributed
-// shared memory.  Per column there is one CTA barrier and one cluster
-// barrier; everything else is done by each warp on its own: it reduces the
-// warps' candidates to the CTA's first maximum, the warp holding that row
-// (or row j) publishes it, and after the cluster barrier every warp fetches
-// the CTAs' candidates, picks the pivot and copies the pivot row and old row
-// j into a private buffer (lane c holds column c; the panel is one warp
-// wide).  Published data and reduction slots alternate between two buffers
-// by column parity: a buffer is rewritten two columns later, after the
-// barrier that every reader of the earlier column has passed.  Rows per
-// thread: L (<= 3 for float, 1 for double).
-template <typename T>
+// Same algorithm and pivot rules as getf2_panel_kernel.  Each thread keeps
+// its L panel rows in registers (updates are predicated FMAs with
+// compile-time column indices; the pivot row is read with 16-byte shared
+// loads) and the per-column exchange goes through distributed shared memory
+// by pushing: the lane holding a warp's best row stages it in shared memory,
+// after one CTA barrier every warp knows the CTA's candidate (first maximum
+// of column j over its rows), and warp w writes that candidate -- value, row
+// index and the 32-element row -- into CTA w's inbox (row j is staged and
+// pushed the same way).  Remote stores are posted, so nothing waits on a
+// remote read; after the cluster barrier every CTA picks the pivot from its
+// own inbox.  Inboxes and slots alternate between two buffers by column
+// parity: a buffer is rewritten two columns later, after the barrier every
+// reader of the earlier column has passed.
+template <typename T, int L>
 __global__ void __launch_bounds__(CPANEL_THREADS, 1)
 getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__restrict__ ipiv,
-                     int64_t row_off, int *__restrict__ info, int L) {
+                     int64_t row_off, int *__restrict__ info) {
   static_assert(PANEL_NB == 32, "one lane per panel column");
+  static_assert(CPANEL_WARPS == CPANEL_MAX_CS, "one pushing warp per destination CTA");
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   const int CS = (int)cluster.num_blocks();
   const int rank = (int)cluster.block_rank();
   extern __shared__ __align__(16) unsigned char smem_raw[];
-  T *rows = reinterpret_cast<T *>(smem_raw);
-  T *cand_row = rows + (size_t)L * CPANEL_THREADS * CPANEL_LD;  // [2][NB] published
-  T *rowj = cand_row + 2 * PANEL_NB;                             // [2][NB] published
-  T *wu = rowj + 2 * PANEL_NB;                                   // [WARPS][NB] pivot row
-  T *woj = wu + CPANEL_WARPS * PANEL_NB;                         // [WARPS][NB] old row j
-  T *cand_val = woj + CPANEL_WARPS * PANEL_NB;                   // [2] published
-  T *red_val = cand_val + 2;                                     // [2][WARPS]
-  long long *cand_idx = reinterpret_cast<long long *>(
-      (reinterpret_cast<uintptr_t>(red_val + 2 * CPANEL_WARPS) + 7) & ~uintptr_t(7));  // [2]
-  long long *red_idx = cand_idx + 2;  // [2][WARPS]
+  T *in_row = reinterpret_cast<T *>(smem_raw);                 // [2][CS][NB] candidates
+  T *w_row = in_row + 2 * CPANEL_MAX_CS * PANEL_NB;             // [2][WARPS][NB] warp bests
+  T *in_rowj = w_row + 2 * CPANEL_WARPS * PANEL_NB;             // [2][NB] row j (inbox)
+  T *j_slot = in_rowj + 2 * PANEL_NB;                           // [2][NB] row j (staged)
+  T *in_val = j_slot + 2 * PANEL_NB;                            // [2][CS]
+  T *red_val = in_val + 2 * CPANEL_MAX_CS;                      // [2][WARPS]
+  int *in_idx = reinterpret_cast<int *>(red_val + 2 * CPANEL_WARPS);  // [2][CS]
+  long long *red_idx = reinterpret_cast<long long *>(
+      (reinterpret_cast<uintptr_t>(in_idx + 2 * CPANEL_MAX_CS) + 7) & ~uintptr_t(7));  // [2][WARPS]
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // rows are dealt to the cluster's threads round robin: row r sits with
-  // thread (r mod nthr), slot (r div nthr).  nthr is a power of two (the
-  // cluster size is), so both are a mask and a shift -- no 64-bit division
-  // on the per-column path
+  // thread (r mod nthr), register slot (r div nthr).  nthr is a power of two
+  // (the cluster size is), so both are a mask and a shift
   const int64_t nthr = (int64_t)CS * CPANEL_THREADS;
   const int lg_nthr = __ffsll(nthr) - 1;
   const int64_t nmask = nthr - 1;
   const int64_t g = (int64_t)rank * CPANEL_THREADS + tid;
-  auto row_ptr = [&](int q) { return rows + ((size_t)q * CPANEL_THREADS + tid) * CPANEL_LD; };
-  T *my_u = wu + warp * PANEL_NB;
-  T *my_oj = woj + warp * PANEL_NB;
 
+  T r[L][PANEL_NB];
+  T colv[L];  // current value of column j of each row
+#pragma unroll
   for (int q = 0; q < L; ++q) {
-    const int64_t r = g + q * nthr;
-    T *v = row_ptr(q);
-    T tmp[PANEL_NB];  // all loads of the row in flight before the shared stores
+    const int64_t row = g + q * nthr;
 #pragma unroll
-    for (int c = 0; c < PANEL_NB; ++c) tmp[c] = (r < m && c < nb) ? A[r + c * lda] : T(0);
-#pragma unroll
-    for (int c = 0; c < PANEL_NB; ++c) v[c] = tmp[c];
+    for (int c = 0; c < PANEL_NB; ++c) r[q][c] = (row < m && c < nb) ? A[row + c * lda] : T(0);
+    colv[q] = r[q][0];
   }
-  cluster.sync();
+  cluster.sync();  // every CTA is running before anyone writes into its inbox
+
+  // 32 values of one register row into shared memory, 16 bytes at a time
+  auto stage_row = [&](T *dst, const T (&src)[PANEL_NB]) {
+    if (sizeof(T) == 4) {
+#pragma unroll
+      for (int c = 0; c < PANEL_NB; c += 4)
+        *reinterpret_cast<float4 *>(dst + c) =
+            make_float4((float)src[c], (float)src[c + 1], (float)src[c + 2], (float)src[c + 3]);
+    } else {
+#pragma unroll
+      for (int c = 0; c < PANEL_NB; c += 2)
+        *reinterpret_cast<double2 *>(dst + c) = make_double2((double)src[c], (double)src[c + 1]);
+    }
+  };
 
   const int ncol = (int)(nb < m ? nb : m);
   for (int j = 0; j < ncol; ++j) {
@@ -486,70 +499,81 @@ getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__r
     // ---- local first maximum of |a_ij| over this thread's rows >= j
     T best = T(-1);
     long long bidx = LLONG_MAX;
+#pragma unroll
     for (int q = 0; q < L; ++q) {
-      const int64_t r = g + q * nthr;
-      if (r < m && r >= j) {
-        T a = row_ptr(q)[j];
+      const int64_t row = g + q * nthr;
+      if (row < m && row >= j) {
+        T a = colv[q];
         a = a < T(0) ? -a : a;
-        if (a > best || (a == best && r < bidx)) {
+        if (a > best || (a == best && row < bidx)) {
           best = a;
-          bidx = r;
+          bidx = row;
         }
       }
     }
     warp_argmax<T>(best, bidx);
+    // the lane holding the warp's best row stages it; the holder of row j too
+    if (bidx != LLONG_MAX && (int)(bidx & 31) == lane) {
+      const int qb = (int)(bidx >> lg_nthr);
+#pragma unroll
+      for (int q = 0; q < L; ++q)
+        if (q == qb) stage_row(w_row + (par * CPANEL_WARPS + warp) * PANEL_NB, r[q]);
+    }
     if (lane == 0) {
       red_val[par * CPANEL_WARPS + warp] = best;
       red_idx[par * CPANEL_WARPS + warp] = bidx;
     }
+    const int jowner = (int)(((int64_t)j & nmask) / CPANEL_THREADS);
+    if (jowner == rank && (int)(((int64_t)j & nmask) - (int64_t)rank * CPANEL_THREADS) == tid) {
+      const int qj = (int)((int64_t)j >> lg_nthr);
+#pragma unroll
+      for (int q = 0; q < L; ++q)
+        if (q == qj) stage_row(j_slot + par * PANEL_NB, r[q]);
+    }
     __syncthreads();
-    // ---- every warp: the CTA's candidate; its holder and row j's holder publish
+    // ---- every warp: the CTA's candidate; warp w pushes it (and row j) to CTA w
     T cb = lane < CPANEL_WARPS ? red_val[par * CPANEL_WARPS + lane] : T(-1);
     long long ci = lane < CPANEL_WARPS ? red_idx[par * CPANEL_WARPS + lane] : LLONG_MAX;
     warp_argmax<T>(cb, ci);
-    if (ci != LLONG_MAX) {
-      const int lt = (int)((ci & nmask) - (int64_t)rank * CPANEL_THREADS);
-      if ((lt >> 5) == warp)
-        cand_row[par * PANEL_NB + lane] =
-            rows[((size_t)(ci >> lg_nthr) * CPANEL_THREADS + lt) * CPANEL_LD + lane];
+    if (warp < CS) {
+      const int dst = warp;
+      T rv = T(0);
+      if (ci != LLONG_MAX) {
+        const int wb = (int)(((ci & nmask) - (int64_t)rank * CPANEL_THREADS) >> 5);
+        rv = w_row[(par * CPANEL_WARPS + wb) * PANEL_NB + lane];
+      }
+      *cluster.map_shared_rank(in_row + (par * CPANEL_MAX_CS + rank) * PANEL_NB + lane, dst) = rv;
+      if (lane == 0) {
+        *cluster.map_shared_rank(in_val + par * CPANEL_MAX_CS + rank, dst) = cb;
+        *cluster.map_shared_rank(in_idx + par * CPANEL_MAX_CS + rank, dst) =
+            ci == LLONG_MAX ? -1 : (int)ci;
+      }
+      if (jowner == rank)
+        *cluster.map_shared_rank(in_rowj + par * PANEL_NB + lane, dst) =
+            j_slot[par * PANEL_NB + lane];
     }
-    if (warp == 0 && lane == 0) {
-      cand_val[par] = cb;
-      cand_idx[par] = (ci == LLONG_MAX) ? -1 : ci;
-    }
-    const int64_t gj = (int64_t)j & nmask, qj = (int64_t)j >> lg_nthr;
-    const int jowner = (int)(gj / CPANEL_THREADS);
-    if (jowner == rank) {
-      const int lt = (int)(gj - (int64_t)rank * CPANEL_THREADS);
-      if ((lt >> 5) == warp)
-        rowj[par * PANEL_NB + lane] = rows[((size_t)qj * CPANEL_THREADS + lt) * CPANEL_LD + lane];
-    }
-    cluster.sync();  // candidates of column j visible cluster-wide
-    // ---- every warp: global pivot (identical everywhere), pivot row, old row j
-    const T oj = *cluster.map_shared_rank(rowj + par * PANEL_NB + lane, jowner);
+    cluster.sync();  // every CTA's inbox for column j is complete
+    // ---- global pivot from the local inbox (identical in every CTA)
     T gb = T(-1);
     long long gi = LLONG_MAX;
     if (lane < CS) {
-      const long long idx = *cluster.map_shared_rank(cand_idx + par, lane);
-      const T val = *cluster.map_shared_rank(cand_val + par, lane);
+      const int idx = in_idx[par * CPANEL_MAX_CS + lane];
       if (idx >= 0) {
-        gb = val;
+        gb = in_val[par * CPANEL_MAX_CS + lane];
         gi = idx;
       }
     }
     warp_argmax<T>(gb, gi);
+    const T *rowj_v = in_rowj + par * PANEL_NB;
     // IAMAX starts from |a_jj| and only a larger value moves it: a NaN at row
     // j (or no comparable entry at all) keeps row j
-    const T ajj = __shfl_sync(0xffffffffu, oj, j);
+    const T ajj = rowj_v[j];
     const bool keep = gi == LLONG_MAX || ajj != ajj;
     const int64_t p = keep ? (int64_t)j : gi;
-    const T u = keep ? oj
-                     : *cluster.map_shared_rank(cand_row + par * PANEL_NB + lane,
-                                                (int)((gi & nmask) / CPANEL_THREADS));
-    my_u[lane] = u;
-    my_oj[lane] = oj;
-    __syncwarp();
-    const T piv = __shfl_sync(0xffffffffu, u, j);
+    const T *u_v = keep ? rowj_v
+                        : in_row + (par * CPANEL_MAX_CS + (int)((gi & nmask) / CPANEL_THREADS)) *
+                                       PANEL_NB;
+    const T piv = u_v[j];
     const T apiv = piv < T(0) ? -piv : piv;
     const bool nonzero = piv != T(0);
     const bool scaled = nonzero && apiv >= tiny_pivot<T>();  // getf2_k.c:103-116
@@ -559,33 +583,57 @@ getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__r
       if (!nonzero && *info == 0) *info = (int)(j + row_off + 1);
     }
     const T rcp = scaled ? T(1) / piv : T(1);
+#pragma unroll
     for (int q = 0; q < L; ++q) {
       const int64_t i = g + q * nthr;
       if (i >= m || i < j) continue;
-      T *v = row_ptr(q);
       if (swap && i == j) {
+#pragma unroll
         for (int c = 0; c < PANEL_NB; ++c)
-          if (scaled || c > j) v[c] = my_u[c];
+          if (scaled || c > j) r[q][c] = u_v[c];
         continue;  // the pivot row is final
       }
-      if (swap && i == p) {
+      const bool take_j = swap && i == p;  // row p receives the old row j
+      if (take_j) {
+#pragma unroll
         for (int c = 0; c < PANEL_NB; ++c)
-          if (scaled || c > j) v[c] = my_oj[c];
+          if (scaled || c > j) r[q][c] = rowj_v[c];
       }
       if (i == j) continue;
-      T l = v[j];
+      T l = take_j ? rowj_v[j] : colv[q];
       if (scaled) l *= rcp;
-      v[j] = l;
-      for (int c = j + 1; c < PANEL_NB; ++c) v[c] = fma(-l, my_u[c], v[c]);
+      T nx = T(0);
+#pragma unroll
+      for (int c = 0; c < PANEL_NB; c += 4) {
+        T u4[4];
+        if (sizeof(T) == 4) {
+          const float4 f = *reinterpret_cast<const float4 *>(u_v + c);
+          u4[0] = (T)f.x; u4[1] = (T)f.y; u4[2] = (T)f.z; u4[3] = (T)f.w;
+        } else {
+          const double2 d0 = *reinterpret_cast<const double2 *>(u_v + c);
+          const double2 d1 = *reinterpret_cast<const double2 *>(u_v + c + 2);
+          u4[0] = (T)d0.x; u4[1] = (T)d0.y; u4[2] = (T)d1.x; u4[3] = (T)d1.y;
+        }
+#pragma unroll
+        for (int t = 0; t < 4; ++t) {
+          const int cc = c + t;
+          if (cc == j) r[q][cc] = l;
+          else if (cc > j) r[q][cc] = fma(-l, u4[t], r[q][cc]);
+          if (cc == j + 1) nx = r[q][cc];
+        }
+      }
+      colv[q] = nx;
     }
   }
+#pragma unroll
   for (int q = 0; q < L; ++q) {
-    const int64_t r = g + q * nthr;
-    if (r >= m) continue;
-    const T *v = row_ptr(q);
-    for (int c = 0; c < nb; ++c) A[r + c * lda] = v[c];
+    const int64_t row = g + q * nthr;
+    if (row >= m) continue;
+#pragma unroll
+    for (int c = 0; c < PANEL_NB; ++c)
+      if (c < nb) A[row + c * lda] = r[q][c];
   }
-  cluster.sync();  // no CTA leaves while another may still read its shared memory
+  cluster.sync();  // no CTA leaves while another may still write into its inbox
 }
 
 template <typename T>
@@ -600,15 +648,19 @@ const ClusterPanel<T> &cluster_panel_caps() {
   static bool done = false;
   if (done) return caps;
   done = true;
-  const int lmax = sizeof(T) == 4 ? 3 : 1;
-  const size_t smem = cpanel_smem_bytes<T>(lmax);
-  if (cudaFuncSetAttribute(getf2_cluster_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)smem) != cudaSuccess ||
-      cudaFuncSetAttribute(getf2_cluster_kernel<T>,
-                           cudaFuncAttributeNonPortableClusterSizeAllowed, 1) != cudaSuccess) {
+  // rows per thread held in registers: 2 for float, 1 for double
+  constexpr int lmax = sizeof(T) == 4 ? 2 : 1;
+  const size_t smem = cpanel_smem_bytes<T>();
+  auto kern = getf2_cluster_kernel<T, lmax>;
+  if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
+      cudaSuccess) {
     cudaGetLastError();
     return caps;
   }
+  if constexpr (lmax > 1)
+    cudaFuncSetAttribute(getf2_cluster_kernel<T, 1>, cudaFuncAttributeNonPortableClusterSizeAllowed,
+                         1);
+  cudaGetLastError();
   for (int cs = 16; cs >= 2; cs /= 2) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(cs);
@@ -622,9 +674,7 @@ const ClusterPanel<T> &cluster_panel_caps() {
     cfg.attrs = at;
     cfg.numAttrs = 1;
     int nclusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&nclusters, getf2_cluster_kernel<T>, &cfg) ==
-            cudaSuccess &&
-        nclusters >= 1) {
+    if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg) == cudaSuccess && nclusters >= 1) {
       caps.max_cs = cs;
       caps.lmax = lmax;
       break;
@@ -656,7 +706,7 @@ int launch_cluster_panel(int64_t rows, int nb, T *A, int64_t lda, int *ipiv, int
   cudaLaunchConfig_t cfg = {};
   cfg.gridDim = dim3((unsigned)csp);
   cfg.blockDim = dim3(CPANEL_THREADS);
-  cfg.dynamicSmemBytes = cpanel_smem_bytes<T>((int)L);
+  cfg.dynamicSmemBytes = cpanel_smem_bytes<T>();
   cfg.stream = s;
   cudaLaunchAttribute at[1];
   at[0].id = cudaLaunchAttributeClusterDimension;
@@ -666,9 +716,16 @@ int launch_cluster_panel(int64_t rows, int nb, T *A, int64_t lda, int *ipiv, int
   cfg.attrs = at;
   cfg.numAttrs = 1;
   count_launch();
-  return check_cuda(cudaLaunchKernelEx(&cfg, getf2_cluster_kernel<T>, rows, nb, A, lda, ipiv,
-                                       row_off, info, (int)L),
-                    "cluster panel launch");
+  cudaError_t e = cudaErrorInvalidValue;
+  if (L == 1) {
+    e = cudaLaunchKernelEx(&cfg, getf2_cluster_kernel<T, 1>, rows, nb, A, lda, ipiv, row_off,
+                           info);
+  } else {
+    if constexpr (sizeof(T) == 4)
+      e = cudaLaunchKernelEx(&cfg, getf2_cluster_kernel<T, 2>, rows, nb, A, lda, ipiv, row_off,
+                             info);
+  }
+  return check_cuda(e, "cluster panel launch");
 }
 
 template <typename T, int R>
@@ -723,6 +780,115 @@ int trsm_any<float>(int side, int uplo, int trans, int unit, int64_t m, int64_t 
 }
 
 }  // namespace
+
+// B := L^-1 B for the unit-lower L11 of an LU step (L n1 x n1, n1 <= 256;
+// B n1 x w): the TRSM_ILTCOPY + TRSM_KERNEL_LT pair of the reference's
+// getrf (driver/level3/trsm_L.c with the inverted diagonal of
+// trsm_ltcopy), in one launch.  Each CTA owns 32 columns of B in shared
+// memory; its warps first invert the 32 x 32 diagonal blocks of L11 (lane c
+// solves for column c), then block row i of B gets B_i -= L_ik B_k (k < i,
+// L tiles read from L2, coalesced) and B_i = inv(L_ii) B_i.  Rows past n1
+// are identity padding.
+constexpr int LT_COLS = 32;   // columns of B per CTA
+constexpr int LT_MAXN = 256;  // largest L11
+
+template <typename T>
+__host__ __device__ constexpr size_t lu_trsm_smem(int nblk) {
+  return (size_t)2 * nblk * 32 * (LT_COLS + 1) * sizeof(T);
+}
+
+template <typename T>
+__global__ void __launch_bounds__(256)
+lu_trsm_kernel(int n1, int64_t w, const T *__restrict__ L, int64_t ldl, T *__restrict__ B,
+               int64_t ldb) {
+  extern __shared__ __align__(16) unsigned char smem_raw[];
+  const int nblk = (n1 + 31) / 32;
+  const int nr = nblk * 32;
+  T *Bs = reinterpret_cast<T *>(smem_raw);  // [nr][LT_COLS + 1]
+  T *Li = Bs + nr * (LT_COLS + 1);           // [nblk][32][33]: L_dd, then its inverse
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t c0 = (int64_t)blockIdx.x * LT_COLS;
+  const int nc = (int)((w - c0) < LT_COLS ? (w - c0) : LT_COLS);
+  for (int e = tid; e < nr * LT_COLS; e += 256) {
+    const int r = e % nr, c = e / nr;
+    Bs[r * (LT_COLS + 1) + c] = (r < n1 && c < nc) ? B[r + (c0 + c) * ldb] : T(0);
+  }
+  for (int d = warp; d < nblk; d += 8) {
+    const int b0 = d * 32;
+    T *Ld = Li + d * 32 * 33;
+#pragma unroll 4
+    for (int c = 0; c < 32; ++c) {
+      const bool in = b0 + lane < n1 && b0 + c < n1;
+      Ld[lane * 33 + c] = in ? L[(b0 + lane) + (int64_t)(b0 + c) * ldl] : T(lane == c ? 1 : 0);
+    }
+    __syncwarp();
+    T x[32];  // column `lane` of inv(L_dd) (unit diagonal)
+#pragma unroll
+    for (int r = 0; r < 32; ++r) {
+      T sum = (r == lane) ? T(1) : T(0);
+#pragma unroll
+      for (int k = 0; k < r; ++k) sum = fma(-Ld[r * 33 + k], x[k], sum);
+      x[r] = sum;
+    }
+    __syncwarp();
+#pragma unroll
+    for (int r = 0; r < 32; ++r) Ld[r * 33 + lane] = x[r];
+  }
+  __syncthreads();
+  const int r = lane, cg = warp;  // row r of a block, columns cg*4 .. cg*4+3
+  for (int i = 0; i < nblk; ++i) {
+    T acc[4] = {T(0), T(0), T(0), T(0)};
+    const bool row_in = i * 32 + r < n1;
+    for (int k = 0; k < i; ++k) {
+      const T *lp = L + (int64_t)(i * 32 + r) + (int64_t)(k * 32) * ldl;
+#pragma unroll 8
+      for (int kk = 0; kk < 32; ++kk) {
+        const T l = row_in ? lp[(int64_t)kk * ldl] : T(0);
+        const T *bk = Bs + (k * 32 + kk) * (LT_COLS + 1) + cg * 4;
+#pragma unroll
+        for (int t = 0; t < 4; ++t) acc[t] = fma(l, bk[t], acc[t]);
+      }
+    }
+    T *bi = Bs + (i * 32 + r) * (LT_COLS + 1) + cg * 4;
+#pragma unroll
+    for (int t = 0; t < 4; ++t) bi[t] -= acc[t];
+    __syncthreads();
+    const T *Ld = Li + i * 32 * 33;
+    T y[4] = {T(0), T(0), T(0), T(0)};
+#pragma unroll 8
+    for (int kk = 0; kk < 32; ++kk) {
+      const T l = Ld[r * 33 + kk];
+      const T *bk = Bs + (i * 32 + kk) * (LT_COLS + 1) + cg * 4;
+#pragma unroll
+      for (int t = 0; t < 4; ++t) y[t] = fma(l, bk[t], y[t]);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int t = 0; t < 4; ++t) bi[t] = y[t];
+    __syncthreads();
+  }
+  for (int e = tid; e < nr * LT_COLS; e += 256) {
+    const int rr = e % nr, c = e / nr;
+    if (rr < n1 && c < nc) B[rr + (c0 + c) * ldb] = Bs[rr * (LT_COLS + 1) + c];
+  }
+}
+
+template <typename T>
+int lu_trsm(int64_t n1, int64_t w, const T *L, int64_t ldl, T *B, int64_t ldb, cudaStream_t s) {
+  if (n1 <= 0 || w <= 0) return GB_SUCCESS;
+  if (n1 > LT_MAXN) return trsm_any<T>(0, 1, 0, 0, n1, w, L, ldl, B, ldb, s);
+  const int nblk = (int)((n1 + 31) / 32);
+  const size_t smem = lu_trsm_smem<T>(nblk);
+  static bool attr = false;
+  if (!attr) {
+    GB_CUDA(cudaFuncSetAttribute(lu_trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)lu_trsm_smem<T>(LT_MAXN / 32)));
+    attr = true;
+  }
+  const int64_t grid = (w + LT_COLS - 1) / LT_COLS;
+  { lu_trsm_kernel<T><<<(unsigned)grid, 256, smem, s>>>((int)n1, w, L, ldl, B, ldb); count_launch(); }
+  return check_cuda(cudaGetLastError(), "lu_trsm");
+}
 
 // Parallel form of a long interchange sequence (incx = 1): one block replays
 // the interchanges on an index vector in shared memory, giving the final
@@ -1031,7 +1197,7 @@ int lu_rec(LuCtx<T> &c, int64_t r0, int64_t m, int64_t n) {
   }
   {
     ProfileScope prof("lu_trsm", c.s);
-    if ((st = trsm_any<T>(0, 1, 0, 0, n1, n - n1, L11, lda, A12, lda, c.s))) return st;
+    if ((st = lu_trsm<T>(n1, n - n1, L11, lda, A12, lda, c.s))) return st;
   }
   if (m > n1) {
     {
@@ -1072,7 +1238,7 @@ int lu_blocked(LuCtx<T> &c, int64_t m, int64_t mn, int64_t n) {
       }
       {
         ProfileScope prof("lu_trsm", c.s);
-        if ((st = trsm_any<T>(0, 1, 0, 0, jb, n - j0 - jb, L11, lda, A12, lda, c.s))) return st;
+        if ((st = lu_trsm<T>(jb, n - j0 - jb, L11, lda, A12, lda, c.s))) return st;
       }
       if (j0 + jb < m) {
         ProfileScope prof("lu_gemm", c.s);
