@@ -67,9 +67,6 @@ static int dgemm_native(int ta, int tb, int64_t m, int64_t n, int64_t k, double 
   return check_cuda(cudaGetLastError(), "dgemm launch");
 }
 
-int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
-                   const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
-                   double *C, int64_t ldc, int slices, cudaStream_t s);
 
 // Selected by the DGEMM mode: emulated when requested, or in auto mode when
 // the product is large enough for the split/recombine passes to pay off.

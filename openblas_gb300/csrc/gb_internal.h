@@ -114,6 +114,14 @@ int sm_count();
 void launch_sgemm_fp32(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha,
                        const float *A, int64_t lda, const float *B, int64_t ldb,
                        float beta, float *C, int64_t ldc, cudaStream_t s);
+// Emulated-FP64 GEMM (Ozaki slices on the bf16 tensor cores).  slices = 0:
+// default count.  tri = 1 (2): only C(i,j) with i >= j (i <= j) is written,
+// tiles wholly in the other triangle are skipped (SYRK-shaped updates).
+// skip: device flag; when nonzero at run time C is left unchanged.
+int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
+                   const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
+                   double *C, int64_t ldc, int slices, cudaStream_t s, int tri = 0,
+                   const int *skip = nullptr);
 // FP32 GEMM on the bf16 tensor cores (three-term split, FP32 accuracy).
 // Assumes m, n, k > 0.
 int sgemm_tc(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha, const float *A,

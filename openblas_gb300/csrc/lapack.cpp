@@ -189,7 +189,8 @@ int dpotrf_(const char *UPLO, const blasint *N, double *a, const blasint *ldA, b
   if (A.bind(true, s)) return 0;
   DevInfo di(s);
   if (!di.buf.p) return 0;
-  if (potrf_device(uplo, n, A.d<double>(), A.dld, di.d(), s)) return 0;
+  const int mode = gb_get_dgemm_mode() == GB_DGEMM_NATIVE ? 0 : 1;
+  if (potrf_device(uplo, n, A.d<double>(), A.dld, di.d(), mode, s)) return 0;
   A.unbind(s);
   int h = 0;
   if (di.read(s, &h)) return 0;
@@ -325,7 +326,8 @@ int gb_dpotrf_dev(char uplo, int64_t n, double *A, int64_t lda, int *info) {
     GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), stream()));
     return GB_SUCCESS;
   }
-  return potrf_device(up, n, A, lda, info, stream());
+  const int mode = gb_get_dgemm_mode() == GB_DGEMM_NATIVE ? 0 : 1;
+  return potrf_device(up, n, A, lda, info, mode, stream());
 }
 
 }  // extern "C"

@@ -48,8 +48,10 @@ template <typename T>
 int apply_perm(int64_t n, int64_t ncol, const int *perm, const T *src, int64_t lds, T *dst,
                int64_t ldd, cudaStream_t s);
 
-// Cholesky (lapack/potrf/potrf_{L,U}_single.c); *info_host receives info.
-int potrf_device(int uplo, int64_t n, double *A, int64_t lda, int *info_dev, cudaStream_t s);
+// Cholesky (lapack/potrf/potrf_{L,U}_single.c); *info_dev receives info.
+// gemm_mode 1: trailing updates on the emulated-FP64 GEMM.
+int potrf_device(int uplo, int64_t n, double *A, int64_t lda, int *info_dev, int gemm_mode,
+                 cudaStream_t s);
 
 int dtrsm_device(int side, int uplo, int trans, int unit, int64_t m, int64_t n, double alpha,
                  const double *A, int64_t lda, double *B, int64_t ldb, cudaStream_t s);

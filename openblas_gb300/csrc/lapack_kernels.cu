@@ -1137,9 +1137,6 @@ struct LuCtx {
   cudaStream_t s;
 };
 
-int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
-                   const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
-                   double *C, int64_t ldc, int slices, cudaStream_t s);
 
 template <typename T>
 int lu_update(LuCtx<T> &c, int64_t m, int64_t n, int64_t k, const T *A21, const T *A12, T *A22);
@@ -1428,27 +1425,68 @@ int getrs_device(int trans, int64_t n, int64_t nrhs, const T *A, int64_t lda, co
 // potrf_U_single.c:79-193): potf2 on the diagonal block, TRSM of the panel,
 // SYRK of the trailing matrix.  Every kernel after a failed potf2 sees info
 // != 0 and does nothing, so the matrix is left as at the failure point.
-int potrf_device(int uplo, int64_t n, double *A, int64_t lda, int *info, cudaStream_t s) {
-  GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
-  const bool upper = uplo == 0;
-  for (int64_t j0 = 0; j0 < n; j0 += PANEL_NB) {
-    const int jb = (int)((n - j0) < PANEL_NB ? (n - j0) : PANEL_NB);
-    double *D = A + j0 + j0 * lda;
-    { potf2_kernel<double><<<1, 256, 0, s>>>(upper ? 1 : 0, jb, D, lda, info, j0); count_launch(); }
-    const int64_t rest = n - j0 - jb;
+// Cholesky, blocked like lapack/potrf/potrf_L_single.c / potrf_U_single.c:
+// 256-wide block columns; the diagonal block is factored in FP64 by 32-wide
+// steps (potf2 + TRSM + SYRK inside the block); the panel below (right of)
+// it is solved against the block's triangle, and the trailing matrix gets
+// one rank-256 SYRK -- the native FP64 tri-masked GEMM, or with gemm_mode 1
+// the emulated-FP64 GEMM restricted to the triangle.  Every step after a
+// non-positive pivot is skipped on the device (info), so the matrix is left
+// as it was at the failing column.
+constexpr int64_t POTRF_NB = 256;
+
+static int potrf_diag_block(bool upper, int64_t nb, double *D, int64_t lda, int *info,
+                            int64_t off, cudaStream_t s) {
+  for (int64_t j0 = 0; j0 < nb; j0 += PANEL_NB) {
+    const int jb = (int)((nb - j0) < PANEL_NB ? (nb - j0) : PANEL_NB);
+    double *E = D + j0 + j0 * lda;
+    { potf2_kernel<double><<<1, 256, 0, s>>>(upper ? 1 : 0, jb, E, lda, info, off + j0); count_launch(); }
+    const int64_t rest = nb - j0 - jb;
     if (rest <= 0) continue;
     int st;
     if (!upper) {
-      double *P = A + (j0 + jb) + j0 * lda;
-      if ((st = dtrsm_device_skip(1, 1, 1, 1, rest, jb, 1.0, D, lda, P, lda, s, info))) return st;
+      double *P = E + jb;
+      if ((st = dtrsm_device_skip(1, 1, 1, 1, rest, jb, 1.0, E, lda, P, lda, s, info))) return st;
       if ((st = dsyrk_device_skip(1, 0, rest, jb, -1.0, P, lda, 1.0, P + jb * lda, lda, s, info)))
         return st;
     } else {
-      double *P = A + j0 + (j0 + jb) * lda;
-      if ((st = dtrsm_device_skip(0, 0, 1, 1, jb, rest, 1.0, D, lda, P, lda, s, info))) return st;
+      double *P = E + jb * lda;
+      if ((st = dtrsm_device_skip(0, 0, 1, 1, jb, rest, 1.0, E, lda, P, lda, s, info))) return st;
       if ((st = dsyrk_device_skip(0, 1, rest, jb, -1.0, P, lda, 1.0, P + jb, lda, s, info)))
         return st;
     }
+  }
+  return GB_SUCCESS;
+}
+
+int potrf_device(int uplo, int64_t n, double *A, int64_t lda, int *info, int gemm_mode,
+                 cudaStream_t s) {
+  GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
+  const bool upper = uplo == 0;
+  for (int64_t j0 = 0; j0 < n; j0 += POTRF_NB) {
+    const int64_t jb = (n - j0) < POTRF_NB ? (n - j0) : POTRF_NB;
+    double *D = A + j0 + j0 * lda;
+    int st = potrf_diag_block(upper, jb, D, lda, info, j0, s);
+    if (st) return st;
+    const int64_t rest = n - j0 - jb;
+    if (rest <= 0) continue;
+    const bool emulated = gemm_mode == 1 && rest >= 256 && jb >= 64;
+    if (!upper) {
+      double *P = A + (j0 + jb) + j0 * lda;  // rest x jb
+      double *C = P + jb * lda;
+      if ((st = dtrsm_device_skip(1, 1, 1, 1, rest, jb, 1.0, D, lda, P, lda, s, info))) return st;
+      st = emulated ? dgemm_emulated(0, 1, rest, rest, jb, -1.0, P, lda, P, lda, 1.0, C, lda, 0, s,
+                                     1, info)
+                    : dsyrk_device_skip(1, 0, rest, jb, -1.0, P, lda, 1.0, C, lda, s, info);
+    } else {
+      double *P = A + j0 + (j0 + jb) * lda;  // jb x rest
+      double *C = P + jb;
+      if ((st = dtrsm_device_skip(0, 0, 1, 1, jb, rest, 1.0, D, lda, P, lda, s, info))) return st;
+      st = emulated ? dgemm_emulated(1, 0, rest, rest, jb, -1.0, P, lda, P, lda, 1.0, C, lda, 0, s,
+                                     2, info)
+                    : dsyrk_device_skip(0, 1, rest, jb, -1.0, P, lda, 1.0, C, lda, s, info);
+    }
+    if (st) return st;
   }
   return check_cuda(cudaGetLastError(), "potrf");
 }

@@ -33,9 +33,6 @@
 
 namespace gb {
 
-int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
-                   const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
-                   double *C, int64_t ldc, int slices, cudaStream_t s);
 
 namespace {
 
@@ -156,6 +153,61 @@ __global__ void gemv_combine_kernel(int64_t n, int nchunks, const double *__rest
   y[i] = (beta == 0.0 ? 0.0 : beta * b[i]) + alpha * s;
 }
 
+// Compensated (double-double) form of the two kernels above, for the
+// Krylov products of GMRES-IR: there z = M^-1 v has a norm near kappa(A)
+// while A z is near v, so a plain FP64 product loses about n*eps*kappa of
+// relative accuracy, which caps what GMRES can reach.  Each product a*x is
+// split exactly with one FMA (TwoProduct) and the sums are carried as
+// hi + lo with TwoSum, so the result is A z rounded once.
+__device__ __forceinline__ void two_sum(double a, double b, double &s, double &e) {
+  s = a + b;
+  const double z = s - a;
+  e = (a - (s - z)) + (b - z);
+}
+
+__global__ void gemv_dd_partial_kernel(int64_t n, const double *__restrict__ A, int64_t lda,
+                                       const double *__restrict__ x, double *__restrict__ part_hi,
+                                       double *__restrict__ part_lo) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  const int64_t j0 = (int64_t)blockIdx.y * GEMV_COL_CHUNK;
+  const int64_t j1 = j0 + GEMV_COL_CHUNK < n ? j0 + GEMV_COL_CHUNK : n;
+  __shared__ double xs[GEMV_COL_CHUNK];
+  for (int64_t j = j0 + threadIdx.x; j < j1; j += blockDim.x) xs[j - j0] = x[j];
+  __syncthreads();
+  if (i >= n) return;
+  double hi = 0.0, lo = 0.0;
+  for (int64_t j = j0; j < j1; ++j) {
+    const double a = A[i + j * lda], b = xs[j - j0];
+    const double p = a * b;
+    const double pe = fma(a, b, -p);  // exact: a*b = p + pe
+    double t, te;
+    two_sum(hi, p, t, te);
+    hi = t;
+    lo += te + pe;
+  }
+  two_sum(hi, lo, hi, lo);
+  part_hi[(int64_t)blockIdx.y * n + i] = hi;
+  part_lo[(int64_t)blockIdx.y * n + i] = lo;
+}
+
+// y = beta*b + alpha*sum(parts), alpha = +-1 and beta in {0, 1} (exact), in
+// double-double, rounded once.
+__global__ void gemv_dd_combine_kernel(int64_t n, int nchunks, const double *__restrict__ part_hi,
+                                       const double *__restrict__ part_lo, double alpha,
+                                       const double *__restrict__ b, double beta,
+                                       double *__restrict__ y) {
+  const int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  double hi = beta == 0.0 ? 0.0 : beta * b[i], lo = 0.0;
+  for (int c = 0; c < nchunks; ++c) {
+    double t, te;
+    two_sum(hi, alpha * part_hi[(int64_t)c * n + i], t, te);
+    hi = t;
+    lo += te + alpha * part_lo[(int64_t)c * n + i];
+  }
+  y[i] = hi + lo;
+}
+
 // out[j] = V(:,j) . w for j < k (one block per j)
 __global__ void multidot_kernel(int64_t n, const double *__restrict__ V, int64_t ldv,
                                 const double *__restrict__ w, double *__restrict__ out) {
@@ -227,6 +279,9 @@ struct Mixed {
   int *dflag = nullptr;
   Host *hx = nullptr;       // pinned host scratch
   double *LU64 = nullptr;   // FP64 copy of the FP32 factors (GMRES-IR stage)
+  double *Linv64 = nullptr, *Uinv64 = nullptr;  // its inverted 64x64 diagonal blocks
+  double *W64 = nullptr;    // n-vector work of the FP64 preconditioner
+  double *part_lo = nullptr;  // low parts of the compensated GEMV
   float *SX2 = nullptr;     // n x nrhs FP32 work (permuted right-hand sides)
   int *perm = nullptr;      // final row permutation of the FP32 LU
   float *Linv = nullptr, *Uinv = nullptr;  // inverted 64x64 diagonal blocks of L, U
@@ -280,7 +335,22 @@ struct Mixed {
   }
 
   // M^-1 v for GMRES-IR: the FP32 factors applied in FP64 arithmetic
-  int precond64(double *v) { return getrs_device<double>(0, n, 1, LU64, n, ipiv, v, n, s); }
+  // v = (LU)^-1 P v with the FP64 copy of the FP32 factors: the chained
+  // block solve (one launch per triangle), in place through W64
+  int precond64(double *v) {
+    int st = apply_perm<double>(n, 1, perm, v, n, W64, n, s);
+    if (st) return st;
+    if ((st = lu_block_solve<double>(n, 1, LU64, n, Linv64, Uinv64, W64, n, s))) return st;
+    GB_CUDA(cudaMemcpyAsync(v, W64, (size_t)n * sizeof(double), cudaMemcpyDeviceToDevice, s));
+    return GB_SUCCESS;
+  }
+
+  // y = beta*b + alpha*A*x in double-double (one column), for the Krylov products
+  void gemv_dd(const double *x, double alpha, const double *b, double beta, double *y) {
+    dim3 gg((unsigned)((n + 255) / 256), (unsigned)nchunks);
+    { gemv_dd_partial_kernel<<<gg, 256, 0, s>>>(n, A, lda, x, part, part_lo); count_launch(); }
+    { gemv_dd_combine_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, nchunks, part, part_lo, alpha, b, beta, y); count_launch(); }
+  }
 
   // FP32 solve of the n x k block V (in place through SX): V = fp64(LU32 \ fp32(V))
   int precond(double *V, int64_t ldv, int64_t k, bool *overflow) {
@@ -318,7 +388,7 @@ int fgmres(Mixed &M, const double *r, double *d, int restart, int max_it, double
   std::vector<double> hh(restart + 1);
   GB_CUDA(cudaMemsetAsync(d, 0, n * sizeof(double), s));
   // initial residual of the correction equation: r - A*0 = r
-  double beta = 0.0;
+  double beta = 0.0, prev_beta = 0.0;
   GB_CUDA(cudaMemcpyAsync(w, r, n * sizeof(double), cudaMemcpyDeviceToDevice, s));
   int total = 0;
   for (int outer = 0; total < max_it; ++outer) {
@@ -333,6 +403,10 @@ int fgmres(Mixed &M, const double *r, double *d, int restart, int max_it, double
               beta, total);
     if (outer == 0) rtol *= beta;
     if (beta <= rtol || beta == 0.0) break;
+    // a full restart cycle that did not halve the residual: GMRES has
+    // stagnated for this correction, return what it has
+    if (outer > 0 && beta > 0.5 * prev_beta) break;
+    prev_beta = beta;
     { scale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, 1.0 / beta, w, V, 0); count_launch(); }
     std::fill(g.begin(), g.end(), 0.0);
     g[0] = beta;
@@ -342,9 +416,7 @@ int fgmres(Mixed &M, const double *r, double *d, int restart, int max_it, double
       GB_CUDA(cudaMemcpyAsync(Z + j * n, V + j * n, n * sizeof(double), cudaMemcpyDeviceToDevice,
                               s));
       if ((st = M.precond64(Z + j * n))) return st;
-      dim3 gg((unsigned)((n + 255) / 256), (unsigned)M.nchunks);
-      { gemv_partial_kernel<<<gg, 256, 0, s>>>(n, M.A, M.lda, Z + j * n, M.part); count_launch(); }
-      { gemv_combine_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, M.nchunks, M.part, 1.0, w, 0.0, w); count_launch(); }
+      M.gemv_dd(Z + j * n, 1.0, w, 0.0, w);
       // classical Gram-Schmidt, twice (CGS2)
       for (int pass = 0; pass < 2; ++pass) {
         { multidot_kernel<<<(unsigned)(j + 1), 256, 0, s>>>(n, V, n, w, hcol); count_launch(); }
@@ -392,9 +464,7 @@ int fgmres(Mixed &M, const double *r, double *d, int restart, int max_it, double
       { scale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, y[i], Z + i * n, d, 1); count_launch(); }
     if (fabs(g[j]) <= rtol) break;
     // new residual of the correction equation: w = r - A d
-    dim3 gg((unsigned)((n + 255) / 256), (unsigned)M.nchunks);
-    { gemv_partial_kernel<<<gg, 256, 0, s>>>(n, M.A, M.lda, d, M.part); count_launch(); }
-    { gemv_combine_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, M.nchunks, M.part, -1.0, r, 1.0, w); count_launch(); }
+    M.gemv_dd(d, -1.0, r, 1.0, w);
   }
   *iters = total;
   return check_cuda(cudaGetLastError(), "fgmres");
@@ -550,6 +620,16 @@ int dsgesv_device(int64_t n, int64_t nrhs, double *A, int64_t lda, int *ipiv, co
       if (!lu64.p) return GB_ERR_ALLOC;
       M.LU64 = lu64.as<double>();
       { lag2d_kernel<<<grid_for(n * n), 256, 0, s>>>(n, n, M.SA, n, M.LU64, n, 0); count_launch(); }
+      const int64_t nblk64 = (n + 63) / 64;
+      Scratch gm_ws(((size_t)2 * nblk64 * 64 * 64 + (size_t)n + (size_t)M.nchunks * n) *
+                        sizeof(double), s);
+      if (!gm_ws.p) return GB_ERR_ALLOC;
+      M.Linv64 = gm_ws.as<double>();
+      M.Uinv64 = M.Linv64 + nblk64 * 64 * 64;
+      M.W64 = M.Uinv64 + nblk64 * 64 * 64;
+      M.part_lo = M.W64 + n;
+      if ((st = lu_block_inverses<double>(n, M.LU64, n, M.Linv64, M.Uinv64, s))) return st;
+      double prev_worst = INFINITY;
       int total_gm = 0;
       const int gm_restart = n < 100 ? (int)n : 100;  // Hessenberg column fits the host scratch
       const int gm_max = n < 400 ? (int)n : 400;
@@ -562,6 +642,8 @@ int dsgesv_device(int64_t n, int64_t nrhs, double *A, int64_t lda, int *ipiv, co
           done = true;
           break;
         }
+        if (worst > 0.5 * prev_worst) break;  // an outer step that gained nothing: FP64 LU
+        prev_worst = worst;
         Scratch dbuf((size_t)n * sizeof(double), s);
         if (!dbuf.p) return GB_ERR_ALLOC;
         if (config().verbose >= 2)

@@ -59,6 +59,7 @@ struct GemmParams {
   int S;
   int m_tiles, n_tiles;
   int group_m;  // m-tiles per group of the tile order
+  int tri;      // 0 all tiles; 1 only tiles meeting i >= j; 2 only tiles meeting i <= j
   int kblocks;
   int m_pad, n_pad;
   int64_t plane_stride;
@@ -78,6 +79,14 @@ __device__ __forceinline__ void tile_coords(int tile, const GemmParams &p, int &
   const int in = tile % span;
   mt = first_m + in % gm;
   nt = in / gm;
+}
+
+// A tile takes part unless it lies entirely in the triangle the caller
+// leaves alone (triangular output of a SYRK-shaped update).
+__device__ __forceinline__ bool tile_active(int mt, int nt, const GemmParams &p) {
+  if (p.tri == 1) return mt * BM + BM - 1 >= nt * BN;  // some i >= j
+  if (p.tri == 2) return mt * BM <= nt * BN + BN - 1;  // some i <= j
+  return true;
 }
 
 __global__ void __launch_bounds__(NUM_THREADS, 1)
@@ -143,6 +152,7 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
         int mt, nt;
         tile_coords(tile, p, mt, nt);
+        if (!tile_active(mt, nt, p)) continue;
         for (int L = 2; ok && L <= S + 1; ++L) {
           const int s_lo = L - S > 1 ? L - S : 1, s_hi = L - 1 < S ? L - 1 : S;
           for (int s = s_lo; ok && s <= s_hi; ++s) {
@@ -186,6 +196,9 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       uint32_t acc_phase = 0;
       bool ok = true;
       for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+        int mt, nt;
+        tile_coords(tile, p, mt, nt);
+        if (!tile_active(mt, nt, p)) continue;
         for (int L = 2; ok && L <= S + 1; ++L) {
           const int s_lo = L - S > 1 ? L - S : 1, s_hi = L - 1 < S ? L - 1 : S;
           for (int s = s_lo; ok && s <= s_hi; ++s) {
@@ -244,6 +257,7 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
       int mt, nt;
       tile_coords(tile, p, mt, nt);
+      if (!tile_active(mt, nt, p)) continue;
       const int64_t plane_tile = (int64_t)nt * p.m_tiles + mt;
       for (int L = 2; ok && L <= S + 1; ++L) {
 #pragma unroll
@@ -429,11 +443,14 @@ __global__ void recombine_kernel(int64_t m, int64_t n, int S, int m_tiles, int64
                                  const int *__restrict__ eb, double alpha, double beta,
                                  double *__restrict__ C, int64_t ldc, int ta, int tb, int64_t k,
                                  const double *__restrict__ A, int64_t lda,
-                                 const double *__restrict__ B, int64_t ldb) {
+                                 const double *__restrict__ B, int64_t ldb, int tri,
+                                 const int *__restrict__ skip) {
+  if (skip && *skip) return;  // a failed factorisation step upstream: leave C as it is
   const int64_t total = m * n;
   for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
        idx += (int64_t)gridDim.x * blockDim.x) {
     const int64_t j = idx / m, i = idx - j * m;
+    if ((tri == 1 && i < j) || (tri == 2 && i > j)) continue;  // the other triangle
     const int ei = ea[i], fj = eb[j];
     double v;
     if (ei == NONFINITE || fj == NONFINITE) {
@@ -512,7 +529,7 @@ void split_operand(bool kcontig, int64_t R, int64_t K, const double *X, int64_t 
 // One pass over a K segment (k <= MAX_K_SEGMENT).
 int emulated_segment(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
                      const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
-                     double *C, int64_t ldc, int S, cudaStream_t s) {
+                     double *C, int64_t ldc, int S, cudaStream_t s, int tri, const int *skip) {
   const int64_t m_pad = round_up(m, BM), n_pad = round_up(n, BN), k_pad = round_up(k, BK);
   const size_t bytes_sa = align256((size_t)S * m_pad * k_pad * 2);
   const size_t bytes_sb = align256((size_t)S * n_pad * k_pad * 2);
@@ -550,6 +567,7 @@ int emulated_segment(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
   gp.m_tiles = (int)(m_pad / BM);
   gp.n_tiles = (int)(n_pad / BN);
   gp.group_m = config().ozaki_group_m;
+  gp.tri = tri;
   gp.kblocks = (int)(k_pad / BK);
   gp.m_pad = (int)m_pad;
   gp.n_pad = (int)n_pad;
@@ -570,7 +588,7 @@ int emulated_segment(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
   const int64_t cap = (int64_t)sm_count() * 32;
   { recombine_kernel<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(
       m, n, S, gp.m_tiles, plane_stride, planes, ea, eb, alpha, beta, C, ldc, ta, tb, k, A, lda,
-      B, ldb); count_launch(); }
+      B, ldb, tri, skip); count_launch(); }
   return check_cuda(cudaGetLastError(), "emulated dgemm");
 }
 
@@ -582,7 +600,8 @@ int ozaki_default_slices() { return oz::MAX_SLICES; }
 
 int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
                    const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
-                   double *C, int64_t ldc, int slices, cudaStream_t s) {
+                   double *C, int64_t ldc, int slices, cudaStream_t s, int tri,
+                   const int *skip) {
   int S = slices > 0 ? slices : ozaki_default_slices();
   if (S > oz::MAX_SLICES) S = oz::MAX_SLICES;
   if (m <= 0 || n <= 0) return GB_SUCCESS;
@@ -594,7 +613,8 @@ int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha
     const int64_t kk = (k - k0) < oz::MAX_K_SEGMENT ? (k - k0) : oz::MAX_K_SEGMENT;
     const double *Ak = ta ? A + k0 : A + k0 * lda;
     const double *Bk = tb ? B + k0 * ldb : B + k0;
-    int st = oz::emulated_segment(ta, tb, m, n, kk, alpha, Ak, lda, Bk, ldb, b, C, ldc, S, s);
+    int st = oz::emulated_segment(ta, tb, m, n, kk, alpha, Ak, lda, Bk, ldb, b, C, ldc, S, s, tri,
+                                  skip);
     if (st) return st;
     b = 1.0;
   }

@@ -205,6 +205,49 @@ def test_dpotrf_residual(F, gb_clean, uplo):
     assert r <= 10
 
 
+@pytest.mark.parametrize("uplo", ["L", "U"])
+@pytest.mark.parametrize("n", [1100, 2600])
+def test_dpotrf_emulated_updates(F, gblib, gb_clean, uplo, n):
+    """DPOTRF whose rank-256 trailing updates run on the emulated-FP64 GEMM
+    restricted to the triangle (DGEMM mode 'emulated'): the other triangle is
+    bit-for-bit untouched and the scaled residual stays at the FP64 bound."""
+    A0 = W.spd(8300 + n, n)
+    A = A0.copy(order="F")
+    gblib.gb_set_dgemm_mode(1)
+    try:
+        assert F.dpotrf(uplo, n, A, n) == 0
+    finally:
+        gblib.gb_set_dgemm_mode(0)
+    other = (lambda X: np.triu(X, 1)) if uplo == "L" else (lambda X: np.tril(X, -1))
+    assert np.array_equal(other(A), other(A0))
+    Lf = np.tril(A) if uplo == "L" else np.triu(A).T
+    r = np.abs(A0 - Lf @ Lf.T).sum(axis=0).max() / (n * EPS * np.abs(A0).sum(axis=0).max())
+    assert r <= 10
+
+
+@pytest.mark.parametrize("mode", [0, 1])
+def test_dpotrf_failure_in_later_block(orc, F, gblib, gb_clean, mode):
+    """A non-positive pivot past the first 256-wide block: info matches the
+    oracle.  After a failure LAPACK leaves the rest of A unspecified and the
+    reference's state depends on its blocking, so the comparison covers what
+    every blocking has completed: the columns before the failing 32-wide
+    diagonal step (530 lies in [512, 544)), and that step's rows of the
+    columns before the failing one."""
+    n = 700
+    A0 = W.spd(8400, n)
+    A0[530, 530] = -3.0
+    A, Ao = A0.copy(order="F"), A0.copy(order="F")
+    gblib.gb_set_dgemm_mode(mode)
+    try:
+        info = F.dpotrf("L", n, A, n)
+    finally:
+        gblib.gb_set_dgemm_mode(0)
+    assert info == orc.dpotrf("L", n, Ao, n) == 531
+    tol = 1e-10 * np.abs(np.tril(Ao)).max()
+    assert np.max(np.abs(np.tril(A)[:, :512] - np.tril(Ao)[:, :512])) <= tol
+    assert np.max(np.abs(np.tril(A)[512:544, 512:530] - np.tril(Ao)[512:544, 512:530])) <= tol
+
+
 def test_dlaswp_golden(golden, F, gb_clean):
     for idx, (n, k1, k2, incx) in enumerate(GG.LASWP_CASES):
         rows = 12
