@@ -494,7 +494,11 @@ getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__r
   };
 
   const int ncol = (int)(nb < m ? nb : m);
-  for (int j = 0; j < ncol; ++j) {
+  // fully unrolled over the 32 columns: every register index and the
+  // length of each row update (31 - j FMAs) are compile-time constants
+#pragma unroll
+  for (int j = 0; j < PANEL_NB; ++j) {
+    if (j >= ncol) break;
     const int par = j & 1;
     // ---- local first maximum of |a_ij| over this thread's rows >= j
     T best = T(-1);
