@@ -321,6 +321,7 @@ __global__ void rowmax_kcontig_kernel(int64_t R, int64_t K, const double *__rest
   if (r >= R) return;
   const double *x = X + r * ld;
   unsigned long long best = 0;
+#pragma unroll 8
   for (int64_t pp = lane; pp < K; pp += 32) {
     unsigned long long b = __double_as_longlong(fabs(x[pp]));
     best = b > best ? b : best;
@@ -341,6 +342,7 @@ __global__ void rowmax_mcontig_kernel(int64_t R, int64_t K, const double *__rest
   const int64_t p0 = (int64_t)blockIdx.y * kspan;
   const int64_t p1 = p0 + kspan < K ? p0 + kspan : K;
   unsigned long long best = 0;
+#pragma unroll 8
   for (int64_t pp = p0; pp < p1; ++pp) {
     unsigned long long b = __double_as_longlong(fabs(X[r + pp * ld]));
     best = b > best ? b : best;
@@ -379,19 +381,20 @@ split_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
   __shared__ double tile[32][65];
   const int64_t r0 = (int64_t)blockIdx.y * 32, p0 = (int64_t)blockIdx.x * 64;
   const int tid = threadIdx.x;
-  for (int e = tid; e < 32 * 64; e += 256) {
-    int rr, pp;
-    if (KCONTIG) {
-      rr = e / 64;
-      pp = e % 64;
-    } else {
-      rr = e % 32;
-      pp = e / 32;
-    }
+  // all eight loads of a thread in flight before the shared-memory stores
+  double vin[8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const int e = tid + 256 * u;
+    const int rr = KCONTIG ? e / 64 : e % 32, pp = KCONTIG ? e % 64 : e / 32;
     const int64_t r = r0 + rr, pk = p0 + pp;
-    double v = 0.0;
-    if (r < R && pk < K) v = KCONTIG ? X[pk + r * ld] : X[r + pk * ld];
-    tile[rr][pp] = v;
+    vin[u] = (r < R && pk < K) ? (KCONTIG ? X[pk + r * ld] : X[r + pk * ld]) : 0.0;
+  }
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const int e = tid + 256 * u;
+    const int rr = KCONTIG ? e / 64 : e % 32, pp = KCONTIG ? e % 64 : e / 32;
+    tile[rr][pp] = vin[u];
   }
   __syncthreads();
   // each thread: row rr = tid / 8, 8 consecutive k values.  The fixed-point
@@ -438,62 +441,88 @@ split_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
 }
 
 // ------------------------------------------------------------------ recombine
-__global__ void recombine_kernel(int64_t m, int64_t n, int S, int m_tiles, int64_t plane_stride,
-                                 const int *__restrict__ planes, const int *__restrict__ ea,
-                                 const int *__restrict__ eb, double alpha, double beta,
-                                 double *__restrict__ C, int64_t ldc, int ta, int tb, int64_t k,
-                                 const double *__restrict__ A, int64_t lda,
-                                 const double *__restrict__ B, int64_t ldb, int tri,
-                                 const int *__restrict__ skip) {
+// One element of C from its exact level sum: acc = sum_L P_L 2^(7(S+1-L))
+// (< 2^81) is rounded once to FP64 (sticky bit), then scaled exactly by
+// alpha * 2^(e_i + f_j - 7(S+1)) through the exponent bits of alpha.
+__device__ __forceinline__ double level_value(__int128 acc, int S, int ei, int fj, double alpha) {
+  if (acc == 0) return 0.0;
+  const bool neg = acc < 0;
+  unsigned __int128 u = neg ? (unsigned __int128)(-acc) : (unsigned __int128)acc;
+  const unsigned long long hi = (unsigned long long)(u >> 64);
+  const int msb = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)(unsigned long long)u);
+  const int sh = msb > 63 ? msb - 63 : 0;
+  unsigned long long top = (unsigned long long)(u >> sh);
+  if (sh && (u & (((unsigned __int128)1 << sh) - 1)) != 0) top |= 1ull;  // sticky bit
+  const double t = __ull2double_rn(top);
+  const int x = sh - 7 * (S + 1) + ei + fj;
+  const long long ab = __double_as_longlong(alpha);
+  const int e_alpha = (int)((ab >> 52) & 0x7ff);
+  double scale;
+  if (e_alpha > 0 && e_alpha < 0x7ff && e_alpha + x > 0 && e_alpha + x < 0x7ff)
+    scale = __longlong_as_double(ab + ((long long)x << 52));
+  else
+    scale = alpha * ldexp(1.0, x);
+  return (neg ? -t : t) * scale;
+}
+
+// Recombine, one CTA per 128 x 256 tile of C (the plane tile layout): every
+// level plane of the tile is one contiguous 128 KB run, read with 16-byte
+// loads (a lane takes 4 consecutive rows of a column), and the shifts of the
+// level sum are compile-time (S is a template argument).  Rows/columns with
+// Inf/NaN use a direct FP64 dot product so IEEE special values propagate.
+template <int S>
+__global__ void __launch_bounds__(256)
+recombine_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
+                      const int *__restrict__ planes, const int *__restrict__ ea,
+                      const int *__restrict__ eb, double alpha, double beta,
+                      double *__restrict__ C, int64_t ldc, int ta, int tb, int64_t k,
+                      const double *__restrict__ A, int64_t lda, const double *__restrict__ B,
+                      int64_t ldb, int tri, const int *__restrict__ skip) {
   if (skip && *skip) return;  // a failed factorisation step upstream: leave C as it is
-  const int64_t total = m * n;
-  for (int64_t idx = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; idx < total;
-       idx += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t j = idx / m, i = idx - j * m;
-    if ((tri == 1 && i < j) || (tri == 2 && i > j)) continue;  // the other triangle
-    const int ei = ea[i], fj = eb[j];
-    double v;
-    if (ei == NONFINITE || fj == NONFINITE) {
-      // Inf/NaN in row i of op(A) or column j of op(B): direct FP64 dot
-      double s = 0.0;
-      for (int64_t pp = 0; pp < k; ++pp) {
-        double a = ta ? A[pp + i * lda] : A[i + pp * lda];
-        double b = tb ? B[j + pp * ldb] : B[pp + j * ldb];
-        s = fma(a, b, s);
+  const int mt = blockIdx.x, nt = blockIdx.y;
+  const int64_t i0 = (int64_t)mt * BM, j0 = (int64_t)nt * BN;
+  if (tri == 1 && i0 + BM - 1 < j0) return;  // tile wholly in the other triangle
+  if (tri == 2 && i0 > j0 + BN - 1) return;
+  const int tid = threadIdx.x;
+  const int il = (tid & 31) * 4, jb = tid >> 5;
+  const int *pt = planes + ((int64_t)nt * m_tiles + mt) * (BM * BN);
+  int e_i[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) e_i[r] = (i0 + il + r < m) ? ea[i0 + il + r] : 0;
+  for (int jl = jb; jl < BN; jl += 8) {
+    const int64_t j = j0 + jl;
+    if (j >= n) break;
+    const int fj = eb[j];
+    int4 P[S];
+#pragma unroll
+    for (int L = 0; L < S; ++L)
+      P[L] = *reinterpret_cast<const int4 *>(pt + (int64_t)L * plane_stride + jl * BM + il);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int64_t i = i0 + il + r;
+      if (i >= m) continue;
+      if ((tri == 1 && i < j) || (tri == 2 && i > j)) continue;  // the other triangle
+      double v;
+      if (e_i[r] == NONFINITE || fj == NONFINITE) {
+        double sum = 0.0;
+        for (int64_t pp = 0; pp < k; ++pp) {
+          const double a = ta ? A[pp + i * lda] : A[i + pp * lda];
+          const double b = tb ? B[j + pp * ldb] : B[pp + j * ldb];
+          sum = fma(a, b, sum);
+        }
+        v = alpha * sum;
+      } else {
+        __int128 acc = 0;
+#pragma unroll
+        for (int L = 0; L < S; ++L) {
+          const int pv = r == 0 ? P[L].x : r == 1 ? P[L].y : r == 2 ? P[L].z : P[L].w;
+          acc += (__int128)pv << (7 * (S - 1 - L));  // level L+2 has weight 2^(7(S+1-(L+2)))
+        }
+        v = level_value(acc, S, e_i[r], fj, alpha);
       }
-      v = alpha * s;
-    } else {
-      // exact integer sum of the levels: sum_L P_L * 2^(7(S+1-L)) (< 2^81)
-      const int64_t tile = (j / 256) * m_tiles + (i / 128);
-      const int64_t off = tile * (128 * 256) + (j % 256) * 128 + (i % 128);
-      __int128 acc = 0;
-      for (int L = 2; L <= S + 1; ++L)
-        acc += (__int128)planes[(int64_t)(L - 2) * plane_stride + off] << (7 * (S + 1 - L));
-      v = 0.0;
-      if (acc != 0) {
-        const bool neg = acc < 0;
-        unsigned __int128 u = neg ? (unsigned __int128)(-acc) : (unsigned __int128)acc;
-        const unsigned long long hi = (unsigned long long)(u >> 64);
-        const int msb = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)(unsigned long long)u);
-        int sh = msb > 63 ? msb - 63 : 0;
-        unsigned long long top = (unsigned long long)(u >> sh);
-        if (sh && (u & (((unsigned __int128)1 << sh) - 1)) != 0) top |= 1ull;  // sticky bit
-        // one correctly rounded conversion, then an exact power-of-two scaling
-        // folded into alpha: value = top * 2^(sh - 7(S+1) + e_i + f_j)
-        const double t = __ull2double_rn(top);
-        const int x = sh - 7 * (S + 1) + ei + fj;
-        const long long ab = __double_as_longlong(alpha);
-        const int ea = (int)((ab >> 52) & 0x7ff);
-        double scale;
-        if (ea > 0 && ea < 0x7ff && ea + x > 0 && ea + x < 0x7ff)
-          scale = __longlong_as_double(ab + ((long long)x << 52));
-        else
-          scale = alpha * ldexp(1.0, x);
-        v = (neg ? -t : t) * scale;
-      }
+      double *c = C + i + j * ldc;
+      *c = (beta == 0.0) ? v : fma(beta, *c, v);
     }
-    double *c = C + i + j * ldc;
-    *c = (beta == 0.0) ? v : fma(beta, *c, v);
   }
 }
 
@@ -583,12 +612,22 @@ int emulated_segment(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
   }
   GB_CUDA(cudaGetLastError());
 
-  const int64_t total = m * n;
-  int64_t blocks = (total + 255) / 256;
-  const int64_t cap = (int64_t)sm_count() * 32;
-  { recombine_kernel<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(
-      m, n, S, gp.m_tiles, plane_stride, planes, ea, eb, alpha, beta, C, ldc, ta, tb, k, A, lda,
-      B, ldb, tri, skip); count_launch(); }
+  {
+    const dim3 g((unsigned)((m + BM - 1) / BM), (unsigned)((n + BN - 1) / BN));
+#define GB_RECOMBINE(SS)                                                                        \
+  case SS:                                                                                      \
+    recombine_tile_kernel<SS><<<g, 256, 0, s>>>(m, n, gp.m_tiles, plane_stride, planes, ea, eb, \
+                                                alpha, beta, C, ldc, ta, tb, k, A, lda, B, ldb, \
+                                                tri, skip);                                     \
+    break;
+    switch (S) {
+      GB_RECOMBINE(1) GB_RECOMBINE(2) GB_RECOMBINE(3) GB_RECOMBINE(4)
+      GB_RECOMBINE(5) GB_RECOMBINE(6) GB_RECOMBINE(7) GB_RECOMBINE(8)
+      default: return set_error(GB_ERR_UNSUPPORTED, "emulated dgemm: %d slices", S);
+    }
+#undef GB_RECOMBINE
+    count_launch();
+  }
   return check_cuda(cudaGetLastError(), "emulated dgemm");
 }
 
