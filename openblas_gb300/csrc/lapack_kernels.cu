@@ -798,7 +798,7 @@ constexpr int LT_MAXN = 256;  // largest L11
 
 template <typename T>
 __host__ __device__ constexpr size_t lu_trsm_smem(int nblk) {
-  return (size_t)2 * nblk * 32 * (LT_COLS + 1) * sizeof(T);
+  return (size_t)(2 * nblk + 1) * 32 * (LT_COLS + 1) * sizeof(T);  // B, inverses, one L tile
 }
 
 template <typename T>
@@ -810,6 +810,7 @@ lu_trsm_kernel(int n1, int64_t w, const T *__restrict__ L, int64_t ldl, T *__res
   const int nr = nblk * 32;
   T *Bs = reinterpret_cast<T *>(smem_raw);  // [nr][LT_COLS + 1]
   T *Li = Bs + nr * (LT_COLS + 1);           // [nblk][32][33]: L_dd, then its inverse
+  T *Lt = Li + nblk * 32 * 33;                // [32][33]: the current L_ik tile
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   const int64_t c0 = (int64_t)blockIdx.x * LT_COLS;
   const int nc = (int)((w - c0) < LT_COLS ? (w - c0) : LT_COLS);
@@ -842,12 +843,19 @@ lu_trsm_kernel(int n1, int64_t w, const T *__restrict__ L, int64_t ldl, T *__res
   const int r = lane, cg = warp;  // row r of a block, columns cg*4 .. cg*4+3
   for (int i = 0; i < nblk; ++i) {
     T acc[4] = {T(0), T(0), T(0), T(0)};
-    const bool row_in = i * 32 + r < n1;
     for (int k = 0; k < i; ++k) {
-      const T *lp = L + (int64_t)(i * 32 + r) + (int64_t)(k * 32) * ldl;
+      // stage L(i-block, k-block) once for all 32 columns of the CTA
+      __syncthreads();
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int e = tid + 256 * u, rr = e & 31, cc = e >> 5;
+        Lt[rr * 33 + cc] = (i * 32 + rr < n1) ? L[(int64_t)(i * 32 + rr) + (int64_t)(k * 32 + cc) * ldl]
+                                              : T(0);
+      }
+      __syncthreads();
 #pragma unroll 8
       for (int kk = 0; kk < 32; ++kk) {
-        const T l = row_in ? lp[(int64_t)kk * ldl] : T(0);
+        const T l = Lt[r * 33 + kk];
         const T *bk = Bs + (k * 32 + kk) * (LT_COLS + 1) + cg * 4;
 #pragma unroll
         for (int t = 0; t < 4; ++t) acc[t] = fma(l, bk[t], acc[t]);
