@@ -125,6 +125,19 @@ int dsgesv_(const blasint *N, const blasint *NRHS, double *A, const blasint *ldA
             blasint *ipiv, const double *B, const blasint *ldB, double *X,
             const blasint *ldX, double *WORK, float *SWORK, blasint *ITER,
             blasint *Info);
+/* replaces dpotrs_ (netlib, compiled into OpenBLAS),
+ * lapack-netlib/SRC/dpotrs.f:109-160: A X = B with the Cholesky factor of
+ * dpotrf_. */
+int dpotrs_(const char *UPLO, const blasint *N, const blasint *NRHS, const double *A,
+            const blasint *ldA, double *B, const blasint *ldB, blasint *Info);
+/* replaces dsposv_ (netlib, compiled into OpenBLAS),
+ * lapack-netlib/SRC/dsposv.f:199-434: FP32 Cholesky + FP64 refinement with
+ * the FP64 DPOTRF/DPOTRS fallback and dsposv's ITER codes.  WORK/SWORK are
+ * accepted for ABI compatibility; the GPU path keeps its own workspace. */
+int dsposv_(const char *UPLO, const blasint *N, const blasint *NRHS, double *A,
+            const blasint *ldA, const double *B, const blasint *ldB, double *X,
+            const blasint *ldX, double *WORK, float *SWORK, blasint *ITER,
+            blasint *Info);
 
 /* replaces xerbla_, driver/others/xerbla.c:56-64.  Weak: an application may
  * define its own.  Prints " ** On entry to %6s parameter number %2d had an
@@ -231,6 +244,9 @@ int gb_sgetrs_dev(char trans, int64_t n, int64_t nrhs, const float *A,
 int gb_dlaswp_dev(int64_t n, double *A, int64_t lda, int64_t k1, int64_t k2,
                   const int *ipiv, int64_t incx);
 int gb_dpotrf_dev(char uplo, int64_t n, double *A, int64_t lda, int *info);
+/* Solve with a Cholesky factor from gb_dpotrf_dev (device pointers). */
+int gb_dpotrs_dev(char uplo, int64_t n, int64_t nrhs, const double *A, int64_t lda,
+                  double *B, int64_t ldb);
 /* Grouped batches of small, uneven problems in one persistent launch (the
  * reference's cblas_dgemm_batch, interface/gemm_batch.c, extended to LU solves
  * and Cholesky).  All pointers are device pointers.  type selects:
@@ -291,6 +307,14 @@ int gb_dgetrf_noalloc_dev(int64_t m, int64_t n, double *A, int64_t lda,
 int gb_dsgesv_dev(int64_t n, int64_t nrhs, double *A, int64_t lda, int *ipiv,
                   const double *B, int64_t ldb, double *X, int64_t ldx,
                   int *iter, int *info);
+/* Mixed-precision Cholesky solve of a symmetric positive definite A (stored
+ * triangle `uplo`): FP32 Cholesky on the GPU + FP64 refinement, FP64
+ * Cholesky fallback (dsposv semantics and ITER codes).  Device pointers
+ * except iter/info (host outputs; this call synchronises).  A is only
+ * overwritten (with its FP64 factor) on a fallback. */
+int gb_dsposv_dev(char uplo, int64_t n, int64_t nrhs, double *A, int64_t lda,
+                  const double *B, int64_t ldb, double *X, int64_t ldx, int *iter,
+                  int *info);
 
 #ifdef __cplusplus
 }

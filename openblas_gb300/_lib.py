@@ -46,6 +46,9 @@ DEV_SIGS = {
     "gb_sgetrs_dev": (_i, [_c, _i64, _i64, _vp, _i64, _vp, _vp, _i64]),
     "gb_dlaswp_dev": (_i, [_i64, _vp, _i64, _i64, _i64, _vp, _i64]),
     "gb_dpotrf_dev": (_i, [_c, _i64, _vp, _i64, _vp]),
+    "gb_dpotrs_dev": (_i, [_c, _i64, _i64, _vp, _i64, _vp, _i64]),
+    "gb_dsposv_dev": (_i, [_c, _i64, _i64, _vp, _i64, _vp, _i64, _vp, _i64, C.POINTER(_i),
+                           C.POINTER(_i)]),
     "gb_dgetrf_noalloc_dev": (_i, [_i64, _i64, _vp, _i64, _vp, _vp, _vp]),
     "gb_dsgesv_dev": (_i, [_i64, _i64, _vp, _i64, _vp, _vp, _i64, _vp, _i64, C.POINTER(_i),
                            C.POINTER(_i)]),

@@ -45,6 +45,8 @@ FORTRAN_SIGS = {
     "dpotrf_": (_i, [_pc, _pi, _vp, _pi, _pi]),
     "dlaswp_": (_i, [_pi, _vp, _pi, _pi, _pi, _vp, _pi]),
     "dsgesv_": (_i, [_pi, _pi, _vp, _pi, _vp, _vp, _pi, _vp, _pi, _vp, _vp, _pi, _pi]),
+    "dpotrs_": (_i, [_pc, _pi, _pi, _vp, _pi, _vp, _pi, _pi]),
+    "dsposv_": (_i, [_pc, _pi, _pi, _vp, _pi, _vp, _pi, _vp, _pi, _vp, _vp, _pi, _pi]),
     "sgetrf_": (_i, [_pi, _pi, _vp, _pi, _vp, _pi]),
 }
 
@@ -149,6 +151,20 @@ class Fortran:
         info = _i(0)
         self.ns.dpotrf_(self._c(uplo), C.byref(_i(n)), _ptr(A), C.byref(_i(lda)), C.byref(info))
         return info.value
+
+    def dpotrs(self, uplo, n, nrhs, A, lda, B, ldb) -> int:
+        info = _i(0)
+        self.ns.dpotrs_(self._c(uplo), C.byref(_i(n)), C.byref(_i(nrhs)), _ptr(A),
+                        C.byref(_i(lda)), _ptr(B), C.byref(_i(ldb)), C.byref(info))
+        return info.value
+
+    def dsposv(self, uplo, n, nrhs, A, lda, B, ldb, X, ldx, work, swork):
+        it = _i(0)
+        info = _i(0)
+        self.ns.dsposv_(self._c(uplo), C.byref(_i(n)), C.byref(_i(nrhs)), _ptr(A),
+                        C.byref(_i(lda)), _ptr(B), C.byref(_i(ldb)), _ptr(X), C.byref(_i(ldx)),
+                        _ptr(work), _ptr(swork), C.byref(it), C.byref(info))
+        return info.value, it.value
 
     def dlaswp(self, n, A, lda, k1, k2, ipiv, incx):
         self.ns.dlaswp_(C.byref(_i(n)), _ptr(A), C.byref(_i(lda)), C.byref(_i(k1)),

@@ -114,6 +114,11 @@ int sm_count();
 void launch_sgemm_fp32(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha,
                        const float *A, int64_t lda, const float *B, int64_t ldb,
                        float beta, float *C, int64_t ldc, cudaStream_t s);
+// Same, restricted to a triangle of C (tri as launch_dgemm_fp64_tri) and
+// cancelled on the device when *skip != 0.
+void launch_sgemm_fp32_tri(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha,
+                           const float *A, int64_t lda, const float *B, int64_t ldb, float beta,
+                           float *C, int64_t ldc, int tri, cudaStream_t s, const int *skip);
 // Emulated-FP64 GEMM (Ozaki slices on the bf16 tensor cores).  slices = 0:
 // default count.  tri = 1 (2): only C(i,j) with i >= j (i <= j) is written,
 // tiles wholly in the other triangle are skipped (SYRK-shaped updates).
@@ -126,7 +131,7 @@ int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha
 // Assumes m, n, k > 0.
 int sgemm_tc(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha, const float *A,
              int64_t lda, const float *B, int64_t ldb, float beta, float *C, int64_t ldc,
-             cudaStream_t s);
+             cudaStream_t s, int tri = 0, const int *skip = nullptr);
 // FP32 GEMM behind sgemm_/cblas_sgemm and the FP32 LU: the tensor-core form
 // for shapes large enough to fill the GPU (GB_SGEMM_MODE=auto, default), or
 // always SIMT / always tensor (GB_SGEMM_MODE=simt|tensor).

@@ -212,19 +212,25 @@ void launch_dbeta_tri(int64_t n, double beta, double *C, int64_t ldc, int tri, c
                                                                                   C, ldc, tri); count_launch(); }
 }
 
-void launch_sgemm_fp32(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha,
-                       const float *A, int64_t lda, const float *B, int64_t ldb, float beta,
-                       float *C, int64_t ldc, cudaStream_t s) {
+void launch_sgemm_fp32_tri(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha,
+                           const float *A, int64_t lda, const float *B, int64_t ldb, float beta,
+                           float *C, int64_t ldc, int tri, cudaStream_t s, const int *skip) {
   const int64_t tiles128 = ((m + 127) / 128) * ((n + 127) / 128);
   if (tiles128 >= (int64_t)sm_count() * 2) {
     dim3 grid((unsigned)((m + 127) / 128), (unsigned)((n + 127) / 128));
     { gemm_simt_kernel<float, 128, 128, 8, 8, 8><<<grid, 256, 0, s>>>(
-        ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, 0, nullptr); count_launch(); }
+        ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, skip); count_launch(); }
   } else {
     dim3 grid((unsigned)((m + 63) / 64), (unsigned)((n + 63) / 64));
     { gemm_simt_kernel<float, 64, 64, 16, 4, 4><<<grid, 256, 0, s>>>(
-        ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, 0, nullptr); count_launch(); }
+        ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, skip); count_launch(); }
   }
+}
+
+void launch_sgemm_fp32(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha,
+                       const float *A, int64_t lda, const float *B, int64_t ldb, float beta,
+                       float *C, int64_t ldc, cudaStream_t s) {
+  launch_sgemm_fp32_tri(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, 0, s, nullptr);
 }
 
 }  // namespace gb

@@ -198,6 +198,37 @@ int dpotrf_(const char *UPLO, const blasint *N, double *a, const blasint *ldA, b
   return 0;
 }
 
+// lapack-netlib/SRC/dpotrs.f:109-160 (the reference builds dpotrs from
+// lapack-netlib): argument checks in order UPLO, N, NRHS, LDA, LDB, quick
+// return, then the two triangular solves with the Cholesky factor.
+int dpotrs_(const char *UPLO, const blasint *N, const blasint *NRHS, const double *a,
+            const blasint *ldA, double *b, const blasint *ldB, blasint *Info) {
+  char u = upch(UPLO);
+  int uplo = u == 'U' ? 0 : u == 'L' ? 1 : -1;
+  int64_t n = *N, nrhs = *NRHS, lda = *ldA, ldb = *ldB;
+  int info = 0;
+  if (uplo < 0) info = 1;
+  else if (n < 0) info = 2;
+  else if (nrhs < 0) info = 3;
+  else if (lda < (n > 1 ? n : 1)) info = 5;
+  else if (ldb < (n > 1 ? n : 1)) info = 7;
+  if (info) {
+    call_xerbla("DPOTRS", info);
+    *Info = -info;
+    return 0;
+  }
+  *Info = 0;
+  if (n == 0 || nrhs == 0) return 0;
+  if (ensure_init()) return 0;
+  cudaStream_t s = stream();
+  Operand A(a, n, n, lda, 8), B(b, n, nrhs, ldb, 8);
+  if (A.bind(true, s) || B.bind(true, s)) return 0;
+  if (potrs_device(uplo, n, nrhs, A.d<double>(), A.dld, B.d<double>(), B.dld, s)) return 0;
+  B.unbind(s);
+  finish_blocking(s);
+  return 0;
+}
+
 int dlaswp_(const blasint *N, double *a, const blasint *LDA, const blasint *K1, const blasint *K2,
             const blasint *ipiv, const blasint *INCX) {
   int64_t n = *N, lda = *LDA, k1 = *K1, k2 = *K2, incx = *INCX;
@@ -328,6 +359,26 @@ int gb_dpotrf_dev(char uplo, int64_t n, double *A, int64_t lda, int *info) {
   }
   const int mode = gb_get_dgemm_mode() == GB_DGEMM_NATIVE ? 0 : 1;
   return potrf_device(up, n, A, lda, info, mode, stream());
+}
+
+int gb_dpotrs_dev(char uplo, int64_t n, int64_t nrhs, const double *A, int64_t lda, double *B,
+                  int64_t ldb) {
+  const char u = upch(uplo);
+  const int up = u == 'U' ? 0 : u == 'L' ? 1 : -1;
+  int code = 0;
+  if (up < 0) code = 1;
+  else if (n < 0) code = 2;
+  else if (nrhs < 0) code = 3;
+  else if (lda < (n > 1 ? n : 1)) code = 5;
+  else if (ldb < (n > 1 ? n : 1)) code = 7;
+  if (code) {
+    call_xerbla("DPOTRS", code);
+    return GB_ERR_INVALID_VALUE;
+  }
+  int st = ensure_init();
+  if (st) return st;
+  if (n == 0 || nrhs == 0) return GB_SUCCESS;
+  return potrs_device(up, n, nrhs, A, lda, B, ldb, stream());
 }
 
 }  // extern "C"

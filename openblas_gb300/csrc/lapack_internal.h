@@ -41,6 +41,17 @@ int lu_block_inverses(int64_t n, const T *A, int64_t lda, T *Linv, T *Uinv, cuda
 template <typename T>
 int lu_block_solve(int64_t n, int64_t nrhs, const T *A, int64_t lda, const T *Linv,
                    const T *Uinv, T *B, int64_t ldb, cudaStream_t s);
+// Cholesky forms: inverses of the non-unit diagonal blocks of both triangles,
+// and the mirror of one strict triangle onto the other (transposed), after
+// which lu_block_solve applies L then L^T (or U^T then U).
+template <typename T>
+int chol_block_inverses(int64_t n, const T *A, int64_t lda, T *Linv, T *Uinv, cudaStream_t s);
+template <typename T>
+int mirror_triangle(int64_t n, T *A, int64_t lda, int from_lower, cudaStream_t s);
+// Solve A X = B with a Cholesky factor from potrf_device (lapack/potrs:
+// two triangular solves).
+int potrs_device(int uplo, int64_t n, int64_t nrhs, const double *A, int64_t lda, double *B,
+                 int64_t ldb, cudaStream_t s);
 // Final permutation of the interchanges ipiv[0..n): row i of P*B is row
 // perm[i] of B; and the gather dst = P*src.
 int pivots_to_perm(int64_t n, const int *ipiv, int *perm, cudaStream_t s);
@@ -52,6 +63,9 @@ int apply_perm(int64_t n, int64_t ncol, const int *perm, const T *src, int64_t l
 // gemm_mode 1: trailing updates on the emulated-FP64 GEMM.
 int potrf_device(int uplo, int64_t n, double *A, int64_t lda, int *info_dev, int gemm_mode,
                  cudaStream_t s);
+// FP32 Cholesky (same blocking; trailing updates on the tensor-core FP32 GEMM
+// when large, per the SGEMM mode).
+int spotrf_device(int uplo, int64_t n, float *A, int64_t lda, int *info_dev, cudaStream_t s);
 
 int dtrsm_device(int side, int uplo, int trans, int unit, int64_t m, int64_t n, double alpha,
                  const double *A, int64_t lda, double *B, int64_t ldb, cudaStream_t s);
@@ -62,6 +76,12 @@ int dtrsm_device_skip(int side, int uplo, int trans, int unit, int64_t m, int64_
                       cudaStream_t s, const int *skip);
 int dsyrk_device_skip(int uplo, int trans, int64_t n, int64_t k, double alpha, const double *A,
                       int64_t lda, double beta, double *C, int64_t ldc, cudaStream_t s,
+                      const int *skip);
+int strsm_device_skip(int side, int uplo, int trans, int unit, int64_t m, int64_t n,
+                      float alpha, const float *A, int64_t lda, float *B, int64_t ldb,
+                      cudaStream_t s, const int *skip);
+int ssyrk_device_skip(int uplo, int trans, int64_t n, int64_t k, float alpha, const float *A,
+                      int64_t lda, float beta, float *C, int64_t ldc, cudaStream_t s,
                       const int *skip);
 int dsyrk_device(int uplo, int trans, int64_t n, int64_t k, double alpha, const double *A,
                  int64_t lda, double beta, double *C, int64_t ldc, cudaStream_t s);

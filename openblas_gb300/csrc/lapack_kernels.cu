@@ -1447,60 +1447,130 @@ int getrs_device(int trans, int64_t n, int64_t nrhs, const T *A, int64_t lda, co
 // as it was at the failing column.
 constexpr int64_t POTRF_NB = 256;
 
-static int potrf_diag_block(bool upper, int64_t nb, double *D, int64_t lda, int *info,
-                            int64_t off, cudaStream_t s) {
+template <typename T>
+int trsm_skip(int side, int uplo, int trans, int unit, int64_t m, int64_t n, const T *A,
+              int64_t lda, T *B, int64_t ldb, cudaStream_t s, const int *skip);
+template <>
+int trsm_skip<double>(int side, int uplo, int trans, int unit, int64_t m, int64_t n,
+                      const double *A, int64_t lda, double *B, int64_t ldb, cudaStream_t s,
+                      const int *skip) {
+  return dtrsm_device_skip(side, uplo, trans, unit, m, n, 1.0, A, lda, B, ldb, s, skip);
+}
+template <>
+int trsm_skip<float>(int side, int uplo, int trans, int unit, int64_t m, int64_t n,
+                     const float *A, int64_t lda, float *B, int64_t ldb, cudaStream_t s,
+                     const int *skip) {
+  return strsm_device_skip(side, uplo, trans, unit, m, n, 1.0f, A, lda, B, ldb, s, skip);
+}
+template <typename T>
+int syrk_skip(int uplo, int trans, int64_t n, int64_t k, const T *A, int64_t lda, T *C,
+              int64_t ldc, cudaStream_t s, const int *skip);
+template <>
+int syrk_skip<double>(int uplo, int trans, int64_t n, int64_t k, const double *A, int64_t lda,
+                      double *C, int64_t ldc, cudaStream_t s, const int *skip) {
+  return dsyrk_device_skip(uplo, trans, n, k, -1.0, A, lda, 1.0, C, ldc, s, skip);
+}
+template <>
+int syrk_skip<float>(int uplo, int trans, int64_t n, int64_t k, const float *A, int64_t lda,
+                     float *C, int64_t ldc, cudaStream_t s, const int *skip) {
+  return ssyrk_device_skip(uplo, trans, n, k, -1.0f, A, lda, 1.0f, C, ldc, s, skip);
+}
+
+template <typename T>
+static int potrf_diag_block(bool upper, int64_t nb, T *D, int64_t lda, int *info, int64_t off,
+                            cudaStream_t s) {
   for (int64_t j0 = 0; j0 < nb; j0 += PANEL_NB) {
     const int jb = (int)((nb - j0) < PANEL_NB ? (nb - j0) : PANEL_NB);
-    double *E = D + j0 + j0 * lda;
-    { potf2_kernel<double><<<1, 256, 0, s>>>(upper ? 1 : 0, jb, E, lda, info, off + j0); count_launch(); }
+    T *E = D + j0 + j0 * lda;
+    { potf2_kernel<T><<<1, 256, 0, s>>>(upper ? 1 : 0, jb, E, lda, info, off + j0); count_launch(); }
     const int64_t rest = nb - j0 - jb;
     if (rest <= 0) continue;
     int st;
     if (!upper) {
-      double *P = E + jb;
-      if ((st = dtrsm_device_skip(1, 1, 1, 1, rest, jb, 1.0, E, lda, P, lda, s, info))) return st;
-      if ((st = dsyrk_device_skip(1, 0, rest, jb, -1.0, P, lda, 1.0, P + jb * lda, lda, s, info)))
-        return st;
+      T *P = E + jb;
+      if ((st = trsm_skip<T>(1, 1, 1, 1, rest, jb, E, lda, P, lda, s, info))) return st;
+      if ((st = syrk_skip<T>(1, 0, rest, jb, P, lda, P + jb * lda, lda, s, info))) return st;
     } else {
-      double *P = E + jb * lda;
-      if ((st = dtrsm_device_skip(0, 0, 1, 1, jb, rest, 1.0, E, lda, P, lda, s, info))) return st;
-      if ((st = dsyrk_device_skip(0, 1, rest, jb, -1.0, P, lda, 1.0, P + jb, lda, s, info)))
-        return st;
+      T *P = E + jb * lda;
+      if ((st = trsm_skip<T>(0, 0, 1, 1, jb, rest, E, lda, P, lda, s, info))) return st;
+      if ((st = syrk_skip<T>(0, 1, rest, jb, P, lda, P + jb, lda, s, info))) return st;
     }
   }
   return GB_SUCCESS;
 }
 
-int potrf_device(int uplo, int64_t n, double *A, int64_t lda, int *info, int gemm_mode,
-                 cudaStream_t s) {
+// Trailing update C -= P P^T (lower) or P^T P (upper) of a 256-wide step:
+// FP64 native or emulated (gemm_mode 1); FP32 on the tensor cores when large.
+static int potrf_trailing(bool upper, int64_t rest, int64_t jb, const double *P, int64_t lda,
+                          double *C, int *info, int gemm_mode, cudaStream_t s) {
+  if (gemm_mode == 1 && rest >= 256 && jb >= 64)
+    return upper ? dgemm_emulated(1, 0, rest, rest, jb, -1.0, P, lda, P, lda, 1.0, C, lda, 0, s, 2,
+                                  info)
+                 : dgemm_emulated(0, 1, rest, rest, jb, -1.0, P, lda, P, lda, 1.0, C, lda, 0, s, 1,
+                                  info);
+  return syrk_skip<double>(upper ? 0 : 1, upper ? 1 : 0, rest, jb, P, lda, C, lda, s, info);
+}
+static int potrf_trailing(bool upper, int64_t rest, int64_t jb, const float *P, int64_t lda,
+                          float *C, int *info, int, cudaStream_t s) {
+  const int mode = gb_get_sgemm_mode();
+  if (mode == GB_SGEMM_TENSOR || (mode == GB_SGEMM_AUTO && rest >= 1024 && jb >= 64))
+    return upper ? sgemm_tc(1, 0, rest, rest, jb, -1.0f, P, lda, P, lda, 1.0f, C, lda, s, 2, info)
+                 : sgemm_tc(0, 1, rest, rest, jb, -1.0f, P, lda, P, lda, 1.0f, C, lda, s, 1, info);
+  return syrk_skip<float>(upper ? 0 : 1, upper ? 1 : 0, rest, jb, P, lda, C, lda, s, info);
+}
+
+// Cholesky, blocked like lapack/potrf/potrf_L_single.c / potrf_U_single.c:
+// 256-wide block columns; the diagonal block is factored by 32-wide steps
+// (potf2 + TRSM + SYRK inside the block); the panel below (right of) it is
+// solved against the block's triangle, and the trailing matrix gets one
+// rank-256 SYRK (see potrf_trailing).  Every step after a non-positive pivot
+// is skipped on the device (info), so the matrix is left as it was at the
+// failing column.
+template <typename T>
+int potrf_device_t(int uplo, int64_t n, T *A, int64_t lda, int *info, int gemm_mode,
+                   cudaStream_t s) {
   GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
   const bool upper = uplo == 0;
   for (int64_t j0 = 0; j0 < n; j0 += POTRF_NB) {
     const int64_t jb = (n - j0) < POTRF_NB ? (n - j0) : POTRF_NB;
-    double *D = A + j0 + j0 * lda;
-    int st = potrf_diag_block(upper, jb, D, lda, info, j0, s);
+    T *D = A + j0 + j0 * lda;
+    int st = potrf_diag_block<T>(upper, jb, D, lda, info, j0, s);
     if (st) return st;
     const int64_t rest = n - j0 - jb;
     if (rest <= 0) continue;
-    const bool emulated = gemm_mode == 1 && rest >= 256 && jb >= 64;
     if (!upper) {
-      double *P = A + (j0 + jb) + j0 * lda;  // rest x jb
-      double *C = P + jb * lda;
-      if ((st = dtrsm_device_skip(1, 1, 1, 1, rest, jb, 1.0, D, lda, P, lda, s, info))) return st;
-      st = emulated ? dgemm_emulated(0, 1, rest, rest, jb, -1.0, P, lda, P, lda, 1.0, C, lda, 0, s,
-                                     1, info)
-                    : dsyrk_device_skip(1, 0, rest, jb, -1.0, P, lda, 1.0, C, lda, s, info);
+      T *P = A + (j0 + jb) + j0 * lda;  // rest x jb
+      if ((st = trsm_skip<T>(1, 1, 1, 1, rest, jb, D, lda, P, lda, s, info))) return st;
+      st = potrf_trailing(false, rest, jb, P, lda, P + jb * lda, info, gemm_mode, s);
     } else {
-      double *P = A + j0 + (j0 + jb) * lda;  // jb x rest
-      double *C = P + jb;
-      if ((st = dtrsm_device_skip(0, 0, 1, 1, jb, rest, 1.0, D, lda, P, lda, s, info))) return st;
-      st = emulated ? dgemm_emulated(1, 0, rest, rest, jb, -1.0, P, lda, P, lda, 1.0, C, lda, 0, s,
-                                     2, info)
-                    : dsyrk_device_skip(0, 1, rest, jb, -1.0, P, lda, 1.0, C, lda, s, info);
+      T *P = A + j0 + (j0 + jb) * lda;  // jb x rest
+      if ((st = trsm_skip<T>(0, 0, 1, 1, jb, rest, D, lda, P, lda, s, info))) return st;
+      st = potrf_trailing(true, rest, jb, P, lda, P + jb, info, gemm_mode, s);
     }
     if (st) return st;
   }
   return check_cuda(cudaGetLastError(), "potrf");
+}
+
+int potrf_device(int uplo, int64_t n, double *A, int64_t lda, int *info, int gemm_mode,
+                 cudaStream_t s) {
+  return potrf_device_t<double>(uplo, n, A, lda, info, gemm_mode, s);
+}
+
+int spotrf_device(int uplo, int64_t n, float *A, int64_t lda, int *info, cudaStream_t s) {
+  return potrf_device_t<float>(uplo, n, A, lda, info, 0, s);
+}
+
+// A X = B with A = L L^T (lower) or U^T U (upper): dpotrs.f:135-160.
+int potrs_device(int uplo, int64_t n, int64_t nrhs, const double *A, int64_t lda, double *B,
+                 int64_t ldb, cudaStream_t s) {
+  int st;
+  if (uplo == 1) {
+    if ((st = dtrsm_device(0, 1, 0, 1, n, nrhs, 1.0, A, lda, B, ldb, s))) return st;
+    return dtrsm_device(0, 1, 1, 1, n, nrhs, 1.0, A, lda, B, ldb, s);
+  }
+  if ((st = dtrsm_device(0, 0, 1, 1, n, nrhs, 1.0, A, lda, B, ldb, s))) return st;
+  return dtrsm_device(0, 0, 0, 1, n, nrhs, 1.0, A, lda, B, ldb, s);
 }
 
 int pivots_to_perm(int64_t n, const int *ipiv, int *perm, cudaStream_t s) {

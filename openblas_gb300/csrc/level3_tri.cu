@@ -117,8 +117,7 @@ template <>
 void gemm_update<float>(int ta, int tb, int64_t m, int64_t n, int64_t k, const float *A,
                         int64_t lda, const float *B, int64_t ldb, float *C, int64_t ldc,
                         cudaStream_t s, const int *skip) {
-  (void)skip;
-  launch_sgemm_fp32(ta, tb, m, n, k, -1.0f, A, lda, B, ldb, 1.0f, C, ldc, s);
+  launch_sgemm_fp32_tri(ta, tb, m, n, k, -1.0f, A, lda, B, ldb, 1.0f, C, ldc, 0, s, skip);
 }
 
 }  // namespace
@@ -193,6 +192,21 @@ int dtrsm_device_skip(int side, int uplo, int trans, int unit, int64_t m, int64_
 int strsm_device(int side, int uplo, int trans, int unit, int64_t m, int64_t n, float alpha,
                  const float *A, int64_t lda, float *B, int64_t ldb, cudaStream_t s) {
   return trsm_device_t<float>(side, uplo, trans, unit, m, n, alpha, A, lda, B, ldb, s);
+}
+
+int strsm_device_skip(int side, int uplo, int trans, int unit, int64_t m, int64_t n,
+                      float alpha, const float *A, int64_t lda, float *B, int64_t ldb,
+                      cudaStream_t s, const int *skip) {
+  return trsm_device_t<float>(side, uplo, trans, unit, m, n, alpha, A, lda, B, ldb, s, skip);
+}
+
+int ssyrk_device_skip(int uplo, int trans, int64_t n, int64_t k, float alpha, const float *A,
+                      int64_t lda, float beta, float *C, int64_t ldc, cudaStream_t s,
+                      const int *skip) {
+  if (n == 0) return GB_SUCCESS;
+  launch_sgemm_fp32_tri(trans ? 1 : 0, trans ? 0 : 1, n, n, k, alpha, A, lda, A, lda, beta, C,
+                        ldc, uplo == 1 ? 1 : 2, s, skip);
+  return check_cuda(cudaGetLastError(), "syrk launch");
 }
 
 // uplo 0 = Upper, 1 = Lower; trans 0: C = alpha*A*A^T + beta*C (A n x k),

@@ -284,14 +284,19 @@ struct Mixed {
   double *part_lo = nullptr;  // low parts of the compensated GEMV
   float *SX2 = nullptr;     // n x nrhs FP32 work (permuted right-hand sides)
   int *perm = nullptr;      // final row permutation of the FP32 LU
+  bool chol = false;        // Cholesky factors (no interchanges, mirrored triangles)
   float *Linv = nullptr, *Uinv = nullptr;  // inverted 64x64 diagonal blocks of L, U
 
   // X32 = (LU)^-1 P * X32 (in place through SX2): the FP32 solve of the refinement
   int solve32(float *V, int64_t k) {
     static const bool trsm_solve = getenv("GB_MIXED_SOLVE") && !strcmp(getenv("GB_MIXED_SOLVE"), "trsm");
-    if (trsm_solve) return getrs_device<float>(0, n, k, SA, n, ipiv, V, n, s);
-    int st = apply_perm<float>(n, k, perm, V, n, SX2, n, s);
-    if (st) return st;
+    int st;
+    if (chol) {
+      GB_CUDA(cudaMemcpyAsync(SX2, V, (size_t)n * k * sizeof(float), cudaMemcpyDeviceToDevice, s));
+    } else {
+      if (trsm_solve) return getrs_device<float>(0, n, k, SA, n, ipiv, V, n, s);
+      if ((st = apply_perm<float>(n, k, perm, V, n, SX2, n, s))) return st;
+    }
     if ((st = lu_block_solve<float>(n, k, SA, n, Linv, Uinv, SX2, n, s))) return st;
     GB_CUDA(cudaMemcpyAsync(V, SX2, (size_t)n * k * sizeof(float), cudaMemcpyDeviceToDevice, s));
     return GB_SUCCESS;
@@ -682,6 +687,154 @@ int dsgesv_device(int64_t n, int64_t nrhs, double *A, int64_t lda, int *ipiv, co
   return finish_blocking(s);
 }
 
+// Mixed-precision Cholesky solve, lapack-netlib/SRC/dsposv.f:232-434: the
+// reference's steps and ITER codes (-2 FP32 overflow, -3 SPOTRF failure,
+// -31 no convergence in ITERMAX=30 steps) with the FP32 factorisation and
+// solves on the GPU.  The symmetric products (DLANSY, DSYMM) use one full
+// FP64 copy of A mirrored from its stored triangle; the FP32 factor is
+// mirrored onto its other half so the chained two-triangle solve applies
+// (L then L^T, or U^T then U).  A is overwritten only by the FP64 fallback
+// (dsposv.f:425-433: DPOTRF, DPOTRS).
+int dsposv_device(int uplo, int64_t n, int64_t nrhs, double *A, int64_t lda, const double *B,
+                  int64_t ldb, double *X, int64_t ldx, int *iter, int *info, cudaStream_t s) {
+  *iter = 0;
+  *info = 0;
+  if (n == 0) return GB_SUCCESS;
+  const int itermax = 30;
+  const int lower = uplo == 1;
+  Scratch full((size_t)n * n * sizeof(double), s);
+  if (!full.p) return GB_ERR_ALLOC;
+  double *Af = full.as<double>();
+  GB_CUDA(cudaMemcpy2DAsync(Af, n * 8, A, lda * 8, n * 8, n, cudaMemcpyDeviceToDevice, s));
+  int st = mirror_triangle<double>(n, Af, n, lower, s);
+  if (st) return st;
+  Mixed M;
+  M.chol = true;
+  M.n = n;
+  M.nrhs = nrhs;
+  M.A = Af;
+  M.lda = n;
+  M.B = B;
+  M.ldb = ldb;
+  M.X = X;
+  M.ldx = ldx;
+  M.s = s;
+  M.nchunks = (int)((n + GEMV_COL_CHUNK - 1) / GEMV_COL_CHUNK);
+  const size_t bytes_sa = ((size_t)n * n * 4 + 255) & ~size_t(255);
+  const size_t bytes_sx = ((size_t)n * nrhs * 4 + 255) & ~size_t(255);
+  const size_t bytes_r = ((size_t)n * nrhs * 8 + 255) & ~size_t(255);
+  const size_t bytes_p = ((size_t)n * (M.nchunks > 64 ? M.nchunks : 64) * 8 + 255) & ~size_t(255);
+  const int64_t nblk64 = (n + 63) / 64;
+  const size_t bytes_inv = ((size_t)nblk64 * 64 * 64 * 4 + 255) & ~size_t(255);
+  Scratch ws2(bytes_sx + 2 * bytes_inv, s);
+  if (!ws2.p) return GB_ERR_ALLOC;
+  M.SX2 = ws2.as<float>();
+  M.Linv = reinterpret_cast<float *>(ws2.as<char>() + bytes_sx);
+  M.Uinv = reinterpret_cast<float *>(ws2.as<char>() + bytes_sx + bytes_inv);
+  Scratch ws(bytes_sa + bytes_sx + bytes_r + bytes_p + 1024 + (size_t)nrhs * 32, s);
+  if (!ws.p) return GB_ERR_ALLOC;
+  char *base = ws.as<char>();
+  M.SA = reinterpret_cast<float *>(base);
+  M.SX = reinterpret_cast<float *>(base + bytes_sa);
+  M.R = reinterpret_cast<double *>(base + bytes_sa + bytes_sx);
+  M.part = reinterpret_cast<double *>(base + bytes_sa + bytes_sx + bytes_r);
+  M.dnorm = reinterpret_cast<double *>(base + bytes_sa + bytes_sx + bytes_r + bytes_p);
+  M.dflag = reinterpret_cast<int *>(M.dnorm + 2 * nrhs + 8);
+  Host hx((size_t)(2 * nrhs > 128 ? 2 * nrhs : 128) + 64);
+  if (!hx.p) return set_error(GB_ERR_ALLOC, "pinned host scratch");
+  M.hx = &hx;
+  bool fallback = false;
+
+  // anrm = DLANSY('I') = ||A||_inf of the symmetric matrix (dsposv.f:282-284)
+  {
+    dim3 g((unsigned)((n + 255) / 256), (unsigned)M.nchunks);
+    { absrowsum_kernel<<<g, 256, 0, s>>>(n, n, Af, n, GEMV_COL_CHUNK, M.part); count_launch(); }
+    { rowsum_max_kernel<<<1, 256, 0, s>>>(n, M.nchunks, M.part, M.dnorm); count_launch(); }
+  }
+  GB_CUDA(cudaMemcpyAsync(hx.p, M.dnorm, sizeof(double), cudaMemcpyDeviceToHost, s));
+  if ((st = finish_blocking(s))) return st;
+  const double cte = hx.p[0] * (DBL_EPSILON * 0.5) * sqrt((double)n) * 1.0;
+
+  // SX = fp32(B), SA = fp32(A) with overflow checks (dsposv.f:291-304; the
+  // mirrored copy holds exactly the stored triangle's values)
+  GB_CUDA(cudaMemsetAsync(M.dflag, 0, 3 * sizeof(int), s));
+  { lag2s_kernel<<<grid_for(n * nrhs), 256, 0, s>>>(n, nrhs, B, ldb, M.SX, n, M.dflag); count_launch(); }
+  { lag2s_kernel<<<grid_for(n * n), 256, 0, s>>>(n, n, Af, n, M.SA, n, M.dflag + 1); count_launch(); }
+  int *dinfo = M.dflag + 2;
+  GB_CUDA(cudaMemcpyAsync(hx.p, M.dflag, 2 * sizeof(int), cudaMemcpyDeviceToHost, s));
+  if ((st = finish_blocking(s))) return st;
+  int flags[2];
+  memcpy(flags, hx.p, sizeof(flags));
+  if (flags[0] || flags[1]) {
+    *iter = -2;
+    fallback = true;
+  }
+  if (!fallback) {
+    // spotrf (dsposv.f:310): a failed FP32 factor sends the solve to FP64
+    {
+      ProfileScope prof("mixed_spotrf", s);
+      if ((st = spotrf_device(uplo, n, M.SA, n, dinfo, s))) return st;
+    }
+    GB_CUDA(cudaMemcpyAsync(hx.p, dinfo, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if ((st = finish_blocking(s))) return st;
+    int sinfo;
+    memcpy(&sinfo, hx.p, sizeof(int));
+    if (sinfo != 0) {
+      *iter = -3;
+      fallback = true;
+    }
+  }
+  if (!fallback) {
+    if ((st = mirror_triangle<float>(n, M.SA, n, lower, s))) return st;
+    if ((st = chol_block_inverses<float>(n, M.SA, n, M.Linv, M.Uinv, s))) return st;
+    if ((st = M.solve32(M.SX, nrhs))) return st;
+    { lag2d_kernel<<<grid_for(n * nrhs), 256, 0, s>>>(n, nrhs, M.SX, n, X, ldx, 0); count_launch(); }
+    bool done = false;
+    for (int it = 0; it <= itermax; ++it) {
+      if ((st = M.residual())) return st;
+      bool ok = false;
+      double worst = 0.0;
+      if ((st = M.converged(cte, &ok, &worst))) return st;
+      if (config().verbose >= 2)
+        fprintf(stderr, "libgbblas dsposv: refinement %d  max|r|/max|x| = %.3e (cte %.3e)\n", it,
+                worst, cte);
+      if (ok) {
+        *iter = it;
+        done = true;
+        break;
+      }
+      if (it == itermax) break;
+      bool ovf = false;
+      if ((st = M.precond(M.R, n, nrhs, &ovf))) return st;
+      if (ovf) {
+        *iter = -2;
+        fallback = true;
+        break;
+      }
+      { lag2d_kernel<<<grid_for(n * nrhs), 256, 0, s>>>(n, nrhs, M.SX, n, X, ldx, 1); count_launch(); }
+    }
+    if (!done && !fallback) {
+      *iter = -itermax - 1;
+      fallback = true;
+    }
+  }
+  if (fallback) {
+    const int mode = gb_get_dgemm_mode() != GB_DGEMM_NATIVE ? 1 : 0;
+    if ((st = potrf_device(uplo, n, A, lda, dinfo, mode, s))) return st;
+    GB_CUDA(cudaMemcpyAsync(hx.p, dinfo, sizeof(int), cudaMemcpyDeviceToHost, s));
+    if ((st = finish_blocking(s))) return st;
+    int dinf;
+    memcpy(&dinf, hx.p, sizeof(int));
+    if (dinf != 0) {
+      *info = dinf;
+      return GB_SUCCESS;
+    }
+    GB_CUDA(cudaMemcpy2DAsync(X, ldx * 8, B, ldb * 8, n * 8, nrhs, cudaMemcpyDeviceToDevice, s));
+    if ((st = potrs_device(uplo, n, nrhs, A, lda, X, ldx, s))) return st;
+  }
+  return finish_blocking(s);
+}
+
 }  // namespace gb
 
 using namespace gb;
@@ -744,6 +897,64 @@ int gb_dsgesv_dev(int64_t n, int64_t nrhs, double *A, int64_t lda, int *ipiv, co
   int st = ensure_init();
   if (st) return st;
   return dsgesv_device(n, nrhs, A, lda, ipiv, B, ldb, X, ldx, iter, info, true, stream());
+}
+
+// dsposv.f:236-251: checks in order UPLO, N, NRHS, LDA, LDB, LDX
+static int dsposv_checks(char u, int64_t n, int64_t nrhs, int64_t lda, int64_t ldb, int64_t ldx,
+                         int *uplo) {
+  *uplo = u == 'U' ? 0 : u == 'L' ? 1 : -1;
+  if (*uplo < 0) return 1;
+  if (n < 0) return 2;
+  if (nrhs < 0) return 3;
+  if (lda < (n > 1 ? n : 1)) return 5;
+  if (ldb < (n > 1 ? n : 1)) return 7;
+  if (ldx < (n > 1 ? n : 1)) return 9;
+  return 0;
+}
+
+int dsposv_(const char *UPLO, const blasint *N, const blasint *NRHS, double *a,
+            const blasint *ldA, const double *b, const blasint *ldB, double *x,
+            const blasint *ldX, double *work, float *swork, blasint *ITER, blasint *Info) {
+  (void)work;
+  (void)swork;
+  int64_t n = *N, nrhs = *NRHS, lda = *ldA, ldb = *ldB, ldx = *ldX;
+  *ITER = 0;
+  int uplo = 0;
+  const int code = dsposv_checks(upch(UPLO), n, nrhs, lda, ldb, ldx, &uplo);
+  if (code) {
+    *Info = -code;
+    call_xerbla("DSPOSV", code);
+    return 0;
+  }
+  *Info = 0;
+  if (n == 0) return 0;
+  if (ensure_init()) return 0;
+  cudaStream_t s = stream();
+  Operand A(a, n, n, lda, 8), B(b, n, nrhs, ldb, 8), X(x, n, nrhs, ldx, 8);
+  if (A.bind(true, s) || B.bind(true, s) || X.bind(false, s)) return 0;
+  int it = 0, inf = 0;
+  if (dsposv_device(uplo, n, nrhs, A.d<double>(), A.dld, B.d<double>(), B.dld, X.d<double>(),
+                    X.dld, &it, &inf, s))
+    return 0;
+  if (it < 0) A.unbind(s);  // A holds the FP64 factor only after a fallback
+  X.unbind(s);
+  if (finish_blocking(s)) return 0;
+  *ITER = it;
+  *Info = inf;
+  return 0;
+}
+
+int gb_dsposv_dev(char uplo, int64_t n, int64_t nrhs, double *A, int64_t lda, const double *B,
+                  int64_t ldb, double *X, int64_t ldx, int *iter, int *info) {
+  int up = 0;
+  const int code = dsposv_checks(upch(uplo), n, nrhs, lda, ldb, ldx, &up);
+  if (code) {
+    call_xerbla("DSPOSV", code);
+    return GB_ERR_INVALID_VALUE;
+  }
+  int st = ensure_init();
+  if (st) return st;
+  return dsposv_device(up, n, nrhs, A, lda, B, ldb, X, ldx, iter, info, stream());
 }
 
 }  // extern "C"

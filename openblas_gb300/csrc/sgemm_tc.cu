@@ -54,6 +54,8 @@ struct Params {
   float *C;
   const int *rflag;  // rows of op(A) holding Inf/NaN: left to the fixup kernel
   const int *cflag;  // columns of op(B) holding Inf/NaN
+  int tri;           // 0 all of C; 1 only i >= j; 2 only i <= j
+  const int *skip;   // device flag: when nonzero C is left unchanged
   int *status;
 };
 
@@ -65,6 +67,13 @@ __device__ __forceinline__ void tile_coords(int tile, const Params &p, int &mt, 
   const int in = tile % span;
   mt = first_m + in % gm;
   nt = in / gm;
+}
+
+// A tile takes part unless it lies wholly in the triangle left alone.
+__device__ __forceinline__ bool tile_active(int mt, int nt, const Params &p) {
+  if (p.tri == 1) return mt * BM + BM - 1 >= nt * BN;
+  if (p.tri == 2) return mt * BM <= nt * BN + BN - 1;
+  return true;
 }
 
 __global__ void __launch_bounds__(NUM_THREADS, 1)
@@ -132,6 +141,7 @@ sgemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tmA,
       for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
         int mt, nt;
         tile_coords(tile, p, mt, nt);
+        if (!tile_active(mt, nt, p)) continue;
         for (int kb = 0; ok && kb < p.kblocks; ++kb) {
           if (!mbar_wait(&aempty[as], aph ^ 1u, abort_flag, WAIT_LIMIT_NS)) {
             fail(1);
@@ -182,6 +192,9 @@ sgemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tmA,
       uint32_t aph = 0, bph = 0, acc_phase = 0;
       bool ok = true;
       for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
+        int mt, nt;
+        tile_coords(tile, p, mt, nt);
+        if (!tile_active(mt, nt, p)) continue;
         if (!mbar_wait(&tempty[acc], acc_phase ^ 1u, abort_flag, WAIT_LIMIT_NS)) {
           fail(3);
           ok = false;
@@ -246,9 +259,11 @@ sgemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tmA,
     int acc = 0;
     uint32_t acc_phase = 0;
     const bool read_c = p.beta != 0.f;
+    const bool skipped = p.skip != nullptr && *p.skip != 0;  // drain TMEM, write nothing
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
       int mt, nt;
       tile_coords(tile, p, mt, nt);
+      if (!tile_active(mt, nt, p)) continue;
       const bool got = mbar_wait(&tfull[acc], acc_phase, abort_flag, WAIT_LIMIT_NS);
       // the warp-wide tcgen05.ld below needs a converged warp: agree first
       if (!__all_sync(0xffffffffu, got)) {
@@ -268,7 +283,7 @@ sgemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tmA,
         // columns of this chunk that the fixup kernel owns (lane j reads column j)
         const int64_t cj = col0 + c * 32 + lane;
         const unsigned skip = __ballot_sync(0xffffffffu, cj < p.n && p.cflag[cj] != 0);
-        if (grow < p.m && p.rflag[grow] == 0) {
+        if (!skipped && grow < p.m && p.rflag[grow] == 0) {
           float *cp = p.C + grow + (col0 + c * 32) * p.ldc;
           const int64_t ncol = p.n - (col0 + c * 32);
           float old[32];
@@ -276,8 +291,11 @@ sgemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tmA,
           for (int j = 0; j < 32; ++j) old[j] = (read_c && j < ncol) ? cp[j * p.ldc] : 0.f;
 #pragma unroll
           for (int j = 0; j < 32; ++j)
-            if (j < ncol && !((skip >> j) & 1u))
+            if (j < ncol && !((skip >> j) & 1u)) {
+              const int64_t col = col0 + c * 32 + j;
+              if ((p.tri == 1 && grow < col) || (p.tri == 2 && grow > col)) continue;
               cp[j * p.ldc] = p.alpha * __uint_as_float(r[j]) + p.beta * old[j];
+            }
         }
       }
       tc_fence_before();
@@ -375,9 +393,11 @@ sgemm_fixup_kernel(int64_t m, int64_t n, int64_t k, float alpha, const float *__
                    int64_t lda, int ta, const float *__restrict__ B, int64_t ldb, int tb,
                    float beta, float *__restrict__ C, int64_t ldc, const int *__restrict__ rflag,
                    const int *__restrict__ rlist, const int *__restrict__ rcount,
-                   const int *__restrict__ clist, const int *__restrict__ ccount) {
+                   const int *__restrict__ clist, const int *__restrict__ ccount, int tri,
+                   const int *__restrict__ skipf) {
   const int64_t nr = *rcount, nc = *ccount;
   if (nr == 0 && nc == 0) return;
+  if (skipf && *skipf) return;
   const int64_t t1 = nr * n, total = t1 + nc * m;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
        e += (int64_t)gridDim.x * blockDim.x) {
@@ -391,6 +411,7 @@ sgemm_fixup_kernel(int64_t m, int64_t n, int64_t k, float alpha, const float *__
       i = e2 % m;
       if (rflag[i]) continue;  // done by the row pass
     }
+    if ((tri == 1 && i < j) || (tri == 2 && i > j)) continue;  // the other triangle
     float acc = 0.f;
     for (int64_t q = 0; q < k; ++q) {
       const float a = ta ? A[q + i * lda] : A[i + q * lda];
@@ -408,7 +429,7 @@ sgemm_fixup_kernel(int64_t m, int64_t n, int64_t k, float alpha, const float *__
 // kernel.  Assumes m, n, k > 0.
 int sgemm_tc(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha, const float *A,
              int64_t lda, const float *B, int64_t ldb, float beta, float *C, int64_t ldc,
-             cudaStream_t s) {
+             cudaStream_t s, int tri, const int *skip) {
   using namespace s3;
   if (m > (int64_t)1 << 22 || n > (int64_t)1 << 22 || k > (int64_t)1 << 24)
     return set_error(GB_ERR_UNSUPPORTED, "sgemm_tc: dimension too large");
@@ -456,6 +477,8 @@ int sgemm_tc(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha, const
   p.C = C;
   p.rflag = rflag;
   p.cflag = cflag;
+  p.tri = tri;
+  p.skip = skip;
   p.status = ctx().d_status;
   const int ntiles = p.m_tiles * p.n_tiles;
   const int grid = ntiles < sm_count() ? ntiles : sm_count();
@@ -466,7 +489,7 @@ int sgemm_tc(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha, const
   }
   { sgemm_fixup_kernel<<<sm_count() * 4, 256, 0, s>>>(m, n, k, alpha, A, lda, ta, B, ldb, tb, beta,
                                                      C, ldc, rflag, rlist, counts, clist,
-                                                     counts + 1); count_launch(); }
+                                                     counts + 1, tri, skip); count_launch(); }
   return check_cuda(cudaGetLastError(), "sgemm_tc");
 }
 

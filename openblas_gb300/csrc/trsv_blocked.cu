@@ -30,12 +30,13 @@ constexpr int TB = 64;           // diagonal block size
 template <typename T>
 constexpr int maxr() { return sizeof(T) == 4 ? 8 : 4; }
 
-// Inverse of the diagonal block of L (unit lower, lower = 1) or U (upper,
-// lower = 0).  One CTA per block, thread c computes column c of the inverse
+// Inverse of a diagonal block of the lower (lower = 1) or upper (lower = 0)
+// triangle, unit diagonal when `unit` (the L of an LU) and non-unit
+// otherwise.  One CTA per block, thread c computes column c of the inverse
 // by substitution on e_c.  Blocks shorter than TB are padded with identity.
 template <typename T>
 __global__ void __launch_bounds__(TB)
-diag_inverse_kernel(int64_t n, const T *__restrict__ A, int64_t lda, int lower,
+diag_inverse_kernel(int64_t n, const T *__restrict__ A, int64_t lda, int lower, int unit,
                     T *__restrict__ inv) {
   __shared__ T D[TB][TB + 1];
   const int64_t b = blockIdx.x;
@@ -45,7 +46,7 @@ diag_inverse_kernel(int64_t n, const T *__restrict__ A, int64_t lda, int lower,
     const int r = e % TB, c = e / TB;
     T v = T(0);
     if (r < nb && c < nb) v = A[(r0 + r) + (r0 + c) * lda];
-    if (r == c && (r >= nb || lower)) v = T(1);  // unit diagonal of L, identity padding
+    if (r == c && (r >= nb || unit)) v = T(1);  // unit diagonal, identity padding
     D[r][c] = v;
   }
   __syncthreads();
@@ -59,7 +60,7 @@ diag_inverse_kernel(int64_t n, const T *__restrict__ A, int64_t lda, int lower,
       T s = x[r];
 #pragma unroll
       for (int k = 0; k < r; ++k) s = fma(-D[r][k], x[k], s);
-      x[r] = s;  // unit diagonal
+      x[r] = unit ? s : s / D[r][r];
     }
   } else {
 #pragma unroll
@@ -239,9 +240,62 @@ chain_solve_kernel(int64_t n, int nrhs, const T *__restrict__ A, int64_t lda,
 template <typename T>
 int lu_block_inverses(int64_t n, const T *A, int64_t lda, T *Linv, T *Uinv, cudaStream_t s) {
   const unsigned nblk = (unsigned)((n + TB - 1) / TB);
-  { diag_inverse_kernel<T><<<nblk, TB, 0, s>>>(n, A, lda, 1, Linv); count_launch(); }
-  { diag_inverse_kernel<T><<<nblk, TB, 0, s>>>(n, A, lda, 0, Uinv); count_launch(); }
+  { diag_inverse_kernel<T><<<nblk, TB, 0, s>>>(n, A, lda, 1, 1, Linv); count_launch(); }
+  { diag_inverse_kernel<T><<<nblk, TB, 0, s>>>(n, A, lda, 0, 0, Uinv); count_launch(); }
   return check_cuda(cudaGetLastError(), "diag_inverse");
+}
+
+// Cholesky: both triangles of the mirrored factor have non-unit diagonals.
+template <typename T>
+int chol_block_inverses(int64_t n, const T *A, int64_t lda, T *Linv, T *Uinv, cudaStream_t s) {
+  const unsigned nblk = (unsigned)((n + TB - 1) / TB);
+  { diag_inverse_kernel<T><<<nblk, TB, 0, s>>>(n, A, lda, 1, 0, Linv); count_launch(); }
+  { diag_inverse_kernel<T><<<nblk, TB, 0, s>>>(n, A, lda, 0, 0, Uinv); count_launch(); }
+  return check_cuda(cudaGetLastError(), "diag_inverse");
+}
+
+// Copy the strictly lower triangle onto the strictly upper one, transposed
+// (from_lower = 1), or the other way round: a Cholesky factor L (or U) then
+// holds L^T (U^T) in its other half, and the two-triangle solve applies.
+template <typename T>
+__global__ void mirror_triangle_kernel(int64_t n, T *__restrict__ A, int64_t lda, int from_lower) {
+  __shared__ T tile[32][33];
+  const int64_t bi = blockIdx.y, bj = blockIdx.x;  // source tile (rows bi, cols bj), bi >= bj
+  if (bi < bj) return;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+  // read the source triangle, coalesced along the rows of the source tile;
+  // tile[a][b] always holds the pair (r, c) = (bi*32 + a, bj*32 + b), r > c
+  if (from_lower) {
+    for (int yy = ty; yy < 32; yy += 8) {
+      const int64_t r = bi * 32 + tx, c = bj * 32 + yy;  // lower element (r, c)
+      if (r < n && c < n && r > c) tile[tx][yy] = A[r + c * lda];
+    }
+  } else {
+    for (int yy = ty; yy < 32; yy += 8) {
+      const int64_t r = bi * 32 + yy, c = bj * 32 + tx;  // upper element (c, r)
+      if (r < n && c < n && r > c) tile[yy][tx] = A[c + r * lda];
+    }
+  }
+  __syncthreads();
+  if (from_lower) {
+    for (int yy = ty; yy < 32; yy += 8) {
+      const int64_t r = bi * 32 + yy, c = bj * 32 + tx;  // write (c, r) = (r, c)
+      if (r < n && c < n && r > c) A[c + r * lda] = tile[yy][tx];
+    }
+  } else {
+    for (int yy = ty; yy < 32; yy += 8) {
+      const int64_t r = bi * 32 + tx, c = bj * 32 + yy;  // write (r, c) = (c, r)
+      if (r < n && c < n && r > c) A[r + c * lda] = tile[tx][yy];
+    }
+  }
+}
+
+template <typename T>
+int mirror_triangle(int64_t n, T *A, int64_t lda, int from_lower, cudaStream_t s) {
+  if (n <= 1) return GB_SUCCESS;
+  const unsigned nt = (unsigned)((n + 31) / 32);
+  { mirror_triangle_kernel<T><<<dim3(nt, nt), 256, 0, s>>>(n, A, lda, from_lower); count_launch(); }
+  return check_cuda(cudaGetLastError(), "mirror_triangle");
 }
 
 template <typename T, int R>
@@ -301,6 +355,12 @@ template int lu_block_inverses<float>(int64_t, const float *, int64_t, float *, 
                                       cudaStream_t);
 template int lu_block_inverses<double>(int64_t, const double *, int64_t, double *, double *,
                                        cudaStream_t);
+template int chol_block_inverses<float>(int64_t, const float *, int64_t, float *, float *,
+                                        cudaStream_t);
+template int chol_block_inverses<double>(int64_t, const double *, int64_t, double *, double *,
+                                         cudaStream_t);
+template int mirror_triangle<float>(int64_t, float *, int64_t, int, cudaStream_t);
+template int mirror_triangle<double>(int64_t, double *, int64_t, int, cudaStream_t);
 template int lu_block_solve<float>(int64_t, int64_t, const float *, int64_t, const float *,
                                    const float *, float *, int64_t, cudaStream_t);
 template int lu_block_solve<double>(int64_t, int64_t, const double *, int64_t, const double *,

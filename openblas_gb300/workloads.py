@@ -89,6 +89,14 @@ def spd(seed: int, n: int) -> np.ndarray:
     return np.asfortranarray(B @ B.T / n + np.eye(n))
 
 
+def spd_ill_conditioned(seed: int, n: int, kappa_exp: float) -> np.ndarray:
+    """U*diag(logspace(0,-kappa))*U^T with U from QR of seeded uniforms (SPD)."""
+    U, _ = np.linalg.qr(uniform(seed, (n, n)))
+    s = np.logspace(0.0, -float(kappa_exp), n)
+    A = (U * s) @ U.T
+    return np.asfortranarray((A + A.T) / 2)
+
+
 def ill_conditioned(seed: int, n: int, kappa_exp: float) -> np.ndarray:
     """U*diag(logspace(0,-kappa))*V^T with U, V from QR of seeded uniforms."""
     U, _ = np.linalg.qr(uniform(seed, (n, n)))

@@ -673,3 +673,138 @@ fallback:
   orc_dgetrs('N', n, nrhs, A, lda, ipiv, X, ldx);
   return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* DPOTRS / DSPOSV                                                           */
+/* ------------------------------------------------------------------------ */
+/* lapack-netlib/SRC/dpotrs.f:135-160: two triangular solves with the factor. */
+int orc_dpotrs(char uplo, int n, int nrhs, const double *A, int lda, double *B, int ldb) {
+  if (n <= 0 || nrhs <= 0) return 0;
+  if (upc(uplo) == 'L') {
+    orc_dtrsm('L', 'L', 'N', 'N', n, nrhs, 1.0, A, lda, B, ldb);
+    orc_dtrsm('L', 'L', 'T', 'N', n, nrhs, 1.0, A, lda, B, ldb);
+  } else {
+    orc_dtrsm('L', 'U', 'T', 'N', n, nrhs, 1.0, A, lda, B, ldb);
+    orc_dtrsm('L', 'U', 'N', 'N', n, nrhs, 1.0, A, lda, B, ldb);
+  }
+  return 0;
+}
+
+static void spotrs(int lower, int n, int nrhs, const float *A, int lda, float *B, int ldb) {
+  if (lower) {
+    orc_strsm('L', 'L', 'N', 'N', n, nrhs, 1.0f, A, lda, B, ldb);
+    orc_strsm('L', 'L', 'T', 'N', n, nrhs, 1.0f, A, lda, B, ldb);
+  } else {
+    orc_strsm('L', 'U', 'T', 'N', n, nrhs, 1.0f, A, lda, B, ldb);
+    orc_strsm('L', 'U', 'N', 'N', n, nrhs, 1.0f, A, lda, B, ldb);
+  }
+}
+
+/* element (i, j) of a symmetric matrix held in one triangle */
+static double sym_at(int lower, const double *A, int lda, int i, int j) {
+  if (lower ? i >= j : i <= j) return A[(size_t)j * lda + i];
+  return A[(size_t)i * lda + j];
+}
+
+/* DLANSY('I') (dlansy.f: infinity norm from the stored triangle) */
+static double dlansy_inf(int lower, int n, const double *A, int lda) {
+  double best = 0.0;
+  for (int i = 0; i < n; ++i) {
+    double s = 0.0;
+    for (int j = 0; j < n; ++j) s += fabs(sym_at(lower, A, lda, i, j));
+    if (s > best || isnan(s)) best = s;
+  }
+  return best;
+}
+
+/* W = W - A X with the stored triangle (DSYMM('L', uplo, ..., -1, A, X, 1, W)) */
+static void dsymm_minus(int lower, int n, int nrhs, const double *A, int lda, const double *X,
+                        int ldx, double *W, int ldw) {
+  for (int c = 0; c < nrhs; ++c)
+    for (int i = 0; i < n; ++i) {
+      double s = 0.0;
+      for (int j = 0; j < n; ++j) s += sym_at(lower, A, lda, i, j) * X[(size_t)c * ldx + j];
+      W[(size_t)c * ldw + i] -= s;
+    }
+}
+
+/* DLAT2S (dlat2s.f): FP32 copy of the stored triangle; 1 on overflow */
+static int lat2s(int lower, int n, const double *A, int lda, float *S, int lds) {
+  const double rmax = (double)FLT_MAX;
+  for (int j = 0; j < n; ++j)
+    for (int i = lower ? j : 0; i < (lower ? n : j + 1); ++i) {
+      const double v = A[(size_t)j * lda + i];
+      if (v < -rmax || v > rmax) return 1;
+      S[(size_t)j * lds + i] = (float)v;
+    }
+  return 0;
+}
+
+/* lapack-netlib/SRC/dsposv.f:232-434 */
+int orc_dsposv(char uplo, int n, int nrhs, double *A, int lda, const double *B, int ldb,
+               double *X, int ldx, int *iter) {
+  *iter = 0;
+  if (n <= 0) return 0;
+  const int lower = upc(uplo) == 'L';
+  const int itermax = 30;
+  const double anrm = dlansy_inf(lower, n, A, lda);
+  const double eps = DBL_EPSILON * 0.5; /* DLAMCH('Epsilon') */
+  const double cte = anrm * eps * sqrt((double)n) * 1.0;
+  float *sa = (float *)calloc((size_t)n * n, sizeof(float));
+  float *sx = (float *)malloc(sizeof(float) * (size_t)n * nrhs);
+  double *w = (double *)malloc(sizeof(double) * (size_t)n * nrhs);
+  int info = 0;
+  if (lag2s(n, nrhs, B, ldb, sx, n)) {
+    *iter = -2;
+    goto fallback;
+  }
+  if (lat2s(lower, n, A, lda, sa, n)) {
+    *iter = -2;
+    goto fallback;
+  }
+  if (orc_spotf2(lower, n, sa, n)) {
+    *iter = -3;
+    goto fallback;
+  }
+  spotrs(lower, n, nrhs, sa, n, sx, n);
+  for (int j = 0; j < nrhs; ++j)
+    for (int i = 0; i < n; ++i) X[(size_t)j * ldx + i] = (double)sx[(size_t)j * n + i];
+  for (int it = 0; it <= itermax; ++it) {
+    for (int j = 0; j < nrhs; ++j) memcpy(w + (size_t)j * n, B + (size_t)j * ldb, sizeof(double) * n);
+    dsymm_minus(lower, n, nrhs, A, lda, X, ldx, w, n);
+    int ok = 1;
+    for (int j = 0; j < nrhs; ++j) {
+      double xn = fabs(X[(size_t)j * ldx + idamax0(n, X + (size_t)j * ldx)]);
+      double rn = fabs(w[(size_t)j * n + idamax0(n, w + (size_t)j * n)]);
+      if (rn > xn * cte) {
+        ok = 0;
+        break;
+      }
+    }
+    if (ok) {
+      *iter = it;
+      free(sa);
+      free(sx);
+      free(w);
+      return 0;
+    }
+    if (it == itermax) break;
+    if (lag2s(n, nrhs, w, n, sx, n)) {
+      *iter = -2;
+      goto fallback;
+    }
+    spotrs(lower, n, nrhs, sa, n, sx, n);
+    for (int j = 0; j < nrhs; ++j)
+      for (int i = 0; i < n; ++i) X[(size_t)j * ldx + i] += (double)sx[(size_t)j * n + i];
+  }
+  *iter = -itermax - 1;
+fallback:
+  free(sa);
+  free(sx);
+  free(w);
+  info = orc_dpotrf(uplo, n, A, lda);
+  if (info) return info;
+  for (int j = 0; j < nrhs; ++j) memcpy(X + (size_t)j * ldx, B + (size_t)j * ldb, sizeof(double) * n);
+  orc_dpotrs(uplo, n, nrhs, A, lda, X, ldx);
+  return 0;
+}

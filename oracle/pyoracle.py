@@ -35,6 +35,8 @@ _SIGS = {
     "orc_dpotrf": (_i, [_c, _i, _vp, _i]),
     "orc_dsgesv": (_i, [_i, _i, _vp, _i, _vp, _vp, _i, _vp, _i, _pi]),
     "orc_dlange_inf": (_d, [_i, _i, _vp, _i]),
+    "orc_dpotrs": (_i, [_c, _i, _i, _vp, _i, _vp, _i]),
+    "orc_dsposv": (_i, [_c, _i, _i, _vp, _i, _vp, _i, _vp, _i, _pi]),
 }
 
 _lib = None
@@ -128,6 +130,16 @@ def dpotrf(uplo, n, A, lda) -> int:
 def dsgesv(n, nrhs, A, lda, ipiv, B, ldb, X, ldx):
     it = C.c_int(0)
     info = lib().orc_dsgesv(n, nrhs, _p(A), lda, _p(ipiv), _p(B), ldb, _p(X), ldx, C.byref(it))
+    return info, it.value
+
+
+def dpotrs(uplo, n, nrhs, A, lda, B, ldb) -> int:
+    return lib().orc_dpotrs(_ch(uplo), n, nrhs, _p(A), lda, _p(B), ldb)
+
+
+def dsposv(uplo, n, nrhs, A, lda, B, ldb, X, ldx):
+    it = C.c_int(0)
+    info = lib().orc_dsposv(_ch(uplo), n, nrhs, _p(A), lda, _p(B), ldb, _p(X), ldx, C.byref(it))
     return info, it.value
 
 

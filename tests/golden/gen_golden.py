@@ -56,6 +56,8 @@ GETRF_PIV_ONLY = [512, 1024]
 POTRF_N = [1, 7, 64, 200]
 LASWP_CASES = [(7, 1, 9, 1), (7, 3, 9, 1), (7, 1, 9, -1), (5, 2, 8, 2), (5, 2, 8, -2)]
 DSGESV_CASES = [(50, 1), (200, 3)]
+DPOTRS_CASES = [("L", 40, 1), ("U", 40, 5), ("L", 129, 3), ("U", 129, 1)]
+DSPOSV_CASES = [("L", 60, 1), ("U", 200, 3), ("L", 150, 2)]
 C1 = dict(m=1024, n=1024, k=1024, alpha=1.5, beta=0.5)
 
 
@@ -188,6 +190,39 @@ def main():
     swork = np.zeros(n * (n + 1), np.float32)
     info, it = ob.dsgesv(n, 1, A, n, ipiv, B, n, X, n, work, swork)
     g["dsgesv_ill_x"], g["dsgesv_ill_iter"], g["dsgesv_ill_ipiv"] = X, it, ipiv
+    # ---- DPOTRS (lapack-netlib/SRC/dpotrs.f) ------------------------
+    for idx, (uplo, n, nrhs) in enumerate(DPOTRS_CASES):
+        A = W.spd(8800 + idx, n)
+        assert ob.dpotrf(uplo, n, A, n) == 0
+        B = W.uniform(8810 + idx, (n, nrhs))
+        g[f"dpotrs_{idx}_info"] = ob.dpotrs(uplo, n, nrhs, A, n, B, n)
+        g[f"dpotrs_{idx}_x"] = B
+    # ---- DSPOSV (lapack-netlib/SRC/dsposv.f) ------------------------
+    for idx, (uplo, n, nrhs) in enumerate(DSPOSV_CASES):
+        A = W.spd(8900 + idx, n)
+        B = W.uniform(8910 + idx, (n, nrhs))
+        X = np.zeros((n, nrhs), order="F")
+        work = np.zeros((n, nrhs), order="F")
+        swork = np.zeros(n * (n + nrhs), np.float32)
+        info, it = ob.dsposv(uplo, n, nrhs, A, n, B, n, X, n, work, swork)
+        g[f"dsposv_{idx}_x"], g[f"dsposv_{idx}_iter"], g[f"dsposv_{idx}_info"] = X, it, info
+    # ill-conditioned SPD: the FP32 Cholesky fails or refinement stalls -> FP64
+    n = 60
+    A = W.spd_ill_conditioned(8920, n, 10)
+    B = W.uniform(8921, (n, 1))
+    X = np.zeros((n, 1), order="F")
+    work = np.zeros((n, 1), order="F")
+    swork = np.zeros(n * (n + 1), np.float32)
+    info, it = ob.dsposv("L", n, 1, A, n, B, n, X, n, work, swork)
+    g["dsposv_ill_x"], g["dsposv_ill_iter"], g["dsposv_ill_info"] = X, it, info
+    # not positive definite: FP32 and FP64 Cholesky both fail, info = column
+    n = 30
+    A = W.spd(8930, n)
+    A[17, 17] = -1.0
+    B = W.uniform(8931, (n, 1))
+    X = np.zeros((n, 1), order="F")
+    info, it = ob.dsposv("L", n, 1, A, n, B, n, X, n, work[:n], swork)
+    g["dsposv_npd_iter"], g["dsposv_npd_info"] = it, info
     # ---- SGETRF pivots (FP32 factorisation of the mixed solver) -------
     for n in (128, 256):
         A = W.uniform(8700 + n, (n, n)).astype(np.float32)

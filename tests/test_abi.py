@@ -156,6 +156,30 @@ def test_dsgesv_argument_errors(gblib, F):
         assert _xerbla(gblib) == ("DSGESV", pos)
 
 
+def test_dsposv_dpotrs_argument_errors(gblib, F):
+    buf = np.zeros((64, 64), order="F")
+    w = np.zeros(64 * 64)
+    sw = np.zeros(64 * 64, np.float32)
+    # lapack-netlib/SRC/dsposv.f:236-251 (UPLO, N, NRHS, LDA, LDB, LDX)
+    for args, pos in [(("X", 4, 1, 4, 4, 4), 1), (("L", -1, 1, 4, 4, 4), 2),
+                      (("U", 4, -1, 4, 4, 4), 3), (("L", 4, 1, 3, 4, 4), 5),
+                      (("L", 4, 1, 4, 3, 4), 7), (("U", 4, 1, 4, 4, 3), 9)]:
+        uplo, n, nrhs, lda, ldb, ldx = args
+        info, it = F.dsposv(uplo, n, nrhs, buf, lda, buf, ldb, buf, ldx, w, sw)
+        assert info == -pos and it == 0
+        assert _xerbla(gblib) == ("DSPOSV", pos)
+    # lapack-netlib/SRC/dpotrs.f:124-137 (UPLO, N, NRHS, LDA, LDB)
+    for args, pos in [(("Q", 4, 1, 4, 4), 1), (("L", -2, 1, 4, 4), 2), (("L", 4, -1, 4, 4), 3),
+                      (("U", 4, 1, 2, 4), 5), (("U", 4, 1, 4, 2), 7)]:
+        uplo, n, nrhs, lda, ldb = args
+        assert F.dpotrs(uplo, n, nrhs, buf, lda, buf, ldb) == -pos
+        assert _xerbla(gblib) == ("DPOTRS", pos)
+    # quick returns (no device call)
+    assert F.dpotrs("L", 0, 3, buf, 4, buf, 4) == 0
+    assert F.dpotrs("U", 4, 0, buf, 4, buf, 4) == 0
+    assert F.dsposv("L", 0, 1, buf, 4, buf, 4, buf, 4, w, sw) == (0, 0)
+
+
 def test_quick_returns_do_not_touch_device(gblib, F):
     """m==0/n==0 quick returns happen before any CUDA call, so they succeed on
     a machine without a GPU (interface/gemm.c:494, getrf.c:83, potrf.c:104)."""

@@ -201,3 +201,42 @@ def test_sgetrf_pivots(golden, orc):
         assert np.array_equal(ipiv, golden[f"sgetrf_{n}_ipiv"])
         if f"sgetrf_{n}_lu" in golden:
             assert np.max(np.abs(A - golden[f"sgetrf_{n}_lu"])) < 1e-3
+
+
+def test_dpotrs_cases(golden, orc):
+    for idx, (uplo, n, nrhs) in enumerate(GG.DPOTRS_CASES):
+        A = W.spd(8800 + idx, n)
+        assert orc.dpotrf(uplo, n, A, n) == 0
+        B = W.uniform(8810 + idx, (n, nrhs))
+        assert orc.dpotrs(uplo, n, nrhs, A, n, B, n) == int(golden[f"dpotrs_{idx}_info"]) == 0
+        ref = golden[f"dpotrs_{idx}_x"]
+        assert np.max(np.abs(B - ref)) <= 64 * n * EPS * np.abs(ref).max()
+
+
+def test_dsposv_cases(golden, orc):
+    for idx, (uplo, n, nrhs) in enumerate(GG.DSPOSV_CASES):
+        A = W.spd(8900 + idx, n)
+        B = W.uniform(8910 + idx, (n, nrhs))
+        X = np.zeros((n, nrhs), order="F")
+        info, it = orc.dsposv(uplo, n, nrhs, A, n, B, n, X, n)
+        assert info == int(golden[f"dsposv_{idx}_info"]) == 0
+        assert it == int(golden[f"dsposv_{idx}_iter"])
+        ref = golden[f"dsposv_{idx}_x"]
+        assert np.max(np.abs(X - ref)) <= 64 * n * EPS * np.abs(ref).max()
+
+
+def test_dsposv_fallbacks(golden, orc):
+    n = 60
+    A = W.spd_ill_conditioned(8920, n, 10)
+    B = W.uniform(8921, (n, 1))
+    X = np.zeros((n, 1), order="F")
+    info, it = orc.dsposv("L", n, 1, A.copy(order="F"), n, B, n, X, n)
+    assert info == int(golden["dsposv_ill_info"]) == 0
+    assert it == int(golden["dsposv_ill_iter"]) and it < 0
+    A = W.spd(8930, 30)
+    A[17, 17] = -1.0
+    B = W.uniform(8931, (30, 1))
+    X = np.zeros((30, 1), order="F")
+    info, it = orc.dsposv("L", 30, 1, A, 30, B, 30, X, 30)
+    assert info == int(golden["dsposv_npd_info"]) == 18
+    assert it == int(golden["dsposv_npd_iter"]) == -3
