@@ -486,7 +486,36 @@ def run_suite(args):
             resid = float(R.abs().sum(dim=1).max() / (n * eps * A0.abs().sum(dim=1).max()))
             del Lw, R
     lib.gb_set_dgemm_mode(0)
+    # DSPOSV on the same matrix: FP32 Cholesky + FP64 refinement vs native
+    # FP64 DPOTRF + DPOTRS (the native factor time is the one just measured)
+    Bm = urand((1, n), 98)
+    X = torch.zeros_like(Bm)
+    it, info = C.c_int(0), C.c_int(0)
+    A.copy_(A0)  # the mixed path leaves A alone unless it falls back
+    check(lib.gb_dsposv_dev(b"L", n, 1, A.data_ptr(), n, Bm.data_ptr(), n, X.data_ptr(), n,
+                            C.byref(it), C.byref(info)))
+    ts = []
+    for _ in range(2):
+        A.copy_(A0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        check(lib.gb_dsposv_dev(b"L", n, 1, A.data_ptr(), n, Bm.data_ptr(), n, X.data_ptr(), n,
+                                C.byref(it), C.byref(info)))
+        torch.cuda.synchronize()
+        ts.append(time.perf_counter() - t0)
+    t_sposv = statistics.median(ts)
+    R = Bm.clone()
+    check(lib.gb_dgemm_native_dev(b"N", b"N", n, 1, n, -1.0, A0.data_ptr(), n, X.data_ptr(), n,
+                                  1.0, R.data_ptr(), n))
+    torch.cuda.synchronize()
+    anorm = float(A0.abs().sum(dim=0).max())
+    berr_sposv = float(R.abs().max() / (anorm * X.abs().max() + Bm.abs().max())) / eps
     flops = n ** 3 / 3.0
+    _emit({"suite": "dsposv_32768_1", "workload": "DSPOSV L N=32768 NRHS=1, A = B B^T/N + I",
+           "value": (flops + 2.0 * n * n) / t_sposv / 1e12, "unit": UNIT, "ms": t_sposv * 1e3,
+           "iter": it.value, "info": info.value, "backward_error_eps": berr_sposv,
+           "bound_n_eps": n,
+           "speedup_over_native_dpotrf": out["native_fp64"][0] / t_sposv})
     _emit({"suite": "dpotrf_32768", "workload": "DPOTRF L N=32768, A = B B^T/N + I",
            "value": flops / out["emulated_updates"][0] / 1e12, "unit": UNIT,
            "ms": out["emulated_updates"][0] * 1e3, "info": out["emulated_updates"][1],

@@ -67,6 +67,19 @@ void cblas_dsyrk(enum CBLAS_ORDER Order, enum CBLAS_UPLO Uplo,
                  enum CBLAS_TRANSPOSE Trans, blasint N, blasint K, double alpha,
                  const double *A, blasint lda, double beta, double *C,
                  blasint ldc);
+/* replaces cblas_dtrmm, interface/trsm.c built as TRMM (cblas.h:349-350) */
+void cblas_dtrmm(enum CBLAS_ORDER Order, enum CBLAS_SIDE Side, enum CBLAS_UPLO Uplo,
+                 enum CBLAS_TRANSPOSE TransA, enum CBLAS_DIAG Diag, blasint M, blasint N,
+                 double alpha, const double *A, blasint lda, double *B, blasint ldb);
+/* replaces cblas_dsyr2k, interface/syr2k.c (cblas.h:340-341) */
+void cblas_dsyr2k(enum CBLAS_ORDER Order, enum CBLAS_UPLO Uplo, enum CBLAS_TRANSPOSE Trans,
+                  blasint N, blasint K, double alpha, const double *A, blasint lda,
+                  const double *B, blasint ldb, double beta, double *C, blasint ldc);
+/* replaces cblas_dgemmt, interface/gemmt.c (cblas.h:313-314) */
+void cblas_dgemmt(enum CBLAS_ORDER Order, enum CBLAS_UPLO Uplo, enum CBLAS_TRANSPOSE TransA,
+                  enum CBLAS_TRANSPOSE TransB, blasint M, blasint K, double alpha,
+                  const double *A, blasint lda, const double *B, blasint ldb, double beta,
+                  double *C, blasint ldc);
 /* replaces cblas_dgemm_batch, interface/gemm_batch.c:117-372 (cblas.h:422-423) */
 void cblas_dgemm_batch(enum CBLAS_ORDER Order,
                        const enum CBLAS_TRANSPOSE *TransA_array,
@@ -96,6 +109,22 @@ void dtrsm_(const char *SIDE, const char *UPLO, const char *TRANSA,
             const char *DIAG, const blasint *M, const blasint *N,
             const double *alpha, const double *A, const blasint *ldA,
             double *B, const blasint *ldB);
+/* replaces dtrmm_, interface/trsm.c built as TRMM (B = alpha*op(A)*B or
+ * alpha*B*op(A), A triangular) */
+void dtrmm_(const char *SIDE, const char *UPLO, const char *TRANSA, const char *DIAG,
+            const blasint *M, const blasint *N, const double *alpha, const double *A,
+            const blasint *ldA, double *B, const blasint *ldB);
+/* replaces dsyr2k_, interface/syr2k.c:96-191 (C = alpha*A*B' + alpha*B*A' + beta*C
+ * on one triangle) */
+void dsyr2k_(const char *UPLO, const char *TRANS, const blasint *N, const blasint *K,
+             const double *alpha, const double *A, const blasint *ldA, const double *B,
+             const blasint *ldB, const double *beta, double *C, const blasint *ldC);
+/* replaces dgemmt_, interface/gemmt.c:80-200 (C = alpha*op(A)*op(B) + beta*C on
+ * one triangle of the M x M matrix C) */
+void dgemmt_(const char *UPLO, const char *TRANSA, const char *TRANSB, const blasint *M,
+             const blasint *K, const double *alpha, const double *A, const blasint *ldA,
+             const double *B, const blasint *ldB, const double *beta, double *C,
+             const blasint *ldC);
 /* replaces dsyrk_, interface/syrk.c:96-191 */
 void dsyrk_(const char *UPLO, const char *TRANS, const blasint *N,
             const blasint *K, const double *alpha, const double *A,
@@ -224,6 +253,14 @@ int gb_sgemm_dev(char transa, char transb, int64_t m, int64_t n, int64_t k,
 int gb_dtrsm_dev(char side, char uplo, char transa, char diag, int64_t m,
                  int64_t n, double alpha, const double *A, int64_t lda,
                  double *B, int64_t ldb);
+int gb_dtrmm_dev(char side, char uplo, char transa, char diag, int64_t m, int64_t n,
+                 double alpha, const double *A, int64_t lda, double *B, int64_t ldb);
+int gb_dsyr2k_dev(char uplo, char trans, int64_t n, int64_t k, double alpha, const double *A,
+                  int64_t lda, const double *B, int64_t ldb, double beta, double *C,
+                  int64_t ldc);
+int gb_dgemmt_dev(char uplo, char transa, char transb, int64_t m, int64_t k, double alpha,
+                  const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
+                  double *C, int64_t ldc);
 int gb_dsyrk_dev(char uplo, char trans, int64_t n, int64_t k, double alpha,
                  const double *A, int64_t lda, double beta, double *C,
                  int64_t ldc);

@@ -40,6 +40,9 @@ DEV_SIGS = {
     "gb_sgemm_dev": (_i, [_c, _c, _i64, _i64, _i64, _f, _vp, _i64, _vp, _i64, _f, _vp, _i64]),
     "gb_dtrsm_dev": (_i, [_c, _c, _c, _c, _i64, _i64, _d, _vp, _i64, _vp, _i64]),
     "gb_dsyrk_dev": (_i, [_c, _c, _i64, _i64, _d, _vp, _i64, _d, _vp, _i64]),
+    "gb_dtrmm_dev": (_i, [_c, _c, _c, _c, _i64, _i64, _d, _vp, _i64, _vp, _i64]),
+    "gb_dsyr2k_dev": (_i, [_c, _c, _i64, _i64, _d, _vp, _i64, _vp, _i64, _d, _vp, _i64]),
+    "gb_dgemmt_dev": (_i, [_c, _c, _c, _i64, _i64, _d, _vp, _i64, _vp, _i64, _d, _vp, _i64]),
     "gb_dgetrf_dev": (_i, [_i64, _i64, _vp, _i64, _vp, _vp]),
     "gb_dgetrs_dev": (_i, [_c, _i64, _i64, _vp, _i64, _vp, _vp, _i64]),
     "gb_sgetrf_dev": (_i, [_i64, _i64, _vp, _i64, _vp, _vp]),

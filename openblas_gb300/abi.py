@@ -38,6 +38,9 @@ FORTRAN_SIGS = {
     "sgemm_": (None, [_pc, _pc, _pi, _pi, _pi, _pf, _vp, _pi, _vp, _pi, _pf, _vp, _pi]),
     "dtrsm_": (None, [_pc, _pc, _pc, _pc, _pi, _pi, _pd, _vp, _pi, _vp, _pi]),
     "dsyrk_": (None, [_pc, _pc, _pi, _pi, _pd, _vp, _pi, _pd, _vp, _pi]),
+    "dtrmm_": (None, [_pc, _pc, _pc, _pc, _pi, _pi, _pd, _vp, _pi, _vp, _pi]),
+    "dsyr2k_": (None, [_pc, _pc, _pi, _pi, _pd, _vp, _pi, _vp, _pi, _pd, _vp, _pi]),
+    "dgemmt_": (None, [_pc, _pc, _pc, _pi, _pi, _pd, _vp, _pi, _vp, _pi, _pd, _vp, _pi]),
     # LAPACK (interface/lapack/*.c)
     "dgetrf_": (_i, [_pi, _pi, _vp, _pi, _vp, _pi]),
     "dgetrs_": (_i, [_pc, _pi, _pi, _vp, _pi, _vp, _vp, _pi, _pi]),
@@ -55,6 +58,9 @@ CBLAS_SIGS = {
     "cblas_sgemm": (None, [_i, _i, _i, _i, _i, _i, _f, _vp, _i, _vp, _i, _f, _vp, _i]),
     "cblas_dtrsm": (None, [_i, _i, _i, _i, _i, _i, _i, _d, _vp, _i, _vp, _i]),
     "cblas_dsyrk": (None, [_i, _i, _i, _i, _i, _d, _vp, _i, _d, _vp, _i]),
+    "cblas_dtrmm": (None, [_i, _i, _i, _i, _i, _i, _i, _d, _vp, _i, _vp, _i]),
+    "cblas_dsyr2k": (None, [_i, _i, _i, _i, _i, _d, _vp, _i, _vp, _i, _d, _vp, _i]),
+    "cblas_dgemmt": (None, [_i, _i, _i, _i, _i, _i, _d, _vp, _i, _vp, _i, _d, _vp, _i]),
     "cblas_dgemm_batch": (None, [_i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                  _vp, _vp, _i, _vp]),
 }
@@ -151,6 +157,21 @@ class Fortran:
         info = _i(0)
         self.ns.dpotrf_(self._c(uplo), C.byref(_i(n)), _ptr(A), C.byref(_i(lda)), C.byref(info))
         return info.value
+
+    def dtrmm(self, side, uplo, ta, diag, m, n, alpha, A, lda, B, ldb):
+        self.ns.dtrmm_(self._c(side), self._c(uplo), self._c(ta), self._c(diag), C.byref(_i(m)),
+                       C.byref(_i(n)), C.byref(_d(alpha)), _ptr(A), C.byref(_i(lda)), _ptr(B),
+                       C.byref(_i(ldb)))
+
+    def dsyr2k(self, uplo, trans, n, k, alpha, A, lda, B, ldb, beta, Cm, ldc):
+        self.ns.dsyr2k_(self._c(uplo), self._c(trans), C.byref(_i(n)), C.byref(_i(k)),
+                        C.byref(_d(alpha)), _ptr(A), C.byref(_i(lda)), _ptr(B), C.byref(_i(ldb)),
+                        C.byref(_d(beta)), _ptr(Cm), C.byref(_i(ldc)))
+
+    def dgemmt(self, uplo, ta, tb, m, k, alpha, A, lda, B, ldb, beta, Cm, ldc):
+        self.ns.dgemmt_(self._c(uplo), self._c(ta), self._c(tb), C.byref(_i(m)), C.byref(_i(k)),
+                        C.byref(_d(alpha)), _ptr(A), C.byref(_i(lda)), _ptr(B), C.byref(_i(ldb)),
+                        C.byref(_d(beta)), _ptr(Cm), C.byref(_i(ldc)))
 
     def dpotrs(self, uplo, n, nrhs, A, lda, B, ldb) -> int:
         info = _i(0)

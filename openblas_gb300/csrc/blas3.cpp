@@ -167,6 +167,68 @@ static void dtrsm_blocking(int side, int uplo, int trans, int unit, int64_t m, i
   finish_blocking(s);
 }
 
+int dgemmt_device(int uplo, int ta, int tb, int64_t m, int64_t k, double alpha, const double *A,
+                  int64_t lda, const double *B, int64_t ldb, double beta, double *C,
+                  int64_t ldc, cudaStream_t s);
+int dsyr2k_device(int uplo, int trans, int64_t n, int64_t k, double alpha, const double *A,
+                  int64_t lda, const double *B, int64_t ldb, double beta, double *C, int64_t ldc,
+                  cudaStream_t s);
+int dtrmm_device(int side, int uplo, int trans, int unit_code, int64_t m, int64_t n,
+                 double alpha, const double *A, int64_t lda, double *B, int64_t ldb,
+                 cudaStream_t s);
+
+static void dgemmt_blocking(int uplo, int ta, int tb, int64_t m, int64_t k, double alpha,
+                            const double *A, int64_t lda, const double *B, int64_t ldb,
+                            double beta, double *C, int64_t ldc) {
+  if (m == 0) return;  // interface/gemmt.c: quick return
+  if (ensure_init()) return;
+  cudaStream_t s = stream();
+  const bool need_ab = k > 0 && alpha != 0.0;
+  Operand a(A, ta ? k : m, ta ? m : k, lda, 8), b(B, tb ? m : k, tb ? k : m, ldb, 8);
+  Operand c(C, m, m, ldc, 8);
+  if (need_ab && (a.bind(true, s) || b.bind(true, s))) return;
+  if (c.bind(true, s)) return;  // the other triangle must survive the round trip
+  if (dgemmt_device(uplo, ta, tb, m, k, alpha, a.d<double>(), a.dld, b.d<double>(), b.dld, beta,
+                    c.d<double>(), c.dld, s))
+    return;
+  c.unbind(s);
+  finish_blocking(s);
+}
+
+static void dsyr2k_blocking(int uplo, int trans, int64_t n, int64_t k, double alpha,
+                            const double *A, int64_t lda, const double *B, int64_t ldb,
+                            double beta, double *C, int64_t ldc) {
+  if (n == 0) return;
+  if (ensure_init()) return;
+  cudaStream_t s = stream();
+  const bool need_ab = k > 0 && alpha != 0.0;
+  Operand a(A, trans ? k : n, trans ? n : k, lda, 8), b(B, trans ? k : n, trans ? n : k, ldb, 8);
+  Operand c(C, n, n, ldc, 8);
+  if (need_ab && (a.bind(true, s) || b.bind(true, s))) return;
+  if (c.bind(true, s)) return;
+  if (dsyr2k_device(uplo, trans, n, k, alpha, a.d<double>(), a.dld, b.d<double>(), b.dld, beta,
+                    c.d<double>(), c.dld, s))
+    return;
+  c.unbind(s);
+  finish_blocking(s);
+}
+
+static void dtrmm_blocking(int side, int uplo, int trans, int unit, int64_t m, int64_t n,
+                           double alpha, const double *A, int64_t lda, double *B, int64_t ldb) {
+  if (m == 0 || n == 0) return;
+  if (ensure_init()) return;
+  cudaStream_t s = stream();
+  const int64_t na = side ? n : m;
+  Operand a(A, na, na, lda, 8), b(B, m, n, ldb, 8);
+  if (alpha != 0.0 && a.bind(true, s)) return;
+  if (b.bind(alpha != 0.0, s)) return;
+  if (dtrmm_device(side, uplo, trans, unit, m, n, alpha, a.d<double>(), a.dld, b.d<double>(),
+                   b.dld, s))
+    return;
+  b.unbind(s);
+  finish_blocking(s);
+}
+
 static void dsyrk_blocking(int uplo, int trans, int64_t n, int64_t k, double alpha,
                            const double *A, int64_t lda, double beta, double *C, int64_t ldc) {
   if (n == 0) return;  // interface/syrk.c:344
@@ -400,6 +462,173 @@ void cblas_dsyrk(enum CBLAS_ORDER order, enum CBLAS_UPLO Uplo, enum CBLAS_TRANSP
 }
 
 // ---------------------------------------------------------------------------
+// TRMM (interface/trsm.c built with TRMM: same checks and row-major mapping)
+// ---------------------------------------------------------------------------
+void dtrmm_(const char *SIDE, const char *UPLO, const char *TRANSA, const char *DIAG,
+            const blasint *M, const blasint *N, const double *alpha, const double *A,
+            const blasint *ldA, double *B, const blasint *ldB) {
+  char sd = upch(SIDE), up = upch(UPLO), tr = upch(TRANSA), dg = upch(DIAG);
+  int side = sd == 'L' ? 0 : sd == 'R' ? 1 : -1;
+  int uplo = up == 'U' ? 0 : up == 'L' ? 1 : -1;
+  int trans = (tr == 'N' || tr == 'R') ? 0 : (tr == 'T' || tr == 'C') ? 1 : -1;
+  int unit = dg == 'U' ? 0 : dg == 'N' ? 1 : -1;
+  int info = trsm_check(side, uplo, trans, unit, *M, *N, *ldA, *ldB);
+  if (info) {
+    call_xerbla("DTRMM ", info);
+    return;
+  }
+  dtrmm_blocking(side, uplo, trans, unit, *M, *N, *alpha, A, *ldA, B, *ldB);
+}
+
+void cblas_dtrmm(enum CBLAS_ORDER order, enum CBLAS_SIDE Side, enum CBLAS_UPLO Uplo,
+                 enum CBLAS_TRANSPOSE Trans, enum CBLAS_DIAG Diag, blasint m, blasint n,
+                 double alpha, const double *a, blasint lda, double *b, blasint ldb) {
+  int side = -1, uplo = -1, trans = -1, unit = -1, info = -1;
+  int64_t M = m, N = n;
+  if (order == CblasColMajor) {
+    side = Side == CblasLeft ? 0 : Side == CblasRight ? 1 : -1;
+    uplo = Uplo == CblasUpper ? 0 : Uplo == CblasLower ? 1 : -1;
+  } else if (order == CblasRowMajor) {
+    M = n;
+    N = m;
+    side = Side == CblasLeft ? 1 : Side == CblasRight ? 0 : -1;
+    uplo = Uplo == CblasUpper ? 1 : Uplo == CblasLower ? 0 : -1;
+  }
+  trans = cblas_trans_code(Trans);
+  unit = Diag == CblasUnit ? 0 : Diag == CblasNonUnit ? 1 : -1;
+  if (order == CblasColMajor || order == CblasRowMajor) {
+    info = trsm_check(side, uplo, trans, unit, M, N, lda, ldb);
+    if (info == 0) info = -1;
+  }
+  if (info >= 0) {
+    call_xerbla("DTRMM ", info);
+    return;
+  }
+  dtrmm_blocking(side, uplo, trans, unit, M, N, alpha, a, lda, b, ldb);
+}
+
+// ---------------------------------------------------------------------------
+// SYR2K (interface/syr2k.c)
+// ---------------------------------------------------------------------------
+static int syr2k_check(int uplo, int trans, int64_t n, int64_t k, int64_t lda, int64_t ldb,
+                       int64_t ldc) {
+  int64_t nrowa = (trans & 1) ? k : n;
+  int info = 0;
+  if (ldc < (n > 1 ? n : 1)) info = 12;
+  if (ldb < (nrowa > 1 ? nrowa : 1)) info = 9;
+  if (lda < (nrowa > 1 ? nrowa : 1)) info = 7;
+  if (k < 0) info = 4;
+  if (n < 0) info = 3;
+  if (trans < 0) info = 2;
+  if (uplo < 0) info = 1;
+  return info;
+}
+
+void dsyr2k_(const char *UPLO, const char *TRANS, const blasint *N, const blasint *K,
+             const double *alpha, const double *A, const blasint *ldA, const double *B,
+             const blasint *ldB, const double *beta, double *C, const blasint *ldC) {
+  char up = upch(UPLO), tr = upch(TRANS);
+  int uplo = up == 'U' ? 0 : up == 'L' ? 1 : -1;
+  int trans = tr == 'N' ? 0 : (tr == 'T' || tr == 'C') ? 1 : -1;
+  int info = syr2k_check(uplo, trans, *N, *K, *ldA, *ldB, *ldC);
+  if (info) {
+    call_xerbla("DSYR2K", info);
+    return;
+  }
+  dsyr2k_blocking(uplo, trans, *N, *K, *alpha, A, *ldA, B, *ldB, *beta, C, *ldC);
+}
+
+void cblas_dsyr2k(enum CBLAS_ORDER order, enum CBLAS_UPLO Uplo, enum CBLAS_TRANSPOSE Trans,
+                  blasint n, blasint k, double alpha, const double *a, blasint lda,
+                  const double *b, blasint ldb, double beta, double *c, blasint ldc) {
+  // interface/syr2k.c: row-major flips uplo and trans (the sum is symmetric in A, B)
+  int uplo = -1, trans = -1, info = -1;
+  if (order == CblasColMajor) {
+    uplo = Uplo == CblasUpper ? 0 : Uplo == CblasLower ? 1 : -1;
+    trans = cblas_trans_code(Trans);
+  } else if (order == CblasRowMajor) {
+    uplo = Uplo == CblasUpper ? 1 : Uplo == CblasLower ? 0 : -1;
+    int t = cblas_trans_code(Trans);
+    trans = t < 0 ? -1 : 1 - t;
+  }
+  if (order == CblasColMajor || order == CblasRowMajor) {
+    info = syr2k_check(uplo, trans, n, k, lda, ldb, ldc);
+    if (info == 0) info = -1;
+  }
+  if (info >= 0) {
+    call_xerbla("DSYR2K", info);
+    return;
+  }
+  dsyr2k_blocking(uplo, trans, n, k, alpha, a, lda, b, ldb, beta, c, ldc);
+}
+
+// ---------------------------------------------------------------------------
+// GEMMT (interface/gemmt.c)
+// ---------------------------------------------------------------------------
+static int gemmt_check(int uplo, int ta, int tb, int64_t m, int64_t k, int64_t lda, int64_t ldb,
+                       int64_t ldc) {
+  const int64_t nrowa = (ta & 1) ? k : m, nrowb = (tb & 1) ? m : k;
+  int info = 0;
+  if (ldc < (m > 1 ? m : 1)) info = 13;
+  if (ldb < (nrowb > 1 ? nrowb : 1)) info = 10;
+  if (lda < (nrowa > 1 ? nrowa : 1)) info = 8;
+  if (k < 0) info = 5;
+  if (m < 0) info = 4;
+  if (tb < 0) info = 3;
+  if (ta < 0) info = 2;
+  if (uplo < 0) info = 1;
+  return info;
+}
+
+void dgemmt_(const char *UPLO, const char *TRANSA, const char *TRANSB, const blasint *M,
+             const blasint *K, const double *alpha, const double *A, const blasint *ldA,
+             const double *B, const blasint *ldB, const double *beta, double *C,
+             const blasint *ldC) {
+  char up = upch(UPLO);
+  int uplo = up == 'U' ? 0 : up == 'L' ? 1 : -1;
+  int ta = trans_code(upch(TRANSA)), tb = trans_code(upch(TRANSB));
+  int info = gemmt_check(uplo, ta, tb, *M, *K, *ldA, *ldB, *ldC);
+  if (info) {
+    call_xerbla("DGEMMT", info);
+    return;
+  }
+  dgemmt_blocking(uplo, ta, tb, *M, *K, *alpha, A, *ldA, B, *ldB, *beta, C, *ldC);
+}
+
+void cblas_dgemmt(enum CBLAS_ORDER order, enum CBLAS_UPLO Uplo, enum CBLAS_TRANSPOSE TransA,
+                  enum CBLAS_TRANSPOSE TransB, blasint m, blasint k, double alpha,
+                  const double *a, blasint lda, const double *b, blasint ldb, double beta,
+                  double *c, blasint ldc) {
+  // interface/gemmt.c: row-major swaps the operands, flips uplo and the roles
+  // of the two transposes
+  int uplo = -1, ta = -1, tb = -1, info = -1;
+  const double *pa = a, *pb = b;
+  blasint la = lda, lb = ldb;
+  if (order == CblasColMajor) {
+    uplo = Uplo == CblasUpper ? 0 : Uplo == CblasLower ? 1 : -1;
+    ta = cblas_trans_code(TransA);
+    tb = cblas_trans_code(TransB);
+  } else if (order == CblasRowMajor) {
+    uplo = Uplo == CblasUpper ? 1 : Uplo == CblasLower ? 0 : -1;
+    ta = cblas_trans_code(TransB);
+    tb = cblas_trans_code(TransA);
+    pa = b;
+    pb = a;
+    la = ldb;
+    lb = lda;
+  }
+  if (order == CblasColMajor || order == CblasRowMajor) {
+    info = gemmt_check(uplo, ta, tb, m, k, la, lb, ldc);
+    if (info == 0) info = -1;
+  }
+  if (info >= 0) {
+    call_xerbla("DGEMMT", info);
+    return;
+  }
+  dgemmt_blocking(uplo, ta, tb, m, k, alpha, pa, la, pb, lb, beta, c, ldc);
+}
+
+// ---------------------------------------------------------------------------
 // grouped batch (interface/gemm_batch.c:117-372)
 // ---------------------------------------------------------------------------
 
@@ -507,6 +736,55 @@ int gb_sgemm_dev(char transa, char transb, int64_t m, int64_t n, int64_t k, floa
     return check_cuda(cudaGetLastError(), "sgemm launch");
   }
   return sgemm_dispatch(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, stream());
+}
+
+int gb_dgemmt_dev(char uplo, char transa, char transb, int64_t m, int64_t k, double alpha,
+                  const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
+                  double *C, int64_t ldc) {
+  const char u = upch(uplo);
+  const int up = u == 'U' ? 0 : u == 'L' ? 1 : -1;
+  const int ta = trans_code(upch(transa)), tb = trans_code(upch(transb));
+  const int info = gemmt_check(up, ta, tb, m, k, lda, ldb, ldc);
+  if (info) {
+    call_xerbla("DGEMMT", info);
+    return GB_ERR_INVALID_VALUE;
+  }
+  int st = ensure_init();
+  if (st) return st;
+  return dgemmt_device(up, ta, tb, m, k, alpha, A, lda, B, ldb, beta, C, ldc, stream());
+}
+
+int gb_dsyr2k_dev(char uplo, char trans, int64_t n, int64_t k, double alpha, const double *A,
+                  int64_t lda, const double *B, int64_t ldb, double beta, double *C,
+                  int64_t ldc) {
+  const char u = upch(uplo), t = upch(trans);
+  const int up = u == 'U' ? 0 : u == 'L' ? 1 : -1;
+  const int tr = t == 'N' ? 0 : (t == 'T' || t == 'C') ? 1 : -1;
+  const int info = syr2k_check(up, tr, n, k, lda, ldb, ldc);
+  if (info) {
+    call_xerbla("DSYR2K", info);
+    return GB_ERR_INVALID_VALUE;
+  }
+  int st = ensure_init();
+  if (st) return st;
+  return dsyr2k_device(up, tr, n, k, alpha, A, lda, B, ldb, beta, C, ldc, stream());
+}
+
+int gb_dtrmm_dev(char side, char uplo, char transa, char diag, int64_t m, int64_t n,
+                 double alpha, const double *A, int64_t lda, double *B, int64_t ldb) {
+  const char sd = upch(side), up = upch(uplo), tr = upch(transa), dg = upch(diag);
+  const int s_ = sd == 'L' ? 0 : sd == 'R' ? 1 : -1;
+  const int u_ = up == 'U' ? 0 : up == 'L' ? 1 : -1;
+  const int t_ = (tr == 'N' || tr == 'R') ? 0 : (tr == 'T' || tr == 'C') ? 1 : -1;
+  const int d_ = dg == 'U' ? 0 : dg == 'N' ? 1 : -1;
+  const int info = trsm_check(s_, u_, t_, d_, m, n, lda, ldb);
+  if (info) {
+    call_xerbla("DTRMM ", info);
+    return GB_ERR_INVALID_VALUE;
+  }
+  int st = ensure_init();
+  if (st) return st;
+  return dtrmm_device(s_, u_, t_, d_, m, n, alpha, A, lda, B, ldb, stream());
 }
 
 int gb_dtrsm_dev(char side, char uplo, char transa, char diag, int64_t m, int64_t n,

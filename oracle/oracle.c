@@ -675,6 +675,86 @@ fallback:
 }
 
 /* ------------------------------------------------------------------------ */
+/* TRMM / SYR2K / GEMMT                                                      */
+/* ------------------------------------------------------------------------ */
+/* driver/level3/trmm_L.c, trmm_R.c (interface/trsm.c built as TRMM):
+ * B = alpha*op(T)*B (side L) or alpha*B*op(T) (side R), T the uplo triangle of
+ * A with a unit diagonal for diag 'U'; alpha == 0 zeroes B (GEMM_BETA). */
+void orc_dtrmm(char side, char uplo, char transa, char diag, int m, int n, double alpha,
+               const double *A, int lda, double *B, int ldb) {
+  if (m <= 0 || n <= 0) return;
+  const int left = upc(side) == 'L', lower = upc(uplo) == 'L';
+  const int tr = upc(transa) == 'T' || upc(transa) == 'C', unit = upc(diag) == 'U';
+  if (alpha == 0.0) {
+    for (int j = 0; j < n; ++j)
+      for (int i = 0; i < m; ++i) B[(size_t)j * ldb + i] = 0.0;
+    return;
+  }
+  const int na = left ? m : n;
+  double *T = (double *)calloc((size_t)na * na, sizeof(double));
+  for (int j = 0; j < na; ++j)
+    for (int i = 0; i < na; ++i) {
+      double v = 0.0;
+      if (i == j) v = unit ? 1.0 : A[(size_t)j * lda + i];
+      else if (lower ? i > j : i < j) v = A[(size_t)j * lda + i];
+      T[(size_t)j * na + i] = v;
+    }
+  double *W = (double *)malloc(sizeof(double) * (size_t)m * n);
+  for (int j = 0; j < n; ++j) memcpy(W + (size_t)j * m, B + (size_t)j * ldb, sizeof(double) * m);
+  if (left)
+    orc_dgemm(tr ? 'T' : 'N', 'N', m, n, m, alpha, T, na, W, m, 0.0, B, ldb);
+  else
+    orc_dgemm('N', tr ? 'T' : 'N', m, n, n, alpha, W, m, T, na, 0.0, B, ldb);
+  free(T);
+  free(W);
+}
+
+/* driver/level3/level3_syr2k.c: C = alpha*op(A)*op(B)^T + alpha*op(B)*op(A)^T
+ * + beta*C on the uplo triangle (trans 'N': A, B n x k; 'T': k x n). */
+void orc_dsyr2k(char uplo, char trans, int n, int k, double alpha, const double *A, int lda,
+                const double *B, int ldb, double beta, double *C, int ldc) {
+  if (n <= 0) return;
+  const int lower = upc(uplo) == 'L', tr = upc(trans) != 'N';
+  for (int j = 0; j < n; ++j)
+    for (int i = lower ? j : 0; i < (lower ? n : j + 1); ++i) {
+      double s = 0.0;
+      if (alpha != 0.0)
+        for (int p = 0; p < k; ++p) {
+          const double aip = tr ? A[(size_t)i * lda + p] : A[(size_t)p * lda + i];
+          const double bjp = tr ? B[(size_t)j * ldb + p] : B[(size_t)p * ldb + j];
+          const double bip = tr ? B[(size_t)i * ldb + p] : B[(size_t)p * ldb + i];
+          const double ajp = tr ? A[(size_t)j * lda + p] : A[(size_t)p * lda + j];
+          s += aip * bjp + bip * ajp;
+        }
+      double *c = C + (size_t)j * ldc + i;
+      *c = (beta == 0.0 ? 0.0 : beta * *c) + alpha * s;
+    }
+}
+
+/* interface/gemmt.c: C = alpha*op(A)*op(B) + beta*C on the uplo triangle of
+ * the m x m matrix C. */
+void orc_dgemmt(char uplo, char transa, char transb, int m, int k, double alpha,
+                const double *A, int lda, const double *B, int ldb, double beta, double *C,
+                int ldc) {
+  if (m <= 0) return;
+  const int lower = upc(uplo) == 'L';
+  const int ta = upc(transa) == 'T' || upc(transa) == 'C';
+  const int tb = upc(transb) == 'T' || upc(transb) == 'C';
+  for (int j = 0; j < m; ++j)
+    for (int i = lower ? j : 0; i < (lower ? m : j + 1); ++i) {
+      double s = 0.0;
+      if (alpha != 0.0)
+        for (int p = 0; p < k; ++p) {
+          const double a = ta ? A[(size_t)i * lda + p] : A[(size_t)p * lda + i];
+          const double b = tb ? B[(size_t)p * ldb + j] : B[(size_t)j * ldb + p];
+          s += a * b;
+        }
+      double *c = C + (size_t)j * ldc + i;
+      *c = (beta == 0.0 ? 0.0 : beta * *c) + alpha * s;
+    }
+}
+
+/* ------------------------------------------------------------------------ */
 /* DPOTRS / DSPOSV                                                           */
 /* ------------------------------------------------------------------------ */
 /* lapack-netlib/SRC/dpotrs.f:135-160: two triangular solves with the factor. */

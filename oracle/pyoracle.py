@@ -36,6 +36,9 @@ _SIGS = {
     "orc_dsgesv": (_i, [_i, _i, _vp, _i, _vp, _vp, _i, _vp, _i, _pi]),
     "orc_dlange_inf": (_d, [_i, _i, _vp, _i]),
     "orc_dpotrs": (_i, [_c, _i, _i, _vp, _i, _vp, _i]),
+    "orc_dtrmm": (None, [_c, _c, _c, _c, _i, _i, _d, _vp, _i, _vp, _i]),
+    "orc_dsyr2k": (None, [_c, _c, _i, _i, _d, _vp, _i, _vp, _i, _d, _vp, _i]),
+    "orc_dgemmt": (None, [_c, _c, _c, _i, _i, _d, _vp, _i, _vp, _i, _d, _vp, _i]),
     "orc_dsposv": (_i, [_c, _i, _i, _vp, _i, _vp, _i, _vp, _i, _pi]),
 }
 
@@ -131,6 +134,19 @@ def dsgesv(n, nrhs, A, lda, ipiv, B, ldb, X, ldx):
     it = C.c_int(0)
     info = lib().orc_dsgesv(n, nrhs, _p(A), lda, _p(ipiv), _p(B), ldb, _p(X), ldx, C.byref(it))
     return info, it.value
+
+
+def dtrmm(side, uplo, ta, diag, m, n, alpha, A, lda, B, ldb):
+    lib().orc_dtrmm(_ch(side), _ch(uplo), _ch(ta), _ch(diag), m, n, alpha, _p(A), lda, _p(B), ldb)
+
+
+def dsyr2k(uplo, trans, n, k, alpha, A, lda, B, ldb, beta, Cm, ldc):
+    lib().orc_dsyr2k(_ch(uplo), _ch(trans), n, k, alpha, _p(A), lda, _p(B), ldb, beta, _p(Cm), ldc)
+
+
+def dgemmt(uplo, ta, tb, m, k, alpha, A, lda, B, ldb, beta, Cm, ldc):
+    lib().orc_dgemmt(_ch(uplo), _ch(ta), _ch(tb), m, k, alpha, _p(A), lda, _p(B), ldb, beta,
+                     _p(Cm), ldc)
 
 
 def dpotrs(uplo, n, nrhs, A, lda, B, ldb) -> int:

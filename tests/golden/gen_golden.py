@@ -3,8 +3,8 @@
 The OpenBLAS used is the one bundled with scipy (libscipy_openblas, OpenBLAS
 0.3.31.dev, DYNAMIC_ARCH; its exported ABI carries a ``scipy_`` prefix).  It
 is called through ctypes with exactly the Fortran-77 ABI the drop-in library
-exports (dgemm_, dtrsm_, dsyrk_, dgetrf_, dgetrs_, dgesv_, dpotrf_, dlaswp_,
-dsgesv_, sgetrf_).  The routines on this path are the same algorithms as the
+exports (dgemm_, dtrsm_, dtrmm_, dsyrk_, dsyr2k_, dgemmt_, dgetrf_, dgetrs_,
+dgesv_, dpotrf_, dpotrs_, dlaswp_, dsgesv_, dsposv_, sgetrf_).  The routines on this path are the same algorithms as the
 0.3.28.dev reference tree (interface/, driver/level3, lapack/).
 
 Inputs come from openblas_gb300.workloads (seeded counter-based splitmix64)
@@ -56,6 +56,17 @@ GETRF_PIV_ONLY = [512, 1024]
 POTRF_N = [1, 7, 64, 200]
 LASWP_CASES = [(7, 1, 9, 1), (7, 3, 9, 1), (7, 1, 9, -1), (5, 2, 8, 2), (5, 2, 8, -2)]
 DSGESV_CASES = [(50, 1), (200, 3)]
+GEMMT_SHAPES = [(1, 1), (7, 3), (35, 35), (33, 64)]
+GEMMT_AB = [(0.0, 1.3), (1.0, 0.0), (0.7, 1.3)]
+
+
+def trmm_operands(idx, side, uplo, m, n):
+    na = m if side == "L" else n
+    A = W.uniform(9000 + idx, (na, na))   # both triangles filled: only one may be read
+    B = W.uniform(9500 + idx, (m, n))
+    return A, B
+
+
 DPOTRS_CASES = [("L", 40, 1), ("U", 40, 5), ("L", 129, 3), ("U", 129, 1)]
 DSPOSV_CASES = [("L", 60, 1), ("U", 200, 3), ("L", 150, 2)]
 C1 = dict(m=1024, n=1024, k=1024, alpha=1.5, beta=0.5)
@@ -118,6 +129,45 @@ def main():
                     ob.dsyrk(uplo, tr, n, k, alpha, A, ra, beta, Cm, n)
                     g[f"dsyrk_{idx}"] = Cm
                     idx += 1
+    # ---- DTRMM (interface/trsm.c built as TRMM) -----------------------
+    idx = 0
+    for (m, n) in TRSM_SHAPES:
+        for side in "LR":
+            for uplo in "UL":
+                for ta in "NT":
+                    for diag in "UN":
+                        for alpha in TRSM_ALPHA:
+                            A, B = trmm_operands(idx, side, uplo, m, n)
+                            ob.dtrmm(side, uplo, ta, diag, m, n, alpha, A, A.shape[0], B, m)
+                            g[f"dtrmm_{idx}"] = B
+                            idx += 1
+    # ---- DSYR2K (interface/syr2k.c) ----------------------------------
+    idx = 0
+    for (n, k) in SYRK_SHAPES:
+        for uplo in "UL":
+            for tr in "NT":
+                for (alpha, beta) in SYRK_AB:
+                    ra, ca = (n, k) if tr == "N" else (k, n)
+                    A = W.uniform(9700 + idx, (ra, ca))
+                    B = W.uniform(9800 + idx, (ra, ca))
+                    Cm = W.uniform(9900 + idx, (n, n))
+                    ob.dsyr2k(uplo, tr, n, k, alpha, A, ra, B, ra, beta, Cm, n)
+                    g[f"dsyr2k_{idx}"] = Cm
+                    idx += 1
+    # ---- DGEMMT (interface/gemmt.c) ----------------------------------
+    idx = 0
+    for (m, k) in GEMMT_SHAPES:
+        for uplo in "UL":
+            for ta in "NT":
+                for tb in "NT":
+                    for (alpha, beta) in GEMMT_AB:
+                        A = W.uniform(10000 + idx, (m, k) if ta == "N" else (k, m))
+                        B = W.uniform(10100 + idx, (k, m) if tb == "N" else (m, k))
+                        Cm = W.uniform(10200 + idx, (m, m))
+                        ob.dgemmt(uplo, ta, tb, m, k, alpha, A, A.shape[0], B, B.shape[0],
+                                  beta, Cm, m)
+                        g[f"dgemmt_{idx}"] = Cm
+                        idx += 1
     # ---- DGETRF / DGETRS / DGESV (interface/lapack) -------------------
     for idx, (m, n) in enumerate(GETRF_SHAPES):
         A = W.uniform(7000 + idx, (m, n))

@@ -156,6 +156,34 @@ def test_dsgesv_argument_errors(gblib, F):
         assert _xerbla(gblib) == ("DSGESV", pos)
 
 
+def test_trmm_syr2k_gemmt_argument_errors(gblib, F):
+    buf = np.zeros((64, 64), order="F")
+    # interface/trsm.c built as TRMM: the TRSM positions under the name DTRMM
+    for args, pos in [(("X", "L", "N", "N", 4, 4, 4, 4), 1), (("L", "X", "N", "N", 4, 4, 4, 4), 2),
+                      (("L", "L", "X", "N", 4, 4, 4, 4), 3), (("L", "L", "N", "X", 4, 4, 4, 4), 4),
+                      (("L", "L", "N", "N", -1, 4, 4, 4), 5), (("L", "L", "N", "N", 4, -1, 4, 4), 6),
+                      (("R", "L", "N", "N", 4, 6, 5, 4), 9), (("L", "L", "N", "N", 4, 4, 4, 3), 11)]:
+        side, uplo, ta, diag, m, n, lda, ldb = args
+        F.dtrmm(side, uplo, ta, diag, m, n, 1.0, buf, lda, buf, ldb)
+        assert _xerbla(gblib) == ("DTRMM ", pos), args
+    # interface/syr2k.c:169-175
+    for args, pos in [(("X", "N", 4, 2, 4, 4, 4), 1), (("L", "X", 4, 2, 4, 4, 4), 2),
+                      (("L", "N", -1, 2, 4, 4, 4), 3), (("L", "N", 4, -1, 4, 4, 4), 4),
+                      (("L", "N", 4, 2, 3, 4, 4), 7), (("L", "T", 4, 6, 6, 5, 4), 9),
+                      (("U", "N", 4, 2, 4, 4, 3), 12)]:
+        uplo, tr, n, k, lda, ldb, ldc = args
+        F.dsyr2k(uplo, tr, n, k, 1.0, buf, lda, buf, ldb, 0.0, buf, ldc)
+        assert _xerbla(gblib) == ("DSYR2K", pos), args
+    # interface/gemmt.c:177-192
+    for args, pos in [(("X", "N", "N", 4, 2, 4, 2, 4), 1), (("L", "X", "N", 4, 2, 4, 2, 4), 2),
+                      (("L", "N", "X", 4, 2, 4, 2, 4), 3), (("L", "N", "N", -1, 2, 4, 2, 4), 4),
+                      (("L", "N", "N", 4, -1, 4, 2, 4), 5), (("L", "N", "N", 4, 2, 3, 2, 4), 8),
+                      (("L", "N", "T", 4, 2, 4, 3, 4), 10), (("U", "N", "N", 4, 2, 4, 2, 3), 13)]:
+        uplo, ta, tb, m, k, lda, ldb, ldc = args
+        F.dgemmt(uplo, ta, tb, m, k, 1.0, buf, lda, buf, ldb, 0.0, buf, ldc)
+        assert _xerbla(gblib) == ("DGEMMT", pos), args
+
+
 def test_dsposv_dpotrs_argument_errors(gblib, F):
     buf = np.zeros((64, 64), order="F")
     w = np.zeros(64 * 64)

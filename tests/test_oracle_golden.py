@@ -240,3 +240,60 @@ def test_dsposv_fallbacks(golden, orc):
     info, it = orc.dsposv("L", 30, 1, A, 30, B, 30, X, 30)
     assert info == int(golden["dsposv_npd_info"]) == 18
     assert it == int(golden["dsposv_npd_iter"]) == -3
+
+
+def _tri_other(uplo, X):
+    return np.triu(X, 1) if uplo == "L" else np.tril(X, -1)
+
+
+def test_dtrmm_cases(golden, orc):
+    idx = 0
+    for (m, n) in GG.TRSM_SHAPES:
+        for side in "LR":
+            for uplo in "UL":
+                for ta in "NT":
+                    for diag in "UN":
+                        for alpha in GG.TRSM_ALPHA:
+                            A, B = GG.trmm_operands(idx, side, uplo, m, n)
+                            orc.dtrmm(side, uplo, ta, diag, m, n, alpha, A, A.shape[0], B, m)
+                            ref = golden[f"dtrmm_{idx}"]
+                            scale = max(1.0, np.abs(ref).max())
+                            assert np.max(np.abs(B - ref)) <= 4 * A.shape[0] * EPS * scale, idx
+                            idx += 1
+
+
+def test_dsyr2k_cases(golden, orc):
+    idx = 0
+    for (n, k) in GG.SYRK_SHAPES:
+        for uplo in "UL":
+            for tr in "NT":
+                for (alpha, beta) in GG.SYRK_AB:
+                    ra, ca = (n, k) if tr == "N" else (k, n)
+                    A = W.uniform(9700 + idx, (ra, ca))
+                    B = W.uniform(9800 + idx, (ra, ca))
+                    Cm = W.uniform(9900 + idx, (n, n))
+                    C0 = Cm.copy(order="F")
+                    orc.dsyr2k(uplo, tr, n, k, alpha, A, ra, B, ra, beta, Cm, n)
+                    ref = golden[f"dsyr2k_{idx}"]
+                    assert np.max(np.abs(Cm - ref)) <= 8 * (k + 2) * EPS * max(1, np.abs(ref).max())
+                    assert np.array_equal(_tri_other(uplo, Cm), _tri_other(uplo, C0))
+                    idx += 1
+
+
+def test_dgemmt_cases(golden, orc):
+    idx = 0
+    for (m, k) in GG.GEMMT_SHAPES:
+        for uplo in "UL":
+            for ta in "NT":
+                for tb in "NT":
+                    for (alpha, beta) in GG.GEMMT_AB:
+                        A = W.uniform(10000 + idx, (m, k) if ta == "N" else (k, m))
+                        B = W.uniform(10100 + idx, (k, m) if tb == "N" else (m, k))
+                        Cm = W.uniform(10200 + idx, (m, m))
+                        C0 = Cm.copy(order="F")
+                        orc.dgemmt(uplo, ta, tb, m, k, alpha, A, A.shape[0], B, B.shape[0],
+                                   beta, Cm, m)
+                        ref = golden[f"dgemmt_{idx}"]
+                        assert np.max(np.abs(Cm - ref)) <= 4 * (k + 2) * EPS * max(1, np.abs(ref).max())
+                        assert np.array_equal(_tri_other(uplo, Cm), _tri_other(uplo, C0))
+                        idx += 1
