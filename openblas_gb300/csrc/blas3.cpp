@@ -68,18 +68,157 @@ static int dgemm_native(int ta, int tb, int64_t m, int64_t n, int64_t k, double 
 }
 
 
+static bool dgemm_wants_emulated(int64_t m, int64_t n, int64_t k) {
+  const int mode = gb_get_dgemm_mode();
+  return mode == GB_DGEMM_EMULATED ||
+         (mode == GB_DGEMM_AUTO && (double)m * n * k >= 256.0 * 256.0 * 256.0 && k >= 64);
+}
+
 // Selected by the DGEMM mode: emulated when requested, or in auto mode when
 // the product is large enough for the split/recombine passes to pay off.
 static int dgemm_dispatch(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
                           const double *A, int64_t lda, const double *B, int64_t ldb,
                           double beta, double *C, int64_t ldc, cudaStream_t s) {
-  int mode = gb_get_dgemm_mode();
-  bool emu = mode == GB_DGEMM_EMULATED ||
-             (mode == GB_DGEMM_AUTO && (double)m * n * k >= 256.0 * 256.0 * 256.0 && k >= 64);
-  if (emu && k > 0 && alpha != 0.0)
+  if (dgemm_wants_emulated(m, n, k) && k > 0 && alpha != 0.0)
     return dgemm_emulated(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
                           gb_get_ozaki_slices_internal(), s);
   return dgemm_native(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s);
+}
+
+// Host-pointer emulated DGEMM pipelined over column blocks of op(B) and C.
+// A goes up first and is split once; block j of op(B) (and of C when beta is
+// non-zero) is uploaded on the copy-in stream while earlier blocks compute,
+// and C's block j is downloaded on the copy-out stream while later blocks
+// compute.  The result is the one of the single-call emulated GEMM bit for
+// bit (each C(i,j) sees only row i of op(A) and column j of op(B)).  The
+// upload of block j+1 and the download of block j-1 are issued after block
+// j's kernels, so that pageable host buffers (whose copies the CUDA runtime
+// performs synchronously) still overlap with the GPU.
+namespace {
+struct PipelinedDgemm : EmuBlockHooks {
+  cudaStream_t s = nullptr, cin = nullptr, cout = nullptr;
+  int tb = 0;
+  int64_t m = 0, n = 0, k = 0, nb = 0, ldb = 0, ldc = 0;
+  const double *B = nullptr;
+  double *C = nullptr;
+  bool load_c = false;
+  double *dB = nullptr, *dC = nullptr;
+  int64_t dldb = 0;
+  std::vector<cudaEvent_t> up, done;
+
+  int upload(int64_t j) {
+    const int64_t j0 = j * nb, jn = (n - j0) < nb ? (n - j0) : nb;
+    if (tb)  // op(B) = B^T: rows j0.. of the n x k matrix B
+      GB_CUDA(cudaMemcpy2DAsync(dB + j0, dldb * 8, B + j0, ldb * 8, jn * 8, k,
+                                cudaMemcpyHostToDevice, cin));
+    else
+      GB_CUDA(cudaMemcpy2DAsync(dB + j0 * dldb, dldb * 8, B + j0 * ldb, ldb * 8, k * 8, jn,
+                                cudaMemcpyHostToDevice, cin));
+    if (load_c) {
+      int st = stage_in(dC + j0 * m, C + j0 * ldc, ldc, m, jn, 8, cin);
+      if (st) return st;
+    }
+    GB_CUDA(cudaEventRecord(up[j], cin));
+    return GB_SUCCESS;
+  }
+  int download(int64_t j) {
+    const int64_t j0 = j * nb, jn = (n - j0) < nb ? (n - j0) : nb;
+    GB_CUDA(cudaStreamWaitEvent(cout, done[j], 0));
+    return stage_out(C + j0 * ldc, dC + j0 * m, ldc, m, jn, 8, cout);
+  }
+  int before(int64_t j0, int64_t, const double **Bj, int64_t *ldbj, double **Cj,
+             int64_t *ldcj) override {
+    GB_CUDA(cudaStreamWaitEvent(s, up[j0 / nb], 0));
+    *Bj = tb ? dB + j0 : dB + j0 * dldb;
+    *ldbj = dldb;
+    *Cj = dC + j0 * m;
+    *ldcj = m;
+    return GB_SUCCESS;
+  }
+  int after(int64_t j0, int64_t) override {
+    const int64_t j = j0 / nb, nblk = (int64_t)up.size();
+    GB_CUDA(cudaEventRecord(done[j], s));
+    int st = GB_SUCCESS;
+    if (j + 1 < nblk && (st = upload(j + 1))) return st;
+    if (j > 0 && (st = download(j - 1))) return st;
+    if (j + 1 == nblk) return download(j);
+    return GB_SUCCESS;
+  }
+};
+}  // namespace
+
+// Returns 1 when the call was handled (successfully or with a recorded
+// error), 0 when the pipelined form does not apply.
+static int dgemm_host_pipelined(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
+                                const double *A, int64_t lda, const double *B, int64_t ldb,
+                                double beta, double *C, int64_t ldc) {
+  if (k <= 0 || alpha == 0.0 || k > 16384 || n < 6144 || m < 2048) return 0;
+  if (!dgemm_wants_emulated(m, n, k)) return 0;
+  if (is_device_pointer(A) || is_device_pointer(B) || is_device_pointer(C)) return 0;
+  PipelinedDgemm p;
+  p.s = stream();
+  if (copy_streams(&p.cin, &p.cout)) return 1;
+  int64_t nblk = n / 4096;
+  nblk = nblk < 2 ? 2 : nblk > 8 ? 8 : nblk;
+  p.nb = ((n + nblk - 1) / nblk + 255) / 256 * 256;
+  nblk = (n + p.nb - 1) / p.nb;
+  p.tb = tb;
+  p.m = m;
+  p.n = n;
+  p.k = k;
+  p.B = B;
+  p.ldb = ldb;
+  p.C = C;
+  p.ldc = ldc;
+  p.load_c = beta != 0.0;
+  const int64_t ra = ta ? k : m, ca = ta ? m : k;
+  p.dldb = tb ? n : k;
+  Scratch ws(((size_t)ra * ca + (size_t)n * k + (size_t)m * n) * 8, p.s);
+  if (!ws.p) {
+    set_error(GB_ERR_ALLOC, "dgemm: device staging of %lld x %lld x %lld", (long long)m,
+              (long long)n, (long long)k);
+    return 1;
+  }
+  double *dA = ws.as<double>();
+  p.dB = dA + ra * ca;
+  p.dC = p.dB + n * k;
+  p.up.assign(nblk, nullptr);
+  p.done.assign(nblk, nullptr);
+  cudaEvent_t ready = nullptr, a_up = nullptr, out_done = nullptr;
+  auto run = [&]() -> int {
+    for (int64_t j = 0; j < nblk; ++j) {
+      GB_CUDA(cudaEventCreateWithFlags(&p.up[j], cudaEventDisableTiming));
+      GB_CUDA(cudaEventCreateWithFlags(&p.done[j], cudaEventDisableTiming));
+    }
+    GB_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
+    GB_CUDA(cudaEventCreateWithFlags(&a_up, cudaEventDisableTiming));
+    GB_CUDA(cudaEventCreateWithFlags(&out_done, cudaEventDisableTiming));
+    // the staging buffer was allocated on the compute stream
+    GB_CUDA(cudaEventRecord(ready, p.s));
+    GB_CUDA(cudaStreamWaitEvent(p.cin, ready, 0));
+    int st = stage_in(dA, A, lda, ra, ca, 8, p.cin);
+    if (st) return st;
+    GB_CUDA(cudaEventRecord(a_up, p.cin));
+    if ((st = p.upload(0))) return st;
+    GB_CUDA(cudaStreamWaitEvent(p.s, a_up, 0));
+    st = dgemm_emulated_blocked(ta, tb, m, n, k, alpha, dA, ra, beta,
+                                gb_get_ozaki_slices_internal(), p.nb, &p, p.s);
+    // the staging buffer is released on the compute stream after the last download
+    GB_CUDA(cudaEventRecord(out_done, p.cout));
+    GB_CUDA(cudaStreamWaitEvent(p.s, out_done, 0));
+    return st;
+  };
+  int st = run();
+  cudaStreamSynchronize(p.cin);
+  cudaStreamSynchronize(p.cout);
+  if (!st) finish_blocking(p.s);
+  else cudaStreamSynchronize(p.s);
+  for (cudaEvent_t e : p.up) if (e) cudaEventDestroy(e);
+  for (cudaEvent_t e : p.done) if (e) cudaEventDestroy(e);
+  if (ready) cudaEventDestroy(ready);
+  if (a_up) cudaEventDestroy(a_up);
+  if (out_done) cudaEventDestroy(out_done);
+  return 1;
 }
 
 // Blocking host-pointer DGEMM after argument checks (column-major form).
@@ -88,6 +227,7 @@ static void dgemm_blocking(int ta, int tb, int64_t m, int64_t n, int64_t k, doub
                            double beta, double *C, int64_t ldc) {
   if (m == 0 || n == 0) return;  // interface/gemm.c:494
   if (ensure_init()) return;
+  if (dgemm_host_pipelined(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc)) return;
   cudaStream_t s = stream();
   bool need_ab = k > 0 && alpha != 0.0;
   Operand a(A, ta ? k : m, ta ? m : k, lda, 8), b(B, tb ? n : k, tb ? k : n, ldb, 8);

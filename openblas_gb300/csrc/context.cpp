@@ -111,6 +111,15 @@ int ensure_init() {
 
 cudaStream_t stream() { return t_ctx.stream; }
 
+int copy_streams(cudaStream_t *in, cudaStream_t *out) {
+  Context &c = t_ctx;
+  if (!c.copy_in) GB_CUDA(cudaStreamCreateWithFlags(&c.copy_in, cudaStreamNonBlocking));
+  if (!c.copy_out) GB_CUDA(cudaStreamCreateWithFlags(&c.copy_out, cudaStreamNonBlocking));
+  *in = c.copy_in;
+  *out = c.copy_out;
+  return GB_SUCCESS;
+}
+
 void *scratch_alloc(size_t bytes, cudaStream_t s) {
   if (bytes == 0) bytes = 256;
   void *p = nullptr;

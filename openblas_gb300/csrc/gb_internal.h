@@ -31,11 +31,15 @@ struct Context {
   cudaStream_t stream = nullptr;     // library stream (or user stream)
   bool user_stream = false;
   int *d_status = nullptr;           // device status word for kernel errors
+  cudaStream_t copy_in = nullptr;    // host->device uploads of pipelined calls
+  cudaStream_t copy_out = nullptr;   // device->host downloads of pipelined calls
 };
 Context &ctx();
 // Lazily initialise CUDA for this thread; returns GB_SUCCESS or an error.
 int ensure_init();
 cudaStream_t stream();
+// The two copy streams of this thread (created on first use).
+int copy_streams(cudaStream_t *in, cudaStream_t *out);
 
 // Stream-ordered device scratch (cudaMallocAsync from a pool that keeps its
 // memory cached between calls, so repeated calls do not hit the driver).
@@ -127,6 +131,20 @@ int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha
                    const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
                    double *C, int64_t ldc, int slices, cudaStream_t s, int tri = 0,
                    const int *skip = nullptr);
+// Column-blocked emulated DGEMM (one K segment, k <= 16384): op(A) is split
+// once; for each block of nb columns of op(B) and C, hooks->before supplies
+// device pointers to the block (after making it available, e.g. waiting for
+// its upload) and hooks->after runs once C's block is final (e.g. to start
+// its download), so transfers overlap the other blocks' work.
+struct EmuBlockHooks {
+  virtual int before(int64_t j0, int64_t jn, const double **Bj, int64_t *ldb, double **Cj,
+                     int64_t *ldc) = 0;
+  virtual int after(int64_t j0, int64_t jn) = 0;
+  virtual ~EmuBlockHooks() = default;
+};
+int dgemm_emulated_blocked(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
+                           const double *A, int64_t lda, double beta, int slices, int64_t nb,
+                           EmuBlockHooks *hooks, cudaStream_t s);
 // FP32 GEMM on the bf16 tensor cores (three-term split, FP32 accuracy).
 // Assumes m, n, k > 0.
 int sgemm_tc(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha, const float *A,

@@ -555,16 +555,24 @@ void split_operand(bool kcontig, int64_t R, int64_t K, const double *X, int64_t 
     { split_kernel<false><<<g2, 256, 0, s>>>(R, K, X, ld, expo, S, Rpad, Kpad, slices); count_launch(); }
 }
 
-// One pass over a K segment (k <= MAX_K_SEGMENT).
+// One pass over a K segment (k <= MAX_K_SEGMENT).  op(A) is split once;
+// the columns of op(B) and C are taken in blocks of `nb` (a multiple of BN):
+// each block is split, multiplied by the slice GEMM and recombined, with the
+// hooks (when given) making block j of op(B) and C available on the device
+// first and told when C's block is final.  Every C(i,j) depends only on row
+// i of op(A) and column j of op(B) (and their own exponents), so the blocked
+// result equals the single-block one bit for bit.
 int emulated_segment(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
                      const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
-                     double *C, int64_t ldc, int S, cudaStream_t s, int tri, const int *skip) {
-  const int64_t m_pad = round_up(m, BM), n_pad = round_up(n, BN), k_pad = round_up(k, BK);
+                     double *C, int64_t ldc, int S, cudaStream_t s, int tri, const int *skip,
+                     int64_t nb = 0, EmuBlockHooks *hooks = nullptr) {
+  if (nb <= 0 || nb >= n) nb = n;
+  const int64_t m_pad = round_up(m, BM), nb_pad = round_up(nb, BN), k_pad = round_up(k, BK);
   const size_t bytes_sa = align256((size_t)S * m_pad * k_pad * 2);
-  const size_t bytes_sb = align256((size_t)S * n_pad * k_pad * 2);
-  const size_t bytes_mx = align256((size_t)(m_pad + n_pad) * 8);
-  const size_t bytes_e = align256((size_t)(m_pad + n_pad) * 4);
-  const int64_t plane_stride = m_pad * n_pad;
+  const size_t bytes_sb = align256((size_t)S * nb_pad * k_pad * 2);
+  const size_t bytes_mx = align256((size_t)(m_pad + nb_pad) * 8);
+  const size_t bytes_e = align256((size_t)(m_pad + nb_pad) * 4);
+  const int64_t plane_stride = m_pad * nb_pad;
   const size_t bytes_pl = align256((size_t)S * plane_stride * 4);
   Scratch ws(bytes_sa + bytes_sb + bytes_mx + bytes_e + bytes_pl, s);
   if (!ws.p) return GB_ERR_ALLOC;
@@ -578,57 +586,67 @@ int emulated_segment(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
 
   // op(A) rows: K-contiguous when A is transposed; op(B) columns: K-contiguous when B is not
   split_operand(ta != 0, m, k, A, lda, S, m_pad, k_pad, mx, ea, sla, s);
-  split_operand(tb == 0, n, k, B, ldb, S, n_pad, k_pad, mx + m_pad, eb, slb, s);
-
   CUtensorMap mapA, mapB;
   int st = make_map(&mapA, sla, (int64_t)S * m_pad, k_pad, BM);
   if (st) return st;
-  if ((st = make_map(&mapB, slb, (int64_t)S * n_pad, k_pad, BN))) return st;
-
   static bool attr_set = false;
   if (!attr_set) {
     GB_CUDA(cudaFuncSetAttribute(slice_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  SMEM_BYTES));
     attr_set = true;
   }
-  GemmParams gp;
-  gp.S = S;
-  gp.m_tiles = (int)(m_pad / BM);
-  gp.n_tiles = (int)(n_pad / BN);
-  gp.group_m = config().ozaki_group_m;
-  gp.tri = tri;
-  gp.kblocks = (int)(k_pad / BK);
-  gp.m_pad = (int)m_pad;
-  gp.n_pad = (int)n_pad;
-  gp.plane_stride = plane_stride;
-  gp.planes = planes;
-  gp.status = ctx().d_status;
-  const int ntiles = gp.m_tiles * gp.n_tiles;
-  const int grid = ntiles < sm_count() ? ntiles : sm_count();
-  {
-    ProfileScope prof("slice_gemm", s);
-    slice_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, gp);
-    count_launch();
-  }
-  GB_CUDA(cudaGetLastError());
-
-  {
-    const dim3 g((unsigned)((m + BM - 1) / BM), (unsigned)((n + BN - 1) / BN));
+  for (int64_t j0 = 0; j0 < n; j0 += nb) {
+    const int64_t jn = (n - j0) < nb ? (n - j0) : nb;
+    const int64_t jn_pad = round_up(jn, BN);
+    const double *Bj = tb ? B + j0 : B + j0 * ldb;
+    double *Cj = C + j0 * ldc;
+    int64_t ldbj = ldb, ldcj = ldc;
+    if (hooks && (st = hooks->before(j0, jn, &Bj, &ldbj, &Cj, &ldcj))) return st;
+    split_operand(tb == 0, jn, k, Bj, ldbj, S, jn_pad, k_pad, mx + m_pad, eb, slb, s);
+    if ((st = make_map(&mapB, slb, (int64_t)S * jn_pad, k_pad, BN))) return st;
+    GemmParams gp;
+    gp.S = S;
+    gp.m_tiles = (int)(m_pad / BM);
+    gp.n_tiles = (int)(jn_pad / BN);
+    gp.group_m = config().ozaki_group_m;
+    // the triangle is relative to C's own indices: only the single-block
+    // form (j0 = 0) is used with tri
+    gp.tri = tri;
+    gp.kblocks = (int)(k_pad / BK);
+    gp.m_pad = (int)m_pad;
+    gp.n_pad = (int)jn_pad;
+    gp.plane_stride = m_pad * jn_pad;
+    gp.planes = planes;
+    gp.status = ctx().d_status;
+    const int ntiles = gp.m_tiles * gp.n_tiles;
+    const int grid = ntiles < sm_count() ? ntiles : sm_count();
+    {
+      ProfileScope prof("slice_gemm", s);
+      slice_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, gp);
+      count_launch();
+    }
+    GB_CUDA(cudaGetLastError());
+    {
+      const dim3 g((unsigned)((m + BM - 1) / BM), (unsigned)((jn + BN - 1) / BN));
+      const int64_t ps = gp.plane_stride;
 #define GB_RECOMBINE(SS)                                                                        \
   case SS:                                                                                      \
-    recombine_tile_kernel<SS><<<g, 256, 0, s>>>(m, n, gp.m_tiles, plane_stride, planes, ea, eb, \
-                                                alpha, beta, C, ldc, ta, tb, k, A, lda, B, ldb, \
+    recombine_tile_kernel<SS><<<g, 256, 0, s>>>(m, jn, gp.m_tiles, ps, planes, ea, eb, alpha,   \
+                                                beta, Cj, ldcj, ta, tb, k, A, lda, Bj, ldbj,    \
                                                 tri, skip);                                     \
     break;
-    switch (S) {
-      GB_RECOMBINE(1) GB_RECOMBINE(2) GB_RECOMBINE(3) GB_RECOMBINE(4)
-      GB_RECOMBINE(5) GB_RECOMBINE(6) GB_RECOMBINE(7) GB_RECOMBINE(8)
-      default: return set_error(GB_ERR_UNSUPPORTED, "emulated dgemm: %d slices", S);
-    }
+      switch (S) {
+        GB_RECOMBINE(1) GB_RECOMBINE(2) GB_RECOMBINE(3) GB_RECOMBINE(4)
+        GB_RECOMBINE(5) GB_RECOMBINE(6) GB_RECOMBINE(7) GB_RECOMBINE(8)
+        default: return set_error(GB_ERR_UNSUPPORTED, "emulated dgemm: %d slices", S);
+      }
 #undef GB_RECOMBINE
-    count_launch();
+      count_launch();
+    }
+    if ((st = check_cuda(cudaGetLastError(), "emulated dgemm"))) return st;
+    if (hooks && (st = hooks->after(j0, jn))) return st;
   }
-  return check_cuda(cudaGetLastError(), "emulated dgemm");
+  return GB_SUCCESS;
 }
 
 }  // namespace oz
@@ -636,6 +654,19 @@ int emulated_segment(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
 // Slice count used when the caller passes 0: 8 slices (56 bits) reach FP64
 // accuracy for operands whose rows/columns span a moderate exponent range.
 int ozaki_default_slices() { return oz::MAX_SLICES; }
+
+int dgemm_emulated_blocked(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
+                           const double *A, int64_t lda, double beta, int slices, int64_t nb,
+                           EmuBlockHooks *hooks, cudaStream_t s) {
+  int S = slices > 0 ? slices : ozaki_default_slices();
+  if (S > oz::MAX_SLICES) S = oz::MAX_SLICES;
+  if (m <= 0 || n <= 0) return GB_SUCCESS;
+  if (k > oz::MAX_K_SEGMENT || m > (int64_t)1 << 22 || n > (int64_t)1 << 22)
+    return set_error(GB_ERR_UNSUPPORTED, "blocked emulated dgemm: one K segment only");
+  nb = (nb + oz::BN - 1) / oz::BN * oz::BN;
+  return oz::emulated_segment(ta, tb, m, n, k, alpha, A, lda, nullptr, 0, beta, nullptr, 0, S, s,
+                              0, nullptr, nb, hooks);
+}
 
 int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
                    const double *A, int64_t lda, const double *B, int64_t ldb, double beta,

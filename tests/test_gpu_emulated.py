@@ -156,3 +156,51 @@ def test_device_entry_point(orc, gblib):
     orc.dgemm_dd("N", "N", m, n, k, 2.0, A, m, B, k, -1.0, Cref, m)
     G = orc.dgemm_absbound("N", "N", m, n, k, 2.0, A, m, B, k, -1.0, C, m)
     assert dmmch_ratio(got, Cref, G, k) <= 16
+
+
+def _device_emulated(gblib, ta, tb, m, n, k, alpha, A, B, beta, C):
+    torch = pytest.importorskip("torch")
+    dA, dB = torch.from_numpy(A.T.copy()).cuda(), torch.from_numpy(B.T.copy()).cuda()
+    dC = torch.from_numpy(C.T.copy()).cuda()
+    assert gblib.gb_dgemm_emulated_dev(ta.encode(), tb.encode(), m, n, k, alpha, dA.data_ptr(),
+                                       A.shape[0], dB.data_ptr(), B.shape[0], beta,
+                                       dC.data_ptr(), C.shape[0], 8) == 0
+    assert gblib.gb_synchronize() == 0
+    return dC.cpu().numpy().T
+
+
+@pytest.mark.parametrize("ta,tb,beta,pad", [("N", "N", 0.0, 0), ("T", "T", 0.5, 8),
+                                            ("N", "T", -1.0, 3)])
+def test_host_pipelined_equals_single_call(F, emulated, gblib, ta, tb, beta, pad):
+    """Host-pointer DGEMM with n >= 6144 runs column block by column block
+    with the uploads and downloads overlapping the other blocks' kernels;
+    every C(i,j) depends only on row i of op(A) and column j of op(B), so
+    the result equals the device-pointer single-call GEMM bit for bit --
+    including a ragged last block, padded leading dimensions, beta != 0
+    (C uploaded per block) and an Inf in a later block's column."""
+    m, n, k = 2100, 6500, 300
+    A, B, C = W.gemm_operands(90, m, n, k, ta, tb, pad=pad)
+    if tb == "N":
+        B[7, 6400] = np.inf
+    else:
+        B[6400, 7] = np.inf
+    ref = _device_emulated(gblib, ta, tb, m, n, k, 1.25, A, B, beta, C)
+    F.dgemm(ta, tb, m, n, k, 1.25, A, A.shape[0], B, B.shape[0], beta, C, C.shape[0])
+    assert np.array_equal(C, ref, equal_nan=True)
+    assert np.isinf(C[:m, 6400]).any()
+
+
+def test_host_pipelined_pinned_buffers(emulated, gblib):
+    """The same through cblas_dgemm on pinned (page-locked) host buffers."""
+    torch = pytest.importorskip("torch")
+    from openblas_gb300 import cblas
+    ns = cblas()
+    m, n, k = 2048, 8192, 512
+    A, B, C = W.gemm_operands(91, m, n, k, "N", "N")
+    ref = _device_emulated(gblib, "N", "N", m, n, k, 1.0, A, B, 0.0, C)
+    Ah = torch.from_numpy(A.T.copy()).pin_memory()
+    Bh = torch.from_numpy(B.T.copy()).pin_memory()
+    Ch = torch.full((n, m), float("nan"), dtype=torch.float64).pin_memory()
+    ns.cblas_dgemm(102, 111, 111, m, n, k, 1.0, Ah.data_ptr(), m, Bh.data_ptr(), k, 0.0,
+                   Ch.data_ptr(), m)
+    assert np.array_equal(Ch.numpy().T, ref)
