@@ -70,12 +70,16 @@ __device__ __forceinline__ void tile_coords(int tile, const Params &p, int &mt, 
 }
 
 // A tile takes part unless it lies wholly in the triangle left alone.
-__device__ __forceinline__ bool tile_active(int mt, int nt, const Params &p) {
-  if (p.tri == 1) return mt * BM + BM - 1 >= nt * BN;
-  if (p.tri == 2) return mt * BM <= nt * BN + BN - 1;
+template <int TRI>
+__device__ __forceinline__ bool tile_active(int mt, int nt) {
+  if (TRI == 1) return mt * BM + BM - 1 >= nt * BN;
+  if (TRI == 2) return mt * BM <= nt * BN + BN - 1;
   return true;
 }
 
+// TRI (0 all of C, 1 lower, 2 upper) is a template parameter so that the
+// full-C instance keeps the plain store loop of the epilogue.
+template <int TRI>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 sgemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tmA,
                     const __grid_constant__ CUtensorMap tmB, const Params p) {
@@ -141,7 +145,7 @@ sgemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tmA,
       for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
         int mt, nt;
         tile_coords(tile, p, mt, nt);
-        if (!tile_active(mt, nt, p)) continue;
+        if (!tile_active<TRI>(mt, nt)) continue;
         for (int kb = 0; ok && kb < p.kblocks; ++kb) {
           if (!mbar_wait(&aempty[as], aph ^ 1u, abort_flag, WAIT_LIMIT_NS)) {
             fail(1);
@@ -194,7 +198,7 @@ sgemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tmA,
       for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
         int mt, nt;
         tile_coords(tile, p, mt, nt);
-        if (!tile_active(mt, nt, p)) continue;
+        if (!tile_active<TRI>(mt, nt)) continue;
         if (!mbar_wait(&tempty[acc], acc_phase ^ 1u, abort_flag, WAIT_LIMIT_NS)) {
           fail(3);
           ok = false;
@@ -263,7 +267,7 @@ sgemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tmA,
     for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x) {
       int mt, nt;
       tile_coords(tile, p, mt, nt);
-      if (!tile_active(mt, nt, p)) continue;
+      if (!tile_active<TRI>(mt, nt)) continue;
       const bool got = mbar_wait(&tfull[acc], acc_phase, abort_flag, WAIT_LIMIT_NS);
       // the warp-wide tcgen05.ld below needs a converged warp: agree first
       if (!__all_sync(0xffffffffu, got)) {
@@ -289,13 +293,25 @@ sgemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tmA,
           float old[32];
 #pragma unroll
           for (int j = 0; j < 32; ++j) old[j] = (read_c && j < ncol) ? cp[j * p.ldc] : 0.f;
+          if constexpr (TRI == 0) {
 #pragma unroll
-          for (int j = 0; j < 32; ++j)
-            if (j < ncol && !((skip >> j) & 1u)) {
-              const int64_t col = col0 + c * 32 + j;
-              if ((p.tri == 1 && grow < col) || (p.tri == 2 && grow > col)) continue;
-              cp[j * p.ldc] = p.alpha * __uint_as_float(r[j]) + p.beta * old[j];
-            }
+            for (int j = 0; j < 32; ++j)
+              if (j < ncol && !((skip >> j) & 1u))
+                cp[j * p.ldc] = p.alpha * __uint_as_float(r[j]) + p.beta * old[j];
+          } else {
+            // columns j of this chunk inside the triangle: one mask per row
+            uint32_t wmask = ncol >= 32 ? 0xffffffffu : (ncol <= 0 ? 0u : (1u << ncol) - 1u);
+            wmask &= ~skip;
+            const int64_t d = grow - (col0 + c * 32);  // row minus the chunk's first column
+            if (TRI == 1)  // keep col <= row: j <= d
+              wmask &= d < 0 ? 0u : (d >= 31 ? 0xffffffffu : (2u << d) - 1u);
+            else           // keep col >= row: j >= d
+              wmask &= d <= 0 ? 0xffffffffu : (d > 31 ? 0u : ~((1u << d) - 1u));
+#pragma unroll
+            for (int j = 0; j < 32; ++j)
+              if ((wmask >> j) & 1u)
+                cp[j * p.ldc] = p.alpha * __uint_as_float(r[j]) + p.beta * old[j];
+          }
         }
       }
       tc_fence_before();
@@ -459,8 +475,12 @@ int sgemm_tc(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha, const
   if ((st = make_bf16_kmajor_map(&mapB, sb, 3 * n_pad, k_pad, BK, BN))) return st;
   static bool attr_set = false;
   if (!attr_set) {
-    GB_CUDA(cudaFuncSetAttribute(sgemm_bf16x3_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 SMEM_BYTES));
+    GB_CUDA(cudaFuncSetAttribute(sgemm_bf16x3_kernel<0>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    GB_CUDA(cudaFuncSetAttribute(sgemm_bf16x3_kernel<1>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    GB_CUDA(cudaFuncSetAttribute(sgemm_bf16x3_kernel<2>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
     attr_set = true;
   }
   Params p;
@@ -484,7 +504,9 @@ int sgemm_tc(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha, const
   const int grid = ntiles < sm_count() ? ntiles : sm_count();
   {
     ProfileScope prof("sgemm_tc", s);
-    sgemm_bf16x3_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, p);
+    if (tri == 1) sgemm_bf16x3_kernel<1><<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, p);
+    else if (tri == 2) sgemm_bf16x3_kernel<2><<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, p);
+    else sgemm_bf16x3_kernel<0><<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, p);
     count_launch();
   }
   { sgemm_fixup_kernel<<<sm_count() * 4, 256, 0, s>>>(m, n, k, alpha, A, lda, ta, B, ldb, tb, beta,
