@@ -80,6 +80,26 @@ void cblas_dgemmt(enum CBLAS_ORDER Order, enum CBLAS_UPLO Uplo, enum CBLAS_TRANS
                   enum CBLAS_TRANSPOSE TransB, blasint M, blasint K, double alpha,
                   const double *A, blasint lda, const double *B, blasint ldb, double beta,
                   double *C, blasint ldc);
+/* replace cblas_zgemm / cblas_cgemm / cblas_zgemm3m / cblas_cgemm3m,
+ * interface/gemm.c compiled with COMPLEX (and GEMM3M), cblas.h:302-309:
+ * alpha and beta point to (re, im); TransA/TransB may be CblasConjNoTrans and
+ * CblasConjTrans; arrays hold interleaved complex elements. */
+void cblas_zgemm(enum CBLAS_ORDER Order, enum CBLAS_TRANSPOSE TransA,
+                 enum CBLAS_TRANSPOSE TransB, blasint M, blasint N, blasint K,
+                 const void *alpha, const void *A, blasint lda, const void *B,
+                 blasint ldb, const void *beta, void *C, blasint ldc);
+void cblas_cgemm(enum CBLAS_ORDER Order, enum CBLAS_TRANSPOSE TransA,
+                 enum CBLAS_TRANSPOSE TransB, blasint M, blasint N, blasint K,
+                 const void *alpha, const void *A, blasint lda, const void *B,
+                 blasint ldb, const void *beta, void *C, blasint ldc);
+void cblas_zgemm3m(enum CBLAS_ORDER Order, enum CBLAS_TRANSPOSE TransA,
+                   enum CBLAS_TRANSPOSE TransB, blasint M, blasint N, blasint K,
+                   const void *alpha, const void *A, blasint lda, const void *B,
+                   blasint ldb, const void *beta, void *C, blasint ldc);
+void cblas_cgemm3m(enum CBLAS_ORDER Order, enum CBLAS_TRANSPOSE TransA,
+                   enum CBLAS_TRANSPOSE TransB, blasint M, blasint N, blasint K,
+                   const void *alpha, const void *A, blasint lda, const void *B,
+                   blasint ldb, const void *beta, void *C, blasint ldc);
 /* replaces cblas_dgemm_batch, interface/gemm_batch.c:117-372 (cblas.h:422-423) */
 void cblas_dgemm_batch(enum CBLAS_ORDER Order,
                        const enum CBLAS_TRANSPOSE *TransA_array,
@@ -104,6 +124,30 @@ void sgemm_(const char *TRANSA, const char *TRANSB, const blasint *M,
             const float *A, const blasint *ldA, const float *B,
             const blasint *ldB, const float *beta, float *C,
             const blasint *ldC);
+/* replace zgemm_ / cgemm_ (interface/gemm.c:181-290 compiled with COMPLEX,
+ * common_interface.h:492-495) and zgemm3m_ / cgemm3m_ (the same file with
+ * GEMM3M, common_interface.h:499-502): TRANSA/TRANSB in N, T, R (conjugate,
+ * no transpose), C (conjugate transpose); alpha/beta point to (re, im). */
+void zgemm_(const char *TRANSA, const char *TRANSB, const blasint *M,
+            const blasint *N, const blasint *K, const double *alpha,
+            const double *A, const blasint *ldA, const double *B,
+            const blasint *ldB, const double *beta, double *C,
+            const blasint *ldC);
+void cgemm_(const char *TRANSA, const char *TRANSB, const blasint *M,
+            const blasint *N, const blasint *K, const float *alpha,
+            const float *A, const blasint *ldA, const float *B,
+            const blasint *ldB, const float *beta, float *C,
+            const blasint *ldC);
+void zgemm3m_(const char *TRANSA, const char *TRANSB, const blasint *M,
+              const blasint *N, const blasint *K, const double *alpha,
+              const double *A, const blasint *ldA, const double *B,
+              const blasint *ldB, const double *beta, double *C,
+              const blasint *ldC);
+void cgemm3m_(const char *TRANSA, const char *TRANSB, const blasint *M,
+              const blasint *N, const blasint *K, const float *alpha,
+              const float *A, const blasint *ldA, const float *B,
+              const blasint *ldB, const float *beta, float *C,
+              const blasint *ldC);
 /* replaces dtrsm_, interface/trsm.c:114-209 */
 void dtrsm_(const char *SIDE, const char *UPLO, const char *TRANSA,
             const char *DIAG, const blasint *M, const blasint *N,
@@ -261,6 +305,25 @@ int gb_dsyr2k_dev(char uplo, char trans, int64_t n, int64_t k, double alpha, con
 int gb_dgemmt_dev(char uplo, char transa, char transb, int64_t m, int64_t k, double alpha,
                   const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
                   double *C, int64_t ldc);
+/* Complex GEMM on device pointers (interleaved complex arrays); alpha/beta
+ * are HOST pointers to (re, im).  zgemm: one real GEMM on the [Ar -Ai; Ai Ar]
+ * embedding with the current DGEMM mode; 3m: three real products. */
+int gb_zgemm_dev(char transa, char transb, int64_t m, int64_t n, int64_t k,
+                 const double *alpha, const double *A, int64_t lda,
+                 const double *B, int64_t ldb, const double *beta, double *C,
+                 int64_t ldc);
+int gb_cgemm_dev(char transa, char transb, int64_t m, int64_t n, int64_t k,
+                 const float *alpha, const float *A, int64_t lda,
+                 const float *B, int64_t ldb, const float *beta, float *C,
+                 int64_t ldc);
+int gb_zgemm3m_dev(char transa, char transb, int64_t m, int64_t n, int64_t k,
+                   const double *alpha, const double *A, int64_t lda,
+                   const double *B, int64_t ldb, const double *beta, double *C,
+                   int64_t ldc);
+int gb_cgemm3m_dev(char transa, char transb, int64_t m, int64_t n, int64_t k,
+                   const float *alpha, const float *A, int64_t lda,
+                   const float *B, int64_t ldb, const float *beta, float *C,
+                   int64_t ldc);
 int gb_dsyrk_dev(char uplo, char trans, int64_t n, int64_t k, double alpha,
                  const double *A, int64_t lda, double beta, double *C,
                  int64_t ldc);

@@ -42,6 +42,10 @@ DEV_SIGS = {
     "gb_dsyrk_dev": (_i, [_c, _c, _i64, _i64, _d, _vp, _i64, _d, _vp, _i64]),
     "gb_dtrmm_dev": (_i, [_c, _c, _c, _c, _i64, _i64, _d, _vp, _i64, _vp, _i64]),
     "gb_dsyr2k_dev": (_i, [_c, _c, _i64, _i64, _d, _vp, _i64, _vp, _i64, _d, _vp, _i64]),
+    "gb_zgemm_dev": (_i, [_c, _c, _i64, _i64, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _i64]),
+    "gb_cgemm_dev": (_i, [_c, _c, _i64, _i64, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _i64]),
+    "gb_zgemm3m_dev": (_i, [_c, _c, _i64, _i64, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _i64]),
+    "gb_cgemm3m_dev": (_i, [_c, _c, _i64, _i64, _i64, _vp, _vp, _i64, _vp, _i64, _vp, _vp, _i64]),
     "gb_dgemmt_dev": (_i, [_c, _c, _c, _i64, _i64, _d, _vp, _i64, _vp, _i64, _d, _vp, _i64]),
     "gb_dgetrf_dev": (_i, [_i64, _i64, _vp, _i64, _vp, _vp]),
     "gb_dgetrs_dev": (_i, [_c, _i64, _i64, _vp, _i64, _vp, _vp, _i64]),

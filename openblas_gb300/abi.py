@@ -41,6 +41,11 @@ FORTRAN_SIGS = {
     "dtrmm_": (None, [_pc, _pc, _pc, _pc, _pi, _pi, _pd, _vp, _pi, _vp, _pi]),
     "dsyr2k_": (None, [_pc, _pc, _pi, _pi, _pd, _vp, _pi, _vp, _pi, _pd, _vp, _pi]),
     "dgemmt_": (None, [_pc, _pc, _pc, _pi, _pi, _pd, _vp, _pi, _vp, _pi, _pd, _vp, _pi]),
+    # complex GEMM (interface/gemm.c with COMPLEX / GEMM3M): alpha, beta -> (re, im)
+    "zgemm_": (None, [_pc, _pc, _pi, _pi, _pi, _vp, _vp, _pi, _vp, _pi, _vp, _vp, _pi]),
+    "cgemm_": (None, [_pc, _pc, _pi, _pi, _pi, _vp, _vp, _pi, _vp, _pi, _vp, _vp, _pi]),
+    "zgemm3m_": (None, [_pc, _pc, _pi, _pi, _pi, _vp, _vp, _pi, _vp, _pi, _vp, _vp, _pi]),
+    "cgemm3m_": (None, [_pc, _pc, _pi, _pi, _pi, _vp, _vp, _pi, _vp, _pi, _vp, _vp, _pi]),
     # LAPACK (interface/lapack/*.c)
     "dgetrf_": (_i, [_pi, _pi, _vp, _pi, _vp, _pi]),
     "dgetrs_": (_i, [_pc, _pi, _pi, _vp, _pi, _vp, _vp, _pi, _pi]),
@@ -61,6 +66,10 @@ CBLAS_SIGS = {
     "cblas_dtrmm": (None, [_i, _i, _i, _i, _i, _i, _i, _d, _vp, _i, _vp, _i]),
     "cblas_dsyr2k": (None, [_i, _i, _i, _i, _i, _d, _vp, _i, _vp, _i, _d, _vp, _i]),
     "cblas_dgemmt": (None, [_i, _i, _i, _i, _i, _i, _d, _vp, _i, _vp, _i, _d, _vp, _i]),
+    "cblas_zgemm": (None, [_i, _i, _i, _i, _i, _i, _vp, _vp, _i, _vp, _i, _vp, _vp, _i]),
+    "cblas_cgemm": (None, [_i, _i, _i, _i, _i, _i, _vp, _vp, _i, _vp, _i, _vp, _vp, _i]),
+    "cblas_zgemm3m": (None, [_i, _i, _i, _i, _i, _i, _vp, _vp, _i, _vp, _i, _vp, _vp, _i]),
+    "cblas_cgemm3m": (None, [_i, _i, _i, _i, _i, _i, _vp, _vp, _i, _vp, _i, _vp, _vp, _i]),
     "cblas_dgemm_batch": (None, [_i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                  _vp, _vp, _i, _vp]),
 }
@@ -113,6 +122,25 @@ class Fortran:
         self.ns.dgemm_(self._c(ta), self._c(tb), C.byref(_i(m)), C.byref(_i(n)), C.byref(_i(k)),
                        C.byref(_d(alpha)), _ptr(A), C.byref(_i(lda)), _ptr(B), C.byref(_i(ldb)),
                        C.byref(_d(beta)), _ptr(Cm), C.byref(_i(ldc)))
+
+    def _complex_gemm(self, fn, real, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, Cm, ldc):
+        al = np.array([complex(alpha).real, complex(alpha).imag], dtype=real)
+        be = np.array([complex(beta).real, complex(beta).imag], dtype=real)
+        fn(self._c(ta), self._c(tb), C.byref(_i(m)), C.byref(_i(n)), C.byref(_i(k)),
+           al.ctypes.data_as(C.c_void_p), _ptr(A), C.byref(_i(lda)), _ptr(B), C.byref(_i(ldb)),
+           be.ctypes.data_as(C.c_void_p), _ptr(Cm), C.byref(_i(ldc)))
+
+    def zgemm(self, *args):
+        self._complex_gemm(self.ns.zgemm_, np.float64, *args)
+
+    def cgemm(self, *args):
+        self._complex_gemm(self.ns.cgemm_, np.float32, *args)
+
+    def zgemm3m(self, *args):
+        self._complex_gemm(self.ns.zgemm3m_, np.float64, *args)
+
+    def cgemm3m(self, *args):
+        self._complex_gemm(self.ns.cgemm3m_, np.float32, *args)
 
     def sgemm(self, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, Cm, ldc):
         self.ns.sgemm_(self._c(ta), self._c(tb), C.byref(_i(m)), C.byref(_i(n)), C.byref(_i(k)),

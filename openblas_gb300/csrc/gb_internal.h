@@ -150,6 +150,11 @@ int dgemm_emulated_blocked(int ta, int tb, int64_t m, int64_t n, int64_t k, doub
 int sgemm_tc(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha, const float *A,
              int64_t lda, const float *B, int64_t ldb, float beta, float *C, int64_t ldc,
              cudaStream_t s, int tri = 0, const int *skip = nullptr);
+// FP64 GEMM on a triangle of C (tri 0 full, 1 lower, 2 upper) with the
+// engine the DGEMM mode selects (native DFMA or emulated); k > 0, alpha != 0.
+int dgemm_select(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha, const double *A,
+                 int64_t lda, const double *B, int64_t ldb, double beta, double *C, int64_t ldc,
+                 int tri, cudaStream_t s);
 // FP32 GEMM behind sgemm_/cblas_sgemm and the FP32 LU: the tensor-core form
 // for shapes large enough to fill the GPU (GB_SGEMM_MODE=auto, default), or
 // always SIMT / always tensor (GB_SGEMM_MODE=simt|tensor).

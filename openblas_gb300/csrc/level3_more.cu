@@ -44,19 +44,20 @@ bool use_emulated(int64_t m, int64_t n, int64_t k) {
          (mode == GB_DGEMM_AUTO && (double)m * n * k >= 256.0 * 256.0 * 256.0 && k >= 64);
 }
 
+}  // namespace
+
 // C = alpha op(A) op(B) + beta C on a triangle of C (tri 0 full, 1 lower,
-// 2 upper); assumes k > 0 and alpha != 0.
-int gemm_tri(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha, const double *A,
-             int64_t lda, const double *B, int64_t ldb, double beta, double *C, int64_t ldc,
-             int tri, cudaStream_t s) {
+// 2 upper) with the FP64 GEMM the DGEMM mode selects; assumes k > 0 and
+// alpha != 0.
+int dgemm_select(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha, const double *A,
+                 int64_t lda, const double *B, int64_t ldb, double beta, double *C, int64_t ldc,
+                 int tri, cudaStream_t s) {
   if (use_emulated(m, n, k))
     return dgemm_emulated(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
                           gb_get_ozaki_slices_internal(), s, tri);
   launch_dgemm_fp64_tri(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, s, nullptr);
   return check_cuda(cudaGetLastError(), "gemm launch");
 }
-
-}  // namespace
 
 int dgemmt_device(int uplo, int ta, int tb, int64_t m, int64_t k, double alpha, const double *A,
                   int64_t lda, const double *B, int64_t ldb, double beta, double *C,
@@ -67,7 +68,7 @@ int dgemmt_device(int uplo, int ta, int tb, int64_t m, int64_t k, double alpha, 
     launch_dbeta_tri(m, beta, C, ldc, tri, s);
     return check_cuda(cudaGetLastError(), "gemmt beta");
   }
-  return gemm_tri(ta, tb, m, m, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, s);
+  return dgemm_select(ta, tb, m, m, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, s);
 }
 
 // trans 0: C = alpha A B^T + alpha B A^T + beta C (A, B n x k);
@@ -82,9 +83,9 @@ int dsyr2k_device(int uplo, int trans, int64_t n, int64_t k, double alpha, const
     return check_cuda(cudaGetLastError(), "syr2k beta");
   }
   const int ta = trans ? 1 : 0, tb = trans ? 0 : 1;
-  int st = gemm_tri(ta, tb, n, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, s);
+  int st = dgemm_select(ta, tb, n, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, s);
   if (st) return st;
-  return gemm_tri(ta, tb, n, n, k, alpha, B, ldb, A, lda, 1.0, C, ldc, tri, s);
+  return dgemm_select(ta, tb, n, n, k, alpha, B, ldb, A, lda, 1.0, C, ldc, tri, s);
 }
 
 // side 0: B = alpha op(A) B (A m x m); side 1: B = alpha B op(A) (A n x n).
@@ -106,8 +107,8 @@ int dtrmm_device(int side, int uplo, int trans, int unit_code, int64_t m, int64_
   { tri_copy_kernel<<<(unsigned)(blocks < cap ? blocks : cap), 256, 0, s>>>(na, A, lda, uplo, unit_code, T); count_launch(); }
   GB_CUDA(cudaMemcpy2DAsync(Bt, m * 8, B, ldb * 8, m * 8, n, cudaMemcpyDeviceToDevice, s));
   if (side == 0)
-    return gemm_tri(trans, 0, m, n, m, alpha, T, na, Bt, m, 0.0, B, ldb, 0, s);
-  return gemm_tri(0, trans, m, n, n, alpha, Bt, m, T, na, 0.0, B, ldb, 0, s);
+    return dgemm_select(trans, 0, m, n, m, alpha, T, na, Bt, m, 0.0, B, ldb, 0, s);
+  return dgemm_select(0, trans, m, n, n, alpha, Bt, m, T, na, 0.0, B, ldb, 0, s);
 }
 
 }  // namespace gb

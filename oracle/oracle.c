@@ -888,3 +888,129 @@ fallback:
   orc_dpotrs(uplo, n, nrhs, A, lda, X, ldx);
   return 0;
 }
+
+/* ------------------------------------------------------------------------ */
+/* Complex GEMM: ZGEMM/CGEMM and the 3M forms ZGEMM3M/CGEMM3M               */
+/* ------------------------------------------------------------------------ */
+/* op codes of interface/gemm.c:253-268 compiled with COMPLEX: N 0, T 1,
+ * R 2 (conjugate, no transpose), C 3 (conjugate transpose); -1 invalid. */
+static int ztrans(char t) {
+  if (t >= 'a' && t <= 'z') t = (char)(t - 32);
+  return t == 'N' ? 0 : t == 'T' ? 1 : t == 'R' ? 2 : t == 'C' ? 3 : -1;
+}
+
+/* C <- beta C, kernel/generic/zgemm_beta.c:38-100: beta = 0 stores zeros;
+ * level3.c:229-249 skips beta = (1, 0). */
+#define DEFINE_ZBETA(NAME, T)                                                  \
+  static void NAME(int m, int n, T br, T bi, T *C, int ldc) {                  \
+    if (br == (T)1 && bi == (T)0) return;                                      \
+    for (int j = 0; j < n; ++j)                                                \
+      for (int i = 0; i < m; ++i) {                                            \
+        T *c = C + 2 * ((size_t)j * ldc + i);                                  \
+        if (br == (T)0 && bi == (T)0) {                                        \
+          c[0] = (T)0;                                                         \
+          c[1] = (T)0;                                                         \
+        } else {                                                               \
+          T r = br * c[0] - bi * c[1], s = br * c[1] + bi * c[0];              \
+          c[0] = r;                                                            \
+          c[1] = s;                                                            \
+        }                                                                      \
+      }                                                                        \
+  }
+DEFINE_ZBETA(zbeta_d, double)
+DEFINE_ZBETA(zbeta_s, float)
+
+/* op(X)(i, p) of a complex matrix stored column-major with leading dimension
+ * ld: transposed for codes 1 and 3, conjugated for codes 2 and 3. */
+#define ZELEM(T, X, ld, code, i, p, re, im)                                    \
+  do {                                                                         \
+    const T *e_ = ((code) & 1) ? (X) + 2 * ((size_t)(i) * (ld) + (p))          \
+                               : (X) + 2 * ((size_t)(p) * (ld) + (i));         \
+    re = e_[0];                                                                \
+    im = (code) >= 2 ? -e_[1] : e_[1];                                         \
+  } while (0)
+
+/* ZGEMM / CGEMM: level3.c:229-259 (beta, then nothing when k = 0 or
+ * alpha = 0) and the complex kernels' accumulate-then-scale
+ * (kernel/generic/zgemmkernel_2x2.c: c += alpha * sum op(a) op(b)). */
+#define DEFINE_ZGEMM(NAME, T, BETA)                                            \
+  void NAME(char transa, char transb, int m, int n, int k, const T *alpha,     \
+            const T *A, int lda, const T *B, int ldb, const T *beta, T *C,     \
+            int ldc) {                                                         \
+    if (m <= 0 || n <= 0) return;                                              \
+    const int ta = ztrans(transa), tb = ztrans(transb);                        \
+    const T ar = alpha[0], ai = alpha[1];                                      \
+    BETA(m, n, beta[0], beta[1], C, ldc);                                      \
+    if (k <= 0 || (ar == (T)0 && ai == (T)0)) return;                          \
+    int nthr = orc_get_threads();                                              \
+    if ((double)m * n * k < 2e5) nthr = 1;                                     \
+    _Pragma("omp parallel for num_threads(nthr) schedule(dynamic, 4)")         \
+    for (int j = 0; j < n; ++j)                                                \
+      for (int i = 0; i < m; ++i) {                                            \
+        T sr = (T)0, si = (T)0;                                                \
+        for (int p = 0; p < k; ++p) {                                          \
+          T a_r, a_i, b_r, b_i;                                                \
+          ZELEM(T, A, lda, ta, i, p, a_r, a_i);                                \
+          ZELEM(T, B, ldb, tb, p, j, b_r, b_i);                                \
+          sr += a_r * b_r - a_i * b_i;                                         \
+          si += a_r * b_i + a_i * b_r;                                         \
+        }                                                                      \
+        T *c = C + 2 * ((size_t)j * ldc + i);                                  \
+        c[0] += ar * sr - ai * si;                                             \
+        c[1] += ar * si + ai * sr;                                             \
+      }                                                                        \
+  }
+DEFINE_ZGEMM(orc_zgemm, double, zbeta_d)
+DEFINE_ZGEMM(orc_cgemm, float, zbeta_s)
+
+/* ZGEMM3M / CGEMM3M, driver/level3/gemm3m_level3.c: B' = alpha op(B) formed
+ * in the copies of B (zgemm3m_ncopy_*.c REAL_PART / IMAGE_PART), then three
+ * real products T1 = (Ar + Ai)(B'r + B'i), T2 = Ar B'r, T3 = Ai B'i added to
+ * C with the ALPHA5..ALPHA18 signs of the NN case (gemm3m_level3.c:155-168):
+ * Im += T1; Re += T2, Im -= T2; Re -= T3, Im -= T3. */
+#define DEFINE_ZGEMM3M(NAME, T, BETA)                                          \
+  void NAME(char transa, char transb, int m, int n, int k, const T *alpha,     \
+            const T *A, int lda, const T *B, int ldb, const T *beta, T *C,     \
+            int ldc) {                                                         \
+    if (m <= 0 || n <= 0) return;                                              \
+    const int ta = ztrans(transa), tb = ztrans(transb);                        \
+    const T ar = alpha[0], ai = alpha[1];                                      \
+    BETA(m, n, beta[0], beta[1], C, ldc);                                      \
+    if (k <= 0 || (ar == (T)0 && ai == (T)0)) return;                          \
+    T *bp = (T *)malloc(sizeof(T) * 3 * (size_t)k * n); /* B'r, B'i, sum */    \
+    for (int j = 0; j < n; ++j)                                                \
+      for (int p = 0; p < k; ++p) {                                            \
+        T b_r, b_i;                                                            \
+        ZELEM(T, B, ldb, tb, p, j, b_r, b_i);                                  \
+        const T wr = ar * b_r - ai * b_i, wi = ai * b_r + ar * b_i;            \
+        const size_t e = (size_t)j * k + p, kn = (size_t)k * n;                \
+        bp[e] = wr;                                                            \
+        bp[kn + e] = wi;                                                       \
+        bp[2 * kn + e] = wr + wi;                                              \
+      }                                                                        \
+    int nthr = orc_get_threads();                                              \
+    if ((double)m * n * k < 2e5) nthr = 1;                                     \
+    _Pragma("omp parallel for num_threads(nthr) schedule(dynamic, 4)")         \
+    for (int j = 0; j < n; ++j)                                                \
+      for (int i = 0; i < m; ++i) {                                            \
+        T t1 = (T)0, t2 = (T)0, t3 = (T)0;                                     \
+        const size_t kn = (size_t)k * n;                                       \
+        for (int p = 0; p < k; ++p) {                                          \
+          T a_r, a_i;                                                          \
+          ZELEM(T, A, lda, ta, i, p, a_r, a_i);                                \
+          const size_t e = (size_t)j * k + p;                                  \
+          t1 += (a_r + a_i) * bp[2 * kn + e];                                  \
+          t2 += a_r * bp[e];                                                   \
+          t3 += a_i * bp[kn + e];                                              \
+        }                                                                      \
+        T *c = C + 2 * ((size_t)j * ldc + i);                                  \
+        c[1] += t1;                                                            \
+        c[0] += t2;                                                            \
+        c[1] -= t2;                                                            \
+        c[0] -= t3;                                                            \
+        c[1] -= t3;                                                            \
+      }                                                                        \
+    free(bp);                                                                  \
+  }
+DEFINE_ZGEMM3M(orc_zgemm3m, double, zbeta_d)
+DEFINE_ZGEMM3M(orc_cgemm3m, float, zbeta_s)

@@ -94,6 +94,22 @@ int orc_dsgesv(int n, int nrhs, double *A, int lda, int *ipiv, const double *B,
 /* ||A||_inf (max row sum). (lapack-netlib/SRC/dlange.f, NORM='I') */
 double orc_dlange_inf(int m, int n, const double *A, int lda);
 
+/* Complex GEMM on interleaved (re, im) arrays, alpha/beta -> (re, im), op
+ * codes N, T, R, C.  4M semantics (interface/gemm.c with COMPLEX,
+ * driver/level3/level3.c) and the 3M driver (driver/level3/gemm3m_level3.c). */
+void orc_zgemm(char transa, char transb, int m, int n, int k, const double *alpha,
+               const double *A, int lda, const double *B, int ldb, const double *beta,
+               double *C, int ldc);
+void orc_cgemm(char transa, char transb, int m, int n, int k, const float *alpha,
+               const float *A, int lda, const float *B, int ldb, const float *beta, float *C,
+               int ldc);
+void orc_zgemm3m(char transa, char transb, int m, int n, int k, const double *alpha,
+                 const double *A, int lda, const double *B, int ldb, const double *beta,
+                 double *C, int ldc);
+void orc_cgemm3m(char transa, char transb, int m, int n, int k, const float *alpha,
+                 const float *A, int lda, const float *B, int ldb, const float *beta, float *C,
+                 int ldc);
+
 #ifdef __cplusplus
 }
 #endif

@@ -40,6 +40,10 @@ _SIGS = {
     "orc_dsyr2k": (None, [_c, _c, _i, _i, _d, _vp, _i, _vp, _i, _d, _vp, _i]),
     "orc_dgemmt": (None, [_c, _c, _c, _i, _i, _d, _vp, _i, _vp, _i, _d, _vp, _i]),
     "orc_dsposv": (_i, [_c, _i, _i, _vp, _i, _vp, _i, _vp, _i, _pi]),
+    "orc_zgemm": (None, [_c, _c, _i, _i, _i, _vp, _vp, _i, _vp, _i, _vp, _vp, _i]),
+    "orc_cgemm": (None, [_c, _c, _i, _i, _i, _vp, _vp, _i, _vp, _i, _vp, _vp, _i]),
+    "orc_zgemm3m": (None, [_c, _c, _i, _i, _i, _vp, _vp, _i, _vp, _i, _vp, _vp, _i]),
+    "orc_cgemm3m": (None, [_c, _c, _i, _i, _i, _vp, _vp, _i, _vp, _i, _vp, _vp, _i]),
 }
 
 _lib = None
@@ -142,6 +146,29 @@ def dtrmm(side, uplo, ta, diag, m, n, alpha, A, lda, B, ldb):
 
 def dsyr2k(uplo, trans, n, k, alpha, A, lda, B, ldb, beta, Cm, ldc):
     lib().orc_dsyr2k(_ch(uplo), _ch(trans), n, k, alpha, _p(A), lda, _p(B), ldb, beta, _p(Cm), ldc)
+
+
+def _complex_gemm(name, real, ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, Cm, ldc):
+    al = np.array([complex(alpha).real, complex(alpha).imag], dtype=real)
+    be = np.array([complex(beta).real, complex(beta).imag], dtype=real)
+    getattr(lib(), name)(_ch(ta), _ch(tb), m, n, k, _p(al), _p(A), lda, _p(B), ldb, _p(be),
+                         _p(Cm), ldc)
+
+
+def zgemm(*args):
+    _complex_gemm("orc_zgemm", np.float64, *args)
+
+
+def cgemm(*args):
+    _complex_gemm("orc_cgemm", np.float32, *args)
+
+
+def zgemm3m(*args):
+    _complex_gemm("orc_zgemm3m", np.float64, *args)
+
+
+def cgemm3m(*args):
+    _complex_gemm("orc_cgemm3m", np.float32, *args)
 
 
 def dgemmt(uplo, ta, tb, m, k, alpha, A, lda, B, ldb, beta, Cm, ldc):

@@ -83,3 +83,37 @@ def dmmch_ratio(Cgot, Cref, G, k):
     with np.errstate(invalid="ignore", divide="ignore"):
         r = np.where(G > 0, d / (EPS * np.where(G > 0, G, 1.0)), 0.0)
     return float(r.max()) if r.size else 0.0
+
+
+def complex_op(X, rows, cols, code):
+    """op(X) of the stored complex matrix X[:rows, :cols] for op code N, T,
+    R (conjugate) or C (conjugate transpose)."""
+    X = X[:rows, :cols]
+    if code in "TC":
+        X = X.T
+    if code in "RC":
+        X = X.conj()
+    return X
+
+
+def zgemm_ratio(Cgot, Cref, A, B, C0, m, n, k, ta, tb, alpha, beta, eps, normwise=False):
+    """DMMCH-style ratio for a complex GEMM: max |Cgot - Cref| / (eps G) with
+    G = |alpha| |op(A)| |op(B)| + |beta| |C0| (moduli), componentwise, or
+    with G replaced by its maximum (normwise: the 3M products and the
+    emulated-FP64 engine are bounded normwise, not per element)."""
+    ra, ca = (m, k) if ta in "NR" else (k, m)
+    rb, cb = (k, n) if tb in "NR" else (n, k)
+    oA = np.abs(complex_op(A, ra, ca, ta)).astype(np.float64)
+    oB = np.abs(complex_op(B, rb, cb, tb)).astype(np.float64)
+    G = abs(alpha) * (oA @ oB) if k > 0 else np.zeros((m, n))
+    if beta != 0:
+        G = G + abs(beta) * np.abs(C0[:m, :n]).astype(np.float64)
+    if normwise:
+        G = np.full_like(G, G.max() if G.size else 0.0)
+    d = np.abs(np.asarray(Cgot[:m, :n], dtype=np.complex128) -
+               np.asarray(Cref[:m, :n], dtype=np.complex128))
+    if ((G == 0) & (d != 0)).any() or np.isnan(d).any():
+        return np.inf
+    with np.errstate(invalid="ignore", divide="ignore"):
+        r = np.where(G > 0, d / (eps * np.where(G > 0, G, 1.0)), 0.0)
+    return float(r.max()) if r.size else 0.0

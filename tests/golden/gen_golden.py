@@ -3,7 +3,7 @@
 The OpenBLAS used is the one bundled with scipy (libscipy_openblas, OpenBLAS
 0.3.31.dev, DYNAMIC_ARCH; its exported ABI carries a ``scipy_`` prefix).  It
 is called through ctypes with exactly the Fortran-77 ABI the drop-in library
-exports (dgemm_, dtrsm_, dtrmm_, dsyrk_, dsyr2k_, dgemmt_, dgetrf_, dgetrs_,
+exports (dgemm_, zgemm_, cgemm_, zgemm3m_, cgemm3m_, dtrsm_, dtrmm_, dsyrk_, dsyr2k_, dgemmt_, dgetrf_, dgetrs_,
 dgesv_, dpotrf_, dpotrs_, dlaswp_, dsgesv_, dsposv_, sgetrf_).  The routines on this path are the same algorithms as the
 0.3.28.dev reference tree (interface/, driver/level3, lapack/).
 
@@ -65,6 +65,43 @@ def trmm_operands(idx, side, uplo, m, n):
     A = W.uniform(9000 + idx, (na, na))   # both triangles filled: only one may be read
     B = W.uniform(9500 + idx, (m, n))
     return A, B
+
+
+# complex GEMM: every op pair (N, T, R, C) on two shapes, edge shapes on two
+# op pairs; alpha/beta as (re, im)
+ZGEMM_SHAPES = [(3, 5, 7), (35, 9, 33)]
+ZGEMM_AB = [(1.0 + 0.0j, 0.0j), (0.7 - 0.4j, 0.3 + 1.2j)]
+ZGEMM_EDGE_SHAPES = [(1, 1, 1), (5, 7, 0)]
+ZGEMM_EDGE_AB = [(0.0j, 0.0j), (0.0j, 1.5 - 0.5j), (1.0 + 0.0j, 1.0 + 0.0j), (0.7 - 0.4j, 0.0j)]
+ZGEMM_ROUTINES = [("zgemm", np.complex128), ("cgemm", np.complex64),
+                  ("zgemm3m", np.complex128), ("cgemm3m", np.complex64)]
+
+
+def zgemm_cases():
+    """(m, n, k, ta, tb, alpha, beta) in the order of the stored outputs."""
+    cases = []
+    for (m, n, k) in ZGEMM_SHAPES:
+        for ta in "NTRC":
+            for tb in "NTRC":
+                for (al, be) in ZGEMM_AB:
+                    cases.append((m, n, k, ta, tb, al, be))
+    for (m, n, k) in ZGEMM_EDGE_SHAPES:
+        for (ta, tb) in (("N", "N"), ("C", "T")):
+            for (al, be) in ZGEMM_EDGE_AB:
+                cases.append((m, n, k, ta, tb, al, be))
+    return cases
+
+
+def complex_operands(idx, m, n, k, ta, tb, dtype):
+    """A, B, C (complex, column-major, ld = rows + 2) for case idx; C holds NaN
+    when beta = 0 (it must be overwritten, not propagated)."""
+    ra, ca = (m, k) if ta in "NR" else (k, m)
+    rb, cb = (k, n) if tb in "NR" else (n, k)
+
+    def cplx(seed, r, c):
+        X = W.uniform(seed, (r + 2, c)) + 1j * W.uniform(seed + 50000, (r + 2, c))
+        return np.asfortranarray(X.astype(dtype))
+    return cplx(11000 + idx, ra, ca), cplx(12000 + idx, rb, cb), cplx(13000 + idx, m, n)
 
 
 DPOTRS_CASES = [("L", 40, 1), ("U", 40, 5), ("L", 129, 3), ("U", 129, 1)]
@@ -168,6 +205,15 @@ def main():
                                   beta, Cm, m)
                         g[f"dgemmt_{idx}"] = Cm
                         idx += 1
+    # ---- ZGEMM / CGEMM / ZGEMM3M / CGEMM3M (interface/gemm.c, COMPLEX) --
+    for name, dt in ZGEMM_ROUTINES:
+        for idx, (m, n, k, ta, tb, al, be) in enumerate(zgemm_cases()):
+            A, B, Cm = complex_operands(idx, m, n, k, ta, tb, dt)
+            if be == 0:
+                Cm[:m, :n] = np.nan
+            getattr(ob, name)(ta, tb, m, n, k, al, A, A.shape[0], B, B.shape[0], be, Cm,
+                              Cm.shape[0])
+            g[f"{name}_{idx}"] = Cm[:m, :n].copy(order="F")
     # ---- DGETRF / DGETRS / DGESV (interface/lapack) -------------------
     for idx, (m, n) in enumerate(GETRF_SHAPES):
         A = W.uniform(7000 + idx, (m, n))

@@ -184,6 +184,35 @@ def test_trmm_syr2k_gemmt_argument_errors(gblib, F):
         assert _xerbla(gblib) == ("DGEMMT", pos), args
 
 
+def test_complex_gemm_argument_errors(gblib, F):
+    """interface/gemm.c with COMPLEX: R and C are the conjugate op codes; the
+    real GEMM's positions under the names ZGEMM, CGEMM, ZGEMM3M, CGEMM3M."""
+    buf = np.zeros((64, 64), np.complex128, order="F")
+    bufs = np.zeros((64, 64), np.complex64, order="F")
+    cases = [(("X", "N", 4, 4, 4, 4, 4, 4), 1), (("N", "X", 4, 4, 4, 4, 4, 4), 2),
+             (("N", "N", -1, 4, 4, 4, 4, 4), 3), (("N", "N", 4, -1, 4, 4, 4, 4), 4),
+             (("N", "N", 4, 4, -1, 4, 4, 4), 5), (("C", "N", 4, 4, 5, 4, 5, 4), 8),
+             (("R", "N", 4, 4, 4, 3, 4, 4), 8), (("N", "C", 4, 5, 4, 4, 4, 4), 10),
+             (("N", "R", 4, 4, 5, 4, 4, 4), 10), (("N", "N", 4, 4, 4, 4, 4, 3), 13)]
+    for fn, name, b in (("zgemm", "ZGEMM ", buf), ("cgemm", "CGEMM ", bufs),
+                        ("zgemm3m", "ZGEMM3M ", buf), ("cgemm3m", "CGEMM3M ", bufs)):
+        for args, pos in cases:
+            ta, tb, m, n, k, lda, ldb, ldc = args
+            gblib.gb_clear_error()
+            getattr(F, fn)(ta, tb, m, n, k, 1.0, b, lda, b, ldb, 0.0, b, ldc)
+            assert _xerbla(gblib) == (name, pos), (fn, args)
+    # CBLAS: ConjNoTrans/ConjTrans are accepted; row-major swaps the operands
+    ns = gb.cblas()
+    one = np.array([1.0, 0.0])
+    gblib.gb_clear_error()
+    ns.cblas_zgemm(101, 114, 113, 4, 4, 4, one.ctypes.data, buf.ctypes.data, 3,
+                   buf.ctypes.data, 4, one.ctypes.data, buf.ctypes.data, 4)
+    assert _xerbla(gblib) == ("ZGEMM ", 10)  # row-major A (lda 3 < k) is the swapped B
+    ns.cblas_zgemm(102, 111, 115, 4, 4, 4, one.ctypes.data, buf.ctypes.data, 4,
+                   buf.ctypes.data, 4, one.ctypes.data, buf.ctypes.data, 4)
+    assert _xerbla(gblib) == ("ZGEMM ", 2)
+
+
 def test_dsposv_dpotrs_argument_errors(gblib, F):
     buf = np.zeros((64, 64), order="F")
     w = np.zeros(64 * 64)

@@ -297,3 +297,23 @@ def test_dgemmt_cases(golden, orc):
                         assert np.max(np.abs(Cm - ref)) <= 4 * (k + 2) * EPS * max(1, np.abs(ref).max())
                         assert np.array_equal(_tri_other(uplo, Cm), _tri_other(uplo, C0))
                         idx += 1
+
+
+@pytest.mark.parametrize("name,dt", GG.ZGEMM_ROUTINES)
+def test_complex_gemm_cases(golden, orc, name, dt):
+    """ZGEMM/CGEMM (componentwise bound) and the 3M forms (normwise bound)
+    for every op pair N/T/R/C, alpha/beta edge values and beta = 0 over NaN."""
+    from conftest import zgemm_ratio
+    eps = float(np.finfo(np.float32 if dt == np.complex64 else np.float64).eps)
+    for idx, (m, n, k, ta, tb, al, be) in enumerate(GG.zgemm_cases()):
+        A, B, Cm = GG.complex_operands(idx, m, n, k, ta, tb, dt)
+        C0 = Cm.copy(order="F")
+        if be == 0:
+            Cm[:m, :n] = np.nan
+        getattr(orc, name)(ta, tb, m, n, k, al, A, A.shape[0], B, B.shape[0], be, Cm,
+                           Cm.shape[0])
+        ref = golden[f"{name}_{idx}"]
+        r = zgemm_ratio(Cm, ref, A, B, C0, m, n, k, ta, tb, al, be, eps,
+                        normwise=name.endswith("3m"))
+        assert r <= 4 * (k + 2), (name, idx, m, n, k, ta, tb, r)
+        assert np.array_equal(Cm[m:], C0[m:])  # padding rows untouched
