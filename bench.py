@@ -362,6 +362,64 @@ def run_suite(args):
                 del Cn, Ga
             torch.cuda.empty_cache()
 
+    # ---- complex GEMM 8192^3 NN: ZGEMM (4M embedding) native and emulated,
+    # ZGEMM3M emulated, CGEMM / CGEMM3M on the tensor-core FP32 engine;
+    # rates count 8 n^3 real flops per complex GEMM (3M forms: effective rate)
+    n = 8192
+    one = np.array([1.0, 0.0])
+    zero = np.array([0.0, 0.0])
+    Az = torch.complex(urand((n, n), 80), urand((n, n), 81))
+    Bz = torch.complex(urand((n, n), 82), urand((n, n), 83))
+    Cn = torch.empty_like(Az)
+    Ce = torch.empty_like(Az)
+
+    def zcall(fn, Cout):
+        return lambda: check(getattr(lib, fn)(b"N", b"N", n, n, n, one.ctypes.data, Az.data_ptr(),
+                                              n, Bz.data_ptr(), n, zero.ctypes.data,
+                                              Cout.data_ptr(), n))
+    zres = {}
+    lib.gb_set_dgemm_mode(0)
+    zres["zgemm_native"] = _time_dev(torch, stream, zcall("gb_zgemm_dev", Cn), reps=1, warm=0)
+    lib.gb_set_dgemm_mode(1)
+    # error scale: max of |A||B| (complex moduli), the DMMCH denominator
+    Am, Bm = Az.abs().contiguous(), Bz.abs().contiguous()
+    Gz = torch.empty((n, n), dtype=torch.float64, device="cuda")
+    check(lib.gb_dgemm_native_dev(b"N", b"N", n, n, n, 1.0, Am.data_ptr(), n, Bm.data_ptr(), n,
+                                  0.0, Gz.data_ptr(), n))
+    torch.cuda.synchronize()
+    gmax = float(Gz.max())
+    del Am, Bm, Gz
+    zres["zgemm_emulated"] = _time_dev(torch, stream, zcall("gb_zgemm_dev", Ce), reps=3)
+    torch.cuda.synchronize()
+    zerr = float((Ce - Cn).abs().max()) / gmax / eps
+    zres["zgemm3m_emulated"] = _time_dev(torch, stream, zcall("gb_zgemm3m_dev", Ce), reps=3)
+    torch.cuda.synchronize()
+    z3err = float((Ce - Cn).abs().max()) / gmax / eps
+    lib.gb_set_dgemm_mode(0)
+    for key, err in (("zgemm_native", None), ("zgemm_emulated", zerr), ("zgemm3m_emulated", z3err)):
+        d = {"suite": f"{key}_{n}", "workload": f"{key.split('_')[0].upper()} NN {n}^3 complex128, "
+             f"{key.split('_')[1]} FP64 engine", "value": 8 * n ** 3 / zres[key] / 1e9,
+             "unit": UNIT, "ms": zres[key], "flops_counted": "8 n^3"}
+        if err is not None:
+            d["normwise_err_vs_native_zgemm_eps_of_max_AB"] = err
+            d["speedup_over_native_zgemm"] = zres["zgemm_native"] / zres[key]
+        _emit(d)
+    del Az, Bz, Cn, Ce
+    Ac = torch.complex(urand((n, n), 84, torch.float32), urand((n, n), 85, torch.float32))
+    Bc = torch.complex(urand((n, n), 86, torch.float32), urand((n, n), 87, torch.float32))
+    Cc = torch.empty_like(Ac)
+    onef, zerof = one.astype(np.float32), zero.astype(np.float32)
+    for fn in ("gb_cgemm_dev", "gb_cgemm3m_dev"):
+        ms = _time_dev(torch, stream, lambda: check(getattr(lib, fn)(
+            b"N", b"N", n, n, n, onef.ctypes.data, Ac.data_ptr(), n, Bc.data_ptr(), n,
+            zerof.ctypes.data, Cc.data_ptr(), n)), reps=3)
+        name = fn[3:-4]
+        _emit({"suite": f"{name}_{n}", "workload": f"{name.upper()} NN {n}^3 complex64, "
+               "bf16x3 tensor-core FP32 engine", "value": 8 * n ** 3 / ms / 1e9, "unit": UNIT,
+               "ms": ms, "flops_counted": "8 n^3"})
+    del Ac, Bc, Cc
+    torch.cuda.empty_cache()
+
     # ---- DGESV N in {8192, 16384, 32768}, NRHS in {1, 64}: mixed vs native
     for n in (8192, 16384, 32768):
         A = urand((n, n), 80 + n)
