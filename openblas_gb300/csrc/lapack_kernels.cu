@@ -1171,6 +1171,7 @@ int lu_panel(LuCtx<T> &c, int64_t r0, int64_t m, int n) {
   ProfileScope prof("lu_panel", c.s);
   T *P = c.A + r0 + r0 * c.lda;
   if (c.use_cluster) {
+    ProfileScope pc("lu_panel_cluster", c.s);
     const int st = launch_cluster_panel<T>(m, n, P, c.lda, c.ipiv + r0, r0, c.info, c.s);
     if (st != 1) return st;
   }
@@ -1240,7 +1241,7 @@ int lu_blocked(LuCtx<T> &c, int64_t m, int64_t mn, int64_t n) {
     if (j0 + jb < n) {
       T *A12 = c.A + j0 + (j0 + jb) * lda;
       {
-        ProfileScope prof("lu_laswp", c.s);
+        ProfileScope prof("lu_laswp_right", c.s);
         if ((st = laswp_device_rows<T>(n - j0 - jb, c.A + (j0 + jb) * lda, lda, j0 + 1, j0 + jb,
                                        c.ipiv, 1, c.rows, c.s)))
           return st;
@@ -1256,7 +1257,7 @@ int lu_blocked(LuCtx<T> &c, int64_t m, int64_t mn, int64_t n) {
       }
     }
     if (j0 > 0) {
-      ProfileScope prof("lu_laswp", c.s);
+      ProfileScope prof("lu_laswp_left", c.s);
       if ((st = laswp_device_rows<T>(j0, c.A, lda, j0 + 1, j0 + jb, c.ipiv, 1, c.rows, c.s)))
         return st;
     }
