@@ -106,7 +106,7 @@ def test_dgetrf_tiny_pivot_rule(orc, F, gb_clean):
 @pytest.mark.parametrize("m,n,where", [
     (300, 300, "column"),   # column 5 all NaN: every later pivot search sees NaN at row j
     (300, 300, "entry"),    # one NaN below the diagonal: skipped, then met at its own step
-    (9000, 40, "entry"),    # taller than one cluster: grid-wide panel kernel
+    (12000, 40, "entry"),   # taller than one FP64 cluster (8192 rows): grid-wide panel kernel
 ])
 def test_dgetrf_nan_pivot_rule(orc, F, gb_clean, m, n, where):
     """IAMAX order with NaN (getf2_k.c pivot search): the running maximum starts
@@ -316,3 +316,38 @@ def _apply_piv(A, piv):
         if p - 1 != i:
             P[[i, p - 1], :] = P[[p - 1, i], :]
     return P
+
+
+@pytest.mark.parametrize("m,n", [(8192, 40), (12000, 40), (16384, 96)])
+def test_dgetrf_tall_panels(orc, F, gb_clean, m, n):
+    """FP64 panels at the edge of the cluster kernel (8192 rows: one row per
+    thread of a 16-CTA cluster) and past it (the grid-wide kernel); pivots
+    identical to the oracle."""
+    A0 = W.uniform(8100 + m + n, (m, n))
+    A, Ao = A0.copy(order="F"), A0.copy(order="F")
+    p, po = np.zeros(n, np.int32), np.zeros(n, np.int32)
+    assert F.dgetrf(m, n, A, m, p) == orc.dgetrf(m, n, Ao, m, po) == 0
+    assert np.array_equal(p, po)
+    assert np.max(np.abs(A - Ao)) <= 1e-9 * np.abs(Ao).max()
+
+
+@pytest.mark.parametrize("m,n", [(16384, 40), (20000, 64), (30000, 40)])
+def test_sgetrf_tall_panels(orc, gblib, gb_clean, m, n):
+    """FP32 panels of the mixed solver's LU at the edge of the cluster kernel
+    (16384 rows: two register rows per thread) and past it (the grid-wide
+    kernel).  Pivots match the oracle's sgetrf (or, on an FP32 near-tie, the
+    factorisation has an FP32-level residual)."""
+    A0 = np.asfortranarray(W.uniform(8200 + m + n, (m, n)).astype(np.float32))
+    LU, piv, info = _sgetrf_dev(gblib, A0)
+    Ao = A0.copy(order="F")
+    po = np.zeros(n, np.int32)
+    assert info == orc.sgetrf(m, n, Ao, m, po) == 0
+    assert piv.min() >= 1 and piv.max() <= m
+    if np.array_equal(piv, po):
+        assert np.abs(LU - Ao).max() <= 1e-4 * np.abs(Ao).max()
+    feps = float(np.finfo(np.float32).eps)
+    L = np.tril(LU.astype(np.float64), -1)[:, :n] + np.eye(m, n)
+    U = np.triu(LU.astype(np.float64)[:n, :])
+    PA = _apply_piv(A0, piv)
+    r = np.abs(PA - L @ U).sum(axis=0).max() / (n * feps * np.abs(A0).sum(axis=0).max())
+    assert r <= 10, r
