@@ -902,66 +902,6 @@ int lu_trsm(int64_t n1, int64_t w, const T *L, int64_t ldl, T *B, int64_t ldb, c
   return check_cuda(cudaGetLastError(), "lu_trsm");
 }
 
-// Parallel form of a long interchange sequence (incx = 1): one block replays
-// the interchanges on an index vector in shared memory, giving the final
-// permutation of the touched rows, and the moved rows are then gathered and
-// scattered by all SMs.  The per-column sequential kernel above costs one
-// memory round trip per interchange; this form costs one for the whole
-// sequence.  rows = number of rows of the matrix (pivots are < rows).
-__global__ void __launch_bounds__(1024)
-laswp_plan_kernel(int64_t k1, int64_t k2, const int *__restrict__ ipiv, int64_t range,
-                  int *__restrict__ dst, int *__restrict__ src, int *__restrict__ count) {
-  extern __shared__ int pos[];
-  for (int64_t p = threadIdx.x; p < range; p += blockDim.x) pos[p] = (int)p;
-  if (threadIdx.x == 0) *count = 0;
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    const int64_t base = k1 - 1;
-    for (int64_t i = k1 - 1; i < k2; ++i) {
-      const int64_t li = i - base, lp = (int64_t)ipiv[i] - 1 - base;
-      if (lp != li) {
-        const int t = pos[li];
-        pos[li] = pos[lp];
-        pos[lp] = t;
-      }
-    }
-  }
-  __syncthreads();
-  for (int64_t p = threadIdx.x; p < range; p += blockDim.x) {
-    if (pos[p] != (int)p) {
-      const int slot = atomicAdd(count, 1);
-      dst[slot] = (int)(p + k1 - 1);
-      src[slot] = pos[p] + (int)(k1 - 1);
-    }
-  }
-}
-
-template <typename T>
-__global__ void laswp_gather_kernel(int64_t ncols, const T *__restrict__ A, int64_t lda,
-                                    const int *__restrict__ src, const int *__restrict__ count,
-                                    int64_t cap, T *__restrict__ tmp) {
-  const int64_t nm = *count;
-  const int64_t total = nm * ncols;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t c = e / nm, t = e - c * nm;
-    tmp[t + c * cap] = A[src[t] + c * lda];
-  }
-}
-
-template <typename T>
-__global__ void laswp_scatter_kernel(int64_t ncols, T *__restrict__ A, int64_t lda,
-                                     const int *__restrict__ dst, const int *__restrict__ count,
-                                     int64_t cap, const T *__restrict__ tmp) {
-  const int64_t nm = *count;
-  const int64_t total = nm * ncols;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t c = e / nm, t = e - c * nm;
-    A[dst[t] + c * lda] = tmp[t + c * cap];
-  }
-}
-
 // Interchange sequences of up to LASWP_FUSED_MAX steps in one launch, any
 // incx.  Every CTA replays the sequence on slot indices in shared memory
 // (slot s < cnt is row k1-1+s of the window; slot cnt+t stands for the pivot
@@ -977,7 +917,8 @@ constexpr int LASWP_FUSED_ELEMS = 4096;
 template <typename T>
 __global__ void __launch_bounds__(256)
 laswp_fused_kernel(int64_t n, T *__restrict__ A, int64_t lda, int64_t k1, int64_t k2,
-                   const int *__restrict__ ipiv, int64_t incx, int cols_per_cta) {
+                   const int *__restrict__ ipiv, int64_t incx, int cols_per_cta, int64_t skip0,
+                   int64_t skipw) {
   __shared__ int prow[LASWP_FUSED_MAX];
   __shared__ int slotp[LASWP_FUSED_MAX];
   __shared__ int pos[2 * LASWP_FUSED_MAX];
@@ -1033,6 +974,8 @@ laswp_fused_kernel(int64_t n, T *__restrict__ A, int64_t lda, int64_t k1, int64_
   const int nm = nmoved;
   if (nm == 0) return;
   auto row_of = [&](int sl) -> int64_t { return sl < cnt ? w0 + sl : (int64_t)prow[sl - cnt]; };
+  // the n columns visited are the matrix's columns with [skip0, skip0 + skipw) left out
+  auto col_of = [&](int64_t c) -> int64_t { return c < skip0 ? c : c + skipw; };
   // the plan is reused for every column chunk this CTA visits; within a
   // chunk each thread keeps 8 loads in flight before it stores to shared
   const int64_t nchunks = (n + cols_per_cta - 1) / cols_per_cta;
@@ -1047,7 +990,7 @@ laswp_fused_kernel(int64_t n, T *__restrict__ A, int64_t lda, int64_t k1, int64_
         const int e = e0 + u * 256;
         if (e < total) {
           const int c = e / nm, q = e - c * nm;
-          v[u] = A[row_of(pos[moved[q]]) + (c0 + c) * lda];
+          v[u] = A[row_of(pos[moved[q]]) + col_of(c0 + c) * lda];
         }
       }
 #pragma unroll
@@ -1057,7 +1000,7 @@ laswp_fused_kernel(int64_t n, T *__restrict__ A, int64_t lda, int64_t k1, int64_
     __syncthreads();
     for (int e = tid; e < total; e += 256) {
       const int c = e / nm, q = e - c * nm;
-      A[row_of(moved[q]) + (c0 + c) * lda] = vals[e];
+      A[row_of(moved[q]) + col_of(c0 + c) * lda] = vals[e];
     }
     __syncthreads();
   }
@@ -1065,55 +1008,17 @@ laswp_fused_kernel(int64_t n, T *__restrict__ A, int64_t lda, int64_t k1, int64_
 
 template <typename T>
 int launch_laswp_fused(int64_t n, T *A, int64_t lda, int64_t k1, int64_t k2, const int *ipiv,
-                       int64_t incx, cudaStream_t s) {
+                       int64_t incx, cudaStream_t s, int64_t skip0 = INT64_MAX,
+                       int64_t skipw = 0) {
   const int64_t cnt = k2 - k1 + 1;
   int cols = (int)(LASWP_FUSED_ELEMS / (2 * cnt));
   if (cols < 1) cols = 1;
   int64_t grid = (n + cols - 1) / cols;
   const int64_t cap = (int64_t)sm_count() * 2;
   if (grid > cap) grid = cap;
-  { laswp_fused_kernel<T><<<(unsigned)grid, 256, 0, s>>>(n, A, lda, k1, k2, ipiv, incx, cols); count_launch(); }
+  { laswp_fused_kernel<T><<<(unsigned)grid, 256, 0, s>>>(n, A, lda, k1, k2, ipiv, incx, cols,
+                                                         skip0, skipw); count_launch(); }
   return check_cuda(cudaGetLastError(), "laswp launch");
-}
-
-constexpr int64_t LASWP_SEQ_MAX = 64;          // short sequences: per-column kernel
-constexpr int64_t LASWP_PLAN_SMEM_ROWS = 50000;  // index vector must fit in shared memory
-
-template <typename T>
-int laswp_device_rows(int64_t n, T *A, int64_t lda, int64_t k1, int64_t k2, const int *ipiv,
-                      int64_t incx, int64_t rows, cudaStream_t s) {
-  if (n <= 0 || incx == 0 || k2 < k1) return GB_SUCCESS;
-  const int64_t cnt = k2 - k1 + 1;
-  if (cnt <= LASWP_FUSED_MAX) return launch_laswp_fused<T>(n, A, lda, k1, k2, ipiv, incx, s);
-  const int64_t range = rows - (k1 - 1);
-  if (incx != 1 || cnt <= LASWP_SEQ_MAX || rows <= 0 || range > LASWP_PLAN_SMEM_ROWS ||
-      n < 4) {
-    { laswp_kernel<T><<<(unsigned)((n + 127) / 128), 128, 0, s>>>(n, A, lda, k1, k2, ipiv, incx); count_launch(); }
-    return check_cuda(cudaGetLastError(), "laswp launch");
-  }
-  const int64_t cap = 2 * cnt < range ? 2 * cnt : range;  // at most 2 rows move per interchange
-  Scratch ws((size_t)(2 * cap + 32) * sizeof(int) + (size_t)cap * n * sizeof(T) + 512, s);
-  if (!ws.p) return GB_ERR_ALLOC;
-  int *dst = ws.as<int>();
-  int *src = dst + cap;
-  int *count = src + cap;
-  T *tmp = reinterpret_cast<T *>(reinterpret_cast<char *>(ws.p) +
-                                 (((2 * cap + 32) * sizeof(int) + 255) & ~size_t(255)));
-  const size_t smem = (size_t)range * sizeof(int);
-  static bool attr = false;
-  if (!attr) {
-    cudaFuncSetAttribute(laswp_plan_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(LASWP_PLAN_SMEM_ROWS * sizeof(int)));
-    attr = true;
-  }
-  { laswp_plan_kernel<<<1, 1024, smem, s>>>(k1, k2, ipiv, range, dst, src, count); count_launch(); }
-  const int64_t total = cap * n;
-  int64_t blocks = (total + 255) / 256;
-  const int64_t lim = (int64_t)sm_count() * 16;
-  const unsigned g = (unsigned)(blocks < lim ? blocks : lim);
-  { laswp_gather_kernel<T><<<g, 256, 0, s>>>(n, A, lda, src, count, cap, tmp); count_launch(); }
-  { laswp_scatter_kernel<T><<<g, 256, 0, s>>>(n, A, lda, dst, count, cap, tmp); count_launch(); }
-  return check_cuda(cudaGetLastError(), "laswp (planned)");
 }
 
 template <typename T>
@@ -1126,11 +1031,12 @@ int laswp_device(int64_t n, T *A, int64_t lda, int64_t k1, int64_t k2, const int
 }
 
 // Recursive LU (lapack/getrf/getrf_single.c:47-180 splits the columns in
-// halves in the same way): factor the left half, apply its interchanges to
-// the right half, solve for U12 with the unit-lower L11, update A22 with one
-// GEMM of rank n1, factor A22 recursively and apply its interchanges back to
-// the left half.  Leaves of PANEL_NB columns go to the cooperative panel
-// kernel.  Compared with a flat right-looking sweep, every trailing element
+// halves in the same way): factor the left half, solve for U12 with the
+// unit-lower L11, update A22 with one GEMM of rank n1 and factor A22
+// recursively.  Leaves of PANEL_NB columns go to the panel kernels, and each
+// leaf's interchanges are applied to all other columns right after it (see
+// lu_panel), which puts every row where the reference's per-level LASWP
+// calls put it.  Compared with a flat right-looking sweep, every trailing element
 // is rounded O(log n) instead of O(n / PANEL_NB) times and the GEMMs are
 // large, which matters most for the FP32 factorisation of the mixed solver.
 template <typename T>
@@ -1144,7 +1050,8 @@ struct LuCtx {
   int *status;
   int lim1, lim2;
   int gemm_mode;  // double only: 0 native FP64 updates, 1 emulated-FP64 updates
-  int64_t rows;   // rows of the whole matrix (interchange targets are below it)
+  int64_t nrows, ncols;          // the whole matrix
+  int64_t blk0 = 0, blk1 = 0;    // columns a panel's interchanges reach (see lu_panel)
   bool use_cluster = true;  // panel on one thread-block cluster when it fits
   cudaStream_t s;
 };
@@ -1167,7 +1074,7 @@ int lu_update<float>(LuCtx<float> &c, int64_t m, int64_t n, int64_t k, const flo
 }
 
 template <typename T>
-int lu_panel(LuCtx<T> &c, int64_t r0, int64_t m, int n) {
+int lu_panel_factor(LuCtx<T> &c, int64_t r0, int64_t m, int n) {
   ProfileScope prof("lu_panel", c.s);
   T *P = c.A + r0 + r0 * c.lda;
   if (c.use_cluster) {
@@ -1188,6 +1095,32 @@ int lu_panel(LuCtx<T> &c, int64_t r0, int64_t m, int n) {
                    (long long)m);
 }
 
+// Factor the leaf panel (columns r0 .. r0+n-1, rows r0 ..) and apply its row
+// interchanges to the other columns of the outer block at once.  The
+// reference's recursion applies them level by level -- to the right half
+// before its TRSM, and to the left half after the right half is factored
+// (getrf_single.c's recursive call) -- but between the panel and each of
+// those points nothing reads or writes rows >= r0 of the columns concerned,
+// so applying them earlier leaves every value where the reference puts it:
+// one launch per panel instead of two per recursion level.  The same holds
+// for the columns outside the outer block (the reference's LASWP before the
+// block's TRSM and on the finished columns to the left), so for a matrix
+// small enough that streaming all of it per panel stays cheap, the panel's
+// interchanges reach every column; for larger ones they reach the outer
+// block only and lu_blocked applies the block's interchanges to the other
+// columns in two wide passes, which keeps the panel's data in L2.
+template <typename T>
+int lu_panel(LuCtx<T> &c, int64_t r0, int64_t m, int n) {
+  int st = lu_panel_factor<T>(c, r0, m, n);
+  if (st) return st;
+  const int64_t npiv = m < n ? m : n;
+  const int64_t width = c.blk1 - c.blk0;
+  if (width <= n || npiv <= 0) return GB_SUCCESS;
+  ProfileScope prof("lu_laswp", c.s);
+  return launch_laswp_fused<T>(width - n, c.A + c.blk0 * c.lda, c.lda, r0 + 1, r0 + npiv, c.ipiv,
+                               1, c.s, r0 - c.blk0, n);
+}
+
 // Factor the m x n block whose top-left corner is the diagonal entry (r0, r0); n <= m.
 template <typename T>
 int lu_rec(LuCtx<T> &c, int64_t r0, int64_t m, int64_t n) {
@@ -1196,15 +1129,10 @@ int lu_rec(LuCtx<T> &c, int64_t r0, int64_t m, int64_t n) {
   if (n1 < PANEL_NB) n1 = PANEL_NB;
   const int64_t lda = c.lda;
   int st;
+  // the left half's interchanges reach the right half inside lu_panel
   if ((st = lu_rec<T>(c, r0, m, n1))) return st;
   T *L11 = c.A + r0 + r0 * lda;
   T *A12 = c.A + r0 + (r0 + n1) * lda;
-  {
-    ProfileScope prof("lu_laswp", c.s);
-    if ((st = laswp_device_rows<T>(n - n1, c.A + (r0 + n1) * lda, lda, r0 + 1, r0 + n1, c.ipiv,
-                                   1, c.rows, c.s)))
-      return st;
-  }
   {
     ProfileScope prof("lu_trsm", c.s);
     if ((st = lu_trsm<T>(n1, n - n1, L11, lda, A12, lda, c.s))) return st;
@@ -1215,11 +1143,6 @@ int lu_rec(LuCtx<T> &c, int64_t r0, int64_t m, int64_t n) {
       if ((st = lu_update<T>(c, m - n1, n - n1, n1, L11 + n1, A12, A12 + n1))) return st;
     }
     if ((st = lu_rec<T>(c, r0 + n1, m - n1, n - n1))) return st;
-    const int64_t kend = r0 + (m < n ? m : n);
-    ProfileScope prof("lu_laswp", c.s);
-    if ((st = laswp_device_rows<T>(n1, c.A + r0 * lda, lda, r0 + n1 + 1, kend, c.ipiv, 1, c.rows,
-                                   c.s)))
-      return st;
   }
   return GB_SUCCESS;
 }
@@ -1229,23 +1152,37 @@ int lu_rec(LuCtx<T> &c, int64_t r0, int64_t m, int64_t n) {
 // min(mn/2, GEMM_Q), recursive call on the panel, LASWP + TRSM + GEMM on the
 // trailing columns, later interchanges applied to the columns on the left).
 constexpr int64_t LU_OUTER_NB = 256;
+static_assert(LU_OUTER_NB <= LASWP_FUSED_MAX, "a block's interchanges fit one fused LASWP");
 
 template <typename T>
 int lu_blocked(LuCtx<T> &c, int64_t m, int64_t mn, int64_t n) {
   const int64_t lda = c.lda;
   int st;
+  // measured on GB300 (FP32 LU): per-panel interchanges over the whole
+  // width win at 8192^2 (268 MB), lose from 16384^2 (1 GB) on
+  const bool whole = (double)c.nrows * (double)c.ncols * sizeof(T) <= 512.0 * 1024 * 1024;
   for (int64_t j0 = 0; j0 < mn; j0 += LU_OUTER_NB) {
     const int64_t jb = (mn - j0) < LU_OUTER_NB ? (mn - j0) : LU_OUTER_NB;
+    c.blk0 = whole ? 0 : j0;
+    c.blk1 = whole ? c.ncols : j0 + jb;
     if ((st = lu_rec<T>(c, j0, m - j0, jb))) return st;
+    // the block's interchanges (at most LU_OUTER_NB <= LASWP_FUSED_MAX) on the
+    // trailing columns, then on the finished columns to the left
+    const int64_t npiv = (m - j0) < jb ? (m - j0) : jb;
+    if (!whole && j0 + jb < n) {
+      ProfileScope prof("lu_laswp_right", c.s);
+      if ((st = launch_laswp_fused<T>(n - j0 - jb, c.A + (j0 + jb) * lda, lda, j0 + 1,
+                                      j0 + npiv, c.ipiv, 1, c.s)))
+        return st;
+    }
+    if (!whole && j0 > 0) {
+      ProfileScope prof("lu_laswp_left", c.s);
+      if ((st = launch_laswp_fused<T>(j0, c.A, lda, j0 + 1, j0 + npiv, c.ipiv, 1, c.s)))
+        return st;
+    }
     T *L11 = c.A + j0 + j0 * lda;
     if (j0 + jb < n) {
       T *A12 = c.A + j0 + (j0 + jb) * lda;
-      {
-        ProfileScope prof("lu_laswp_right", c.s);
-        if ((st = laswp_device_rows<T>(n - j0 - jb, c.A + (j0 + jb) * lda, lda, j0 + 1, j0 + jb,
-                                       c.ipiv, 1, c.rows, c.s)))
-          return st;
-      }
       {
         ProfileScope prof("lu_trsm", c.s);
         if ((st = lu_trsm<T>(jb, n - j0 - jb, L11, lda, A12, lda, c.s))) return st;
@@ -1255,11 +1192,6 @@ int lu_blocked(LuCtx<T> &c, int64_t m, int64_t mn, int64_t n) {
         if ((st = lu_update<T>(c, m - j0 - jb, n - j0 - jb, jb, L11 + jb, A12, A12 + jb)))
           return st;
       }
-    }
-    if (j0 > 0) {
-      ProfileScope prof("lu_laswp_left", c.s);
-      if ((st = laswp_device_rows<T>(j0, c.A, lda, j0 + 1, j0 + jb, c.ipiv, 1, c.rows, c.s)))
-        return st;
     }
   }
   return GB_SUCCESS;
@@ -1287,7 +1219,8 @@ int getrf_device_mode(int64_t m, int64_t n, T *A, int64_t lda, int *ipiv, int *i
                                        ((slot_elems * sizeof(T) + 127) & ~size_t(127)));
   c.status = ctx().d_status;
   c.gemm_mode = gemm_mode;
-  c.rows = m;
+  c.nrows = m;
+  c.ncols = n;
   c.s = s;
   // the outer loop already covers the columns right of the square part
   int st = lu_blocked<T>(c, m, mn, n);
@@ -1392,7 +1325,8 @@ extern "C" int gb_dgetrf_noalloc_dev(int64_t m, int64_t n, double *A, int64_t ld
   c.bar = reinterpret_cast<unsigned *>(b + ((NOALLOC_SLOT_BYTES + 127) & ~size_t(127)));
   c.status = reinterpret_cast<int *>(c.bar + 32);
   c.gemm_mode = 0;  // native FP64 trailing updates: no scratch anywhere below
-  c.rows = 0;       // 0 selects the per-column interchange kernel, which needs no scratch
+  c.nrows = m;      // the panels' interchanges use the fused kernel: no scratch either
+  c.ncols = n;
   c.s = s;
   // the shared array keeps the previous call's contents: clear the words that
   // must start at zero (barrier counters are cleared again before every panel)
