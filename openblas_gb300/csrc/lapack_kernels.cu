@@ -1469,18 +1469,25 @@ int potrf_device_t(int uplo, int64_t n, T *A, int64_t lda, int *info, int gemm_m
   for (int64_t j0 = 0; j0 < n; j0 += POTRF_NB) {
     const int64_t jb = (n - j0) < POTRF_NB ? (n - j0) : POTRF_NB;
     T *D = A + j0 + j0 * lda;
-    int st = potrf_diag_block<T>(upper, jb, D, lda, info, j0, s);
-    if (st) return st;
+    int st;
+    {
+      ProfileScope prof("potrf_diag", s);
+      if ((st = potrf_diag_block<T>(upper, jb, D, lda, info, j0, s))) return st;
+    }
     const int64_t rest = n - j0 - jb;
     if (rest <= 0) continue;
-    if (!upper) {
-      T *P = A + (j0 + jb) + j0 * lda;  // rest x jb
-      if ((st = trsm_skip<T>(1, 1, 1, 1, rest, jb, D, lda, P, lda, s, info))) return st;
-      st = potrf_trailing(false, rest, jb, P, lda, P + jb * lda, info, gemm_mode, s);
-    } else {
-      T *P = A + j0 + (j0 + jb) * lda;  // jb x rest
-      if ((st = trsm_skip<T>(0, 0, 1, 1, jb, rest, D, lda, P, lda, s, info))) return st;
-      st = potrf_trailing(true, rest, jb, P, lda, P + jb, info, gemm_mode, s);
+    T *P = upper ? A + j0 + (j0 + jb) * lda   // jb x rest
+                 : A + (j0 + jb) + j0 * lda;  // rest x jb
+    {
+      ProfileScope prof("potrf_trsm", s);
+      st = upper ? trsm_skip<T>(0, 0, 1, 1, jb, rest, D, lda, P, lda, s, info)
+                 : trsm_skip<T>(1, 1, 1, 1, rest, jb, D, lda, P, lda, s, info);
+      if (st) return st;
+    }
+    {
+      ProfileScope prof("potrf_update", s);
+      st = upper ? potrf_trailing(true, rest, jb, P, lda, P + jb, info, gemm_mode, s)
+                 : potrf_trailing(false, rest, jb, P, lda, P + jb * lda, info, gemm_mode, s);
     }
     if (st) return st;
   }
