@@ -150,6 +150,47 @@ def test_sgemm_tensor_cores(F, gb_clean, sgemm_tensor, ta, tb):
     assert np.array_equal(Cm[m:], C0[m:])          # padding rows untouched
 
 
+@pytest.mark.parametrize("alpha,beta,shape", [
+    (-1.0, 1.0, (5000, 2900, 256)),   # the LU trailing update C - A B; 40 x 12 tiles, 3+ per CTA
+    (0.5, 0.5, (1100, 1300, 333)),
+    (2.0, -2.0, (4100, 1030, 200)),   # 33 x 5 tiles with ragged edges
+])
+def test_sgemm_tensor_many_tiles(F, gb_clean, sgemm_tensor, alpha, beta, shape):
+    """More tiles than SMs (each persistent CTA cycles both TMEM accumulators
+    several times), ragged edges, beta = +-alpha as in the LU update: every
+    tile and the padding rows come out within the FP32 GEMM bound."""
+    m, n, k = shape
+    A, B, Cm = W.gemm_operands(81, m, n, k, "N", "N", pad=3, dtype=np.float32)
+    C0 = Cm.copy(order="F")
+    F.sgemm("N", "N", m, n, k, alpha, A, A.shape[0], B, B.shape[0], beta, Cm, Cm.shape[0])
+    ref, G = _sgemm_ref("N", "N", alpha, A, B, beta, C0, m, n, k)
+    feps = np.finfo(np.float32).eps
+    assert np.max(np.abs(Cm[:m, :n] - ref) / (feps * G)) <= k + 2
+    assert np.array_equal(Cm[m:], C0[m:])
+
+
+def test_sgemm_tensor_update_specials(F, gb_clean, sgemm_tensor):
+    """The LU-style update C - A B: rows and columns holding Inf/NaN go to the
+    FP32 fixup, and an Inf already in C propagates."""
+    m, n, k = 1200, 1100, 96
+    A, B, Cm = W.gemm_operands(82, m, n, k, dtype=np.float32)
+    A[5, 3] = np.inf
+    B[7, 900] = np.nan
+    Cm[600, 20] = -np.inf
+    C0 = Cm.copy(order="F")
+    F.sgemm("N", "N", m, n, k, -1.0, A, m, B, k, 1.0, Cm, m)
+    with np.errstate(invalid="ignore"):
+        ref = C0.astype(np.float64) - A.astype(np.float64) @ B.astype(np.float64)
+    assert np.array_equal(np.isnan(Cm), np.isnan(ref))
+    assert np.array_equal(np.isposinf(Cm), np.isposinf(ref))
+    assert np.array_equal(np.isneginf(Cm), np.isneginf(ref))
+    fin = np.isfinite(ref)
+    G = np.abs(A.astype(np.float64)) @ np.abs(B.astype(np.float64)) + np.abs(C0)
+    feps = np.finfo(np.float32).eps
+    with np.errstate(invalid="ignore"):
+        assert np.max(np.abs(Cm[fin] - ref[fin]) / (feps * G[fin])) <= k + 2
+
+
 def test_sgemm_tensor_beta_zero_and_specials(F, gb_clean, sgemm_tensor):
     """beta = 0 overwrites C without reading it (NaN in C is not propagated);
     Inf in A propagates as in an FP32 product."""
