@@ -78,8 +78,9 @@ __device__ __forceinline__ bool tile_active(int mt, int nt) {
 }
 
 // TRI (0 all of C, 1 lower, 2 upper) is a template parameter so that the
-// full-C instance keeps the plain store loop of the epilogue.
-template <int TRI>
+// full-C instance keeps the plain store loop of the epilogue.  RC (full C
+// only): beta != 0, C is read -- ahead of its use, see the epilogue.
+template <int TRI, bool RC>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 sgemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tmA,
                     const __grid_constant__ CUtensorMap tmB, const Params p) {
@@ -268,49 +269,99 @@ sgemm_bf16x3_kernel(const __grid_constant__ CUtensorMap tmA,
       int mt, nt;
       tile_coords(tile, p, mt, nt);
       if (!tile_active<TRI>(mt, nt)) continue;
-      const bool got = mbar_wait(&tfull[acc], acc_phase, abort_flag, WAIT_LIMIT_NS);
-      // the warp-wide tcgen05.ld below needs a converged warp: agree first
-      if (!__all_sync(0xffffffffu, got)) {
-        if (lane == 0) fail(6);
-        break;
-      }
-      tc_fence_after();
-      const int64_t grow = (int64_t)mt * BM + row;
-      const int64_t col0 = (int64_t)nt * BN + half * 128;
-      const uint32_t taddr =
-          tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + half * 128);
-#pragma unroll 1
-      for (int c = 0; c < 4; ++c) {
-        uint32_t r[32];
-        tmem_ld_32x32b_x32(taddr + c * 32, r);
-        tmem_ld_wait();
-        // columns of this chunk that the fixup kernel owns (lane j reads column j)
-        const int64_t cj = col0 + c * 32 + lane;
-        const unsigned skip = __ballot_sync(0xffffffffu, cj < p.n && p.cflag[cj] != 0);
-        if (!skipped && grow < p.m && p.rflag[grow] == 0) {
-          float *cp = p.C + grow + (col0 + c * 32) * p.ldc;
+      if constexpr (TRI == 0) {
+        const int64_t grow = (int64_t)mt * BM + row;
+        const int64_t col0 = (int64_t)nt * BN + half * 128;
+        const bool row_ok = !skipped && grow < p.m && p.rflag[grow] == 0;
+        const bool load_c = RC && row_ok;
+        // C is requested ahead of its use: chunk 0 before the accumulator is
+        // ready (the loads overlap the MMAs), each later chunk while the one
+        // before it is drained -- the old values are not read between a
+        // finished accumulator and its stores
+        float nxt[32];
+        auto load_chunk = [&](int c) {
           const int64_t ncol = p.n - (col0 + c * 32);
+          const float *cp = p.C + grow + (col0 + c * 32) * p.ldc;
+#pragma unroll
+          for (int j = 0; j < 32; ++j) nxt[j] = (load_c && j < ncol) ? cp[j * p.ldc] : 0.f;
+        };
+        load_chunk(0);
+        const bool got = mbar_wait(&tfull[acc], acc_phase, abort_flag, WAIT_LIMIT_NS);
+        // the warp-wide tcgen05.ld below needs a converged warp: agree first
+        if (!__all_sync(0xffffffffu, got)) {
+          if (lane == 0) fail(6);
+          break;
+        }
+        tc_fence_after();
+        const uint32_t taddr =
+            tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + half * 128);
+#pragma unroll 1
+        for (int c = 0; c < 4; ++c) {
           float old[32];
 #pragma unroll
-          for (int j = 0; j < 32; ++j) old[j] = (read_c && j < ncol) ? cp[j * p.ldc] : 0.f;
-          if constexpr (TRI == 0) {
+          for (int j = 0; j < 32; ++j) old[j] = nxt[j];
+          if (c < 3) load_chunk(c + 1);
+          uint32_t r[32];
+          tmem_ld_32x32b_x32(taddr + c * 32, r);
+          tmem_ld_wait();
+          // columns of this chunk that the fixup kernel owns (lane j reads column j)
+          const int64_t cj = col0 + c * 32 + lane;
+          const unsigned skip = __ballot_sync(0xffffffffu, cj < p.n && p.cflag[cj] != 0);
+          if (row_ok) {
+            float *cp = p.C + grow + (col0 + c * 32) * p.ldc;
+            const int64_t ncol = p.n - (col0 + c * 32);
 #pragma unroll
             for (int j = 0; j < 32; ++j)
               if (j < ncol && !((skip >> j) & 1u))
-                cp[j * p.ldc] = p.alpha * __uint_as_float(r[j]) + p.beta * old[j];
-          } else {
-            // columns j of this chunk inside the triangle: one mask per row
-            uint32_t wmask = ncol >= 32 ? 0xffffffffu : (ncol <= 0 ? 0u : (1u << ncol) - 1u);
-            wmask &= ~skip;
-            const int64_t d = grow - (col0 + c * 32);  // row minus the chunk's first column
-            if (TRI == 1)  // keep col <= row: j <= d
-              wmask &= d < 0 ? 0u : (d >= 31 ? 0xffffffffu : (2u << d) - 1u);
-            else           // keep col >= row: j >= d
-              wmask &= d <= 0 ? 0xffffffffu : (d > 31 ? 0u : ~((1u << d) - 1u));
+                cp[j * p.ldc] = RC ? p.alpha * __uint_as_float(r[j]) + p.beta * old[j]
+                                   : p.alpha * __uint_as_float(r[j]);
+          }
+        }
+      } else {
+        const bool got = mbar_wait(&tfull[acc], acc_phase, abort_flag, WAIT_LIMIT_NS);
+        // the warp-wide tcgen05.ld below needs a converged warp: agree first
+        if (!__all_sync(0xffffffffu, got)) {
+          if (lane == 0) fail(6);
+          break;
+        }
+        tc_fence_after();
+        const int64_t grow = (int64_t)mt * BM + row;
+        const int64_t col0 = (int64_t)nt * BN + half * 128;
+        const uint32_t taddr =
+            tmem_base + ((uint32_t)(q * 32) << 16) + (uint32_t)(acc * BN + half * 128);
+#pragma unroll 1
+        for (int c = 0; c < 4; ++c) {
+          uint32_t r[32];
+          tmem_ld_32x32b_x32(taddr + c * 32, r);
+          tmem_ld_wait();
+          // columns of this chunk that the fixup kernel owns (lane j reads column j)
+          const int64_t cj = col0 + c * 32 + lane;
+          const unsigned skip = __ballot_sync(0xffffffffu, cj < p.n && p.cflag[cj] != 0);
+          if (!skipped && grow < p.m && p.rflag[grow] == 0) {
+            float *cp = p.C + grow + (col0 + c * 32) * p.ldc;
+            const int64_t ncol = p.n - (col0 + c * 32);
+            float old[32];
 #pragma unroll
-            for (int j = 0; j < 32; ++j)
-              if ((wmask >> j) & 1u)
-                cp[j * p.ldc] = p.alpha * __uint_as_float(r[j]) + p.beta * old[j];
+            for (int j = 0; j < 32; ++j) old[j] = (read_c && j < ncol) ? cp[j * p.ldc] : 0.f;
+            if constexpr (TRI == 0) {
+#pragma unroll
+              for (int j = 0; j < 32; ++j)
+                if (j < ncol && !((skip >> j) & 1u))
+                  cp[j * p.ldc] = p.alpha * __uint_as_float(r[j]) + p.beta * old[j];
+            } else {
+              // columns j of this chunk inside the triangle: one mask per row
+              uint32_t wmask = ncol >= 32 ? 0xffffffffu : (ncol <= 0 ? 0u : (1u << ncol) - 1u);
+              wmask &= ~skip;
+              const int64_t d = grow - (col0 + c * 32);  // row minus the chunk's first column
+              if (TRI == 1)  // keep col <= row: j <= d
+                wmask &= d < 0 ? 0u : (d >= 31 ? 0xffffffffu : (2u << d) - 1u);
+              else           // keep col >= row: j >= d
+                wmask &= d <= 0 ? 0xffffffffu : (d > 31 ? 0u : ~((1u << d) - 1u));
+#pragma unroll
+              for (int j = 0; j < 32; ++j)
+                if ((wmask >> j) & 1u)
+                  cp[j * p.ldc] = p.alpha * __uint_as_float(r[j]) + p.beta * old[j];
+            }
           }
         }
       }
@@ -475,11 +526,13 @@ int sgemm_tc(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha, const
   if ((st = make_bf16_kmajor_map(&mapB, sb, 3 * n_pad, k_pad, BK, BN))) return st;
   static bool attr_set = false;
   if (!attr_set) {
-    GB_CUDA(cudaFuncSetAttribute(sgemm_bf16x3_kernel<0>,
+    GB_CUDA(cudaFuncSetAttribute(sgemm_bf16x3_kernel<0, true>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    GB_CUDA(cudaFuncSetAttribute(sgemm_bf16x3_kernel<1>,
+    GB_CUDA(cudaFuncSetAttribute(sgemm_bf16x3_kernel<0, false>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    GB_CUDA(cudaFuncSetAttribute(sgemm_bf16x3_kernel<2>,
+    GB_CUDA(cudaFuncSetAttribute(sgemm_bf16x3_kernel<1, true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    GB_CUDA(cudaFuncSetAttribute(sgemm_bf16x3_kernel<2, true>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
     attr_set = true;
   }
@@ -504,9 +557,14 @@ int sgemm_tc(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha, const
   const int grid = ntiles < sm_count() ? ntiles : sm_count();
   {
     ProfileScope prof("sgemm_tc", s);
-    if (tri == 1) sgemm_bf16x3_kernel<1><<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, p);
-    else if (tri == 2) sgemm_bf16x3_kernel<2><<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, p);
-    else sgemm_bf16x3_kernel<0><<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, p);
+    if (tri == 1)
+      sgemm_bf16x3_kernel<1, true><<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, p);
+    else if (tri == 2)
+      sgemm_bf16x3_kernel<2, true><<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, p);
+    else if (beta != 0.f)
+      sgemm_bf16x3_kernel<0, true><<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, p);
+    else
+      sgemm_bf16x3_kernel<0, false><<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, p);
     count_launch();
   }
   { sgemm_fixup_kernel<<<sm_count() * 4, 256, 0, s>>>(m, n, k, alpha, A, lda, ta, B, ldb, tb, beta,
