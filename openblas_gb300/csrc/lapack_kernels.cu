@@ -1368,18 +1368,7 @@ int getrs_device(int trans, int64_t n, int64_t nrhs, const T *A, int64_t lda, co
   return check_cuda(cudaGetLastError(), "getrs");
 }
 
-// Right-looking blocked Cholesky (lapack/potrf/potrf_L_single.c:81-236,
-// potrf_U_single.c:79-193): potf2 on the diagonal block, TRSM of the panel,
-// SYRK of the trailing matrix.  Every kernel after a failed potf2 sees info
-// != 0 and does nothing, so the matrix is left as at the failure point.
-// Cholesky, blocked like lapack/potrf/potrf_L_single.c / potrf_U_single.c:
-// 256-wide block columns; the diagonal block is factored in FP64 by 32-wide
-// steps (potf2 + TRSM + SYRK inside the block); the panel below (right of)
-// it is solved against the block's triangle, and the trailing matrix gets
-// one rank-256 SYRK -- the native FP64 tri-masked GEMM, or with gemm_mode 1
-// the emulated-FP64 GEMM restricted to the triangle.  Every step after a
-// non-positive pivot is skipped on the device (info), so the matrix is left
-// as it was at the failing column.
+// Block columns of the blocked Cholesky (potrf_device_t below).
 constexpr int64_t POTRF_NB = 256;
 
 template <typename T>
@@ -1454,11 +1443,51 @@ static int potrf_trailing(bool upper, int64_t rest, int64_t jb, const float *P, 
   return syrk_skip<float>(upper ? 0 : 1, upper ? 1 : 0, rest, jb, P, lda, C, lda, s, info);
 }
 
+__global__ void set_identity_kernel(int64_t n, double *__restrict__ W) {
+  const int64_t total = n * n;
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
+       e += (int64_t)gridDim.x * blockDim.x)
+    W[e] = (e % n == e / n) ? 1.0 : 0.0;
+}
+
+// The panel solve of a 256-wide step: L21 = A21 L11^-T (lower) or
+// U12 = U11^-T A12 (upper).  Native: one FP64 TRSM.  In the emulated-FP64
+// mode the block's triangle is inverted once by substitution on the identity
+// (native FP64, jb^3/3 flops) and the panel becomes one FP64-accurate GEMM on
+// the tensor cores -- the native TRSM over the whole panel ran at the FP64
+// pipe's rate (152 of 884 ms at n = 32768).  Steps after a failed pivot are
+// skipped on the device (info), as in the native form.
+static int potrf_panel_solve(bool upper, int64_t rest, int64_t jb, const double *D,
+                             int64_t lda, double *P, int *info, int gemm_mode, cudaStream_t s) {
+  if (!(gemm_mode == 1 && rest >= 256 && jb >= 64))
+    return upper ? trsm_skip<double>(0, 0, 1, 1, jb, rest, D, lda, P, lda, s, info)
+                 : trsm_skip<double>(1, 1, 1, 1, rest, jb, D, lda, P, lda, s, info);
+  Scratch ws((size_t)(jb * jb + rest * jb) * sizeof(double), s);
+  if (!ws.p) return GB_ERR_ALLOC;
+  double *W = ws.as<double>(), *T = W + jb * jb;
+  { set_identity_kernel<<<(unsigned)((jb * jb + 255) / 256), 256, 0, s>>>(jb, W); count_launch(); }
+  // W := tri(D)^-1 (the block's lower or upper triangle, non-unit)
+  int st = dtrsm_device_skip(0, upper ? 0 : 1, 0, 1, jb, jb, 1.0, D, lda, W, jb, s, info);
+  if (st) return st;
+  if (upper) {  // P (jb x rest) := W^T P
+    GB_CUDA(cudaMemcpy2DAsync(T, jb * 8, P, lda * 8, jb * 8, rest, cudaMemcpyDeviceToDevice, s));
+    return dgemm_emulated(1, 0, jb, rest, jb, 1.0, W, jb, T, jb, 0.0, P, lda, 0, s, 0, info);
+  }
+  // P (rest x jb) := P W^T
+  GB_CUDA(cudaMemcpy2DAsync(T, rest * 8, P, lda * 8, rest * 8, jb, cudaMemcpyDeviceToDevice, s));
+  return dgemm_emulated(0, 1, rest, jb, jb, 1.0, T, rest, W, jb, 0.0, P, lda, 0, s, 0, info);
+}
+static int potrf_panel_solve(bool upper, int64_t rest, int64_t jb, const float *D, int64_t lda,
+                             float *P, int *info, int, cudaStream_t s) {
+  return upper ? trsm_skip<float>(0, 0, 1, 1, jb, rest, D, lda, P, lda, s, info)
+               : trsm_skip<float>(1, 1, 1, 1, rest, jb, D, lda, P, lda, s, info);
+}
+
 // Cholesky, blocked like lapack/potrf/potrf_L_single.c / potrf_U_single.c:
 // 256-wide block columns; the diagonal block is factored by 32-wide steps
 // (potf2 + TRSM + SYRK inside the block); the panel below (right of) it is
-// solved against the block's triangle, and the trailing matrix gets one
-// rank-256 SYRK (see potrf_trailing).  Every step after a non-positive pivot
+// solved against the block's triangle (potrf_panel_solve), and the trailing
+// matrix gets one rank-256 SYRK (see potrf_trailing).  Every step after a non-positive pivot
 // is skipped on the device (info), so the matrix is left as it was at the
 // failing column.
 template <typename T>
@@ -1480,9 +1509,7 @@ int potrf_device_t(int uplo, int64_t n, T *A, int64_t lda, int *info, int gemm_m
                  : A + (j0 + jb) + j0 * lda;  // rest x jb
     {
       ProfileScope prof("potrf_trsm", s);
-      st = upper ? trsm_skip<T>(0, 0, 1, 1, jb, rest, D, lda, P, lda, s, info)
-                 : trsm_skip<T>(1, 1, 1, 1, rest, jb, D, lda, P, lda, s, info);
-      if (st) return st;
+      if ((st = potrf_panel_solve(upper, rest, jb, D, lda, P, info, gemm_mode, s))) return st;
     }
     {
       ProfileScope prof("potrf_update", s);
