@@ -383,7 +383,6 @@ potf2_kernel(int upper, int nb, T *__restrict__ A, int64_t lda, int *__restrict_
 
 constexpr int CPANEL_THREADS = 512;
 constexpr int CPANEL_WARPS = CPANEL_THREADS / 32;
-constexpr int CPANEL_LD = PANEL_NB + 1;  // padded row stride in shared memory
 constexpr int CPANEL_MAX_CS = 16;       // one pushing warp per destination CTA
 
 // Shared memory of the cluster panel kernel: candidate inboxes (rows,
@@ -762,11 +761,6 @@ template <>
 void gemm_minus<double>(int64_t m, int64_t n, int64_t k, const double *A, int64_t lda,
                         const double *B, int64_t ldb, double *C, int64_t ldc, cudaStream_t s) {
   launch_dgemm_fp64(0, 0, m, n, k, -1.0, A, lda, B, ldb, 1.0, C, ldc, s);
-}
-template <>
-void gemm_minus<float>(int64_t m, int64_t n, int64_t k, const float *A, int64_t lda,
-                       const float *B, int64_t ldb, float *C, int64_t ldc, cudaStream_t s) {
-  launch_sgemm_fp32(0, 0, m, n, k, -1.0f, A, lda, B, ldb, 1.0f, C, ldc, s);
 }
 
 template <typename T>
