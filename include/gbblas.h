@@ -232,7 +232,7 @@ int xerbla_(const char *name, const blasint *info, blasint len);
 
 /* DGEMM precision modes */
 #define GB_DGEMM_NATIVE 0   /* FP64 FMA units */
-#define GB_DGEMM_EMULATED 1 /* Ozaki split into 7-bit slices on bf16 tensor cores */
+#define GB_DGEMM_EMULATED 1 /* Ozaki split into 8-bit slices on bf16 tensor cores */
 #define GB_DGEMM_AUTO 2     /* emulated when the shape is large enough to win */
 
 /* Stream used by every entry point of the calling thread (NULL = the
@@ -286,7 +286,8 @@ int gb_dgemm_native_dev(char transa, char transb, int64_t m, int64_t n,
                         int64_t k, double alpha, const double *A, int64_t lda,
                         const double *B, int64_t ldb, double beta, double *C,
                         int64_t ldc);
-/* Emulated FP64 GEMM with `slices` 7-bit slices per operand (0 = auto). */
+/* Emulated FP64 GEMM with `slices` 8-bit slices per operand (1..8; 0 = the
+ * default, 7: 56 bits, FP64-level accuracy). */
 int gb_dgemm_emulated_dev(char transa, char transb, int64_t m, int64_t n,
                           int64_t k, double alpha, const double *A, int64_t lda,
                           const double *B, int64_t ldb, double beta, double *C,

@@ -2,20 +2,22 @@
 //
 // C = alpha*op(A)*op(B) + beta*C is computed from fixed-point slices:
 //   1. split: every row i of op(A) is scaled by 2^-e_i (e_i = exponent of
-//      the row's max |a|), truncated to S*7 bits and cut into S signed 7-bit
-//      digits A_1..A_S (|digit| <= 127, exactly representable in bf16);
-//      columns of op(B) likewise with exponents f_j.  Slices are stored
-//      K-contiguous and zero-padded to the tile grid, whatever the caller's
-//      transpose and leading dimension.
+//      the row's max |a|), truncated to S*8 bits and cut into S signed 8-bit
+//      digits A_1..A_S (|digit| <= 255: eight significant bits, exactly
+//      representable in bf16); columns of op(B) likewise with exponents f_j.
+//      Slices are stored K-contiguous and zero-padded to the tile grid,
+//      whatever the caller's transpose and leading dimension.  S = 7 keeps
+//      56 bits (FP64-level accuracy) with S(S+1)/2 = 28 products.
 //   2. slice GEMM (tcgen05, kind::f16): for each output tile and each level
-//      L = s+t (2..S+1, the Ozaki triangle), the products A_s*B_t^T are
-//      accumulated in TMEM in FP32 over K-chunks of 1024.  With |digit| <=
-//      127, every partial sum of a chunk is an integer below 2^24, so the
-//      FP32 accumulation is exact; each chunk is drained to int32 registers
-//      (exact conversion) and summed per level.  A level sum of up to S
-//      products over K <= 16384 stays below 2^31.  Level sums are written as
-//      int32 planes.
-//   3. recombine (FP64): C_ij = alpha * 2^(e_i+f_j) * sum_L P_L,ij 2^(-7L)
+//      L = s+t (2..S+1, the Ozaki triangle), each product A_s*B_t^T is
+//      accumulated in TMEM in FP32 over K-chunks of 256.  With |digit| <=
+//      255, every partial sum of a chunk is an integer of magnitude at most
+//      256 * 255^2 < 2^24, so the FP32 accumulation is exact; each chunk is
+//      drained to int32 registers (exact conversion) and summed per level.
+//      A level sum of up to S <= 8 products over K <= 4096 stays below 2^31
+//      (8 * 4096 * 255^2 < 2^31); longer K runs as accumulated segments.
+//      Level sums are written as int32 planes.
+//   3. recombine (FP64): C_ij = alpha * 2^(e_i+f_j) * sum_L P_L,ij 2^(-8L)
 //      + beta*C_ij.  Rows/columns holding Inf/NaN fall back to a direct FP64
 //      dot product so IEEE special values propagate.
 //
@@ -43,7 +45,9 @@ namespace oz {
 
 constexpr int BM = 128, BN = 256, BK = 64;
 constexpr int STAGES = 4;
-constexpr int KC_BLOCKS = 16;  // K chunk of one exact FP32 accumulation: 1024
+constexpr int DIGIT_BITS = 8;  // bits of one slice digit, |digit| <= 255
+constexpr unsigned long long DIGIT_MASK = (1ull << DIGIT_BITS) - 1;
+constexpr int KC_BLOCKS = 4;   // K chunk of one exact FP32 accumulation: 256
 constexpr int A_BYTES = BM * BK * 2;
 constexpr int B_BYTES = BN * BK * 2;
 constexpr int STAGE_BYTES = A_BYTES + B_BYTES;
@@ -51,7 +55,9 @@ constexpr int NUM_THREADS = 320;
 constexpr int TMEM_COLS = 512;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr int MAX_SLICES = 8;
-constexpr int64_t MAX_K_SEGMENT = 16384;  // keeps a level sum below 2^31
+constexpr int64_t MAX_K_SEGMENT = 4096;   // keeps a level sum below 2^31
+static_assert(256LL * 255 * 255 < (1LL << 24), "a 256-deep chunk of one product is exact in FP32");
+static_assert(8LL * MAX_K_SEGMENT * 255 * 255 < (1LL << 31), "a level sum fits int32");
 constexpr uint64_t WAIT_LIMIT_NS = 4000000000ull;
 constexpr int NONFINITE = -100000;  // exponent marker of a row/column with Inf/NaN
 
@@ -398,7 +404,7 @@ split_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
   }
   __syncthreads();
   // each thread: row rr = tid / 8, 8 consecutive k values.  The fixed-point
-  // value trunc(|x| * 2^(7S - e)) is taken straight from the IEEE bits
+  // value trunc(|x| * 2^(8S - e)) (< 2^64 for S <= 8) is taken straight from the IEEE bits
   // (mantissa shifted by the exponent difference): integer work only, as
   // FP64 arithmetic is the scarcest unit on this part.
   const int rr = tid >> 3, pc = (tid & 7) * 8;
@@ -419,20 +425,20 @@ split_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
       M |= 1ull << 52;
       sh = E - 1075;
     }
-    sh += 7 * S - e;
+    sh += DIGIT_BITS * S - e;
     unsigned long long t;
     if (e == NONFINITE || M == 0) t = 0;
-    else if (sh >= 0) t = M << sh;       // |x| < 2^e keeps t < 2^(7S)
+    else if (sh >= 0) t = M << sh;       // |x| < 2^e keeps t < 2^(8S)
     else if (sh > -64) t = M >> (-sh);   // truncation toward zero
     else t = 0;
     mag[j] = t;
   }
   for (int s = 1; s <= S; ++s) {
-    const int sh = 7 * (S - s);
+    const int sh = DIGIT_BITS * (S - s);
     __align__(16) __nv_bfloat16 out[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
-      int d = (int)((mag[j] >> sh) & 127ull);
+      int d = (int)((mag[j] >> sh) & DIGIT_MASK);
       out[j] = __float2bfloat16_rn((float)(neg[j] ? -d : d));
     }
     __nv_bfloat16 *dst = slices + ((int64_t)(s - 1) * Rpad + r) * Kpad + p0 + pc;
@@ -441,9 +447,9 @@ split_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
 }
 
 // ------------------------------------------------------------------ recombine
-// One element of C from its exact level sum: acc = sum_L P_L 2^(7(S+1-L))
-// (< 2^81) is rounded once to FP64 (sticky bit), then scaled exactly by
-// alpha * 2^(e_i + f_j - 7(S+1)) through the exponent bits of alpha.
+// One element of C from its exact level sum: acc = sum_L P_L 2^(8(S+1-L))
+// (< 2^88) is rounded once to FP64 (sticky bit), then scaled exactly by
+// alpha * 2^(e_i + f_j - 8(S+1)) through the exponent bits of alpha.
 __device__ __forceinline__ double level_value(__int128 acc, int S, int ei, int fj, double alpha) {
   if (acc == 0) return 0.0;
   const bool neg = acc < 0;
@@ -454,7 +460,7 @@ __device__ __forceinline__ double level_value(__int128 acc, int S, int ei, int f
   unsigned long long top = (unsigned long long)(u >> sh);
   if (sh && (u & (((unsigned __int128)1 << sh) - 1)) != 0) top |= 1ull;  // sticky bit
   const double t = __ull2double_rn(top);
-  const int x = sh - 7 * (S + 1) + ei + fj;
+  const int x = sh - DIGIT_BITS * (S + 1) + ei + fj;
   const long long ab = __double_as_longlong(alpha);
   const int e_alpha = (int)((ab >> 52) & 0x7ff);
   double scale;
@@ -516,7 +522,7 @@ recombine_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
 #pragma unroll
         for (int L = 0; L < S; ++L) {
           const int pv = r == 0 ? P[L].x : r == 1 ? P[L].y : r == 2 ? P[L].z : P[L].w;
-          acc += (__int128)pv << (7 * (S - 1 - L));  // level L+2 has weight 2^(7(S+1-(L+2)))
+          acc += (__int128)pv << (DIGIT_BITS * (S - 1 - L));  // level L+2: 2^(8(S+1-(L+2)))
         }
         v = level_value(acc, S, e_i[r], fj, alpha);
       }
@@ -555,25 +561,29 @@ void split_operand(bool kcontig, int64_t R, int64_t K, const double *X, int64_t 
     { split_kernel<false><<<g2, 256, 0, s>>>(R, K, X, ld, expo, S, Rpad, Kpad, slices); count_launch(); }
 }
 
-// One pass over a K segment (k <= MAX_K_SEGMENT).  op(A) is split once;
-// the columns of op(B) and C are taken in blocks of `nb` (a multiple of BN):
-// each block is split, multiplied by the slice GEMM and recombined, with the
-// hooks (when given) making block j of op(B) and C available on the device
-// first and told when C's block is final.  Every C(i,j) depends only on row
-// i of op(A) and column j of op(B) (and their own exponents), so the blocked
-// result equals the single-block one bit for bit.
-int emulated_segment(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
+// The whole emulated product.  K is cut into segments of at most
+// MAX_K_SEGMENT (so every int32 level sum is exact); each segment is split,
+// multiplied by the slice GEMM and recombined, later segments accumulating
+// into C (beta = 1).  The columns of op(B) and C are taken in blocks of `nb`
+// (a multiple of BN), all segments of a block before the next block, with
+// the hooks (when given) making block j of op(B) and C available on the
+// device first and told when C's block is final.  op(A) is split once when K
+// is one segment and per segment and block otherwise.  Every C(i,j) depends
+// only on row i of op(A) and column j of op(B) (and their own exponents), so
+// the blocked result equals the single-block one bit for bit.
+int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
                      const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
                      double *C, int64_t ldc, int S, cudaStream_t s, int tri, const int *skip,
                      int64_t nb = 0, EmuBlockHooks *hooks = nullptr) {
   if (nb <= 0 || nb >= n) nb = n;
-  const int64_t m_pad = round_up(m, BM), nb_pad = round_up(nb, BN), k_pad = round_up(k, BK);
-  const size_t bytes_sa = align256((size_t)S * m_pad * k_pad * 2);
-  const size_t bytes_sb = align256((size_t)S * nb_pad * k_pad * 2);
+  const int64_t kseg = k < MAX_K_SEGMENT ? k : MAX_K_SEGMENT;
+  const int64_t nseg = (k + MAX_K_SEGMENT - 1) / MAX_K_SEGMENT;
+  const int64_t m_pad = round_up(m, BM), nb_pad = round_up(nb, BN), ks_pad = round_up(kseg, BK);
+  const size_t bytes_sa = align256((size_t)S * m_pad * ks_pad * 2);
+  const size_t bytes_sb = align256((size_t)S * nb_pad * ks_pad * 2);
   const size_t bytes_mx = align256((size_t)(m_pad + nb_pad) * 8);
   const size_t bytes_e = align256((size_t)(m_pad + nb_pad) * 4);
-  const int64_t plane_stride = m_pad * nb_pad;
-  const size_t bytes_pl = align256((size_t)S * plane_stride * 4);
+  const size_t bytes_pl = align256((size_t)S * m_pad * nb_pad * 4);
   Scratch ws(bytes_sa + bytes_sb + bytes_mx + bytes_e + bytes_pl, s);
   if (!ws.p) return GB_ERR_ALLOC;
   char *base = ws.as<char>();
@@ -584,17 +594,21 @@ int emulated_segment(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
   int *eb = ea + m_pad;
   int *planes = reinterpret_cast<int *>(base + bytes_sa + bytes_sb + bytes_mx + bytes_e);
 
-  // op(A) rows: K-contiguous when A is transposed; op(B) columns: K-contiguous when B is not
-  split_operand(ta != 0, m, k, A, lda, S, m_pad, k_pad, mx, ea, sla, s);
-  CUtensorMap mapA, mapB;
-  int st = make_map(&mapA, sla, (int64_t)S * m_pad, k_pad, BM);
-  if (st) return st;
   static bool attr_set = false;
   if (!attr_set) {
     GB_CUDA(cudaFuncSetAttribute(slice_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  SMEM_BYTES));
     attr_set = true;
   }
+  CUtensorMap mapA, mapB;
+  int st;
+  // op(A) rows: K-contiguous when A is transposed; op(B) columns: K-contiguous when B is not
+  auto split_a = [&](int64_t k0, int64_t kk) -> int {
+    const int64_t kp = round_up(kk, BK);
+    split_operand(ta != 0, m, kk, ta ? A + k0 : A + k0 * lda, lda, S, m_pad, kp, mx, ea, sla, s);
+    return make_map(&mapA, sla, (int64_t)S * m_pad, kp, BM);
+  };
+  if (nseg == 1 && (st = split_a(0, k))) return st;
   for (int64_t j0 = 0; j0 < n; j0 += nb) {
     const int64_t jn = (n - j0) < nb ? (n - j0) : nb;
     const int64_t jn_pad = round_up(jn, BN);
@@ -602,37 +616,44 @@ int emulated_segment(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
     double *Cj = C + j0 * ldc;
     int64_t ldbj = ldb, ldcj = ldc;
     if (hooks && (st = hooks->before(j0, jn, &Bj, &ldbj, &Cj, &ldcj))) return st;
-    split_operand(tb == 0, jn, k, Bj, ldbj, S, jn_pad, k_pad, mx + m_pad, eb, slb, s);
-    if ((st = make_map(&mapB, slb, (int64_t)S * jn_pad, k_pad, BN))) return st;
-    GemmParams gp;
-    gp.S = S;
-    gp.m_tiles = (int)(m_pad / BM);
-    gp.n_tiles = (int)(jn_pad / BN);
-    gp.group_m = config().ozaki_group_m;
-    // the triangle is relative to C's own indices: only the single-block
-    // form (j0 = 0) is used with tri
-    gp.tri = tri;
-    gp.kblocks = (int)(k_pad / BK);
-    gp.m_pad = (int)m_pad;
-    gp.n_pad = (int)jn_pad;
-    gp.plane_stride = m_pad * jn_pad;
-    gp.planes = planes;
-    gp.status = ctx().d_status;
-    const int ntiles = gp.m_tiles * gp.n_tiles;
-    const int grid = ntiles < sm_count() ? ntiles : sm_count();
-    {
-      ProfileScope prof("slice_gemm", s);
-      slice_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, gp);
-      count_launch();
-    }
-    GB_CUDA(cudaGetLastError());
-    {
+    for (int64_t sg = 0; sg < nseg; ++sg) {
+      const int64_t k0 = sg * MAX_K_SEGMENT;
+      const int64_t kk = (k - k0) < MAX_K_SEGMENT ? (k - k0) : MAX_K_SEGMENT;
+      const int64_t kp = round_up(kk, BK);
+      if (nseg > 1 && (st = split_a(k0, kk))) return st;
+      const double *Ak = ta ? A + k0 : A + k0 * lda;
+      const double *Bk = tb ? Bj + k0 * ldbj : Bj + k0;
+      split_operand(tb == 0, jn, kk, Bk, ldbj, S, jn_pad, kp, mx + m_pad, eb, slb, s);
+      if ((st = make_map(&mapB, slb, (int64_t)S * jn_pad, kp, BN))) return st;
+      GemmParams gp;
+      gp.S = S;
+      gp.m_tiles = (int)(m_pad / BM);
+      gp.n_tiles = (int)(jn_pad / BN);
+      gp.group_m = config().ozaki_group_m;
+      // the triangle is relative to C's own indices: only the single-block
+      // form (j0 = 0) is used with tri
+      gp.tri = tri;
+      gp.kblocks = (int)(kp / BK);
+      gp.m_pad = (int)m_pad;
+      gp.n_pad = (int)jn_pad;
+      gp.plane_stride = m_pad * jn_pad;
+      gp.planes = planes;
+      gp.status = ctx().d_status;
+      const int ntiles = gp.m_tiles * gp.n_tiles;
+      const int grid = ntiles < sm_count() ? ntiles : sm_count();
+      {
+        ProfileScope prof("slice_gemm", s);
+        slice_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, gp);
+        count_launch();
+      }
+      GB_CUDA(cudaGetLastError());
+      const double bseg = sg == 0 ? beta : 1.0;  // later segments accumulate
       const dim3 g((unsigned)((m + BM - 1) / BM), (unsigned)((jn + BN - 1) / BN));
       const int64_t ps = gp.plane_stride;
 #define GB_RECOMBINE(SS)                                                                        \
   case SS:                                                                                      \
     recombine_tile_kernel<SS><<<g, 256, 0, s>>>(m, jn, gp.m_tiles, ps, planes, ea, eb, alpha,   \
-                                                beta, Cj, ldcj, ta, tb, k, A, lda, Bj, ldbj,    \
+                                                bseg, Cj, ldcj, ta, tb, kk, Ak, lda, Bk, ldbj,  \
                                                 tri, skip);                                     \
     break;
       switch (S) {
@@ -642,8 +663,8 @@ int emulated_segment(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       }
 #undef GB_RECOMBINE
       count_launch();
+      if ((st = check_cuda(cudaGetLastError(), "emulated dgemm"))) return st;
     }
-    if ((st = check_cuda(cudaGetLastError(), "emulated dgemm"))) return st;
     if (hooks && (st = hooks->after(j0, jn))) return st;
   }
   return GB_SUCCESS;
@@ -653,7 +674,8 @@ int emulated_segment(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
 
 // Slice count used when the caller passes 0: 8 slices (56 bits) reach FP64
 // accuracy for operands whose rows/columns span a moderate exponent range.
-int ozaki_default_slices() { return oz::MAX_SLICES; }
+// 7 slices of 8-bit digits: 56 bits, FP64-level accuracy
+int ozaki_default_slices() { return 7; }
 
 int dgemm_emulated_blocked(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
                            const double *A, int64_t lda, double beta, int slices, int64_t nb,
@@ -661,10 +683,10 @@ int dgemm_emulated_blocked(int ta, int tb, int64_t m, int64_t n, int64_t k, doub
   int S = slices > 0 ? slices : ozaki_default_slices();
   if (S > oz::MAX_SLICES) S = oz::MAX_SLICES;
   if (m <= 0 || n <= 0) return GB_SUCCESS;
-  if (k > oz::MAX_K_SEGMENT || m > (int64_t)1 << 22 || n > (int64_t)1 << 22)
-    return set_error(GB_ERR_UNSUPPORTED, "blocked emulated dgemm: one K segment only");
+  if (m > (int64_t)1 << 22 || n > (int64_t)1 << 22)
+    return set_error(GB_ERR_UNSUPPORTED, "blocked emulated dgemm: dimension too large");
   nb = (nb + oz::BN - 1) / oz::BN * oz::BN;
-  return oz::emulated_segment(ta, tb, m, n, k, alpha, A, lda, nullptr, 0, beta, nullptr, 0, S, s,
+  return oz::emulated_product(ta, tb, m, n, k, alpha, A, lda, nullptr, 0, beta, nullptr, 0, S, s,
                               0, nullptr, nb, hooks);
 }
 
@@ -677,18 +699,8 @@ int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha
   if (m <= 0 || n <= 0) return GB_SUCCESS;
   if (m > (int64_t)1 << 22 || n > (int64_t)1 << 22)
     return set_error(GB_ERR_UNSUPPORTED, "emulated dgemm: dimension too large");
-  // K segments keep every int32 level sum exact; later segments accumulate.
-  double b = beta;
-  for (int64_t k0 = 0; k0 < k; k0 += oz::MAX_K_SEGMENT) {
-    const int64_t kk = (k - k0) < oz::MAX_K_SEGMENT ? (k - k0) : oz::MAX_K_SEGMENT;
-    const double *Ak = ta ? A + k0 : A + k0 * lda;
-    const double *Bk = tb ? B + k0 * ldb : B + k0;
-    int st = oz::emulated_segment(ta, tb, m, n, kk, alpha, Ak, lda, Bk, ldb, b, C, ldc, S, s, tri,
-                                  skip);
-    if (st) return st;
-    b = 1.0;
-  }
-  return GB_SUCCESS;
+  return oz::emulated_product(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, S, s, tri,
+                              skip);
 }
 
 }  // namespace gb

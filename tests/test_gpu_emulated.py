@@ -2,12 +2,13 @@
 
 1. Exactness: integer operands are represented exactly by their slices, so
    the result must equal the exact integer product bit for bit -- including
-   the worst case where every digit is +-127 and each 1024-deep FP32
-   accumulation reaches its largest value (1024*127^2 < 2^24).
+   the worst case where every digit is +-255 and each 256-deep FP32
+   accumulation reaches its largest value (256*255^2 < 2^24), over several
+   4096-deep K segments.
 2. Accuracy against a double-double reference on uniform(-1,1) and
    exponent-spread operands U*2^E: normwise error
    ||C - Cref||_max / ||G||_max, G = |alpha||A||B| + |beta||C| (the DMMCH
-   denominator), bounded by 8*eps for 8 slices on e = 0 operands.
+   denominator), bounded by 8*eps for 7 slices (56 bits) on e = 0 operands.
 3. The DGEMM contract: transposes, padded leading dimensions, alpha/beta,
    beta = 0 overwriting NaN, and Inf/NaN inputs propagating.
 """
@@ -47,20 +48,23 @@ def test_integer_operands_exact(F, emulated, m, n, k):
 
 
 def test_worst_case_digits_exact(F, emulated):
-    """All digits +-127 with aligned signs: every chunk sum is 1024*16129."""
-    m, n, k = 130, 260, 4096
-    A = np.full((m, k), 127.0, order="F")
-    B = np.full((k, n), 127.0, order="F")
-    A[::2] = -127.0
+    """All digits +-255 with aligned signs: every 256-deep chunk sum is
+    256*65025 (just below 2^24) and every level sum of a 4096-deep segment
+    4096*65025; k = 9000 spans three segments."""
+    m, n, k = 130, 260, 9000
+    A = np.full((m, k), 255.0, order="F")
+    B = np.full((k, n), 255.0, order="F")
+    A[::2] = -255.0
     C = np.zeros((m, n), order="F")
     F.dgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, C, m)
-    exact = np.where(np.arange(m)[:, None] % 2 == 0, -1.0, 1.0) * (k * 127.0 * 127.0)
+    exact = np.where(np.arange(m)[:, None] % 2 == 0, -1.0, 1.0) * (k * 255.0 * 255.0)
     assert np.array_equal(C, np.broadcast_to(exact, (m, n)))
 
 
 def test_multi_digit_exact(F, emulated):
-    """Operands with several nonzero 7-bit digits (integers below 2^40 with a
-    common row scale) are still represented exactly by 8 slices."""
+    """Operands with several nonzero 8-bit digits (integers below 2^41 with a
+    common row scale) are represented exactly by the default 7 slices
+    (56 bits)."""
     m, n, k = 96, 96, 300
     A = _int_matrix(3, (m, k), -(2 ** 20), 2 ** 20)
     B = _int_matrix(4, (k, n), -(2 ** 20), 2 ** 20)
@@ -77,7 +81,9 @@ def _normwise(Cg, Cref, G):
     return np.abs(Cg - Cref).max() / G.max()
 
 
-@pytest.mark.parametrize("e,slices,bound", [(0, 8, 8), (0, 7, 200), (8, 8, 32), (16, 8, 256)])
+# 8-bit slices: 7 keep 56 bits (the default), 6 keep 48
+@pytest.mark.parametrize("e,slices,bound", [(0, 7, 8), (0, 6, 200), (8, 7, 32), (16, 7, 256),
+                                            (0, 8, 8)])
 def test_accuracy_vs_double_double(orc, F, emulated, gblib, e, slices, bound):
     m = n = k = 384
     A = W.exponent_spread(10 + e, (m, k), e)
@@ -164,7 +170,7 @@ def _device_emulated(gblib, ta, tb, m, n, k, alpha, A, B, beta, C):
     dC = torch.from_numpy(C.T.copy()).cuda()
     assert gblib.gb_dgemm_emulated_dev(ta.encode(), tb.encode(), m, n, k, alpha, dA.data_ptr(),
                                        A.shape[0], dB.data_ptr(), B.shape[0], beta,
-                                       dC.data_ptr(), C.shape[0], 8) == 0
+                                       dC.data_ptr(), C.shape[0], 0) == 0  # default slices
     assert gblib.gb_synchronize() == 0
     return dC.cpu().numpy().T
 
