@@ -83,11 +83,14 @@ def barrier(world):
 
 
 def allreduce_max(x, world):
+    """The slowest rank's value (replica timing); the tensor lives where the
+    process group's backend wants it (NCCL on the GPU, gloo on the host)."""
     if world == 1:
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
