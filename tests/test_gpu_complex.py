@@ -72,6 +72,24 @@ def test_zgemm_vs_oracle(orc, F, gblib, gb_clean, mode, ta, tb):
     assert np.array_equal(Cm[m:], C0[m:])
 
 
+def test_zgemm_emulated_several_k_segments(orc, F, gblib, gb_clean):
+    """The 4M embedding doubles K (2k = 5000 here): the emulated engine runs
+    it as two K segments accumulating into the product; normwise bound."""
+    m, n, k = 300, 260, 2500
+    A, B, Cm = _operands(14050, m, n, k, "C", "N", np.complex128)
+    C0, Co = Cm.copy(order="F"), Cm.copy(order="F")
+    al, be = 0.6 + 0.8j, 0.25 - 1.0j
+    gblib.gb_set_dgemm_mode(1)
+    try:
+        F.zgemm("C", "N", m, n, k, al, A, k, B, k, be, Cm, m)
+    finally:
+        gblib.gb_set_dgemm_mode(0)
+    orc.zgemm("C", "N", m, n, k, al, A, k, B, k, be, Co, m)
+    r = zgemm_ratio(Cm, Co, A, B, C0, m, n, k, "C", "N", al, be, _eps(np.complex128),
+                    normwise=True)
+    assert r <= 2 * (k + 2), r
+
+
 @pytest.mark.parametrize("ta,tb", [("N", "T"), ("C", "N")])
 def test_zgemm3m_vs_oracle(orc, F, gb_clean, ta, tb):
     m, n, k = 650, 520, 390

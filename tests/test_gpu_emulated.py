@@ -196,6 +196,17 @@ def test_host_pipelined_equals_single_call(F, emulated, gblib, ta, tb, beta, pad
     assert np.isinf(C[:m, 6400]).any()
 
 
+def test_host_pipelined_several_k_segments(F, emulated, gblib):
+    """K beyond one 4096-deep segment on the column-blocked host path: op(A)
+    is split again per segment inside each block, and the segments
+    accumulate into C; still bit-identical to the single device call."""
+    m, n, k = 2048, 6200, 5000
+    A, B, C = W.gemm_operands(92, m, n, k, "T", "N", pad=2)
+    ref = _device_emulated(gblib, "T", "N", m, n, k, -0.5, A, B, 2.0, C)
+    F.dgemm("T", "N", m, n, k, -0.5, A, A.shape[0], B, B.shape[0], 2.0, C, C.shape[0])
+    assert np.array_equal(C, ref)
+
+
 def test_host_pipelined_pinned_buffers(emulated, gblib):
     """The same through cblas_dgemm on pinned (page-locked) host buffers."""
     torch = pytest.importorskip("torch")
