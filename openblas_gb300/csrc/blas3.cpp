@@ -265,21 +265,6 @@ static void sgemm_blocking(int ta, int tb, int64_t m, int64_t n, int64_t k, floa
 
 // GEMM argument check shared by the Fortran and CBLAS forms
 // (interface/gemm.c:264-278, 409-418).  Returns the xerbla position or 0.
-static int gemm_check(int transa, int transb, int64_t m, int64_t n, int64_t k, int64_t lda,
-                      int64_t ldb, int64_t ldc) {
-  int64_t nrowa = (transa & 1) ? k : m;
-  int64_t nrowb = (transb & 1) ? n : k;
-  int info = 0;
-  if (ldc < m) info = 13;
-  if (ldb < nrowb) info = 10;
-  if (lda < nrowa) info = 8;
-  if (k < 0) info = 5;
-  if (n < 0) info = 4;
-  if (m < 0) info = 3;
-  if (transb < 0) info = 2;
-  if (transa < 0) info = 1;
-  return info;
-}
 
 int dtrsm_device(int side, int uplo, int trans, int unit, int64_t m, int64_t n, double alpha,
                  const double *A, int64_t lda, double *B, int64_t ldb, cudaStream_t s);

@@ -38,22 +38,6 @@ inline int zcblas_trans_code(int t) {
   return -1;
 }
 
-int zgemm_check(int transa, int transb, int64_t m, int64_t n, int64_t k, int64_t lda,
-                int64_t ldb, int64_t ldc) {
-  const int64_t nrowa = (transa & 1) ? k : m;
-  const int64_t nrowb = (transb & 1) ? n : k;
-  int info = 0;
-  if (ldc < m) info = 13;
-  if (ldb < nrowb) info = 10;
-  if (lda < nrowa) info = 8;
-  if (k < 0) info = 5;
-  if (n < 0) info = 4;
-  if (m < 0) info = 3;
-  if (transb < 0) info = 2;
-  if (transa < 0) info = 1;
-  return info;
-}
-
 template <typename T>
 void cgemm_blocking(int ta, int tb, int64_t m, int64_t n, int64_t k, const T *alpha, const T *A,
                     int64_t lda, const T *B, int64_t ldb, const T *beta, T *C, int64_t ldc,
@@ -82,7 +66,7 @@ void fortran_cgemm(const char *TRANSA, const char *TRANSB, const blasint *M, con
                    const blasint *ldB, const T *beta, T *C, const blasint *ldC, const char *name,
                    int three_m) {
   const int ta = ztrans_code(*TRANSA), tb = ztrans_code(*TRANSB);
-  const int info = zgemm_check(ta, tb, *M, *N, *K, *ldA, *ldB, *ldC);
+  const int info = gemm_check(ta, tb, *M, *N, *K, *ldA, *ldB, *ldC);
   if (info) {
     call_xerbla(name, info);
     return;
@@ -112,7 +96,7 @@ void cblas_cgemm_t(int order, int TransA, int TransB, blasint m, blasint n, blas
     tb = zcblas_trans_code(TransA);
   }
   if (order == CblasColMajor || order == CblasRowMajor) {
-    info = zgemm_check(ta, tb, M, N, k, la, lb, ldc);
+    info = gemm_check(ta, tb, M, N, k, la, lb, ldc);
     if (info == 0) info = -1;
   }
   if (info >= 0) {
@@ -128,7 +112,7 @@ int dev_cgemm(char transa, char transb, int64_t m, int64_t n, int64_t k, const T
               const T *A, int64_t lda, const T *B, int64_t ldb, const T *beta, T *C, int64_t ldc,
               const char *name, int three_m) {
   const int ta = ztrans_code(transa), tb = ztrans_code(transb);
-  const int info = zgemm_check(ta, tb, m, n, k, lda, ldb, ldc);
+  const int info = gemm_check(ta, tb, m, n, k, lda, ldb, ldc);
   if (info) {
     call_xerbla(name, info);
     return GB_ERR_INVALID_VALUE;

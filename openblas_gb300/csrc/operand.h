@@ -60,6 +60,25 @@ inline char upch(const char *c) {
 }
 inline char upch(char x) { return (x >= 'a' && x <= 'z') ? (char)(x - 32) : x; }
 
+// GEMM argument checks in the order of interface/gemm.c:274-286 (real and
+// COMPLEX builds alike); returns the xerbla parameter position or 0.  Op
+// codes: bit 0 set for a transposed operand (T, and C for complex).
+inline int gemm_check(int transa, int transb, int64_t m, int64_t n, int64_t k, int64_t lda,
+                      int64_t ldb, int64_t ldc) {
+  const int64_t nrowa = (transa & 1) ? k : m;
+  const int64_t nrowb = (transb & 1) ? n : k;
+  int info = 0;
+  if (ldc < m) info = 13;
+  if (ldb < nrowb) info = 10;
+  if (lda < nrowa) info = 8;
+  if (k < 0) info = 5;
+  if (n < 0) info = 4;
+  if (m < 0) info = 3;
+  if (transb < 0) info = 2;
+  if (transa < 0) info = 1;
+  return info;
+}
+
 // Records the argument error and calls xerbla_ (which may be overridden).
 void call_xerbla(const char *name, int info);
 void record_xerbla(const char *name, int info);
