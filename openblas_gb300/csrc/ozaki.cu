@@ -672,9 +672,9 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
 
 }  // namespace oz
 
-// Slice count used when the caller passes 0: 8 slices (56 bits) reach FP64
-// accuracy for operands whose rows/columns span a moderate exponent range.
-// 7 slices of 8-bit digits: 56 bits, FP64-level accuracy
+// Slice count used when the caller passes 0: 7 slices of 8-bit digits keep
+// 56 bits, FP64-level accuracy for operands whose rows/columns span a
+// moderate exponent range.
 int ozaki_default_slices() { return 7; }
 
 int dgemm_emulated_blocked(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
