@@ -786,12 +786,12 @@ void cblas_dgemm_batch(enum CBLAS_ORDER order, const enum CBLAS_TRANSPOSE *trans
       a_code = cblas_trans_code(transb_array[g]);
       b_code = cblas_trans_code(transa_array[g]);
     } else {
-      call_xerbla("DGEMM ", 0);
+      call_xerbla("DGEMM_BATCH ", 0);  // gemm_batch.c:44, info 0 for a bad order
       return;
     }
     int info = gemm_check(a_code, b_code, M, N, k_array[g], la, lb, ldc_array[g]);
     if (info) {
-      call_xerbla("DGEMM ", info);
+      call_xerbla("DGEMM_BATCH ", info);
       return;
     }
     ta[g] = a_code;

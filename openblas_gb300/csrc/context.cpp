@@ -165,7 +165,7 @@ int stage_out(void *dst_host, const void *src_dev, size_t ld, size_t m, size_t n
 // Called from the xerbla_ entry point (also when the application overrides
 // xerbla_, the library records the argument error before calling it).
 void record_xerbla(const char *name, int info) {
-  size_t n = strnlen(name, 8);
+  size_t n = strnlen(name, sizeof(t_err.xerbla_name) - 1);
   memcpy(t_err.xerbla_name, name, n);
   t_err.xerbla_name[n] = 0;
   t_err.xerbla_info = info;
@@ -214,9 +214,12 @@ ProfileScope::~ProfileScope() {
 extern "C" {
 
 __attribute__((weak)) int xerbla_(const char *name, const blasint *info, blasint len) {
-  (void)len;
+  // The whole routine name, padded to at least six columns (driver/others/
+  // xerbla.c:58); a Fortran caller passes it without a terminator, so the
+  // hidden length bounds it.
   char buf[16];
-  size_t n = strnlen(name, 6);
+  const size_t cap = (len > 0 && len < 15) ? (size_t)len : 15;
+  size_t n = strnlen(name, cap);
   memcpy(buf, name, n);
   buf[n] = 0;
   printf(" ** On entry to %6s parameter number %2d had an illegal value\n", buf, *info);

@@ -254,8 +254,51 @@ def test_quick_returns_do_not_touch_device(gblib, F):
 
 
 def test_xerbla_message_format(gblib, capfd):
-    """driver/others/xerbla.c:58: ' ** On entry to %6s parameter number %2d ...'"""
+    """driver/others/xerbla.c:58: ' ** On entry to %6s parameter number %2d ...'
+    -- %6s pads short names and keeps long ones whole; a Fortran caller's name
+    carries no terminator and is bounded by the hidden length."""
     info = C.c_int(3)
     gblib.xerbla_(b"DGEMM ", C.byref(info), 6)
+    gblib.xerbla_(b"ZGEMM3M ", C.byref(info), 8)
+    gblib.xerbla_(b"DGEMM_BATCH ", C.byref(info), 12)
+    gblib.xerbla_(b"DGETRFXYZ", C.byref(info), 6)
     out = capfd.readouterr().out
     assert " ** On entry to DGEMM  parameter number  3 had an illegal value" in out
+    assert " ** On entry to ZGEMM3M  parameter number  3 had an illegal value" in out
+    assert " ** On entry to DGEMM_BATCH  parameter number  3 had an illegal value" in out
+    assert " ** On entry to DGETRF parameter number  3 had an illegal value" in out
+
+
+def test_dgemm_batch_argument_errors(gblib):
+    """interface/gemm_batch.c:195-283: every group is checked before any group
+    runs; errors are reported as DGEMM_BATCH (gemm_batch.c:44) with the GEMM
+    positions (row-major swaps the operands first), and an unknown order
+    with position 0.  All pointers are null: nothing may run."""
+    from openblas_gb300 import abi
+
+    def iarr(v):
+        return (C.c_int * len(v))(*v)
+
+    def call(order, ta, tb, ms, ns, ks, lda, ldb, ldc):
+        g = len(ms)
+        nulls = (C.c_void_p * g)()
+        gblib.gb_clear_error()
+        gblib.cblas_dgemm_batch(order, iarr(ta), iarr(tb), iarr(ms), iarr(ns), iarr(ks),
+                                (C.c_double * g)(*[1.0] * g), nulls, iarr(lda), nulls,
+                                iarr(ldb), (C.c_double * g)(*[0.0] * g), nulls, iarr(ldc),
+                                g, iarr([1] * g))
+        name, info = gb.last_xerbla(gblib)
+        return name.strip(), info
+
+    N, T = abi.CblasNoTrans, abi.CblasTrans
+    col, row = abi.CblasColMajor, abi.CblasRowMajor
+    # the second group is bad: the first, valid one must not have run
+    assert call(col, [N, N], [N, N], [4, 4], [4, 4], [4, 4], [4, 4], [4, 4], [4, 3]) == \
+        ("DGEMM_BATCH", 13)
+    assert call(col, [N, 7], [N, N], [4, 4], [4, 4], [4, 4], [4, 4], [4, 4], [4, 4]) == \
+        ("DGEMM_BATCH", 1)
+    assert call(col, [N], [T], [4], [5], [4], [4], [4], [4]) == ("DGEMM_BATCH", 10)
+    assert call(col, [N], [N], [4], [4], [-1], [4], [4], [4]) == ("DGEMM_BATCH", 5)
+    # row-major A (m x k, lda >= k) with lda < k: the swapped B operand's ldb (10)
+    assert call(row, [N], [N], [4], [5], [6], [5], [5], [5]) == ("DGEMM_BATCH", 10)
+    assert call(999, [N], [N], [4], [4], [4], [4], [4], [4]) == ("DGEMM_BATCH", 0)
