@@ -714,7 +714,7 @@ void dgemmt_(const char *UPLO, const char *TRANSA, const char *TRANSB, const bla
   int ta = trans_code(upch(TRANSA)), tb = trans_code(upch(TRANSB));
   int info = gemmt_check(uplo, ta, tb, *M, *K, *ldA, *ldB, *ldC);
   if (info) {
-    call_xerbla("DGEMMT", info);
+    call_xerbla("DGEMMT ", info);
     return;
   }
   dgemmt_blocking(uplo, ta, tb, *M, *K, *alpha, A, *ldA, B, *ldB, *beta, C, *ldC);
@@ -747,7 +747,7 @@ void cblas_dgemmt(enum CBLAS_ORDER order, enum CBLAS_UPLO Uplo, enum CBLAS_TRANS
     if (info == 0) info = -1;
   }
   if (info >= 0) {
-    call_xerbla("DGEMMT", info);
+    call_xerbla("DGEMMT ", info);
     return;
   }
   dgemmt_blocking(uplo, ta, tb, m, k, alpha, pa, la, pb, lb, beta, c, ldc);
@@ -871,7 +871,7 @@ int gb_dgemmt_dev(char uplo, char transa, char transb, int64_t m, int64_t k, dou
   const int ta = trans_code(upch(transa)), tb = trans_code(upch(transb));
   const int info = gemmt_check(up, ta, tb, m, k, lda, ldb, ldc);
   if (info) {
-    call_xerbla("DGEMMT", info);
+    call_xerbla("DGEMMT ", info);
     return GB_ERR_INVALID_VALUE;
   }
   int st = ensure_init();

@@ -139,7 +139,7 @@ int dgesv_(const blasint *N, const blasint *NRHS, double *a, const blasint *ldA,
   if (nrhs < 0) info = 2;
   if (n < 0) info = 1;
   if (info) {
-    call_xerbla("DGESV ", info);
+    call_xerbla("DGESV", info);
     *Info = -info;
     return 0;
   }

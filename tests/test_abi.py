@@ -135,6 +135,7 @@ def test_lapack_argument_errors(gblib, F):
     assert F.dgesv(4, -1, buf, 4, piv, buf, 4) == -2
     assert F.dgesv(4, 1, buf, 3, piv, buf, 4) == -4
     assert F.dgesv(4, 1, buf, 4, piv, buf, 3) == -7
+    assert _xerbla(gblib) == ("DGESV", 7)  # interface/lapack/gesv.c:49, no padding
     gblib.gb_clear_error()
     F.dgetrs("X", 4, 1, buf, 4, piv, buf, 4)
     assert _xerbla(gblib) == ("DGETRS", 1)
@@ -181,7 +182,7 @@ def test_trmm_syr2k_gemmt_argument_errors(gblib, F):
                       (("L", "N", "T", 4, 2, 4, 3, 4), 10), (("U", "N", "N", 4, 2, 4, 2, 3), 13)]:
         uplo, ta, tb, m, k, lda, ldb, ldc = args
         F.dgemmt(uplo, ta, tb, m, k, 1.0, buf, lda, buf, ldb, 0.0, buf, ldc)
-        assert _xerbla(gblib) == ("DGEMMT", pos), args
+        assert _xerbla(gblib) == ("DGEMMT ", pos), args  # gemmt.c:44
 
 
 def test_complex_gemm_argument_errors(gblib, F):
