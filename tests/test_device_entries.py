@@ -163,6 +163,30 @@ def test_device_entry_without_device_fails_loudly(L, case, call):
     assert st == GB_ERR_NO_DEVICE and msg
 
 
+@pytest.mark.skipif(_cuda_usable(), reason="a CUDA device is present")
+def test_host_entries_without_device_report_and_leave_outputs():
+    """The host-pointer (Fortran) entries have no status to return: without a
+    device they record GB_ERR_NO_DEVICE and leave the caller's arrays as they
+    were -- nothing is computed on the CPU instead."""
+    import numpy as np
+
+    import openblas_gb300 as gb
+    L = gb.load()
+    F = gb.fortran()
+    A = np.asfortranarray(np.arange(16.0).reshape(4, 4))
+    C = np.full((4, 4), 7.0, order="F")
+    L.gb_clear_error()
+    F.dgemm("N", "N", 4, 4, 4, 1.0, A, 4, A, 4, 0.0, C, 4)
+    assert gb.last_error(L)[0] == GB_ERR_NO_DEVICE
+    assert np.all(C == 7.0)
+    L.gb_clear_error()
+    piv = np.zeros(4, np.int32)
+    A0 = A.copy(order="F")
+    F.dgetrf(4, 4, A, 4, piv)
+    assert gb.last_error(L)[0] == GB_ERR_NO_DEVICE
+    assert np.array_equal(A, A0)
+
+
 def test_argument_error_wins_over_missing_device(L):
     """The argument check comes first even when no device could be used, so the
     xerbla position is the same on every machine."""
