@@ -573,8 +573,14 @@ void *gb_batch_plan_create(const gb_batch_problem *problems, int count, int flag
   for (int i = 0; i < count; ++i)
     if (pl->mixed && v[i].type == GB_BATCH_DGESV) d[i].work = pl->d_work + work_off[i];
   if (count) {
-    cudaMemcpy(pl->d_probs, d.data(), bytes, cudaMemcpyHostToDevice);
-    cudaMemcpy(pl->d_order, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice);
+    cudaError_t e = cudaMemcpy(pl->d_probs, d.data(), bytes, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess)
+      e = cudaMemcpy(pl->d_order, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+      check_cuda(e, "gb_batch_plan_create: table upload");
+      gb_batch_plan_destroy(pl);
+      return nullptr;
+    }
   }
   pl->grid = sm_count() * 2;
   // CTA size from the autotuner cache (keyed by the problem-size histogram)
@@ -617,8 +623,11 @@ int gb_batch_plan_tune(void *plan) {
   float best_ms = 1e30f;
   int best_t = pl->threads;
   cudaEvent_t e0, e1;
-  cudaEventCreate(&e0);
-  cudaEventCreate(&e1);
+  if ((st = check_cuda(cudaEventCreate(&e0), "gb_batch_plan_tune: event"))) return st;
+  if ((st = check_cuda(cudaEventCreate(&e1), "gb_batch_plan_tune: event"))) {
+    cudaEventDestroy(e0);
+    return st;
+  }
   for (int t : cands) {
     cudaEventRecord(e0, s);
     if ((st = launch_grouped(pl, t, s))) break;
