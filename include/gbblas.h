@@ -396,7 +396,10 @@ void gb_batch_plan_destroy(void *plan);
  * up the array's device address with that device current; make that first
  * call before any stream capture.  All calls share the array: calls whose GPU
  * work overlaps (other streams, other threads) race and must be serialised by
- * the caller. */
+ * the caller.  The status word of the panel kernel's bounded grid barrier
+ * also lives in that array, so gb_synchronize does not report an expired
+ * wait from this call (the barrier's blocks are co-resident by cooperative
+ * launch, so it has no expected cause). */
 int gb_dgetrf_noalloc_dev(int64_t m, int64_t n, double *A, int64_t lda,
                           int *ipiv, int *info, void *stream);
 /* Mixed-precision solve (FP32 LU on the GPU + FP64 refinement, GMRES-IR
