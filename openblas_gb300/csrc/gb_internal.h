@@ -7,6 +7,7 @@
 #include <stdint.h>
 
 #include "../../include/gbblas.h"
+#include "per_device.h"
 
 namespace gb {
 
@@ -114,6 +115,15 @@ void launch_dgemm_fp64_tri(int ta, int tb, int64_t m, int64_t n, int64_t k, doub
 void launch_dbeta_tri(int64_t n, double beta, double *C, int64_t ldc, int tri, cudaStream_t s);
 // Number of SMs of the current device.
 int sm_count();
+// Ordinal of the calling thread's current device (0 if it cannot be read).
+inline int current_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) {
+    cudaGetLastError();
+    dev = 0;
+  }
+  return dev;
+}
 // Native FP32 GEMM (FFMA).
 void launch_sgemm_fp32(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha,
                        const float *A, int64_t lda, const float *B, int64_t ldb,

@@ -153,14 +153,16 @@ __global__ void gemm_beta_kernel(int64_t m, int64_t n, T beta, T *__restrict__ C
 }  // namespace
 
 int sm_count() {
-  static int n = 0;
-  if (!n) {
-    int dev = 0;
-    cudaGetDevice(&dev);
-    cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev);
-    if (n <= 0) n = 152;
-  }
-  return n;
+  static PerDeviceValue<int> cache;
+  const int dev = current_device();
+  return cache.get(dev, [dev] {
+    int n = 0;
+    if (cudaDeviceGetAttribute(&n, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess) {
+      cudaGetLastError();
+      n = 0;
+    }
+    return n > 0 ? n : 152;
+  });
 }
 
 void launch_dgemm_beta(int64_t m, int64_t n, double beta, double *C, int64_t ldc,

@@ -645,12 +645,10 @@ struct ClusterPanel {
   int lmax = 0;
 };
 
+// Largest cluster the panel kernel launches with on the current device.
 template <typename T>
-const ClusterPanel<T> &cluster_panel_caps() {
-  static ClusterPanel<T> caps;
-  static bool done = false;
-  if (done) return caps;
-  done = true;
+ClusterPanel<T> probe_cluster_panel() {
+  ClusterPanel<T> caps;
   // rows per thread held in registers: 2 for float, 1 for double
   constexpr int lmax = sizeof(T) == 4 ? 2 : 1;
   const size_t smem = cpanel_smem_bytes<T>();
@@ -690,12 +688,19 @@ const ClusterPanel<T> &cluster_panel_caps() {
   return caps;
 }
 
+// The probe's result, found once per device.
+template <typename T>
+ClusterPanel<T> cluster_panel_caps() {
+  static PerDeviceValue<ClusterPanel<T>> cache;
+  return cache.get(current_device(), [] { return probe_cluster_panel<T>(); });
+}
+
 // Launch the cluster panel when the panel fits one cluster; returns 1 when
 // it does not (the caller then uses the grid-wide kernel).
 template <typename T>
 int launch_cluster_panel(int64_t rows, int nb, T *A, int64_t lda, int *ipiv, int64_t row_off,
                          int *info, cudaStream_t s) {
-  const ClusterPanel<T> &caps = cluster_panel_caps<T>();
+  const ClusterPanel<T> caps = cluster_panel_caps<T>();
   if (caps.max_cs < 2) return 1;
   int64_t cs = (rows + CPANEL_THREADS - 1) / CPANEL_THREADS;
   if (cs < 2) cs = 2;
@@ -743,15 +748,17 @@ int launch_panel(int64_t rows, int nb, T *A, int64_t lda, int *ipiv, int64_t row
 
 template <typename T, int R>
 int coop_limit() {
-  static int lim = 0;
-  if (!lim) {
+  static PerDeviceValue<int> cache;
+  return cache.get(current_device(), [] {
     int per_sm = 0;
-    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, getf2_panel_kernel<T, R>,
-                                                  PANEL_THREADS, 0);
-    lim = per_sm * sm_count();
-    if (lim <= 0) lim = 1;
-  }
-  return lim;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, getf2_panel_kernel<T, R>,
+                                                      PANEL_THREADS, 0) != cudaSuccess) {
+      cudaGetLastError();
+      per_sm = 0;
+    }
+    const int lim = per_sm * sm_count();
+    return lim > 0 ? lim : 1;
+  });
 }
 
 template <typename T>
@@ -885,12 +892,13 @@ int lu_trsm(int64_t n1, int64_t w, const T *L, int64_t ldl, T *B, int64_t ldb, c
   if (n1 > LT_MAXN) return trsm_any<T>(0, 1, 0, 0, n1, w, L, ldl, B, ldb, s);
   const int nblk = (int)((n1 + 31) / 32);
   const size_t smem = lu_trsm_smem<T>(nblk);
-  static bool attr = false;
-  if (!attr) {
+  static PerDeviceOnce attr_once;
+  const int ast = attr_once.run(current_device(), [] {
     GB_CUDA(cudaFuncSetAttribute(lu_trsm_kernel<T>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)lu_trsm_smem<T>(LT_MAXN / 32)));
-    attr = true;
-  }
+    return GB_SUCCESS;
+  });
+  if (ast) return ast;
   const int64_t grid = (w + LT_COLS - 1) / LT_COLS;
   { lu_trsm_kernel<T><<<(unsigned)grid, 256, smem, s>>>((int)n1, w, L, ldl, B, ldb); count_launch(); }
   return check_cuda(cudaGetLastError(), "lu_trsm");

@@ -594,14 +594,14 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
   int *eb = ea + m_pad;
   int *planes = reinterpret_cast<int *>(base + bytes_sa + bytes_sb + bytes_mx + bytes_e);
 
-  static bool attr_set = false;
-  if (!attr_set) {
+  static PerDeviceOnce attr_once;
+  int st = attr_once.run(current_device(), [] {
     GB_CUDA(cudaFuncSetAttribute(slice_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  SMEM_BYTES));
-    attr_set = true;
-  }
+    return GB_SUCCESS;
+  });
+  if (st) return st;
   CUtensorMap mapA, mapB;
-  int st;
   // op(A) rows: K-contiguous when A is transposed; op(B) columns: K-contiguous when B is not
   auto split_a = [&](int64_t k0, int64_t kk) -> int {
     const int64_t kp = round_up(kk, BK);

@@ -524,8 +524,8 @@ int sgemm_tc(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha, const
   int st = make_bf16_kmajor_map(&mapA, sa, 3 * m_pad, k_pad, BK, BM);
   if (st) return st;
   if ((st = make_bf16_kmajor_map(&mapB, sb, 3 * n_pad, k_pad, BK, BN))) return st;
-  static bool attr_set = false;
-  if (!attr_set) {
+  static PerDeviceOnce attr_once;
+  st = attr_once.run(current_device(), [] {
     GB_CUDA(cudaFuncSetAttribute(sgemm_bf16x3_kernel<0, true>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
     GB_CUDA(cudaFuncSetAttribute(sgemm_bf16x3_kernel<0, false>,
@@ -534,8 +534,9 @@ int sgemm_tc(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha, const
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
     GB_CUDA(cudaFuncSetAttribute(sgemm_bf16x3_kernel<2, true>,
                                  cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
-    attr_set = true;
-  }
+    return GB_SUCCESS;
+  });
+  if (st) return st;
   Params p;
   p.m_tiles = (int)(m_pad / BM);
   p.n_tiles = (int)(n_pad / BN);
