@@ -201,7 +201,10 @@ ProfileScope::ProfileScope(const char *nm, cudaStream_t st) : name(nm), s(st) {
 ProfileScope::~ProfileScope() {
   if (!e0) return;
   cudaEvent_t e1;
-  if (cudaEventCreate(&e1) != cudaSuccess) return;
+  if (cudaEventCreate(&e1) != cudaSuccess) {
+    cudaEventDestroy(e0);
+    return;
+  }
   cudaEventRecord(e1, s);
   t_prof.push_back({name, e0, e1});
 }
