@@ -153,6 +153,7 @@ static int dgemm_host_pipelined(int ta, int tb, int64_t m, int64_t n, int64_t k,
                                 const double *A, int64_t lda, const double *B, int64_t ldb,
                                 double beta, double *C, int64_t ldc) {
   if (k <= 0 || alpha == 0.0 || k > 16384 || n < 6144 || m < 2048) return 0;
+  if (m > GEMM_BLOCK_EXTENT || n > GEMM_BLOCK_EXTENT) return 0;  // the blocked device path
   if (!dgemm_wants_emulated(m, n, k)) return 0;
   if (is_device_pointer(A) || is_device_pointer(B) || is_device_pointer(C)) return 0;
   PipelinedDgemm p;

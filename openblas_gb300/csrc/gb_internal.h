@@ -7,6 +7,7 @@
 #include <stdint.h>
 
 #include "../../include/gbblas.h"
+#include "gemm_blocks.h"
 #include "per_device.h"
 
 namespace gb {

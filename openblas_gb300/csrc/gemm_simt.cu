@@ -187,6 +187,16 @@ void launch_dgemm_fp64_tri(int ta, int tb, int64_t m, int64_t n, int64_t k, doub
                            const double *A, int64_t lda, const double *B, int64_t ldb,
                            double beta, double *C, int64_t ldc, int tri, cudaStream_t s,
                            const int *skip) {
+  if (n > GEMM_BLOCK_EXTENT && tri == 0) {  // column tiles sit on gridDim.y
+    gemm_over_blocks(ta, tb, m, n, A, lda, B, ldb, C, ldc, GEMM_BLOCK_EXTENT,
+                     [&](int64_t mb, int64_t nb, const double *Ai, const double *Bj,
+                         double *Cij) {
+                       launch_dgemm_fp64_tri(ta, tb, mb, nb, k, alpha, Ai, lda, Bj, ldb, beta,
+                                             Cij, ldc, 0, s, skip);
+                       return 0;
+                     });
+    return;
+  }
   ProfileScope prof("dgemm_fp64", s);
   const int64_t tiles64 = ((m + 63) / 64) * ((n + 63) / 64);
   if (tiles64 >= (int64_t)sm_count() * 8) {
@@ -217,6 +227,15 @@ void launch_dbeta_tri(int64_t n, double beta, double *C, int64_t ldc, int tri, c
 void launch_sgemm_fp32_tri(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha,
                            const float *A, int64_t lda, const float *B, int64_t ldb, float beta,
                            float *C, int64_t ldc, int tri, cudaStream_t s, const int *skip) {
+  if (n > GEMM_BLOCK_EXTENT && tri == 0) {  // column tiles sit on gridDim.y
+    gemm_over_blocks(ta, tb, m, n, A, lda, B, ldb, C, ldc, GEMM_BLOCK_EXTENT,
+                     [&](int64_t mb, int64_t nb, const float *Ai, const float *Bj, float *Cij) {
+                       launch_sgemm_fp32_tri(ta, tb, mb, nb, k, alpha, Ai, lda, Bj, ldb, beta,
+                                             Cij, ldc, 0, s, skip);
+                       return 0;
+                     });
+    return;
+  }
   const int64_t tiles128 = ((m + 127) / 128) * ((n + 127) / 128);
   if (tiles128 >= (int64_t)sm_count() * 2) {
     dim3 grid((unsigned)((m + 127) / 128), (unsigned)((n + 127) / 128));

@@ -697,8 +697,15 @@ int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha
   int S = slices > 0 ? slices : ozaki_default_slices();
   if (S > oz::MAX_SLICES) S = oz::MAX_SLICES;
   if (m <= 0 || n <= 0) return GB_SUCCESS;
-  if (m > (int64_t)1 << 22 || n > (int64_t)1 << 22)
-    return set_error(GB_ERR_UNSUPPORTED, "emulated dgemm: dimension too large");
+  if ((m > GEMM_BLOCK_EXTENT || n > GEMM_BLOCK_EXTENT) && tri == 0 && !skip)
+    return gemm_over_blocks(ta, tb, m, n, A, lda, B, ldb, C, ldc, GEMM_BLOCK_EXTENT,
+                            [&](int64_t mb, int64_t nb, const double *Ai, const double *Bj,
+                                double *Cij) {
+                              return oz::emulated_product(ta, tb, mb, nb, k, alpha, Ai, lda, Bj,
+                                                          ldb, beta, Cij, ldc, S, s, 0, nullptr);
+                            });
+  if (m > GEMM_BLOCK_EXTENT || n > GEMM_BLOCK_EXTENT)
+    return set_error(GB_ERR_UNSUPPORTED, "emulated dgemm: triangular update too large");
   return oz::emulated_product(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, S, s, tri,
                               skip);
 }

@@ -498,7 +498,14 @@ int sgemm_tc(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha, const
              int64_t lda, const float *B, int64_t ldb, float beta, float *C, int64_t ldc,
              cudaStream_t s, int tri, const int *skip) {
   using namespace s3;
-  if (m > (int64_t)1 << 22 || n > (int64_t)1 << 22 || k > (int64_t)1 << 24)
+  if ((m > GEMM_BLOCK_EXTENT || n > GEMM_BLOCK_EXTENT) && tri == 0 && !skip)
+    return gemm_over_blocks(ta, tb, m, n, A, lda, B, ldb, C, ldc, GEMM_BLOCK_EXTENT,
+                            [&](int64_t mb, int64_t nb, const float *Ai, const float *Bj,
+                                float *Cij) {
+                              return sgemm_tc(ta, tb, mb, nb, k, alpha, Ai, lda, Bj, ldb, beta,
+                                              Cij, ldc, s, 0, nullptr);
+                            });
+  if (m > GEMM_BLOCK_EXTENT || n > GEMM_BLOCK_EXTENT || k > (int64_t)1 << 24)
     return set_error(GB_ERR_UNSUPPORTED, "sgemm_tc: dimension too large");
   const int64_t m_pad = round_up(m, BM), n_pad = round_up(n, BN), k_pad = round_up(k, BK);
   const size_t a_elems = 3 * (size_t)m_pad * k_pad, b_elems = 3 * (size_t)n_pad * k_pad;
