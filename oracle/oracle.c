@@ -1,8 +1,9 @@
 /*
  * oracle.c -- CPU restatement of OpenBLAS's level-3 + blocked-LAPACK hot path.
  *
- * TEST INFRASTRUCTURE ONLY (the checker).  Loaded by the tests, the smoke
- * check and bench.py's CPU-baseline leg; never by the product library.
+ * TEST INFRASTRUCTURE ONLY: the reference results the library is tested
+ * against.  Loaded by the tests, the smoke check and bench.py's CPU-baseline
+ * leg; never by the product library.
  *
  * Each function cites the OpenBLAS 0.3.28.dev source it restates.  The code
  * is written from those algorithms, not copied: the GotoBLAS packing/kernel

@@ -1,8 +1,9 @@
 /*
  * oracle.h -- CPU restatement of OpenBLAS's level-3 + blocked-LAPACK hot path.
  *
- * TEST INFRASTRUCTURE ONLY.  This library is the checker: only the tests, the
- * smoke check and the CPU-baseline leg of bench.py may load it.  The product
+ * TEST INFRASTRUCTURE ONLY.  This library gives the results the product is
+ * tested against: only the tests, the smoke check and the CPU-baseline leg of
+ * bench.py may load it.  The product
  * (libgbblas.so) never links, loads or calls it.
  *
  * Every routine restates the reference algorithm it cites (paths are relative

@@ -1,7 +1,7 @@
 """ctypes front-end of the oracle library (oracle/liborc.so).
 
 TEST INFRASTRUCTURE ONLY: used by the tests, the smoke check and the
-CPU-baseline leg of bench.py as the checker / CPU baseline.  Same argument
+CPU-baseline leg of bench.py, as the reference results and the CPU baseline.  Same argument
 order as the Fortran ABI wrappers in openblas_gb300.abi.Fortran so a test can
 run one case through either.
 """
