@@ -187,6 +187,34 @@ def test_host_entries_without_device_report_and_leave_outputs():
     assert np.array_equal(A, A0)
 
 
+def test_error_state_is_per_thread(L):
+    """Each host thread has its own error record: threads that raise different
+    argument errors at the same time each read back their own (ctypes drops
+    the interpreter lock during the call, so the calls overlap)."""
+    import threading
+
+    cases = [(dict(ta=b"X"), 1), (dict(tb=b"X"), 2), (dict(m=-1), 3), (dict(n=-1), 4),
+             (dict(k=-1), 5), (dict(lda=3), 8), (dict(ldb=3), 10), (dict(ldc=3), 13)]
+    errors = []
+    start = threading.Barrier(len(cases))
+
+    def worker(kw, pos):
+        call = _gemm("gb_dgemm_dev", **kw)
+        start.wait()
+        for _ in range(300):
+            L.gb_clear_error()
+            if call(L) != GB_ERR_INVALID_VALUE or _lib.last_xerbla(L) != ("DGEMM ", pos):
+                errors.append((pos, _lib.last_xerbla(L)))
+                return
+
+    threads = [threading.Thread(target=worker, args=c) for c in cases]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join()
+    assert not errors, errors[:5]
+
+
 def test_argument_error_wins_over_missing_device(L):
     """The argument check comes first even when no device could be used, so the
     xerbla position is the same on every machine."""
