@@ -49,6 +49,46 @@ def test_dgemm_cases(golden, orc):
                     idx += 1
 
 
+def test_double_double_gemm_against_exact_sums(orc):
+    """The double-double GEMM is the accuracy yardstick of the emulated FP64
+    engine, so it is pinned itself: against exact rational sums of
+    alpha*A*B + beta*C.  Two cases:
+    - operands spread over 2^±20;
+    - columns of B built to cancel almost all of each dot product (with and
+      without a beta*C term).
+    The result must be the exact value rounded to double, up to a
+    double-double residue: |dd - exact| <= 2^-53 |exact| + 2^-100 G."""
+    from fractions import Fraction
+
+    m, n, k = 6, 5, 240
+    cases = []
+    A = np.asfortranarray(W.exponent_spread(300, (m, k), 20))
+    B = np.asfortranarray(W.exponent_spread(301, (k, n), 20))
+    cases.append((A, B, 1.0, 0.0))
+    # cancellation: A's second half repeats its first and B's second half negates its
+    # first, so every dot product is one small perturbed term
+    A2 = np.asfortranarray(W.uniform(302, (m, k)))
+    B2 = np.asfortranarray(W.uniform(303, (k, n)))
+    h = k // 2
+    A2[:, h:] = A2[:, :h]
+    B2[h:, :] = -B2[:h, :]
+    B2[0, :] += 2.0 ** -40
+    cases.append((A2, B2, -1.5, 0.75))
+    cases.append((A2, B2, -1.5, 0.0))  # the cancelled dot product alone
+    for A, B, alpha, beta in cases:
+        C0 = np.asfortranarray(W.uniform(304, (m, n)))
+        C = C0.copy(order="F")
+        orc.dgemm_dd("N", "N", m, n, k, alpha, A, m, B, k, beta, C, m)
+        for i in range(m):
+            for j in range(n):
+                dot = sum(Fraction(float(A[i, p])) * Fraction(float(B[p, j])) for p in range(k))
+                exact = Fraction(alpha) * dot + Fraction(beta) * Fraction(float(C0[i, j]))
+                G = abs(alpha) * float(np.abs(A[i]) @ np.abs(B[:, j])) + abs(beta * C0[i, j])
+                err = abs(Fraction(float(C[i, j])) - exact)
+                assert err <= Fraction(2.0 ** -53) * abs(exact) + Fraction(2.0 ** -100) * \
+                    Fraction(G), (i, j, float(err), float(exact))
+
+
 def test_dgemm_c1(golden, orc):
     A, B, Cm = W.gemm_operands(42, 1024, 1024, 1024)
     orc.dgemm("N", "N", 1024, 1024, 1024, 1.5, A, 1024, B, 1024, 0.5, Cm, 1024)
