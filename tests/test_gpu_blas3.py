@@ -79,6 +79,28 @@ def test_dgemm_rowmajor_cblas(gb_clean):
     assert np.max(np.abs(C - ref)) <= 4 * (k + 2) * EPS * (np.abs(A) @ np.abs(B) + 2).max()
 
 
+@pytest.mark.parametrize("mode", [0, 1])  # native FP64, emulated FP64
+def test_svd_reconstruction_rowmajor(gblib, gb_clean, mode):
+    """The reference's utest/test_kernel_regress.c check:
+    - a 100 x 100 matrix of uniform [0, 10) values is factored by an SVD on the host;
+    - it is rebuilt as (U S) Vt by a row-major cblas_dgemm;
+    - the Frobenius norm of the difference must stay below 1e-10."""
+    ns = gb.cblas()
+    N = 100
+    M = W.uniform(4242, (N, N), 0.0, 10.0)
+    u, s, vt = np.linalg.svd(M)
+    us = np.ascontiguousarray(u * s)      # row-major U diag(s)
+    vt = np.ascontiguousarray(vt)
+    X = np.zeros((N, N))                  # row-major result
+    gblib.gb_set_dgemm_mode(mode)
+    try:
+        ns.cblas_dgemm(abi.CblasRowMajor, abi.CblasNoTrans, abi.CblasNoTrans, N, N, N, 1.0,
+                       us.ctypes.data, N, vt.ctypes.data, N, 0.0, X.ctypes.data, N)
+    finally:
+        gblib.gb_set_dgemm_mode(0)
+    assert np.linalg.norm(X - M) < 1e-10
+
+
 def test_dgemm_device_pointers(orc, gblib, gb_clean):
     torch = pytest.importorskip("torch")
     m, n, k = 300, 257, 190
