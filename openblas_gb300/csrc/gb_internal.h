@@ -66,9 +66,10 @@ struct Scratch {
 // True when `p` is device-accessible memory owned by CUDA (device or managed).
 bool is_device_pointer(const void *p);
 
-// Host<->device staging of a column-major m x n block with leading
-// dimension ld (elements of `esize` bytes).  Device copies are packed with
-// the same ld so kernels see the caller's layout.
+// Host<->device staging of a column-major m x n block whose host copy has
+// leading dimension ld (elements of `esize` bytes).  The device copy is
+// packed (leading dimension m), so only the m x n elements cross the link;
+// rows between m and ld on the host are neither read nor written.
 int stage_in(void *dst_dev, const void *src_host, size_t ld, size_t m, size_t n,
              size_t esize, cudaStream_t s);
 int stage_out(void *dst_host, const void *src_dev, size_t ld, size_t m, size_t n,
