@@ -1,18 +1,29 @@
 // FP32 GEMM on the bf16 tensor cores: C = alpha*op(A)*op(B) + beta*C.
 //
-// Every FP32 operand element x is split into three bf16 terms,
-// x = x1 + x2 + x3 + d with x1 = bf16(x), x2 = bf16(x - x1),
-// x3 = bf16(x - x1 - x2) (each residual is exact in FP32) and |d| <= 2^-27|x|
-// -- finer than FP32's own 2^-24 spacing.  The product keeps the six terms
-// whose weight is at least 2^-24 relative (A_i B_j with i + j <= 4, 1-based);
-// the three dropped terms are below 2^-27 relative.  Every bf16 x bf16
-// product is exact in FP32 and the six products are accumulated in FP32 in
-// TMEM, so the result has the accuracy of an FP32 GEMM (errors of order
+// Every FP32 operand element x is split into three bf16 terms, x1 = bf16(x),
+// x2 = bf16(x - x1), x3 = bf16(x - x1 - x2); each residual is exact in FP32.
+// For |x| >= 2^-110 the split is exact, x = x1 + x2 + x3, with
+// |x2| <= 2^-8 |x| and |x3| <= 2^-17 |x| (|x2| <= 2^-7 |x| for the values
+// next to FLT_MAX whose x1 rounds toward zero).  The product keeps the six terms
+// A_i B_j with i + j <= 4 (1-based).  The three dropped terms together are
+// at most (2^-24 + 2^-34) |a b| (2^-8 * 2^-17 twice, plus 2^-17 * 2^-17),
+// about FP32's unit roundoff.  Every bf16 x bf16
+// product is exact in FP32, and the six products are accumulated in FP32 in
+// TMEM.  So the result has the accuracy of an FP32 GEMM (errors of order
 // K * 2^-24 * sum|a||b|), at six bf16 MMA passes instead of one FP32 FMA
 // pass: the FP32 SIMT rate is 128 FMA/clk/SM, the bf16 tensor rate 4096
-// MAC/clk/SM.  Serves the trailing updates of the FP32 LU of the mixed
-// solver (sgemm semantics of interface/gemm.c; kernel/generic/gemm_beta.c
-// for beta).
+// MAC/clk/SM.
+//
+// Below 2^-110, x2 and x3 fall into bf16's subnormal range, which keeps
+// fewer bits than FP32's.  The split then loses bits: the relative error is
+// about 2^-23 at 2^-111 and doubles with each binade below, to 2^-8 at
+// 2^-126, and values below 2^-133 are lost.  This is harmless for an
+// element next to larger ones in its row or column.  But a product whose
+// operands are all that small loses accuracy in this form; the SIMT form
+// (GB_SGEMM_MODE=simt) has none of this limit.
+//
+// Serves the trailing updates of the FP32 LU of the mixed solver (sgemm
+// semantics of interface/gemm.c; kernel/generic/gemm_beta.c for beta).
 //
 // Kernel layout: persistent, one CTA per SM, warp-specialised.  Per
 // 64-wide K block, warp 0 loads the three A slices of the 128-row tile into
