@@ -450,6 +450,18 @@ split_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
 // One element of C from its exact level sum: acc = sum_L P_L 2^(8(S+1-L))
 // (< 2^88) is rounded once to FP64 (sticky bit), then scaled exactly by
 // alpha * 2^(e_i + f_j - 8(S+1)) through the exponent bits of alpha.
+// y * alpha * 2^x when alpha * 2^x is not a normal number (or alpha is
+// subnormal, zero, Inf or NaN).  The product can still be a normal number
+// (y is up to 2^64), so y is scaled by alpha's significand first and by the
+// whole power of two once: a subnormal or underflowed alpha * 2^x would lose
+// it.  Rarely taken, so kept out of line, away from the recombine loop's
+// registers.
+__device__ __noinline__ double scale_out_of_range(double y, double alpha, int x) {
+  int e_sig;
+  const double m_alpha = frexp(alpha, &e_sig);
+  return ldexp(y * m_alpha, x + e_sig);
+}
+
 __device__ __forceinline__ double level_value(__int128 acc, int S, int ei, int fj, double alpha) {
   if (acc == 0) return 0.0;
   const bool neg = acc < 0;
@@ -463,12 +475,9 @@ __device__ __forceinline__ double level_value(__int128 acc, int S, int ei, int f
   const int x = sh - DIGIT_BITS * (S + 1) + ei + fj;
   const long long ab = __double_as_longlong(alpha);
   const int e_alpha = (int)((ab >> 52) & 0x7ff);
-  double scale;
   if (e_alpha > 0 && e_alpha < 0x7ff && e_alpha + x > 0 && e_alpha + x < 0x7ff)
-    scale = __longlong_as_double(ab + ((long long)x << 52));
-  else
-    scale = alpha * ldexp(1.0, x);
-  return (neg ? -t : t) * scale;
+    return (neg ? -t : t) * __longlong_as_double(ab + ((long long)x << 52));
+  return scale_out_of_range(neg ? -t : t, alpha, x);
 }
 
 // Recombine, one CTA per 128 x 256 tile of C (the plane tile layout): every

@@ -82,7 +82,11 @@ def emulated_gemm(A: np.ndarray, B: np.ndarray, S: int, alpha: float = 1.0) -> n
         acc = acc + PL.astype(object) * (1 << (DIGIT_BITS * (S + 1 - L)))
     t = acc.astype(np.float64)                     # one correctly rounded conversion
     x = ea[:, None] + fb[None, :] - DIGIT_BITS * (S + 1)
-    return t * np.ldexp(alpha, x)
+    # t * alpha rounded once, then the power of two.  Where alpha * 2^x is a
+    # normal number the device multiplies by it instead, which gives the same
+    # value whenever the result is a normal number.
+    m_alpha, e_alpha = np.frexp(alpha)
+    return np.ldexp(t * m_alpha, x + e_alpha)
 
 
 def _dd(orc, A, B, alpha=1.0):
@@ -177,6 +181,27 @@ def test_elementwise_error_bound(orc):
     bound = (abs(alpha) * k * (S + 4) * np.ldexp(1.0, ea[:, None] + fb[None, :] - 8 * S)
              + 2 * EPS * np.abs(Cx))
     assert np.all(np.abs(C - Cx) <= bound)
+
+
+@pytest.mark.parametrize("alpha", [1.0, -1.5])
+def test_results_near_the_underflow_threshold(alpha):
+    """Rows of A near 2^-512 and columns of B near 2^-500 give C near 2^-1010,
+    still normal numbers.  The recombine's power-of-two scale alone
+    (alpha * 2^(e_i + f_j - 8(S+1))) is far below the smallest subnormal
+    there, so the scaling must not form it on its own; the results must be
+    the exactly rounded products up to the usual 56-bit truncation."""
+    from fractions import Fraction
+
+    A = W.uniform(70, (5, 40)) * 2.0 ** -512
+    B = W.uniform(71, (40, 4)) * 2.0 ** -500
+    C = emulated_gemm(A, B, 7, alpha)
+    for i in range(5):
+        for j in range(4):
+            exact = Fraction(alpha) * sum(Fraction(float(A[i, p])) * Fraction(float(B[p, j]))
+                                          for p in range(40))
+            G = abs(alpha) * float(np.abs(A[i]) @ np.abs(B[:, j]))
+            assert abs(float(exact)) > np.finfo(np.float64).tiny      # a normal result
+            assert abs(Fraction(float(C[i, j])) - exact) <= Fraction(8 * EPS) * Fraction(G)
 
 
 # the (exponent spread, slices, bound) cases the device parity tests use
