@@ -7,9 +7,9 @@ value truncated toward zero to 8*S bits below 2^e and cut into S signed
 triangle of S(S+1)/2 products), and one rounding of sum_L P_L 2^(8(S+1-L))
 to FP64 before the exact scale alpha * 2^(e_i + f_j - 8(S+1)).  The device
 rounds that sum with a sticky bit and a round-to-nearest conversion, which
-is the correctly rounded value that Python's int -> float conversion gives;
-for one K segment, beta = 0 and finite operands the model is the device's
-arithmetic step by step.
+is the correctly rounded value that Python's int -> float conversion gives.
+For one K segment, beta = 0, finite operands and results that are normal
+numbers, the model is the device's arithmetic step by step.
 
 The tests check the digit decomposition, the exactness bounds the device
 relies on (read from the kernel source, so the constants cannot drift), and
