@@ -240,7 +240,9 @@ int dlaswp_(const blasint *N, double *a, const blasint *LDA, const blasint *K1, 
   // rows touched: 1..max(k2, max pivot); stage the whole leading block
   int64_t rows = k2;
   const int64_t ainc = incx < 0 ? -incx : incx;
-  const int64_t npiv = (k1 - 1) + (k2 - k1 + 1) * ainc;
+  // entries the interchanges read: row i uses ipiv[(k1-1) + (i-k1)*|incx|]
+  // (0-based), i = k1..k2, so no more than the caller has to supply
+  const int64_t npiv = (k1 - 1) + (k2 - k1) * ainc + 1;
   bool pdev = is_device_pointer(ipiv);
   if (!pdev)
     for (int64_t t = 0; t < npiv; ++t)

@@ -275,6 +275,26 @@ def test_dlaswp_random_pivots(orc, F, gb_clean, rows, n, k1, k2, incx):
     assert np.array_equal(A, ref)
 
 
+@pytest.mark.parametrize("incx", [1, 2, -2, 3])
+def test_dlaswp_reads_only_the_pivots_it_uses(orc, F, gb_clean, incx):
+    """Row i (k1..k2) takes its pivot from ipiv[(k1-1) + (i-k1)*|incx|], so a
+    caller may pass exactly (k1-1) + (k2-k1)*|incx| + 1 entries.  Here the
+    array is a view whose next element is a poison value.  A longer read
+    would take it as a pivot row far outside A."""
+    import openblas_gb300 as gb
+    rows, n, k1, k2 = 50, 7, 3, 9
+    need = (k1 - 1) + (k2 - k1) * abs(incx) + 1
+    buf = np.full(need + 4, 10 ** 9, np.int32)
+    buf[:need] = W.randint(8800 + need, (need,), 1, rows).astype(np.int32)
+    ipiv = buf[:need]
+    A = W.uniform(8900 + need, (rows, n))
+    ref = A.copy(order="F")
+    orc.dlaswp(n, ref, rows, k1, k2, ipiv, incx)
+    F.dlaswp(n, A, rows, k1, k2, ipiv, incx)
+    assert gb.last_error(gb_clean)[0] == 0
+    assert np.array_equal(A, ref)
+
+
 def _sgetrf_dev(gblib, A32):
     torch = pytest.importorskip("torch")
     m, n = A32.shape
