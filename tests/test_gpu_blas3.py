@@ -101,6 +101,48 @@ def test_svd_reconstruction_rowmajor(gblib, gb_clean, mode):
     assert np.linalg.norm(X - M) < 1e-10
 
 
+@pytest.mark.parametrize("side,uplo,trans", [
+    ("L", "L", "N"), ("L", "U", "T"), ("R", "L", "T"), ("R", "U", "N")])
+def test_dtrsm_rowmajor_cblas(gb_clean, side, uplo, trans):
+    """Row-major cblas_dtrsm on row-major data (interface/trsm.c:315-351 maps
+    it to the column-major solve with m and n swapped, side and uplo flipped):
+    X = alpha * op(A)^-1 B (left) or alpha * B op(A)^-1 (right)."""
+    ns = gb.cblas()
+    m, n, alpha = 70, 45, -0.75
+    na = m if side == "L" else n
+    L = W.trsm_lower(9100 + na, na)
+    A = np.ascontiguousarray(L if uplo == "L" else L.T)      # row-major triangle
+    B = np.ascontiguousarray(W.uniform(9200 + na, (m, n)))
+    opA = A.T if trans == "T" else A
+    tri = np.tril(opA) if (uplo == "L") == (trans == "N") else np.triu(opA)
+    X = alpha * (np.linalg.solve(tri, B) if side == "L" else np.linalg.solve(tri.T, B.T).T)
+    ns.cblas_dtrsm(abi.CblasRowMajor, abi.CblasLeft if side == "L" else abi.CblasRight,
+                   abi.CblasLower if uplo == "L" else abi.CblasUpper,
+                   abi.CblasTrans if trans == "T" else abi.CblasNoTrans, abi.CblasNonUnit,
+                   m, n, alpha, A.ctypes.data, na, B.ctypes.data, n)
+    assert np.max(np.abs(B - X)) <= 64 * na * EPS * max(1.0, np.abs(X).max())
+
+
+@pytest.mark.parametrize("uplo,trans", [("U", "N"), ("L", "T")])
+def test_dsyrk_rowmajor_cblas(gb_clean, uplo, trans):
+    """Row-major cblas_dsyrk (interface/syrk.c:309-335 flips uplo and trans):
+    the stored triangle of C becomes alpha op(A) op(A)^T + beta C and the
+    other triangle is left as it was."""
+    ns = gb.cblas()
+    n, k, alpha, beta = 60, 33, 1.25, 0.5
+    A = np.ascontiguousarray(W.uniform(9300, (n, k) if trans == "N" else (k, n)))
+    C0 = np.ascontiguousarray(W.uniform(9301, (n, n)))
+    C = C0.copy()
+    opA = A if trans == "N" else A.T
+    full = alpha * opA @ opA.T + beta * C0
+    ns.cblas_dsyrk(abi.CblasRowMajor, abi.CblasUpper if uplo == "U" else abi.CblasLower,
+                   abi.CblasNoTrans if trans == "N" else abi.CblasTrans, n, k, alpha,
+                   A.ctypes.data, A.shape[1], beta, C.ctypes.data, n)
+    keep = np.triu(np.ones((n, n), bool)) if uplo == "U" else np.tril(np.ones((n, n), bool))
+    assert np.max(np.abs(C[keep] - full[keep])) <= 4 * (k + 2) * EPS * (abs(alpha) * k + beta)
+    assert np.array_equal(C[~keep], C0[~keep])
+
+
 def test_dgemm_device_pointers(orc, gblib, gb_clean):
     torch = pytest.importorskip("torch")
     m, n, k = 300, 257, 190
