@@ -375,6 +375,41 @@ static void dsyrk_blocking(int uplo, int trans, int64_t n, int64_t k, double alp
 
 using namespace gb;
 
+// interface/gemm.c:374-471: row-major is the column-major product of the
+// transposes, so A<->B, m<->n and transa<->transb swap.
+template <typename T, void (*Blocking)(int, int, int64_t, int64_t, int64_t, T, const T *, int64_t,
+                                       const T *, int64_t, T, T *, int64_t)>
+static void cblas_gemm_t(int order, int TransA, int TransB, blasint m, blasint n, blasint k,
+                         T alpha, const T *a, blasint lda, const T *b, blasint ldb, T beta, T *c,
+                         blasint ldc, const char *name) {
+  int info = -1, ta = -1, tb = -1;
+  int64_t M = m, N = n;
+  const T *pa = a, *pb = b;
+  int64_t la = lda, lb = ldb;
+  if (order == CblasColMajor) {
+    ta = cblas_trans_code(TransA);
+    tb = cblas_trans_code(TransB);
+  } else if (order == CblasRowMajor) {
+    M = n;
+    N = m;
+    pa = b;
+    pb = a;
+    la = ldb;
+    lb = lda;
+    ta = cblas_trans_code(TransB);
+    tb = cblas_trans_code(TransA);
+  }
+  if (order == CblasColMajor || order == CblasRowMajor) {
+    info = gemm_check(ta, tb, M, N, k, la, lb, ldc);
+    if (info == 0) info = -1;
+  }
+  if (info >= 0) {
+    call_xerbla(name, info);
+    return;
+  }
+  Blocking(ta, tb, M, N, k, alpha, pa, la, pb, lb, beta, c, ldc);
+}
+
 extern "C" {
 
 // ---------------------------------------------------------------------------
@@ -410,66 +445,16 @@ void cblas_dgemm(enum CBLAS_ORDER order, enum CBLAS_TRANSPOSE TransA,
                  enum CBLAS_TRANSPOSE TransB, blasint m, blasint n, blasint k, double alpha,
                  const double *a, blasint lda, const double *b, blasint ldb, double beta,
                  double *c, blasint ldc) {
-  // interface/gemm.c:374-471: row-major is the column-major product of the
-  // transposes, so A<->B, m<->n and transa<->transb swap.
-  int info = -1, ta = -1, tb = -1;
-  int64_t M = m, N = n;
-  const double *pa = a, *pb = b;
-  int64_t la = lda, lb = ldb;
-  if (order == CblasColMajor) {
-    ta = cblas_trans_code(TransA);
-    tb = cblas_trans_code(TransB);
-  } else if (order == CblasRowMajor) {
-    M = n;
-    N = m;
-    pa = b;
-    pb = a;
-    la = ldb;
-    lb = lda;
-    ta = cblas_trans_code(TransB);
-    tb = cblas_trans_code(TransA);
-  }
-  if (order == CblasColMajor || order == CblasRowMajor) {
-    info = gemm_check(ta, tb, M, N, k, la, lb, ldc);
-    if (info == 0) info = -1;
-  }
-  if (info >= 0) {
-    call_xerbla("DGEMM ", info);
-    return;
-  }
-  dgemm_blocking(ta, tb, M, N, k, alpha, pa, la, pb, lb, beta, c, ldc);
+  cblas_gemm_t<double, dgemm_blocking>(order, TransA, TransB, m, n, k, alpha, a, lda, b, ldb,
+                                       beta, c, ldc, "DGEMM ");
 }
 
 void cblas_sgemm(enum CBLAS_ORDER order, enum CBLAS_TRANSPOSE TransA,
                  enum CBLAS_TRANSPOSE TransB, blasint m, blasint n, blasint k, float alpha,
                  const float *a, blasint lda, const float *b, blasint ldb, float beta, float *c,
                  blasint ldc) {
-  int info = -1, ta = -1, tb = -1;
-  int64_t M = m, N = n;
-  const float *pa = a, *pb = b;
-  int64_t la = lda, lb = ldb;
-  if (order == CblasColMajor) {
-    ta = cblas_trans_code(TransA);
-    tb = cblas_trans_code(TransB);
-  } else if (order == CblasRowMajor) {
-    M = n;
-    N = m;
-    pa = b;
-    pb = a;
-    la = ldb;
-    lb = lda;
-    ta = cblas_trans_code(TransB);
-    tb = cblas_trans_code(TransA);
-  }
-  if (order == CblasColMajor || order == CblasRowMajor) {
-    info = gemm_check(ta, tb, M, N, k, la, lb, ldc);
-    if (info == 0) info = -1;
-  }
-  if (info >= 0) {
-    call_xerbla("SGEMM ", info);
-    return;
-  }
-  sgemm_blocking(ta, tb, M, N, k, alpha, pa, la, pb, lb, beta, c, ldc);
+  cblas_gemm_t<float, sgemm_blocking>(order, TransA, TransB, m, n, k, alpha, a, lda, b, ldb,
+                                      beta, c, ldc, "SGEMM ");
 }
 
 // ---------------------------------------------------------------------------

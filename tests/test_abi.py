@@ -77,6 +77,14 @@ def test_cblas_rowmajor_positions(gblib):
                    buf.ctypes.data, 4, buf.ctypes.data, 3, 0.0, buf.ctypes.data, 3)
     assert _xerbla(gblib) == ("DGEMM ", 10)
     gblib.gb_clear_error()
+    ns.cblas_sgemm(abi.CblasRowMajor, abi.CblasNoTrans, abi.CblasNoTrans, 4, 3, 5, 1.0,
+                   buf.ctypes.data, 4, buf.ctypes.data, 3, 0.0, buf.ctypes.data, 3)
+    assert _xerbla(gblib) == ("SGEMM ", 10)
+    gblib.gb_clear_error()
+    ns.cblas_sgemm(abi.CblasRowMajor, abi.CblasNoTrans, abi.CblasTrans, 4, 3, 5, 1.0,
+                   buf.ctypes.data, 5, buf.ctypes.data, 5, 0.0, buf.ctypes.data, 2)
+    assert _xerbla(gblib) == ("SGEMM ", 13)  # row-major C is m x n with ldc >= n
+    gblib.gb_clear_error()
     ns.cblas_dgemm(77, abi.CblasNoTrans, abi.CblasNoTrans, 4, 3, 5, 1.0, buf.ctypes.data, 4,
                    buf.ctypes.data, 5, 0.0, buf.ctypes.data, 4)
     assert _xerbla(gblib)[1] == 0  # invalid order: xerbla with position 0
