@@ -793,7 +793,16 @@ int gb_dgemm_batch_grouped(int order, const int *ta, const int *tb, const blasin
     }
   }
   Scratch dev(on_device ? 0 : elems * sizeof(double), s);
-  double *hbuf = nullptr;
+  // the pinned staging buffer and the plan, released on every return path
+  struct Held {
+    double *hbuf = nullptr;
+    void *plan = nullptr;
+    ~Held() {
+      if (plan) gb_batch_plan_destroy(plan);
+      if (hbuf) cudaFreeHost(hbuf);
+    }
+  } held;
+  double *&hbuf = held.hbuf;
   if (!on_device) {
     if (!dev.p) return GB_ERR_ALLOC;
     GB_CUDA(cudaMallocHost((void **)&hbuf, elems * sizeof(double)));
@@ -817,11 +826,8 @@ int gb_dgemm_batch_grouped(int order, const int *ta, const int *tb, const blasin
       if (p.ldb < 1) p.ldb = 1;
     }
   }
-  void *plan = gb_batch_plan_create(probs.data(), (int)probs.size(), 0);
-  if (!plan) {
-    if (hbuf) cudaFreeHost(hbuf);
-    return GB_ERR_CUDA;
-  }
+  void *plan = held.plan = gb_batch_plan_create(probs.data(), (int)probs.size(), 0);
+  if (!plan) return GB_ERR_CUDA;
   st = gb_batch_execute(plan);
   if (!st && !on_device) {
     GB_CUDA(cudaMemcpyAsync(hbuf, dev.p, elems * sizeof(double), cudaMemcpyDeviceToHost, s));
@@ -834,8 +840,6 @@ int gb_dgemm_batch_grouped(int order, const int *ta, const int *tb, const blasin
   } else if (!st) {
     st = finish_blocking(s);
   }
-  gb_batch_plan_destroy(plan);
-  if (hbuf) cudaFreeHost(hbuf);
   return st;
 }
 
