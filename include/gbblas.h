@@ -391,15 +391,20 @@ void gb_batch_plan_destroy(void *plan);
  * Same contract as gb_dgetrf_dev (native FP64 trailing updates), on the given
  * stream (NULL = the legacy default stream).  Its scratch is a 1 MiB
  * file-scope device array inside the library, held by every GPU that loads
- * the library until the process exits; it serves m <= 524288 rows, and larger
- * m is rejected with GB_ERR_UNSUPPORTED.  The first call on each device looks
- * up the array's device address with that device current; make that first
- * call before any stream capture.  All calls share the array: calls whose GPU
- * work overlaps (other streams, other threads) race and must be serialised by
- * the caller.  The status word of the panel kernel's bounded grid barrier
- * also lives in that array, so gb_synchronize does not report an expired
- * wait from this call (the barrier's blocks are co-resident by cooperative
- * launch, so it has no expected cause). */
+ * the library until the process exits.  The array has candidate slots for
+ * 1024 blocks of the grid-wide panel kernel, so m is limited to the rows one
+ * panel can cover on the device: 524288 at most, fewer where fewer of those
+ * blocks can be co-resident (the cluster panel covers up to 8192 rows without
+ * slots).  A larger m is rejected with GB_ERR_UNSUPPORTED before any work is
+ * queued; the error message states the device's limit.  The first call on
+ * each device looks up the array's device address with that device current;
+ * make that first call before any stream capture.  All calls share the array:
+ * calls whose GPU work overlaps (other streams, other threads) race and must
+ * be serialised by the caller.  The panel kernel's bounded grid barrier keeps
+ * its status word in that array too; if one of its waits ever gives up, the
+ * call sets *info to GB_INFO_WAIT_EXPIRED (a negative value no argument check
+ * produces) and the factors are incomplete. */
+#define GB_INFO_WAIT_EXPIRED (-1000)
 int gb_dgetrf_noalloc_dev(int64_t m, int64_t n, double *A, int64_t lda,
                           int *ipiv, int *info, void *stream);
 /* Mixed-precision solve (FP32 LU on the GPU + FP64 refinement, GMRES-IR

@@ -264,9 +264,7 @@ static void sgemm_blocking(int ta, int tb, int64_t m, int64_t n, int64_t k, floa
   finish_blocking(s);
 }
 
-// GEMM argument check shared by the Fortran and CBLAS forms
-// (interface/gemm.c:264-278, 409-418).  Returns the xerbla position or 0.
-
+// Device-side drivers defined in the other translation units.
 int dtrsm_device(int side, int uplo, int trans, int unit, int64_t m, int64_t n, double alpha,
                  const double *A, int64_t lda, double *B, int64_t ldb, cudaStream_t s);
 int dsyrk_device(int uplo, int trans, int64_t n, int64_t k, double alpha, const double *A,

@@ -1286,6 +1286,30 @@ int lu_scratch_address(void **out) {
   return GB_SUCCESS;
 }
 
+// Rows one panel can have on this device with the scratch above: the
+// cluster panel (no slots) or the cooperative panel, whose grid is capped
+// both by co-residency and by the NOALLOC_MAX_BLOCKS candidate slots.
+int64_t noalloc_row_limit() {
+  const ClusterPanel<double> caps = cluster_panel_caps<double>();
+  const int64_t cl = caps.max_cs >= 2 ? (int64_t)caps.max_cs * CPANEL_THREADS * caps.lmax : 0;
+  const int64_t b1 = coop_limit<double, 1>() < NOALLOC_MAX_BLOCKS ? coop_limit<double, 1>()
+                                                                   : NOALLOC_MAX_BLOCKS;
+  const int64_t b2 = coop_limit<double, 2>() < NOALLOC_MAX_BLOCKS ? coop_limit<double, 2>()
+                                                                   : NOALLOC_MAX_BLOCKS;
+  int64_t lim = cl;
+  if (b1 * PANEL_THREADS > lim) lim = b1 * PANEL_THREADS;
+  if (b2 * 2 * PANEL_THREADS > lim) lim = b2 * 2 * PANEL_THREADS;
+  return lim;
+}
+
+// After the factorisation: a panel whose bounded grid barrier gave up left
+// its status in the shared array, which no other call reads; report it
+// through the caller's info word instead.
+__global__ void noalloc_status_to_info_kernel(const int *__restrict__ status,
+                                              int *__restrict__ info) {
+  if (blockIdx.x == 0 && threadIdx.x == 0 && status[0] != 0) *info = GB_INFO_WAIT_EXPIRED;
+}
+
 }  // namespace
 
 }  // namespace gb
@@ -1310,8 +1334,17 @@ extern "C" int gb_dgetrf_noalloc_dev(int64_t m, int64_t n, double *A, int64_t ld
   void *base = nullptr;
   int st = lu_scratch_address(&base);
   if (st) return st;
-  GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
   const int64_t mn = m < n ? m : n;
+  if (mn > 0) {
+    // the first panel has all m rows: refuse before any work is queued
+    const int64_t lim = noalloc_row_limit();
+    if (m > lim)
+      return set_error(GB_ERR_UNSUPPORTED,
+                       "gb_dgetrf_noalloc_dev: m = %lld exceeds the %lld rows one panel can "
+                       "have on this device with the fixed scratch",
+                       (long long)m, (long long)lim);
+  }
+  GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
   if (mn <= 0) return GB_SUCCESS;
   LuCtx<double> c;
   c.lim1 = coop_limit<double, 1>();
@@ -1334,6 +1367,7 @@ extern "C" int gb_dgetrf_noalloc_dev(int64_t m, int64_t n, double *A, int64_t ld
   // must start at zero (barrier counters are cleared again before every panel)
   GB_CUDA(cudaMemsetAsync(c.bar, 0, 32 * sizeof(unsigned) + 4 * sizeof(int), s));
   if ((st = lu_blocked<double>(c, m, mn, n))) return st;
+  { noalloc_status_to_info_kernel<<<1, 32, 0, s>>>(c.status, info); count_launch(); }
   return check_cuda(cudaGetLastError(), "gb_dgetrf_noalloc_dev");
 }
 

@@ -38,6 +38,45 @@ def uniform(seed: int, shape, lo: float = -1.0, hi: float = 1.0, offset: int = 0
     return (lo + (hi - lo) * u).reshape(shape, order="F")
 
 
+def _signed64(x: int) -> int:
+    return x - (1 << 64) if x >= (1 << 63) else x
+
+
+def uniform_device(seed: int, shape, device="cuda", lo: float = -1.0, hi: float = 1.0,
+                   chunk: int = 1 << 26):
+    """The same numbers as ``uniform`` generated by torch on ``device``.
+
+    Returns a torch float64 tensor holding the column-major matrix as its
+    transpose (``out.T`` is ``uniform(seed, shape)``; for a 1-D shape the
+    vector itself), so ``out.data_ptr()`` is a column-major buffer with
+    leading dimension ``shape[0]``.  The splitmix64 rounds run in int64
+    arithmetic (products wrap modulo 2^64, right shifts are masked to be
+    logical), in chunks of ``chunk`` elements to bound temporary memory.
+    """
+    import torch
+    shape = tuple(int(s) for s in (shape if isinstance(shape, (tuple, list)) else (shape,)))
+    n = int(np.prod(shape))
+    gold, m1, m2 = (_signed64(int(c)) for c in (_GOLD, _M1, _M2))
+    base = _signed64((seed * (1 << 32)) & 0xFFFFFFFFFFFFFFFF)
+
+    def lshr(z, s):
+        return (z >> s) & ((1 << (64 - s)) - 1)
+
+    out = torch.empty(n, dtype=torch.float64, device=device)
+    for c0 in range(0, n, chunk):
+        cn = min(chunk, n - c0)
+        z = torch.arange(c0 + 1, c0 + cn + 1, dtype=torch.int64, device=device) * gold + base
+        z = (z ^ lshr(z, 30)) * m1
+        z = (z ^ lshr(z, 27)) * m2
+        z = z ^ lshr(z, 31)
+        u = lshr(z, 11).to(torch.float64) * (2.0 ** -53)
+        out[c0:c0 + cn] = lo + (hi - lo) * u
+        del z, u
+    if len(shape) == 1:
+        return out
+    return out.view(shape[1], shape[0]) if len(shape) == 2 else out
+
+
 def randint(seed: int, shape, lo: int, hi: int) -> np.ndarray:
     """Integers uniform in [lo, hi] inclusive."""
     n = int(np.prod(shape))

@@ -3,15 +3,22 @@
 gb_dgetrf_noalloc_dev serves callers that cannot let a library allocate
 (their own arena owns HBM, a fixed memory budget, or no tolerance for the
 latency of cudaMalloc/cudaFree).  Its scratch lives in a fixed device array
-inside the library.  Here it is called through the C ABI twice in a row, on
-different matrices, and each result is checked against the allocating entry
-point gb_dgetrf_dev on the same input: identical pivots, identical info, and
-LU factors within the tolerance the LU tests use.  The file runs last so a
-failure here comes after every other test has run.
+inside the library.  Here it is called through the C ABI on several matrices
+in a row and each result is checked against the allocating entry point
+gb_dgetrf_dev on the same input: identical pivots, identical info, and LU
+factors within the tolerance the LU tests use.  Two of the matrices are
+taller than one FP64 thread-block cluster covers (8192 rows), so their panels
+run on the grid-wide kernel, the only reader and writer of the array's
+candidate slots and barrier words, one call right after the other.  Around
+every call the test reads the device's default memory pool (where the
+library's stream-ordered scratch comes from) and the free device memory: the
+call must make neither grow.  The file runs last so a failure here comes after
+every other test has run.
 """
 from __future__ import annotations
 
 import ctypes as C
+import ctypes.util
 
 import numpy as np
 import pytest
@@ -21,41 +28,119 @@ from openblas_gb300 import workloads as W
 pytestmark = pytest.mark.gpu
 
 GB_ERR_UNSUPPORTED = 6
+GB_INFO_WAIT_EXPIRED = -1000
+CU_MEMPOOL_ATTR_USED_MEM_CURRENT = 7
+CU_MEMPOOL_ATTR_USED_MEM_HIGH = 8
+
+CASES = [
+    (401, 1500, 1500, None),   # cluster panel
+    (402, 2100, 1700, 37),     # cluster panel, exact zero pivot at column 38
+    (403, 12000, 64, None),    # grid-wide panel (slots + barrier words)
+    (404, 10000, 96, 50),      # grid-wide panel again, exact zero pivot
+]
 
 
-def _factor(gblib, fn, A, stream_ptr):
-    torch = pytest.importorskip("torch")
+class DeviceMemory:
+    """Default memory pool usage and free memory of the current device,
+    read through the CUDA driver API (the pool is a driver object, so this
+    sees the library's cudaMallocAsync scratch whatever runtime it uses)."""
+
+    def __init__(self):
+        name = ctypes.util.find_library("cuda") or "libcuda.so.1"
+        self.cu = C.CDLL(name)
+        dev = C.c_int(0)
+        assert self.cu.cuCtxGetDevice(C.byref(dev)) == 0
+        self.pool = C.c_void_p()
+        assert self.cu.cuDeviceGetDefaultMemPool(C.byref(self.pool), dev) == 0
+
+    def _attr(self, a):
+        v = C.c_uint64(0)
+        assert self.cu.cuMemPoolGetAttribute(self.pool, a, C.byref(v)) == 0
+        return v.value
+
+    def reset_high(self):
+        zero = C.c_uint64(0)
+        assert self.cu.cuMemPoolSetAttribute(self.pool, CU_MEMPOOL_ATTR_USED_MEM_HIGH,
+                                             C.byref(zero)) == 0
+
+    def used(self):
+        return self._attr(CU_MEMPOOL_ATTR_USED_MEM_CURRENT)
+
+    def used_high(self):
+        return self._attr(CU_MEMPOOL_ATTR_USED_MEM_HIGH)
+
+    def free(self):
+        f, t = C.c_size_t(0), C.c_size_t(0)
+        assert self.cu.cuMemGetInfo_v2(C.byref(f), C.byref(t)) == 0
+        return f.value
+
+
+def _matrix(seed, m, n, zero_col):
+    A = W.uniform(seed, (m, n))
+    if zero_col is not None:
+        A[:, zero_col] = 0.0
+    return A
+
+
+def _buffers(torch, A):
     m, n = A.shape
     dA = torch.from_numpy(np.ascontiguousarray(A.T)).cuda()   # column-major buffer
     dp = torch.zeros(min(m, n), dtype=torch.int32, device="cuda")
     di = torch.full((1,), -7, dtype=torch.int32, device="cuda")
+    return dA, dp, di
+
+
+def _noalloc(gblib, torch, A, stream_ptr, mem=None):
+    m, n = A.shape
+    dA, dp, di = _buffers(torch, A)
     torch.cuda.synchronize()
-    if fn == "noalloc":
-        st = gblib.gb_dgetrf_noalloc_dev(m, n, dA.data_ptr(), m, dp.data_ptr(), di.data_ptr(),
-                                         C.c_void_p(stream_ptr))
-    else:
-        st = gblib.gb_dgetrf_dev(m, n, dA.data_ptr(), m, dp.data_ptr(), di.data_ptr())
+    if mem is not None:
+        mem.reset_high()
+        used0, free0 = mem.used(), mem.free()
+    st = gblib.gb_dgetrf_noalloc_dev(m, n, dA.data_ptr(), m, dp.data_ptr(), di.data_ptr(),
+                                     C.c_void_p(stream_ptr))
     assert st == 0
     torch.cuda.synchronize()
+    if mem is not None:
+        assert mem.used_high() <= used0, "the call allocated from the device memory pool"
+        assert mem.free() >= free0, "the call reduced the free device memory"
+    return dA.cpu().numpy().T, dp.cpu().numpy(), int(di.item())
+
+
+def _alloc(gblib, torch, A):
+    m, n = A.shape
+    dA, dp, di = _buffers(torch, A)
+    torch.cuda.synchronize()
+    assert gblib.gb_dgetrf_dev(m, n, dA.data_ptr(), m, dp.data_ptr(), di.data_ptr()) == 0
     assert gblib.gb_synchronize() == 0
+    torch.cuda.synchronize()
     return dA.cpu().numpy().T, dp.cpu().numpy(), int(di.item())
 
 
 def test_noalloc_lu_matches_allocating_entry(gblib):
     torch = pytest.importorskip("torch")
+    torch.cuda.init()
     stream = torch.cuda.Stream()
+    mats = [_matrix(seed, m, n, z) for seed, m, n, z in CASES]
+    # the allocating results first, so nothing of that path runs between the
+    # no-allocation calls below
     gblib.gb_set_stream(C.c_void_p(stream.cuda_stream))
     try:
-        for seed, (m, n) in ((401, (1500, 1500)), (402, (2100, 1700))):
-            A = W.uniform(seed, (m, n))
-            A[:, 37] *= 0.0 if seed == 402 else 1.0  # second call: an exact zero pivot
-            LUn, pn, in_ = _factor(gblib, "noalloc", A, stream.cuda_stream)
-            LUa, pa, ia = _factor(gblib, "alloc", A, stream.cuda_stream)
-            assert in_ == ia
-            assert np.array_equal(pn, pa)
-            assert np.max(np.abs(LUn - LUa)) <= 1e-12 * max(1.0, np.abs(LUa).max())
+        ref = [_alloc(gblib, torch, A) for A in mats]
     finally:
         gblib.gb_set_stream(None)
+    # first pass: per-device set-up (symbol address, occupancy queries) and
+    # the first launch of each kernel; second pass: the measured calls, back
+    # to back, every one checked for allocations
+    for A in mats:
+        _noalloc(gblib, torch, A, stream.cuda_stream)
+    mem = DeviceMemory()
+    for A, (LUa, pa, ia) in zip(mats, ref):
+        LUn, pn, in_ = _noalloc(gblib, torch, A, stream.cuda_stream, mem)
+        assert in_ != GB_INFO_WAIT_EXPIRED
+        assert in_ == ia
+        assert np.array_equal(pn, pa)
+        assert np.max(np.abs(LUn - LUa)) <= 1e-12 * max(1.0, np.abs(LUa).max())
 
 
 def test_noalloc_rejects_sizes_beyond_its_scratch(gblib):
@@ -64,3 +149,31 @@ def test_noalloc_rejects_sizes_beyond_its_scratch(gblib):
     st = gblib.gb_dgetrf_noalloc_dev(m, 4, dummy, m, dummy, dummy, dummy)
     assert st == GB_ERR_UNSUPPORTED
     gblib.gb_clear_error()
+
+
+def test_noalloc_checks_the_device_row_limit_before_any_work(gblib):
+    """m = 524288 passes the array's own bound, but one panel of that height
+    needs 1024 co-resident blocks of the grid-wide kernel (two rows per
+    thread); a device that cannot hold them rejects the call at entry.  Real
+    buffers, so a device that can hold them simply factors the matrix."""
+    torch = pytest.importorskip("torch")
+    import openblas_gb300 as gb
+    m, n = 524288, 4
+    dA = torch.zeros((n, m), dtype=torch.float64, device="cuda")
+    dA[0, :] = 1.0
+    dA.diagonal().fill_(2.0)
+    dp = torch.zeros(n, dtype=torch.int32, device="cuda")
+    di = torch.full((1,), -7, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    gblib.gb_clear_error()
+    st = gblib.gb_dgetrf_noalloc_dev(m, n, dA.data_ptr(), m, dp.data_ptr(), di.data_ptr(),
+                                     C.c_void_p(0))
+    if st == GB_ERR_UNSUPPORTED:
+        code, msg = gb.last_error(gblib)
+        assert code == GB_ERR_UNSUPPORTED and "on this device" in msg
+        assert int(di.item()) == -7          # nothing was queued
+        gblib.gb_clear_error()
+    else:
+        assert st == 0
+        torch.cuda.synchronize()
+        assert int(di.item()) == 0
