@@ -42,7 +42,9 @@ def parse_args():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--n", type=int, default=8192)
-    ap.add_argument("--slices", type=int, default=7)
+    ap.add_argument("--slices", type=int, default=0,
+                    help="8-bit slices of the emulated DGEMM (0: chosen from the operands and "
+                         "the accuracy target, the library default)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the DGESV and batched legs (profiling runs)")
     ap.add_argument("--suite", action="store_true",
@@ -52,10 +54,11 @@ def parse_args():
 
 
 def workload_config(n, slices):
+    how = f"{slices} 8-bit slices" if slices > 0 else "8-bit slices chosen for 8 eps"
     return {
         "workload": f"DGEMM NN M=N=K={n}, alpha=1, beta=0, A,B,C uniform(-1,1) seeded; "
-                    f"FP64-accuracy emulation with {slices} 8-bit slices vs native FP64",
-        "m": n, "n": n, "k": n, "transa": "N", "transb": "N", "slices": slices,
+                    f"FP64-accuracy emulation ({how}) vs native FP64",
+        "m": n, "n": n, "k": n, "transa": "N", "transb": "N", "slices": slices or "auto",
         "l2": "inputs larger than L2 (3 x 512 MiB), no flush",
         "parallelism": "replicas",
     }
@@ -345,13 +348,19 @@ def run_suite(args):
                                               Ba.data_ptr(), n, 0.0, Ga.data_ptr(), n))
                 del Aa, Ba
             Ce = torch.empty((n, n), dtype=torch.float64, device="cuda")
-            for S in ((5, 6, 7, 8) if n == 8192 else (7,)):
+            # S = 0: the automatic count (the library default), recorded as chosen
+            for S in ((0, 5, 6, 7, 8) if n == 8192 else (0, 7)):
                 ms = _time_dev(torch, stream, lambda: check(lib.gb_dgemm_emulated_dev(
                     b"N", b"N", n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.0,
                     Ce.data_ptr(), n, S)), reps=3 if n == 8192 else 2)
-                d = {"suite": f"dgemm_emulated_{n}_e{e}_s{S}",
-                     "workload": f"emulated DGEMM NN {n}^3, A,B = U.*2^E, E in [-{e},{e}], {S} slices",
+                tag = f"s{S}" if S else "auto"
+                how = f"{S} slices" if S else \
+                    f"automatic count ({lib.gb_last_ozaki_slices()} slices chosen)"
+                d = {"suite": f"dgemm_emulated_{n}_e{e}_{tag}",
+                     "workload": f"emulated DGEMM NN {n}^3, A,B = U.*2^E, E in [-{e},{e}], {how}",
                      "value": 2 * n ** 3 / ms / 1e9, "unit": UNIT, "ms": ms}
+                if not S:
+                    d["slices_chosen"] = lib.gb_last_ozaki_slices()
                 if Cn is not None:
                     torch.cuda.synchronize()
                     diff = (Ce - Cn).abs()
@@ -837,6 +846,7 @@ def main():
     for _ in range(args.warmup):
         emulated_step()
     torch.cuda.synchronize()
+    S_used = S if S > 0 else lib.gb_last_ozaki_slices()  # the count the step runs with
 
     clocks = ClockSampler(local)
     clocks.start()
@@ -927,7 +937,7 @@ def main():
     peaks, src = measured_peaks()
     # K runs in segments (4096 deep), one slice-GEMM launch per segment
     launches_per_step = max(cnt.value / args.steps, 1.0)
-    slice_flops = S * (S + 1) / 2 * flops / launches_per_step
+    slice_flops = S_used * (S_used + 1) / 2 * flops / launches_per_step
     achieved = slice_flops / (kern_ms * 1e-3) / 1e12
     peak = float(peaks.get("bf16_tflops_sustained", 1700.0))
     traffic, traffic_src = profiled_traffic(n)
@@ -936,7 +946,9 @@ def main():
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(n, S),
-        "precision": {"method": "ozaki-8bit-slices-bf16-tcgen05", "slices": S,
+        "precision": {"method": "ozaki-8bit-slices-bf16-tcgen05", "slices": S_used,
+                      "slice_choice": "fixed" if S > 0 else
+                      "automatic: smallest count whose worst-case bound is <= 8 eps",
                       "normwise_err_vs_native_fp64_eps": err_norm,
                       "componentwise_err_vs_native_fp64_eps": err_comp},
         "native_fp64": {"value": native_tflops * world, "unit": UNIT, "ms_per_step": native_ms,

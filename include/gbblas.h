@@ -261,8 +261,20 @@ int gb_get_dgemm_mode(void);
 #define GB_SGEMM_TENSOR 2 /* always the bf16x3 tensor-core form */
 int gb_set_sgemm_mode(int mode);
 int gb_get_sgemm_mode(void);
-/* Slice count of the emulated DGEMM (0 = chosen from K and accuracy target). */
+/* Slice count of the emulated DGEMM behind dgemm_/cblas_dgemm and the other
+ * caller-facing GEMMs (1..8 fixed).  0 (the default; GB_OZAKI_SLICES=auto)
+ * chooses the count per 256-column tile of C on the device: the smallest S
+ * for which a worst-case bound on every column's error,
+ *   sum_i |dC_ij| <= 2^-8S (T_e ||b_j||_1 + 2^f_j (T_1 + 7.06 k T_e)) + roundings,
+ * stays within GB_OZAKI_TOL (default 8) x 2^-52 times that column's
+ * sum_i (|A||B|)_ij (2^f_j: column j's scale, T_e: the sum of the rows'
+ * scales, T_1 = sum |A|, k: the K segment).  Uniform operands get 7 slices,
+ * operands whose entries span 2^16 or more get 8; 8 is the most there is.
+ * The LU/Cholesky trailing updates always use 7. */
 int gb_set_ozaki_slices(int slices);
+/* Largest slice count chosen by the calling thread's last automatic-mode
+ * emulated DGEMM (0 if none); synchronises the thread's stream. */
+int gb_last_ozaki_slices(void);
 /* Library version string. */
 const char *gb_version(void);
 
@@ -287,7 +299,7 @@ int gb_dgemm_native_dev(char transa, char transb, int64_t m, int64_t n,
                         const double *B, int64_t ldb, double beta, double *C,
                         int64_t ldc);
 /* Emulated FP64 GEMM with `slices` 8-bit slices per operand (1..8; 0 = the
- * default, 7: 56 bits, FP64-level accuracy). */
+ * thread's setting, automatic unless fixed by gb_set_ozaki_slices). */
 int gb_dgemm_emulated_dev(char transa, char transb, int64_t m, int64_t n,
                           int64_t k, double alpha, const double *A, int64_t lda,
                           const double *B, int64_t ldb, double beta, double *C,

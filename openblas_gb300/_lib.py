@@ -28,6 +28,7 @@ DEV_SIGS = {
     "gb_set_sgemm_mode": (_i, [_i]),
     "gb_get_sgemm_mode": (_i, []),
     "gb_set_ozaki_slices": (_i, [_i]),
+    "gb_last_ozaki_slices": (_i, []),
     "gb_version": (C.c_char_p, []),
     "gb_kernel_launches": (C.c_int64, []),
     "gb_profile_enable": (_i, [_i]),

@@ -81,7 +81,7 @@ static int dgemm_dispatch(int ta, int tb, int64_t m, int64_t n, int64_t k, doubl
                           double beta, double *C, int64_t ldc, cudaStream_t s) {
   if (dgemm_wants_emulated(m, n, k) && k > 0 && alpha != 0.0)
     return dgemm_emulated(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
-                          gb_get_ozaki_slices_internal(), s);
+                          ozaki_caller_slices(), s);
   return dgemm_native(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s);
 }
 
@@ -203,7 +203,7 @@ static int dgemm_host_pipelined(int ta, int tb, int64_t m, int64_t n, int64_t k,
     if ((st = p.upload(0))) return st;
     GB_CUDA(cudaStreamWaitEvent(p.s, a_up, 0));
     st = dgemm_emulated_blocked(ta, tb, m, n, k, alpha, dA, ra, beta,
-                                gb_get_ozaki_slices_internal(), p.nb, &p, p.s);
+                                ozaki_caller_slices(), p.nb, &p, p.s);
     // the staging buffer is released on the compute stream after the last download
     GB_CUDA(cudaEventRecord(out_done, p.cout));
     GB_CUDA(cudaStreamWaitEvent(p.s, out_done, 0));
@@ -830,7 +830,8 @@ int gb_dgemm_emulated_dev(char transa, char transb, int64_t m, int64_t n, int64_
     launch_dgemm_beta(m, n, beta, C, ldc, stream());
     return check_cuda(cudaGetLastError(), "dgemm_beta launch");
   }
-  return dgemm_emulated(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, slices, stream());
+  return dgemm_emulated(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
+                        slices > 0 ? slices : ozaki_caller_slices(), stream());
 }
 
 int gb_sgemm_dev(char transa, char transb, int64_t m, int64_t n, int64_t k, float alpha,

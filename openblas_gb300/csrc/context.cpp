@@ -69,6 +69,8 @@ const Config &config() {
     if (v) g_cfg.verbose = atoi(v);
     const char *sm = getenv("GB_SGEMM_MODE");
     if (sm) g_cfg.sgemm_mode = !strcmp(sm, "simt") ? 1 : !strcmp(sm, "tensor") ? 2 : 0;
+    const char *tol = getenv("GB_OZAKI_TOL");
+    if (tol && atof(tol) > 0.0) g_cfg.ozaki_tol = atof(tol);
     const char *g = getenv("GB_OZAKI_GROUP_M");
     if (g && atoi(g) > 0) g_cfg.ozaki_group_m = atoi(g);
   });
@@ -92,8 +94,8 @@ int ensure_init() {
     GB_CUDA(cudaStreamCreateWithFlags(&c.stream, cudaStreamNonBlocking));
   }
   if (!c.d_status) {
-    GB_CUDA(cudaMalloc(&c.d_status, sizeof(int) * 4));
-    GB_CUDA(cudaMemsetAsync(c.d_status, 0, sizeof(int) * 4, c.stream));
+    GB_CUDA(cudaMalloc(&c.d_status, sizeof(int) * STATUS_WORDS));
+    GB_CUDA(cudaMemsetAsync(c.d_status, 0, sizeof(int) * STATUS_WORDS, c.stream));
   }
   {
     std::lock_guard<std::mutex> lk(g_pool_mu);
@@ -323,6 +325,17 @@ int gb_get_ozaki_slices_internal(void) {
   return t_ozaki_slices >= 0 ? t_ozaki_slices : gb::config().ozaki_slices;
 }
 
+int gb_last_ozaki_slices(void) {
+  if (!gb::ctx().d_status || !gb::ctx().stream) return 0;
+  cudaError_t e = cudaStreamSynchronize(gb::stream());
+  if (e != cudaSuccess) return -gb::check_cuda(e, "gb_last_ozaki_slices");
+  int v = 0;
+  e = cudaMemcpy(&v, gb::ctx().d_status + gb::STATUS_LAST_SLICES, sizeof(int),
+                 cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return -gb::check_cuda(e, "gb_last_ozaki_slices");
+  return v;
+}
+
 const char *gb_version(void) { return "libgbblas 0.1 (sm_103a)"; }
 
 int64_t gb_kernel_launches(void) { return gb::g_launches.load(); }
@@ -354,3 +367,10 @@ double gb_profile_kernel_ms(const char *name, int *launches, int reset) {
 }
 
 }  // extern "C"
+
+namespace gb {
+int ozaki_caller_slices() {
+  const int s = gb_get_ozaki_slices_internal();
+  return s > 0 ? s : OZAKI_SLICES_AUTO;
+}
+}  // namespace gb

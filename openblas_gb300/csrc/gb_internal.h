@@ -32,10 +32,15 @@ struct Context {
   int device = -1;
   cudaStream_t stream = nullptr;     // library stream (or user stream)
   bool user_stream = false;
-  int *d_status = nullptr;           // device status word for kernel errors
+  int *d_status = nullptr;           // device status words (STATUS_WORDS ints, see below)
   cudaStream_t copy_in = nullptr;    // host->device uploads of pipelined calls
   cudaStream_t copy_out = nullptr;   // device->host downloads of pipelined calls
 };
+// d_status[0..3]: kernel error code and site (read and cleared by
+// gb_synchronize / the blocking entries); d_status[STATUS_LAST_SLICES]: the
+// largest slice count the last automatic-mode emulated DGEMM chose.
+constexpr int STATUS_WORDS = 8;
+constexpr int STATUS_LAST_SLICES = 4;
 Context &ctx();
 // Lazily initialise CUDA for this thread; returns GB_SUCCESS or an error.
 int ensure_init();
@@ -93,6 +98,7 @@ struct Config {
   int verbose = 0;                    // GB_VERBOSE
   int sgemm_mode = 0;                 // GB_SGEMM_MODE: 0 auto, 1 simt, 2 tensor
   int ozaki_group_m = 8;              // GB_OZAKI_GROUP_M: m-tiles per slice-GEMM tile group
+  double ozaki_tol = 8.0;             // GB_OZAKI_TOL: automatic slice count's bound, units of 2^-52
 };
 const Config &config();
 
@@ -135,8 +141,14 @@ void launch_sgemm_fp32(int ta, int tb, int64_t m, int64_t n, int64_t k, float al
 void launch_sgemm_fp32_tri(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha,
                            const float *A, int64_t lda, const float *B, int64_t ldb, float beta,
                            float *C, int64_t ldc, int tri, cudaStream_t s, const int *skip);
+// Slice count argument meaning "choose per 256-column tile of C from the
+// operands and the accuracy target" (see ozaki.cu).
+constexpr int OZAKI_SLICES_AUTO = -1;
+// The count for a caller-facing emulated GEMM: the thread's fixed setting
+// (gb_set_ozaki_slices / GB_OZAKI_SLICES), or OZAKI_SLICES_AUTO when unset/0.
+int ozaki_caller_slices();
 // Emulated-FP64 GEMM (Ozaki slices on the bf16 tensor cores).  slices = 0:
-// default count.  tri = 1 (2): only C(i,j) with i >= j (i <= j) is written,
+// default count (7); OZAKI_SLICES_AUTO: chosen on the device.  tri = 1 (2): only C(i,j) with i >= j (i <= j) is written,
 // tiles wholly in the other triangle are skipped (SYRK-shaped updates).
 // skip: device flag; when nonzero at run time C is left unchanged.
 int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,

@@ -54,7 +54,7 @@ int dgemm_select(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha, 
                  int tri, cudaStream_t s) {
   if (use_emulated(m, n, k))
     return dgemm_emulated(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc,
-                          gb_get_ozaki_slices_internal(), s, tri);
+                          ozaki_caller_slices(), s, tri);
   launch_dgemm_fp64_tri(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, s, nullptr);
   return check_cuda(cudaGetLastError(), "gemm launch");
 }

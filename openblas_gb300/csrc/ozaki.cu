@@ -71,6 +71,7 @@ struct GemmParams {
   int64_t plane_stride;
   int *planes;
   int *status;
+  const int *s_tiles;  // per n-tile slice count (automatic mode), or null: S everywhere
 };
 
 // Tile order: groups of group_m m-tiles, walked column by column inside a
@@ -135,7 +136,6 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
 
-  const int S = p.S;
   const int ntiles = p.m_tiles * p.n_tiles;
   const int nkc = (p.kblocks + KC_BLOCKS - 1) / KC_BLOCKS;
   auto fail = [&](int site) {
@@ -159,6 +159,7 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         int mt, nt;
         tile_coords(tile, p, mt, nt);
         if (!tile_active(mt, nt, p)) continue;
+        const int S = p.s_tiles ? p.s_tiles[nt] : p.S;
         for (int L = 2; ok && L <= S + 1; ++L) {
           const int s_lo = L - S > 1 ? L - S : 1, s_hi = L - 1 < S ? L - 1 : S;
           for (int s = s_lo; ok && s <= s_hi; ++s) {
@@ -205,6 +206,7 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         int mt, nt;
         tile_coords(tile, p, mt, nt);
         if (!tile_active(mt, nt, p)) continue;
+        const int S = p.s_tiles ? p.s_tiles[nt] : p.S;
         for (int L = 2; ok && L <= S + 1; ++L) {
           const int s_lo = L - S > 1 ? L - S : 1, s_hi = L - 1 < S ? L - 1 : S;
           for (int s = s_lo; ok && s <= s_hi; ++s) {
@@ -264,6 +266,7 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       int mt, nt;
       tile_coords(tile, p, mt, nt);
       if (!tile_active(mt, nt, p)) continue;
+      const int S = p.s_tiles ? p.s_tiles[nt] : p.S;
       const int64_t plane_tile = (int64_t)nt * p.m_tiles + mt;
       for (int L = 2; ok && L <= S + 1; ++L) {
 #pragma unroll
@@ -356,6 +359,184 @@ __global__ void rowmax_mcontig_kernel(int64_t R, int64_t K, const double *__rest
   atomicMax(out + r, best);
 }
 
+// ------------------------------------------------------------- slice choice
+// Automatic slice count (caller-facing GEMMs with no fixed count).  For one
+// K segment of length k, truncating row i of op(A) to S digits below 2^e_i
+// and column j of op(B) below 2^f_j, and dropping the products of levels
+// s + t >= S + 2, bounds the error of every C(i,j) by
+//   2^-8S (2^e_i ||b_j||_1 + 2^f_j ||a_i||_1 + c k 2^(e_i + f_j)),
+// c = (S - 1)(1 + 2^-7) <= 7.06 (at most S - 1 dropped pairs per level, each
+// below 2^16 of the level's unit, and a geometric tail), plus the final
+// roundings.  Summed over the rows of column j and set against that column's
+// sum of |A||B|, w_j = sum_k alpha_k |b_kj| with alpha_k = sum_i |a_ik|, the
+// ratio is 2^-8S rho_j with
+//   rho_j = (T_e ||b_j||_1 + 2^f_j (T_1 + c k T_e)) / w_j,
+// T_e = sum_i 2^e_i (over non-zero finite rows), T_1 = sum_k alpha_k.  Every
+// 256-column tile of C gets the smallest S whose 2^-8S max rho_j + (nseg + 2)
+// 2^-53 stays within the tolerance (GB_OZAKI_TOL, in units of 2^-52).  Rows and
+// columns with Inf/NaN are recomputed directly and left out.  A ratio that is
+// not finite (operands near the overflow or underflow threshold) gets the
+// largest count.  Digits are prefix-consistent (the first S digits of an
+// S'-digit split, S < S', are the S-digit split), so op(A) is split once with
+// MAX_SLICES digits and every tile uses the first S of them.
+constexpr double DROP_C = 7.0 * (1.0 + 1.0 / 128.0);
+
+// alpha_k = sum over the finite rows r of op(A) (R x K view) of |x_rk|.
+// KCONTIG (op(A) row r is K-contiguous): a thread per k, a chunk of rows per
+// blockIdx.y.  Otherwise a block per k, the rows read down the column.
+template <bool KCONTIG>
+__global__ void __launch_bounds__(256)
+abs_colsum_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
+                  const int *__restrict__ expo, int64_t rspan, double *__restrict__ alpha) {
+  if (KCONTIG) {
+    const int64_t kk = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (kk >= K) return;
+    const int64_t r0 = (int64_t)blockIdx.y * rspan;
+    const int64_t r1 = r0 + rspan < R ? r0 + rspan : R;
+    double s = 0.0;
+    for (int64_t r = r0; r < r1; ++r)
+      if (expo[r] != NONFINITE) s += fabs(X[kk + r * ld]);
+    atomicAdd(alpha + kk, s);
+  } else {
+    const int64_t kk = blockIdx.x;
+    const int64_t r0 = (int64_t)blockIdx.y * rspan;
+    const int64_t r1 = r0 + rspan < R ? r0 + rspan : R;
+    double s = 0.0;
+    for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
+      if (expo[r] != NONFINITE) s += fabs(X[r + kk * ld]);
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
+    __shared__ double part[8];
+    if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      double t = 0.0;
+      for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
+      atomicAdd(alpha + kk, t);
+    }
+  }
+}
+
+// totals[0] = T_e = sum of 2^e_r over the non-zero finite rows of op(A),
+// totals[1] = T_1 = sum_k alpha_k.  One block.
+__global__ void __launch_bounds__(256)
+a_totals_kernel(int64_t R, int64_t K, const int *__restrict__ expo,
+                const unsigned long long *__restrict__ mx, const double *__restrict__ alpha,
+                double *__restrict__ totals) {
+  double te = 0.0, t1 = 0.0;
+  for (int64_t r = threadIdx.x; r < R; r += blockDim.x)
+    if (mx[r] != 0 && expo[r] != NONFINITE) te += ldexp(1.0, expo[r]);
+  for (int64_t kk = threadIdx.x; kk < K; kk += blockDim.x) t1 += alpha[kk];
+  __shared__ double pe[256], p1[256];
+  pe[threadIdx.x] = te;
+  p1[threadIdx.x] = t1;
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) {
+      pe[threadIdx.x] += pe[threadIdx.x + h];
+      p1[threadIdx.x] += p1[threadIdx.x + h];
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    totals[0] = pe[0];
+    totals[1] = p1[0];
+  }
+}
+
+// The row maxima of op(B)'s R x K view (R = columns of op(B)) together with
+// the column sums ||b_j||_1 (s1) and w_j = sum_k alpha_k |b_kj| (s2).
+__global__ void rowmax_stats_kcontig_kernel(int64_t R, int64_t K, const double *__restrict__ X,
+                                            int64_t ld, const double *__restrict__ alpha,
+                                            unsigned long long *__restrict__ out,
+                                            double *__restrict__ s1, double *__restrict__ s2) {
+  const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  if (r >= R) return;
+  const double *x = X + r * ld;
+  unsigned long long best = 0;
+  double a1 = 0.0, a2 = 0.0;
+#pragma unroll 4
+  for (int64_t pp = lane; pp < K; pp += 32) {
+    const double v = fabs(x[pp]);
+    const unsigned long long b = __double_as_longlong(v);
+    best = b > best ? b : best;
+    a1 += v;
+    a2 = fma(alpha[pp], v, a2);
+  }
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    unsigned long long o = __shfl_down_sync(0xffffffffu, best, off);
+    best = o > best ? o : best;
+    a1 += __shfl_down_sync(0xffffffffu, a1, off);
+    a2 += __shfl_down_sync(0xffffffffu, a2, off);
+  }
+  if (lane == 0) {
+    out[r] = best;
+    s1[r] = a1;
+    s2[r] = a2;
+  }
+}
+
+__global__ void rowmax_stats_mcontig_kernel(int64_t R, int64_t K, const double *__restrict__ X,
+                                            int64_t ld, int64_t kspan,
+                                            const double *__restrict__ alpha,
+                                            unsigned long long *__restrict__ out,
+                                            double *__restrict__ s1, double *__restrict__ s2) {
+  const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (r >= R) return;
+  const int64_t p0 = (int64_t)blockIdx.y * kspan;
+  const int64_t p1 = p0 + kspan < K ? p0 + kspan : K;
+  unsigned long long best = 0;
+  double a1 = 0.0, a2 = 0.0;
+#pragma unroll 4
+  for (int64_t pp = p0; pp < p1; ++pp) {
+    const double v = fabs(X[r + pp * ld]);
+    const unsigned long long b = __double_as_longlong(v);
+    best = b > best ? b : best;
+    a1 += v;
+    a2 = fma(alpha[pp], v, a2);
+  }
+  atomicMax(out + r, best);
+  atomicAdd(s1 + r, a1);
+  atomicAdd(s2 + r, a2);
+}
+
+// One block per 256-column tile of C: the tile's largest rho_j and from it
+// the slice count; the largest count of the call is kept in *last.
+__global__ void __launch_bounds__(256)
+choose_slices_kernel(int64_t R, const int *__restrict__ expo,
+                     const unsigned long long *__restrict__ mx, const double *__restrict__ s1,
+                     const double *__restrict__ s2, const double *__restrict__ totals, int64_t k,
+                     double budget, int *__restrict__ s_tiles, int *__restrict__ last) {
+  const int64_t j = (int64_t)blockIdx.x * BN + threadIdx.x;
+  double rho = 0.0;
+  if (j < R && mx[j] != 0 && expo[j] != NONFINITE && s2[j] > 0.0) {
+    const double te = totals[0], t1 = totals[1];
+    rho = (te * s1[j] + ldexp(t1 + DROP_C * (double)k * te, expo[j])) / s2[j];
+    if (!(rho <= 1e300)) rho = 1e300;  // Inf or NaN: the largest count
+  } else if (j < R && mx[j] != 0 && expo[j] != NONFINITE && s2[j] != 0.0) {
+    rho = 1e300;  // w_j NaN
+  }
+  __shared__ double red[256];
+  red[threadIdx.x] = rho;
+  __syncthreads();
+  for (int h = 128; h > 0; h >>= 1) {
+    if ((int)threadIdx.x < h) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + h]);
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    int S = MAX_SLICES;
+    for (int c = 1; c < MAX_SLICES; ++c)
+      if (ldexp(red[0], -DIGIT_BITS * c) <= budget) {
+        S = c;
+        break;
+      }
+    s_tiles[blockIdx.x] = S;
+    atomicMax(last, S);
+  }
+}
+
 __global__ void exponent_kernel(int64_t Rpad, int64_t R, const unsigned long long *__restrict__ mx,
                                 int *__restrict__ expo) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -383,9 +564,10 @@ template <bool KCONTIG>
 __global__ void __launch_bounds__(256)
 split_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
              const int *__restrict__ expo, int S, int64_t Rpad, int64_t Kpad,
-             __nv_bfloat16 *__restrict__ slices) {
+             __nv_bfloat16 *__restrict__ slices, const int *__restrict__ s_tiles) {
   __shared__ double tile[32][65];
   const int64_t r0 = (int64_t)blockIdx.y * 32, p0 = (int64_t)blockIdx.x * 64;
+  if (s_tiles) S = s_tiles[r0 / BN];  // the slice count of this 256-row tile (automatic mode)
   const int tid = threadIdx.x;
   // all eight loads of a thread in flight before the shared-memory stores
   double vin[8];
@@ -486,14 +668,13 @@ __device__ __forceinline__ double level_value(__int128 acc, int S, int ei, int f
 // level sum are compile-time (S is a template argument).  Rows/columns with
 // Inf/NaN use a direct FP64 dot product so IEEE special values propagate.
 template <int S>
-__global__ void __launch_bounds__(256)
-recombine_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
-                      const int *__restrict__ planes, const int *__restrict__ ea,
-                      const int *__restrict__ eb, double alpha, double beta,
-                      double *__restrict__ C, int64_t ldc, int ta, int tb, int64_t k,
-                      const double *__restrict__ A, int64_t lda, const double *__restrict__ B,
-                      int64_t ldb, int tri, const int *__restrict__ skip) {
-  if (skip && *skip) return;  // a failed factorisation step upstream: leave C as it is
+__device__ __forceinline__ void
+recombine_tile(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
+               const int *__restrict__ planes, const int *__restrict__ ea,
+               const int *__restrict__ eb, double alpha, double beta,
+               double *__restrict__ C, int64_t ldc, int ta, int tb, int64_t k,
+               const double *__restrict__ A, int64_t lda, const double *__restrict__ B,
+               int64_t ldb, int tri) {
   const int mt = blockIdx.x, nt = blockIdx.y;
   const int64_t i0 = (int64_t)mt * BM, j0 = (int64_t)nt * BN;
   if (tri == 1 && i0 + BM - 1 < j0) return;  // tile wholly in the other triangle
@@ -541,6 +722,42 @@ recombine_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
   }
 }
 
+template <int S>
+__global__ void __launch_bounds__(256)
+recombine_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
+                      const int *__restrict__ planes, const int *__restrict__ ea,
+                      const int *__restrict__ eb, double alpha, double beta,
+                      double *__restrict__ C, int64_t ldc, int ta, int tb, int64_t k,
+                      const double *__restrict__ A, int64_t lda, const double *__restrict__ B,
+                      int64_t ldb, int tri, const int *__restrict__ skip) {
+  if (skip && *skip) return;  // a failed factorisation step upstream: leave C as it is
+  recombine_tile<S>(m, n, m_tiles, plane_stride, planes, ea, eb, alpha, beta, C, ldc, ta, tb, k,
+                    A, lda, B, ldb, tri);
+}
+
+// Automatic mode: each 256-column tile has its own slice count (s_tiles).
+__global__ void __launch_bounds__(256)
+recombine_auto_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
+                      const int *__restrict__ planes, const int *__restrict__ ea,
+                      const int *__restrict__ eb, double alpha, double beta,
+                      double *__restrict__ C, int64_t ldc, int ta, int tb, int64_t k,
+                      const double *__restrict__ A, int64_t lda, const double *__restrict__ B,
+                      int64_t ldb, int tri, const int *__restrict__ skip,
+                      const int *__restrict__ s_tiles) {
+  if (skip && *skip) return;
+  switch (s_tiles[blockIdx.y]) {
+#define GB_RECOMBINE_CASE(SS)                                                                  \
+  case SS:                                                                                     \
+    recombine_tile<SS>(m, n, m_tiles, plane_stride, planes, ea, eb, alpha, beta, C, ldc, ta,   \
+                       tb, k, A, lda, B, ldb, tri);                                            \
+    break;
+    GB_RECOMBINE_CASE(1) GB_RECOMBINE_CASE(2) GB_RECOMBINE_CASE(3) GB_RECOMBINE_CASE(4)
+    GB_RECOMBINE_CASE(5) GB_RECOMBINE_CASE(6) GB_RECOMBINE_CASE(7) GB_RECOMBINE_CASE(8)
+#undef GB_RECOMBINE_CASE
+    default: break;
+  }
+}
+
 // ------------------------------------------------------------------ host
 // 2-D tensor map over `rows` x `kpad` bf16 (K innermost), box 64 x box_rows.
 int make_map(CUtensorMap *map, void *base, int64_t rows, int64_t kpad, int box_rows) {
@@ -549,6 +766,16 @@ int make_map(CUtensorMap *map, void *base, int64_t rows, int64_t kpad, int box_r
 
 inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
+
+void launch_split(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld,
+                  const int *expo, int S, int64_t Rpad, int64_t Kpad, __nv_bfloat16 *slices,
+                  const int *s_tiles, cudaStream_t s) {
+  dim3 g2((unsigned)(Kpad / 64), (unsigned)(Rpad / 32));
+  if (kcontig)
+    { split_kernel<true><<<g2, 256, 0, s>>>(R, K, X, ld, expo, S, Rpad, Kpad, slices, s_tiles); count_launch(); }
+  else
+    { split_kernel<false><<<g2, 256, 0, s>>>(R, K, X, ld, expo, S, Rpad, Kpad, slices, s_tiles); count_launch(); }
+}
 
 // Split an R x K op-view operand into S K-contiguous bf16 slices + exponents.
 void split_operand(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld, int S,
@@ -563,11 +790,48 @@ void split_operand(bool kcontig, int64_t R, int64_t K, const double *X, int64_t 
     { rowmax_mcontig_kernel<<<g, 256, 0, s>>>(R, K, X, ld, kspan, mx); count_launch(); }
   }
   { exponent_kernel<<<(unsigned)((Rpad + 255) / 256), 256, 0, s>>>(Rpad, R, mx, expo); count_launch(); }
-  dim3 g2((unsigned)(Kpad / 64), (unsigned)(Rpad / 32));
-  if (kcontig)
-    { split_kernel<true><<<g2, 256, 0, s>>>(R, K, X, ld, expo, S, Rpad, Kpad, slices); count_launch(); }
-  else
-    { split_kernel<false><<<g2, 256, 0, s>>>(R, K, X, ld, expo, S, Rpad, Kpad, slices); count_launch(); }
+  launch_split(kcontig, R, K, X, ld, expo, S, Rpad, Kpad, slices, nullptr, s);
+}
+
+// Automatic slice choice, op(A) side: the column sums alpha_k of |op(A)| and
+// the totals T_e, T_1 (after op(A)'s exponents are known).
+void a_side_stats(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld,
+                  const int *expo, const unsigned long long *mx, double *alpha, double *totals,
+                  cudaStream_t s) {
+  cudaMemsetAsync(alpha, 0, sizeof(double) * K, s);
+  const int64_t rspan = 1024;
+  if (kcontig) {
+    dim3 g((unsigned)((K + 255) / 256), (unsigned)((R + rspan - 1) / rspan));
+    { abs_colsum_kernel<true><<<g, 256, 0, s>>>(R, K, X, ld, expo, rspan, alpha); count_launch(); }
+  } else {
+    dim3 g((unsigned)K, (unsigned)((R + rspan - 1) / rspan));
+    { abs_colsum_kernel<false><<<g, 256, 0, s>>>(R, K, X, ld, expo, rspan, alpha); count_launch(); }
+  }
+  { a_totals_kernel<<<1, 256, 0, s>>>(R, K, expo, mx, alpha, totals); count_launch(); }
+}
+
+// Automatic slice choice, op(B) side: exponents and column statistics of
+// op(B) in one pass, the slice count of every 256-column tile, then the
+// split with those counts.
+void split_b_auto(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld,
+                  int64_t Rpad, int64_t Kpad, unsigned long long *mx, int *expo,
+                  const double *alpha, const double *totals, double *s1, double *s2,
+                  double budget, int *s_tiles, int *last, __nv_bfloat16 *slices, cudaStream_t s) {
+  cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * Rpad, s);
+  if (kcontig) {
+    { rowmax_stats_kcontig_kernel<<<(unsigned)((R + 7) / 8), 256, 0, s>>>(R, K, X, ld, alpha, mx,
+                                                                          s1, s2); count_launch(); }
+  } else {
+    cudaMemsetAsync(s1, 0, sizeof(double) * Rpad, s);
+    cudaMemsetAsync(s2, 0, sizeof(double) * Rpad, s);
+    const int64_t kspan = 256;
+    dim3 g((unsigned)((R + 255) / 256), (unsigned)((K + kspan - 1) / kspan));
+    { rowmax_stats_mcontig_kernel<<<g, 256, 0, s>>>(R, K, X, ld, kspan, alpha, mx, s1, s2); count_launch(); }
+  }
+  { exponent_kernel<<<(unsigned)((Rpad + 255) / 256), 256, 0, s>>>(Rpad, R, mx, expo); count_launch(); }
+  { choose_slices_kernel<<<(unsigned)(Rpad / BN), 256, 0, s>>>(R, expo, mx, s1, s2, totals, K,
+                                                                budget, s_tiles, last); count_launch(); }
+  launch_split(kcontig, R, K, X, ld, expo, MAX_SLICES, Rpad, Kpad, slices, s_tiles, s);
 }
 
 // The whole emulated product.  K is cut into segments of at most
@@ -585,15 +849,21 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
                      double *C, int64_t ldc, int S, cudaStream_t s, int tri, const int *skip,
                      int64_t nb = 0, EmuBlockHooks *hooks = nullptr) {
   if (nb <= 0 || nb >= n) nb = n;
+  const bool automatic = S == OZAKI_SLICES_AUTO;
+  const int Sa = automatic ? MAX_SLICES : S;  // slices allocated (and cut from op(A))
   const int64_t kseg = k < MAX_K_SEGMENT ? k : MAX_K_SEGMENT;
   const int64_t nseg = (k + MAX_K_SEGMENT - 1) / MAX_K_SEGMENT;
   const int64_t m_pad = round_up(m, BM), nb_pad = round_up(nb, BN), ks_pad = round_up(kseg, BK);
-  const size_t bytes_sa = align256((size_t)S * m_pad * ks_pad * 2);
-  const size_t bytes_sb = align256((size_t)S * nb_pad * ks_pad * 2);
+  const size_t bytes_sa = align256((size_t)Sa * m_pad * ks_pad * 2);
+  const size_t bytes_sb = align256((size_t)Sa * nb_pad * ks_pad * 2);
   const size_t bytes_mx = align256((size_t)(m_pad + nb_pad) * 8);
   const size_t bytes_e = align256((size_t)(m_pad + nb_pad) * 4);
-  const size_t bytes_pl = align256((size_t)S * m_pad * nb_pad * 4);
-  Scratch ws(bytes_sa + bytes_sb + bytes_mx + bytes_e + bytes_pl, s);
+  const size_t bytes_pl = align256((size_t)Sa * m_pad * nb_pad * 4);
+  // automatic mode: alpha_k, the two op(A) totals, the column sums of op(B)
+  // and the per-tile slice counts
+  const size_t bytes_auto =
+      automatic ? align256((size_t)(ks_pad + 2 + 2 * nb_pad) * 8 + (size_t)(nb_pad / BN) * 4) : 0;
+  Scratch ws(bytes_sa + bytes_sb + bytes_mx + bytes_e + bytes_pl + bytes_auto, s);
   if (!ws.p) return GB_ERR_ALLOC;
   char *base = ws.as<char>();
   __nv_bfloat16 *sla = reinterpret_cast<__nv_bfloat16 *>(base);
@@ -602,6 +872,20 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
   int *ea = reinterpret_cast<int *>(base + bytes_sa + bytes_sb + bytes_mx);
   int *eb = ea + m_pad;
   int *planes = reinterpret_cast<int *>(base + bytes_sa + bytes_sb + bytes_mx + bytes_e);
+  double *st_alpha = nullptr, *st_tot = nullptr, *st_s1 = nullptr, *st_s2 = nullptr;
+  int *s_tiles = nullptr;
+  double budget = 0.0;
+  if (automatic) {
+    st_alpha = reinterpret_cast<double *>(base + bytes_sa + bytes_sb + bytes_mx + bytes_e +
+                                          bytes_pl);
+    st_tot = st_alpha + ks_pad;
+    st_s1 = st_tot + 2;
+    st_s2 = st_s1 + nb_pad;
+    s_tiles = reinterpret_cast<int *>(st_s2 + nb_pad);
+    // the tolerance in units of 2^-52 less the roundings of the recombine
+    // (one conversion, the alpha/beta step) and of the segment accumulation
+    budget = ldexp(config().ozaki_tol, -52) - ldexp((double)(nseg + 2), -53);
+  }
 
   static PerDeviceOnce attr_once;
   int st = attr_once.run(current_device(), [] {
@@ -614,8 +898,10 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
   // op(A) rows: K-contiguous when A is transposed; op(B) columns: K-contiguous when B is not
   auto split_a = [&](int64_t k0, int64_t kk) -> int {
     const int64_t kp = round_up(kk, BK);
-    split_operand(ta != 0, m, kk, ta ? A + k0 : A + k0 * lda, lda, S, m_pad, kp, mx, ea, sla, s);
-    return make_map(&mapA, sla, (int64_t)S * m_pad, kp, BM);
+    const double *Ak = ta ? A + k0 : A + k0 * lda;
+    split_operand(ta != 0, m, kk, Ak, lda, Sa, m_pad, kp, mx, ea, sla, s);
+    if (automatic) a_side_stats(ta != 0, m, kk, Ak, lda, ea, mx, st_alpha, st_tot, s);
+    return make_map(&mapA, sla, (int64_t)Sa * m_pad, kp, BM);
   };
   if (nseg == 1 && (st = split_a(0, k))) return st;
   for (int64_t j0 = 0; j0 < n; j0 += nb) {
@@ -632,10 +918,14 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       if (nseg > 1 && (st = split_a(k0, kk))) return st;
       const double *Ak = ta ? A + k0 : A + k0 * lda;
       const double *Bk = tb ? Bj + k0 * ldbj : Bj + k0;
-      split_operand(tb == 0, jn, kk, Bk, ldbj, S, jn_pad, kp, mx + m_pad, eb, slb, s);
-      if ((st = make_map(&mapB, slb, (int64_t)S * jn_pad, kp, BN))) return st;
+      if (automatic)
+        split_b_auto(tb == 0, jn, kk, Bk, ldbj, jn_pad, kp, mx + m_pad, eb, st_alpha, st_tot,
+                     st_s1, st_s2, budget, s_tiles, ctx().d_status + STATUS_LAST_SLICES, slb, s);
+      else
+        split_operand(tb == 0, jn, kk, Bk, ldbj, S, jn_pad, kp, mx + m_pad, eb, slb, s);
+      if ((st = make_map(&mapB, slb, (int64_t)Sa * jn_pad, kp, BN))) return st;
       GemmParams gp;
-      gp.S = S;
+      gp.S = Sa;
       gp.m_tiles = (int)(m_pad / BM);
       gp.n_tiles = (int)(jn_pad / BN);
       gp.group_m = config().ozaki_group_m;
@@ -648,6 +938,7 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       gp.plane_stride = m_pad * jn_pad;
       gp.planes = planes;
       gp.status = ctx().d_status;
+      gp.s_tiles = s_tiles;
       const int ntiles = gp.m_tiles * gp.n_tiles;
       const int grid = ntiles < sm_count() ? ntiles : sm_count();
       {
@@ -659,18 +950,24 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       const double bseg = sg == 0 ? beta : 1.0;  // later segments accumulate
       const dim3 g((unsigned)((m + BM - 1) / BM), (unsigned)((jn + BN - 1) / BN));
       const int64_t ps = gp.plane_stride;
+      if (automatic) {
+        recombine_auto_kernel<<<g, 256, 0, s>>>(m, jn, gp.m_tiles, ps, planes, ea, eb, alpha,
+                                                 bseg, Cj, ldcj, ta, tb, kk, Ak, lda, Bk, ldbj,
+                                                 tri, skip, s_tiles);
+      } else {
 #define GB_RECOMBINE(SS)                                                                        \
   case SS:                                                                                      \
     recombine_tile_kernel<SS><<<g, 256, 0, s>>>(m, jn, gp.m_tiles, ps, planes, ea, eb, alpha,   \
                                                 bseg, Cj, ldcj, ta, tb, kk, Ak, lda, Bk, ldbj,  \
                                                 tri, skip);                                     \
     break;
-      switch (S) {
-        GB_RECOMBINE(1) GB_RECOMBINE(2) GB_RECOMBINE(3) GB_RECOMBINE(4)
-        GB_RECOMBINE(5) GB_RECOMBINE(6) GB_RECOMBINE(7) GB_RECOMBINE(8)
-        default: return set_error(GB_ERR_UNSUPPORTED, "emulated dgemm: %d slices", S);
-      }
+        switch (S) {
+          GB_RECOMBINE(1) GB_RECOMBINE(2) GB_RECOMBINE(3) GB_RECOMBINE(4)
+          GB_RECOMBINE(5) GB_RECOMBINE(6) GB_RECOMBINE(7) GB_RECOMBINE(8)
+          default: return set_error(GB_ERR_UNSUPPORTED, "emulated dgemm: %d slices", S);
+        }
 #undef GB_RECOMBINE
+      }
       count_launch();
       if ((st = check_cuda(cudaGetLastError(), "emulated dgemm"))) return st;
     }
@@ -681,17 +978,29 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
 
 }  // namespace oz
 
-// Slice count used when the caller passes 0: 7 slices of 8-bit digits keep
-// 56 bits, FP64-level accuracy for operands whose rows/columns span a
-// moderate exponent range.
+// Slice count used when the caller passes 0 (the LU and Cholesky trailing
+// updates and panel solves): 7 slices of 8-bit digits keep 56 bits,
+// FP64-level accuracy for operands whose rows/columns span a moderate
+// exponent range.
 int ozaki_default_slices() { return 7; }
+
+// Resolves a requested slice count: > 0 fixed (at most MAX_SLICES), 0 the
+// default, OZAKI_SLICES_AUTO chosen per tile on the device (the record of
+// the largest count chosen is reset for the new call).
+static int resolve_slices(int slices, cudaStream_t s) {
+  if (slices == OZAKI_SLICES_AUTO) {
+    cudaMemsetAsync(ctx().d_status + STATUS_LAST_SLICES, 0, sizeof(int), s);
+    return OZAKI_SLICES_AUTO;
+  }
+  int S = slices > 0 ? slices : ozaki_default_slices();
+  return S > oz::MAX_SLICES ? oz::MAX_SLICES : S;
+}
 
 int dgemm_emulated_blocked(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
                            const double *A, int64_t lda, double beta, int slices, int64_t nb,
                            EmuBlockHooks *hooks, cudaStream_t s) {
-  int S = slices > 0 ? slices : ozaki_default_slices();
-  if (S > oz::MAX_SLICES) S = oz::MAX_SLICES;
   if (m <= 0 || n <= 0) return GB_SUCCESS;
+  const int S = resolve_slices(slices, s);
   if (m > (int64_t)1 << 22 || n > (int64_t)1 << 22)
     return set_error(GB_ERR_UNSUPPORTED, "blocked emulated dgemm: dimension too large");
   nb = (nb + oz::BN - 1) / oz::BN * oz::BN;
@@ -703,9 +1012,8 @@ int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha
                    const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
                    double *C, int64_t ldc, int slices, cudaStream_t s, int tri,
                    const int *skip) {
-  int S = slices > 0 ? slices : ozaki_default_slices();
-  if (S > oz::MAX_SLICES) S = oz::MAX_SLICES;
   if (m <= 0 || n <= 0) return GB_SUCCESS;
+  const int S = resolve_slices(slices, s);
   if ((m > GEMM_BLOCK_EXTENT || n > GEMM_BLOCK_EXTENT) && tri == 0 && !skip)
     return gemm_over_blocks(ta, tb, m, n, A, lda, B, ldb, C, ldc, GEMM_BLOCK_EXTENT,
                             [&](int64_t mb, int64_t nb, const double *Ai, const double *Bj,

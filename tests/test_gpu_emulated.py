@@ -221,3 +221,54 @@ def test_host_pipelined_pinned_buffers(emulated, gblib):
     ns.cblas_dgemm(102, 111, 111, m, n, k, 1.0, Ah.data_ptr(), m, Bh.data_ptr(), k, 0.0,
                    Ch.data_ptr(), m)
     assert np.array_equal(Ch.numpy().T, ref)
+
+
+def _column_normwise(Cg, Cref, G):
+    """max over columns of sum_i |Cg - Cref| / sum_i G: the measure the
+    automatic slice count bounds (G = |alpha||A||B| + |beta||C|)."""
+    d = np.abs(Cg - Cref).sum(axis=0)
+    g = G.sum(axis=0)
+    return float((d / np.where(g > 0, g, 1.0)).max())
+
+
+# automatic slice count (the default): 7 slices where 56 bits meet the bound,
+# 8 where the exponent spread needs them; the error stays within the
+# GB_OZAKI_TOL default of 8 eps, column-normwise and normwise
+@pytest.mark.parametrize("e,expect", [(0, 7), (8, 8), (16, 8)])
+def test_automatic_slice_count_meets_tolerance(orc, F, emulated, gblib, e, expect):
+    m = n = k = 1024
+    A = W.exponent_spread(40 + e, (m, k), e)
+    B = W.exponent_spread(50 + e, (k, n), e)
+    C = W.uniform(60, (m, n))
+    assert gblib.gb_set_ozaki_slices(0) == 0
+    Cg = C.copy(order="F")
+    F.dgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, Cg, m)
+    assert gblib.gb_last_ozaki_slices() == expect
+    Cref = C.copy(order="F")
+    orc.dgemm_dd("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, Cref, m)
+    G = orc.dgemm_absbound("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, C, m)
+    assert _column_normwise(Cg, Cref, G) <= 8 * EPS, _column_normwise(Cg, Cref, G) / EPS
+    assert _normwise(Cg, Cref, G) <= 8 * EPS, _normwise(Cg, Cref, G) / EPS
+
+
+def test_automatic_slice_count_per_column_tile(F, emulated, gblib):
+    """One 256-column tile of uniform columns next to one of exponent-spread
+    columns: each tile gets its own count, and because the first S digits of
+    an 8-digit split are the S-digit split, each tile's columns equal the
+    fixed-count result for its count bit for bit."""
+    m, k = 300, 700
+    A = W.uniform(70, (m, k))
+    B = np.asfortranarray(np.hstack([W.uniform(71, (k, 256)),
+                                     W.exponent_spread(72, (k, 200), 16)]))
+    n = B.shape[1]
+    out = {}
+    for s in (0, 7, 8):
+        assert gblib.gb_set_ozaki_slices(s) == 0
+        Cs = np.zeros((m, n), order="F")
+        F.dgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, Cs, m)
+        out[s] = Cs
+        if s == 0:
+            assert gblib.gb_last_ozaki_slices() == 8
+    gblib.gb_set_ozaki_slices(0)
+    assert np.array_equal(out[0][:, :256], out[7][:, :256])
+    assert np.array_equal(out[0][:, 256:], out[8][:, 256:])
