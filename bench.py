@@ -47,6 +47,9 @@ def parse_args():
                          "the accuracy target, the library default)")
     ap.add_argument("--no-extras", action="store_true",
                     help="skip the DGESV and batched legs (profiling runs)")
+    ap.add_argument("--peaks", action="store_true",
+                    help="measure the FP64 peak rates (DFMA, DMMA probes) and the native DGEMM's "
+                         "fraction of them instead of the headline step")
     ap.add_argument("--suite", action="store_true",
                     help="measure every configuration of the level-3/LAPACK sweep (one JSON "
                          "line each) instead of the headline step")
@@ -806,6 +809,45 @@ def batched_compare(lib, torch, gb, count=20000, loop_sample=1000):
 
 
 # --------------------------------------------------------------------------
+# FP64 peaks: the denominator of the native DGEMM's roofline
+# --------------------------------------------------------------------------
+def run_peaks(args):
+    """The FP64 rate of this GPU measured two ways (probe kernels of independent
+    DFMA chains and of mma.sync m8n8k4 f64 MMAs, one timed launch each after a
+    warm-up) and the library's native DGEMM NN at 4096^3 and 8192^3 against
+    the larger of the two (one JSON line)."""
+    import torch
+
+    import openblas_gb300 as gb
+    probes = C.CDLL(os.path.join(ROOT, "openblas_gb300", "libgbprobes.so"))
+    out = {"probe": "fp64 peaks", "unit": UNIT}
+    for name in ("dfma", "dmma"):
+        fn = getattr(probes, f"gbp_fp64_{name}_tflops")
+        fn.restype, fn.argtypes = C.c_int, [C.POINTER(C.c_double)]
+        v = C.c_double(0.0)
+        out[f"fp64_{name}"] = v.value if fn(C.byref(v)) == 0 else None
+    lib = gb.load()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    lib.gb_set_stream(C.c_void_p(stream.cuda_stream))
+    peak = max(x for x in (out["fp64_dfma"], out["fp64_dmma"]) if x)
+    clocks = ClockSampler(0)
+    clocks.start()
+    for n in (4096, 8192):
+        A = torch.rand((n, n), dtype=torch.float64, device="cuda") * 2 - 1
+        B = torch.rand((n, n), dtype=torch.float64, device="cuda") * 2 - 1
+        Cd = torch.empty((n, n), dtype=torch.float64, device="cuda")
+        ms = _time_dev(torch, stream, lambda: lib.gb_dgemm_native_dev(
+            b"N", b"N", n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.0, Cd.data_ptr(), n),
+            reps=2, warm=1)
+        out[f"native_dgemm_{n}"] = 2 * n ** 3 / ms / 1e9
+        out[f"native_dgemm_{n}_frac_of_fp64_peak"] = out[f"native_dgemm_{n}"] / peak
+        del A, B, Cd
+    out["clocks"] = clocks.stop()
+    print(json.dumps(out), flush=True)
+
+
+# --------------------------------------------------------------------------
 # main arm
 # --------------------------------------------------------------------------
 def main():
@@ -815,6 +857,9 @@ def main():
         return
     if args.suite:
         run_suite(args)
+        return
+    if args.peaks:
+        run_peaks(args)
         return
     import numpy as np
     import torch

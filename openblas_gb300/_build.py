@@ -76,5 +76,26 @@ def build(force: bool = False, verbose: bool = False) -> str:
     return SO
 
 
+PROBES = os.path.join(HERE, "probes")
+PROBES_SO = os.path.join(HERE, "libgbprobes.so")
+
+
+def build_probes(verbose: bool = False) -> str:
+    """libgbprobes.so: the peak-rate probes behind ``bench.py --peaks``
+    (measurement infrastructure, not part of the BLAS library)."""
+    srcs = sorted(glob.glob(os.path.join(PROBES, "*.cu")))
+    if os.path.exists(PROBES_SO) and os.path.getmtime(PROBES_SO) >= max(
+            os.path.getmtime(f) for f in srcs):
+        return PROBES_SO
+    cmd = [nvcc(), "-shared", "-o", PROBES_SO + ".tmp", "-O3", "-std=c++17", "-lineinfo",
+           "-Xcompiler", "-fPIC"] + srcs + ARCH + ["-lcudart"]
+    if verbose:
+        print(" ".join(cmd), file=sys.stderr)
+    subprocess.check_call(cmd)
+    os.replace(PROBES_SO + ".tmp", PROBES_SO)
+    return PROBES_SO
+
+
 if __name__ == "__main__":
     print(build(force="--force" in sys.argv, verbose="-v" in sys.argv))
+    print(build_probes(verbose="-v" in sys.argv))

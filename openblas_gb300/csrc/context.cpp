@@ -7,6 +7,7 @@
 // stream-ordered memory pool: concurrent callers never share a stream, and
 // scratch comes from cudaMallocAsync on that stream, cached by the pool.
 #include <cuda_runtime.h>
+#include <pthread.h>
 #include <stdarg.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -34,6 +35,19 @@ std::once_flag g_cfg_once;
 Config g_cfg;
 std::mutex g_pool_mu;
 bool g_pool_ready[64] = {false};
+
+// Fork safety (the reference re-initialises its memory pool in a forked
+// child, driver/others/memory.c:432-443 pthread_atfork).  A CUDA context does
+// not survive fork(): a child of a process that already called into CUDA
+// through this library cannot use the GPU, so the child is marked and every
+// entry point reports GB_ERR_NO_DEVICE with that reason instead of failing
+// in CUDA in an undefined way.
+std::atomic<int> g_cuda_touched{0};
+std::atomic<int> g_forked_child{0};
+std::once_flag g_atfork_once;
+void atfork_child() {
+  if (g_cuda_touched.load()) g_forked_child.store(1);
+}
 }  // namespace
 
 int set_error(int status, const char *fmt, ...) {
@@ -71,6 +85,8 @@ const Config &config() {
     if (sm) g_cfg.sgemm_mode = !strcmp(sm, "simt") ? 1 : !strcmp(sm, "tensor") ? 2 : 0;
     const char *tol = getenv("GB_OZAKI_TOL");
     if (tol && atof(tol) > 0.0) g_cfg.ozaki_tol = atof(tol);
+    const char *la = getenv("GB_LU_LOOKAHEAD");
+    if (la) g_cfg.lu_lookahead = atoi(la) != 0;
     const char *g = getenv("GB_OZAKI_GROUP_M");
     if (g && atoi(g) > 0) g_cfg.ozaki_group_m = atoi(g);
   });
@@ -80,6 +96,13 @@ const Config &config() {
 Context &ctx() { return t_ctx; }
 
 int ensure_init() {
+  std::call_once(g_atfork_once, [] { pthread_atfork(nullptr, nullptr, atfork_child); });
+  if (g_forked_child.load())
+    return set_error(GB_ERR_NO_DEVICE,
+                     "this process was forked after its parent used CUDA through libgbblas; a "
+                     "CUDA context does not survive fork(), so the child cannot use the GPU "
+                     "(fork before the first call, or use spawn)");
+  g_cuda_touched.store(1);
   Context &c = t_ctx;
   if (c.stream && c.d_status) return GB_SUCCESS;
   int dev = 0;
@@ -112,6 +135,29 @@ int ensure_init() {
 }
 
 cudaStream_t stream() { return t_ctx.stream; }
+
+int lookahead_streams(cudaStream_t *panel, cudaEvent_t *to_panel, cudaEvent_t *to_main) {
+  Context &c = t_ctx;
+  if (!c.panel) {
+    int least = 0, greatest = 0;
+    GB_CUDA(cudaDeviceGetStreamPriorityRange(&least, &greatest));
+    GB_CUDA(cudaStreamCreateWithPriority(&c.panel, cudaStreamNonBlocking, greatest));
+  }
+  for (int i = 0; i < 2; ++i)
+    if (!c.la_ev[i]) GB_CUDA(cudaEventCreateWithFlags(&c.la_ev[i], cudaEventDisableTiming));
+  *panel = c.panel;
+  *to_panel = c.la_ev[0];
+  *to_main = c.la_ev[1];
+  return GB_SUCCESS;
+}
+
+static thread_local int t_sm_reserve = 0;
+int persistent_ctas() {
+  const int n = sm_count() - t_sm_reserve;
+  return n > 0 ? n : 1;
+}
+SmReserve::SmReserve(int sms) : prev(t_sm_reserve) { t_sm_reserve = sms; }
+SmReserve::~SmReserve() { t_sm_reserve = prev; }
 
 int copy_streams(cudaStream_t *in, cudaStream_t *out) {
   Context &c = t_ctx;

@@ -35,6 +35,8 @@ struct Context {
   int *d_status = nullptr;           // device status words (STATUS_WORDS ints, see below)
   cudaStream_t copy_in = nullptr;    // host->device uploads of pipelined calls
   cudaStream_t copy_out = nullptr;   // device->host downloads of pipelined calls
+  cudaStream_t panel = nullptr;      // the LU's look-ahead panel stream (highest priority)
+  cudaEvent_t la_ev[2] = {nullptr, nullptr};  // ordering events between it and `stream`
 };
 // d_status[0..3]: kernel error code and site (read and cleared by
 // gb_synchronize / the blocking entries); d_status[STATUS_LAST_SLICES]: the
@@ -47,6 +49,19 @@ int ensure_init();
 cudaStream_t stream();
 // The two copy streams of this thread (created on first use).
 int copy_streams(cudaStream_t *in, cudaStream_t *out);
+// The look-ahead panel stream of this thread (highest priority) and its two
+// ordering events (created on first use).
+int lookahead_streams(cudaStream_t *panel, cudaEvent_t *to_panel, cudaEvent_t *to_main);
+
+// CTAs of a persistent (one CTA per SM) kernel launched by this thread: the
+// SM count less the SMs the thread keeps free for concurrent work (the LU's
+// look-ahead panel), set for a scope by SmReserve.
+int persistent_ctas();
+struct SmReserve {
+  int prev;
+  explicit SmReserve(int sms);
+  ~SmReserve();
+};
 
 // Stream-ordered device scratch (cudaMallocAsync from a pool that keeps its
 // memory cached between calls, so repeated calls do not hit the driver).
@@ -99,6 +114,7 @@ struct Config {
   int sgemm_mode = 0;                 // GB_SGEMM_MODE: 0 auto, 1 simt, 2 tensor
   int ozaki_group_m = 8;              // GB_OZAKI_GROUP_M: m-tiles per slice-GEMM tile group
   double ozaki_tol = 8.0;             // GB_OZAKI_TOL: automatic slice count's bound, units of 2^-52
+  int lu_lookahead = 1;               // GB_LU_LOOKAHEAD: factor the next LU panel ahead (0: off)
 };
 const Config &config();
 

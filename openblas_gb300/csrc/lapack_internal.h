@@ -12,6 +12,7 @@ constexpr int PANEL_NB = 32;
 // Kernel error codes written to the context status word.
 constexpr int GB_KERR_BARRIER_TIMEOUT = 1;
 constexpr int GB_KERR_MBARRIER_TIMEOUT = 2;
+constexpr int GB_KERR_CLUSTER_TIMEOUT = 4;  // a cluster panel CTA waited too long for a message
 constexpr int GB_KERR_CHAIN_TIMEOUT = 3;  // a solve block waited too long for its predecessor
 
 // LU with partial pivoting of an m x n matrix (device pointers).  ipiv gets

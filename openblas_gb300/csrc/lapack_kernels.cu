@@ -386,13 +386,15 @@ constexpr int CPANEL_WARPS = CPANEL_THREADS / 32;
 constexpr int CPANEL_MAX_CS = 16;       // one pushing warp per destination CTA
 
 // Shared memory of the cluster panel kernel: candidate inboxes (rows,
-// values, indices), per-warp candidate rows and row j, by column parity.
+// values, indices), per-warp candidate rows and row j, by column parity, and
+// the two inbox mbarriers.
 template <typename T>
 __host__ __device__ constexpr size_t cpanel_smem_bytes() {
   return (size_t)2 * (2 * CPANEL_MAX_CS + 2) * PANEL_NB * sizeof(T)  // inbox + warp rows, row j x2
          + (size_t)2 * (CPANEL_MAX_CS + CPANEL_WARPS) * sizeof(T)     // inbox/warp values
          + (size_t)2 * CPANEL_MAX_CS * sizeof(int) + 8                // inbox row indices
-         + (size_t)2 * CPANEL_WARPS * sizeof(long long) + 64;         // warp row indices
+         + (size_t)2 * CPANEL_WARPS * sizeof(long long) + 64          // warp row indices
+         + 2 * sizeof(unsigned long long) + 8;                        // inbox mbarriers
 }
 
 // First maximum of (value, row) pairs over a warp: the largest value, the
@@ -423,26 +425,85 @@ __device__ __forceinline__ void warp_argmax<float>(float &v, long long &i) {
   i = imin == 0xffffffffu ? LLONG_MAX : (long long)imin;
 }
 
+// Distributed-shared-memory messages of the cluster panel.  A value is stored
+// into another CTA's shared memory with st.async, which completes its bytes on
+// that CTA's mbarrier; the receiver waits on its own mbarrier only.
+__device__ __forceinline__ uint32_t cl_smem_addr(const void *local, int rank) {
+  uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(local)), r;
+  asm volatile("mapa.shared::cluster.u32 %0, %1, %2;" : "=r"(r) : "r"(a), "r"(rank));
+  return r;
+}
+__device__ __forceinline__ void st_async(uint32_t dst, float v, uint32_t mbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];"
+               ::"r"(dst), "r"(__float_as_uint(v)), "r"(mbar) : "memory");
+}
+__device__ __forceinline__ void st_async(uint32_t dst, double v, uint32_t mbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b64 [%0], %1, [%2];"
+               ::"r"(dst), "l"((unsigned long long)__double_as_longlong(v)), "r"(mbar)
+               : "memory");
+}
+__device__ __forceinline__ void st_async(uint32_t dst, int v, uint32_t mbar) {
+  asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];"
+               ::"r"(dst), "r"(v), "r"(mbar) : "memory");
+}
+__device__ __forceinline__ void cl_mbar_init(unsigned long long *bar, unsigned count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;"
+               ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(bar))), "r"(count)
+               : "memory");
+}
+__device__ __forceinline__ void cl_mbar_expect(unsigned long long *bar, unsigned bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;"
+               ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(bar))), "r"(bytes)
+               : "memory");
+}
+// Wait (acquire, cluster scope) for the phase of `parity` of a local
+// mbarrier; false after about `limit_ns` nanoseconds.
+__device__ __forceinline__ bool cl_mbar_wait(unsigned long long *bar, unsigned parity,
+                                             unsigned long long limit_ns) {
+  const uint32_t a = static_cast<uint32_t>(__cvta_generic_to_shared(bar));
+  unsigned long long t0 = 0;
+  for (unsigned i = 0;; ++i) {
+    uint32_t ok;
+    asm volatile(
+        "{\n .reg .pred p;\n"
+        " mbarrier.try_wait.parity.acquire.cluster.shared::cta.b64 p, [%1], %2;\n"
+        " selp.u32 %0, 1, 0, p;\n}\n"
+        : "=r"(ok) : "r"(a), "r"(parity) : "memory");
+    if (ok) return true;
+    if ((i & 63u) == 0) {
+      unsigned long long t;
+      asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+      if (i == 0) t0 = t;
+      else if (t - t0 > limit_ns) return false;
+    }
+  }
+}
+constexpr unsigned long long CPANEL_WAIT_NS = 2000000000ull;  // 2 s: never expected
+
 // Panel LU on one thread-block cluster (up to 16 CTAs of 512 threads).
 // Same algorithm and pivot rules as getf2_panel_kernel.  Each thread keeps
 // its L panel rows in registers (updates are predicated FMAs with
 // compile-time column indices; the pivot row is read with 16-byte shared
-// loads) and the per-column exchange goes through distributed shared memory
-// by pushing: the lane holding a warp's best row stages it in shared memory,
-// after one CTA barrier every warp knows the CTA's candidate (first maximum
-// of column j over its rows), and warp w writes that candidate -- value, row
-// index and the 32-element row -- into CTA w's inbox (row j is staged and
-// pushed the same way).  Remote stores are posted, so nothing waits on a
-// remote read; after the cluster barrier every CTA picks the pivot from its
-// own inbox.  Inboxes and slots alternate between two buffers by column
-// parity: a buffer is rewritten two columns later, after the barrier every
-// reader of the earlier column has passed.
-template <typename T, int L>
+// loads).  Per column: after one CTA barrier every warp knows the CTA's
+// candidate (first maximum of column j over its rows), and warp w sends that
+// candidate -- value, row index and the 32-element row -- into CTA w's inbox
+// with st.async (row j is sent the same way by the CTA that holds it).  Each
+// store completes its bytes on the receiving CTA's inbox mbarrier, so a CTA
+// waits for exactly its own CS messages and never for the whole cluster.
+// Inboxes and mbarriers alternate between two buffers by column parity.  A
+// buffer is written again two columns later; a CTA can only send for column
+// j+2 after it received every column j+1 message, and each CTA sends its
+// column j+1 messages after all its warps passed the CTA barrier of column
+// j+1, i.e. after they finished reading the column-j buffer.  Every wait is
+// bounded: a CTA that gives up records GB_KERR_CLUSTER_TIMEOUT, stops, waits
+// (bounded) for the messages of the columns it armed, and meets the others
+// at the final cluster barrier.
+template <typename T, int L, int NB>
 __global__ void __launch_bounds__(CPANEL_THREADS, 1)
 getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__restrict__ ipiv,
-                     int64_t row_off, int *__restrict__ info) {
-  static_assert(PANEL_NB == 32, "one lane per panel column");
-  static_assert(CPANEL_WARPS == CPANEL_MAX_CS, "one pushing warp per destination CTA");
+                     int64_t row_off, int *__restrict__ info, int *__restrict__ status) {
+  static_assert(NB <= PANEL_NB && NB % 4 == 0, "one lane per panel column");
+  static_assert(CPANEL_WARPS == CPANEL_MAX_CS, "one sending warp per destination CTA");
   namespace cg = cooperative_groups;
   cg::cluster_group cluster = cg::this_cluster();
   const int CS = (int)cluster.num_blocks();
@@ -457,6 +518,9 @@ getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__r
   int *in_idx = reinterpret_cast<int *>(red_val + 2 * CPANEL_WARPS);  // [2][CS]
   long long *red_idx = reinterpret_cast<long long *>(
       (reinterpret_cast<uintptr_t>(in_idx + 2 * CPANEL_MAX_CS) + 7) & ~uintptr_t(7));  // [2][WARPS]
+  unsigned long long *mbar = reinterpret_cast<unsigned long long *>(
+      red_idx + 2 * CPANEL_WARPS);                                                    // [2]
+  __shared__ int s_abort;
 
   const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
   // rows are dealt to the cluster's threads round robin: row r sits with
@@ -466,37 +530,50 @@ getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__r
   const int lg_nthr = __ffsll(nthr) - 1;
   const int64_t nmask = nthr - 1;
   const int64_t g = (int64_t)rank * CPANEL_THREADS + tid;
+  const int ncol = (int)(nb < m ? nb : m);
+  // bytes one CTA receives per column: CS candidates (row, value, index) and row j
+  const unsigned expect_bytes =
+      (unsigned)(CS * (NB * sizeof(T) + sizeof(T) + sizeof(int)) + NB * sizeof(T));
 
-  T r[L][PANEL_NB];
-  T colv[L];  // current value of column j of each row
+  T r[L][NB];
 #pragma unroll
   for (int q = 0; q < L; ++q) {
     const int64_t row = g + q * nthr;
 #pragma unroll
-    for (int c = 0; c < PANEL_NB; ++c) r[q][c] = (row < m && c < nb) ? A[row + c * lda] : T(0);
-    colv[q] = r[q][0];
+    for (int c = 0; c < NB; ++c) r[q][c] = (row < m && c < nb) ? A[row + c * lda] : T(0);
   }
-  cluster.sync();  // every CTA is running before anyone writes into its inbox
+  if (tid == 0) {
+    s_abort = 0;
+    cl_mbar_init(&mbar[0], 1);
+    cl_mbar_init(&mbar[1], 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    // arm the buffers of columns 0 and 1
+    if (ncol > 0) cl_mbar_expect(&mbar[0], expect_bytes);
+    if (ncol > 1) cl_mbar_expect(&mbar[1], expect_bytes);
+  }
+  cluster.sync();  // every CTA's mbarriers are armed before anyone sends
 
   // 32 values of one register row into shared memory, 16 bytes at a time
-  auto stage_row = [&](T *dst, const T (&src)[PANEL_NB]) {
+  auto stage_row = [&](T *dst, const T (&src)[NB]) {
     if (sizeof(T) == 4) {
 #pragma unroll
-      for (int c = 0; c < PANEL_NB; c += 4)
+      for (int c = 0; c < NB; c += 4)
         *reinterpret_cast<float4 *>(dst + c) =
             make_float4((float)src[c], (float)src[c + 1], (float)src[c + 2], (float)src[c + 3]);
     } else {
 #pragma unroll
-      for (int c = 0; c < PANEL_NB; c += 2)
+      for (int c = 0; c < NB; c += 2)
         *reinterpret_cast<double2 *>(dst + c) = make_double2((double)src[c], (double)src[c + 1]);
     }
   };
 
-  const int ncol = (int)(nb < m ? nb : m);
-  // fully unrolled over the 32 columns: every register index and the
-  // length of each row update (31 - j FMAs) are compile-time constants
+  int armed_to = ncol < 2 ? ncol : 2;  // columns whose inbox phase has been armed
+  int waited = 0;                      // columns whose messages have all arrived here
+  bool ok = true;
+  // fully unrolled over the NB columns: every register index and the
+  // length of each row update (NB - 1 - j FMAs) are compile-time constants
 #pragma unroll
-  for (int j = 0; j < PANEL_NB; ++j) {
+  for (int j = 0; j < NB; ++j) {
     if (j >= ncol) break;
     const int par = j & 1;
     // ---- local first maximum of |a_ij| over this thread's rows >= j
@@ -506,7 +583,7 @@ getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__r
     for (int q = 0; q < L; ++q) {
       const int64_t row = g + q * nthr;
       if (row < m && row >= j) {
-        T a = colv[q];
+        T a = r[q][j];  // j is a compile-time index in the unrolled loop
         a = a < T(0) ? -a : a;
         if (a > best || (a == best && row < bidx)) {
           best = a;
@@ -534,28 +611,52 @@ getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__r
         if (q == qj) stage_row(j_slot + par * PANEL_NB, r[q]);
     }
     __syncthreads();
-    // ---- every warp: the CTA's candidate; warp w pushes it (and row j) to CTA w
+    if (s_abort) {
+      ok = false;
+      break;
+    }
+    // ---- every warp: the CTA's candidate; warp w sends it (and row j) to CTA w
     T cb = lane < CPANEL_WARPS ? red_val[par * CPANEL_WARPS + lane] : T(-1);
     long long ci = lane < CPANEL_WARPS ? red_idx[par * CPANEL_WARPS + lane] : LLONG_MAX;
     warp_argmax<T>(cb, ci);
     if (warp < CS) {
       const int dst = warp;
       T rv = T(0);
-      if (ci != LLONG_MAX) {
+      if (ci != LLONG_MAX && lane < NB) {
         const int wb = (int)(((ci & nmask) - (int64_t)rank * CPANEL_THREADS) >> 5);
         rv = w_row[(par * CPANEL_WARPS + wb) * PANEL_NB + lane];
       }
-      *cluster.map_shared_rank(in_row + (par * CPANEL_MAX_CS + rank) * PANEL_NB + lane, dst) = rv;
+      const uint32_t rb = cl_smem_addr(&mbar[par], dst);
+      if (lane < NB)
+        st_async(cl_smem_addr(in_row + (par * CPANEL_MAX_CS + rank) * PANEL_NB + lane, dst), rv,
+                 rb);
       if (lane == 0) {
-        *cluster.map_shared_rank(in_val + par * CPANEL_MAX_CS + rank, dst) = cb;
-        *cluster.map_shared_rank(in_idx + par * CPANEL_MAX_CS + rank, dst) =
-            ci == LLONG_MAX ? -1 : (int)ci;
+        st_async(cl_smem_addr(in_val + par * CPANEL_MAX_CS + rank, dst), cb, rb);
+        st_async(cl_smem_addr(in_idx + par * CPANEL_MAX_CS + rank, dst),
+                 ci == LLONG_MAX ? -1 : (int)ci, rb);
       }
-      if (jowner == rank)
-        *cluster.map_shared_rank(in_rowj + par * PANEL_NB + lane, dst) =
-            j_slot[par * PANEL_NB + lane];
+      if (jowner == rank && lane < NB)
+        st_async(cl_smem_addr(in_rowj + par * PANEL_NB + lane, dst), j_slot[par * PANEL_NB + lane],
+                 rb);
     }
-    cluster.sync();  // every CTA's inbox for column j is complete
+    // ---- this CTA's inbox for column j is complete.  A thread that gives up
+    // raises s_abort and carries on with whatever the inbox holds (every index
+    // below stays in range); the whole CTA stops together after the next CTA
+    // barrier, before any message of the next column is sent.
+    const bool arrived = cl_mbar_wait(&mbar[par], (unsigned)((j >> 1) & 1), CPANEL_WAIT_NS);
+    if (!arrived) {
+      if (status) {
+        atomicCAS(status, 0, GB_KERR_CLUSTER_TIMEOUT);
+        atomicExch(status + 1, 200 + j);
+      }
+      s_abort = 1;
+    } else {
+      waited = j + 1;
+    }
+    if (arrived && tid == 0 && j + 2 < ncol) {
+      cl_mbar_expect(&mbar[par], expect_bytes);  // re-arm this buffer for column j + 2
+      armed_to = j + 3;
+    }
     // ---- global pivot from the local inbox (identical in every CTA)
     T gb = T(-1);
     long long gi = LLONG_MAX;
@@ -592,22 +693,21 @@ getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__r
       if (i >= m || i < j) continue;
       if (swap && i == j) {
 #pragma unroll
-        for (int c = 0; c < PANEL_NB; ++c)
+        for (int c = 0; c < NB; ++c)
           if (scaled || c > j) r[q][c] = u_v[c];
         continue;  // the pivot row is final
       }
       const bool take_j = swap && i == p;  // row p receives the old row j
       if (take_j) {
 #pragma unroll
-        for (int c = 0; c < PANEL_NB; ++c)
+        for (int c = 0; c < NB; ++c)
           if (scaled || c > j) r[q][c] = rowj_v[c];
       }
       if (i == j) continue;
-      T l = take_j ? rowj_v[j] : colv[q];
+      T l = take_j ? rowj_v[j] : r[q][j];
       if (scaled) l *= rcp;
-      T nx = T(0);
 #pragma unroll
-      for (int c = 0; c < PANEL_NB; c += 4) {
+      for (int c = 0; c < NB; c += 4) {
         T u4[4];
         if (sizeof(T) == 4) {
           const float4 f = *reinterpret_cast<const float4 *>(u_v + c);
@@ -622,19 +722,27 @@ getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__r
           const int cc = c + t;
           if (cc == j) r[q][cc] = l;
           else if (cc > j) r[q][cc] = fma(-l, u4[t], r[q][cc]);
-          if (cc == j + 1) nx = r[q][cc];
         }
       }
-      colv[q] = nx;
     }
   }
+  __syncthreads();
+  ok = ok && !s_abort;  // uniform across the CTA after the barrier
+  if (ok) {
 #pragma unroll
-  for (int q = 0; q < L; ++q) {
-    const int64_t row = g + q * nthr;
-    if (row >= m) continue;
+    for (int q = 0; q < L; ++q) {
+      const int64_t row = g + q * nthr;
+      if (row >= m) continue;
 #pragma unroll
-    for (int c = 0; c < PANEL_NB; ++c)
-      if (c < nb) A[row + c * lda] = r[q][c];
+      for (int c = 0; c < NB; ++c)
+        if (c < nb) A[row + c * lda] = r[q][c];
+    }
+  } else {
+    // gave up: let the messages of every armed column land (bounded) before
+    // this CTA's shared memory can go away
+    if (tid == 0)
+      for (int jj = waited; jj < armed_to; ++jj)
+        cl_mbar_wait(&mbar[jj & 1], (unsigned)((jj >> 1) & 1), CPANEL_WAIT_NS / 8);
   }
   cluster.sync();  // no CTA leaves while another may still write into its inbox
 }
@@ -642,26 +750,33 @@ getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__r
 template <typename T>
 struct ClusterPanel {
   int max_cs = 0;  // largest launchable cluster size (0: unavailable)
-  int lmax = 0;
+  int lmax = 0;    // register rows per thread of the 32-column kernel
+  int lmax16 = 0;  // register rows per thread of the 16-column kernel (FP32 only; 0: none)
 };
 
-// Largest cluster the panel kernel launches with on the current device.
+// Rows per thread held in registers: 32 columns x 2 rows (FP32) or 1 row
+// (FP64); for taller FP32 panels, 16 columns x 4 rows.
 template <typename T>
-ClusterPanel<T> probe_cluster_panel() {
-  ClusterPanel<T> caps;
-  // rows per thread held in registers: 2 for float, 1 for double
-  constexpr int lmax = sizeof(T) == 4 ? 2 : 1;
-  const size_t smem = cpanel_smem_bytes<T>();
-  auto kern = getf2_cluster_kernel<T, lmax>;
-  if (cudaFuncSetAttribute(kern, cudaFuncAttributeNonPortableClusterSizeAllowed, 1) !=
-      cudaSuccess) {
-    cudaGetLastError();
-    return caps;
-  }
-  if constexpr (lmax > 1)
-    cudaFuncSetAttribute(getf2_cluster_kernel<T, 1>, cudaFuncAttributeNonPortableClusterSizeAllowed,
-                         1);
+constexpr int cpanel_lmax() { return sizeof(T) == 4 ? 2 : 1; }
+template <typename T>
+constexpr int cpanel_lmax16() { return sizeof(T) == 4 ? 4 : 0; }
+
+template <typename T>
+void cpanel_allow_large_clusters() {
+  cudaFuncSetAttribute(getf2_cluster_kernel<T, 1, PANEL_NB>,
+                       cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if constexpr (cpanel_lmax<T>() > 1)
+    cudaFuncSetAttribute(getf2_cluster_kernel<T, cpanel_lmax<T>(), PANEL_NB>,
+                         cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
+  if constexpr (cpanel_lmax16<T>() > 0)
+    cudaFuncSetAttribute(getf2_cluster_kernel<T, cpanel_lmax16<T>(), 16>,
+                         cudaFuncAttributeNonPortableClusterSizeAllowed, 1);
   cudaGetLastError();
+}
+
+// Largest cluster size with at least one co-resident cluster of `kern`.
+template <typename K>
+int largest_cluster(K kern, size_t smem) {
   for (int cs = 16; cs >= 2; cs /= 2) {
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(cs);
@@ -675,16 +790,32 @@ ClusterPanel<T> probe_cluster_panel() {
     cfg.attrs = at;
     cfg.numAttrs = 1;
     int nclusters = 0;
-    if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg) == cudaSuccess && nclusters >= 1) {
-      caps.max_cs = cs;
-      caps.lmax = lmax;
-      break;
-    }
+    if (cudaOccupancyMaxActiveClusters(&nclusters, kern, &cfg) == cudaSuccess && nclusters >= 1)
+      return cs;
     cudaGetLastError();
   }
+  return 0;
+}
+
+// Largest cluster the panel kernel launches with on the current device.
+template <typename T>
+ClusterPanel<T> probe_cluster_panel() {
+  ClusterPanel<T> caps;
+  const size_t smem = cpanel_smem_bytes<T>();
+  cpanel_allow_large_clusters<T>();
+  caps.max_cs = largest_cluster(getf2_cluster_kernel<T, cpanel_lmax<T>(), PANEL_NB>, smem);
+  caps.lmax = caps.max_cs >= 2 ? cpanel_lmax<T>() : 0;
+  if constexpr (cpanel_lmax16<T>() > 0) {
+    // the 16-column kernel is used only with the same cluster size
+    if (caps.max_cs >= 2 &&
+        largest_cluster(getf2_cluster_kernel<T, cpanel_lmax16<T>(), 16>, smem) >= caps.max_cs)
+      caps.lmax16 = cpanel_lmax16<T>();
+  }
   if (config().verbose)
-    fprintf(stderr, "libgbblas: cluster panel (%s): max cluster %d CTAs, %d rows/thread\n",
-            sizeof(T) == 4 ? "fp32" : "fp64", caps.max_cs, caps.lmax);
+    fprintf(stderr,
+            "libgbblas: cluster panel (%s): max cluster %d CTAs, %d rows/thread (32 columns), "
+            "%d rows/thread (16 columns)\n",
+            sizeof(T) == 4 ? "fp32" : "fp64", caps.max_cs, caps.lmax, caps.lmax16);
   return caps;
 }
 
@@ -695,18 +826,31 @@ ClusterPanel<T> cluster_panel_caps() {
   return cache.get(current_device(), [] { return probe_cluster_panel<T>(); });
 }
 
+// Widest leaf (32 or 16 columns) whose cluster panel holds `rows` rows; 32
+// when neither does (the grid-wide kernel then takes 32 columns).
+template <typename T>
+int lu_leaf_width(int64_t rows) {
+  const ClusterPanel<T> caps = cluster_panel_caps<T>();
+  if (caps.max_cs < 2) return PANEL_NB;
+  const int64_t cap32 = (int64_t)caps.max_cs * CPANEL_THREADS * caps.lmax;
+  const int64_t cap16 = (int64_t)caps.max_cs * CPANEL_THREADS * caps.lmax16;
+  return (rows > cap32 && rows <= cap16) ? 16 : PANEL_NB;
+}
+
 // Launch the cluster panel when the panel fits one cluster; returns 1 when
 // it does not (the caller then uses the grid-wide kernel).
 template <typename T>
 int launch_cluster_panel(int64_t rows, int nb, T *A, int64_t lda, int *ipiv, int64_t row_off,
-                         int *info, cudaStream_t s) {
+                         int *info, int *status, cudaStream_t s) {
   const ClusterPanel<T> caps = cluster_panel_caps<T>();
   if (caps.max_cs < 2) return 1;
   int64_t cs = (rows + CPANEL_THREADS - 1) / CPANEL_THREADS;
   if (cs < 2) cs = 2;
   if (cs > caps.max_cs) cs = caps.max_cs;
   const int64_t L = (rows + cs * CPANEL_THREADS - 1) / (cs * CPANEL_THREADS);
-  if (L > caps.lmax) return 1;
+  // 16-column panels may take up to lmax16 rows per thread
+  const bool narrow = nb <= 16 && L > caps.lmax && L <= caps.lmax16;
+  if (L > caps.lmax && !narrow) return 1;
   // cluster sizes must divide the grid; use a power of two
   int csp = 2;
   while (csp < cs) csp *= 2;
@@ -725,13 +869,17 @@ int launch_cluster_panel(int64_t rows, int nb, T *A, int64_t lda, int *ipiv, int
   cfg.numAttrs = 1;
   count_launch();
   cudaError_t e = cudaErrorInvalidValue;
-  if (L == 1) {
-    e = cudaLaunchKernelEx(&cfg, getf2_cluster_kernel<T, 1>, rows, nb, A, lda, ipiv, row_off,
-                           info);
+  if (narrow) {
+    if constexpr (cpanel_lmax16<T>() > 0)
+      e = cudaLaunchKernelEx(&cfg, getf2_cluster_kernel<T, cpanel_lmax16<T>(), 16>, rows, nb, A,
+                             lda, ipiv, row_off, info, status);
+  } else if (L == 1) {
+    e = cudaLaunchKernelEx(&cfg, getf2_cluster_kernel<T, 1, PANEL_NB>, rows, nb, A, lda, ipiv,
+                           row_off, info, status);
   } else {
-    if constexpr (sizeof(T) == 4)
-      e = cudaLaunchKernelEx(&cfg, getf2_cluster_kernel<T, 2>, rows, nb, A, lda, ipiv, row_off,
-                             info);
+    if constexpr (cpanel_lmax<T>() > 1)
+      e = cudaLaunchKernelEx(&cfg, getf2_cluster_kernel<T, cpanel_lmax<T>(), PANEL_NB>, rows, nb,
+                             A, lda, ipiv, row_off, info, status);
   }
   return check_cuda(e, "cluster panel launch");
 }
@@ -1059,20 +1207,44 @@ struct LuCtx {
 };
 
 
+// The engine of a trailing update A22 -= A21 A12 of shape m x n x k: 1 for
+// the tensor-core form (emulated FP64 / bf16x3 FP32), 0 for the FMA units.
+// The look-ahead LU splits one update into column pieces and runs every
+// piece on the engine the whole update would use, so each element gets the
+// same arithmetic either way.
 template <typename T>
-int lu_update(LuCtx<T> &c, int64_t m, int64_t n, int64_t k, const T *A21, const T *A12, T *A22);
+int lu_update_engine(const LuCtx<T> &c, int64_t m, int64_t n, int64_t k);
+template <>
+int lu_update_engine<double>(const LuCtx<double> &c, int64_t m, int64_t n, int64_t k) {
+  return (c.gemm_mode == 1 && m >= 256 && n >= 256 && k >= 64) ? 1 : 0;
+}
+template <>
+int lu_update_engine<float>(const LuCtx<float> &, int64_t m, int64_t n, int64_t k) {
+  const int mode = gb_get_sgemm_mode();
+  return (mode == GB_SGEMM_TENSOR || (mode == GB_SGEMM_AUTO && m >= 1024 && n >= 1024 && k >= 64))
+             ? 1 : 0;
+}
+
+template <typename T>
+int lu_update(LuCtx<T> &c, int64_t m, int64_t n, int64_t k, const T *A21, const T *A12, T *A22,
+              int engine = -1);
 template <>
 int lu_update<double>(LuCtx<double> &c, int64_t m, int64_t n, int64_t k, const double *A21,
-                      const double *A12, double *A22) {
-  if (c.gemm_mode == 1 && m >= 256 && n >= 256 && k >= 64)
+                      const double *A12, double *A22, int engine) {
+  if (engine < 0) engine = lu_update_engine<double>(c, m, n, k);
+  if (engine == 1)
     return dgemm_emulated(0, 0, m, n, k, -1.0, A21, c.lda, A12, c.lda, 1.0, A22, c.lda, 0, c.s);
   gemm_minus<double>(m, n, k, A21, c.lda, A12, c.lda, A22, c.lda, c.s);
   return GB_SUCCESS;
 }
 template <>
 int lu_update<float>(LuCtx<float> &c, int64_t m, int64_t n, int64_t k, const float *A21,
-                     const float *A12, float *A22) {
-  return sgemm_dispatch(0, 0, m, n, k, -1.0f, A21, c.lda, A12, c.lda, 1.0f, A22, c.lda, c.s);
+                     const float *A12, float *A22, int engine) {
+  if (engine < 0) engine = lu_update_engine<float>(c, m, n, k);
+  if (engine == 1)
+    return sgemm_tc(0, 0, m, n, k, -1.0f, A21, c.lda, A12, c.lda, 1.0f, A22, c.lda, c.s);
+  launch_sgemm_fp32(0, 0, m, n, k, -1.0f, A21, c.lda, A12, c.lda, 1.0f, A22, c.lda, c.s);
+  return check_cuda(cudaGetLastError(), "sgemm launch");
 }
 
 template <typename T>
@@ -1081,7 +1253,8 @@ int lu_panel_factor(LuCtx<T> &c, int64_t r0, int64_t m, int n) {
   T *P = c.A + r0 + r0 * c.lda;
   if (c.use_cluster) {
     ProfileScope pc("lu_panel_cluster", c.s);
-    const int st = launch_cluster_panel<T>(m, n, P, c.lda, c.ipiv + r0, r0, c.info, c.s);
+    const int st = launch_cluster_panel<T>(m, n, P, c.lda, c.ipiv + r0, r0, c.info, c.status,
+                                           c.s);
     if (st != 1) return st;
   }
   GB_CUDA(cudaMemsetAsync(c.bar, 0, 2 * sizeof(unsigned), c.s));
@@ -1126,9 +1299,12 @@ int lu_panel(LuCtx<T> &c, int64_t r0, int64_t m, int n) {
 // Factor the m x n block whose top-left corner is the diagonal entry (r0, r0); n <= m.
 template <typename T>
 int lu_rec(LuCtx<T> &c, int64_t r0, int64_t m, int64_t n) {
-  if (n <= PANEL_NB) return lu_panel<T>(c, r0, m, (int)n);
-  int64_t n1 = (n / 2) / PANEL_NB * PANEL_NB;
-  if (n1 < PANEL_NB) n1 = PANEL_NB;
+  // leaves of 32 columns, or 16 where a 32-column panel of m rows is too
+  // tall for one cluster but a 16-column one fits (FP32)
+  const int64_t leaf = c.use_cluster ? lu_leaf_width<T>(m) : PANEL_NB;
+  if (n <= leaf) return lu_panel<T>(c, r0, m, (int)n);
+  int64_t n1 = (n / 2) / leaf * leaf;
+  if (n1 < leaf) n1 = leaf;
   const int64_t lda = c.lda;
   int st;
   // the left half's interchanges reach the right half inside lu_panel
@@ -1199,6 +1375,93 @@ int lu_blocked(LuCtx<T> &c, int64_t m, int64_t mn, int64_t n) {
   return GB_SUCCESS;
 }
 
+// Right-looking blocked LU with a look-ahead of one block (the structure of
+// lapack/getrf/getrf_parallel.c, where the thread that owns the next panel
+// factors it as soon as its columns are updated, inner_advanced_thread, while
+// the others finish the trailing update).  Block J+1's columns (the "slab")
+// get block J's interchanges, triangular solve and update first, on the main
+// stream; then block J+1 is factored on the highest-priority panel stream
+// while the main stream applies block J's interchanges, solve and update to
+// the remaining columns and its interchanges to the finished columns on the
+// left.  Persistent GEMM kernels on the main stream leave SMs free for the
+// panel meanwhile.  Every element sees exactly the operations of lu_blocked
+// in the same order, so the factors and pivots are the same; the panels'
+// interchanges reach their own block only, the rest being applied by the
+// main stream once no kernel reads those rows.
+//   main:   ... G(J-1, rest) | wait P(J) | X,T,G(J, slab) -> | X,T,G(J, rest), X(J, left) | ...
+//   panel:  P(J) ------------------------------------------ | wait | P(J+1) -------------- |
+template <typename T>
+int lu_blocked_lookahead(LuCtx<T> &c, int64_t m, int64_t mn, int64_t n) {
+  const int64_t lda = c.lda;
+  cudaStream_t s = c.s, p = nullptr;
+  cudaEvent_t to_panel = nullptr, to_main = nullptr;
+  int st = lookahead_streams(&p, &to_panel, &to_main);
+  if (st) return st;
+  LuCtx<T> cp = c;  // the panel stream's context
+  cp.s = p;
+  const int64_t nb = LU_OUTER_NB;
+  auto block_w = [&](int64_t j0) { return (mn - j0) < nb ? (mn - j0) : nb; };
+  auto panel = [&](int64_t j0) -> int {
+    cp.blk0 = j0;
+    cp.blk1 = j0 + block_w(j0);
+    int r = lu_rec<T>(cp, j0, m - j0, block_w(j0));
+    if (r) return r;
+    GB_CUDA(cudaEventRecord(to_main, p));
+    return GB_SUCCESS;
+  };
+  // the panel stream starts after the work already queued on the main stream
+  GB_CUDA(cudaEventRecord(to_panel, s));
+  GB_CUDA(cudaStreamWaitEvent(p, to_panel, 0));
+  if ((st = panel(0))) return st;
+  // SMs the persistent GEMMs leave to the panel: one FP64/FP32 panel cluster
+  const int reserve = 16;
+  for (int64_t j0 = 0; j0 < mn; j0 += nb) {
+    const int64_t jb = block_w(j0);
+    const int64_t npiv = (m - j0) < jb ? (m - j0) : jb;
+    const int64_t c0 = j0 + jb;                       // first trailing column
+    const int64_t wslab = c0 < mn ? block_w(c0) : 0;  // the next block's columns
+    GB_CUDA(cudaStreamWaitEvent(s, to_main, 0));      // block J is factored
+    T *L11 = c.A + j0 + j0 * lda;
+    // one engine for every column piece: the one the whole update would use
+    const int engine = lu_update_engine<T>(c, m - c0, n - c0, jb);
+    // block J's interchanges, solve and update on columns [a, a + w)
+    auto update = [&](int64_t a, int64_t w) -> int {
+      if (w <= 0) return GB_SUCCESS;
+      int r;
+      {
+        ProfileScope prof("lu_laswp_right", s);
+        if ((r = launch_laswp_fused<T>(w, c.A + a * lda, lda, j0 + 1, j0 + npiv, c.ipiv, 1, s)))
+          return r;
+      }
+      T *A12 = c.A + j0 + a * lda;
+      {
+        ProfileScope prof("lu_trsm", s);
+        if ((r = lu_trsm<T>(jb, w, L11, lda, A12, lda, s))) return r;
+      }
+      if (c0 < m) {
+        ProfileScope prof("lu_gemm", s);
+        if ((r = lu_update<T>(c, m - c0, w, jb, L11 + jb, A12, A12 + jb, engine))) return r;
+      }
+      return GB_SUCCESS;
+    };
+    if ((st = update(c0, wslab))) return st;
+    if (wslab > 0) {
+      GB_CUDA(cudaEventRecord(to_panel, s));
+      GB_CUDA(cudaStreamWaitEvent(p, to_panel, 0));
+      if ((st = panel(c0))) return st;
+    }
+    {
+      SmReserve keep(reserve);
+      if ((st = update(c0 + wslab, n - c0 - wslab))) return st;
+    }
+    if (j0 > 0) {
+      ProfileScope prof("lu_laswp_left", s);
+      if ((st = launch_laswp_fused<T>(j0, c.A, lda, j0 + 1, j0 + npiv, c.ipiv, 1, s))) return st;
+    }
+  }
+  return GB_SUCCESS;
+}
+
 template <typename T>
 int getrf_device_mode(int64_t m, int64_t n, T *A, int64_t lda, int *ipiv, int *info,
                       int gemm_mode, cudaStream_t s) {
@@ -1224,8 +1487,18 @@ int getrf_device_mode(int64_t m, int64_t n, T *A, int64_t lda, int *ipiv, int *i
   c.nrows = m;
   c.ncols = n;
   c.s = s;
-  // the outer loop already covers the columns right of the square part
-  int st = lu_blocked<T>(c, m, mn, n);
+  // the outer loop already covers the columns right of the square part.
+  // With two or more blocks and trailing updates on the FMA units, the next
+  // panel is factored ahead (GB_LU_LOOKAHEAD=0 turns that off).  Not with the
+  // tensor-core updates: their persistent kernels hold one CTA on every SM
+  // (less the reserve) for the whole update, the panel's 16-CTA cluster then
+  // finds no GPC with 16 free SMs and waits for the update anyway (measured:
+  // FP32 LU 8192^2 24.9 -> 26.7 ms with look-ahead, 32768^2 panel time
+  // 142 -> 266 ms), while the FMA kernels' CTAs retire and let it in (FP64
+  // LU 8192^2 404 -> 361 ms).
+  const bool ahead = mn > LU_OUTER_NB && config().lu_lookahead &&
+                     lu_update_engine<T>(c, m - LU_OUTER_NB, n - LU_OUTER_NB, LU_OUTER_NB) == 0;
+  int st = ahead ? lu_blocked_lookahead<T>(c, m, mn, n) : lu_blocked<T>(c, m, mn, n);
   if (st) return st;
   return check_cuda(cudaGetLastError(), "getrf");
 }

@@ -940,7 +940,7 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       gp.status = ctx().d_status;
       gp.s_tiles = s_tiles;
       const int ntiles = gp.m_tiles * gp.n_tiles;
-      const int grid = ntiles < sm_count() ? ntiles : sm_count();
+      const int grid = ntiles < persistent_ctas() ? ntiles : persistent_ctas();
       {
         ProfileScope prof("slice_gemm", s);
         slice_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, gp);

@@ -573,7 +573,7 @@ int sgemm_tc(int ta, int tb, int64_t m, int64_t n, int64_t k, float alpha, const
   p.skip = skip;
   p.status = ctx().d_status;
   const int ntiles = p.m_tiles * p.n_tiles;
-  const int grid = ntiles < sm_count() ? ntiles : sm_count();
+  const int grid = ntiles < persistent_ctas() ? ntiles : persistent_ctas();
   {
     ProfileScope prof("sgemm_tc", s);
     if (tri == 1)

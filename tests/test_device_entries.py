@@ -221,3 +221,38 @@ def test_argument_error_wins_over_missing_device(L):
     L.gb_clear_error()
     assert _gemm("gb_dgemm_dev", m=-1)(L) == GB_ERR_INVALID_VALUE
     assert _lib.last_xerbla(L)[1] == 3
+
+
+def test_forked_child_reports_no_device_with_the_reason(gblib):
+    """A child forked after the parent called into the library cannot use the
+    parent's CUDA context (memory.c's pthread_atfork re-initialisation has no
+    GPU counterpart): every entry point then returns GB_ERR_NO_DEVICE and the
+    message names fork, before any CUDA call."""
+    import ctypes as C
+    import os
+    import openblas_gb300 as gb
+    dummy = C.c_void_p(0)
+    gblib.gb_dgetrf_dev(0, 0, dummy, 1, dummy, dummy)  # the parent touches the library
+    gblib.gb_clear_error()
+    r, w = os.pipe()
+    pid = os.fork()
+    if pid == 0:  # child: report the status and message through the pipe, then leave
+        os.close(r)
+        try:
+            st = gblib.gb_dgetrf_dev(4, 4, dummy, 4, dummy, dummy)
+            code, msg = gb.last_error(gblib)
+            os.write(w, f"{st}|{code}|{msg}".encode())
+        finally:
+            os._exit(0)
+    os.close(w)
+    out = b""
+    while True:
+        chunk = os.read(r, 4096)
+        if not chunk:
+            break
+        out += chunk
+    os.close(r)
+    os.waitpid(pid, 0)
+    st, code, msg = out.decode().split("|", 2)
+    assert int(st) == 3 and int(code) == 3, out
+    assert "fork" in msg

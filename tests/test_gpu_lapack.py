@@ -371,3 +371,59 @@ def test_sgetrf_tall_panels(orc, gblib, gb_clean, m, n):
     PA = _apply_piv(A0, piv)
     r = np.abs(PA - L @ U).sum(axis=0).max() / (n * feps * np.abs(A0).sum(axis=0).max())
     assert r <= 10, r
+
+
+_PLAIN_LU = r'''
+import sys, numpy as np, torch
+sys.path.insert(0, sys.argv[1])
+import openblas_gb300 as gb
+from openblas_gb300 import workloads as W
+lib = gb.load()
+n, dt, out = int(sys.argv[2]), sys.argv[3], sys.argv[4]
+A = W.uniform_device(7800 + n, (n, n), "cuda")
+if dt == "f32":
+    A = A.float()
+ipiv = torch.zeros(n, dtype=torch.int32, device="cuda")
+info = torch.zeros(1, dtype=torch.int32, device="cuda")
+torch.cuda.synchronize()   # the library works on its own stream
+f = lib.gb_sgetrf_dev if dt == "f32" else lib.gb_dgetrf_dev
+assert f(n, n, A.data_ptr(), n, ipiv.data_ptr(), info.data_ptr()) == 0
+assert lib.gb_synchronize() == 0
+np.savez(out, lu=A.cpu().numpy(), ipiv=ipiv.cpu().numpy(), info=info.cpu().numpy())
+'''
+
+
+@pytest.mark.parametrize("n,dt", [(3000, "f64"), (5000, "f32")])
+def test_lookahead_lu_equals_plain_blocked(gblib, gb_clean, tmp_path, n, dt):
+    """The look-ahead LU (next panel factored on a second stream while the
+    trailing update runs) performs every element's operations in the same
+    order as the plain blocked loop, so factors, pivots and info are
+    identical bit for bit; the plain loop runs in a child process with
+    GB_LU_LOOKAHEAD=0.  Look-ahead is used with trailing updates on the FMA
+    units, so the FP32 case selects them (GB_SGEMM_MODE=simt)."""
+    import subprocess
+    torch = pytest.importorskip("torch")
+    root = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+    script = tmp_path / "plain_lu.py"
+    script.write_text(_PLAIN_LU)
+    out = tmp_path / "plain.npz"
+    env = dict(os.environ, GB_LU_LOOKAHEAD="0", GB_SGEMM_MODE="simt")
+    subprocess.run([sys.executable, str(script), root, str(n), dt, str(out)], env=env,
+                   check=True, timeout=600)
+    ref = np.load(out)
+    A = W.uniform_device(7800 + n, (n, n), "cuda")
+    if dt == "f32":
+        A = A.float()
+    ipiv = torch.zeros(n, dtype=torch.int32, device="cuda")
+    info = torch.zeros(1, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()   # the library works on its own stream
+    f = gblib.gb_sgetrf_dev if dt == "f32" else gblib.gb_dgetrf_dev
+    gblib.gb_set_sgemm_mode(1)
+    try:
+        assert f(n, n, A.data_ptr(), n, ipiv.data_ptr(), info.data_ptr()) == 0
+        assert gblib.gb_synchronize() == 0
+    finally:
+        gblib.gb_set_sgemm_mode(0)
+    assert np.array_equal(ipiv.cpu().numpy(), ref["ipiv"])
+    assert int(info.item()) == int(ref["info"][0])
+    assert np.array_equal(A.cpu().numpy(), ref["lu"])
