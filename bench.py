@@ -628,6 +628,10 @@ def run_reference(args):
         "warmup": args.warmup, "ms_per_step": dt * 1e3, "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(n, args.slices), "impl": "reference",
+        "same_config": False,
+        "sample": f"each step computes a {n}x{slab} column slab ({slab / n:.3f} of the flops) of "
+                  f"the configured {n}^3 product, and the line reports its rate; the whole "
+                  f"product would take ~{n / slab:.0f}x the step time",
         "cpu_baseline": {"value": val, "unit": UNIT, "cores": cores, "kind": "port",
                          "sample": f"DGEMM NN {n}x{slab}x{n} column slab per step "
                                    f"(oracle C restatement of the reference's GEMM, OpenMP "
@@ -712,11 +716,13 @@ def dgesv_compare(lib, torch, gb, world, n=8192, nrhs=1, reps=3):
             "speedup_mixed_over_native": t_native / t_mixed}
 
 
-def batched_compare(lib, torch, gb, count=20000, loop_sample=1000):
+def batched_compare(lib, torch, gb, count=20000, loop_sample=1000, cpu_sample=2000):
     """20,000 uneven problems (n uniform in [8,256]; 40% DGEMM, 40% DGESV with
     one right-hand side, 20% DPOTRF), FP64, one grouped persistent launch
     replayed from a CUDA graph; the per-problem loop of the same kernel is
-    timed on the first `loop_sample` problems of the table and scaled."""
+    timed on the first `loop_sample` problems of the table, and the host
+    cores (the oracle's routines with OpenMP over problems) on the first
+    `cpu_sample` problems."""
     from openblas_gb300 import batch as BT
     import numpy as np
     BT.bind(lib)
@@ -739,7 +745,10 @@ def batched_compare(lib, torch, gb, count=20000, loop_sample=1000):
     oa = ob = oc = op = 0
     flops = np.zeros(count)
     spd = []
+    sample_end = None
     for i in range(count):
+        if i == cpu_sample:
+            sample_end = (oa, ob, oc, op)
         m, n, k = (int(x) for x in sizes[i])
         q = table[i]
         if kinds[i] == 0:
@@ -800,6 +809,45 @@ def batched_compare(lib, torch, gb, count=20000, loop_sample=1000):
     torch.cuda.synchronize()
     dt = time.perf_counter() - t0
     lib.gb_batch_plan_destroy(plan)
+    # host cores: the oracle's batch loop on the first cpu_sample problems,
+    # same inputs, all host threads (one problem per thread)
+    if sample_end is not None:
+        from oracle import pyoracle
+        sa, sb, sc, sp = sample_end
+        init()
+        torch.cuda.synchronize()
+        hA = bufA[:sa].cpu().numpy().copy()
+        hB = bufB[:max(sb, 1)].cpu().numpy().copy()
+        hC = bufC[:max(sc, 1)].cpu().numpy().copy()
+        hp = np.zeros(max(sp, 1), np.int32)
+        hinfo = np.zeros(cpu_sample, np.int32)
+        ht = (BT.Problem * cpu_sample)()
+        for i in range(cpu_sample):
+            q, h = table[i], ht[i]
+            for f, _ in BT.Problem._fields_:
+                setattr(h, f, getattr(q, f))
+            h.A = hA.ctypes.data + (q.A - bufA.data_ptr())
+            if q.type == 0:
+                h.B = hB.ctypes.data + (q.B - bufB.data_ptr())
+                h.C = hC.ctypes.data + (q.C - bufC.data_ptr())
+            else:
+                h.info = hinfo.ctypes.data + 4 * i
+                if q.type == 1:
+                    h.B = hB.ctypes.data + (q.B - bufB.data_ptr())
+                    h.C = hp.ctypes.data + (q.C - piv.data_ptr())
+        ncores = os.cpu_count() or 1
+        orc = pyoracle.lib()
+        orc.orc_set_threads(ncores)
+        t0 = time.perf_counter()
+        orc.orc_batch(C.cast(ht, C.c_void_p), cpu_sample)
+        cdt = time.perf_counter() - t0
+        cflops = float(flops[:cpu_sample].sum())
+        out["host_cores_oracle_fp64"] = {
+            "value": cflops / cdt / 1e12, "ms_sample": cdt * 1e3, "cores": ncores, "kind": "port",
+            "sample": f"first {cpu_sample} problems of the table, one problem per thread "
+                      "(OpenMP over problems)",
+            "nonzero_info": int((hinfo != 0).sum())}
+        del hA, hB, hC
     sflops = float(flops[:loop_sample].sum())
     out["per_problem_loop_fp64"] = {"value": sflops / dt / 1e12, "ms_sample": dt * 1e3,
                                     "sample": f"first {loop_sample} problems of the table"}
@@ -831,6 +879,8 @@ def run_peaks(args):
     torch.cuda.set_stream(stream)
     lib.gb_set_stream(C.c_void_p(stream.cuda_stream))
     peak = max(x for x in (out["fp64_dfma"], out["fp64_dmma"]) if x)
+    out["fp64_nominal"] = 1.25  # GB300's dense FP64 figure
+    out["peak_used"] = "max(fp64_dfma, fp64_dmma) probes"
     clocks = ClockSampler(0)
     clocks.start()
     for n in (4096, 8192):
@@ -842,6 +892,7 @@ def run_peaks(args):
             reps=2, warm=1)
         out[f"native_dgemm_{n}"] = 2 * n ** 3 / ms / 1e9
         out[f"native_dgemm_{n}_frac_of_fp64_peak"] = out[f"native_dgemm_{n}"] / peak
+        out[f"native_dgemm_{n}_frac_of_fp64_nominal"] = out[f"native_dgemm_{n}"] / 1.25
         del A, B, Cd
     out["clocks"] = clocks.stop()
     print(json.dumps(out), flush=True)

@@ -374,7 +374,9 @@ int gb_dpotrs_dev(char uplo, int64_t n, int64_t nrhs, const double *A, int64_t l
  * candidate CTA sizes on the batch itself (it executes the batch, so inputs
  * must be re-initialised afterwards) and caches the winner for batches with
  * the same size histogram.  gb_batch_execute_loop runs the same per-problem
- * code with one launch per problem (the comparison baseline). */
+ * code with one launch per problem (the comparison baseline).  The tuner also
+ * picks the DGEMM tile (32x32 or 64x64) per size bin; DGESV and DPOTRF orders
+ * are limited to 12288. */
 #define GB_BATCH_DGEMM 0
 #define GB_BATCH_DGESV 1
 #define GB_BATCH_DPOTRF 2

@@ -11,19 +11,30 @@
 // problem-size histogram), and captures the launch in a CUDA graph that is
 // replayed for every execution.
 //
-// Per-problem algorithms (one CTA each, operands in global memory where they
-// stay resident in L2; FP64 throughput bounds these sizes on this part):
-//   DGEMM   C = alpha op(A) op(B) + beta C, 64x64 register-tiled CTA loop;
+// Per-problem algorithms (one CTA each; FP64 throughput bounds these sizes
+// on this part, so each is arranged to keep the FP64 pipe busy):
+//   DGEMM   C = alpha op(A) op(B) + beta C, register-tiled CTA loop over
+//           64x64 or 32x32 tiles of C (the tile per size bin is picked by the
+//           autotuner: small problems waste less padding on 32x32 tiles);
 //           beta == 0 overwrites C (gemm_beta.c:41-94).
-//   DGESV   right-looking LU with the getf2_k.c pivot rules (first maximum
-//           |a|, swap and reciprocal scaling only when |pivot| >= DBL_MIN,
-//           info = first zero pivot), then forward/back substitution of the
-//           right-hand sides when info == 0 (gesv.c:131-135).
+//   DGESV   blocked right-looking LU (lapack/getrf/getrf_single.c structure,
+//           16-column panels): each panel is factored in shared memory with
+//           the getf2_k.c pivot rules (first maximum |a|, swap of the panel's
+//           processed columns and reciprocal scaling only when |pivot| >=
+//           DBL_MIN, info = first zero pivot), its interchanges go to the
+//           columns on both sides (laswp), then U12 and the trailing matrix
+//           are updated once per panel, every element taking the panel's
+//           multipliers in column order (the arithmetic of the column-by-column
+//           rank-1 updates, read and written once per panel instead of once per
+//           column); then forward/back substitution of the right-hand sides
+//           when info == 0 (gesv.c:131-135).
 //           Mixed variant: the LU runs in FP32 on a scratch copy, the solution
 //           is refined in FP64 with the dsgesv.f stopping test; problems that
 //           do not converge in 30 steps are redone in FP64 by the same CTA.
-//   DPOTRF  right-looking Cholesky (potf2_L.c / potf2_U.c contract: info =
-//           first non-positive pivot, whose value is written back).
+//   DPOTRF  blocked right-looking Cholesky, 16-column panels in shared memory
+//           (potf2_L.c / potf2_U.c contract: info = first non-positive pivot,
+//           whose value is left in place; columns before it are final and the
+//           rest carries the updates of those columns).
 #include <cuda_runtime.h>
 #include <float.h>
 #include <math.h>
@@ -47,7 +58,7 @@ namespace {
 
 struct DevProblem {
   int type, m, n, k;
-  int ta, tb, uplo, pad;
+  int ta, tb, uplo, tile;  // tile: DGEMM tile edge (32 or 64)
   double alpha, beta;
   void *A, *B, *C;
   int lda, ldb, ldc, pad2;
@@ -56,13 +67,18 @@ struct DevProblem {
 };
 
 // ---------------------------------------------------------------- DGEMM
-template <int NT>
-__device__ void cta_dgemm(const DevProblem &p) {
-  constexpr int BM = 64, BN = 64, BK = 16;
-  constexpr int TX = 16, TY = NT / 16;  // thread grid over the tile
+constexpr int DG_BK = 16;
+constexpr int PANEL_B = 16;  // panel width of the blocked LU and Cholesky
+constexpr int TILE_BINS = 4; // size bins of the DGEMM tile choice
+
+template <int NT, int BM>
+__device__ void cta_dgemm(const DevProblem &p, double *smem) {
+  constexpr int BN = BM, BK = DG_BK;
+  constexpr int TX = 16, TY = NT / TX;  // thread grid over the tile
+  static_assert(BM % TX == 0 && BN % TY == 0 && TX * TY == NT, "tile split");
   constexpr int RM = BM / TX, RN = BN / TY;
-  __shared__ double As[BK][BM];
-  __shared__ double Bs[BK][BN];
+  double(*As)[BM] = reinterpret_cast<double(*)[BM]>(smem);
+  double(*Bs)[BN] = reinterpret_cast<double(*)[BN]>(smem + BK * BM);
   const double *A = (const double *)p.A, *B = (const double *)p.B;
   double *C = (double *)p.C;
   const int m = p.m, n = p.n, k = p.k;
@@ -212,35 +228,153 @@ __device__ int cta_getrf(int n, T *M, int ld, int *ipiv) {
   return info;
 }
 
-// Solve (LU) X = P B for nrhs columns (B overwritten), forward/back substitution.
+// Blocked LU of an n x n matrix at M (leading dimension ld), 16-column
+// panels (the structure of lapack/getrf/getrf_single.c): the panel is
+// factored in shared memory P (rows x jb, column-major, ld = rows) with the
+// getf2_k.c rules, its interchanges are applied to the columns left of the
+// panel and to the columns right of it (laswp), and U12 and A22 receive the
+// panel's rank-1 updates in column order, each element read and written once
+// per panel.  ipiv 1-based.  Returns info.
+template <typename T, int NT>
+__device__ int cta_getrf_blk(int n, T *M, int ld, int *ipiv, T *P) {
+  __shared__ T sv[NT / 32];
+  __shared__ int si[NT / 32];
+  __shared__ T s_piv;
+  __shared__ int s_p;
+  const T tiny = sizeof(T) == 8 ? (T)DBL_MIN : (T)FLT_MIN;
+  int info = 0;
+  for (int j0 = 0; j0 < n; j0 += PANEL_B) {
+    const int jb = (n - j0) < PANEL_B ? (n - j0) : PANEL_B;
+    const int rows = n - j0;
+    for (int e = threadIdx.x; e < rows * jb; e += NT) {
+      const int r = e % rows, c = e / rows;
+      P[e] = M[(j0 + r) + (int64_t)(j0 + c) * ld];
+    }
+    __syncthreads();
+    // ---- panel (getf2) in shared memory
+    for (int j = 0; j < jb; ++j) {
+      T best = T(-1);
+      int bidx = 1 << 30;
+      for (int r = j + threadIdx.x; r < rows; r += NT) {
+        T a = P[r + j * rows];
+        a = a < T(0) ? -a : a;
+        if (a > best) {  // rows visited in increasing order: first maximum per thread
+          best = a;
+          bidx = r;
+        }
+      }
+      cta_argmax<T, NT>(best, bidx, sv, si, &s_piv, &s_p);
+      const int p = s_p;
+      const T piv = P[p + j * rows];
+      __syncthreads();  // every thread has the pivot before any row moves
+      const T apiv = piv < T(0) ? -piv : piv;
+      const bool nonzero = piv != T(0);
+      const bool scaled = nonzero && apiv >= tiny;
+      if (threadIdx.x == 0) ipiv[j0 + j] = j0 + p + 1;
+      if (!nonzero && info == 0) info = j0 + j + 1;
+      if (p != j)
+        for (int c = threadIdx.x; c < jb; c += NT)
+          if (scaled || c > j) {
+            const T t = P[j + c * rows];
+            P[j + c * rows] = P[p + c * rows];
+            P[p + c * rows] = t;
+          }
+      __syncthreads();
+      if (scaled) {
+        const T r = T(1) / piv;
+        for (int i = j + 1 + threadIdx.x; i < rows; i += NT) P[i + j * rows] *= r;
+      }
+      __syncthreads();
+      const int pr = rows - j - 1, pc = jb - j - 1;
+      for (int e = threadIdx.x; e < pr * pc; e += NT) {
+        const int i = j + 1 + e % pr, c = j + 1 + e / pr;
+        P[i + c * rows] = fma(-P[i + j * rows], P[j + c * rows], P[i + c * rows]);
+      }
+      __syncthreads();
+    }
+    for (int e = threadIdx.x; e < rows * jb; e += NT) {
+      const int r = e % rows, c = e / rows;
+      M[(j0 + r) + (int64_t)(j0 + c) * ld] = P[e];
+    }
+    // ---- the panel's interchanges on the other columns (one thread per column)
+    for (int c = threadIdx.x; c < n; c += NT) {
+      if (c >= j0 && c < j0 + jb) continue;
+      T *col = M + (int64_t)c * ld;
+      for (int j = 0; j < jb; ++j) {
+        const int p = ipiv[j0 + j] - 1;
+        if (p != j0 + j) {
+          const T t = col[j0 + j];
+          col[j0 + j] = col[p];
+          col[p] = t;
+        }
+      }
+    }
+    __syncthreads();
+    const int ncols = n - j0 - jb;
+    if (ncols <= 0) continue;
+    // ---- U12: row t of the right columns takes the multipliers of rows < t
+    for (int c = threadIdx.x; c < ncols; c += NT) {
+      T *col = M + (int64_t)(j0 + jb + c) * ld + j0;
+      for (int t = 1; t < jb; ++t) {
+        T a = col[t];
+        for (int k = 0; k < t; ++k) a = fma(-P[t + k * rows], col[k], a);
+        col[t] = a;
+      }
+    }
+    __syncthreads();
+    // ---- A22 -= L21 U12, k in column order
+    const int mr = rows - jb;
+    const int64_t total = (int64_t)mr * ncols;
+    for (int64_t e = threadIdx.x; e < total; e += NT) {
+      const int i = (int)(e % mr), c = (int)(e / mr);
+      const T *u = M + (int64_t)(j0 + jb + c) * ld + j0;
+      T *dst = M + (j0 + jb + i) + (int64_t)(j0 + jb + c) * ld;
+      T a = *dst;
+#pragma unroll 4
+      for (int k = 0; k < jb; ++k) a = fma(-P[(jb + i) + k * rows], u[k], a);
+      *dst = a;
+    }
+    __syncthreads();
+  }
+  return info;
+}
+
+// Solve (LU) X = P B for nrhs columns (B overwritten), forward/back
+// substitution.  Each right-hand side is staged in shared memory `w` (n
+// entries): the interchanges, applied in order by one thread, and the two
+// triangular sweeps then touch shared memory only.
 template <typename TM, typename TB_, int NT>
 __device__ void cta_getrs(int n, int nrhs, const TM *LU, int ld, const int *ipiv, TB_ *B,
-                          int ldb) {
+                          int ldb, TB_ *w) {
   for (int r = 0; r < nrhs; ++r) {
     TB_ *b = B + (int64_t)r * ldb;
+    for (int i = threadIdx.x; i < n; i += NT) w[i] = b[i];
+    __syncthreads();
     if (threadIdx.x == 0)
       for (int i = 0; i < n; ++i) {
         const int p = ipiv[i] - 1;
         if (p != i) {
-          TB_ t = b[i];
-          b[i] = b[p];
-          b[p] = t;
+          TB_ t = w[i];
+          w[i] = w[p];
+          w[p] = t;
         }
       }
     __syncthreads();
     for (int j = 0; j < n; ++j) {  // L y = b (unit diagonal)
-      const TB_ xj = b[j];
+      const TB_ xj = w[j];
       for (int i = j + 1 + threadIdx.x; i < n; i += NT)
-        b[i] = fma(-(TB_)LU[i + (int64_t)j * ld], xj, b[i]);
+        w[i] = fma(-(TB_)LU[i + (int64_t)j * ld], xj, w[i]);
       __syncthreads();
     }
     for (int j = n - 1; j >= 0; --j) {  // U x = y
-      if (threadIdx.x == 0) b[j] = b[j] / (TB_)LU[j + (int64_t)j * ld];
+      if (threadIdx.x == 0) w[j] = w[j] / (TB_)LU[j + (int64_t)j * ld];
       __syncthreads();
-      const TB_ xj = b[j];
-      for (int i = threadIdx.x; i < j; i += NT) b[i] = fma(-(TB_)LU[i + (int64_t)j * ld], xj, b[i]);
+      const TB_ xj = w[j];
+      for (int i = threadIdx.x; i < j; i += NT) w[i] = fma(-(TB_)LU[i + (int64_t)j * ld], xj, w[i]);
       __syncthreads();
     }
+    for (int i = threadIdx.x; i < n; i += NT) b[i] = w[i];
+    __syncthreads();
   }
 }
 
@@ -279,9 +413,73 @@ __device__ int cta_potrf(int n, double *M, int ld, bool upper) {
   return 0;
 }
 
+// Blocked Cholesky (16-column panels in shared memory P, rows x jb): the
+// operations of cta_potrf per element and in the same order.  On a
+// non-positive pivot the columns before it are final and everything after it
+// carries exactly the updates of those columns, as in the unblocked form.
+template <int NT>
+__device__ int cta_potrf_blk(int n, double *M, int ld, bool upper, double *P) {
+  __shared__ double s_d;
+  __shared__ int s_fail;
+  auto at = [&](int i, int c) -> double & {  // element (i, c) of the lower view
+    return upper ? M[c + (int64_t)i * ld] : M[i + (int64_t)c * ld];
+  };
+  for (int j0 = 0; j0 < n; j0 += PANEL_B) {
+    const int jb = (n - j0) < PANEL_B ? (n - j0) : PANEL_B;
+    const int rows = n - j0;
+    for (int e = threadIdx.x; e < rows * jb; e += NT) {
+      const int r = e % rows, c = e / rows;
+      if (r >= c) P[e] = at(j0 + r, j0 + c);
+    }
+    __syncthreads();
+    int done = jb;  // panel columns completed
+    for (int j = 0; j < jb; ++j) {
+      if (threadIdx.x == 0) {
+        const double ajj = P[j + j * rows];
+        s_fail = 0;
+        if (ajj <= 0.0) s_fail = 1;  // potf2_L.c:67-71: the pivot stays, info = j + 1
+        else P[j + j * rows] = sqrt(ajj);
+        s_d = P[j + j * rows];
+      }
+      __syncthreads();
+      if (s_fail) {
+        done = j;
+        break;
+      }
+      const double r = 1.0 / s_d;
+      for (int i = j + 1 + threadIdx.x; i < rows; i += NT) P[i + j * rows] *= r;
+      __syncthreads();
+      const int pr = rows - j - 1, pc = jb - j - 1;
+      for (int e = threadIdx.x; e < pr * pc; e += NT) {
+        const int i = j + 1 + e % pr, c = j + 1 + e / pr;
+        if (i >= c) P[i + c * rows] = fma(-P[i + j * rows], P[c + j * rows], P[i + c * rows]);
+      }
+      __syncthreads();
+    }
+    for (int e = threadIdx.x; e < rows * jb; e += NT) {
+      const int r = e % rows, c = e / rows;
+      if (r >= c) at(j0 + r, j0 + c) = P[e];
+    }
+    // trailing lower triangle: the updates of the completed panel columns
+    const int mr = rows - jb;
+    const int64_t total = (int64_t)mr * mr;
+    for (int64_t e = threadIdx.x; e < total; e += NT) {
+      const int i = (int)(e % mr), c = (int)(e / mr);
+      if (i < c) continue;
+      double a = at(j0 + jb + i, j0 + jb + c);
+      for (int k = 0; k < done; ++k)
+        a = fma(-P[(jb + i) + k * rows], P[(jb + c) + k * rows], a);
+      at(j0 + jb + i, j0 + jb + c) = a;
+    }
+    __syncthreads();
+    if (done < jb) return j0 + done + 1;
+  }
+  return 0;
+}
+
 // ---------------------------------------------------------------- mixed DGESV
 template <int NT>
-__device__ int cta_dsgesv(const DevProblem &p) {
+__device__ int cta_dsgesv(const DevProblem &p, double *smem, int blk_nmax) {
   const int n = p.n, nrhs = p.k;
   double *A = (double *)p.A;
   double *B = (double *)p.B;
@@ -315,7 +513,8 @@ __device__ int cta_dsgesv(const DevProblem &p) {
     __syncthreads();
   }
   const double cte = s_anrm * (DBL_EPSILON * 0.5) * sqrt((double)n);
-  int sinfo = cta_getrf<float, NT>(n, S, n, ipiv);
+  int sinfo = n <= blk_nmax ? cta_getrf_blk<float, NT>(n, S, n, ipiv, reinterpret_cast<float *>(smem))
+                            : cta_getrf<float, NT>(n, S, n, ipiv);
   __syncthreads();
   bool ok = sinfo == 0;
   int r = 0;  // columns < r hold converged solutions
@@ -324,7 +523,7 @@ __device__ int cta_dsgesv(const DevProblem &p) {
     // x0 = fp64(LU32 \ fp32(b))
     for (int i = threadIdx.x; i < n; i += NT) sr[i] = (float)b[i];
     __syncthreads();
-    cta_getrs<float, float, NT>(n, 1, S, n, ipiv, sr, n);
+    cta_getrs<float, float, NT>(n, 1, S, n, ipiv, sr, n, reinterpret_cast<float *>(smem));
     for (int i = threadIdx.x; i < n; i += NT) x[i] = (double)sr[i];
     __syncthreads();
     bool conv = false;
@@ -365,7 +564,7 @@ __device__ int cta_dsgesv(const DevProblem &p) {
         conv = true;
         break;
       }
-      cta_getrs<float, float, NT>(n, 1, S, n, ipiv, sr, n);
+      cta_getrs<float, float, NT>(n, 1, S, n, ipiv, sr, n, reinterpret_cast<float *>(smem));
       for (int i = threadIdx.x; i < n; i += NT) x[i] += (double)sr[i];
       __syncthreads();
     }
@@ -379,18 +578,35 @@ __device__ int cta_dsgesv(const DevProblem &p) {
   if (ok) return 0;
   // FP64 fallback (dsgesv.f:410-425): factor A in place and solve the
   // right-hand sides that have no converged solution yet
-  const int info = cta_getrf<double, NT>(n, A, p.lda, ipiv);
+  const int info = n <= blk_nmax ? cta_getrf_blk<double, NT>(n, A, p.lda, ipiv, smem)
+                                 : cta_getrf<double, NT>(n, A, p.lda, ipiv);
   __syncthreads();
   if (info == 0)
-    cta_getrs<double, double, NT>(n, nrhs - r, A, p.lda, ipiv, B + (int64_t)r * p.ldb, p.ldb);
+    cta_getrs<double, double, NT>(n, nrhs - r, A, p.lda, ipiv, B + (int64_t)r * p.ldb, p.ldb,
+                                  smem);
   return info;
 }
 
 // ---------------------------------------------------------------- kernel
+// Dynamic shared memory of the grouped kernel: the DGEMM tiles, or the
+// panel of the blocked LU / Cholesky (blk_nmax rows x PANEL_B columns).
+constexpr int BLK_SMEM_MAX = 96 * 1024;
+// Largest LU / Cholesky order of a batched problem.  A right-hand side is
+// staged in the kernel's shared memory, which holds PANEL_B doubles per row
+// of the largest order factored by panels, and BLK_SMEM_MAX / 8 = 12288
+// doubles once that order is capped.
+constexpr int BATCH_MAX_ORDER = BLK_SMEM_MAX / (int)sizeof(double);
+__host__ __device__ constexpr size_t grouped_smem(int blk_nmax) {
+  return (size_t)blk_nmax * PANEL_B * sizeof(double) > 2 * DG_BK * 64 * sizeof(double)
+             ? (size_t)blk_nmax * PANEL_B * sizeof(double)
+             : 2 * DG_BK * 64 * sizeof(double);
+}
+
 template <int NT>
 __global__ void __launch_bounds__(NT)
 grouped_kernel(const DevProblem *__restrict__ probs, const int *__restrict__ order, int count,
-               int *__restrict__ next, int mixed) {
+               int *__restrict__ next, int mixed, int blk_nmax) {
+  extern __shared__ __align__(16) double dsm[];
   __shared__ int s_idx;
   for (;;) {
     if (threadIdx.x == 0) s_idx = atomicAdd(next, 1);
@@ -400,21 +616,28 @@ grouped_kernel(const DevProblem *__restrict__ probs, const int *__restrict__ ord
     if (q >= count) break;
     const DevProblem p = probs[order[q]];
     if (p.type == GB_BATCH_DGEMM) {
-      cta_dgemm<NT>(p);
+      if (p.tile == 32)
+        cta_dgemm<NT, 32>(p, dsm);
+      else
+        cta_dgemm<NT, 64>(p, dsm);
     } else if (p.type == GB_BATCH_DGESV) {
       int info;
       if (mixed) {
-        info = cta_dsgesv<NT>(p);
+        info = cta_dsgesv<NT>(p, dsm, blk_nmax);
       } else {
-        info = cta_getrf<double, NT>(p.n, (double *)p.A, p.lda, (int *)p.C);
+        info = p.n <= blk_nmax
+                   ? cta_getrf_blk<double, NT>(p.n, (double *)p.A, p.lda, (int *)p.C, dsm)
+                   : cta_getrf<double, NT>(p.n, (double *)p.A, p.lda, (int *)p.C);
         __syncthreads();
         if (info == 0)
           cta_getrs<double, double, NT>(p.n, p.k, (const double *)p.A, p.lda, (const int *)p.C,
-                                        (double *)p.B, p.ldb);
+                                        (double *)p.B, p.ldb, dsm);
       }
       if (threadIdx.x == 0 && p.info) *p.info = info;
     } else if (p.type == GB_BATCH_DPOTRF) {
-      const int info = cta_potrf<NT>(p.n, (double *)p.A, p.lda, p.uplo == 0);
+      const int info = p.n <= blk_nmax
+                           ? cta_potrf_blk<NT>(p.n, (double *)p.A, p.lda, p.uplo == 0, dsm)
+                           : cta_potrf<NT>(p.n, (double *)p.A, p.lda, p.uplo == 0);
       if (threadIdx.x == 0 && p.info) *p.info = info;
     }
     __syncthreads();
@@ -444,28 +667,89 @@ struct BatchPlan {
   cudaStream_t stream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
-  int grid = 0;
+  int blk_nmax = 0;      // LU/Cholesky problems up to this order use the blocked forms
+  size_t smem = 0;       // dynamic shared memory of the grouped kernel
+  std::vector<int> bin_tile;  // DGEMM tile edge per size bin (autotuned)
+  std::vector<DevProblem> host_probs;  // the table as uploaded (tiles re-set by the tuner)
 };
 
 namespace {
 
+// What the autotuner found for a histogram key: threads per CTA and the
+// DGEMM tile edge of every size bin.
+struct Tuned {
+  int threads = 0;
+  int tile[TILE_BINS] = {0, 0, 0, 0};
+};
 std::mutex g_tune_mu;
-std::map<std::string, int> g_tuned;  // histogram key -> threads per CTA
+std::map<std::string, Tuned> g_tuned;  // histogram key -> tuned choice
 
-int launch_grouped(BatchPlan *pl, int threads, cudaStream_t s) {
-  GB_CUDA(cudaMemsetAsync(pl->d_next, 0, sizeof(int), s));
+// The grouped kernel's instances accept up to BLK_SMEM_MAX bytes of dynamic
+// shared memory (set once per device).
+int grouped_smem_attr() {
+  static PerDeviceOnce once;
+  return once.run(current_device(), [] {
+    GB_CUDA(cudaFuncSetAttribute(grouped_kernel<128>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 BLK_SMEM_MAX));
+    GB_CUDA(cudaFuncSetAttribute(grouped_kernel<256>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 BLK_SMEM_MAX));
+    GB_CUDA(cudaFuncSetAttribute(grouped_kernel<512>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 BLK_SMEM_MAX));
+    return GB_SUCCESS;
+  });
+}
+
+// CTAs of the persistent grouped kernel: as many as fit on every SM (a CTA
+// waiting at a barrier of a small problem leaves the FP64 pipe to the others).
+int grouped_grid(int threads, size_t smem) {
+  int per_sm = 0;
+  cudaError_t e = cudaErrorInvalidValue;
   if (threads == 128)
-    grouped_kernel<128><<<pl->grid, 128, 0, s>>>(pl->d_probs, pl->d_order, pl->count, pl->d_next,
-                                                 pl->mixed);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grouped_kernel<128>, 128, smem);
   else if (threads == 512)
-    grouped_kernel<512><<<pl->grid, 512, 0, s>>>(pl->d_probs, pl->d_order, pl->count, pl->d_next,
-                                                 pl->mixed);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grouped_kernel<512>, 512, smem);
   else
-    grouped_kernel<256><<<pl->grid, 256, 0, s>>>(pl->d_probs, pl->d_order, pl->count, pl->d_next,
-                                                 pl->mixed);
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grouped_kernel<256>, 256, smem);
+  if (e != cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 2;
+  }
+  if (per_sm > 8) per_sm = 8;
+  return sm_count() * per_sm;
+}
+
+// One launch of the grouped kernel over `count` entries of `order`.
+int launch_grouped_on(BatchPlan *pl, int threads, const int *order, int count, int *next,
+                      int grid, cudaStream_t s) {
+  int st = grouped_smem_attr();
+  if (st) return st;
+  if (grid <= 0) grid = grouped_grid(threads, pl->smem);
+  GB_CUDA(cudaMemsetAsync(next, 0, sizeof(int), s));
+  const size_t sm = pl->smem;
+  if (threads == 128)
+    grouped_kernel<128><<<grid, 128, sm, s>>>(pl->d_probs, order, count, next, pl->mixed,
+                                              pl->blk_nmax);
+  else if (threads == 512)
+    grouped_kernel<512><<<grid, 512, sm, s>>>(pl->d_probs, order, count, next, pl->mixed,
+                                              pl->blk_nmax);
+  else
+    grouped_kernel<256><<<grid, 256, sm, s>>>(pl->d_probs, order, count, next, pl->mixed,
+                                              pl->blk_nmax);
   count_launch();
   return check_cuda(cudaGetLastError(), "grouped batch launch");
 }
+
+int launch_grouped(BatchPlan *pl, int threads, cudaStream_t s) {
+  return launch_grouped_on(pl, threads, pl->d_order, pl->count, pl->d_next, 0, s);
+}
+
+// Size bins of the DGEMM tile choice: the larger of m and n.
+inline int tile_bin(int m, int n) {
+  const int d = m > n ? m : n;
+  return d <= 48 ? 0 : d <= 96 ? 1 : d <= 160 ? 2 : 3;
+}
+// Untuned default: 32x32 tiles up to 96 (less padding), 64x64 above.
+inline int default_tile(int bin) { return bin <= 1 ? 32 : 64; }
 
 // Key of the autotuner: type counts and a log2 histogram of the dominant size.
 std::string histogram_key(const std::vector<gb_batch_problem> &v, int mixed) {
@@ -509,7 +793,8 @@ void *gb_batch_plan_create(const gb_batch_problem *problems, int count, int flag
     const bool bad = p.type < GB_BATCH_DGEMM || p.type > GB_BATCH_DPOTRF || p.n < 0 ||
                      (p.type == GB_BATCH_DGEMM && (p.m < 0 || p.k < 0 || p.ldc < (p.m > 1 ? p.m : 1))) ||
                      (p.type != GB_BATCH_DGEMM && p.lda < (p.n > 1 ? p.n : 1)) ||
-                     (p.type == GB_BATCH_DGESV && (p.k < 0 || p.ldb < (p.n > 1 ? p.n : 1)));
+                     (p.type == GB_BATCH_DGESV && (p.k < 0 || p.ldb < (p.n > 1 ? p.n : 1))) ||
+                     (p.type != GB_BATCH_DGEMM && p.n > BATCH_MAX_ORDER);
     if (bad) {
       set_error(GB_ERR_INVALID_VALUE, "gb_batch_plan_create: problem %d is invalid", i);
       return nullptr;
@@ -534,10 +819,12 @@ void *gb_batch_plan_create(const gb_batch_problem *problems, int count, int flag
         work_floats = (work_floats + 63) & ~size_t(63);
       }
   std::vector<DevProblem> d(count);
+  int nmax = 0;  // largest LU / Cholesky order
   for (int i = 0; i < count; ++i) {
     const gb_batch_problem &p = v[i];
     DevProblem &q = d[i];
     memset(&q, 0, sizeof(q));
+    if (p.type != GB_BATCH_DGEMM && p.n > nmax) nmax = p.n;
     q.type = p.type;
     q.m = p.m;
     q.n = p.n;
@@ -572,6 +859,26 @@ void *gb_batch_plan_create(const gb_batch_problem *problems, int count, int flag
   }
   for (int i = 0; i < count; ++i)
     if (pl->mixed && v[i].type == GB_BATCH_DGESV) d[i].work = pl->d_work + work_off[i];
+  // blocked LU / Cholesky for the orders whose panel fits the shared memory
+  pl->blk_nmax = nmax;
+  if ((size_t)pl->blk_nmax * PANEL_B * sizeof(double) > (size_t)BLK_SMEM_MAX)
+    pl->blk_nmax = BLK_SMEM_MAX / (PANEL_B * (int)sizeof(double));
+  pl->smem = grouped_smem(pl->blk_nmax);
+  // DGEMM tiles and CTA size from the autotuner cache (keyed by the
+  // problem-size histogram), else the defaults
+  const std::string key = histogram_key(v, pl->mixed);
+  pl->key = key;
+  Tuned tuned;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(key);
+    if (it != g_tuned.end()) tuned = it->second;
+  }
+  pl->bin_tile.resize(TILE_BINS);
+  for (int b = 0; b < TILE_BINS; ++b) pl->bin_tile[b] = tuned.tile[b] ? tuned.tile[b] : default_tile(b);
+  for (int i = 0; i < count; ++i)
+    if (d[i].type == GB_BATCH_DGEMM) d[i].tile = pl->bin_tile[tile_bin(d[i].m, d[i].n)];
+  pl->host_probs = d;
   if (count) {
     cudaError_t e = cudaMemcpy(pl->d_probs, d.data(), bytes, cudaMemcpyHostToDevice);
     if (e == cudaSuccess)
@@ -582,18 +889,8 @@ void *gb_batch_plan_create(const gb_batch_problem *problems, int count, int flag
       return nullptr;
     }
   }
-  pl->grid = sm_count() * 2;
-  // CTA size from the autotuner cache (keyed by the problem-size histogram)
-  const std::string key = histogram_key(v, pl->mixed);
-  pl->key = key;
-  int best_t = 0;
-  {
-    std::lock_guard<std::mutex> lk(g_tune_mu);
-    auto it = g_tuned.find(key);
-    if (it != g_tuned.end()) best_t = it->second;
-  }
-  if (!best_t) best_t = 256;  // untuned default; gb_batch_plan_tune refines and caches
-  pl->threads = best_t;
+  // untuned default 256 threads; gb_batch_plan_tune refines and caches
+  pl->threads = tuned.threads ? tuned.threads : 256;
   // capture the launch in a CUDA graph on a private capture stream
   cudaStream_t cap;
   if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) == cudaSuccess) {
@@ -619,22 +916,64 @@ int gb_batch_plan_tune(void *plan) {
   int st = ensure_init();
   if (st) return st;
   cudaStream_t s = stream();
-  const int cands[3] = {128, 256, 512};
-  float best_ms = 1e30f;
-  int best_t = pl->threads;
   cudaEvent_t e0, e1;
   if ((st = check_cuda(cudaEventCreate(&e0), "gb_batch_plan_tune: event"))) return st;
   if ((st = check_cuda(cudaEventCreate(&e1), "gb_batch_plan_tune: event"))) {
     cudaEventDestroy(e0);
     return st;
   }
-  for (int t : cands) {
+  auto timed = [&](int threads, const int *order, int cnt, float *ms) -> int {
     cudaEventRecord(e0, s);
-    if ((st = launch_grouped(pl, t, s))) break;
+    int r = launch_grouped_on(pl, threads, order, cnt, pl->d_next, 0, s);
+    if (r) return r;
     cudaEventRecord(e1, s);
     cudaEventSynchronize(e1);
+    *ms = 0.f;
+    cudaEventElapsedTime(ms, e0, e1);
+    return GB_SUCCESS;
+  };
+  auto upload = [&]() -> int {
+    return check_cuda(cudaMemcpyAsync(pl->d_probs, pl->host_probs.data(),
+                                      sizeof(DevProblem) * pl->host_probs.size(),
+                                      cudaMemcpyHostToDevice, s),
+                      "gb_batch_plan_tune: table");
+  };
+  // 1. DGEMM tile edge per size bin: time each candidate on that bin's
+  //    problems alone (the same CTA size for both)
+  int *d_sub = nullptr;
+  st = check_cuda(cudaMalloc(&d_sub, sizeof(int) * (size_t)pl->count), "gb_batch_plan_tune");
+  for (int b = 0; b < TILE_BINS && !st; ++b) {
+    std::vector<int> sub;
+    for (int i = 0; i < pl->count; ++i) {
+      const DevProblem &q = pl->host_probs[i];
+      if (q.type == GB_BATCH_DGEMM && tile_bin(q.m, q.n) == b) sub.push_back(i);
+    }
+    if (sub.size() < 8) continue;  // too few problems to time
+    st = check_cuda(cudaMemcpyAsync(d_sub, sub.data(), sizeof(int) * sub.size(),
+                                    cudaMemcpyHostToDevice, s), "gb_batch_plan_tune");
+    float best = 1e30f;
+    for (int tile : {32, 64}) {
+      for (int i : sub) pl->host_probs[i].tile = tile;
+      if (st || (st = upload())) break;
+      float ms = 0.f;
+      if ((st = timed(pl->threads, d_sub, (int)sub.size(), &ms))) break;
+      if (ms < best) {
+        best = ms;
+        pl->bin_tile[b] = tile;
+      }
+    }
+    for (int i : sub) pl->host_probs[i].tile = pl->bin_tile[b];
+  }
+  cudaFree(d_sub);
+  if (!st) st = upload();
+  // 2. CTA size on the whole batch with the chosen tiles
+  const int cands[3] = {128, 256, 512};
+  float best_ms = 1e30f;
+  int best_t = pl->threads;
+  for (int t : cands) {
+    if (st) break;
     float ms = 0.f;
-    cudaEventElapsedTime(&ms, e0, e1);
+    if ((st = timed(t, pl->d_order, pl->count, &ms))) break;
     if (ms < best_ms) {
       best_ms = ms;
       best_t = t;
@@ -646,8 +985,14 @@ int gb_batch_plan_tune(void *plan) {
   pl->threads = best_t;
   {
     std::lock_guard<std::mutex> lk(g_tune_mu);
-    g_tuned[pl->key] = best_t;
+    Tuned t;
+    t.threads = best_t;
+    for (int b = 0; b < TILE_BINS; ++b) t.tile[b] = pl->bin_tile[b];
+    g_tuned[pl->key] = t;
   }
+  if (config().verbose)
+    fprintf(stderr, "libgbblas batch tune: %d threads, DGEMM tiles %d/%d/%d/%d by size bin\n",
+            best_t, pl->bin_tile[0], pl->bin_tile[1], pl->bin_tile[2], pl->bin_tile[3]);
   if (pl->exec) {
     cudaGraphExecDestroy(pl->exec);
     pl->exec = nullptr;
@@ -703,13 +1048,17 @@ int gb_batch_execute_loop(void *plan) {
   }
   GB_CUDA(cudaMemsetAsync(pl->d_loopnext, 0, sizeof(int) * (size_t)pl->count, s));
   // one launch of the same per-problem code for every problem, in table order
+  if ((st = grouped_smem_attr())) return st;
   for (int q = 0; q < pl->count; ++q) {
     if (pl->threads == 128)
-      grouped_kernel<128><<<1, 128, 0, s>>>(pl->d_probs, pl->d_order + q, 1, pl->d_loopnext + q, pl->mixed);
+      grouped_kernel<128><<<1, 128, pl->smem, s>>>(pl->d_probs, pl->d_order + q, 1,
+                                                   pl->d_loopnext + q, pl->mixed, pl->blk_nmax);
     else if (pl->threads == 512)
-      grouped_kernel<512><<<1, 512, 0, s>>>(pl->d_probs, pl->d_order + q, 1, pl->d_loopnext + q, pl->mixed);
+      grouped_kernel<512><<<1, 512, pl->smem, s>>>(pl->d_probs, pl->d_order + q, 1,
+                                                   pl->d_loopnext + q, pl->mixed, pl->blk_nmax);
     else
-      grouped_kernel<256><<<1, 256, 0, s>>>(pl->d_probs, pl->d_order + q, 1, pl->d_loopnext + q, pl->mixed);
+      grouped_kernel<256><<<1, 256, pl->smem, s>>>(pl->d_probs, pl->d_order + q, 1,
+                                                   pl->d_loopnext + q, pl->mixed, pl->blk_nmax);
     count_launch();
   }
   return check_cuda(cudaGetLastError(), "batch loop");

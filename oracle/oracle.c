@@ -1015,3 +1015,28 @@ DEFINE_ZGEMM(orc_cgemm, float, zbeta_s)
   }
 DEFINE_ZGEMM3M(orc_zgemm3m, double, zbeta_d)
 DEFINE_ZGEMM3M(orc_cgemm3m, float, zbeta_s)
+
+/* ------------------------------------------------------------------------ */
+/* Grouped batch on the host cores                                           */
+/* ------------------------------------------------------------------------ */
+/* One problem per thread (the inner routines run single-threaded inside the
+ * parallel loop: nested OpenMP regions are not activated), dynamic schedule
+ * over the problems as gemm_batch_thread.c:79-156 hands them to its threads. */
+void orc_batch(const orc_batch_problem *probs, int count) {
+  int nthr = orc_get_threads();
+#pragma omp parallel for num_threads(nthr) schedule(dynamic, 1)
+  for (int i = 0; i < count; ++i) {
+    const orc_batch_problem *p = &probs[i];
+    if (p->type == 0) {
+      orc_dgemm(p->transa, p->transb, p->m, p->n, p->k, p->alpha, (const double *)p->A, p->lda,
+                (const double *)p->B, p->ldb, p->beta, (double *)p->C, p->ldc);
+    } else if (p->type == 1) {
+      int info = orc_dgesv(p->n, p->k, (double *)p->A, p->lda, (int *)p->C, (double *)p->B,
+                           p->ldb);
+      if (p->info) *p->info = info;
+    } else if (p->type == 2) {
+      int info = orc_dpotrf(p->uplo, p->n, (double *)p->A, p->lda);
+      if (p->info) *p->info = info;
+    }
+  }
+}

@@ -111,6 +111,24 @@ void orc_cgemm3m(char transa, char transb, int m, int n, int k, const float *alp
                  const float *A, int lda, const float *B, int ldb, const float *beta, float *C,
                  int ldc);
 
+/* Grouped batch on the host cores: the per-problem oracle routines with
+ * OpenMP over the problems (each problem on one thread), the CPU
+ * counterpart of the grouped GPU batch.  The layout matches the library's
+ * gb_batch_problem; type 0 DGEMM (C = alpha op(A) op(B) + beta C), 1 DGESV
+ * (A n x n factored, B n x k solved, C = int ipiv[n], *info), 2 DPOTRF
+ * (uplo 'L'/'U', *info).  driver/level3/gemm_batch_thread.c:79-156 threads
+ * cblas_dgemm_batch over problems the same way. */
+typedef struct orc_batch_problem {
+  int type;
+  int m, n, k;
+  char transa, transb, uplo, pad;
+  double alpha, beta;
+  void *A, *B, *C;
+  int lda, ldb, ldc;
+  int *info;
+} orc_batch_problem;
+void orc_batch(const orc_batch_problem *probs, int count);
+
 #ifdef __cplusplus
 }
 #endif

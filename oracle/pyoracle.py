@@ -44,6 +44,7 @@ _SIGS = {
     "orc_cgemm": (None, [_c, _c, _i, _i, _i, _vp, _vp, _i, _vp, _i, _vp, _vp, _i]),
     "orc_zgemm3m": (None, [_c, _c, _i, _i, _i, _vp, _vp, _i, _vp, _i, _vp, _vp, _i]),
     "orc_cgemm3m": (None, [_c, _c, _i, _i, _i, _vp, _vp, _i, _vp, _i, _vp, _vp, _i]),
+    "orc_batch": (None, [_vp, _i]),
 }
 
 _lib = None
