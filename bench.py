@@ -50,6 +50,10 @@ def parse_args():
     ap.add_argument("--peaks", action="store_true",
                     help="measure the FP64 peak rates (DFMA, DMMA probes) and the native DGEMM's "
                          "fraction of them instead of the headline step")
+    ap.add_argument("--batch", action="store_true",
+                    help="run only the batched-solver comparison (one JSON line)")
+    ap.add_argument("--batch-count", type=int, default=20000,
+                    help="problems in the batched comparison")
     ap.add_argument("--suite", action="store_true",
                     help="measure every configuration of the level-3/LAPACK sweep (one JSON "
                          "line each) instead of the headline step")
@@ -785,7 +789,9 @@ def batched_compare(lib, torch, gb, count=20000, loop_sample=1000, cpu_sample=20
     out = {"workload": f"{count} problems, n uniform in [8,256]: 40% DGEMM (m,n,k independent), "
                        "40% DGETRF+DGETRS (1 RHS), 20% DPOTRF; FP64", "unit": UNIT}
     total = float(flops.sum())
-    for flags, name in ((0, "grouped_graph_fp64"), (BT.GB_BATCH_MIXED, "grouped_graph_mixed")):
+    for flags, name in ((0, "grouped_graph_fp64"), (BT.GB_BATCH_MIXED, "grouped_graph_mixed"),
+                        (BT.GB_BATCH_MIXED | BT.GB_BATCH_EMULATED,
+                         "grouped_graph_emulated_dgemm_mixed_dgesv")):
         init()
         plan = lib.gb_batch_plan_create(table, count, flags)
         lib.gb_batch_plan_tune(plan)
@@ -911,6 +917,16 @@ def main():
         return
     if args.peaks:
         run_peaks(args)
+        return
+    if args.batch:
+        import torch
+
+        import openblas_gb300 as gb
+        lib = gb.load()
+        out = batched_compare(lib, torch, gb, count=args.batch_count,
+                              loop_sample=min(1000, args.batch_count),
+                              cpu_sample=min(2000, args.batch_count))
+        print(json.dumps(out), flush=True)
         return
     import numpy as np
     import torch

@@ -381,6 +381,11 @@ int gb_dpotrs_dev(char uplo, int64_t n, int64_t nrhs, const double *A, int64_t l
 #define GB_BATCH_DGESV 1
 #define GB_BATCH_DPOTRF 2
 #define GB_BATCH_MIXED 1
+/* flag: the DGEMM problems run on the emulated-FP64 kernel (Ozaki split into
+ * seven 8-bit digit slices multiplied on the bf16 tensor cores, FP64-level
+ * accuracy; K up to 4096 and m, n up to 2048: larger problems and tiles
+ * holding Inf/NaN use the FP64 loop) */
+#define GB_BATCH_EMULATED 2
 typedef struct gb_batch_problem {
   int type;
   int m, n, k;

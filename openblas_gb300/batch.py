@@ -5,6 +5,7 @@ import ctypes as C
 
 GB_BATCH_DGEMM, GB_BATCH_DGESV, GB_BATCH_DPOTRF = 0, 1, 2
 GB_BATCH_MIXED = 1
+GB_BATCH_EMULATED = 2
 
 
 class Problem(C.Structure):

@@ -51,6 +51,8 @@
 
 #include "gb_internal.h"
 #include "operand.h"
+#include "ozaki_digits.cuh"
+#include <cuda_bf16.h>
 
 namespace gb {
 
@@ -137,6 +139,209 @@ __device__ void cta_dgemm(const DevProblem &p, double *smem) {
         }
       }
     }
+}
+
+// ---------------------------------------------------------------- DGEMM, emulated FP64
+// The Ozaki split of the large-product engine (ozaki.cu) for one small
+// problem per CTA, on the warp-level bf16 tensor-core MMA: per 32 x 32 tile
+// of C (eight warps of 16 x 8), the rows of op(A) and the columns of op(B) get their scale exponents
+// over the whole K; every 64-deep K chunk is cut into EM_S = 7 slices of
+// 8-bit digits (56 bits) in shared memory; each product of digit slices
+// A_s B_t with s + t <= 8 (the Ozaki triangle, 28 products) is summed by
+// mma.sync m16n8k16 in FP32, exact for one chunk (64 * 255^2 < 2^24), and
+// added to the int32 sum of its level s + t (at most 7 products x 64 chunks
+// x 64 * 255^2 < 2^31 for K <= 4096); the levels are recombined as an exact
+// int128 and rounded once (ozd::level_value).  The exponents are found once
+// per problem.  Tiles whose rows or columns hold Inf/NaN, K > 4096 and m or n
+// above 2048 use the FP64 loop instead.
+constexpr int EM_BM = 32, EM_KC = 64, EM_S = 7, EM_KP = 72;  // KP: padded row of a slice
+constexpr int EM_NT = 256;
+constexpr int EM_KMAX = 4096;
+constexpr int EM_DMAX = 2048;  // rows of op(A) / columns of op(B) whose exponents are kept
+constexpr size_t EM_SLICE_ELEMS = (size_t)EM_S * EM_BM * EM_KP;
+constexpr size_t EM_SMEM = 2 * EM_SLICE_ELEMS * sizeof(__nv_bfloat16) + 2 * EM_DMAX * sizeof(int) + 16;
+
+__device__ __forceinline__ void mma_bf16_16816(float (&d)[4], const uint32_t (&a)[4],
+                                               uint32_t b0, uint32_t b1) {
+  asm volatile(
+      "mma.sync.aligned.m16n8k16.row.col.f32.bf16.bf16.f32 {%0,%1,%2,%3}, {%4,%5,%6,%7}, "
+      "{%8,%9}, {%0,%1,%2,%3};"
+      : "+f"(d[0]), "+f"(d[1]), "+f"(d[2]), "+f"(d[3])
+      : "r"(a[0]), "r"(a[1]), "r"(a[2]), "r"(a[3]), "r"(b0), "r"(b1));
+}
+
+// FP64 loop for one tile (Inf/NaN present, or K too long for exact levels)
+__device__ void emu_tile_fp64(const DevProblem &p, int m0, int n0) {
+  const double *A = (const double *)p.A, *B = (const double *)p.B;
+  double *C = (double *)p.C;
+  for (int e = threadIdx.x; e < EM_BM * EM_BM; e += EM_NT) {
+    const int i = m0 + e % EM_BM, j = n0 + e / EM_BM;
+    if (i >= p.m || j >= p.n) continue;
+    double sum = 0.0;
+    if (p.alpha != 0.0)
+      for (int k = 0; k < p.k; ++k) {
+        const double a = p.ta ? A[k + (int64_t)i * p.lda] : A[i + (int64_t)k * p.lda];
+        const double b = p.tb ? B[j + (int64_t)k * p.ldb] : B[k + (int64_t)j * p.ldb];
+        sum = fma(a, b, sum);
+      }
+    double *c = C + i + (int64_t)j * p.ldc;
+    const double v = p.alpha * sum;
+    *c = (p.beta == 0.0) ? v : fma(p.beta, *c, v);
+  }
+}
+
+__device__ void cta_dgemm_emu(const DevProblem &p, unsigned char *smem) {
+  using namespace ozd;
+  __nv_bfloat16 *As = reinterpret_cast<__nv_bfloat16 *>(smem);  // [S][BM][KP]
+  __nv_bfloat16 *Bs = As + EM_SLICE_ELEMS;                        // [S][BN][KP]
+  int *e_row = reinterpret_cast<int *>(Bs + EM_SLICE_ELEMS);      // [m] exponents of op(A) rows
+  int *f_col = e_row + EM_DMAX;                                   // [n] of op(B) columns
+  __shared__ int s_special;
+  const double *A = (const double *)p.A, *B = (const double *)p.B;
+  double *C = (double *)p.C;
+  const int m = p.m, n = p.n, k = p.k;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int g = lane >> 2, tg = lane & 3;
+  const int wm = (warp & 1) * 16, wn = (warp >> 1) * 8;  // warp's 16 x 8 sub-tile
+  const bool fp64 = p.alpha == 0.0 || k == 0 || k > EM_KMAX || m > EM_DMAX || n > EM_DMAX;
+  if (!fp64) {
+    // scale exponents of every row of op(A) and column of op(B), once: a
+    // warp per row or column, its lanes along K (coalesced when the K
+    // direction is contiguous; otherwise lanes of neighbouring warps read
+    // neighbouring rows of the same column)
+    for (int r = warp; r < m + n; r += EM_NT / 32) {
+      const bool row = r < m;
+      const int rr = row ? r : r - m;
+      unsigned long long best = 0;
+      for (int kk = lane; kk < k; kk += 32) {
+        const double v = row ? (p.ta ? A[kk + (int64_t)rr * p.lda] : A[rr + (int64_t)kk * p.lda])
+                             : (p.tb ? B[rr + (int64_t)kk * p.ldb] : B[kk + (int64_t)rr * p.ldb]);
+        const unsigned long long b = (unsigned long long)__double_as_longlong(fabs(v));
+        best = b > best ? b : best;
+      }
+#pragma unroll
+      for (int off = 16; off > 0; off >>= 1) {
+        const unsigned long long o = __shfl_down_sync(0xffffffffu, best, off);
+        best = o > best ? o : best;
+      }
+      if (lane == 0) (row ? e_row : f_col)[rr] = exponent_of_max(best);
+    }
+    __syncthreads();
+  }
+  for (int m0 = 0; m0 < m; m0 += EM_BM)
+    for (int n0 = 0; n0 < n; n0 += EM_BM) {
+      if (fp64) {
+        emu_tile_fp64(p, m0, n0);
+        __syncthreads();
+        continue;
+      }
+      // a tile whose rows or columns hold Inf/NaN: the FP64 loop
+      if (tid == 0) s_special = 0;
+      __syncthreads();
+      if (tid < 2 * EM_BM) {
+        const bool row = tid < EM_BM;
+        const int r = row ? m0 + tid : n0 + tid - EM_BM;
+        if (r < (row ? m : n) && (row ? e_row[r] : f_col[r]) == NONFINITE) s_special = 1;
+      }
+      __syncthreads();
+      if (s_special) {
+        emu_tile_fp64(p, m0, n0);
+        __syncthreads();
+        continue;
+      }
+      int lev[EM_S][4];
+#pragma unroll
+      for (int l = 0; l < EM_S; ++l)
+#pragma unroll
+        for (int c = 0; c < 4; ++c) lev[l][c] = 0;
+      for (int k0 = 0; k0 < k; k0 += EM_KC) {
+        // digits of the chunk: op(A)(m0 + i, k0 + kk) and op(B)(k0 + kk, n0 + j)
+        for (int e = tid; e < EM_BM * EM_KC; e += EM_NT) {
+          // A: i fastest when op(A) columns are contiguous (ta = 0), else kk fastest
+          const int i = p.ta ? e / EM_KC : e % EM_BM, kk = p.ta ? e % EM_KC : e / EM_BM;
+          const int gi = m0 + i, gk = k0 + kk;
+          double x = 0.0;
+          if (gi < m && gk < k) x = p.ta ? A[gk + (int64_t)gi * p.lda] : A[gi + (int64_t)gk * p.lda];
+          bool neg;
+          const unsigned long long mag = digit_magnitude(x, gi < m ? e_row[gi] : 0, EM_S, neg);
+#pragma unroll
+          for (int sl = 0; sl < EM_S; ++sl) {
+            const int d = (int)((mag >> (DIGIT_BITS * (EM_S - 1 - sl))) & DIGIT_MASK);
+            As[((size_t)sl * EM_BM + i) * EM_KP + kk] = __float2bfloat16_rn((float)(neg ? -d : d));
+          }
+          // B: kk fastest when op(B) columns are contiguous (tb = 0)
+          const int j = p.tb ? e % EM_BM : e / EM_KC, kb = p.tb ? e / EM_BM : e % EM_KC;
+          const int gj = n0 + j, gkb = k0 + kb;
+          double y = 0.0;
+          if (gj < n && gkb < k)
+            y = p.tb ? B[gj + (int64_t)gkb * p.ldb] : B[gkb + (int64_t)gj * p.ldb];
+          const unsigned long long magb = digit_magnitude(y, gj < n ? f_col[gj] : 0, EM_S, neg);
+#pragma unroll
+          for (int sl = 0; sl < EM_S; ++sl) {
+            const int d = (int)((magb >> (DIGIT_BITS * (EM_S - 1 - sl))) & DIGIT_MASK);
+            Bs[((size_t)sl * EM_BM + j) * EM_KP + kb] = __float2bfloat16_rn((float)(neg ? -d : d));
+          }
+        }
+        __syncthreads();
+        // the Ozaki triangle: products of level L = s + t <= S + 1 (s, t 1-based)
+#pragma unroll
+        for (int L = 2; L <= EM_S + 1; ++L) {
+          const int s_lo = L - EM_S > 1 ? L - EM_S : 1, s_hi = L - 1 < EM_S ? L - 1 : EM_S;
+#pragma unroll 1
+          for (int s1 = s_lo; s1 <= s_hi; ++s1) {
+            const int t1 = L - s1;
+            float acc[4] = {0.f, 0.f, 0.f, 0.f};
+            const __nv_bfloat16 *as = As + (size_t)(s1 - 1) * EM_BM * EM_KP;
+            const __nv_bfloat16 *bs = Bs + (size_t)(t1 - 1) * EM_BM * EM_KP;
+#pragma unroll
+            for (int ks = 0; ks < EM_KC; ks += 16) {
+              uint32_t a[4];
+              a[0] = *reinterpret_cast<const uint32_t *>(as + (wm + g) * EM_KP + ks + 2 * tg);
+              a[1] = *reinterpret_cast<const uint32_t *>(as + (wm + g + 8) * EM_KP + ks + 2 * tg);
+              a[2] = *reinterpret_cast<const uint32_t *>(as + (wm + g) * EM_KP + ks + 2 * tg + 8);
+              a[3] = *reinterpret_cast<const uint32_t *>(as + (wm + g + 8) * EM_KP + ks + 2 * tg + 8);
+              const __nv_bfloat16 *bc = bs + (wn + g) * EM_KP + ks + 2 * tg;
+              mma_bf16_16816(acc, a, *reinterpret_cast<const uint32_t *>(bc),
+                             *reinterpret_cast<const uint32_t *>(bc + 8));
+            }
+#pragma unroll
+            for (int c = 0; c < 4; ++c) lev[L - 2][c] += __float2int_rn(acc[c]);
+          }
+        }
+        __syncthreads();  // the slices are rewritten by the next chunk
+      }
+      // recombine the thread's 4 elements: rows g, g + 8 of the warp's
+      // sub-tile, columns 2 tg, 2 tg + 1
+#pragma unroll
+        for (int c = 0; c < 4; ++c) {
+          const int il = wm + g + (c >= 2 ? 8 : 0), jl = wn + 2 * tg + (c & 1);
+          const int i = m0 + il, j = n0 + jl;
+          if (i >= m || j >= n) continue;
+          __int128 acc = 0;
+#pragma unroll
+          for (int l = 0; l < EM_S; ++l) acc += (__int128)lev[l][c] << (DIGIT_BITS * (EM_S - 1 - l));
+          const double v = level_value(acc, EM_S, e_row[i], f_col[j], p.alpha);
+          double *cp = C + i + (int64_t)j * p.ldc;
+          *cp = (p.beta == 0.0) ? v : fma(p.beta, *cp, v);
+        }
+      __syncthreads();
+    }
+}
+
+__global__ void __launch_bounds__(EM_NT, 2)
+grouped_emu_kernel(const DevProblem *__restrict__ probs, const int *__restrict__ order, int count,
+                   int *__restrict__ next) {
+  extern __shared__ __align__(16) unsigned char emsm[];
+  __shared__ int s_idx;
+  for (;;) {
+    if (threadIdx.x == 0) s_idx = atomicAdd(next, 1);
+    __syncthreads();
+    const int q = s_idx;
+    __syncthreads();
+    if (q >= count) break;
+    cta_dgemm_emu(probs[order[q]], emsm);
+    __syncthreads();
+  }
 }
 
 // ---------------------------------------------------------------- reductions
@@ -667,6 +872,10 @@ struct BatchPlan {
   cudaStream_t stream = nullptr;
   cudaGraph_t graph = nullptr;
   cudaGraphExec_t exec = nullptr;
+  int emulated = 0;      // DGEMM problems on the emulated-FP64 kernel
+  int *d_order_emu = nullptr;  // their order (the other problems stay in d_order)
+  int count_emu = 0, count_main = 0;
+  std::vector<int> h_order, h_order_emu;  // host copies of both orders
   int blk_nmax = 0;      // LU/Cholesky problems up to this order use the blocked forms
   size_t smem = 0;       // dynamic shared memory of the grouped kernel
   std::vector<int> bin_tile;  // DGEMM tile edge per size bin (autotuned)
@@ -739,8 +948,83 @@ int launch_grouped_on(BatchPlan *pl, int threads, const int *order, int count, i
   return check_cuda(cudaGetLastError(), "grouped batch launch");
 }
 
+int emu_attr() {
+  static PerDeviceOnce once;
+  return once.run(current_device(), [] {
+    GB_CUDA(cudaFuncSetAttribute(grouped_emu_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                 (int)EM_SMEM));
+    return GB_SUCCESS;
+  });
+}
+
+int launch_grouped_emu(BatchPlan *pl, const int *order, int count, int *next, cudaStream_t s) {
+  int st = emu_attr();
+  if (st) return st;
+  int per_sm = 0;
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, grouped_emu_kernel, EM_NT, EM_SMEM) !=
+          cudaSuccess || per_sm < 1) {
+    cudaGetLastError();
+    per_sm = 1;
+  }
+  GB_CUDA(cudaMemsetAsync(next, 0, sizeof(int), s));
+  grouped_emu_kernel<<<sm_count() * per_sm, EM_NT, EM_SMEM, s>>>(pl->d_probs, order, count, next);
+  count_launch();
+  return check_cuda(cudaGetLastError(), "grouped emulated batch launch");
+}
+
+int launch_grouped(BatchPlan *pl, int threads, cudaStream_t s);
+
+// The plan's launches captured in a CUDA graph (pl->graph / pl->exec).  With
+// both kernels (emulated DGEMM problems and the rest) the graph forks: the two
+// persistent kernels run side by side and join at the end.
+void capture_plan(BatchPlan *pl) {
+  cudaStream_t cap = nullptr, cap2 = nullptr;
+  cudaEvent_t fork = nullptr, join = nullptr;
+  const bool both = pl->count_emu > 0 && pl->count_main > 0;
+  if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) != cudaSuccess) {
+    cudaGetLastError();
+    return;
+  }
+  bool ok = !both || (cudaStreamCreateWithFlags(&cap2, cudaStreamNonBlocking) == cudaSuccess &&
+                      cudaEventCreateWithFlags(&fork, cudaEventDisableTiming) == cudaSuccess &&
+                      cudaEventCreateWithFlags(&join, cudaEventDisableTiming) == cudaSuccess);
+  if (ok && cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
+    int st = GB_SUCCESS;
+    if (both) {
+      cudaEventRecord(fork, cap);
+      cudaStreamWaitEvent(cap2, fork, 0);
+      st = launch_grouped_emu(pl, pl->d_order_emu, pl->count_emu, pl->d_next + 1, cap2);
+      if (!st) st = launch_grouped_on(pl, pl->threads, pl->d_order, pl->count_main, pl->d_next, 0,
+                                      cap);
+      cudaEventRecord(join, cap2);
+      cudaStreamWaitEvent(cap, join, 0);
+    } else {
+      st = launch_grouped(pl, pl->threads, cap);
+    }
+    cudaGraph_t g = nullptr;
+    if (cudaStreamEndCapture(cap, &g) == cudaSuccess && !st &&
+        cudaGraphInstantiate(&pl->exec, g, 0) == cudaSuccess) {
+      pl->graph = g;
+    } else {
+      if (g) cudaGraphDestroy(g);
+      pl->exec = nullptr;
+    }
+  }
+  cudaGetLastError();
+  if (fork) cudaEventDestroy(fork);
+  if (join) cudaEventDestroy(join);
+  if (cap2) cudaStreamDestroy(cap2);
+  cudaStreamDestroy(cap);
+}
+
 int launch_grouped(BatchPlan *pl, int threads, cudaStream_t s) {
-  return launch_grouped_on(pl, threads, pl->d_order, pl->count, pl->d_next, 0, s);
+  int st = GB_SUCCESS;
+  if (pl->count_emu > 0 &&
+      (st = launch_grouped_emu(pl, pl->d_order_emu, pl->count_emu, pl->d_next + 1, s)))
+    return st;
+  if (pl->count_main > 0)
+    st = launch_grouped_on(pl, threads, pl->d_order, pl->count_main, pl->d_next, 0, s);
+  return st;
 }
 
 // Size bins of the DGEMM tile choice: the larger of m and n.
@@ -842,15 +1126,27 @@ void *gb_batch_plan_create(const gb_batch_problem *problems, int count, int flag
     q.ldc = p.ldc;
     q.info = p.info;
   }
-  // order: decreasing cost (longest-processing-time first)
-  std::vector<int> order(count);
-  for (int i = 0; i < count; ++i) order[i] = i;
-  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
-    return problem_cost(v[a]) > problem_cost(v[b]);
-  });
+  // order: decreasing cost (longest-processing-time first); with the
+  // emulated flag the DGEMM problems form their own list for their kernel
+  pl->emulated = (flags & GB_BATCH_EMULATED) ? 1 : 0;
+  std::vector<int> order, order_emu;
+  for (int i = 0; i < count; ++i)
+    (pl->emulated && v[i].type == GB_BATCH_DGEMM ? order_emu : order).push_back(i);
+  auto lpt = [&](std::vector<int> &o) {
+    std::stable_sort(o.begin(), o.end(), [&](int a, int b) {
+      return problem_cost(v[a]) > problem_cost(v[b]);
+    });
+  };
+  lpt(order);
+  lpt(order_emu);
+  pl->count_main = (int)order.size();
+  pl->count_emu = (int)order_emu.size();
+  pl->h_order = order;
+  pl->h_order_emu = order_emu;
   const size_t bytes = sizeof(DevProblem) * (size_t)(count > 0 ? count : 1);
   if (cudaMalloc(&pl->d_probs, bytes) != cudaSuccess ||
       cudaMalloc(&pl->d_order, sizeof(int) * (size_t)(count > 0 ? count : 1)) != cudaSuccess ||
+      cudaMalloc(&pl->d_order_emu, sizeof(int) * (size_t)(count > 0 ? count : 1)) != cudaSuccess ||
       cudaMalloc(&pl->d_next, sizeof(int) * 4) != cudaSuccess ||
       (work_floats && cudaMalloc(&pl->d_work, work_floats * sizeof(float)) != cudaSuccess)) {
     check_cuda(cudaErrorMemoryAllocation, "gb_batch_plan_create");
@@ -881,8 +1177,12 @@ void *gb_batch_plan_create(const gb_batch_problem *problems, int count, int flag
   pl->host_probs = d;
   if (count) {
     cudaError_t e = cudaMemcpy(pl->d_probs, d.data(), bytes, cudaMemcpyHostToDevice);
-    if (e == cudaSuccess)
-      e = cudaMemcpy(pl->d_order, order.data(), sizeof(int) * count, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !order.empty())
+      e = cudaMemcpy(pl->d_order, order.data(), sizeof(int) * order.size(),
+                     cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && !order_emu.empty())
+      e = cudaMemcpy(pl->d_order_emu, order_emu.data(), sizeof(int) * order_emu.size(),
+                     cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
       check_cuda(e, "gb_batch_plan_create: table upload");
       gb_batch_plan_destroy(pl);
@@ -891,21 +1191,8 @@ void *gb_batch_plan_create(const gb_batch_problem *problems, int count, int flag
   }
   // untuned default 256 threads; gb_batch_plan_tune refines and caches
   pl->threads = tuned.threads ? tuned.threads : 256;
-  // capture the launch in a CUDA graph on a private capture stream
-  cudaStream_t cap;
-  if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) == cudaSuccess) {
-    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-      launch_grouped(pl, pl->threads, cap);
-      if (cudaStreamEndCapture(cap, &pl->graph) == cudaSuccess &&
-          cudaGraphInstantiate(&pl->exec, pl->graph, 0) == cudaSuccess) {
-        // ready
-      } else {
-        cudaGetLastError();
-        pl->exec = nullptr;
-      }
-    }
-    cudaStreamDestroy(cap);
-  }
+  // capture the launch(es) in a CUDA graph on private capture streams
+  capture_plan(pl);
   return pl;
 }
 
@@ -946,7 +1233,7 @@ int gb_batch_plan_tune(void *plan) {
     std::vector<int> sub;
     for (int i = 0; i < pl->count; ++i) {
       const DevProblem &q = pl->host_probs[i];
-      if (q.type == GB_BATCH_DGEMM && tile_bin(q.m, q.n) == b) sub.push_back(i);
+        if (!pl->emulated && q.type == GB_BATCH_DGEMM && tile_bin(q.m, q.n) == b) sub.push_back(i);
     }
     if (sub.size() < 8) continue;  // too few problems to time
     st = check_cuda(cudaMemcpyAsync(d_sub, sub.data(), sizeof(int) * sub.size(),
@@ -971,9 +1258,9 @@ int gb_batch_plan_tune(void *plan) {
   float best_ms = 1e30f;
   int best_t = pl->threads;
   for (int t : cands) {
-    if (st) break;
+    if (st || pl->count_main == 0) break;
     float ms = 0.f;
-    if ((st = timed(t, pl->d_order, pl->count, &ms))) break;
+    if ((st = timed(t, pl->d_order, pl->count_main, &ms))) break;
     if (ms < best_ms) {
       best_ms = ms;
       best_t = t;
@@ -1001,18 +1288,7 @@ int gb_batch_plan_tune(void *plan) {
     cudaGraphDestroy(pl->graph);
     pl->graph = nullptr;
   }
-  cudaStream_t cap;
-  if (cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking) == cudaSuccess) {
-    if (cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal) == cudaSuccess) {
-      launch_grouped(pl, pl->threads, cap);
-      if (cudaStreamEndCapture(cap, &pl->graph) != cudaSuccess ||
-          cudaGraphInstantiate(&pl->exec, pl->graph, 0) != cudaSuccess) {
-        cudaGetLastError();
-        pl->exec = nullptr;
-      }
-    }
-    cudaStreamDestroy(cap);
-  }
+  capture_plan(pl);
   return finish_blocking(s);
 }
 
@@ -1049,16 +1325,23 @@ int gb_batch_execute_loop(void *plan) {
   GB_CUDA(cudaMemsetAsync(pl->d_loopnext, 0, sizeof(int) * (size_t)pl->count, s));
   // one launch of the same per-problem code for every problem, in table order
   if ((st = grouped_smem_attr())) return st;
-  for (int q = 0; q < pl->count; ++q) {
+  if (pl->count_emu && (st = emu_attr())) return st;
+  for (int q = 0; q < pl->count_emu; ++q) {
+    grouped_emu_kernel<<<1, EM_NT, EM_SMEM, s>>>(pl->d_probs, pl->d_order_emu + q, 1,
+                                                 pl->d_loopnext + q);
+    count_launch();
+  }
+  int *next = pl->d_loopnext + pl->count_emu;
+  for (int q = 0; q < pl->count_main; ++q) {
     if (pl->threads == 128)
-      grouped_kernel<128><<<1, 128, pl->smem, s>>>(pl->d_probs, pl->d_order + q, 1,
-                                                   pl->d_loopnext + q, pl->mixed, pl->blk_nmax);
+      grouped_kernel<128><<<1, 128, pl->smem, s>>>(pl->d_probs, pl->d_order + q, 1, next + q,
+                                                   pl->mixed, pl->blk_nmax);
     else if (pl->threads == 512)
-      grouped_kernel<512><<<1, 512, pl->smem, s>>>(pl->d_probs, pl->d_order + q, 1,
-                                                   pl->d_loopnext + q, pl->mixed, pl->blk_nmax);
+      grouped_kernel<512><<<1, 512, pl->smem, s>>>(pl->d_probs, pl->d_order + q, 1, next + q,
+                                                   pl->mixed, pl->blk_nmax);
     else
-      grouped_kernel<256><<<1, 256, pl->smem, s>>>(pl->d_probs, pl->d_order + q, 1,
-                                                   pl->d_loopnext + q, pl->mixed, pl->blk_nmax);
+      grouped_kernel<256><<<1, 256, pl->smem, s>>>(pl->d_probs, pl->d_order + q, 1, next + q,
+                                                   pl->mixed, pl->blk_nmax);
     count_launch();
   }
   return check_cuda(cudaGetLastError(), "batch loop");
@@ -1203,6 +1486,7 @@ void gb_batch_plan_destroy(void *plan) {
   if (pl->graph) cudaGraphDestroy(pl->graph);
   cudaFree(pl->d_probs);
   cudaFree(pl->d_order);
+  cudaFree(pl->d_order_emu);
   cudaFree(pl->d_next);
   cudaFree(pl->d_work);
   cudaFree(pl->d_loopnext);

@@ -36,6 +36,7 @@
 
 #include "gb_internal.h"
 #include "lapack_internal.h"
+#include "ozaki_digits.cuh"
 #include "sm100_primitives.cuh"
 #include "tma_host.h"
 
@@ -45,8 +46,8 @@ namespace oz {
 
 constexpr int BM = 128, BN = 256, BK = 64;
 constexpr int STAGES = 4;
-constexpr int DIGIT_BITS = 8;  // bits of one slice digit, |digit| <= 255
-constexpr unsigned long long DIGIT_MASK = (1ull << DIGIT_BITS) - 1;
+constexpr int DIGIT_BITS = ozd::DIGIT_BITS;  // bits of one slice digit, |digit| <= 255
+constexpr unsigned long long DIGIT_MASK = ozd::DIGIT_MASK;
 constexpr int KC_BLOCKS = 4;   // K chunk of one exact FP32 accumulation: 256
 constexpr int A_BYTES = BM * BK * 2;
 constexpr int B_BYTES = BN * BK * 2;
@@ -59,7 +60,7 @@ constexpr int64_t MAX_K_SEGMENT = 4096;   // keeps a level sum below 2^31
 static_assert(256LL * 255 * 255 < (1LL << 24), "a 256-deep chunk of one product is exact in FP32");
 static_assert(8LL * MAX_K_SEGMENT * 255 * 255 < (1LL << 31), "a level sum fits int32");
 constexpr uint64_t WAIT_LIMIT_NS = 4000000000ull;
-constexpr int NONFINITE = -100000;  // exponent marker of a row/column with Inf/NaN
+constexpr int NONFINITE = ozd::NONFINITE;  // exponent marker of a row/column with Inf/NaN
 
 struct GemmParams {
   int S;
@@ -541,20 +542,7 @@ __global__ void exponent_kernel(int64_t Rpad, int64_t R, const unsigned long lon
                                 int *__restrict__ expo) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= Rpad) return;
-  int e = 0;
-  if (r < R) {
-    double v = __longlong_as_double((long long)mx[r]);
-    const unsigned long long b = mx[r];
-    const int E = (int)((b >> 52) & 0x7ff);
-    if (E == 0x7ff) {
-      e = NONFINITE;
-    } else if (E > 0) {
-      e = E - 1022;  // max = 1.f * 2^(E-1023) < 2^(E-1022): |x| < 2^e on the row
-    } else if (b != 0) {
-      frexp(v, &e);  // subnormal maximum
-    }
-  }
-  expo[r] = e;
+  expo[r] = r < R ? ozd::exponent_of_max(mx[r]) : 0;  // |x| < 2^e on the row
 }
 
 // Digits of a 32-row x 64-K tile.  The tile is staged through shared memory
@@ -595,26 +583,7 @@ split_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
   unsigned long long mag[8];
   bool neg[8];
 #pragma unroll
-  for (int j = 0; j < 8; ++j) {
-    const unsigned long long bits = (unsigned long long)__double_as_longlong(tile[rr][pc + j]);
-    neg[j] = (bits >> 63) != 0;
-    const int E = (int)((bits >> 52) & 0x7ff);
-    unsigned long long M = bits & 0xFFFFFFFFFFFFFull;
-    int sh;  // |x| = M * 2^(sh0) with sh0 = E - 1075 (normal) or -1074 (subnormal)
-    if (E == 0) {
-      sh = -1074;
-    } else {
-      M |= 1ull << 52;
-      sh = E - 1075;
-    }
-    sh += DIGIT_BITS * S - e;
-    unsigned long long t;
-    if (e == NONFINITE || M == 0) t = 0;
-    else if (sh >= 0) t = M << sh;       // |x| < 2^e keeps t < 2^(8S)
-    else if (sh > -64) t = M >> (-sh);   // truncation toward zero
-    else t = 0;
-    mag[j] = t;
-  }
+  for (int j = 0; j < 8; ++j) mag[j] = ozd::digit_magnitude(tile[rr][pc + j], e, S, neg[j]);
   for (int s = 1; s <= S; ++s) {
     const int sh = DIGIT_BITS * (S - s);
     __align__(16) __nv_bfloat16 out[8];
@@ -629,38 +598,8 @@ split_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
 }
 
 // ------------------------------------------------------------------ recombine
-// One element of C from its exact level sum: acc = sum_L P_L 2^(8(S+1-L))
-// (< 2^88) is rounded once to FP64 (sticky bit), then scaled exactly by
-// alpha * 2^(e_i + f_j - 8(S+1)) through the exponent bits of alpha.
-// y * alpha * 2^x when alpha * 2^x is not a normal number (or alpha is
-// subnormal, zero, Inf or NaN).  The product can still be a normal number
-// (y is up to 2^64), so y is scaled by alpha's significand first and by the
-// whole power of two once: a subnormal or underflowed alpha * 2^x would lose
-// it.  Rarely taken, so kept out of line, away from the recombine loop's
-// registers.
-__device__ __noinline__ double scale_out_of_range(double y, double alpha, int x) {
-  int e_sig;
-  const double m_alpha = frexp(alpha, &e_sig);
-  return ldexp(y * m_alpha, x + e_sig);
-}
-
-__device__ __forceinline__ double level_value(__int128 acc, int S, int ei, int fj, double alpha) {
-  if (acc == 0) return 0.0;
-  const bool neg = acc < 0;
-  unsigned __int128 u = neg ? (unsigned __int128)(-acc) : (unsigned __int128)acc;
-  const unsigned long long hi = (unsigned long long)(u >> 64);
-  const int msb = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)(unsigned long long)u);
-  const int sh = msb > 63 ? msb - 63 : 0;
-  unsigned long long top = (unsigned long long)(u >> sh);
-  if (sh && (u & (((unsigned __int128)1 << sh) - 1)) != 0) top |= 1ull;  // sticky bit
-  const double t = __ull2double_rn(top);
-  const int x = sh - DIGIT_BITS * (S + 1) + ei + fj;
-  const long long ab = __double_as_longlong(alpha);
-  const int e_alpha = (int)((ab >> 52) & 0x7ff);
-  if (e_alpha > 0 && e_alpha < 0x7ff && e_alpha + x > 0 && e_alpha + x < 0x7ff)
-    return (neg ? -t : t) * __longlong_as_double(ab + ((long long)x << 52));
-  return scale_out_of_range(neg ? -t : t, alpha, x);
-}
+// One element of C from its exact level sum: ozd::level_value.
+using ozd::level_value;
 
 // Recombine, one CTA per 128 x 256 tile of C (the plane tile layout): every
 // level plane of the tile is one contiguous 128 KB run, read with 16-byte

@@ -179,3 +179,50 @@ def test_autotune_then_run(orc, gblib, gb_clean):
     keep = _run(gblib, probs, tune=True)
     check(probs, orc)
     del keep
+
+
+def test_emulated_dgemm_and_mixed_dgesv_variant(orc, gblib, gb_clean):
+    """GB_BATCH_EMULATED | GB_BATCH_MIXED: the DGEMM problems on the
+    emulated-FP64 kernel (Ozaki digit slices on the bf16 tensor cores) within
+    the DMMCH bound, the DGESV problems on FP32 LU + FP64 refinement within
+    n*eps backward error, the DPOTRF problems in FP64."""
+    probs = make_batch(120, 7, 8, 200)
+    keep = _run(gblib, probs, flags=BT.GB_BATCH_EMULATED | BT.GB_BATCH_MIXED)
+    check(probs, orc, mixed=True)
+    del keep
+
+
+def test_emulated_dgemm_exact_on_integers_and_special_tiles(gblib, gb_clean):
+    """Integer operands are represented exactly by the 7 digit slices, so the
+    emulated batch DGEMM equals the exact product; a tile holding NaN/Inf
+    and a K beyond 4096 take the FP64 loop and propagate IEEE values."""
+    torch = pytest.importorskip("torch")
+    probs = []
+    for i, (m, n, k) in enumerate([(70, 45, 300), (33, 64, 64), (96, 96, 17)]):
+        A = np.asfortranarray(W.randint(40 + i, (m, k), -(2 ** 20), 2 ** 20).astype(np.float64))
+        B = np.asfortranarray(W.randint(50 + i, (k, n), -255, 255).astype(np.float64))
+        probs.append(dict(type=BT.GB_BATCH_DGEMM, m=m, n=n, k=k, ta="N", tb="N", alpha=1.0,
+                          beta=0.0, A=A, B=B, C=np.zeros((m, n), order="F")))
+    A = W.uniform(60, (40, 50))
+    A[3, 7] = np.nan
+    A[30, 1] = np.inf
+    probs.append(dict(type=BT.GB_BATCH_DGEMM, m=40, n=20, k=50, ta="N", tb="N", alpha=1.0,
+                      beta=0.0, A=A, B=W.uniform(61, (50, 20)), C=np.zeros((40, 20), order="F")))
+    probs.append(dict(type=BT.GB_BATCH_DGEMM, m=24, n=16, k=5000, ta="T", tb="N", alpha=0.5,
+                      beta=0.0, A=W.uniform(62, (5000, 24)), B=W.uniform(63, (5000, 16)),
+                      C=np.zeros((24, 16), order="F")))
+    keep = _run(gblib, probs, flags=BT.GB_BATCH_EMULATED)
+    for p in probs[:3]:
+        exact = (p["A"].astype(object) @ p["B"].astype(object)).astype(np.float64)
+        assert np.array_equal(fetch(p["dC"]), exact)
+    p = probs[3]
+    ref = p["A"] @ p["B"]
+    got = fetch(p["dC"])
+    assert np.array_equal(np.isnan(got), np.isnan(ref))
+    assert np.array_equal(np.isinf(got), np.isinf(ref))
+    fin = np.isfinite(ref)
+    assert np.abs(got[fin] - ref[fin]).max() <= 1e-12 * np.abs(ref[fin]).max()
+    p = probs[4]
+    ref = 0.5 * p["A"].T @ p["B"]
+    assert np.abs(fetch(p["dC"]) - ref).max() <= 1e-11 * np.abs(ref).max()
+    del keep

@@ -272,3 +272,65 @@ def test_automatic_slice_count_per_column_tile(F, emulated, gblib):
     gblib.gb_set_ozaki_slices(0)
     assert np.array_equal(out[0][:, :256], out[7][:, :256])
     assert np.array_equal(out[0][:, 256:], out[8][:, 256:])
+
+
+def test_near_underflow_recombine_matches_native(gblib):
+    """Operands near 2^-512 and 2^-500 give C near 2^-1010: the recombine's
+    scale alpha * 2^x alone would be subnormal there, so the level total is
+    rounded once and scaled by the whole power of two once; the emulated
+    result stays within a few eps of |A||B| of the native FP64 one."""
+    torch = pytest.importorskip("torch")
+    m, n, k = 96, 80, 64
+    A = torch.from_numpy(np.ldexp(W.uniform(90, (m, k)), -512).T.copy()).cuda()
+    B = torch.from_numpy(np.ldexp(W.uniform(91, (k, n)), -500).T.copy()).cuda()
+    Ce = torch.zeros((n, m), dtype=torch.float64, device="cuda")
+    Cn = torch.zeros((n, m), dtype=torch.float64, device="cuda")
+    G = torch.zeros((n, m), dtype=torch.float64, device="cuda")
+    Aa, Ba = A.abs(), B.abs()
+    torch.cuda.synchronize()
+    for Cx, fn, AA, BB in ((Ce, gblib.gb_dgemm_emulated_dev, A, B),
+                           (Cn, gblib.gb_dgemm_native_dev, A, B),
+                           (G, gblib.gb_dgemm_native_dev, Aa, Ba)):
+        args = [b"N", b"N", m, n, k, 1.0, AA.data_ptr(), m, BB.data_ptr(), k, 0.0, Cx.data_ptr(), m]
+        if fn is gblib.gb_dgemm_emulated_dev:
+            args.append(0)
+        assert fn(*args) == 0
+    assert gblib.gb_synchronize() == 0
+    torch.cuda.synchronize()
+    assert float(G.min()) > 0 and float(G.max()) < 2.0 ** -1000
+    err = float(((Ce - Cn).abs() / G).max())
+    assert err <= 4 * (k + 2) * EPS, err / EPS
+
+
+@pytest.mark.parametrize("mode", ["native", "emulated"])
+def test_gemm_taller_than_2_20_rows_equals_row_slices(gblib, mode):
+    """m = 2^20 + 300 rows (beyond the 2^20 block extent, so the product runs
+    block by block over C): every element sees the same row of op(A) and
+    column of op(B), so the result equals, bit for bit, the same GEMM called
+    on row slices that each fit one block."""
+    torch = pytest.importorskip("torch")
+    m, n, k = (1 << 20) + 300, 96, 256
+    g = torch.Generator(device="cuda")
+    g.manual_seed(5)
+    A = torch.rand((k, m), dtype=torch.float64, device="cuda", generator=g) * 2 - 1  # A column-major m x k
+    B = torch.rand((n, k), dtype=torch.float64, device="cuda", generator=g) * 2 - 1  # B column-major k x n
+    C = torch.empty((n, m), dtype=torch.float64, device="cuda")
+    R = torch.empty((n, m), dtype=torch.float64, device="cuda")
+    torch.cuda.synchronize()
+
+    def gemm(rows, r0, out):
+        a = A.data_ptr() + 8 * r0
+        c = out.data_ptr() + 8 * r0
+        if mode == "native":
+            return gblib.gb_dgemm_native_dev(b"N", b"N", rows, n, k, 1.0, a, m, B.data_ptr(), k,
+                                             0.0, c, m)
+        return gblib.gb_dgemm_emulated_dev(b"N", b"N", rows, n, k, 1.0, a, m, B.data_ptr(), k,
+                                           0.0, c, m, 7)
+
+    assert gemm(m, 0, C) == 0
+    step = 1 << 19
+    for r0 in range(0, m, step):
+        assert gemm(min(step, m - r0), r0, R) == 0
+    assert gblib.gb_synchronize() == 0
+    torch.cuda.synchronize()
+    assert torch.equal(C, R)

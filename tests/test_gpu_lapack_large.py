@@ -130,3 +130,40 @@ def test_dsgesv_ill_conditioned_8192(gblib, gb_clean, kappa_exp):
     berr = r / den
     print(f"kappa=1e{kappa_exp}: ITER={it.value} berr={berr / EPS:.2f} eps")
     assert berr <= n * EPS, (it.value, berr / EPS)
+
+
+def _cluster_spectrum_device(torch, seed, n, kappa_exp, nsmall=8):
+    """U diag(s) V^T with s = 1 except the last `nsmall` values, 10^-kappa."""
+    U, _ = torch.linalg.qr(W.uniform_device(seed, (n, n), "cuda").T)
+    V, _ = torch.linalg.qr(W.uniform_device(seed + 1, (n, n), "cuda").T)
+    s = torch.ones(n, dtype=torch.float64, device="cuda")
+    s[-nsmall:] = 10.0 ** -kappa_exp
+    A = (U * s) @ V.T
+    del U, V
+    return A.T.contiguous()
+
+
+@pytest.mark.parametrize("kappa_exp", [8, 12])
+def test_gmres_ir_finishes_when_few_directions_are_small(gblib, gb_clean, kappa_exp):
+    """N = 4096, kappa = 1e8 / 1e12 with 8 tiny singular values: the FP32
+    factors precondition every other direction, so GMRES-IR (ITER = 100 +
+    GMRES iterations) finishes the solve to n*eps backward error without the
+    FP64-accurate fallback."""
+    torch = pytest.importorskip("torch")
+    n = 4096
+    At = _cluster_spectrum_device(torch, 8900 + kappa_exp, n, kappa_exp)
+    A0t = At.clone()
+    b = W.uniform_device(8910 + kappa_exp, (n,), "cuda")
+    x = torch.zeros(n, dtype=torch.float64, device="cuda")
+    ipiv = torch.zeros(n, dtype=torch.int32, device="cuda")
+    it, info = C.c_int(0), C.c_int(0)
+    torch.cuda.synchronize()
+    st = gblib.gb_dsgesv_dev(n, 1, At.data_ptr(), n, ipiv.data_ptr(), b.data_ptr(), n,
+                             x.data_ptr(), n, C.byref(it), C.byref(info))
+    assert st == 0 and info.value == 0
+    assert gblib.gb_synchronize() == 0
+    assert 100 <= it.value < 200, it.value
+    A = A0t.T
+    r = (b - A @ x).abs().max().item()
+    den = A.abs().sum(dim=1).max().item() * x.abs().max().item() + b.abs().max().item()
+    assert r / den <= n * EPS
