@@ -105,8 +105,12 @@ def _const(src: str, name: str) -> int:
     return int(m.group(1))
 
 
+def _csrc(*names):
+    return "".join(open(os.path.join(ROOT, "openblas_gb300", "csrc", n)).read() for n in names)
+
+
 def test_exactness_bounds_of_the_kernel_constants():
-    src = open(os.path.join(ROOT, "openblas_gb300", "csrc", "ozaki.cu")).read()
+    src = _csrc("ozaki_digits.cuh", "ozaki.cu")
     bits = _const(src, "DIGIT_BITS")
     bk = _const(src, "BK")
     chunk = bk * _const(src, "KC_BLOCKS")            # FP32 accumulation depth in TMEM
@@ -227,3 +231,17 @@ def test_fewer_slices_lose_accuracy(orc):
     for lo, hi in zip(errs[1:], errs[:-1]):
         assert lo < hi / 16                          # each slice adds 8 bits
     assert errs[0] > 2 ** -30
+
+
+def test_exactness_bounds_of_the_batched_emulated_kernel():
+    """The grouped emulated DGEMM sums one 64-deep chunk of a digit product in
+    FP32 (mma.sync) and the level sums over all chunks of K <= EM_KMAX in
+    int32; both must stay exact."""
+    src = _csrc("ozaki_digits.cuh", "batched.cu")
+    bits = _const(src, "DIGIT_BITS")
+    dmax = (1 << bits) - 1
+    kc, kmax, s = _const(src, "EM_KC"), _const(src, "EM_KMAX"), _const(src, "EM_S")
+    assert kc % 16 == 0                          # whole m16n8k16 steps
+    assert kc * dmax * dmax < 2 ** 24            # one chunk of one product is exact in FP32
+    assert s * kmax * dmax * dmax < 2 ** 31      # a level sum (<= S products) fits int32
+    assert bits * s <= 64
