@@ -85,40 +85,69 @@ static int dgemm_dispatch(int ta, int tb, int64_t m, int64_t n, int64_t k, doubl
   return dgemm_native(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s);
 }
 
-// Host-pointer emulated DGEMM pipelined over column blocks of op(B) and C.
-// A goes up first and is split once; block j of op(B) (and of C when beta is
-// non-zero) is uploaded on the copy-in stream while earlier blocks compute,
-// and C's block j is downloaded on the copy-out stream while later blocks
-// compute.  The result is the one of the single-call emulated GEMM bit for
-// bit (each C(i,j) sees only row i of op(A) and column j of op(B)).  The
-// upload of block j+1 and the download of block j-1 are issued after block
-// j's kernels, so that pageable host buffers (whose copies the CUDA runtime
-// performs synchronously) still overlap with the GPU.
+// Host-pointer emulated DGEMM pipelined over column blocks of op(B) and C
+// and over the 4096-deep K segments the emulated engine works in.  op(A) and
+// every block of op(B) go up segment by segment, so the first slice GEMM
+// starts once the first segment of op(A) and of block 0 are on the device,
+// while the rest is still on its way; block j+1 uploads on the copy-in
+// stream while block j computes, and C's block j comes down on the copy-out
+// stream while later blocks compute.  The result is the one of the
+// single-call emulated GEMM bit for bit (each C(i,j) sees only row i of
+// op(A) and column j of op(B)).  The upload of block j+1 and the download of
+// block j-1 are issued after block j's kernels, so that pageable host
+// buffers (whose copies the CUDA runtime performs synchronously) still
+// overlap with the GPU.
 namespace {
+constexpr int64_t PIPE_K_SEGMENT = EMU_K_SEGMENT;  // the emulated engine's K segment
 struct PipelinedDgemm : EmuBlockHooks {
   cudaStream_t s = nullptr, cin = nullptr, cout = nullptr;
-  int tb = 0;
-  int64_t m = 0, n = 0, k = 0, nb = 0, ldb = 0, ldc = 0;
-  const double *B = nullptr;
+  int ta = 0, tb = 0;
+  int64_t m = 0, n = 0, k = 0, nb = 0, nseg = 1, lda = 0, ldb = 0, ldc = 0;
+  const double *A = nullptr, *B = nullptr;
   double *C = nullptr;
   bool load_c = false;
-  double *dB = nullptr, *dC = nullptr;
-  int64_t dldb = 0;
-  std::vector<cudaEvent_t> up, done;
+  double *dA = nullptr, *dB = nullptr, *dC = nullptr;
+  int64_t dlda = 0, dldb = 0;
+  std::vector<cudaEvent_t> a_up, up, done;  // a_up[seg], up[block * nseg + seg], done[block]
 
-  int upload(int64_t j) {
-    const int64_t j0 = j * nb, jn = (n - j0) < nb ? (n - j0) : nb;
-    if (tb)  // op(B) = B^T: rows j0.. of the n x k matrix B
-      GB_CUDA(cudaMemcpy2DAsync(dB + j0, dldb * 8, B + j0, ldb * 8, jn * 8, k,
+  int64_t seg_len(int64_t sg) const {
+    const int64_t k0 = sg * PIPE_K_SEGMENT;
+    return (k - k0) < PIPE_K_SEGMENT ? (k - k0) : PIPE_K_SEGMENT;
+  }
+  // segment sg of op(A): columns of A (ta = 0) or rows of A (ta = 1)
+  int upload_a(int64_t sg) {
+    const int64_t k0 = sg * PIPE_K_SEGMENT, kk = seg_len(sg);
+    if (ta)
+      GB_CUDA(cudaMemcpy2DAsync(dA + k0, dlda * 8, A + k0, lda * 8, kk * 8, m,
                                 cudaMemcpyHostToDevice, cin));
     else
-      GB_CUDA(cudaMemcpy2DAsync(dB + j0 * dldb, dldb * 8, B + j0 * ldb, ldb * 8, k * 8, jn,
+      GB_CUDA(cudaMemcpy2DAsync(dA + k0 * dlda, dlda * 8, A + k0 * lda, lda * 8, m * 8, kk,
                                 cudaMemcpyHostToDevice, cin));
-    if (load_c) {
+    GB_CUDA(cudaEventRecord(a_up[sg], cin));
+    return GB_SUCCESS;
+  }
+  // segment sg of block j of op(B) (and C's block with the first segment)
+  int upload(int64_t j, int64_t sg) {
+    const int64_t j0 = j * nb, jn = (n - j0) < nb ? (n - j0) : nb;
+    const int64_t k0 = sg * PIPE_K_SEGMENT, kk = seg_len(sg);
+    if (tb)  // op(B) = B^T: rows j0.. and columns k0.. of the n x k matrix B
+      GB_CUDA(cudaMemcpy2DAsync(dB + j0 + k0 * dldb, dldb * 8, B + j0 + k0 * ldb, ldb * 8, jn * 8,
+                                kk, cudaMemcpyHostToDevice, cin));
+    else
+      GB_CUDA(cudaMemcpy2DAsync(dB + j0 * dldb + k0, dldb * 8, B + j0 * ldb + k0, ldb * 8, kk * 8,
+                                jn, cudaMemcpyHostToDevice, cin));
+    if (load_c && sg == 0) {
       int st = stage_in(dC + j0 * m, C + j0 * ldc, ldc, m, jn, 8, cin);
       if (st) return st;
     }
-    GB_CUDA(cudaEventRecord(up[j], cin));
+    GB_CUDA(cudaEventRecord(up[j * nseg + sg], cin));
+    return GB_SUCCESS;
+  }
+  int upload_block(int64_t j) {
+    for (int64_t sg = 0; sg < nseg; ++sg) {
+      int st = upload(j, sg);
+      if (st) return st;
+    }
     return GB_SUCCESS;
   }
   int download(int64_t j) {
@@ -128,18 +157,23 @@ struct PipelinedDgemm : EmuBlockHooks {
   }
   int before(int64_t j0, int64_t, const double **Bj, int64_t *ldbj, double **Cj,
              int64_t *ldcj) override {
-    GB_CUDA(cudaStreamWaitEvent(s, up[j0 / nb], 0));
     *Bj = tb ? dB + j0 : dB + j0 * dldb;
     *ldbj = dldb;
     *Cj = dC + j0 * m;
     *ldcj = m;
     return GB_SUCCESS;
   }
+  int segment(int64_t j0, int64_t, int64_t k0, int64_t) override {
+    const int64_t sg = k0 / PIPE_K_SEGMENT;
+    GB_CUDA(cudaStreamWaitEvent(s, a_up[sg], 0));
+    GB_CUDA(cudaStreamWaitEvent(s, up[(j0 / nb) * nseg + sg], 0));
+    return GB_SUCCESS;
+  }
   int after(int64_t j0, int64_t) override {
-    const int64_t j = j0 / nb, nblk = (int64_t)up.size();
+    const int64_t j = j0 / nb, nblk = (int64_t)done.size();
     GB_CUDA(cudaEventRecord(done[j], s));
     int st = GB_SUCCESS;
-    if (j + 1 < nblk && (st = upload(j + 1))) return st;
+    if (j + 1 < nblk && (st = upload_block(j + 1))) return st;
     if (j > 0 && (st = download(j - 1))) return st;
     if (j + 1 == nblk) return download(j);
     return GB_SUCCESS;
@@ -163,16 +197,21 @@ static int dgemm_host_pipelined(int ta, int tb, int64_t m, int64_t n, int64_t k,
   nblk = nblk < 2 ? 2 : nblk > 8 ? 8 : nblk;
   p.nb = ((n + nblk - 1) / nblk + 255) / 256 * 256;
   nblk = (n + p.nb - 1) / p.nb;
+  p.ta = ta;
   p.tb = tb;
   p.m = m;
   p.n = n;
   p.k = k;
+  p.nseg = (k + PIPE_K_SEGMENT - 1) / PIPE_K_SEGMENT;
+  p.A = A;
+  p.lda = lda;
   p.B = B;
   p.ldb = ldb;
   p.C = C;
   p.ldc = ldc;
   p.load_c = beta != 0.0;
   const int64_t ra = ta ? k : m, ca = ta ? m : k;
+  p.dlda = ra;
   p.dldb = tb ? n : k;
   Scratch ws(((size_t)ra * ca + (size_t)n * k + (size_t)m * n) * 8, p.s);
   if (!ws.p) {
@@ -180,28 +219,30 @@ static int dgemm_host_pipelined(int ta, int tb, int64_t m, int64_t n, int64_t k,
               (long long)n, (long long)k);
     return 1;
   }
-  double *dA = ws.as<double>();
+  double *dA = p.dA = ws.as<double>();
   p.dB = dA + ra * ca;
   p.dC = p.dB + n * k;
-  p.up.assign(nblk, nullptr);
+  p.a_up.assign(p.nseg, nullptr);
+  p.up.assign(nblk * p.nseg, nullptr);
   p.done.assign(nblk, nullptr);
-  cudaEvent_t ready = nullptr, a_up = nullptr, out_done = nullptr;
+  cudaEvent_t ready = nullptr, out_done = nullptr;
   auto run = [&]() -> int {
-    for (int64_t j = 0; j < nblk; ++j) {
-      GB_CUDA(cudaEventCreateWithFlags(&p.up[j], cudaEventDisableTiming));
-      GB_CUDA(cudaEventCreateWithFlags(&p.done[j], cudaEventDisableTiming));
-    }
+    for (auto *v : {&p.a_up, &p.up, &p.done})
+      for (cudaEvent_t &e : *v) GB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     GB_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
-    GB_CUDA(cudaEventCreateWithFlags(&a_up, cudaEventDisableTiming));
     GB_CUDA(cudaEventCreateWithFlags(&out_done, cudaEventDisableTiming));
     // the staging buffer was allocated on the compute stream
     GB_CUDA(cudaEventRecord(ready, p.s));
     GB_CUDA(cudaStreamWaitEvent(p.cin, ready, 0));
-    int st = stage_in(dA, A, lda, ra, ca, 8, p.cin);
-    if (st) return st;
-    GB_CUDA(cudaEventRecord(a_up, p.cin));
-    if ((st = p.upload(0))) return st;
-    GB_CUDA(cudaStreamWaitEvent(p.s, a_up, 0));
+    // op(A) and block 0 of op(B) segment by segment, interleaved: the first
+    // segment's slice GEMM needs only the first of each
+    int st;
+    for (int64_t sg = 0; sg < p.nseg; ++sg) {
+      if ((st = p.upload_a(sg))) return st;
+      if ((st = p.upload(0, sg))) return st;
+    }
+    // one K segment: op(A) is split once, before the block loop
+    if (p.nseg == 1) GB_CUDA(cudaStreamWaitEvent(p.s, p.a_up[0], 0));
     st = dgemm_emulated_blocked(ta, tb, m, n, k, alpha, dA, ra, beta,
                                 ozaki_caller_slices(), p.nb, &p, p.s);
     // the staging buffer is released on the compute stream after the last download
@@ -214,10 +255,10 @@ static int dgemm_host_pipelined(int ta, int tb, int64_t m, int64_t n, int64_t k,
   cudaStreamSynchronize(p.cout);
   if (!st) finish_blocking(p.s);
   else cudaStreamSynchronize(p.s);
-  for (cudaEvent_t e : p.up) if (e) cudaEventDestroy(e);
-  for (cudaEvent_t e : p.done) if (e) cudaEventDestroy(e);
+  for (auto *v : {&p.a_up, &p.up, &p.done})
+    for (cudaEvent_t e : *v)
+      if (e) cudaEventDestroy(e);
   if (ready) cudaEventDestroy(ready);
-  if (a_up) cudaEventDestroy(a_up);
   if (out_done) cudaEventDestroy(out_done);
   return 1;
 }

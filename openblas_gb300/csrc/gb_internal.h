@@ -176,9 +176,15 @@ int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha
 // device pointers to the block (after making it available, e.g. waiting for
 // its upload) and hooks->after runs once C's block is final (e.g. to start
 // its download), so transfers overlap the other blocks' work.
+// K segment of the emulated engine: every int32 level sum of one segment is
+// exact (8 products x 4096 x 255^2 < 2^31); longer K runs segment by segment.
+constexpr int64_t EMU_K_SEGMENT = 4096;
+// hooks->segment(j0, jn, k0, kk) runs before the K segment [k0, k0 + kk) of
+// the block is used (e.g. to wait for that segment of op(A) and op(B)).
 struct EmuBlockHooks {
   virtual int before(int64_t j0, int64_t jn, const double **Bj, int64_t *ldb, double **Cj,
                      int64_t *ldc) = 0;
+  virtual int segment(int64_t, int64_t, int64_t, int64_t) { return GB_SUCCESS; }
   virtual int after(int64_t j0, int64_t jn) = 0;
   virtual ~EmuBlockHooks() = default;
 };

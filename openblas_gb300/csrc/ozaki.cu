@@ -56,7 +56,7 @@ constexpr int NUM_THREADS = 320;
 constexpr int TMEM_COLS = 512;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr int MAX_SLICES = 8;
-constexpr int64_t MAX_K_SEGMENT = 4096;   // keeps a level sum below 2^31
+constexpr int64_t MAX_K_SEGMENT = EMU_K_SEGMENT;   // keeps a level sum below 2^31
 static_assert(256LL * 255 * 255 < (1LL << 24), "a 256-deep chunk of one product is exact in FP32");
 static_assert(8LL * MAX_K_SEGMENT * 255 * 255 < (1LL << 31), "a level sum fits int32");
 constexpr uint64_t WAIT_LIMIT_NS = 4000000000ull;
@@ -854,6 +854,7 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       const int64_t k0 = sg * MAX_K_SEGMENT;
       const int64_t kk = (k - k0) < MAX_K_SEGMENT ? (k - k0) : MAX_K_SEGMENT;
       const int64_t kp = round_up(kk, BK);
+      if (hooks && (st = hooks->segment(j0, jn, k0, kk))) return st;
       if (nseg > 1 && (st = split_a(k0, kk))) return st;
       const double *Ak = ta ? A + k0 : A + k0 * lda;
       const double *Bk = tb ? Bj + k0 * ldbj : Bj + k0;

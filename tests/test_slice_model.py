@@ -110,11 +110,11 @@ def _csrc(*names):
 
 
 def test_exactness_bounds_of_the_kernel_constants():
-    src = _csrc("ozaki_digits.cuh", "ozaki.cu")
+    src = _csrc("ozaki_digits.cuh", "ozaki.cu", "gb_internal.h")
     bits = _const(src, "DIGIT_BITS")
     bk = _const(src, "BK")
     chunk = bk * _const(src, "KC_BLOCKS")            # FP32 accumulation depth in TMEM
-    seg = _const(src, "MAX_K_SEGMENT")               # int32 level-sum depth
+    seg = int(re.search(r"EMU_K_SEGMENT\s*=\s*(\d+)", src).group(1))  # int32 level-sum depth
     dmax = (1 << bits) - 1
     assert bits == DIGIT_BITS
     assert chunk * dmax * dmax < 2 ** 24             # every FP32 partial sum is an exact integer
