@@ -61,7 +61,8 @@ def parse_args():
 
 
 def workload_config(n, slices):
-    how = f"{slices} 8-bit slices" if slices > 0 else "8-bit slices chosen for 8 eps"
+    how = f"{slices} 8-bit slices" if slices > 0 else \
+        "per 256-column tile the modular scheme or the fewest 8-bit slices meeting 8 eps"
     return {
         "workload": f"DGEMM NN M=N=K={n}, alpha=1, beta=0, A,B,C uniform(-1,1) seeded; "
                     f"FP64-accuracy emulation ({how}) vs native FP64",
@@ -170,13 +171,14 @@ def measured_peaks():
             "fallback"
 
 
-def profiled_traffic(n):
-    """DRAM bytes per slice-GEMM launch from the committed ncu summary
-    (dram__bytes_read.sum + dram__bytes_write.sum, one-pass capture).  A
-    capture at exactly n is used as is; otherwise the nearest captured size
-    is scaled by n^3 (every tile re-reads its K-panel of slices for each
-    product) and the result says so."""
-    path = os.path.join(ROOT, "profiles", "slice_gemm_ncu.txt")
+def profiled_traffic(n, kernel="slice_gemm"):
+    """DRAM bytes per launch of the tensor-core kernel (`slice_gemm` or
+    `residue_gemm`) from its committed ncu summary (dram__bytes_read.sum +
+    dram__bytes_write.sum, one-pass capture).  A capture at exactly n is used
+    as is; otherwise the nearest captured size is scaled by n^3 (every tile
+    re-reads its K-panel of operands for each product) and the result says
+    so."""
+    path = os.path.join(ROOT, "profiles", f"{kernel}_ncu.txt")
     caps = {}
     try:
         for line in open(path):
@@ -355,19 +357,28 @@ def run_suite(args):
                                               Ba.data_ptr(), n, 0.0, Ga.data_ptr(), n))
                 del Aa, Ba
             Ce = torch.empty((n, n), dtype=torch.float64, device="cuda")
-            # S = 0: the automatic count (the library default), recorded as chosen
-            for S in ((0, 5, 6, 7, 8) if n == 8192 else (0, 7)):
+            # S = 0: the automatic choice (the library default: modular
+            # scheme or slice count per tile), "0s": automatic with digit
+            # slices only
+            variants = (0, "0s", 5, 6, 7, 8) if n == 8192 else (0, "0s", 7)
+            for S in variants:
+                modular = 0 if S == "0s" else 1
+                Sv = 0 if S == "0s" else S
+                lib.gb_set_ozaki_modular(modular)
                 ms = _time_dev(torch, stream, lambda: check(lib.gb_dgemm_emulated_dev(
                     b"N", b"N", n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.0,
-                    Ce.data_ptr(), n, S)), reps=3 if n == 8192 else 2)
-                tag = f"s{S}" if S else "auto"
-                how = f"{S} slices" if S else \
-                    f"automatic count ({lib.gb_last_ozaki_slices()} slices chosen)"
+                    Ce.data_ptr(), n, Sv)), reps=3 if n == 8192 else 2)
+                lib.gb_set_ozaki_modular(1)
+                tag = f"s{S}" if Sv else ("auto" if modular else "auto_slices")
+                chosen_m, chosen_s = lib.gb_last_ozaki_moduli(), lib.gb_last_ozaki_slices()
+                how = f"{Sv} slices" if Sv else \
+                    f"automatic choice ({chosen_m} moduli, {chosen_s} slices)"
                 d = {"suite": f"dgemm_emulated_{n}_e{e}_{tag}",
                      "workload": f"emulated DGEMM NN {n}^3, A,B = U.*2^E, E in [-{e},{e}], {how}",
                      "value": 2 * n ** 3 / ms / 1e9, "unit": UNIT, "ms": ms}
-                if not S:
-                    d["slices_chosen"] = lib.gb_last_ozaki_slices()
+                if not Sv:
+                    d["slices_chosen"] = chosen_s
+                    d["moduli_chosen"] = chosen_m
                 if Cn is not None:
                     torch.cuda.synchronize()
                     diff = (Ce - Cn).abs()
@@ -958,14 +969,19 @@ def main():
     for _ in range(args.warmup):
         emulated_step()
     torch.cuda.synchronize()
-    S_used = S if S > 0 else lib.gb_last_ozaki_slices()  # the count the step runs with
+    # what the step runs with: the modular scheme (14 residue products per
+    # output tile) or S digit slices (S(S+1)/2 products)
+    moduli = 0 if S > 0 else lib.gb_last_ozaki_moduli()
+    S_used = S if S > 0 else lib.gb_last_ozaki_slices()
+    kernel = "residue_gemm" if moduli else "slice_gemm"
+    products = moduli if moduli else S_used * (S_used + 1) // 2
 
     clocks = ClockSampler(local)
     clocks.start()
     time.sleep(0.3)
     e0 = torch.cuda.Event(enable_timing=True)
     e1 = torch.cuda.Event(enable_timing=True)
-    lib.gb_profile_kernel_ms(b"slice_gemm", None, 1)
+    lib.gb_profile_kernel_ms(kernel.encode(), None, 1)
     lib.gb_profile_enable(1)
     launches0 = lib.gb_kernel_launches()
     barrier(world)
@@ -979,7 +995,7 @@ def main():
     launches = lib.gb_kernel_launches() - launches0
     lib.gb_profile_enable(0)
     cnt = C.c_int(0)
-    kern_ms = lib.gb_profile_kernel_ms(b"slice_gemm", C.byref(cnt), 1) / max(cnt.value, 1)
+    kern_ms = lib.gb_profile_kernel_ms(kernel.encode(), C.byref(cnt), 1) / max(cnt.value, 1)
     clk = clocks.stop()
     ms = allreduce_max(e0.elapsed_time(e1) / args.steps, world)
     flops = 2.0 * n ** 3
@@ -1047,20 +1063,23 @@ def main():
         batched = batched_compare(lib, torch, gb)
 
     peaks, src = measured_peaks()
-    # K runs in segments (4096 deep), one slice-GEMM launch per segment
+    # K runs in segments (4096 deep), one tensor-core launch per segment
     launches_per_step = max(cnt.value / args.steps, 1.0)
-    slice_flops = S_used * (S_used + 1) / 2 * flops / launches_per_step
+    slice_flops = products * flops / launches_per_step
     achieved = slice_flops / (kern_ms * 1e-3) / 1e12
     peak = float(peaks.get("bf16_tflops_sustained", 1700.0))
-    traffic, traffic_src = profiled_traffic(n)
+    traffic, traffic_src = profiled_traffic(n, kernel)
     line = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
         "warmup": args.warmup, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak",
         "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": workload_config(n, S),
-        "precision": {"method": "ozaki-8bit-slices-bf16-tcgen05", "slices": S_used,
+        "precision": {"method": ("ozaki-modular-residues-bf16-tcgen05" if moduli else
+                                 "ozaki-8bit-slices-bf16-tcgen05"),
+                      "moduli": moduli, "slices": S_used, "tensor_products_per_tile": products,
                       "slice_choice": "fixed" if S > 0 else
-                      "automatic: smallest count whose worst-case bound is <= 8 eps",
+                      "automatic: per 256-column tile the modular scheme where its worst-case "
+                      "bound is <= 8 eps, else the fewest slices that meet it",
                       "normwise_err_vs_native_fp64_eps": err_norm,
                       "componentwise_err_vs_native_fp64_eps": err_comp},
         "native_fp64": {"value": native_tflops * world, "unit": UNIT, "ms_per_step": native_ms,
@@ -1068,7 +1087,9 @@ def main():
         "e2e": {"value": world * flops / e2e_dt / 1e12, "unit": UNIT,
                 "h2d_bytes_per_step": 2 * n * n * 8, "d2h_bytes_per_step": n * n * 8,
                 "api": "cblas_dgemm (host pointers, pinned), GB_DGEMM_MODE=emulated"},
-        "roofline": {"bound": "tensor", "kernel": "slice_gemm_kernel (tcgen05 kind::f16)",
+        "roofline": {"bound": "tensor",
+                     "kernel": f"slice_gemm_kernel<{'true' if moduli else 'false'}> ({kernel}, "
+                               "tcgen05 kind::f16)",
                      "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
                      "frac": achieved / peak, "traffic": traffic, "traffic_source": traffic_src,
                      "peak_source": f"{src} bf16_tflops_sustained",

@@ -263,18 +263,35 @@ int gb_set_sgemm_mode(int mode);
 int gb_get_sgemm_mode(void);
 /* Slice count of the emulated DGEMM behind dgemm_/cblas_dgemm and the other
  * caller-facing GEMMs (1..8 fixed).  0 (the default; GB_OZAKI_SLICES=auto)
- * chooses the count per 256-column tile of C on the device: the smallest S
- * for which a worst-case bound on every column's error,
- *   sum_i |dC_ij| <= 2^-8S (T_e ||b_j||_1 + 2^f_j (T_1 + 7.06 k T_e)) + roundings,
- * stays within GB_OZAKI_TOL (default 8) x 2^-52 times that column's
- * sum_i (|A||B|)_ij (2^f_j: column j's scale, T_e: the sum of the rows'
- * scales, T_1 = sum |A|, k: the K segment).  Uniform operands get 7 slices,
- * operands whose entries span 2^16 or more get 8; 8 is the most there is.
- * The LU/Cholesky trailing updates always use 7. */
+ * chooses per 256-column tile of C on the device, from worst-case bounds on
+ * every column's error measured against GB_OZAKI_TOL (default 8) x 2^-52
+ * times that column's sum_i (|A||B|)_ij:
+ *  - the modular scheme (unless turned off, below) when its bound
+ *      sum_i |dC_ij| <= 2^-t (T_e ||b_j||_1 + 2^f_j (T_1 + 2^-t k T_e)) + roundings
+ *    meets the tolerance: op(A) and op(B) cut to t-bit integers (t = 56 for a
+ *    K segment of 4096), their product computed exactly from 14 residue
+ *    products (moduli 461..511, residues on the bf16 tensor cores) and the
+ *    Chinese remainder theorem;
+ *  - otherwise the smallest slice count S of the digit-slice scheme with
+ *      sum_i |dC_ij| <= 2^-8S (T_e ||b_j||_1 + 2^f_j (T_1 + 7.06 k T_e)) + roundings
+ *    within the tolerance (S(S+1)/2 slice products; 8 is the most there is).
+ * (2^f_j: column j's scale, T_e: the sum of the rows' scales, T_1 = sum |A|,
+ * k: the K segment.)  Uniform and exponent-spread operands take the
+ * modular scheme; digit slices (8) are left for columns whose error bound it
+ * cannot meet, e.g. rows scaled far above the entries that meet the column.
+ * The LU/Cholesky trailing updates always use 7 slices. */
 int gb_set_ozaki_slices(int slices);
 /* Largest slice count chosen by the calling thread's last automatic-mode
- * emulated DGEMM (0 if none); synchronises the thread's stream. */
+ * emulated DGEMM for its digit-slice tiles (0 if none); synchronises the
+ * thread's stream. */
 int gb_last_ozaki_slices(void);
+/* Moduli used by the calling thread's last automatic-mode emulated DGEMM
+ * (14 when any tile took the modular scheme, else 0); synchronises the
+ * thread's stream. */
+int gb_last_ozaki_moduli(void);
+/* Automatic mode's modular scheme for the calling thread: 1 allowed (the
+ * default; GB_OZAKI_MODULAR=0 changes it), 0 digit slices only. */
+int gb_set_ozaki_modular(int on);
 /* Library version string. */
 const char *gb_version(void);
 

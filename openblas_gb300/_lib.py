@@ -29,6 +29,8 @@ DEV_SIGS = {
     "gb_get_sgemm_mode": (_i, []),
     "gb_set_ozaki_slices": (_i, [_i]),
     "gb_last_ozaki_slices": (_i, []),
+    "gb_last_ozaki_moduli": (_i, []),
+    "gb_set_ozaki_modular": (_i, [_i]),
     "gb_version": (C.c_char_p, []),
     "gb_kernel_launches": (C.c_int64, []),
     "gb_profile_enable": (_i, [_i]),

@@ -85,6 +85,8 @@ const Config &config() {
     if (sm) g_cfg.sgemm_mode = !strcmp(sm, "simt") ? 1 : !strcmp(sm, "tensor") ? 2 : 0;
     const char *tol = getenv("GB_OZAKI_TOL");
     if (tol && atof(tol) > 0.0) g_cfg.ozaki_tol = atof(tol);
+    const char *om = getenv("GB_OZAKI_MODULAR");
+    if (om) g_cfg.ozaki_modular = atoi(om) != 0;
     const char *la = getenv("GB_LU_LOOKAHEAD");
     if (la) g_cfg.lu_lookahead = atoi(la) != 0;
     const char *g = getenv("GB_OZAKI_GROUP_M");
@@ -336,6 +338,7 @@ int gb_last_xerbla(char *name, int len) {
 
 static thread_local int t_dgemm_mode = -1;
 static thread_local int t_ozaki_slices = -1;
+static thread_local int t_ozaki_modular = -1;
 static thread_local int t_sgemm_mode = -1;
 
 int gb_set_sgemm_mode(int mode) {
@@ -382,6 +385,22 @@ int gb_last_ozaki_slices(void) {
   return v;
 }
 
+int gb_last_ozaki_moduli(void) {
+  if (!gb::ctx().d_status || !gb::ctx().stream) return 0;
+  cudaError_t e = cudaStreamSynchronize(gb::stream());
+  if (e != cudaSuccess) return -gb::check_cuda(e, "gb_last_ozaki_moduli");
+  int v = 0;
+  e = cudaMemcpy(&v, gb::ctx().d_status + gb::STATUS_LAST_MODULI, sizeof(int),
+                 cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return -gb::check_cuda(e, "gb_last_ozaki_moduli");
+  return v;
+}
+
+int gb_set_ozaki_modular(int on) {
+  t_ozaki_modular = on != 0;
+  return GB_SUCCESS;
+}
+
 const char *gb_version(void) { return "libgbblas 0.1 (sm_103a)"; }
 
 int64_t gb_kernel_launches(void) { return gb::g_launches.load(); }
@@ -418,5 +437,8 @@ namespace gb {
 int ozaki_caller_slices() {
   const int s = gb_get_ozaki_slices_internal();
   return s > 0 ? s : OZAKI_SLICES_AUTO;
+}
+bool ozaki_modular_enabled() {
+  return t_ozaki_modular >= 0 ? t_ozaki_modular != 0 : config().ozaki_modular != 0;
 }
 }  // namespace gb

@@ -40,9 +40,11 @@ struct Context {
 };
 // d_status[0..3]: kernel error code and site (read and cleared by
 // gb_synchronize / the blocking entries); d_status[STATUS_LAST_SLICES]: the
-// largest slice count the last automatic-mode emulated DGEMM chose.
+// largest slice count the last automatic-mode emulated DGEMM chose;
+// d_status[STATUS_LAST_MODULI]: its moduli count (0: no modular tile).
 constexpr int STATUS_WORDS = 8;
 constexpr int STATUS_LAST_SLICES = 4;
+constexpr int STATUS_LAST_MODULI = 5;
 Context &ctx();
 // Lazily initialise CUDA for this thread; returns GB_SUCCESS or an error.
 int ensure_init();
@@ -114,6 +116,7 @@ struct Config {
   int sgemm_mode = 0;                 // GB_SGEMM_MODE: 0 auto, 1 simt, 2 tensor
   int ozaki_group_m = 8;              // GB_OZAKI_GROUP_M: m-tiles per slice-GEMM tile group
   double ozaki_tol = 8.0;             // GB_OZAKI_TOL: automatic slice count's bound, units of 2^-52
+  int ozaki_modular = 1;              // GB_OZAKI_MODULAR: automatic mode may take the modular scheme
   int lu_lookahead = 1;               // GB_LU_LOOKAHEAD: factor the next LU panel ahead (0: off)
 };
 const Config &config();
@@ -163,6 +166,9 @@ constexpr int OZAKI_SLICES_AUTO = -1;
 // The count for a caller-facing emulated GEMM: the thread's fixed setting
 // (gb_set_ozaki_slices / GB_OZAKI_SLICES), or OZAKI_SLICES_AUTO when unset/0.
 int ozaki_caller_slices();
+// Whether the calling thread's automatic mode may take the modular scheme
+// (gb_set_ozaki_modular / GB_OZAKI_MODULAR).
+bool ozaki_modular_enabled();
 // Emulated-FP64 GEMM (Ozaki slices on the bf16 tensor cores).  slices = 0:
 // default count (7); OZAKI_SLICES_AUTO: chosen on the device.  tri = 1 (2): only C(i,j) with i >= j (i <= j) is written,
 // tiles wholly in the other triangle are skipped (SYRK-shaped updates).

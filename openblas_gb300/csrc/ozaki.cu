@@ -21,6 +21,24 @@
 //      + beta*C_ij.  Rows/columns holding Inf/NaN fall back to a direct FP64
 //      dot product so IEEE special values propagate.
 //
+// Modular scheme (automatic mode, tiles whose error bound it meets; Ozaki,
+// Uchino and Imamura, "Ozaki Scheme II: a GEMM-oriented emulation of
+// floating-point matrix multiplication using an integer modular technique"):
+//   1. split: row i of op(A) is cut to the t-bit integers
+//      A'_ik = sign(a_ik) trunc(|a_ik| 2^(t - e_i)), |A'_ik| < 2^t, column j of
+//      op(B) likewise, and each is stored as its symmetric residues modulo
+//      14 pairwise coprime odd moduli p_l in [461, 511] (|residue| <= 255,
+//      exact in bf16, the same bound as a slice digit).
+//   2. residue GEMM: the same tensor-core kernel, one product per modulus
+//      (A' mod p_l)(B' mod p_l)^T with exact FP32 chunks and int32 sums,
+//      reduced mod p_l in the epilogue: 14 products instead of the 28 of
+//      7 digit slices.
+//   3. reconstruct: the Chinese remainder theorem gives C' = A'B' exactly
+//      (M = prod p_l ~ 2^125.06 > 2 k 2^2t: t = 56 for K segments of 4096),
+//      then C_ij = alpha 2^(e_i + f_j - 2t) C'_ij + beta C_ij, rounded once.
+//   No product is dropped: the only error is the cut of the operands, so the
+//   bound is 2^-t (2^e_i ||b_j||_1 + 2^f_j ||a_i||_1 + 2^-t k 2^(e_i + f_j)).
+//
 // The slice GEMM is a persistent warp-specialised kernel, one CTA per SM:
 // warp 0 issues TMA loads of 128x64 (A) and 256x64 (B) bf16 tiles into a
 // 4-stage shared-memory ring, warp 1 issues tcgen05.mma (M=128, N=256,
@@ -62,6 +80,24 @@ static_assert(8LL * MAX_K_SEGMENT * 255 * 255 < (1LL << 31), "a level sum fits i
 constexpr uint64_t WAIT_LIMIT_NS = 4000000000ull;
 constexpr int NONFINITE = ozd::NONFINITE;  // exponent marker of a row/column with Inf/NaN
 
+// ------------------------------------------------------------ modular scheme
+constexpr int MOD_COUNT = 14;       // moduli of the modular scheme
+constexpr int MOD_CHUNK_BITS = 12;  // A' is read in 12-bit chunks to form its residues
+constexpr int MOD_CHUNKS = 5;       // 60 bits: t <= 60
+constexpr int MOD_MAX_BITS = MOD_CHUNK_BITS * MOD_CHUNKS;
+static_assert(4096.0 * 511 * MOD_CHUNKS < 16777216.0, "a residue's chunk sum is exact in FP32");
+
+// Constants of the modular scheme for one call (kernel argument).
+struct ModTable {
+  int bits;                          // t: operands are cut to t-bit integers
+  float pf[MOD_COUNT];               // p_l
+  float pinv[MOD_COUNT];             // 1 / p_l (rounded)
+  float pw[MOD_COUNT][MOD_CHUNKS];   // 2^(12 d) mod p_l
+  uint32_t F[MOD_COUNT];             // round(2^32 u_l / p_l), u_l = (M / p_l)^-1 mod p_l
+  uint32_t W[MOD_COUNT][4];          // CRT weight (M / p_l) u_l, 32-bit limbs, low first
+  uint32_t M[4];                     // M = prod p_l, 32-bit limbs
+};
+
 struct GemmParams {
   int S;
   int m_tiles, n_tiles;
@@ -72,8 +108,42 @@ struct GemmParams {
   int64_t plane_stride;
   int *planes;
   int *status;
-  const int *s_tiles;  // per n-tile slice count (automatic mode), or null: S everywhere
+  // Digit slices: per n-tile slice count (automatic mode; 0 = a modular
+  // tile, skipped), or null: S everywhere.  Modular: the tiles with
+  // s_tiles[nt] == 0 (all when null) take part.
+  const int *s_tiles;
+  const int *run_if;   // when non-null and *run_if == 0 the launch does nothing
+  int mod_p[MOD_COUNT];  // moduli (modular scheme)
 };
+
+// Products of one output tile, in levels that share an accumulation: digit
+// slices have levels L = s + t = 2..S+1 (the Ozaki triangle) holding the
+// pairs (s, L - s); the modular scheme has one level per modulus holding
+// its residue product.  Slice indices are 0-based here.
+template <bool MOD>
+__device__ __forceinline__ int tile_levels(int nt, const GemmParams &p) {
+  if (MOD) return (!p.s_tiles || p.s_tiles[nt] == 0) ? MOD_COUNT : 0;
+  return p.s_tiles ? p.s_tiles[nt] : p.S;
+}
+template <bool MOD>
+__device__ __forceinline__ void level_products(int l, int nl, int &lo, int &hi) {
+  if (MOD) {
+    lo = hi = l;
+    return;
+  }
+  const int L = l + 2;
+  lo = L - nl > 1 ? L - nl : 1;
+  hi = L - 1 < nl ? L - 1 : nl;
+}
+template <bool MOD>
+__device__ __forceinline__ void product_slices(int l, int s, int &sa, int &sb) {
+  if (MOD) {
+    sa = sb = l;
+    return;
+  }
+  sa = s - 1;
+  sb = l + 1 - s;  // t - 1 with t = L - s, L = l + 2
+}
 
 // Tile order: groups of group_m m-tiles, walked column by column inside a
 // group, so the tiles resident at one time cover a near-square block of C
@@ -97,10 +167,12 @@ __device__ __forceinline__ bool tile_active(int mt, int nt, const GemmParams &p)
   return true;
 }
 
+template <bool MOD>
 __global__ void __launch_bounds__(NUM_THREADS, 1)
 slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
-                  const GemmParams p) {
+                  const __grid_constant__ GemmParams p) {
   using namespace sm100;
+  if (p.run_if && *p.run_if == 0) return;  // every thread reads the same word
   extern __shared__ uint8_t smem_raw[];
   uint8_t *smem = reinterpret_cast<uint8_t *>(
       (reinterpret_cast<uintptr_t>(smem_raw) + 1023) & ~uintptr_t(1023));
@@ -160,13 +232,15 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         int mt, nt;
         tile_coords(tile, p, mt, nt);
         if (!tile_active(mt, nt, p)) continue;
-        const int S = p.s_tiles ? p.s_tiles[nt] : p.S;
-        for (int L = 2; ok && L <= S + 1; ++L) {
-          const int s_lo = L - S > 1 ? L - S : 1, s_hi = L - 1 < S ? L - 1 : S;
+        const int nl = tile_levels<MOD>(nt, p);
+        for (int l = 0; ok && l < nl; ++l) {
+          int s_lo, s_hi;
+          level_products<MOD>(l, nl, s_lo, s_hi);
           for (int s = s_lo; ok && s <= s_hi; ++s) {
-            const int t = L - s;
-            const int rowA = (s - 1) * p.m_pad + mt * BM;
-            const int rowB = (t - 1) * p.n_pad + nt * BN;
+            int sa, sb;
+            product_slices<MOD>(l, s, sa, sb);
+            const int rowA = sa * p.m_pad + mt * BM;
+            const int rowB = sb * p.n_pad + nt * BN;
             for (int kc = 0; ok && kc < nkc; ++kc) {
               const int kb1 = min(p.kblocks, (kc + 1) * KC_BLOCKS);
               for (int kb = kc * KC_BLOCKS; kb < kb1; ++kb) {
@@ -207,9 +281,10 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         int mt, nt;
         tile_coords(tile, p, mt, nt);
         if (!tile_active(mt, nt, p)) continue;
-        const int S = p.s_tiles ? p.s_tiles[nt] : p.S;
-        for (int L = 2; ok && L <= S + 1; ++L) {
-          const int s_lo = L - S > 1 ? L - S : 1, s_hi = L - 1 < S ? L - 1 : S;
+        const int nl = tile_levels<MOD>(nt, p);
+        for (int l = 0; ok && l < nl; ++l) {
+          int s_lo, s_hi;
+          level_products<MOD>(l, nl, s_lo, s_hi);
           for (int s = s_lo; ok && s <= s_hi; ++s) {
             for (int kc = 0; ok && kc < nkc; ++kc) {
               if (!mbar_wait(&tempty[acc], acc_phase ^ 1u, abort_flag, WAIT_LIMIT_NS)) {
@@ -267,12 +342,13 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       int mt, nt;
       tile_coords(tile, p, mt, nt);
       if (!tile_active(mt, nt, p)) continue;
-      const int S = p.s_tiles ? p.s_tiles[nt] : p.S;
+      const int nl = tile_levels<MOD>(nt, p);
       const int64_t plane_tile = (int64_t)nt * p.m_tiles + mt;
-      for (int L = 2; ok && L <= S + 1; ++L) {
+      for (int l = 0; ok && l < nl; ++l) {
 #pragma unroll
         for (int c = 0; c < 128; ++c) sum[c] = 0;
-        const int s_lo = L - S > 1 ? L - S : 1, s_hi = L - 1 < S ? L - 1 : S;
+        int s_lo, s_hi;
+        level_products<MOD>(l, nl, s_lo, s_hi);
         for (int s = s_lo; ok && s <= s_hi; ++s) {
           for (int kc = 0; kc < nkc; ++kc) {
             const bool got = mbar_wait(&tfull[acc], acc_phase, abort_flag, WAIT_LIMIT_NS);
@@ -302,11 +378,23 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         }
         if (!ok) break;
         // level plane, tile-blocked and column-major inside the tile so a
-        // warp's store of one column is 128 contiguous bytes
-        int *dst = p.planes + (int64_t)(L - 2) * p.plane_stride + plane_tile * (BM * BN) +
-                   (int64_t)(half * 128) * BM + row;
+        // warp's store of one column is contiguous
+        const int64_t at = (int64_t)l * p.plane_stride + plane_tile * (BM * BN) +
+                           (int64_t)(half * 128) * BM + row;
+        if (MOD) {
+          // residue of the product modulo p_l, in [0, p_l), as 16 bits
+          const int pm = p.mod_p[l];
+          uint16_t *dst = reinterpret_cast<uint16_t *>(p.planes) + at;
 #pragma unroll
-        for (int c = 0; c < 128; ++c) dst[c * BM] = sum[c];
+          for (int c = 0; c < 128; ++c) {
+            int r = sum[c] % pm;
+            dst[c * BM] = (uint16_t)(r < 0 ? r + pm : r);
+          }
+        } else {
+          int *dst = p.planes + at;
+#pragma unroll
+          for (int c = 0; c < 128; ++c) dst[c * BM] = sum[c];
+        }
       }
     }
   }
@@ -503,30 +591,49 @@ __global__ void rowmax_stats_mcontig_kernel(int64_t R, int64_t K, const double *
   atomicAdd(s2 + r, a2);
 }
 
-// One block per 256-column tile of C: the tile's largest rho_j and from it
-// the slice count; the largest count of the call is kept in *last.
+// One block per 256-column tile of C: the tile's largest rho_j (digit
+// slices) and rho2_j (modular scheme, t = mod_t bits; 0: not allowed), in
+//   rho2_j = (T_e ||b_j||_1 + 2^f_j (T_1 + 2^-t k T_e)) / w_j
+// (no dropped products, only the cut of the operands).  The tile takes the
+// modular scheme when 2^-t max rho2_j meets the budget (s_tiles = 0,
+// counted in pass[0], the call's moduli count kept in *last_moduli), else
+// the smallest slice count that does (counted in pass[1], the largest count
+// of the call kept in *last).
 __global__ void __launch_bounds__(256)
 choose_slices_kernel(int64_t R, const int *__restrict__ expo,
                      const unsigned long long *__restrict__ mx, const double *__restrict__ s1,
                      const double *__restrict__ s2, const double *__restrict__ totals, int64_t k,
-                     double budget, int *__restrict__ s_tiles, int *__restrict__ last) {
+                     double budget, int mod_t, int *__restrict__ s_tiles, int *__restrict__ last,
+                     int *__restrict__ last_moduli, int *__restrict__ pass) {
   const int64_t j = (int64_t)blockIdx.x * BN + threadIdx.x;
-  double rho = 0.0;
+  double rho = 0.0, rho2 = 0.0;
   if (j < R && mx[j] != 0 && expo[j] != NONFINITE && s2[j] > 0.0) {
     const double te = totals[0], t1 = totals[1];
     rho = (te * s1[j] + ldexp(t1 + DROP_C * (double)k * te, expo[j])) / s2[j];
+    rho2 = (te * s1[j] + ldexp(t1 + ldexp((double)k * te, -mod_t), expo[j])) / s2[j];
     if (!(rho <= 1e300)) rho = 1e300;  // Inf or NaN: the largest count
+    if (!(rho2 <= 1e300)) rho2 = 1e300;
   } else if (j < R && mx[j] != 0 && expo[j] != NONFINITE && s2[j] != 0.0) {
-    rho = 1e300;  // w_j NaN
+    rho = rho2 = 1e300;  // w_j NaN
   }
-  __shared__ double red[256];
+  __shared__ double red[256], red2[256];
   red[threadIdx.x] = rho;
+  red2[threadIdx.x] = rho2;
   __syncthreads();
   for (int h = 128; h > 0; h >>= 1) {
-    if ((int)threadIdx.x < h) red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + h]);
+    if ((int)threadIdx.x < h) {
+      red[threadIdx.x] = fmax(red[threadIdx.x], red[threadIdx.x + h]);
+      red2[threadIdx.x] = fmax(red2[threadIdx.x], red2[threadIdx.x + h]);
+    }
     __syncthreads();
   }
   if (threadIdx.x == 0) {
+    if (mod_t > 0 && ldexp(red2[0], -mod_t) <= budget) {
+      s_tiles[blockIdx.x] = 0;
+      atomicAdd(pass, 1);
+      atomicMax(last_moduli, MOD_COUNT);
+      return;
+    }
     int S = MAX_SLICES;
     for (int c = 1; c < MAX_SLICES; ++c)
       if (ldexp(red[0], -DIGIT_BITS * c) <= budget) {
@@ -534,6 +641,7 @@ choose_slices_kernel(int64_t R, const int *__restrict__ expo,
         break;
       }
     s_tiles[blockIdx.x] = S;
+    atomicAdd(pass + 1, 1);
     atomicMax(last, S);
   }
 }
@@ -552,10 +660,13 @@ template <bool KCONTIG>
 __global__ void __launch_bounds__(256)
 split_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
              const int *__restrict__ expo, int S, int64_t Rpad, int64_t Kpad,
-             __nv_bfloat16 *__restrict__ slices, const int *__restrict__ s_tiles) {
+             __nv_bfloat16 *__restrict__ slices, const int *__restrict__ s_tiles,
+             const int *__restrict__ run_if) {
   __shared__ double tile[32][65];
+  if (run_if && *run_if == 0) return;
   const int64_t r0 = (int64_t)blockIdx.y * 32, p0 = (int64_t)blockIdx.x * 64;
   if (s_tiles) S = s_tiles[r0 / BN];  // the slice count of this 256-row tile (automatic mode)
+  if (S == 0) return;                 // a modular tile
   const int tid = threadIdx.x;
   // all eight loads of a thread in flight before the shared-memory stores
   double vin[8];
@@ -593,6 +704,73 @@ split_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
       out[j] = __float2bfloat16_rn((float)(neg[j] ? -d : d));
     }
     __nv_bfloat16 *dst = slices + ((int64_t)(s - 1) * Rpad + r) * Kpad + p0 + pc;
+    *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<const uint4 *>(out);
+  }
+}
+
+// Residues of a 32-row x 64-K tile for the modular scheme: the t-bit
+// integer A' = sign(x) trunc(|x| 2^(t - e)) is read in five 12-bit chunks
+// c_d, and A' mod p_l = sum_d c_d (2^(12 d) mod p_l) mod p_l is formed in
+// FP32 (every partial sum is an integer below 2^24, so exact), reduced to the
+// symmetric range [-(p_l - 1)/2, (p_l - 1)/2] and signed.  Residue planes
+// share the slices' layout.  For op(B) (s_tiles non-null) only the rows of
+// modular tiles are written.
+template <bool KCONTIG>
+__global__ void __launch_bounds__(256)
+split_mod_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
+                 const int *__restrict__ expo, int64_t Rpad, int64_t Kpad,
+                 __nv_bfloat16 *__restrict__ res, const int *__restrict__ s_tiles,
+                 const int *__restrict__ run_if, const __grid_constant__ ModTable tab) {
+  __shared__ double tile[32][65];
+  if (run_if && *run_if == 0) return;
+  const int64_t r0 = (int64_t)blockIdx.y * 32, p0 = (int64_t)blockIdx.x * 64;
+  if (s_tiles && s_tiles[r0 / BN] != 0) return;  // a digit-slice tile
+  const int tid = threadIdx.x;
+  double vin[8];
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const int e = tid + 256 * u;
+    const int rr = KCONTIG ? e / 64 : e % 32, pp = KCONTIG ? e % 64 : e / 32;
+    const int64_t r = r0 + rr, pk = p0 + pp;
+    vin[u] = (r < R && pk < K) ? (KCONTIG ? X[pk + r * ld] : X[r + pk * ld]) : 0.0;
+  }
+#pragma unroll
+  for (int u = 0; u < 8; ++u) {
+    const int e = tid + 256 * u;
+    const int rr = KCONTIG ? e / 64 : e % 32, pp = KCONTIG ? e % 64 : e / 32;
+    tile[rr][pp] = vin[u];
+  }
+  __syncthreads();
+  const int rr = tid >> 3, pc = (tid & 7) * 8;
+  const int64_t r = r0 + rr;
+  const int e = (r < R) ? expo[r] : 0;
+  float ch[8][MOD_CHUNKS];
+  bool neg[8];
+#pragma unroll
+  for (int j = 0; j < 8; ++j) {
+    const unsigned long long mag = ozd::fixed_magnitude(tile[rr][pc + j], e, tab.bits, neg[j]);
+#pragma unroll
+    for (int d = 0; d < MOD_CHUNKS; ++d) {
+      // exact int -> float of a 12-bit value: 2^23 + c, less 2^23
+      const unsigned c = (unsigned)(mag >> (MOD_CHUNK_BITS * d)) & ((1u << MOD_CHUNK_BITS) - 1);
+      ch[j][d] = __uint_as_float(0x4B000000u | c) - 8388608.0f;
+    }
+  }
+#pragma unroll 2
+  for (int l = 0; l < MOD_COUNT; ++l) {
+    const float pl = tab.pf[l], pinv = tab.pinv[l], half = 0.5f * (pl - 1.0f);
+    __align__(16) __nv_bfloat16 out[8];
+#pragma unroll
+    for (int j = 0; j < 8; ++j) {
+      float v = 0.0f;
+#pragma unroll
+      for (int d = 0; d < MOD_CHUNKS; ++d) v = fmaf(ch[j][d], tab.pw[l][d], v);
+      v = fmaf(-rintf(v * pinv), pl, v);  // exact: both terms are integers below 2^24
+      if (v > half) v -= pl;              // the rounded quotient can be one off
+      if (v < -half) v += pl;
+      out[j] = __float2bfloat16_rn(neg[j] ? -v : v);
+    }
+    __nv_bfloat16 *dst = res + ((int64_t)l * Rpad + r) * Kpad + p0 + pc;
     *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<const uint4 *>(out);
   }
 }
@@ -682,9 +860,10 @@ recombine_auto_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
                       double *__restrict__ C, int64_t ldc, int ta, int tb, int64_t k,
                       const double *__restrict__ A, int64_t lda, const double *__restrict__ B,
                       int64_t ldb, int tri, const int *__restrict__ skip,
-                      const int *__restrict__ s_tiles) {
+                      const int *__restrict__ s_tiles, const int *__restrict__ run_if) {
   if (skip && *skip) return;
-  switch (s_tiles[blockIdx.y]) {
+  if (run_if && *run_if == 0) return;
+  switch (s_tiles[blockIdx.y]) {  // 0: a modular tile, reconstructed elsewhere
 #define GB_RECOMBINE_CASE(SS)                                                                  \
   case SS:                                                                                     \
     recombine_tile<SS>(m, n, m_tiles, plane_stride, planes, ea, eb, alpha, beta, C, ldc, ta,   \
@@ -697,7 +876,153 @@ recombine_auto_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
   }
 }
 
+// Modular scheme: C from the residue planes, one CTA per 128 x 256 tile of C
+// (tiles with s_tiles[nt] != 0 belong to the digit-slice pass).  With r_l
+// the residue of C'_ij mod p_l (in [0, p_l)), X = sum_l r_l W_l is
+// congruent to C' mod M, and X / M = sum_l r_l u_l / p_l, so the quotient
+// q = round(sum_l r_l F_l 2^-32) (error below 2^-20) gives C' = X - q M:
+// |C'| < M / (2 + 2^-5) by the choice of t leaves a margin of 0.007 to the
+// rounding.
+// X - q M is formed exactly in four signed 64-bit limbs of 32 bits (every
+// limb sum is below 2^45) and combined modulo 2^128, which holds C' as
+// |C'| < 2^127.
+__global__ void __launch_bounds__(256)
+reconstruct_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
+                        const uint16_t *__restrict__ planes, const int *__restrict__ ea,
+                        const int *__restrict__ eb, double alpha, double beta,
+                        double *__restrict__ C, int64_t ldc, int ta, int tb, int64_t k,
+                        const double *__restrict__ A, int64_t lda, const double *__restrict__ B,
+                        int64_t ldb, int tri, const int *__restrict__ skip,
+                        const int *__restrict__ s_tiles, const int *__restrict__ run_if,
+                        const __grid_constant__ ModTable tab) {
+  if (skip && *skip) return;
+  if (run_if && *run_if == 0) return;
+  const int mt = blockIdx.x, nt = blockIdx.y;
+  if (s_tiles && s_tiles[nt] != 0) return;
+  const int64_t i0 = (int64_t)mt * BM, j0 = (int64_t)nt * BN;
+  if (tri == 1 && i0 + BM - 1 < j0) return;
+  if (tri == 2 && i0 > j0 + BN - 1) return;
+  const int tid = threadIdx.x;
+  const int il = (tid & 31) * 4, jb = tid >> 5;
+  const uint16_t *pt = planes + ((int64_t)nt * m_tiles + mt) * (BM * BN);
+  int e_i[4];
+#pragma unroll
+  for (int r = 0; r < 4; ++r) e_i[r] = (i0 + il + r < m) ? ea[i0 + il + r] : 0;
+  for (int jl = jb; jl < BN; jl += 8) {
+    const int64_t j = j0 + jl;
+    if (j >= n) break;
+    const int fj = eb[j];
+    uint2 P[MOD_COUNT];
+#pragma unroll
+    for (int l = 0; l < MOD_COUNT; ++l)
+      P[l] = *reinterpret_cast<const uint2 *>(pt + (int64_t)l * plane_stride + jl * BM + il);
+#pragma unroll
+    for (int r = 0; r < 4; ++r) {
+      const int64_t i = i0 + il + r;
+      if (i >= m) continue;
+      if ((tri == 1 && i < j) || (tri == 2 && i > j)) continue;
+      double v;
+      if (e_i[r] == NONFINITE || fj == NONFINITE) {
+        double sum = 0.0;
+        for (int64_t pp = 0; pp < k; ++pp) {
+          const double a = ta ? A[pp + i * lda] : A[i + pp * lda];
+          const double b = tb ? B[j + pp * ldb] : B[pp + j * ldb];
+          sum = fma(a, b, sum);
+        }
+        v = alpha * sum;
+      } else {
+        unsigned long long qa = 0;
+        long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+#pragma unroll
+        for (int l = 0; l < MOD_COUNT; ++l) {
+          const unsigned w = (r < 2) ? P[l].x : P[l].y;
+          const unsigned long long rl = (r & 1) ? (w >> 16) : (w & 0xFFFFu);
+          qa += rl * tab.F[l];
+          a0 += (long long)(rl * tab.W[l][0]);
+          a1 += (long long)(rl * tab.W[l][1]);
+          a2 += (long long)(rl * tab.W[l][2]);
+          a3 += (long long)(rl * tab.W[l][3]);
+        }
+        const long long q = (long long)((qa + 0x80000000ull) >> 32);
+        a0 -= q * (long long)tab.M[0];
+        a1 -= q * (long long)tab.M[1];
+        a2 -= q * (long long)tab.M[2];
+        a3 -= q * (long long)tab.M[3];
+        const unsigned __int128 u = (unsigned __int128)(__int128)a0 +
+                                    ((unsigned __int128)(__int128)a1 << 32) +
+                                    ((unsigned __int128)(__int128)a2 << 64) +
+                                    ((unsigned __int128)(__int128)a3 << 96);
+        v = ozd::scaled_value((__int128)u, e_i[r] + fj - 2 * tab.bits, alpha);
+      }
+      double *c = C + i + j * ldc;
+      *c = (beta == 0.0) ? v : fma(beta, *c, v);
+    }
+  }
+}
+
 // ------------------------------------------------------------------ host
+// The modular scheme's moduli: the 14 largest odd numbers <= 511 that are
+// pairwise coprime (511 = 7 * 73, 507 = 3 * 13^2, 505 = 5 * 101,
+// 493 = 17 * 29, 473 = 11 * 43, the rest prime).  M = prod p_l ~ 2^125.06.
+constexpr int MODULI[MOD_COUNT] = {511, 509, 507, 505, 503, 499, 493,
+                                   491, 487, 479, 473, 467, 463, 461};
+
+static int mod_inverse(int a, int p) {  // a^-1 mod p, gcd(a, p) = 1
+  int t0 = 0, t1 = 1, r0 = p, r1 = a % p;
+  while (r1) {
+    const int q = r0 / r1, t2 = t0 - q * t1, r2 = r0 - q * r1;
+    t0 = t1;
+    t1 = t2;
+    r0 = r1;
+    r1 = r2;
+  }
+  return t0 < 0 ? t0 + p : t0;
+}
+
+static unsigned __int128 mod_product() {
+  unsigned __int128 M = 1;
+  for (int l = 0; l < MOD_COUNT; ++l) M *= (unsigned)MODULI[l];
+  return M;
+}
+
+// The table without t (computed once).
+static const ModTable &mod_base() {
+  static const ModTable tab = [] {
+    ModTable t{};
+    const unsigned __int128 M = mod_product();
+    for (int q = 0; q < 4; ++q) t.M[q] = (uint32_t)(M >> (32 * q));
+    for (int l = 0; l < MOD_COUNT; ++l) {
+      const int p = MODULI[l];
+      const unsigned __int128 Ml = M / (unsigned)p;
+      const int u = mod_inverse((int)(Ml % (unsigned)p), p);
+      const unsigned __int128 W = Ml * (unsigned)u;  // < M
+      for (int q = 0; q < 4; ++q) t.W[l][q] = (uint32_t)(W >> (32 * q));
+      t.F[l] = (uint32_t)((((unsigned long long)u << 32) + (unsigned)p / 2) / (unsigned)p);
+      t.pf[l] = (float)p;
+      t.pinv[l] = 1.0f / (float)p;
+      for (int d = 0; d < MOD_CHUNKS; ++d)
+        t.pw[l][d] = (float)((1ull << (MOD_CHUNK_BITS * d)) % (unsigned)p);
+    }
+    return t;
+  }();
+  return tab;
+}
+
+// Largest t <= 60 with M > 2 k 2^2t (1 + 2^-6): every |C'_ij| < k 2^2t then
+// lies below M / 2 with room for the quotient's rounding.  t = 56 for
+// k = 4096.
+int mod_bits(int64_t k) {
+  const unsigned __int128 M = mod_product();
+  int kb = 0;
+  while (kb < 63 && ((int64_t)1 << kb) < k) ++kb;  // k <= 2^kb
+  for (int t = MOD_MAX_BITS; t > 0; --t) {
+    if (2 * t + 1 + kb > 126) continue;
+    const unsigned __int128 lhs = (unsigned __int128)k << (2 * t + 1);
+    if (lhs + (lhs >> 6) < M) return t;
+  }
+  return 0;
+}
+
 // 2-D tensor map over `rows` x `kpad` bf16 (K innermost), box 64 x box_rows.
 int make_map(CUtensorMap *map, void *base, int64_t rows, int64_t kpad, int box_rows) {
   return make_bf16_kmajor_map(map, base, rows, kpad, BK, box_rows);
@@ -708,18 +1033,34 @@ inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
 void launch_split(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld,
                   const int *expo, int S, int64_t Rpad, int64_t Kpad, __nv_bfloat16 *slices,
-                  const int *s_tiles, cudaStream_t s) {
+                  const int *s_tiles, const int *run_if, cudaStream_t s) {
   dim3 g2((unsigned)(Kpad / 64), (unsigned)(Rpad / 32));
   if (kcontig)
-    { split_kernel<true><<<g2, 256, 0, s>>>(R, K, X, ld, expo, S, Rpad, Kpad, slices, s_tiles); count_launch(); }
+    split_kernel<true><<<g2, 256, 0, s>>>(R, K, X, ld, expo, S, Rpad, Kpad, slices, s_tiles,
+                                          run_if);
   else
-    { split_kernel<false><<<g2, 256, 0, s>>>(R, K, X, ld, expo, S, Rpad, Kpad, slices, s_tiles); count_launch(); }
+    split_kernel<false><<<g2, 256, 0, s>>>(R, K, X, ld, expo, S, Rpad, Kpad, slices, s_tiles,
+                                           run_if);
+  count_launch();
 }
 
-// Split an R x K op-view operand into S K-contiguous bf16 slices + exponents.
-void split_operand(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld, int S,
-                   int64_t Rpad, int64_t Kpad, unsigned long long *mx, int *expo,
-                   __nv_bfloat16 *slices, cudaStream_t s) {
+void launch_split_mod(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld,
+                      const int *expo, int64_t Rpad, int64_t Kpad, __nv_bfloat16 *res,
+                      const int *s_tiles, const int *run_if, const ModTable &tab,
+                      cudaStream_t s) {
+  dim3 g2((unsigned)(Kpad / 64), (unsigned)(Rpad / 32));
+  if (kcontig)
+    split_mod_kernel<true><<<g2, 256, 0, s>>>(R, K, X, ld, expo, Rpad, Kpad, res, s_tiles,
+                                              run_if, tab);
+  else
+    split_mod_kernel<false><<<g2, 256, 0, s>>>(R, K, X, ld, expo, Rpad, Kpad, res, s_tiles,
+                                               run_if, tab);
+  count_launch();
+}
+
+// Row maxima and exponents of an R x K op-view operand.
+void operand_exponents(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld,
+                       int64_t Rpad, unsigned long long *mx, int *expo, cudaStream_t s) {
   cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * Rpad, s);
   if (kcontig) {
     { rowmax_kcontig_kernel<<<(unsigned)((R + 7) / 8), 256, 0, s>>>(R, K, X, ld, mx); count_launch(); }
@@ -729,11 +1070,18 @@ void split_operand(bool kcontig, int64_t R, int64_t K, const double *X, int64_t 
     { rowmax_mcontig_kernel<<<g, 256, 0, s>>>(R, K, X, ld, kspan, mx); count_launch(); }
   }
   { exponent_kernel<<<(unsigned)((Rpad + 255) / 256), 256, 0, s>>>(Rpad, R, mx, expo); count_launch(); }
-  launch_split(kcontig, R, K, X, ld, expo, S, Rpad, Kpad, slices, nullptr, s);
 }
 
-// Automatic slice choice, op(A) side: the column sums alpha_k of |op(A)| and
-// the totals T_e, T_1 (after op(A)'s exponents are known).
+// Split an R x K op-view operand into S K-contiguous bf16 slices + exponents.
+void split_operand(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld, int S,
+                   int64_t Rpad, int64_t Kpad, unsigned long long *mx, int *expo,
+                   __nv_bfloat16 *slices, cudaStream_t s) {
+  operand_exponents(kcontig, R, K, X, ld, Rpad, mx, expo, s);
+  launch_split(kcontig, R, K, X, ld, expo, S, Rpad, Kpad, slices, nullptr, nullptr, s);
+}
+
+// Automatic choice, op(A) side: the column sums alpha_k of |op(A)| and the
+// totals T_e, T_1 (after op(A)'s exponents are known).
 void a_side_stats(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld,
                   const int *expo, const unsigned long long *mx, double *alpha, double *totals,
                   cudaStream_t s) {
@@ -749,14 +1097,14 @@ void a_side_stats(bool kcontig, int64_t R, int64_t K, const double *X, int64_t l
   { a_totals_kernel<<<1, 256, 0, s>>>(R, K, expo, mx, alpha, totals); count_launch(); }
 }
 
-// Automatic slice choice, op(B) side: exponents and column statistics of
-// op(B) in one pass, the slice count of every 256-column tile, then the
-// split with those counts.
-void split_b_auto(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld,
-                  int64_t Rpad, int64_t Kpad, unsigned long long *mx, int *expo,
-                  const double *alpha, const double *totals, double *s1, double *s2,
-                  double budget, int *s_tiles, int *last, __nv_bfloat16 *slices, cudaStream_t s) {
+// Automatic choice, op(B) side: exponents and column statistics of op(B)
+// in one pass, then the scheme (and slice count) of every 256-column tile.
+void choose_b(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld, int64_t Rpad,
+              unsigned long long *mx, int *expo, const double *alpha, const double *totals,
+              double *s1, double *s2, double budget, int mod_t, int *s_tiles, int *pass,
+              cudaStream_t s) {
   cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * Rpad, s);
+  cudaMemsetAsync(pass, 0, 2 * sizeof(int), s);
   if (kcontig) {
     { rowmax_stats_kcontig_kernel<<<(unsigned)((R + 7) / 8), 256, 0, s>>>(R, K, X, ld, alpha, mx,
                                                                           s1, s2); count_launch(); }
@@ -768,14 +1116,15 @@ void split_b_auto(bool kcontig, int64_t R, int64_t K, const double *X, int64_t l
     { rowmax_stats_mcontig_kernel<<<g, 256, 0, s>>>(R, K, X, ld, kspan, alpha, mx, s1, s2); count_launch(); }
   }
   { exponent_kernel<<<(unsigned)((Rpad + 255) / 256), 256, 0, s>>>(Rpad, R, mx, expo); count_launch(); }
-  { choose_slices_kernel<<<(unsigned)(Rpad / BN), 256, 0, s>>>(R, expo, mx, s1, s2, totals, K,
-                                                                budget, s_tiles, last); count_launch(); }
-  launch_split(kcontig, R, K, X, ld, expo, MAX_SLICES, Rpad, Kpad, slices, s_tiles, s);
+  int *status = ctx().d_status;
+  { choose_slices_kernel<<<(unsigned)(Rpad / BN), 256, 0, s>>>(
+        R, expo, mx, s1, s2, totals, K, budget, mod_t, s_tiles, status + STATUS_LAST_SLICES,
+        status + STATUS_LAST_MODULI, pass); count_launch(); }
 }
 
 // The whole emulated product.  K is cut into segments of at most
 // MAX_K_SEGMENT (so every int32 level sum is exact); each segment is split,
-// multiplied by the slice GEMM and recombined, later segments accumulating
+// multiplied on the tensor cores and recombined, later segments accumulating
 // into C (beta = 1).  The columns of op(B) and C are taken in blocks of `nb`
 // (a multiple of BN), all segments of a block before the next block, with
 // the hooks (when given) making block j of op(B) and C available on the
@@ -783,6 +1132,12 @@ void split_b_auto(bool kcontig, int64_t R, int64_t K, const double *X, int64_t l
 // is one segment and per segment and block otherwise.  Every C(i,j) depends
 // only on row i of op(A) and column j of op(B) (and their own exponents), so
 // the blocked result equals the single-block one bit for bit.
+//
+// Automatic mode runs two passes per segment, each predicated on the device
+// by the count of tiles the choice gave it (a pass with none launches
+// kernels that return at once): the modular pass (residues, residue GEMM,
+// reconstruction) and the digit-slice pass (slices, slice GEMM, recombine).
+// They share op(B)'s buffer and the planes and write disjoint tiles of C.
 int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
                      const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
                      double *C, int64_t ldc, int S, cudaStream_t s, int tri, const int *skip,
@@ -792,57 +1147,125 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
   const int Sa = automatic ? MAX_SLICES : S;  // slices allocated (and cut from op(A))
   const int64_t kseg = k < MAX_K_SEGMENT ? k : MAX_K_SEGMENT;
   const int64_t nseg = (k + MAX_K_SEGMENT - 1) / MAX_K_SEGMENT;
+  // the modular scheme's t for the longest segment (0: digit slices only)
+  const int mod_t = automatic && ozaki_modular_enabled() ? mod_bits(kseg) : 0;
+  const bool modular = mod_t > 0;
   const int64_t m_pad = round_up(m, BM), nb_pad = round_up(nb, BN), ks_pad = round_up(kseg, BK);
+  const int b_planes = modular && MOD_COUNT > Sa ? MOD_COUNT : Sa;
   const size_t bytes_sa = align256((size_t)Sa * m_pad * ks_pad * 2);
-  const size_t bytes_sb = align256((size_t)Sa * nb_pad * ks_pad * 2);
+  const size_t bytes_ra = modular ? align256((size_t)MOD_COUNT * m_pad * ks_pad * 2) : 0;
+  const size_t bytes_sb = align256((size_t)b_planes * nb_pad * ks_pad * 2);
   const size_t bytes_mx = align256((size_t)(m_pad + nb_pad) * 8);
   const size_t bytes_e = align256((size_t)(m_pad + nb_pad) * 4);
-  const size_t bytes_pl = align256((size_t)Sa * m_pad * nb_pad * 4);
-  // automatic mode: alpha_k, the two op(A) totals, the column sums of op(B)
-  // and the per-tile slice counts
+  const size_t plane_bytes = (size_t)Sa * 4 > (size_t)MOD_COUNT * 2 || !modular
+                                 ? (size_t)Sa * 4 : (size_t)MOD_COUNT * 2;
+  const size_t bytes_pl = align256(plane_bytes * m_pad * nb_pad);
+  // automatic mode: alpha_k, the two op(A) totals, the column sums of op(B),
+  // the per-tile choices and the two pass counts
   const size_t bytes_auto =
-      automatic ? align256((size_t)(ks_pad + 2 + 2 * nb_pad) * 8 + (size_t)(nb_pad / BN) * 4) : 0;
-  Scratch ws(bytes_sa + bytes_sb + bytes_mx + bytes_e + bytes_pl + bytes_auto, s);
+      automatic ? align256((size_t)(ks_pad + 2 + 2 * nb_pad) * 8 + (size_t)(nb_pad / BN + 2) * 4)
+                : 0;
+  Scratch ws(bytes_sa + bytes_ra + bytes_sb + bytes_mx + bytes_e + bytes_pl + bytes_auto, s);
   if (!ws.p) return GB_ERR_ALLOC;
   char *base = ws.as<char>();
   __nv_bfloat16 *sla = reinterpret_cast<__nv_bfloat16 *>(base);
-  __nv_bfloat16 *slb = reinterpret_cast<__nv_bfloat16 *>(base + bytes_sa);
-  unsigned long long *mx = reinterpret_cast<unsigned long long *>(base + bytes_sa + bytes_sb);
-  int *ea = reinterpret_cast<int *>(base + bytes_sa + bytes_sb + bytes_mx);
+  base += bytes_sa;
+  __nv_bfloat16 *rsa = reinterpret_cast<__nv_bfloat16 *>(base);
+  base += bytes_ra;
+  __nv_bfloat16 *slb = reinterpret_cast<__nv_bfloat16 *>(base);
+  base += bytes_sb;
+  unsigned long long *mx = reinterpret_cast<unsigned long long *>(base);
+  base += bytes_mx;
+  int *ea = reinterpret_cast<int *>(base);
   int *eb = ea + m_pad;
-  int *planes = reinterpret_cast<int *>(base + bytes_sa + bytes_sb + bytes_mx + bytes_e);
+  base += bytes_e;
+  int *planes = reinterpret_cast<int *>(base);
+  base += bytes_pl;
   double *st_alpha = nullptr, *st_tot = nullptr, *st_s1 = nullptr, *st_s2 = nullptr;
-  int *s_tiles = nullptr;
+  int *s_tiles = nullptr, *pass = nullptr;
   double budget = 0.0;
   if (automatic) {
-    st_alpha = reinterpret_cast<double *>(base + bytes_sa + bytes_sb + bytes_mx + bytes_e +
-                                          bytes_pl);
+    st_alpha = reinterpret_cast<double *>(base);
     st_tot = st_alpha + ks_pad;
     st_s1 = st_tot + 2;
     st_s2 = st_s1 + nb_pad;
     s_tiles = reinterpret_cast<int *>(st_s2 + nb_pad);
+    pass = s_tiles + nb_pad / BN;  // [0] modular tiles, [1] digit-slice tiles
     // the tolerance in units of 2^-52 less the roundings of the recombine
     // (one conversion, the alpha/beta step) and of the segment accumulation
     budget = ldexp(config().ozaki_tol, -52) - ldexp((double)(nseg + 2), -53);
   }
+  ModTable tab = mod_base();
+  tab.bits = mod_t;
 
   static PerDeviceOnce attr_once;
   int st = attr_once.run(current_device(), [] {
-    GB_CUDA(cudaFuncSetAttribute(slice_gemm_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                 SMEM_BYTES));
+    GB_CUDA(cudaFuncSetAttribute(slice_gemm_kernel<false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
+    GB_CUDA(cudaFuncSetAttribute(slice_gemm_kernel<true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES));
     return GB_SUCCESS;
   });
   if (st) return st;
-  CUtensorMap mapA, mapB;
+  CUtensorMap mapA, mapB, mapAr, mapBr;
   // op(A) rows: K-contiguous when A is transposed; op(B) columns: K-contiguous when B is not
-  auto split_a = [&](int64_t k0, int64_t kk) -> int {
+  auto seg_a = [&](int64_t k0) { return ta ? A + k0 : A + k0 * lda; };
+  auto prep_a = [&](int64_t k0, int64_t kk) {
+    operand_exponents(ta != 0, m, kk, seg_a(k0), lda, m_pad, mx, ea, s);
+    if (automatic) a_side_stats(ta != 0, m, kk, seg_a(k0), lda, ea, mx, st_alpha, st_tot, s);
+  };
+  auto split_a = [&](int64_t k0, int64_t kk, const int *run_if) -> int {
     const int64_t kp = round_up(kk, BK);
-    const double *Ak = ta ? A + k0 : A + k0 * lda;
-    split_operand(ta != 0, m, kk, Ak, lda, Sa, m_pad, kp, mx, ea, sla, s);
-    if (automatic) a_side_stats(ta != 0, m, kk, Ak, lda, ea, mx, st_alpha, st_tot, s);
+    launch_split(ta != 0, m, kk, seg_a(k0), lda, ea, Sa, m_pad, kp, sla, nullptr, run_if, s);
     return make_map(&mapA, sla, (int64_t)Sa * m_pad, kp, BM);
   };
-  if (nseg == 1 && (st = split_a(0, k))) return st;
+  auto split_a_mod = [&](int64_t k0, int64_t kk, const int *run_if) -> int {
+    const int64_t kp = round_up(kk, BK);
+    launch_split_mod(ta != 0, m, kk, seg_a(k0), lda, ea, m_pad, kp, rsa, nullptr, run_if, tab, s);
+    return make_map(&mapAr, rsa, (int64_t)MOD_COUNT * m_pad, kp, BM);
+  };
+  auto gemm = [&](bool mod, const CUtensorMap &ma, const CUtensorMap &mb, int64_t jn_pad,
+                  int64_t kp, const int *run_if) -> int {
+    GemmParams gp{};
+    gp.S = Sa;
+    gp.m_tiles = (int)(m_pad / BM);
+    gp.n_tiles = (int)(jn_pad / BN);
+    gp.group_m = config().ozaki_group_m;
+    // the triangle is relative to C's own indices: only the single-block
+    // form (j0 = 0) is used with tri
+    gp.tri = tri;
+    gp.kblocks = (int)(kp / BK);
+    gp.m_pad = (int)m_pad;
+    gp.n_pad = (int)jn_pad;
+    gp.plane_stride = m_pad * jn_pad;
+    gp.planes = planes;
+    gp.status = ctx().d_status;
+    gp.s_tiles = s_tiles;
+    gp.run_if = run_if;
+    for (int l = 0; l < MOD_COUNT; ++l) gp.mod_p[l] = MODULI[l];
+    const int ntiles = gp.m_tiles * gp.n_tiles;
+    const int grid = ntiles < persistent_ctas() ? ntiles : persistent_ctas();
+    if (mod) {
+      ProfileScope prof("residue_gemm", s);
+      slice_gemm_kernel<true><<<grid, NUM_THREADS, SMEM_BYTES, s>>>(ma, mb, gp);
+    } else {
+      ProfileScope prof("slice_gemm", s);
+      slice_gemm_kernel<false><<<grid, NUM_THREADS, SMEM_BYTES, s>>>(ma, mb, gp);
+    }
+    count_launch();
+    GB_CUDA(cudaGetLastError());
+    return GB_SUCCESS;
+  };
+  // one segment: op(A) is prepared once; with several column blocks (and
+  // automatic mode) it is split in both forms up front, as the blocks'
+  // choices are not known yet
+  const bool a_once = nseg == 1;
+  const bool a_early = a_once && (!automatic || nb < n);
+  if (a_once) {
+    prep_a(0, k);
+    if (a_early && (st = split_a(0, k, nullptr))) return st;
+    if (a_early && modular && (st = split_a_mod(0, k, nullptr))) return st;
+  }
   for (int64_t j0 = 0; j0 < n; j0 += nb) {
     const int64_t jn = (n - j0) < nb ? (n - j0) : nb;
     const int64_t jn_pad = round_up(jn, BN);
@@ -855,49 +1278,21 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       const int64_t kk = (k - k0) < MAX_K_SEGMENT ? (k - k0) : MAX_K_SEGMENT;
       const int64_t kp = round_up(kk, BK);
       if (hooks && (st = hooks->segment(j0, jn, k0, kk))) return st;
-      if (nseg > 1 && (st = split_a(k0, kk))) return st;
-      const double *Ak = ta ? A + k0 : A + k0 * lda;
+      if (!a_once) prep_a(k0, kk);
+      const double *Ak = seg_a(k0);
       const double *Bk = tb ? Bj + k0 * ldbj : Bj + k0;
-      if (automatic)
-        split_b_auto(tb == 0, jn, kk, Bk, ldbj, jn_pad, kp, mx + m_pad, eb, st_alpha, st_tot,
-                     st_s1, st_s2, budget, s_tiles, ctx().d_status + STATUS_LAST_SLICES, slb, s);
-      else
-        split_operand(tb == 0, jn, kk, Bk, ldbj, S, jn_pad, kp, mx + m_pad, eb, slb, s);
-      if ((st = make_map(&mapB, slb, (int64_t)Sa * jn_pad, kp, BN))) return st;
-      GemmParams gp;
-      gp.S = Sa;
-      gp.m_tiles = (int)(m_pad / BM);
-      gp.n_tiles = (int)(jn_pad / BN);
-      gp.group_m = config().ozaki_group_m;
-      // the triangle is relative to C's own indices: only the single-block
-      // form (j0 = 0) is used with tri
-      gp.tri = tri;
-      gp.kblocks = (int)(kp / BK);
-      gp.m_pad = (int)m_pad;
-      gp.n_pad = (int)jn_pad;
-      gp.plane_stride = m_pad * jn_pad;
-      gp.planes = planes;
-      gp.status = ctx().d_status;
-      gp.s_tiles = s_tiles;
-      const int ntiles = gp.m_tiles * gp.n_tiles;
-      const int grid = ntiles < persistent_ctas() ? ntiles : persistent_ctas();
-      {
-        ProfileScope prof("slice_gemm", s);
-        slice_gemm_kernel<<<grid, NUM_THREADS, SMEM_BYTES, s>>>(mapA, mapB, gp);
-        count_launch();
-      }
-      GB_CUDA(cudaGetLastError());
       const double bseg = sg == 0 ? beta : 1.0;  // later segments accumulate
       const dim3 g((unsigned)((m + BM - 1) / BM), (unsigned)((jn + BN - 1) / BN));
-      const int64_t ps = gp.plane_stride;
-      if (automatic) {
-        recombine_auto_kernel<<<g, 256, 0, s>>>(m, jn, gp.m_tiles, ps, planes, ea, eb, alpha,
-                                                 bseg, Cj, ldcj, ta, tb, kk, Ak, lda, Bk, ldbj,
-                                                 tri, skip, s_tiles);
-      } else {
+      const int m_tiles = (int)(m_pad / BM);
+      const int64_t ps = m_pad * jn_pad;
+      if (!automatic) {
+        if (!a_once && (st = split_a(k0, kk, nullptr))) return st;
+        split_operand(tb == 0, jn, kk, Bk, ldbj, S, jn_pad, kp, mx + m_pad, eb, slb, s);
+        if ((st = make_map(&mapB, slb, (int64_t)Sa * jn_pad, kp, BN))) return st;
+        if ((st = gemm(false, mapA, mapB, jn_pad, kp, nullptr))) return st;
 #define GB_RECOMBINE(SS)                                                                        \
   case SS:                                                                                      \
-    recombine_tile_kernel<SS><<<g, 256, 0, s>>>(m, jn, gp.m_tiles, ps, planes, ea, eb, alpha,   \
+    recombine_tile_kernel<SS><<<g, 256, 0, s>>>(m, jn, m_tiles, ps, planes, ea, eb, alpha,      \
                                                 bseg, Cj, ldcj, ta, tb, kk, Ak, lda, Bk, ldbj,  \
                                                 tri, skip);                                     \
     break;
@@ -907,7 +1302,33 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
           default: return set_error(GB_ERR_UNSUPPORTED, "emulated dgemm: %d slices", S);
         }
 #undef GB_RECOMBINE
+        count_launch();
+        if ((st = check_cuda(cudaGetLastError(), "emulated dgemm"))) return st;
+        continue;
       }
+      choose_b(tb == 0, jn, kk, Bk, ldbj, jn_pad, mx + m_pad, eb, st_alpha, st_tot, st_s1, st_s2,
+               budget, mod_t, s_tiles, pass, s);
+      if (modular) {
+        // ---- modular pass (tiles with s_tiles = 0)
+        if (!a_early && (st = split_a_mod(k0, kk, pass))) return st;
+        launch_split_mod(tb == 0, jn, kk, Bk, ldbj, eb, jn_pad, kp, slb, s_tiles, pass, tab, s);
+        if ((st = make_map(&mapBr, slb, (int64_t)MOD_COUNT * jn_pad, kp, BN))) return st;
+        if ((st = gemm(true, mapAr, mapBr, jn_pad, kp, pass))) return st;
+        reconstruct_tile_kernel<<<g, 256, 0, s>>>(
+            m, jn, m_tiles, ps, reinterpret_cast<const uint16_t *>(planes), ea, eb, alpha, bseg,
+            Cj, ldcj, ta, tb, kk, Ak, lda, Bk, ldbj, tri, skip, s_tiles, pass, tab);
+        count_launch();
+        if ((st = check_cuda(cudaGetLastError(), "emulated dgemm"))) return st;
+      }
+      // ---- digit-slice pass (tiles with s_tiles = S > 0)
+      if (!a_early && (st = split_a(k0, kk, pass + 1))) return st;
+      launch_split(tb == 0, jn, kk, Bk, ldbj, eb, MAX_SLICES, jn_pad, kp, slb, s_tiles, pass + 1,
+                   s);
+      if ((st = make_map(&mapB, slb, (int64_t)Sa * jn_pad, kp, BN))) return st;
+      if ((st = gemm(false, mapA, mapB, jn_pad, kp, pass + 1))) return st;
+      recombine_auto_kernel<<<g, 256, 0, s>>>(m, jn, m_tiles, ps, planes, ea, eb, alpha, bseg, Cj,
+                                              ldcj, ta, tb, kk, Ak, lda, Bk, ldbj, tri, skip,
+                                              s_tiles, pass + 1);
       count_launch();
       if ((st = check_cuda(cudaGetLastError(), "emulated dgemm"))) return st;
     }
@@ -925,11 +1346,12 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
 int ozaki_default_slices() { return 7; }
 
 // Resolves a requested slice count: > 0 fixed (at most MAX_SLICES), 0 the
-// default, OZAKI_SLICES_AUTO chosen per tile on the device (the record of
-// the largest count chosen is reset for the new call).
+// default, OZAKI_SLICES_AUTO chosen per tile on the device (the records of
+// the largest count and of the moduli chosen are reset for the new call).
 static int resolve_slices(int slices, cudaStream_t s) {
   if (slices == OZAKI_SLICES_AUTO) {
-    cudaMemsetAsync(ctx().d_status + STATUS_LAST_SLICES, 0, sizeof(int), s);
+    static_assert(STATUS_LAST_MODULI == STATUS_LAST_SLICES + 1, "adjacent status words");
+    cudaMemsetAsync(ctx().d_status + STATUS_LAST_SLICES, 0, 2 * sizeof(int), s);
     return OZAKI_SLICES_AUTO;
   }
   int S = slices > 0 ? slices : ozaki_default_slices();

@@ -3,11 +3,12 @@
 // (batched.cu):
 //   * the scale exponent of a row (column) from the bits of its largest |x|:
 //     every |x| on the row is below 2^e;
-//   * the truncated fixed-point magnitude trunc(|x| 2^(8S - e)) (< 2^64 for
-//     S <= 8) taken straight from the IEEE bits, whose base-256 digits (most
+//   * the truncated fixed-point magnitude trunc(|x| 2^(t - e)) (< 2^t, t <= 64)
+//     taken straight from the IEEE bits; with t = 8S its base-256 digits (most
 //     significant first) are the S slices of x;
-//   * one element of C from its exact level sum acc = sum_L P_L 2^(8(S+1-L)),
-//     rounded once to FP64 and scaled by alpha 2^(e_i + f_j - 8(S+1)).
+//   * one element of C from an exact integer (a level sum
+//     acc = sum_L P_L 2^(8(S+1-L)), or the CRT value of the modular scheme),
+//     rounded once to FP64 and scaled by alpha and a power of two.
 // Integer work only where it can be: FP64 is the scarcest unit on this part.
 #pragma once
 
@@ -36,9 +37,9 @@ __device__ __forceinline__ int exponent_of_max(unsigned long long b) {
   return e;
 }
 
-// trunc(|x| 2^(8S - e)) (truncation toward zero) and the sign of x; 0 for a
-// row marked NONFINITE.
-__device__ __forceinline__ unsigned long long digit_magnitude(double x, int e, int S, bool &neg) {
+// trunc(|x| 2^(t - e)) (truncation toward zero, < 2^t for |x| < 2^e, t <= 64)
+// and the sign of x; 0 for a row marked NONFINITE.
+__device__ __forceinline__ unsigned long long fixed_magnitude(double x, int e, int t, bool &neg) {
   const unsigned long long bits = (unsigned long long)__double_as_longlong(x);
   neg = (bits >> 63) != 0;
   const int E = (int)((bits >> 52) & 0x7ff);
@@ -50,11 +51,17 @@ __device__ __forceinline__ unsigned long long digit_magnitude(double x, int e, i
     M |= 1ull << 52;
     sh = E - 1075;
   }
-  sh += DIGIT_BITS * S - e;
+  sh += t - e;
   if (e == NONFINITE || M == 0) return 0;
-  if (sh >= 0) return M << sh;        // |x| < 2^e keeps the result below 2^(8S)
+  if (sh >= 0) return M << sh;        // |x| < 2^e keeps the result below 2^t
   if (sh > -64) return M >> (-sh);    // truncation toward zero
   return 0;
+}
+
+// The S-digit fixed-point value trunc(|x| 2^(8S - e)) whose base-256 digits
+// are the slices of x.
+__device__ __forceinline__ unsigned long long digit_magnitude(double x, int e, int S, bool &neg) {
+  return fixed_magnitude(x, e, DIGIT_BITS * S, neg);
 }
 
 // y * alpha * 2^x when alpha * 2^x is not a normal number (or alpha is
@@ -68,8 +75,8 @@ static __device__ __noinline__ double scale_out_of_range(double y, double alpha,
   return ldexp(y * m_alpha, x + e_sig);
 }
 
-// alpha * 2^(ei + fj - 8(S+1)) * acc, acc rounded once to FP64 (sticky bit).
-__device__ __forceinline__ double level_value(__int128 acc, int S, int ei, int fj, double alpha) {
+// alpha * 2^x0 * acc, acc rounded once to FP64 (sticky bit).
+__device__ __forceinline__ double scaled_value(__int128 acc, int x0, double alpha) {
   if (acc == 0) return 0.0;
   const bool neg = acc < 0;
   unsigned __int128 u = neg ? (unsigned __int128)(-acc) : (unsigned __int128)acc;
@@ -79,12 +86,17 @@ __device__ __forceinline__ double level_value(__int128 acc, int S, int ei, int f
   unsigned long long top = (unsigned long long)(u >> sh);
   if (sh && (u & (((unsigned __int128)1 << sh) - 1)) != 0) top |= 1ull;  // sticky bit
   const double t = __ull2double_rn(top);
-  const int x = sh - DIGIT_BITS * (S + 1) + ei + fj;
+  const int x = sh + x0;
   const long long ab = __double_as_longlong(alpha);
   const int e_alpha = (int)((ab >> 52) & 0x7ff);
   if (e_alpha > 0 && e_alpha < 0x7ff && e_alpha + x > 0 && e_alpha + x < 0x7ff)
     return (neg ? -t : t) * __longlong_as_double(ab + ((long long)x << 52));
   return scale_out_of_range(neg ? -t : t, alpha, x);
+}
+
+// alpha * 2^(ei + fj - 8(S+1)) * acc: one element of C from its level sum.
+__device__ __forceinline__ double level_value(__int128 acc, int S, int ei, int fj, double alpha) {
+  return scaled_value(acc, ei + fj - DIGIT_BITS * (S + 1), alpha);
 }
 
 }  // namespace ozd

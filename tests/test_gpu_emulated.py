@@ -1,4 +1,5 @@
-"""Emulated FP64 GEMM (Ozaki slices on bf16 tensor cores) parity.
+"""Emulated FP64 GEMM (Ozaki slices and the modular scheme on bf16 tensor
+cores) parity.
 
 1. Exactness: integer operands are represented exactly by their slices, so
    the result must equal the exact integer product bit for bit -- including
@@ -11,13 +12,20 @@
    denominator), bounded by 8*eps for 7 slices (56 bits) on e = 0 operands.
 3. The DGEMM contract: transposes, padded leading dimensions, alpha/beta,
    beta = 0 overwriting NaN, and Inf/NaN inputs propagating.
+4. The modular scheme (automatic mode): bit for bit the exact integer product
+   of the t-bit cut operands, rounded once (a restatement in Python
+   integers), over transposes and K segments; the per-tile choice between the
+   schemes follows the bounds restated in numpy.
 """
 from __future__ import annotations
+
+import math
 
 import numpy as np
 import pytest
 
 from conftest import EPS, dmmch_ratio
+from test_modular_model import MOD_COUNT, mod_bits
 
 from openblas_gb300 import workloads as W
 
@@ -36,27 +44,37 @@ def _int_matrix(seed, shape, lo=-127, hi=127):
 
 
 # (2200, 3000, 200): 18 m-tiles, so the tile order's last group is a ragged 2
+@pytest.fixture(params=[1, 0], ids=["modular", "slices"])
+def scheme(request, gblib):
+    """Automatic mode with the modular scheme allowed (1) or digit slices only (0)."""
+    assert gblib.gb_set_ozaki_modular(request.param) == 0
+    yield request.param
+    gblib.gb_set_ozaki_modular(1)
+
+
 @pytest.mark.parametrize("m,n,k", [(64, 48, 1000), (300, 520, 2100), (128, 256, 5000),
                                    (2200, 3000, 200)])
-def test_integer_operands_exact(F, emulated, m, n, k):
+def test_integer_operands_exact(F, emulated, gblib, scheme, m, n, k):
     A = _int_matrix(1, (m, k))
     B = _int_matrix(2, (k, n))
     C = np.zeros((m, n), order="F")
     F.dgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, C, m)
+    assert gblib.gb_last_ozaki_moduli() == (MOD_COUNT if scheme else 0)
     exact = (A.astype(np.int64) @ B.astype(np.int64)).astype(np.float64)
     assert np.array_equal(C, exact)
 
 
-def test_worst_case_digits_exact(F, emulated):
-    """All digits +-255 with aligned signs: every 256-deep chunk sum is
-    256*65025 (just below 2^24) and every level sum of a 4096-deep segment
-    4096*65025; k = 9000 spans three segments."""
+def test_worst_case_digits_exact(F, emulated, gblib, scheme):
+    """All digits (residues) +-255 with aligned signs: every 256-deep chunk
+    sum is 256*65025 (just below 2^24) and every level sum of a 4096-deep
+    segment 4096*65025; k = 9000 spans three segments."""
     m, n, k = 130, 260, 9000
     A = np.full((m, k), 255.0, order="F")
     B = np.full((k, n), 255.0, order="F")
     A[::2] = -255.0
     C = np.zeros((m, n), order="F")
     F.dgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, C, m)
+    assert gblib.gb_last_ozaki_moduli() == (MOD_COUNT if scheme else 0)
     exact = np.where(np.arange(m)[:, None] % 2 == 0, -1.0, 1.0) * (k * 255.0 * 255.0)
     assert np.array_equal(C, np.broadcast_to(exact, (m, n)))
 
@@ -231,11 +249,48 @@ def _column_normwise(Cg, Cref, G):
     return float((d / np.where(g > 0, g, 1.0)).max())
 
 
-# automatic slice count (the default): 7 slices where 56 bits meet the bound,
-# 8 where the exponent spread needs them; the error stays within the
-# GB_OZAKI_TOL default of 8 eps, column-normwise and normwise
-@pytest.mark.parametrize("e,expect", [(0, 7), (8, 8), (16, 8)])
-def test_automatic_slice_count_meets_tolerance(orc, F, emulated, gblib, e, expect):
+DROP_C = 7.0 * (1.0 + 1.0 / 128.0)
+
+
+def _predict_choice(opA, opB, tol=8.0, modular=True):
+    """The automatic choice restated (ozaki.cu choose_slices_kernel) for a
+    single-segment product op(A) (m x k) op(B) (k x n): per 256-column tile,
+    the modular scheme if 2^-t max rho2_j meets the budget, else the
+    smallest slice count S with 2^-8S max rho_j within it.  Returns whether
+    any tile is modular and the largest slice count (0 if none)."""
+    m, k = opA.shape
+    n = opB.shape[1]
+    t = mod_bits(k) if modular else 0
+    ra = np.abs(opA).max(axis=1)
+    cb = np.abs(opB).max(axis=0)
+    e = np.where(ra > 0, np.frexp(ra)[1], 0)
+    f = np.where(cb > 0, np.frexp(cb)[1], 0)
+    te = np.ldexp(1.0, e[ra > 0]).sum()
+    alpha = np.abs(opA).sum(axis=0)
+    t1 = alpha.sum()
+    s1 = np.abs(opB).sum(axis=0)
+    s2 = alpha @ np.abs(opB)
+    ok = (cb > 0) & (s2 > 0)
+    rho = np.where(ok, (te * s1 + np.ldexp(t1 + DROP_C * k * te, f)) / np.where(ok, s2, 1), 0)
+    rho2 = np.where(ok, (te * s1 + np.ldexp(t1 + np.ldexp(k * te, -t), f))
+                    / np.where(ok, s2, 1), 0)
+    budget = tol * 2.0 ** -52 - 3 * 2.0 ** -53
+    any_mod, smax = False, 0
+    for j0 in range(0, n, 256):
+        if t and np.ldexp(rho2[j0:j0 + 256].max(), -t) <= budget:
+            any_mod = True
+            continue
+        S = next((c for c in range(1, 8) if np.ldexp(rho[j0:j0 + 256].max(), -8 * c) <= budget),
+                 8)
+        smax = max(smax, S)
+    return any_mod, smax
+
+
+# automatic choice (the default): the modular scheme where its bound meets
+# the GB_OZAKI_TOL default of 8 eps, else the smallest slice count that does;
+# the error stays within 8 eps, column-normwise and normwise
+@pytest.mark.parametrize("e", [0, 8, 16])
+def test_automatic_slice_count_meets_tolerance(orc, F, emulated, gblib, scheme, e):
     m = n = k = 1024
     A = W.exponent_spread(40 + e, (m, k), e)
     B = W.exponent_spread(50 + e, (k, n), e)
@@ -243,7 +298,11 @@ def test_automatic_slice_count_meets_tolerance(orc, F, emulated, gblib, e, expec
     assert gblib.gb_set_ozaki_slices(0) == 0
     Cg = C.copy(order="F")
     F.dgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, Cg, m)
-    assert gblib.gb_last_ozaki_slices() == expect
+    any_mod, smax = _predict_choice(A, B, modular=bool(scheme))
+    if e == 0:
+        assert any_mod == bool(scheme) and smax == (0 if scheme else 7)
+    assert gblib.gb_last_ozaki_moduli() == (MOD_COUNT if any_mod else 0)
+    assert gblib.gb_last_ozaki_slices() == smax
     Cref = C.copy(order="F")
     orc.dgemm_dd("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, Cref, m)
     G = orc.dgemm_absbound("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, C, m)
@@ -252,26 +311,110 @@ def test_automatic_slice_count_meets_tolerance(orc, F, emulated, gblib, e, expec
 
 
 def test_automatic_slice_count_per_column_tile(F, emulated, gblib):
-    """One 256-column tile of uniform columns next to one of exponent-spread
-    columns: each tile gets its own count, and because the first S digits of
-    an 8-digit split are the S-digit split, each tile's columns equal the
-    fixed-count result for its count bit for bit."""
+    """One 256-column tile of uniform columns next to a tile whose columns
+    are dominated by one entry that meets a tiny column of op(A) (so the
+    rows' scales are 2^30 above what the products use): each tile gets its
+    own scheme.  The uniform tile takes the modular scheme and equals the
+    automatic product of its columns alone; the other takes 8 slices and,
+    because the first S digits of an 8-digit split are the S-digit split,
+    equals the fixed 8-slice result bit for bit.  With the modular scheme
+    off, the uniform tile takes 7 slices and equals the fixed 7-slice
+    result."""
     m, k = 300, 700
     A = W.uniform(70, (m, k))
-    B = np.asfortranarray(np.hstack([W.uniform(71, (k, 256)),
-                                     W.exponent_spread(72, (k, 200), 16)]))
-    n = B.shape[1]
-    out = {}
-    for s in (0, 7, 8):
+    A[:, 0] *= 2.0 ** -30
+    hard = np.ldexp(W.uniform(72, (k, 200)), -40)
+    hard[0] = 1.0
+    B = np.asfortranarray(np.hstack([W.uniform(71, (k, 256)), hard]))
+    assert _predict_choice(A, B) == (True, 8)
+    assert _predict_choice(A, B, modular=False) == (False, 8)
+
+    def run(s, BB, modular=1):
         assert gblib.gb_set_ozaki_slices(s) == 0
-        Cs = np.zeros((m, n), order="F")
-        F.dgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, Cs, m)
-        out[s] = Cs
-        if s == 0:
-            assert gblib.gb_last_ozaki_slices() == 8
-    gblib.gb_set_ozaki_slices(0)
-    assert np.array_equal(out[0][:, :256], out[7][:, :256])
-    assert np.array_equal(out[0][:, 256:], out[8][:, 256:])
+        assert gblib.gb_set_ozaki_modular(modular) == 0
+        Cs = np.zeros((m, BB.shape[1]), order="F")
+        F.dgemm("N", "N", m, BB.shape[1], k, 1.0, A, m, BB, k, 0.0, Cs, m)
+        got = (gblib.gb_last_ozaki_moduli(), gblib.gb_last_ozaki_slices()) if s == 0 else None
+        return Cs, got
+
+    try:
+        mixed, got = run(0, B)
+        assert got == (MOD_COUNT, 8)
+        left, got = run(0, np.asfortranarray(B[:, :256]))
+        assert got == (MOD_COUNT, 0)
+        off, got = run(0, B, modular=0)
+        assert got == (0, 8)
+        c7, _ = run(7, B)
+        c8, _ = run(8, B)
+    finally:
+        gblib.gb_set_ozaki_slices(0)
+        gblib.gb_set_ozaki_modular(1)
+    assert np.array_equal(mixed[:, :256], left)
+    assert np.array_equal(mixed[:, 256:], c8[:, 256:])
+    assert np.array_equal(off[:, :256], c7[:, :256])
+    assert np.array_equal(off[:, 256:], c8[:, 256:])
+
+
+def _cut(X, e, t, axis):
+    """sign(x) trunc(|x| 2^(t - e)) as Python integers, e per row (axis 1)
+    or per column (axis 0)."""
+    out = np.empty(X.shape, dtype=object)
+    for idx, x in np.ndenumerate(X):
+        ee = int(e[idx[0]] if axis == 1 else e[idx[1]])
+        num, den = abs(float(x)).as_integer_ratio()
+        sh = t - ee
+        v = (num << sh) // den if sh >= 0 else num // (den << -sh)
+        out[idx] = -v if x < 0 else v
+    return out
+
+
+def _modular_expected(opA, opB):
+    """alpha = 1, beta = 0: per 4096-deep K segment, C' = A'B' exactly (the
+    t-bit cut operands, t from the segment length), C += round(C') 2^(e_i +
+    f_j - 2t), the first segment storing."""
+    m, k = opA.shape
+    n = opB.shape[1]
+    t = mod_bits(min(k, 4096))
+    C = np.zeros((m, n))
+    for k0 in range(0, k, 4096):
+        Ak, Bk = opA[:, k0:k0 + 4096], opB[k0:k0 + 4096, :]
+        ra, cb = np.abs(Ak).max(axis=1), np.abs(Bk).max(axis=0)
+        e = np.where(ra > 0, np.frexp(ra)[1], 0)
+        f = np.where(cb > 0, np.frexp(cb)[1], 0)
+        Cp = _cut(Ak, e, t, 1).dot(_cut(Bk, f, t, 0))
+        for (i, j), c in np.ndenumerate(Cp):
+            v = math.ldexp(float(c), int(e[i] + f[j]) - 2 * t)
+            C[i, j] = v if k0 == 0 else C[i, j] + v
+    return C
+
+
+@pytest.mark.parametrize("ta,tb", [("N", "N"), ("N", "T"), ("T", "N"), ("T", "T")])
+def test_modular_equals_exact_product_of_cut_operands(F, emulated, gblib, ta, tb):
+    """Every element is the exact integer product of the cut operands
+    rounded once and scaled: bit for bit, over transposes and padded
+    leading dimensions (two column tiles, the second ragged)."""
+    m, n, k = 40, 280, 257
+    A, B, C = W.gemm_operands(80, m, n, k, ta, tb, pad=5)
+    A = np.asfortranarray(A * np.ldexp(1.0, W.randint(81, A.shape, -4, 4)))
+    opA = A[:m, :k] if ta == "N" else A[:k, :m].T
+    opB = B[:k, :n] if tb == "N" else B[:n, :k].T
+    assert _predict_choice(opA, opB)[0]
+    Cg = np.full_like(C, np.nan)
+    F.dgemm(ta, tb, m, n, k, 1.0, A, A.shape[0], B, B.shape[0], 0.0, Cg, Cg.shape[0])
+    assert (gblib.gb_last_ozaki_moduli(), gblib.gb_last_ozaki_slices()) == (MOD_COUNT, 0)
+    assert np.array_equal(Cg[:m], _modular_expected(opA, opB))
+
+
+def test_modular_equals_exact_product_over_k_segments(F, emulated, gblib):
+    """k = 4096 + 333: two K segments, each exact and rounded once, the
+    second added to the first in FP64."""
+    m, n, k = 20, 36, 4096 + 333
+    A = W.exponent_spread(82, (m, k), 3)
+    B = W.uniform(83, (k, n))
+    C = np.zeros((m, n), order="F")
+    F.dgemm("N", "N", m, n, k, 1.0, A, m, B, k, 0.0, C, m)
+    assert gblib.gb_last_ozaki_moduli() == MOD_COUNT
+    assert np.array_equal(C, _modular_expected(A, B))
 
 
 def test_near_underflow_recombine_matches_native(gblib):

@@ -1,0 +1,160 @@
+"""The modular scheme of the emulated DGEMM, restated on the CPU.
+
+The automatic mode of the emulated DGEMM may compute a column tile of C from
+residues: op(A) and op(B) are cut to t-bit integers A', B', each residue
+product (A' mod p_l)(B' mod p_l) runs on the tensor cores like a digit-slice
+product, and the Chinese remainder theorem recovers C' = A'B' exactly.
+These tests take the moduli and chunk constants from the CUDA source and
+check, in exact integer arithmetic:
+
+* the moduli are odd, pairwise coprime and at most 511, so a symmetric
+  residue has |r| <= 255 (exact in bf16, and a 256-deep FP32 chunk of
+  residue products stays below 2^24, as for 8-bit digits);
+* the bit count t chosen for a K segment keeps every |C'| < k 2^2t below
+  M / 2 with room for the rounded CRT quotient (t = 56 for K = 4096);
+* the residues the split kernel forms in FP32 from 12-bit chunks equal the
+  exact symmetric residues, over random and extreme t-bit integers;
+* the reconstruction (quotient from 32-bit fixed-point fractions, four
+  signed 64-bit limbs, the value taken modulo 2^128) returns C' for
+  random and extreme values of C', including +-(k 2^2t - 1).
+"""
+from __future__ import annotations
+
+import math
+import os
+import re
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+CSRC = os.path.join(HERE, "..", "openblas_gb300", "csrc")
+
+
+def _src():
+    with open(os.path.join(CSRC, "ozaki.cu")) as f:
+        return f.read()
+
+
+def _const(src, name):
+    return int(re.search(r"constexpr int " + name + r"\s*=\s*(\d+)", src).group(1))
+
+
+SRC = _src()
+MODULI = [int(x) for x in
+          re.search(r"MODULI\[MOD_COUNT\]\s*=\s*\{([^}]*)\}", SRC).group(1).replace("\n", " ")
+          .split(",")]
+MOD_COUNT = _const(SRC, "MOD_COUNT")
+CHUNK_BITS = _const(SRC, "MOD_CHUNK_BITS")
+CHUNKS = _const(SRC, "MOD_CHUNKS")
+M = math.prod(MODULI)
+
+
+def mod_bits(k):
+    """The largest t <= 60 with M > 2 k 2^2t (1 + 2^-6) (ozaki.cu mod_bits)."""
+    kb = 0
+    while kb < 63 and (1 << kb) < k:
+        kb += 1
+    for t in range(CHUNK_BITS * CHUNKS, 0, -1):
+        if 2 * t + 1 + kb > 126:
+            continue
+        lhs = k << (2 * t + 1)
+        if lhs + (lhs >> 6) < M:
+            return t
+    return 0
+
+
+def crt_table():
+    F, W = [], []
+    for p in MODULI:
+        Ml = M // p
+        u = pow(Ml % p, -1, p)
+        W.append(Ml * u)
+        F.append(((u << 32) + p // 2) // p)
+    return F, W
+
+
+def reconstruct(residues, F, W):
+    """C' from its residues in [0, p_l), as the reconstruction kernel forms it."""
+    qa = sum(r * f for r, f in zip(residues, F))
+    q = (qa + (1 << 31)) >> 32
+    limbs = []
+    for j in range(4):
+        a = sum(r * ((w >> (32 * j)) & 0xFFFFFFFF) for r, w in zip(residues, W))
+        a -= q * ((M >> (32 * j)) & 0xFFFFFFFF)
+        assert -(1 << 63) <= a < (1 << 63)       # a signed 64-bit limb
+        assert abs(a) < (1 << 46)
+        limbs.append(a)
+    u = sum(a << (32 * j) for j, a in enumerate(limbs)) % (1 << 128)
+    return u - (1 << 128) if u >= (1 << 127) else u
+
+
+def test_moduli_are_odd_coprime_and_small():
+    assert len(MODULI) == MOD_COUNT == 14
+    for i, p in enumerate(MODULI):
+        assert p % 2 == 1 and p <= 511
+        for q in MODULI[i + 1:]:
+            assert math.gcd(p, q) == 1
+    assert 256 * 255 * 255 < 2 ** 24           # a residue-product chunk is exact in FP32
+    assert 2 ** 125 < M < 2 ** 126
+
+
+def test_bit_count_keeps_products_below_half_the_modulus():
+    assert mod_bits(4096) == 56
+    for k in (1, 2, 3, 64, 255, 256, 257, 1000, 4095, 4096, 5000, 65536):
+        t = mod_bits(k)
+        assert 1 <= t <= CHUNK_BITS * CHUNKS
+        bound = k * (1 << (2 * t))              # |C'| < k 2^2t
+        assert 2 * bound * (1 + 2 ** -6) < M
+        assert bound < (1 << 127)
+        if t < CHUNK_BITS * CHUNKS:              # t is the largest such count
+            assert 2 * k * (1 << (2 * t + 2)) * (1 + 2 ** -6) >= M
+
+
+def _fp32_residues(mag, p):
+    """The split kernel's FP32 residue of the non-negative t-bit integers
+    `mag` (uint64 array) modulo p, in [-(p-1)/2, (p-1)/2]."""
+    f32 = np.float32
+    v = np.zeros(mag.shape, f32)
+    for d in range(CHUNKS):
+        c = ((mag >> np.uint64(CHUNK_BITS * d)) & np.uint64((1 << CHUNK_BITS) - 1)).astype(f32)
+        pw = f32((1 << (CHUNK_BITS * d)) % p)
+        v = (c * pw + v).astype(f32)             # exact: every term and sum < 2^24
+    q = np.rint(v * f32(1.0 / f32(p))).astype(f32)
+    v = (v - q * f32(p)).astype(f32)
+    half = f32(0.5) * (f32(p) - f32(1))
+    v = np.where(v > half, v - f32(p), v)
+    v = np.where(v < -half, v + f32(p), v)
+    return v
+
+
+def test_fp32_residues_are_exact():
+    rng = np.random.default_rng(11)
+    t = 60
+    mags = [rng.integers(0, 1 << 62, 20000, dtype=np.uint64) >> np.uint64(62 - t)]
+    edge = []
+    for p in MODULI:                              # values next to multiples of p and p/2
+        for base in (p * 12345678901, p * 987654321012345, (1 << t) - 1 - p, p // 2, p):
+            edge += [max(0, base + d) for d in range(-3, 4)]
+    mags.append(np.array([x % (1 << t) for x in edge], dtype=np.uint64))
+    mag = np.concatenate(mags)
+    for p in MODULI:
+        got = _fp32_residues(mag, p)
+        exact = np.array([((int(x) + p // 2) % p) - p // 2 for x in mag], dtype=np.float64)
+        assert np.array_equal(got.astype(np.float64), exact), p
+        assert np.abs(got).max() <= (p - 1) // 2
+
+
+def test_crt_reconstruction_recovers_the_product():
+    F, W = crt_table()
+    rng = np.random.default_rng(12)
+    for k in (64, 1000, 4096):
+        t = mod_bits(k)
+        lim = k * (1 << (2 * t)) - 1
+        vals = [0, 1, -1, lim, -lim, lim // 2, -(lim // 3)]
+        vals += [int(x) for x in rng.integers(-(1 << 62), 1 << 62, 300)]
+        vals += [(int(a) << 62) + int(b) for a, b in
+                 zip(rng.integers(-(lim >> 62), lim >> 62, 300), rng.integers(0, 1 << 62, 300))]
+        for c in vals:
+            assert abs(c) <= lim
+            residues = [c % p for p in MODULI]
+            assert reconstruct(residues, F, W) == c
