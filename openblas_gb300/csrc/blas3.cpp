@@ -10,6 +10,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <chrono>
 #include <vector>
 
 #include "gb_internal.h"
@@ -98,7 +99,7 @@ static int dgemm_dispatch(int ta, int tb, int64_t m, int64_t n, int64_t k, doubl
 // buffers (whose copies the CUDA runtime performs synchronously) still
 // overlap with the GPU.
 namespace {
-constexpr int64_t PIPE_K_SEGMENT = EMU_K_SEGMENT;  // the emulated engine's K segment
+constexpr int64_t PIPE_K_SEGMENT = EMU_K_SEGMENT;  // upload piece of op(A) and op(B) along K
 struct PipelinedDgemm : EmuBlockHooks {
   cudaStream_t s = nullptr, cin = nullptr, cout = nullptr;
   int ta = 0, tb = 0;
@@ -109,6 +110,40 @@ struct PipelinedDgemm : EmuBlockHooks {
   double *dA = nullptr, *dB = nullptr, *dC = nullptr;
   int64_t dlda = 0, dldb = 0;
   std::vector<cudaEvent_t> a_up, up, done;  // a_up[seg], up[block * nseg + seg], done[block]
+  // GB_VERBOSE >= 3: a timeline of the copies and blocks (timing events)
+  struct Mark {
+    cudaEvent_t e;
+    const char *what;
+    int64_t idx;
+  };
+  std::vector<Mark> marks;
+  bool trace = false;
+  void mark(cudaStream_t st, const char *what, int64_t idx) {
+    if (!trace) return;
+    cudaEvent_t e = nullptr;
+    if (cudaEventCreate(&e) != cudaSuccess) return;
+    cudaEventRecord(e, st);
+    marks.push_back({e, what, idx});
+  }
+  std::chrono::steady_clock::time_point h0, h1, h2;  // host: entry, enqueued, finished
+  void report() {
+    if (marks.empty()) return;
+    auto ms = [](std::chrono::steady_clock::time_point a, std::chrono::steady_clock::time_point b) {
+      return std::chrono::duration<double, std::milli>(b - a).count();
+    };
+    fprintf(stderr, "[gbblas] pipelined dgemm host: %.3f ms enqueueing, %.3f ms to completion\n",
+            ms(h0, h1), ms(h0, h2));
+    cudaEventSynchronize(marks.back().e);
+    for (const Mark &mk : marks) {
+      float ms = 0.f;
+      cudaEventSynchronize(mk.e);
+      cudaEventElapsedTime(&ms, marks.front().e, mk.e);
+      fprintf(stderr, "[gbblas] pipelined dgemm %8.3f ms  %s %lld\n", ms, mk.what,
+              (long long)mk.idx);
+    }
+    for (const Mark &mk : marks) cudaEventDestroy(mk.e);
+    marks.clear();
+  }
 
   int64_t seg_len(int64_t sg) const {
     const int64_t k0 = sg * PIPE_K_SEGMENT;
@@ -124,6 +159,7 @@ struct PipelinedDgemm : EmuBlockHooks {
       GB_CUDA(cudaMemcpy2DAsync(dA + k0 * dlda, dlda * 8, A + k0 * lda, lda * 8, m * 8, kk,
                                 cudaMemcpyHostToDevice, cin));
     GB_CUDA(cudaEventRecord(a_up[sg], cin));
+    mark(cin, "op(A) segment uploaded", sg);
     return GB_SUCCESS;
   }
   // segment sg of block j of op(B) (and C's block with the first segment)
@@ -141,6 +177,7 @@ struct PipelinedDgemm : EmuBlockHooks {
       if (st) return st;
     }
     GB_CUDA(cudaEventRecord(up[j * nseg + sg], cin));
+    mark(cin, "op(B) block segment uploaded", j * nseg + sg);
     return GB_SUCCESS;
   }
   int upload_block(int64_t j) {
@@ -153,7 +190,9 @@ struct PipelinedDgemm : EmuBlockHooks {
   int download(int64_t j) {
     const int64_t j0 = j * nb, jn = (n - j0) < nb ? (n - j0) : nb;
     GB_CUDA(cudaStreamWaitEvent(cout, done[j], 0));
-    return stage_out(C + j0 * ldc, dC + j0 * m, ldc, m, jn, 8, cout);
+    const int st = stage_out(C + j0 * ldc, dC + j0 * m, ldc, m, jn, 8, cout);
+    mark(cout, "C block downloaded", j);
+    return st;
   }
   int before(int64_t j0, int64_t, const double **Bj, int64_t *ldbj, double **Cj,
              int64_t *ldcj) override {
@@ -163,15 +202,23 @@ struct PipelinedDgemm : EmuBlockHooks {
     *ldcj = m;
     return GB_SUCCESS;
   }
-  int segment(int64_t j0, int64_t, int64_t k0, int64_t) override {
-    const int64_t sg = k0 / PIPE_K_SEGMENT;
-    GB_CUDA(cudaStreamWaitEvent(s, a_up[sg], 0));
-    GB_CUDA(cudaStreamWaitEvent(s, up[(j0 / nb) * nseg + sg], 0));
+  // every upload piece overlapping [k0, k0 + kk)
+  int segment(int64_t j0, int64_t, int64_t k0, int64_t kk) override {
+    for (int64_t sg = k0 / PIPE_K_SEGMENT; sg * PIPE_K_SEGMENT < k0 + kk; ++sg) {
+      GB_CUDA(cudaStreamWaitEvent(s, a_up[sg], 0));
+      GB_CUDA(cudaStreamWaitEvent(s, up[(j0 / nb) * nseg + sg], 0));
+    }
+    return GB_SUCCESS;
+  }
+  int a_range(int64_t k0, int64_t kk) override {
+    for (int64_t sg = k0 / PIPE_K_SEGMENT; sg * PIPE_K_SEGMENT < k0 + kk; ++sg)
+      GB_CUDA(cudaStreamWaitEvent(s, a_up[sg], 0));
     return GB_SUCCESS;
   }
   int after(int64_t j0, int64_t) override {
     const int64_t j = j0 / nb, nblk = (int64_t)done.size();
     GB_CUDA(cudaEventRecord(done[j], s));
+    mark(s, "C block computed", j);
     int st = GB_SUCCESS;
     if (j + 1 < nblk && (st = upload_block(j + 1))) return st;
     if (j > 0 && (st = download(j - 1))) return st;
@@ -191,6 +238,7 @@ static int dgemm_host_pipelined(int ta, int tb, int64_t m, int64_t n, int64_t k,
   if (!dgemm_wants_emulated(m, n, k)) return 0;
   if (is_device_pointer(A) || is_device_pointer(B) || is_device_pointer(C)) return 0;
   PipelinedDgemm p;
+  p.h0 = std::chrono::steady_clock::now();
   p.s = stream();
   if (copy_streams(&p.cin, &p.cout)) return 1;
   int64_t nblk = n / 4096;
@@ -234,6 +282,7 @@ static int dgemm_host_pipelined(int ta, int tb, int64_t m, int64_t n, int64_t k,
     // the staging buffer was allocated on the compute stream
     GB_CUDA(cudaEventRecord(ready, p.s));
     GB_CUDA(cudaStreamWaitEvent(p.cin, ready, 0));
+    p.mark(p.cin, "start", 0);
     // op(A) and block 0 of op(B) segment by segment, interleaved: the first
     // segment's slice GEMM needs only the first of each
     int st;
@@ -241,8 +290,6 @@ static int dgemm_host_pipelined(int ta, int tb, int64_t m, int64_t n, int64_t k,
       if ((st = p.upload_a(sg))) return st;
       if ((st = p.upload(0, sg))) return st;
     }
-    // one K segment: op(A) is split once, before the block loop
-    if (p.nseg == 1) GB_CUDA(cudaStreamWaitEvent(p.s, p.a_up[0], 0));
     st = dgemm_emulated_blocked(ta, tb, m, n, k, alpha, dA, ra, beta,
                                 ozaki_caller_slices(), p.nb, &p, p.s);
     // the staging buffer is released on the compute stream after the last download
@@ -250,9 +297,13 @@ static int dgemm_host_pipelined(int ta, int tb, int64_t m, int64_t n, int64_t k,
     GB_CUDA(cudaStreamWaitEvent(p.s, out_done, 0));
     return st;
   };
+  p.trace = config().verbose >= 3;
   int st = run();
+  p.h1 = std::chrono::steady_clock::now();
   cudaStreamSynchronize(p.cin);
   cudaStreamSynchronize(p.cout);
+  p.h2 = std::chrono::steady_clock::now();
+  p.report();
   if (!st) finish_blocking(p.s);
   else cudaStreamSynchronize(p.s);
   for (auto *v : {&p.a_up, &p.up, &p.done})

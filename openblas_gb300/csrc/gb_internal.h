@@ -177,20 +177,24 @@ int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha
                    const double *A, int64_t lda, const double *B, int64_t ldb, double beta,
                    double *C, int64_t ldc, int slices, cudaStream_t s, int tri = 0,
                    const int *skip = nullptr);
-// Column-blocked emulated DGEMM (one K segment, k <= 16384): op(A) is split
-// once; for each block of nb columns of op(B) and C, hooks->before supplies
-// device pointers to the block (after making it available, e.g. waiting for
-// its upload) and hooks->after runs once C's block is final (e.g. to start
-// its download), so transfers overlap the other blocks' work.
-// K segment of the emulated engine: every int32 level sum of one segment is
-// exact (8 products x 4096 x 255^2 < 2^31); longer K runs segment by segment.
+// Column-blocked emulated DGEMM (k <= 16384): op(A) is prepared once per K
+// segment; for each block of nb columns of op(B) and C, hooks->before
+// supplies device pointers to the block (after making it available, e.g.
+// waiting for its upload) and hooks->after runs once C's block is final
+// (e.g. to start its download), so transfers overlap the other blocks' work.
+// K segment of the digit-slice engine: every int32 level sum of one segment
+// is exact (8 products x 4096 x 255^2 < 2^31); longer K runs segment by
+// segment (the automatic mode's modular scheme takes segments of twice
+// this).
 constexpr int64_t EMU_K_SEGMENT = 4096;
-// hooks->segment(j0, jn, k0, kk) runs before the K segment [k0, k0 + kk) of
-// the block is used (e.g. to wait for that segment of op(A) and op(B)).
+// hooks->segment(j0, jn, k0, kk) runs before the K range [k0, k0 + kk) of
+// the block is used (e.g. to wait for that range of op(A) and op(B)), and
+// hooks->a_range(k0, kk) before op(A)'s columns [k0, k0 + kk) are first read.
 struct EmuBlockHooks {
   virtual int before(int64_t j0, int64_t jn, const double **Bj, int64_t *ldb, double **Cj,
                      int64_t *ldc) = 0;
   virtual int segment(int64_t, int64_t, int64_t, int64_t) { return GB_SUCCESS; }
+  virtual int a_range(int64_t, int64_t) { return GB_SUCCESS; }
   virtual int after(int64_t j0, int64_t jn) = 0;
   virtual ~EmuBlockHooks() = default;
 };

@@ -52,6 +52,8 @@
 #include <math.h>
 #include <stdint.h>
 
+#include <vector>
+
 #include "gb_internal.h"
 #include "lapack_internal.h"
 #include "ozaki_digits.cuh"
@@ -75,6 +77,11 @@ constexpr int TMEM_COLS = 512;
 constexpr int SMEM_BYTES = STAGES * STAGE_BYTES + 1024 /*align*/ + 256 /*barriers*/;
 constexpr int MAX_SLICES = 8;
 constexpr int64_t MAX_K_SEGMENT = EMU_K_SEGMENT;   // keeps a level sum below 2^31
+// K segment of the automatic mode when the modular scheme is allowed: one
+// residue product's int32 sum stays below 2^29; digit-slice tiles run the
+// segment as sub-segments of MAX_K_SEGMENT.
+constexpr int64_t MOD_K_SEGMENT = 2 * MAX_K_SEGMENT;
+static_assert(MOD_K_SEGMENT * 255 * 255 < (1LL << 29), "a residue sum fits the epilogue's reduction");
 static_assert(256LL * 255 * 255 < (1LL << 24), "a 256-deep chunk of one product is exact in FP32");
 static_assert(8LL * MAX_K_SEGMENT * 255 * 255 < (1LL << 31), "a level sum fits int32");
 constexpr uint64_t WAIT_LIMIT_NS = 4000000000ull;
@@ -104,6 +111,7 @@ struct GemmParams {
   int group_m;  // m-tiles per group of the tile order
   int tri;      // 0 all tiles; 1 only tiles meeting i >= j; 2 only tiles meeting i <= j
   int kblocks;
+  int kblock0;  // first K block of the operands' tensor maps this launch reads
   int m_pad, n_pad;
   int64_t plane_stride;
   int *planes;
@@ -113,7 +121,8 @@ struct GemmParams {
   // s_tiles[nt] == 0 (all when null) take part.
   const int *s_tiles;
   const int *run_if;   // when non-null and *run_if == 0 the launch does nothing
-  int mod_p[MOD_COUNT];  // moduli (modular scheme)
+  int mod_p[MOD_COUNT];          // moduli (modular scheme)
+  uint32_t mod_magic[MOD_COUNT];  // ceil(2^40 / p_l): u / p_l = umulhi(u, magic) >> 8 for u < 2^31
 };
 
 // Products of one output tile, in levels that share an accumulation: digit
@@ -250,8 +259,8 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
                   break;
                 }
                 mbar_arrive_expect_tx(&full[stage], STAGE_BYTES);
-                tma_load_2d(sA + stage * A_BYTES, &tmA, &full[stage], kb * BK, rowA);
-                tma_load_2d(sB + stage * B_BYTES, &tmB, &full[stage], kb * BK, rowB);
+                tma_load_2d(sA + stage * A_BYTES, &tmA, &full[stage], (p.kblock0 + kb) * BK, rowA);
+                tma_load_2d(sB + stage * B_BYTES, &tmB, &full[stage], (p.kblock0 + kb) * BK, rowB);
                 issued[stage] = true;
                 issued_phase[stage] = phase;
                 if (++stage == STAGES) {
@@ -382,13 +391,18 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
         const int64_t at = (int64_t)l * p.plane_stride + plane_tile * (BM * BN) +
                            (int64_t)(half * 128) * BM + row;
         if (MOD) {
-          // residue of the product modulo p_l, in [0, p_l), as 16 bits
-          const int pm = p.mod_p[l];
+          // residue of the product modulo p_l, in [0, p_l), as 16 bits:
+          // u = sum + p_l 2^21 is positive and below 2^31 (|sum| < 2^29), and
+          // with magic = ceil(2^40 / p_l) the quotient umulhi(u, magic) >> 8
+          // is exact (u * (magic - 2^40 / p_l) / 2^40 < 2^-9 < 1 / p_l)
+          const uint32_t pm = (uint32_t)p.mod_p[l], magic = p.mod_magic[l];
+          const uint32_t off = pm << 21;
           uint16_t *dst = reinterpret_cast<uint16_t *>(p.planes) + at;
 #pragma unroll
           for (int c = 0; c < 128; ++c) {
-            int r = sum[c] % pm;
-            dst[c * BM] = (uint16_t)(r < 0 ? r + pm : r);
+            const uint32_t u = (uint32_t)sum[c] + off;
+            const uint32_t q = __umulhi(u, magic) >> 8;
+            dst[c * BM] = (uint16_t)(u - q * pm);
           }
         } else {
           int *dst = p.planes + at;
@@ -470,36 +484,66 @@ __global__ void rowmax_mcontig_kernel(int64_t R, int64_t K, const double *__rest
 // MAX_SLICES digits and every tile uses the first S of them.
 constexpr double DROP_C = 7.0 * (1.0 + 1.0 / 128.0);
 
-// alpha_k = sum over the finite rows r of op(A) (R x K view) of |x_rk|.
-// KCONTIG (op(A) row r is K-contiguous): a thread per k, a chunk of rows per
+// The statistics run in FP32 (FP64 is the scarcest unit on this part):
+// every |x| is scaled by a power of two that puts it below 1 (the largest
+// row exponent of op(A) for alpha_k, the column's own exponent for op(B)),
+// truncated to FP32 (|x| 2^-e below FP32's normal range counts as 0) and
+// summed in FP32.  Each sum is then within 2^-12 relative of its exact value
+// (24-bit truncation; at most 256 terms summed in one register, then a tree
+// or an atomic reduction of at most 2^12 partial sums), less the dropped
+// values, each below 2^-126 of the largest.  The choice multiplies every
+// ratio by RHO_SLACK = 1 + 2^-8, which covers both.
+constexpr double RHO_SLACK = 1.0 + 1.0 / 256.0;
+
+// |x| 2^-e as FP32, truncated (|x| < 2^(e + 1) assumed), 0 below 2^-126.
+__device__ __forceinline__ float scaled_abs(double x, int e) {
+  const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+  int E = (int)(b >> 52);
+  unsigned long long mant = b & 0xFFFFFFFFFFFFFull;
+  if (E == 0) {  // subnormal double: normalise
+    if (mant == 0) return 0.0f;
+    const int top = 63 - __clzll((long long)mant);  // value = 1.f 2^(top - 1074)
+    mant = (mant << (52 - top)) & 0xFFFFFFFFFFFFFull;
+    E = top - 51;
+  }
+  const int fe = E - 1023 - e + 127;
+  if (fe <= 0) return 0.0f;
+  return __uint_as_float(((unsigned)fe << 23) | (unsigned)(mant >> 29));
+}
+
+// alpha_k 2^-E_A in FP32, E_A = *emax (the largest row exponent of op(A)),
+// summed over the finite rows r of op(A) (R x K view) of |x_rk|.  KCONTIG
+// (op(A) row r is K-contiguous): a thread per k, a chunk of rows per
 // blockIdx.y.  Otherwise a block per k, the rows read down the column.
 template <bool KCONTIG>
 __global__ void __launch_bounds__(256)
 abs_colsum_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
-                  const int *__restrict__ expo, int64_t rspan, double *__restrict__ alpha) {
+                  const int *__restrict__ expo, const int *__restrict__ emax, int64_t rspan,
+                  float *__restrict__ alpha) {
+  const int ea = *emax;
   if (KCONTIG) {
     const int64_t kk = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (kk >= K) return;
     const int64_t r0 = (int64_t)blockIdx.y * rspan;
     const int64_t r1 = r0 + rspan < R ? r0 + rspan : R;
-    double s = 0.0;
+    float s = 0.0f;
     for (int64_t r = r0; r < r1; ++r)
-      if (expo[r] != NONFINITE) s += fabs(X[kk + r * ld]);
+      if (expo[r] != NONFINITE) s += scaled_abs(X[kk + r * ld], ea);
     atomicAdd(alpha + kk, s);
   } else {
     const int64_t kk = blockIdx.x;
     const int64_t r0 = (int64_t)blockIdx.y * rspan;
     const int64_t r1 = r0 + rspan < R ? r0 + rspan : R;
-    double s = 0.0;
+    float s = 0.0f;
     for (int64_t r = r0 + threadIdx.x; r < r1; r += blockDim.x)
-      if (expo[r] != NONFINITE) s += fabs(X[r + kk * ld]);
+      if (expo[r] != NONFINITE) s += scaled_abs(X[r + kk * ld], ea);
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) s += __shfl_down_sync(0xffffffffu, s, off);
-    __shared__ double part[8];
+    __shared__ float part[8];
     if ((threadIdx.x & 31) == 0) part[threadIdx.x >> 5] = s;
     __syncthreads();
     if (threadIdx.x == 0) {
-      double t = 0.0;
+      float t = 0.0f;
       for (int w = 0; w < (int)(blockDim.x >> 5); ++w) t += part[w];
       atomicAdd(alpha + kk, t);
     }
@@ -507,15 +551,16 @@ abs_colsum_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld
 }
 
 // totals[0] = T_e = sum of 2^e_r over the non-zero finite rows of op(A),
-// totals[1] = T_1 = sum_k alpha_k.  One block.
+// totals[1] = T_1 = sum_k alpha_k, totals[2] = E_A (the scale of the FP32
+// alpha_k).  One block.
 __global__ void __launch_bounds__(256)
 a_totals_kernel(int64_t R, int64_t K, const int *__restrict__ expo,
-                const unsigned long long *__restrict__ mx, const double *__restrict__ alpha,
-                double *__restrict__ totals) {
+                const unsigned long long *__restrict__ mx, const float *__restrict__ alpha,
+                const int *__restrict__ emax, double *__restrict__ totals) {
   double te = 0.0, t1 = 0.0;
   for (int64_t r = threadIdx.x; r < R; r += blockDim.x)
     if (mx[r] != 0 && expo[r] != NONFINITE) te += ldexp(1.0, expo[r]);
-  for (int64_t kk = threadIdx.x; kk < K; kk += blockDim.x) t1 += alpha[kk];
+  for (int64_t kk = threadIdx.x; kk < K; kk += blockDim.x) t1 += (double)alpha[kk];
   __shared__ double pe[256], p1[256];
   pe[threadIdx.x] = te;
   p1[threadIdx.x] = t1;
@@ -529,64 +574,89 @@ a_totals_kernel(int64_t R, int64_t K, const int *__restrict__ expo,
   }
   if (threadIdx.x == 0) {
     totals[0] = pe[0];
-    totals[1] = p1[0];
+    totals[1] = ldexp(p1[0], *emax);
+    totals[2] = (double)*emax;
   }
 }
 
-// The row maxima of op(B)'s R x K view (R = columns of op(B)) together with
-// the column sums ||b_j||_1 (s1) and w_j = sum_k alpha_k |b_kj| (s2).
-__global__ void rowmax_stats_kcontig_kernel(int64_t R, int64_t K, const double *__restrict__ X,
-                                            int64_t ld, const double *__restrict__ alpha,
-                                            unsigned long long *__restrict__ out,
-                                            double *__restrict__ s1, double *__restrict__ s2) {
+// op(B)'s R x K view (R = columns of op(B)), a warp per column: the column
+// maximum and exponent f_j, then (a second read, from L2) the column sums
+// s1_j 2^-f_j = sum_k |b_kj| 2^-f_j and s2_j 2^-(f_j + E_A) =
+// sum_k (alpha_k 2^-E_A)(|b_kj| 2^-f_j) in FP32.  Rows R..Rpad-1 get
+// exponent 0 and zero sums.
+__global__ void col_stats_kcontig_kernel(int64_t R, int64_t Rpad, int64_t K,
+                                         const double *__restrict__ X, int64_t ld,
+                                         const float *__restrict__ alpha,
+                                         unsigned long long *__restrict__ out,
+                                         int *__restrict__ expo, float *__restrict__ s1,
+                                         float *__restrict__ s2) {
   const int64_t r = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
-  if (r >= R) return;
+  if (r >= Rpad) return;
+  if (r >= R) {
+    if (lane == 0) {
+      out[r] = 0;
+      expo[r] = 0;
+      s1[r] = s2[r] = 0.0f;
+    }
+    return;
+  }
   const double *x = X + r * ld;
   unsigned long long best = 0;
-  double a1 = 0.0, a2 = 0.0;
 #pragma unroll 4
   for (int64_t pp = lane; pp < K; pp += 32) {
-    const double v = fabs(x[pp]);
-    const unsigned long long b = __double_as_longlong(v);
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x[pp]) &
+                                 0x7FFFFFFFFFFFFFFFull;
     best = b > best ? b : best;
-    a1 += v;
-    a2 = fma(alpha[pp], v, a2);
   }
 #pragma unroll
   for (int off = 16; off > 0; off >>= 1) {
-    unsigned long long o = __shfl_down_sync(0xffffffffu, best, off);
+    const unsigned long long o = __shfl_xor_sync(0xffffffffu, best, off);
     best = o > best ? o : best;
-    a1 += __shfl_down_sync(0xffffffffu, a1, off);
-    a2 += __shfl_down_sync(0xffffffffu, a2, off);
+  }
+  const int f = ozd::exponent_of_max(best);
+  float a1 = 0.0f, a2 = 0.0f;
+  if (best != 0 && f != NONFINITE) {
+#pragma unroll 4
+    for (int64_t pp = lane; pp < K; pp += 32) {
+      const float v = scaled_abs(x[pp], f);
+      a1 += v;
+      a2 = fmaf(alpha[pp], v, a2);
+    }
+#pragma unroll
+    for (int off = 16; off > 0; off >>= 1) {
+      a1 += __shfl_down_sync(0xffffffffu, a1, off);
+      a2 += __shfl_down_sync(0xffffffffu, a2, off);
+    }
   }
   if (lane == 0) {
     out[r] = best;
+    expo[r] = f;
     s1[r] = a1;
     s2[r] = a2;
   }
 }
 
-__global__ void rowmax_stats_mcontig_kernel(int64_t R, int64_t K, const double *__restrict__ X,
-                                            int64_t ld, int64_t kspan,
-                                            const double *__restrict__ alpha,
-                                            unsigned long long *__restrict__ out,
-                                            double *__restrict__ s1, double *__restrict__ s2) {
+// The same sums when op(B)'s columns are strided (B transposed): a thread per
+// column and a K span per blockIdx.y, after the column exponents are known.
+__global__ void col_stats_mcontig_kernel(int64_t R, int64_t K, const double *__restrict__ X,
+                                         int64_t ld, int64_t kspan,
+                                         const float *__restrict__ alpha,
+                                         const int *__restrict__ expo, float *__restrict__ s1,
+                                         float *__restrict__ s2) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= R) return;
+  const int f = expo[r];
+  if (f == NONFINITE) return;
   const int64_t p0 = (int64_t)blockIdx.y * kspan;
   const int64_t p1 = p0 + kspan < K ? p0 + kspan : K;
-  unsigned long long best = 0;
-  double a1 = 0.0, a2 = 0.0;
+  float a1 = 0.0f, a2 = 0.0f;
 #pragma unroll 4
   for (int64_t pp = p0; pp < p1; ++pp) {
-    const double v = fabs(X[r + pp * ld]);
-    const unsigned long long b = __double_as_longlong(v);
-    best = b > best ? b : best;
+    const float v = scaled_abs(X[r + pp * ld], f);
     a1 += v;
-    a2 = fma(alpha[pp], v, a2);
+    a2 = fmaf(alpha[pp], v, a2);
   }
-  atomicMax(out + r, best);
   atomicAdd(s1 + r, a1);
   atomicAdd(s2 + r, a2);
 }
@@ -595,26 +665,32 @@ __global__ void rowmax_stats_mcontig_kernel(int64_t R, int64_t K, const double *
 // slices) and rho2_j (modular scheme, t = mod_t bits; 0: not allowed), in
 //   rho2_j = (T_e ||b_j||_1 + 2^f_j (T_1 + 2^-t k T_e)) / w_j
 // (no dropped products, only the cut of the operands).  The tile takes the
-// modular scheme when 2^-t max rho2_j meets the budget (s_tiles = 0,
+// modular scheme when 2^-t max rho2_j meets budget_mod (s_tiles = 0,
 // counted in pass[0], the call's moduli count kept in *last_moduli), else
-// the smallest slice count that does (counted in pass[1], the largest count
-// of the call kept in *last).
+// the smallest slice count whose bound meets budget_dig (counted in
+// pass[1], the largest count of the call kept in *last).  k is the segment:
+// the digit-slice bound summed over its sub-segments is the same bound with
+// k the whole segment; the budgets differ by the roundings of the segment
+// and sub-segment accumulations.
 __global__ void __launch_bounds__(256)
 choose_slices_kernel(int64_t R, const int *__restrict__ expo,
-                     const unsigned long long *__restrict__ mx, const double *__restrict__ s1,
-                     const double *__restrict__ s2, const double *__restrict__ totals, int64_t k,
-                     double budget, int mod_t, int *__restrict__ s_tiles, int *__restrict__ last,
+                     const unsigned long long *__restrict__ mx, const float *__restrict__ s1f,
+                     const float *__restrict__ s2f, const double *__restrict__ totals, int64_t k,
+                     double budget_mod, double budget_dig, int mod_t, int *__restrict__ s_tiles,
+                     int *__restrict__ last,
                      int *__restrict__ last_moduli, int *__restrict__ pass) {
   const int64_t j = (int64_t)blockIdx.x * BN + threadIdx.x;
   double rho = 0.0, rho2 = 0.0;
-  if (j < R && mx[j] != 0 && expo[j] != NONFINITE && s2[j] > 0.0) {
+  if (j < R && mx[j] != 0 && expo[j] != NONFINITE && s2f[j] > 0.0f) {
     const double te = totals[0], t1 = totals[1];
-    rho = (te * s1[j] + ldexp(t1 + DROP_C * (double)k * te, expo[j])) / s2[j];
-    rho2 = (te * s1[j] + ldexp(t1 + ldexp((double)k * te, -mod_t), expo[j])) / s2[j];
+    const int fj = expo[j], ea = (int)totals[2];
+    const double s1 = ldexp((double)s1f[j], fj), s2 = ldexp((double)s2f[j], fj + ea);
+    rho = RHO_SLACK * (te * s1 + ldexp(t1 + DROP_C * (double)k * te, fj)) / s2;
+    rho2 = RHO_SLACK * (te * s1 + ldexp(t1 + ldexp((double)k * te, -mod_t), fj)) / s2;
     if (!(rho <= 1e300)) rho = 1e300;  // Inf or NaN: the largest count
     if (!(rho2 <= 1e300)) rho2 = 1e300;
-  } else if (j < R && mx[j] != 0 && expo[j] != NONFINITE && s2[j] != 0.0) {
-    rho = rho2 = 1e300;  // w_j NaN
+  } else if (j < R && mx[j] != 0 && expo[j] != NONFINITE) {
+    rho = rho2 = 1e300;  // every product of the column too small for the FP32 sums
   }
   __shared__ double red[256], red2[256];
   red[threadIdx.x] = rho;
@@ -628,7 +704,7 @@ choose_slices_kernel(int64_t R, const int *__restrict__ expo,
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    if (mod_t > 0 && ldexp(red2[0], -mod_t) <= budget) {
+    if (mod_t > 0 && ldexp(red2[0], -mod_t) <= budget_mod) {
       s_tiles[blockIdx.x] = 0;
       atomicAdd(pass, 1);
       atomicMax(last_moduli, MOD_COUNT);
@@ -636,7 +712,7 @@ choose_slices_kernel(int64_t R, const int *__restrict__ expo,
     }
     int S = MAX_SLICES;
     for (int c = 1; c < MAX_SLICES; ++c)
-      if (ldexp(red[0], -DIGIT_BITS * c) <= budget) {
+      if (ldexp(red[0], -DIGIT_BITS * c) <= budget_dig) {
         S = c;
         break;
       }
@@ -646,11 +722,15 @@ choose_slices_kernel(int64_t R, const int *__restrict__ expo,
   }
 }
 
+// Row exponents (|x| < 2^e on the row); with emax, also their maximum over
+// the non-zero finite rows (emax preset to a large negative value).
 __global__ void exponent_kernel(int64_t Rpad, int64_t R, const unsigned long long *__restrict__ mx,
-                                int *__restrict__ expo) {
+                                int *__restrict__ expo, int *__restrict__ emax) {
   const int64_t r = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   if (r >= Rpad) return;
-  expo[r] = r < R ? ozd::exponent_of_max(mx[r]) : 0;  // |x| < 2^e on the row
+  const int e = r < R ? ozd::exponent_of_max(mx[r]) : 0;
+  expo[r] = e;
+  if (emax && r < R && mx[r] != 0 && e != NONFINITE) atomicMax(emax, e);
 }
 
 // Digits of a 32-row x 64-K tile.  The tile is staged through shared memory
@@ -744,31 +824,42 @@ split_mod_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
   const int rr = tid >> 3, pc = (tid & 7) * 8;
   const int64_t r = r0 + rr;
   const int e = (r < R) ? expo[r] : 0;
+  // the chunks of sign(x) |A'| as signed floats (the residue of -A' is minus
+  // the residue of A': no modulus is even, so no quotient is a tie)
   float ch[8][MOD_CHUNKS];
-  bool neg[8];
 #pragma unroll
   for (int j = 0; j < 8; ++j) {
-    const unsigned long long mag = ozd::fixed_magnitude(tile[rr][pc + j], e, tab.bits, neg[j]);
+    bool neg;
+    const unsigned long long mag = ozd::fixed_magnitude(tile[rr][pc + j], e, tab.bits, neg);
+    const unsigned sgn = neg ? 0x80000000u : 0u;
 #pragma unroll
     for (int d = 0; d < MOD_CHUNKS; ++d) {
       // exact int -> float of a 12-bit value: 2^23 + c, less 2^23
       const unsigned c = (unsigned)(mag >> (MOD_CHUNK_BITS * d)) & ((1u << MOD_CHUNK_BITS) - 1);
-      ch[j][d] = __uint_as_float(0x4B000000u | c) - 8388608.0f;
+      ch[j][d] = __uint_as_float(sgn ^ __float_as_uint(__uint_as_float(0x4B000000u | c) -
+                                                       8388608.0f));
     }
   }
+  constexpr float ROUND = 12582912.0f;  // 1.5 * 2^23: adding it rounds |y| < 2^22 to an integer
 #pragma unroll 2
   for (int l = 0; l < MOD_COUNT; ++l) {
     const float pl = tab.pf[l], pinv = tab.pinv[l], half = 0.5f * (pl - 1.0f);
-    __align__(16) __nv_bfloat16 out[8];
+    __align__(16) __nv_bfloat162 out[4];
 #pragma unroll
-    for (int j = 0; j < 8; ++j) {
-      float v = 0.0f;
+    for (int j = 0; j < 8; j += 2) {
+      float v[2];
 #pragma unroll
-      for (int d = 0; d < MOD_CHUNKS; ++d) v = fmaf(ch[j][d], tab.pw[l][d], v);
-      v = fmaf(-rintf(v * pinv), pl, v);  // exact: both terms are integers below 2^24
-      if (v > half) v -= pl;              // the rounded quotient can be one off
-      if (v < -half) v += pl;
-      out[j] = __float2bfloat16_rn(neg[j] ? -v : v);
+      for (int h = 0; h < 2; ++h) {
+        float x = 0.0f;
+#pragma unroll
+        for (int d = 0; d < MOD_CHUNKS; ++d) x = fmaf(ch[j + h][d], tab.pw[l][d], x);
+        const float q = fmaf(x, pinv, ROUND) - ROUND;  // round(x / p_l), possibly one off
+        x = fmaf(-q, pl, x);  // exact: both terms are integers below 2^24
+        if (x > half) x -= pl;
+        if (x < -half) x += pl;
+        v[h] = x;
+      }
+      out[j >> 1] = __floats2bfloat162_rn(v[0], v[1]);
     }
     __nv_bfloat16 *dst = res + ((int64_t)l * Rpad + r) * Kpad + p0 + pc;
     *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<const uint4 *>(out);
@@ -902,22 +993,25 @@ reconstruct_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
   const int64_t i0 = (int64_t)mt * BM, j0 = (int64_t)nt * BN;
   if (tri == 1 && i0 + BM - 1 < j0) return;
   if (tri == 2 && i0 > j0 + BN - 1) return;
+  // a thread takes two consecutive rows of a column (one 4-byte load per
+  // plane), 64 threads a column; few registers per thread keep enough warps
+  // resident to hide the integer multiply chains
   const int tid = threadIdx.x;
-  const int il = (tid & 31) * 4, jb = tid >> 5;
+  const int il = (tid & 63) * 2, jb = tid >> 6;
   const uint16_t *pt = planes + ((int64_t)nt * m_tiles + mt) * (BM * BN);
-  int e_i[4];
+  int e_i[2];
 #pragma unroll
-  for (int r = 0; r < 4; ++r) e_i[r] = (i0 + il + r < m) ? ea[i0 + il + r] : 0;
-  for (int jl = jb; jl < BN; jl += 8) {
+  for (int r = 0; r < 2; ++r) e_i[r] = (i0 + il + r < m) ? ea[i0 + il + r] : 0;
+  for (int jl = jb; jl < BN; jl += 4) {
     const int64_t j = j0 + jl;
     if (j >= n) break;
     const int fj = eb[j];
-    uint2 P[MOD_COUNT];
+    uint32_t P[MOD_COUNT];
 #pragma unroll
     for (int l = 0; l < MOD_COUNT; ++l)
-      P[l] = *reinterpret_cast<const uint2 *>(pt + (int64_t)l * plane_stride + jl * BM + il);
+      P[l] = *reinterpret_cast<const uint32_t *>(pt + (int64_t)l * plane_stride + jl * BM + il);
 #pragma unroll
-    for (int r = 0; r < 4; ++r) {
+    for (int r = 0; r < 2; ++r) {
       const int64_t i = i0 + il + r;
       if (i >= m) continue;
       if ((tri == 1 && i < j) || (tri == 2 && i > j)) continue;
@@ -935,8 +1029,7 @@ reconstruct_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
         long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
 #pragma unroll
         for (int l = 0; l < MOD_COUNT; ++l) {
-          const unsigned w = (r < 2) ? P[l].x : P[l].y;
-          const unsigned long long rl = (r & 1) ? (w >> 16) : (w & 0xFFFFu);
+          const unsigned long long rl = r ? (P[l] >> 16) : (P[l] & 0xFFFFu);
           qa += rl * tab.F[l];
           a0 += (long long)(rl * tab.W[l][0]);
           a1 += (long long)(rl * tab.W[l][1]);
@@ -952,7 +1045,13 @@ reconstruct_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
                                     ((unsigned __int128)(__int128)a1 << 32) +
                                     ((unsigned __int128)(__int128)a2 << 64) +
                                     ((unsigned __int128)(__int128)a3 << 96);
-        v = ozd::scaled_value((__int128)u, e_i[r] + fj - 2 * tab.bits, alpha);
+        const int x0 = e_i[r] + fj - 2 * tab.bits;
+        bool ok;
+        v = ozd::int_scaled((__int128)u, x0, ok);
+        if (!ok)
+          v = ozd::scaled_value((__int128)u, x0, alpha);
+        else if (alpha != 1.0)
+          v *= alpha;
       }
       double *c = C + i + j * ldc;
       *c = (beta == 0.0) ? v : fma(beta, *c, v);
@@ -1058,10 +1157,13 @@ void launch_split_mod(bool kcontig, int64_t R, int64_t K, const double *X, int64
   count_launch();
 }
 
-// Row maxima and exponents of an R x K op-view operand.
+// Row maxima and exponents of an R x K op-view operand (with emax: their
+// maximum over the non-zero finite rows as well).
 void operand_exponents(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld,
-                       int64_t Rpad, unsigned long long *mx, int *expo, cudaStream_t s) {
+                       int64_t Rpad, unsigned long long *mx, int *expo, cudaStream_t s,
+                       int *emax = nullptr) {
   cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * Rpad, s);
+  if (emax) cudaMemsetAsync(emax, 0x80, sizeof(int), s);  // a large negative value
   if (kcontig) {
     { rowmax_kcontig_kernel<<<(unsigned)((R + 7) / 8), 256, 0, s>>>(R, K, X, ld, mx); count_launch(); }
   } else {
@@ -1069,7 +1171,7 @@ void operand_exponents(bool kcontig, int64_t R, int64_t K, const double *X, int6
     dim3 g((unsigned)((R + 255) / 256), (unsigned)((K + kspan - 1) / kspan));
     { rowmax_mcontig_kernel<<<g, 256, 0, s>>>(R, K, X, ld, kspan, mx); count_launch(); }
   }
-  { exponent_kernel<<<(unsigned)((Rpad + 255) / 256), 256, 0, s>>>(Rpad, R, mx, expo); count_launch(); }
+  { exponent_kernel<<<(unsigned)((Rpad + 255) / 256), 256, 0, s>>>(Rpad, R, mx, expo, emax); count_launch(); }
 }
 
 // Split an R x K op-view operand into S K-contiguous bf16 slices + exponents.
@@ -1080,52 +1182,54 @@ void split_operand(bool kcontig, int64_t R, int64_t K, const double *X, int64_t 
   launch_split(kcontig, R, K, X, ld, expo, S, Rpad, Kpad, slices, nullptr, nullptr, s);
 }
 
-// Automatic choice, op(A) side: the column sums alpha_k of |op(A)| and the
-// totals T_e, T_1 (after op(A)'s exponents are known).
+// Automatic choice, op(A) side (after op(A)'s exponents and their maximum
+// emax are known): alpha_k 2^-E_A in FP32 and the totals T_e, T_1, E_A.
 void a_side_stats(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld,
-                  const int *expo, const unsigned long long *mx, double *alpha, double *totals,
-                  cudaStream_t s) {
-  cudaMemsetAsync(alpha, 0, sizeof(double) * K, s);
-  const int64_t rspan = 1024;
+                  const int *expo, const unsigned long long *mx, const int *emax, float *alpha,
+                  double *totals, cudaStream_t s) {
+  cudaMemsetAsync(alpha, 0, sizeof(float) * K, s);
+  const int64_t rspan = kcontig ? 256 : 1024;  // at most 256 rows summed by one thread
   if (kcontig) {
     dim3 g((unsigned)((K + 255) / 256), (unsigned)((R + rspan - 1) / rspan));
-    { abs_colsum_kernel<true><<<g, 256, 0, s>>>(R, K, X, ld, expo, rspan, alpha); count_launch(); }
+    { abs_colsum_kernel<true><<<g, 256, 0, s>>>(R, K, X, ld, expo, emax, rspan, alpha); count_launch(); }
   } else {
     dim3 g((unsigned)K, (unsigned)((R + rspan - 1) / rspan));
-    { abs_colsum_kernel<false><<<g, 256, 0, s>>>(R, K, X, ld, expo, rspan, alpha); count_launch(); }
+    { abs_colsum_kernel<false><<<g, 256, 0, s>>>(R, K, X, ld, expo, emax, rspan, alpha); count_launch(); }
   }
-  { a_totals_kernel<<<1, 256, 0, s>>>(R, K, expo, mx, alpha, totals); count_launch(); }
+  { a_totals_kernel<<<1, 256, 0, s>>>(R, K, expo, mx, alpha, emax, totals); count_launch(); }
 }
 
-// Automatic choice, op(B) side: exponents and column statistics of op(B)
-// in one pass, then the scheme (and slice count) of every 256-column tile.
+// Automatic choice, op(B) side: exponents and FP32 column statistics of
+// op(B), then the scheme (and slice count) of every 256-column tile.
 void choose_b(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld, int64_t Rpad,
-              unsigned long long *mx, int *expo, const double *alpha, const double *totals,
-              double *s1, double *s2, double budget, int mod_t, int *s_tiles, int *pass,
-              cudaStream_t s) {
-  cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * Rpad, s);
+              unsigned long long *mx, int *expo, const float *alpha, const double *totals,
+              float *s1, float *s2, double budget_mod, double budget_dig, int mod_t,
+              int *s_tiles, int *pass, cudaStream_t s) {
   cudaMemsetAsync(pass, 0, 2 * sizeof(int), s);
   if (kcontig) {
-    { rowmax_stats_kcontig_kernel<<<(unsigned)((R + 7) / 8), 256, 0, s>>>(R, K, X, ld, alpha, mx,
-                                                                          s1, s2); count_launch(); }
+    { col_stats_kcontig_kernel<<<(unsigned)((Rpad + 7) / 8), 256, 0, s>>>(R, Rpad, K, X, ld, alpha,
+                                                                          mx, expo, s1, s2); count_launch(); }
   } else {
-    cudaMemsetAsync(s1, 0, sizeof(double) * Rpad, s);
-    cudaMemsetAsync(s2, 0, sizeof(double) * Rpad, s);
+    operand_exponents(false, R, K, X, ld, Rpad, mx, expo, s);
+    cudaMemsetAsync(s1, 0, sizeof(float) * Rpad, s);
+    cudaMemsetAsync(s2, 0, sizeof(float) * Rpad, s);
     const int64_t kspan = 256;
     dim3 g((unsigned)((R + 255) / 256), (unsigned)((K + kspan - 1) / kspan));
-    { rowmax_stats_mcontig_kernel<<<g, 256, 0, s>>>(R, K, X, ld, kspan, alpha, mx, s1, s2); count_launch(); }
+    { col_stats_mcontig_kernel<<<g, 256, 0, s>>>(R, K, X, ld, kspan, alpha, expo, s1, s2); count_launch(); }
   }
-  { exponent_kernel<<<(unsigned)((Rpad + 255) / 256), 256, 0, s>>>(Rpad, R, mx, expo); count_launch(); }
   int *status = ctx().d_status;
   { choose_slices_kernel<<<(unsigned)(Rpad / BN), 256, 0, s>>>(
-        R, expo, mx, s1, s2, totals, K, budget, mod_t, s_tiles, status + STATUS_LAST_SLICES,
+        R, expo, mx, s1, s2, totals, K, budget_mod, budget_dig, mod_t, s_tiles,
+        status + STATUS_LAST_SLICES,
         status + STATUS_LAST_MODULI, pass); count_launch(); }
 }
 
 // The whole emulated product.  K is cut into segments of at most
-// MAX_K_SEGMENT (so every int32 level sum is exact); each segment is split,
-// multiplied on the tensor cores and recombined, later segments accumulating
-// into C (beta = 1).  The columns of op(B) and C are taken in blocks of `nb`
+// MAX_K_SEGMENT (so every int32 level sum is exact; MOD_K_SEGMENT in
+// automatic mode with the modular scheme allowed, the digit-slice tiles then
+// taking each segment in sub-segments of MAX_K_SEGMENT); each segment is
+// split, multiplied on the tensor cores and recombined, later segments
+// accumulating into C (beta = 1).  The columns of op(B) and C are taken in blocks of `nb`
 // (a multiple of BN), all segments of a block before the next block, with
 // the hooks (when given) making block j of op(B) and C available on the
 // device first and told when C's block is final.  op(A) is split once when K
@@ -1145,56 +1249,94 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
   if (nb <= 0 || nb >= n) nb = n;
   const bool automatic = S == OZAKI_SLICES_AUTO;
   const int Sa = automatic ? MAX_SLICES : S;  // slices allocated (and cut from op(A))
-  const int64_t kseg = k < MAX_K_SEGMENT ? k : MAX_K_SEGMENT;
-  const int64_t nseg = (k + MAX_K_SEGMENT - 1) / MAX_K_SEGMENT;
-  // the modular scheme's t for the longest segment (0: digit slices only)
-  const int mod_t = automatic && ozaki_modular_enabled() ? mod_bits(kseg) : 0;
-  const bool modular = mod_t > 0;
+  const bool modular = automatic && ozaki_modular_enabled();
+  const int64_t seg_len = modular ? MOD_K_SEGMENT : MAX_K_SEGMENT;
+  const int64_t kseg = k < seg_len ? k : seg_len;
+  const int64_t nseg = (k + seg_len - 1) / seg_len;
+  // the modular scheme's t for the longest segment
+  const int mod_t = modular ? mod_bits(kseg) : 0;
   const int64_t m_pad = round_up(m, BM), nb_pad = round_up(nb, BN), ks_pad = round_up(kseg, BK);
+  // How op(A) is prepared (row maxima, exponents, statistics, splits):
+  //  - one K segment: once, before the block loop (with several column
+  //    blocks in automatic mode, split in both forms, as the blocks' choices
+  //    are not known yet);
+  //  - several segments and several blocks: each segment once, while the
+  //    first block runs, kept for the later blocks (both forms);
+  //  - several segments, one block: per segment, each form predicated on the
+  //    choice.
+  const bool a_once = nseg == 1;
+  const bool a_cache = !a_once && nb < n;
+  const bool a_early = a_once && (!automatic || nb < n);
+  const bool a_both = a_early || a_cache;  // both forms split unpredicated
+  const int64_t a_copies = a_cache ? nseg : 1;
   const int b_planes = modular && MOD_COUNT > Sa ? MOD_COUNT : Sa;
-  const size_t bytes_sa = align256((size_t)Sa * m_pad * ks_pad * 2);
-  const size_t bytes_ra = modular ? align256((size_t)MOD_COUNT * m_pad * ks_pad * 2) : 0;
+  const size_t seg_sa = align256((size_t)Sa * m_pad * ks_pad * 2);
+  const size_t seg_ra = modular ? align256((size_t)MOD_COUNT * m_pad * ks_pad * 2) : 0;
+  const size_t seg_ea = align256((size_t)m_pad * 4);
+  // automatic mode, op(A) side: alpha_k (FP32), the three totals and emax
+  const size_t seg_st = automatic ? align256((size_t)ks_pad * 4) + 256 : 0;
   const size_t bytes_sb = align256((size_t)b_planes * nb_pad * ks_pad * 2);
   const size_t bytes_mx = align256((size_t)(m_pad + nb_pad) * 8);
-  const size_t bytes_e = align256((size_t)(m_pad + nb_pad) * 4);
+  const size_t bytes_eb = align256((size_t)nb_pad * 4);
   const size_t plane_bytes = (size_t)Sa * 4 > (size_t)MOD_COUNT * 2 || !modular
                                  ? (size_t)Sa * 4 : (size_t)MOD_COUNT * 2;
   const size_t bytes_pl = align256(plane_bytes * m_pad * nb_pad);
-  // automatic mode: alpha_k, the two op(A) totals, the column sums of op(B),
-  // the per-tile choices and the two pass counts
+  // automatic mode, op(B) side: its column sums, the per-tile choices and
+  // the two pass counts
   const size_t bytes_auto =
-      automatic ? align256((size_t)(ks_pad + 2 + 2 * nb_pad) * 8 + (size_t)(nb_pad / BN + 2) * 4)
-                : 0;
-  Scratch ws(bytes_sa + bytes_ra + bytes_sb + bytes_mx + bytes_e + bytes_pl + bytes_auto, s);
+      automatic ? align256((size_t)(2 * nb_pad) * 4 + (size_t)(nb_pad / BN + 2) * 4) : 0;
+  Scratch ws((seg_sa + seg_ra + seg_ea + seg_st) * a_copies + bytes_sb + bytes_mx + bytes_eb +
+                 bytes_pl + bytes_auto, s);
   if (!ws.p) return GB_ERR_ALLOC;
   char *base = ws.as<char>();
-  __nv_bfloat16 *sla = reinterpret_cast<__nv_bfloat16 *>(base);
-  base += bytes_sa;
-  __nv_bfloat16 *rsa = reinterpret_cast<__nv_bfloat16 *>(base);
-  base += bytes_ra;
+  char *a_base = base;  // per-segment op(A) data: digits, residues, exponents, statistics
+  base += (seg_sa + seg_ra + seg_ea + seg_st) * a_copies;
   __nv_bfloat16 *slb = reinterpret_cast<__nv_bfloat16 *>(base);
   base += bytes_sb;
   unsigned long long *mx = reinterpret_cast<unsigned long long *>(base);
   base += bytes_mx;
-  int *ea = reinterpret_cast<int *>(base);
-  int *eb = ea + m_pad;
-  base += bytes_e;
+  int *eb = reinterpret_cast<int *>(base);
+  base += bytes_eb;
   int *planes = reinterpret_cast<int *>(base);
   base += bytes_pl;
-  double *st_alpha = nullptr, *st_tot = nullptr, *st_s1 = nullptr, *st_s2 = nullptr;
+  float *st_s1 = nullptr, *st_s2 = nullptr;
   int *s_tiles = nullptr, *pass = nullptr;
-  double budget = 0.0;
+  double budget_mod = 0.0, budget_dig = 0.0;
   if (automatic) {
-    st_alpha = reinterpret_cast<double *>(base);
-    st_tot = st_alpha + ks_pad;
-    st_s1 = st_tot + 2;
+    st_s1 = reinterpret_cast<float *>(base);
     st_s2 = st_s1 + nb_pad;
     s_tiles = reinterpret_cast<int *>(st_s2 + nb_pad);
     pass = s_tiles + nb_pad / BN;  // [0] modular tiles, [1] digit-slice tiles
     // the tolerance in units of 2^-52 less the roundings of the recombine
-    // (one conversion, the alpha/beta step) and of the segment accumulation
-    budget = ldexp(config().ozaki_tol, -52) - ldexp((double)(nseg + 2), -53);
+    // (one conversion, the alpha/beta step) and of the accumulation over
+    // the segments (modular tiles) or the digit passes' sub-segments
+    int64_t nsub = 0;
+    for (int64_t k0 = 0; k0 < k; k0 += seg_len) {
+      const int64_t kk = (k - k0) < seg_len ? (k - k0) : seg_len;
+      nsub += (kk + MAX_K_SEGMENT - 1) / MAX_K_SEGMENT;
+    }
+    budget_mod = ldexp(config().ozaki_tol, -52) - ldexp((double)(nseg + 2), -53);
+    budget_dig = ldexp(config().ozaki_tol, -52) - ldexp((double)(nsub + 2), -53);
   }
+  struct ASeg {
+    __nv_bfloat16 *dig, *res;
+    int *ea;
+    float *alpha;
+    double *tot;
+    int *emax;
+  };
+  auto aseg = [&](int64_t sg) {
+    char *p = a_base + (a_cache ? sg : 0) * (seg_sa + seg_ra + seg_ea + seg_st);
+    ASeg a;
+    a.dig = reinterpret_cast<__nv_bfloat16 *>(p);
+    a.res = reinterpret_cast<__nv_bfloat16 *>(p + seg_sa);
+    a.ea = reinterpret_cast<int *>(p + seg_sa + seg_ra);
+    char *st = p + seg_sa + seg_ra + seg_ea;
+    a.alpha = automatic ? reinterpret_cast<float *>(st) : nullptr;
+    a.tot = automatic ? reinterpret_cast<double *>(st + align256((size_t)ks_pad * 4)) : nullptr;
+    a.emax = automatic ? reinterpret_cast<int *>(a.tot + 3) : nullptr;
+    return a;
+  };
   ModTable tab = mod_base();
   tab.bits = mod_t;
 
@@ -1207,25 +1349,31 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
     return GB_SUCCESS;
   });
   if (st) return st;
-  CUtensorMap mapA, mapB, mapAr, mapBr;
+  std::vector<CUtensorMap> mapA((size_t)a_copies), mapAr((size_t)a_copies);
+  CUtensorMap mapB, mapBr;
   // op(A) rows: K-contiguous when A is transposed; op(B) columns: K-contiguous when B is not
   auto seg_a = [&](int64_t k0) { return ta ? A + k0 : A + k0 * lda; };
-  auto prep_a = [&](int64_t k0, int64_t kk) {
-    operand_exponents(ta != 0, m, kk, seg_a(k0), lda, m_pad, mx, ea, s);
-    if (automatic) a_side_stats(ta != 0, m, kk, seg_a(k0), lda, ea, mx, st_alpha, st_tot, s);
+  auto prep_a = [&](int64_t sg, int64_t k0, int64_t kk) {
+    const ASeg a = aseg(sg);
+    operand_exponents(ta != 0, m, kk, seg_a(k0), lda, m_pad, mx, a.ea, s, a.emax);
+    if (automatic)
+      a_side_stats(ta != 0, m, kk, seg_a(k0), lda, a.ea, mx, a.emax, a.alpha, a.tot, s);
   };
-  auto split_a = [&](int64_t k0, int64_t kk, const int *run_if) -> int {
+  auto split_a = [&](int64_t sg, int64_t k0, int64_t kk, const int *run_if) -> int {
     const int64_t kp = round_up(kk, BK);
-    launch_split(ta != 0, m, kk, seg_a(k0), lda, ea, Sa, m_pad, kp, sla, nullptr, run_if, s);
-    return make_map(&mapA, sla, (int64_t)Sa * m_pad, kp, BM);
+    const ASeg a = aseg(sg);
+    launch_split(ta != 0, m, kk, seg_a(k0), lda, a.ea, Sa, m_pad, kp, a.dig, nullptr, run_if, s);
+    return make_map(&mapA[a_cache ? sg : 0], a.dig, (int64_t)Sa * m_pad, kp, BM);
   };
-  auto split_a_mod = [&](int64_t k0, int64_t kk, const int *run_if) -> int {
+  auto split_a_mod = [&](int64_t sg, int64_t k0, int64_t kk, const int *run_if) -> int {
     const int64_t kp = round_up(kk, BK);
-    launch_split_mod(ta != 0, m, kk, seg_a(k0), lda, ea, m_pad, kp, rsa, nullptr, run_if, tab, s);
-    return make_map(&mapAr, rsa, (int64_t)MOD_COUNT * m_pad, kp, BM);
+    const ASeg a = aseg(sg);
+    launch_split_mod(ta != 0, m, kk, seg_a(k0), lda, a.ea, m_pad, kp, a.res, nullptr, run_if, tab,
+                     s);
+    return make_map(&mapAr[a_cache ? sg : 0], a.res, (int64_t)MOD_COUNT * m_pad, kp, BM);
   };
   auto gemm = [&](bool mod, const CUtensorMap &ma, const CUtensorMap &mb, int64_t jn_pad,
-                  int64_t kp, const int *run_if) -> int {
+                  int64_t kb0, int64_t kp, const int *run_if) -> int {
     GemmParams gp{};
     gp.S = Sa;
     gp.m_tiles = (int)(m_pad / BM);
@@ -1235,6 +1383,7 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
     // form (j0 = 0) is used with tri
     gp.tri = tri;
     gp.kblocks = (int)(kp / BK);
+    gp.kblock0 = (int)kb0;
     gp.m_pad = (int)m_pad;
     gp.n_pad = (int)jn_pad;
     gp.plane_stride = m_pad * jn_pad;
@@ -1242,7 +1391,10 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
     gp.status = ctx().d_status;
     gp.s_tiles = s_tiles;
     gp.run_if = run_if;
-    for (int l = 0; l < MOD_COUNT; ++l) gp.mod_p[l] = MODULI[l];
+    for (int l = 0; l < MOD_COUNT; ++l) {
+      gp.mod_p[l] = MODULI[l];
+      gp.mod_magic[l] = (uint32_t)(((1ull << 40) + MODULI[l] - 1) / MODULI[l]);
+    }
     const int ntiles = gp.m_tiles * gp.n_tiles;
     const int grid = ntiles < persistent_ctas() ? ntiles : persistent_ctas();
     if (mod) {
@@ -1256,15 +1408,11 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
     GB_CUDA(cudaGetLastError());
     return GB_SUCCESS;
   };
-  // one segment: op(A) is prepared once; with several column blocks (and
-  // automatic mode) it is split in both forms up front, as the blocks'
-  // choices are not known yet
-  const bool a_once = nseg == 1;
-  const bool a_early = a_once && (!automatic || nb < n);
   if (a_once) {
-    prep_a(0, k);
-    if (a_early && (st = split_a(0, k, nullptr))) return st;
-    if (a_early && modular && (st = split_a_mod(0, k, nullptr))) return st;
+    if (hooks && (st = hooks->a_range(0, k))) return st;
+    prep_a(0, 0, k);
+    if (a_early && (st = split_a(0, 0, k, nullptr))) return st;
+    if (a_early && modular && (st = split_a_mod(0, 0, k, nullptr))) return st;
   }
   for (int64_t j0 = 0; j0 < n; j0 += nb) {
     const int64_t jn = (n - j0) < nb ? (n - j0) : nb;
@@ -1274,11 +1422,17 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
     int64_t ldbj = ldb, ldcj = ldc;
     if (hooks && (st = hooks->before(j0, jn, &Bj, &ldbj, &Cj, &ldcj))) return st;
     for (int64_t sg = 0; sg < nseg; ++sg) {
-      const int64_t k0 = sg * MAX_K_SEGMENT;
-      const int64_t kk = (k - k0) < MAX_K_SEGMENT ? (k - k0) : MAX_K_SEGMENT;
+      const int64_t k0 = sg * seg_len;
+      const int64_t kk = (k - k0) < seg_len ? (k - k0) : seg_len;
       const int64_t kp = round_up(kk, BK);
       if (hooks && (st = hooks->segment(j0, jn, k0, kk))) return st;
-      if (!a_once) prep_a(k0, kk);
+      if (!a_once && (!a_cache || j0 == 0)) {
+        if (hooks && (st = hooks->a_range(k0, kk))) return st;
+        prep_a(sg, k0, kk);
+        if (a_cache && (st = split_a(sg, k0, kk, nullptr))) return st;
+        if (a_cache && modular && (st = split_a_mod(sg, k0, kk, nullptr))) return st;
+      }
+      const ASeg a = aseg(sg);
       const double *Ak = seg_a(k0);
       const double *Bk = tb ? Bj + k0 * ldbj : Bj + k0;
       const double bseg = sg == 0 ? beta : 1.0;  // later segments accumulate
@@ -1286,13 +1440,13 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       const int m_tiles = (int)(m_pad / BM);
       const int64_t ps = m_pad * jn_pad;
       if (!automatic) {
-        if (!a_once && (st = split_a(k0, kk, nullptr))) return st;
+        if (!a_both && (st = split_a(sg, k0, kk, nullptr))) return st;
         split_operand(tb == 0, jn, kk, Bk, ldbj, S, jn_pad, kp, mx + m_pad, eb, slb, s);
         if ((st = make_map(&mapB, slb, (int64_t)Sa * jn_pad, kp, BN))) return st;
-        if ((st = gemm(false, mapA, mapB, jn_pad, kp, nullptr))) return st;
+        if ((st = gemm(false, mapA[a_cache ? sg : 0], mapB, jn_pad, 0, kp, nullptr))) return st;
 #define GB_RECOMBINE(SS)                                                                        \
   case SS:                                                                                      \
-    recombine_tile_kernel<SS><<<g, 256, 0, s>>>(m, jn, m_tiles, ps, planes, ea, eb, alpha,      \
+    recombine_tile_kernel<SS><<<g, 256, 0, s>>>(m, jn, m_tiles, ps, planes, a.ea, eb, alpha,    \
                                                 bseg, Cj, ldcj, ta, tb, kk, Ak, lda, Bk, ldbj,  \
                                                 tri, skip);                                     \
     break;
@@ -1306,31 +1460,40 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
         if ((st = check_cuda(cudaGetLastError(), "emulated dgemm"))) return st;
         continue;
       }
-      choose_b(tb == 0, jn, kk, Bk, ldbj, jn_pad, mx + m_pad, eb, st_alpha, st_tot, st_s1, st_s2,
-               budget, mod_t, s_tiles, pass, s);
+      choose_b(tb == 0, jn, kk, Bk, ldbj, jn_pad, mx + m_pad, eb, a.alpha, a.tot, st_s1, st_s2,
+               budget_mod, budget_dig, mod_t, s_tiles, pass, s);
       if (modular) {
         // ---- modular pass (tiles with s_tiles = 0)
-        if (!a_early && (st = split_a_mod(k0, kk, pass))) return st;
+        if (!a_both && (st = split_a_mod(sg, k0, kk, pass))) return st;
         launch_split_mod(tb == 0, jn, kk, Bk, ldbj, eb, jn_pad, kp, slb, s_tiles, pass, tab, s);
         if ((st = make_map(&mapBr, slb, (int64_t)MOD_COUNT * jn_pad, kp, BN))) return st;
-        if ((st = gemm(true, mapAr, mapBr, jn_pad, kp, pass))) return st;
+        if ((st = gemm(true, mapAr[a_cache ? sg : 0], mapBr, jn_pad, 0, kp, pass))) return st;
         reconstruct_tile_kernel<<<g, 256, 0, s>>>(
-            m, jn, m_tiles, ps, reinterpret_cast<const uint16_t *>(planes), ea, eb, alpha, bseg,
+            m, jn, m_tiles, ps, reinterpret_cast<const uint16_t *>(planes), a.ea, eb, alpha, bseg,
             Cj, ldcj, ta, tb, kk, Ak, lda, Bk, ldbj, tri, skip, s_tiles, pass, tab);
         count_launch();
         if ((st = check_cuda(cudaGetLastError(), "emulated dgemm"))) return st;
       }
-      // ---- digit-slice pass (tiles with s_tiles = S > 0)
-      if (!a_early && (st = split_a(k0, kk, pass + 1))) return st;
+      // ---- digit-slice pass (tiles with s_tiles = S > 0), over sub-segments
+      // of at most MAX_K_SEGMENT (each level sum exact in int32), each
+      // recombined into C in turn
+      if (!a_both && (st = split_a(sg, k0, kk, pass + 1))) return st;
       launch_split(tb == 0, jn, kk, Bk, ldbj, eb, MAX_SLICES, jn_pad, kp, slb, s_tiles, pass + 1,
                    s);
       if ((st = make_map(&mapB, slb, (int64_t)Sa * jn_pad, kp, BN))) return st;
-      if ((st = gemm(false, mapA, mapB, jn_pad, kp, pass + 1))) return st;
-      recombine_auto_kernel<<<g, 256, 0, s>>>(m, jn, m_tiles, ps, planes, ea, eb, alpha, bseg, Cj,
-                                              ldcj, ta, tb, kk, Ak, lda, Bk, ldbj, tri, skip,
-                                              s_tiles, pass + 1);
-      count_launch();
-      if ((st = check_cuda(cudaGetLastError(), "emulated dgemm"))) return st;
+      for (int64_t u0 = 0; u0 < kk; u0 += MAX_K_SEGMENT) {
+        const int64_t uk = (kk - u0) < MAX_K_SEGMENT ? (kk - u0) : MAX_K_SEGMENT;
+        if ((st = gemm(false, mapA[a_cache ? sg : 0], mapB, jn_pad, u0 / BK, round_up(uk, BK),
+                       pass + 1)))
+          return st;
+        const double *Au = ta ? Ak + u0 : Ak + u0 * lda;
+        const double *Bu = tb ? Bk + u0 * ldbj : Bk + u0;
+        recombine_auto_kernel<<<g, 256, 0, s>>>(m, jn, m_tiles, ps, planes, a.ea, eb, alpha,
+                                                u0 == 0 ? bseg : 1.0, Cj, ldcj, ta, tb, uk, Au,
+                                                lda, Bu, ldbj, tri, skip, s_tiles, pass + 1);
+        count_launch();
+        if ((st = check_cuda(cudaGetLastError(), "emulated dgemm"))) return st;
+      }
     }
     if (hooks && (st = hooks->after(j0, jn))) return st;
   }

@@ -94,6 +94,42 @@ __device__ __forceinline__ double scaled_value(__int128 acc, int x0, double alph
   return scale_out_of_range(neg ? -t : t, alpha, x);
 }
 
+// acc * 2^x0 rounded to nearest (ties to even) with integer operations only,
+// when the result is a normal number (ok = true); FP64 arithmetic is the
+// scarcest unit on this part.  Equal to scaled_value(acc, x0, 1.0) whenever
+// ok is set.
+__device__ __forceinline__ double int_scaled(__int128 acc, int x0, bool &ok) {
+  ok = true;
+  if (acc == 0) return 0.0;
+  const bool neg = acc < 0;
+  const unsigned __int128 u = neg ? (unsigned __int128)(-acc) : (unsigned __int128)acc;
+  const unsigned long long hi = (unsigned long long)(u >> 64);
+  int msb = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)(unsigned long long)u);
+  unsigned long long mant;  // 53 significant bits
+  const int sh = msb - 52;
+  if (sh <= 0) {
+    mant = (unsigned long long)u << (-sh);
+  } else {
+    mant = (unsigned long long)(u >> sh);
+    const unsigned __int128 rem = u & (((unsigned __int128)1 << sh) - 1);
+    const unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
+    if (rem > half || (rem == half && (mant & 1ull))) {
+      if (++mant >> 53) {  // rounded up to the next power of two
+        mant >>= 1;
+        ++msb;
+      }
+    }
+  }
+  const int E = msb + x0 + 1023;  // biased exponent of mant * 2^(msb - 52 + x0)
+  if (E <= 0 || E >= 0x7ff) {
+    ok = false;
+    return 0.0;
+  }
+  const unsigned long long bits = ((unsigned long long)neg << 63) |
+                                  ((unsigned long long)E << 52) | (mant & 0xFFFFFFFFFFFFFull);
+  return __longlong_as_double((long long)bits);
+}
+
 // alpha * 2^(ei + fj - 8(S+1)) * acc: one element of C from its level sum.
 __device__ __forceinline__ double level_value(__int128 acc, int S, int ei, int fj, double alpha) {
   return scaled_value(acc, ei + fj - DIGIT_BITS * (S + 1), alpha);

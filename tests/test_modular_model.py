@@ -11,9 +11,12 @@ check, in exact integer arithmetic:
   residue has |r| <= 255 (exact in bf16, and a 256-deep FP32 chunk of
   residue products stays below 2^24, as for 8-bit digits);
 * the bit count t chosen for a K segment keeps every |C'| < k 2^2t below
-  M / 2 with room for the rounded CRT quotient (t = 56 for K = 4096);
+  M / 2 with room for the rounded CRT quotient (t = 55 for K = 8192);
 * the residues the split kernel forms in FP32 from 12-bit chunks equal the
   exact symmetric residues, over random and extreme t-bit integers;
+* the residue GEMM's epilogue reduction (offset, then the quotient from a
+  multiply-high by ceil(2^40 / p)) equals the residue for every sum an
+  8192-deep segment can produce;
 * the reconstruction (quotient from 32-bit fixed-point fractions, four
   signed 64-bit limbs, the value taken modulo 2^128) returns C' for
   random and extreme values of C', including +-(k 2^2t - 1).
@@ -99,7 +102,7 @@ def test_moduli_are_odd_coprime_and_small():
 
 
 def test_bit_count_keeps_products_below_half_the_modulus():
-    assert mod_bits(4096) == 56
+    assert mod_bits(4096) == 56 and mod_bits(8192) == 55
     for k in (1, 2, 3, 64, 255, 256, 257, 1000, 4095, 4096, 5000, 65536):
         t = mod_bits(k)
         assert 1 <= t <= CHUNK_BITS * CHUNKS
@@ -110,21 +113,35 @@ def test_bit_count_keeps_products_below_half_the_modulus():
             assert 2 * k * (1 << (2 * t + 2)) * (1 + 2 ** -6) >= M
 
 
-def _fp32_residues(mag, p):
-    """The split kernel's FP32 residue of the non-negative t-bit integers
-    `mag` (uint64 array) modulo p, in [-(p-1)/2, (p-1)/2]."""
+def _fp32_residues(mag, neg, p):
+    """The split kernel's FP32 residue of sign * mag (mag: non-negative t-bit
+    integers, uint64 array; neg: bool array) modulo p, in
+    [-(p-1)/2, (p-1)/2].  The chunk sums are exact in FP32 (every term and
+    partial sum is an integer below 2^24); the quotient fmaf(x, 1/p, 1.5 2^23)
+    - 1.5 2^23 is restated exactly in integers (one rounding of the exact
+    x * fl(1/p) + 1.5 2^23 to FP32, whose spacing there is 1)."""
     f32 = np.float32
-    v = np.zeros(mag.shape, f32)
+    sign = np.where(neg, -1, 1).astype(np.int64)
+    x = np.zeros(mag.shape, np.int64)
     for d in range(CHUNKS):
-        c = ((mag >> np.uint64(CHUNK_BITS * d)) & np.uint64((1 << CHUNK_BITS) - 1)).astype(f32)
-        pw = f32((1 << (CHUNK_BITS * d)) % p)
-        v = (c * pw + v).astype(f32)             # exact: every term and sum < 2^24
-    q = np.rint(v * f32(1.0 / f32(p))).astype(f32)
-    v = (v - q * f32(p)).astype(f32)
-    half = f32(0.5) * (f32(p) - f32(1))
-    v = np.where(v > half, v - f32(p), v)
-    v = np.where(v < -half, v + f32(p), v)
-    return v
+        c = ((mag >> np.uint64(CHUNK_BITS * d)) & np.uint64((1 << CHUNK_BITS) - 1)).astype(np.int64)
+        x += sign * c * ((1 << (CHUNK_BITS * d)) % p)
+    assert np.abs(x).max() < 2 ** 24
+    pinv = f32(1.0) / f32(p)
+    mant, ex = np.frexp(np.float64(pinv))            # pinv = mant 2^ex, mant in [0.5, 1)
+    M = int(mant * 2 ** 24)                         # pinv = M 2^(ex - 24), M < 2^24
+    sh = 24 - int(ex)                               # x * pinv = x M 2^-sh
+    S = x * M + (3 << (22 + sh))                    # (x pinv + 1.5 2^23) 2^sh, exact
+    unit = 1 << sh                                  # FP32 spacing 1 in [2^23, 2^24)
+    low = S % unit
+    rounded = S - low + np.where((low > unit // 2) | ((low == unit // 2) & ((S // unit) % 2 == 1)),
+                                 unit, 0)
+    q = rounded // unit - (3 << 22)
+    r = x - q * p
+    half = (p - 1) // 2
+    r = np.where(r > half, r - p, r)
+    r = np.where(r < -half, r + p, r)
+    return r
 
 
 def test_fp32_residues_are_exact():
@@ -137,10 +154,12 @@ def test_fp32_residues_are_exact():
             edge += [max(0, base + d) for d in range(-3, 4)]
     mags.append(np.array([x % (1 << t) for x in edge], dtype=np.uint64))
     mag = np.concatenate(mags)
+    neg = rng.integers(0, 2, mag.size).astype(bool)
     for p in MODULI:
-        got = _fp32_residues(mag, p)
-        exact = np.array([((int(x) + p // 2) % p) - p // 2 for x in mag], dtype=np.float64)
-        assert np.array_equal(got.astype(np.float64), exact), p
+        got = _fp32_residues(mag, neg, p)
+        exact = np.array([((v + p // 2) % p) - p // 2 for v in
+                          (-int(x) if n else int(x) for x, n in zip(mag, neg))], dtype=np.int64)
+        assert np.array_equal(got, exact), p
         assert np.abs(got).max() <= (p - 1) // 2
 
 
@@ -158,3 +177,24 @@ def test_crt_reconstruction_recovers_the_product():
             assert abs(c) <= lim
             residues = [c % p for p in MODULI]
             assert reconstruct(residues, F, W) == c
+
+
+def test_epilogue_reduction_is_exact():
+    off_shift = int(re.search(r"off = pm << (\d+)", SRC).group(1))
+    magic_shift = int(re.search(r"\(\(1ull << (\d+)\) \+ MODULI\[l\] - 1\) / MODULI\[l\]",
+                                SRC).group(1))
+    q_shift = int(re.search(r"__umulhi\(u, magic\) >> (\d+)", SRC).group(1))
+    assert magic_shift == 32 + q_shift
+    assert re.search(r"MOD_K_SEGMENT = 2 \* MAX_K_SEGMENT;", SRC)
+    bound = 2 * 4096 * 255 * 255                 # |residue sum| of one 8192-deep segment
+    rng = np.random.default_rng(13)
+    for p in MODULI:
+        magic = ((1 << magic_shift) + p - 1) // p
+        assert magic < 1 << 32
+        sums = list(range(-bound, -bound + 2000)) + list(range(bound - 2000, bound + 1))
+        sums += [int(x) for x in rng.integers(-bound, bound + 1, 20000)]
+        for v in sums:
+            u = (v + (p << off_shift)) & 0xFFFFFFFF
+            assert 0 <= u < 1 << 31
+            q = ((u * magic) >> 32) >> q_shift
+            assert u - q * p == v % p
