@@ -283,12 +283,17 @@ static int dgemm_host_pipelined(int ta, int tb, int64_t m, int64_t n, int64_t k,
     GB_CUDA(cudaEventRecord(ready, p.s));
     GB_CUDA(cudaStreamWaitEvent(p.cin, ready, 0));
     p.mark(p.cin, "start", 0);
-    // op(A) and block 0 of op(B) segment by segment, interleaved: the first
-    // segment's slice GEMM needs only the first of each
+    // op(A) and block 0 of op(B) engine segment by engine segment: all of
+    // op(A)'s pieces of a segment first (its preparation needs the whole
+    // segment and overlaps block 0's upload), then block 0's
     int st;
-    for (int64_t sg = 0; sg < p.nseg; ++sg) {
-      if ((st = p.upload_a(sg))) return st;
-      if ((st = p.upload(0, sg))) return st;
+    const int64_t eseg = emulated_k_segment(ozaki_caller_slices()) / PIPE_K_SEGMENT;
+    for (int64_t g0 = 0; g0 < p.nseg; g0 += eseg) {
+      const int64_t g1 = g0 + eseg < p.nseg ? g0 + eseg : p.nseg;
+      for (int64_t sg = g0; sg < g1; ++sg)
+        if ((st = p.upload_a(sg))) return st;
+      for (int64_t sg = g0; sg < g1; ++sg)
+        if ((st = p.upload(0, sg))) return st;
     }
     st = dgemm_emulated_blocked(ta, tb, m, n, k, alpha, dA, ra, beta,
                                 ozaki_caller_slices(), p.nb, &p, p.s);

@@ -198,6 +198,8 @@ struct EmuBlockHooks {
   virtual int after(int64_t j0, int64_t jn) = 0;
   virtual ~EmuBlockHooks() = default;
 };
+// The K segment the emulated engine runs for a slice-count argument.
+int64_t emulated_k_segment(int slices);
 int dgemm_emulated_blocked(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
                            const double *A, int64_t lda, double beta, int slices, int64_t nb,
                            EmuBlockHooks *hooks, cudaStream_t s);

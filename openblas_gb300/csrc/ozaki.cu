@@ -89,19 +89,27 @@ constexpr int NONFINITE = ozd::NONFINITE;  // exponent marker of a row/column wi
 
 // ------------------------------------------------------------ modular scheme
 constexpr int MOD_COUNT = 14;       // moduli of the modular scheme
+constexpr int MOD_PAIRS = MOD_COUNT / 2;
 constexpr int MOD_CHUNK_BITS = 12;  // A' is read in 12-bit chunks to form its residues
 constexpr int MOD_CHUNKS = 5;       // 60 bits: t <= 60
 constexpr int MOD_MAX_BITS = MOD_CHUNK_BITS * MOD_CHUNKS;
-static_assert(4096.0 * 511 * MOD_CHUNKS < 16777216.0, "a residue's chunk sum is exact in FP32");
+// |chunk sum| < 5 * 4096 * 255 < 2^22.33: exact in FP32, and small enough
+// that the rounded quotient below is exact (see split_mod_kernel)
+static_assert(4096.0 * 255 * MOD_CHUNKS < 5300000.0, "a residue's chunk sum stays below 2^22.33");
 
 // Constants of the modular scheme for one call (kernel argument).
 struct ModTable {
   int bits;                          // t: operands are cut to t-bit integers
   float pf[MOD_COUNT];               // p_l
   float pinv[MOD_COUNT];             // 1 / p_l (rounded)
-  float pw[MOD_COUNT][MOD_CHUNKS];   // 2^(12 d) mod p_l
-  uint32_t F[MOD_COUNT];             // round(2^32 u_l / p_l), u_l = (M / p_l)^-1 mod p_l
-  uint32_t W[MOD_COUNT][4];          // CRT weight (M / p_l) u_l, 32-bit limbs, low first
+  float pw[MOD_COUNT][MOD_CHUNKS];   // 2^(12 d) mod p_l, symmetric (|pw| <= (p_l - 1) / 2)
+  // The reconstruction pairs the moduli, m_i = a_i b_i with a_i = p_2i,
+  // b_i = p_2i+1 (M = prod m_i), and runs the CRT over the seven pairs:
+  uint32_t pa[MOD_PAIRS], pb[MOD_PAIRS];
+  uint32_t pinv_ab[MOD_PAIRS];       // a_i^-1 mod b_i
+  uint32_t pmagic[MOD_PAIRS];        // ceil(2^32 / b_i): u / b_i = umulhi(u, pmagic) for u < 2^20
+  uint32_t F[MOD_PAIRS];             // round(2^32 u_i / m_i), u_i = (M / m_i)^-1 mod m_i
+  uint32_t W[MOD_PAIRS][4];          // CRT weight (M / m_i) u_i, 32-bit limbs, low first
   uint32_t M[4];                     // M = prod p_l, 32-bit limbs
 };
 
@@ -789,12 +797,15 @@ split_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
 }
 
 // Residues of a 32-row x 64-K tile for the modular scheme: the t-bit
-// integer A' = sign(x) trunc(|x| 2^(t - e)) is read in five 12-bit chunks
-// c_d, and A' mod p_l = sum_d c_d (2^(12 d) mod p_l) mod p_l is formed in
-// FP32 (every partial sum is an integer below 2^24, so exact), reduced to the
-// symmetric range [-(p_l - 1)/2, (p_l - 1)/2] and signed.  Residue planes
-// share the slices' layout.  For op(B) (s_tiles non-null) only the rows of
-// modular tiles are written.
+// integer A' = sign(x) trunc(|x| 2^(t - e)) is read in five signed 12-bit
+// chunks c_d, and x = sum_d c_d w_d with w_d = 2^(12 d) mod p_l in the
+// symmetric range is formed in FP32 (|x| < 2^22.33, every partial sum an
+// exact integer).  The residue is x - q p_l with q = round(x fl(1/p_l)):
+// |x fl(1/p_l) - x / p_l| <= 2^22.33 2^-33 = 2^-10.67, below the distance
+// 1 / (2 p_l) >= 2^-10 from x / p_l to the nearest half-integer (p_l odd),
+// so q is the exact nearest quotient and the residue lies in
+// [-(p_l - 1)/2, (p_l - 1)/2].  Residue planes share the slices' layout.
+// For op(B) (s_tiles non-null) only the rows of modular tiles are written.
 template <bool KCONTIG>
 __global__ void __launch_bounds__(256)
 split_mod_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
@@ -843,7 +854,7 @@ split_mod_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
   constexpr float ROUND = 12582912.0f;  // 1.5 * 2^23: adding it rounds |y| < 2^22 to an integer
 #pragma unroll 2
   for (int l = 0; l < MOD_COUNT; ++l) {
-    const float pl = tab.pf[l], pinv = tab.pinv[l], half = 0.5f * (pl - 1.0f);
+    const float pl = tab.pf[l], pinv = tab.pinv[l];
     __align__(16) __nv_bfloat162 out[4];
 #pragma unroll
     for (int j = 0; j < 8; j += 2) {
@@ -853,11 +864,8 @@ split_mod_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
         float x = 0.0f;
 #pragma unroll
         for (int d = 0; d < MOD_CHUNKS; ++d) x = fmaf(ch[j + h][d], tab.pw[l][d], x);
-        const float q = fmaf(x, pinv, ROUND) - ROUND;  // round(x / p_l), possibly one off
-        x = fmaf(-q, pl, x);  // exact: both terms are integers below 2^24
-        if (x > half) x -= pl;
-        if (x < -half) x += pl;
-        v[h] = x;
+        const float q = fmaf(x, pinv, ROUND) - ROUND;  // the nearest quotient, exactly
+        v[h] = fmaf(-q, pl, x);  // exact: both terms are integers below 2^24
       }
       out[j >> 1] = __floats2bfloat162_rn(v[0], v[1]);
     }
@@ -968,15 +976,16 @@ recombine_auto_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
 }
 
 // Modular scheme: C from the residue planes, one CTA per 128 x 256 tile of C
-// (tiles with s_tiles[nt] != 0 belong to the digit-slice pass).  With r_l
-// the residue of C'_ij mod p_l (in [0, p_l)), X = sum_l r_l W_l is
-// congruent to C' mod M, and X / M = sum_l r_l u_l / p_l, so the quotient
-// q = round(sum_l r_l F_l 2^-32) (error below 2^-20) gives C' = X - q M:
-// |C'| < M / (2 + 2^-5) by the choice of t leaves a margin of 0.007 to the
-// rounding.
-// X - q M is formed exactly in four signed 64-bit limbs of 32 bits (every
-// limb sum is below 2^45) and combined modulo 2^128, which holds C' as
-// |C'| < 2^127.
+// (tiles with s_tiles[nt] != 0 belong to the digit-slice pass).  The
+// residues r of C'_ij modulo a_i and b_i (in [0, a_i), [0, b_i)) first
+// combine into its residue modulo m_i = a_i b_i (32-bit arithmetic):
+//   y_i = r_a + a_i ((r_b - r_a) a_i^-1 mod b_i),  0 <= y_i < m_i < 2^18.
+// Then X = sum_i y_i W_i is congruent to C' mod M, and
+// X / M = sum_i y_i u_i / m_i, so the quotient q = round(sum_i y_i F_i 2^-32)
+// (error below 7 2^18 2^-33 < 2^-12) gives C' = X - q M: |C'| < M / (2 + 2^-5)
+// by the choice of t leaves a margin of 0.007 to the rounding.  X - q M is
+// formed exactly in four signed 64-bit limbs of 32 bits (every limb sum is
+// below 2^53) and combined modulo 2^128, which holds C' as |C'| < 2^127.
 __global__ void __launch_bounds__(256)
 reconstruct_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
                         const uint16_t *__restrict__ planes, const int *__restrict__ ea,
@@ -998,18 +1007,32 @@ reconstruct_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
   // resident to hide the integer multiply chains
   const int tid = threadIdx.x;
   const int il = (tid & 63) * 2, jb = tid >> 6;
+  // FP64 compares run on the FP64 pipe: decide alpha = 1 and beta = 0 once
+  const bool alpha_one = alpha == 1.0, beta_zero = beta == 0.0;
   const uint16_t *pt = planes + ((int64_t)nt * m_tiles + mt) * (BM * BN);
   int e_i[2];
 #pragma unroll
   for (int r = 0; r < 2; ++r) e_i[r] = (i0 + il + r < m) ? ea[i0 + il + r] : 0;
-  for (int jl = jb; jl < BN; jl += 4) {
+  // the planes of the next column are loaded while this one is combined
+  const int jend = (n - j0) < BN ? (int)(n - j0) : BN;
+  uint32_t Pn[MOD_COUNT];
+  if (jb < jend) {
+#pragma unroll
+    for (int l = 0; l < MOD_COUNT; ++l)
+      Pn[l] = *reinterpret_cast<const uint32_t *>(pt + (int64_t)l * plane_stride + jb * BM + il);
+  }
+  for (int jl = jb; jl < jend; jl += 4) {
     const int64_t j = j0 + jl;
-    if (j >= n) break;
     const int fj = eb[j];
     uint32_t P[MOD_COUNT];
 #pragma unroll
-    for (int l = 0; l < MOD_COUNT; ++l)
-      P[l] = *reinterpret_cast<const uint32_t *>(pt + (int64_t)l * plane_stride + jl * BM + il);
+    for (int l = 0; l < MOD_COUNT; ++l) P[l] = Pn[l];
+    if (jl + 4 < jend) {
+#pragma unroll
+      for (int l = 0; l < MOD_COUNT; ++l)
+        Pn[l] = *reinterpret_cast<const uint32_t *>(pt + (int64_t)l * plane_stride +
+                                                    (jl + 4) * BM + il);
+    }
 #pragma unroll
     for (int r = 0; r < 2; ++r) {
       const int64_t i = i0 + il + r;
@@ -1028,13 +1051,20 @@ reconstruct_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
         unsigned long long qa = 0;
         long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
 #pragma unroll
-        for (int l = 0; l < MOD_COUNT; ++l) {
-          const unsigned long long rl = r ? (P[l] >> 16) : (P[l] & 0xFFFFu);
-          qa += rl * tab.F[l];
-          a0 += (long long)(rl * tab.W[l][0]);
-          a1 += (long long)(rl * tab.W[l][1]);
-          a2 += (long long)(rl * tab.W[l][2]);
-          a3 += (long long)(rl * tab.W[l][3]);
+        for (int i2 = 0; i2 < MOD_PAIRS; ++i2) {
+          const uint32_t ra = r ? (P[2 * i2] >> 16) : (P[2 * i2] & 0xFFFFu);
+          const uint32_t rb = r ? (P[2 * i2 + 1] >> 16) : (P[2 * i2 + 1] & 0xFFFFu);
+          const uint32_t b = tab.pb[i2];
+          // (r_b - r_a) a^-1 mod b: the difference made positive, < 3 b;
+          // the product below 2^20, its quotient by b exact from the magic
+          const uint32_t u = (rb + 2 * b - ra) * tab.pinv_ab[i2];
+          const uint32_t tq = u - __umulhi(u, tab.pmagic[i2]) * b;
+          const unsigned long long y = ra + tab.pa[i2] * tq;  // C' mod a b
+          qa += y * tab.F[i2];
+          a0 += (long long)(y * tab.W[i2][0]);
+          a1 += (long long)(y * tab.W[i2][1]);
+          a2 += (long long)(y * tab.W[i2][2]);
+          a3 += (long long)(y * tab.W[i2][3]);
         }
         const long long q = (long long)((qa + 0x80000000ull) >> 32);
         a0 -= q * (long long)tab.M[0];
@@ -1050,11 +1080,11 @@ reconstruct_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
         v = ozd::int_scaled((__int128)u, x0, ok);
         if (!ok)
           v = ozd::scaled_value((__int128)u, x0, alpha);
-        else if (alpha != 1.0)
+        else if (!alpha_one)
           v *= alpha;
       }
       double *c = C + i + j * ldc;
-      *c = (beta == 0.0) ? v : fma(beta, *c, v);
+      *c = beta_zero ? v : fma(beta, *c, v);
     }
   }
 }
@@ -1090,17 +1120,38 @@ static const ModTable &mod_base() {
     ModTable t{};
     const unsigned __int128 M = mod_product();
     for (int q = 0; q < 4; ++q) t.M[q] = (uint32_t)(M >> (32 * q));
+    for (int i = 0; i < MOD_PAIRS; ++i) {
+      const unsigned a = (unsigned)MODULI[2 * i], b = (unsigned)MODULI[2 * i + 1];
+      const unsigned long long mi = (unsigned long long)a * b;
+      t.pa[i] = a;
+      t.pb[i] = b;
+      t.pinv_ab[i] = (uint32_t)mod_inverse((int)(a % b), (int)b);
+      t.pmagic[i] = (uint32_t)(((1ull << 32) + b - 1) / b);
+      const unsigned __int128 Mi = M / mi;
+      const unsigned long long mr = (unsigned long long)(Mi % mi);
+      // (M / m_i)^-1 mod m_i by the extended Euclid algorithm in 64 bits
+      long long t0 = 0, t1 = 1, r0 = (long long)mi, r1 = (long long)mr;
+      while (r1) {
+        const long long q = r0 / r1, t2 = t0 - q * t1, r2 = r0 - q * r1;
+        t0 = t1;
+        t1 = t2;
+        r0 = r1;
+        r1 = r2;
+      }
+      const unsigned long long u = (unsigned long long)(t0 < 0 ? t0 + (long long)mi : t0);
+      const unsigned __int128 W = Mi * u;  // < M
+      for (int q = 0; q < 4; ++q) t.W[i][q] = (uint32_t)(W >> (32 * q));
+      t.F[i] = (uint32_t)(((unsigned __int128)u << 32) / mi +
+                          ((((unsigned __int128)u << 32) % mi) * 2 >= mi ? 1 : 0));
+    }
     for (int l = 0; l < MOD_COUNT; ++l) {
       const int p = MODULI[l];
-      const unsigned __int128 Ml = M / (unsigned)p;
-      const int u = mod_inverse((int)(Ml % (unsigned)p), p);
-      const unsigned __int128 W = Ml * (unsigned)u;  // < M
-      for (int q = 0; q < 4; ++q) t.W[l][q] = (uint32_t)(W >> (32 * q));
-      t.F[l] = (uint32_t)((((unsigned long long)u << 32) + (unsigned)p / 2) / (unsigned)p);
       t.pf[l] = (float)p;
       t.pinv[l] = 1.0f / (float)p;
-      for (int d = 0; d < MOD_CHUNKS; ++d)
-        t.pw[l][d] = (float)((1ull << (MOD_CHUNK_BITS * d)) % (unsigned)p);
+      for (int d = 0; d < MOD_CHUNKS; ++d) {
+        const int w = (int)((1ull << (MOD_CHUNK_BITS * d)) % (unsigned)p);
+        t.pw[l][d] = (float)(w > p / 2 ? w - p : w);
+      }
     }
     return t;
   }();
@@ -1519,6 +1570,11 @@ static int resolve_slices(int slices, cudaStream_t s) {
   }
   int S = slices > 0 ? slices : ozaki_default_slices();
   return S > oz::MAX_SLICES ? oz::MAX_SLICES : S;
+}
+
+int64_t emulated_k_segment(int slices) {
+  return slices == OZAKI_SLICES_AUTO && ozaki_modular_enabled() ? oz::MOD_K_SEGMENT
+                                                                 : oz::MAX_K_SEGMENT;
 }
 
 int dgemm_emulated_blocked(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,

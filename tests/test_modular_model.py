@@ -12,14 +12,17 @@ check, in exact integer arithmetic:
   residue products stays below 2^24, as for 8-bit digits);
 * the bit count t chosen for a K segment keeps every |C'| < k 2^2t below
   M / 2 with room for the rounded CRT quotient (t = 55 for K = 8192);
-* the residues the split kernel forms in FP32 from 12-bit chunks equal the
-  exact symmetric residues, over random and extreme t-bit integers;
+* the residues the split kernel forms in FP32 from 12-bit chunks and
+  symmetric chunk weights equal the exact symmetric residues with no
+  correction step (the rounded quotient is exact), over random and extreme
+  t-bit integers of both signs;
 * the residue GEMM's epilogue reduction (offset, then the quotient from a
   multiply-high by ceil(2^40 / p)) equals the residue for every sum an
   8192-deep segment can produce;
-* the reconstruction (quotient from 32-bit fixed-point fractions, four
-  signed 64-bit limbs, the value taken modulo 2^128) returns C' for
-  random and extreme values of C', including +-(k 2^2t - 1).
+* the reconstruction (moduli combined in pairs with 32-bit arithmetic, the
+  quotient from 32-bit fixed-point fractions, four signed 64-bit limbs, the
+  value taken modulo 2^128) returns C' for random and extreme values of C',
+  including +-(k 2^2t - 1).
 """
 from __future__ import annotations
 
@@ -67,25 +70,41 @@ def mod_bits(k):
 
 
 def crt_table():
-    F, W = [], []
-    for p in MODULI:
-        Ml = M // p
-        u = pow(Ml % p, -1, p)
-        W.append(Ml * u)
-        F.append(((u << 32) + p // 2) // p)
-    return F, W
+    """The reconstruction's constants: moduli paired (a_i, b_i) = (p_2i,
+    p_2i+1), m_i = a_i b_i; a_i^-1 mod b_i, ceil(2^32 / b_i), and the CRT
+    weights W_i = (M / m_i) u_i with u_i = (M / m_i)^-1 mod m_i and their
+    32-bit fixed-point fractions F_i = round(2^32 u_i / m_i)."""
+    pairs = []
+    for i in range(0, MOD_COUNT, 2):
+        a, b = MODULI[i], MODULI[i + 1]
+        mi = a * b
+        u = pow((M // mi) % mi, -1, mi)
+        F = ((u << 32) // mi) + (1 if ((u << 32) % mi) * 2 >= mi else 0)
+        pairs.append(dict(a=a, b=b, inv=pow(a, -1, b), magic=((1 << 32) + b - 1) // b,
+                          W=(M // mi) * u, F=F))
+    return pairs
 
 
-def reconstruct(residues, F, W):
-    """C' from its residues in [0, p_l), as the reconstruction kernel forms it."""
-    qa = sum(r * f for r, f in zip(residues, F))
+def reconstruct(residues, pairs):
+    """C' from its residues in [0, p_l), as the reconstruction kernel forms it:
+    each pair combined in 32-bit arithmetic, then the CRT over the pairs in
+    four signed 64-bit limbs, the value taken modulo 2^128."""
+    ys = []
+    for i, pr in enumerate(pairs):
+        ra, rb, a, b = residues[2 * i], residues[2 * i + 1], pr["a"], pr["b"]
+        u = ((rb + 2 * b - ra) * pr["inv"]) & 0xFFFFFFFF
+        assert 0 <= u < 1 << 20
+        t = u - ((u * pr["magic"]) >> 32) * b
+        assert 0 <= t < b
+        ys.append(ra + a * t)
+    qa = sum(y * pr["F"] for y, pr in zip(ys, pairs))
+    assert qa < 1 << 64
     q = (qa + (1 << 31)) >> 32
     limbs = []
     for j in range(4):
-        a = sum(r * ((w >> (32 * j)) & 0xFFFFFFFF) for r, w in zip(residues, W))
+        a = sum(y * ((pr["W"] >> (32 * j)) & 0xFFFFFFFF) for y, pr in zip(ys, pairs))
         a -= q * ((M >> (32 * j)) & 0xFFFFFFFF)
-        assert -(1 << 63) <= a < (1 << 63)       # a signed 64-bit limb
-        assert abs(a) < (1 << 46)
+        assert abs(a) < (1 << 53)                # a signed 64-bit limb
         limbs.append(a)
     u = sum(a << (32 * j) for j, a in enumerate(limbs)) % (1 << 128)
     return u - (1 << 128) if u >= (1 << 127) else u
@@ -113,35 +132,40 @@ def test_bit_count_keeps_products_below_half_the_modulus():
             assert 2 * k * (1 << (2 * t + 2)) * (1 + 2 ** -6) >= M
 
 
-def _fp32_residues(mag, neg, p):
-    """The split kernel's FP32 residue of sign * mag (mag: non-negative t-bit
-    integers, uint64 array; neg: bool array) modulo p, in
-    [-(p-1)/2, (p-1)/2].  The chunk sums are exact in FP32 (every term and
-    partial sum is an integer below 2^24); the quotient fmaf(x, 1/p, 1.5 2^23)
-    - 1.5 2^23 is restated exactly in integers (one rounding of the exact
-    x * fl(1/p) + 1.5 2^23 to FP32, whose spacing there is 1)."""
+def _fp32_quotient(x, p):
+    """fmaf(x, fl(1/p), 1.5 2^23) - 1.5 2^23 for integer x (int64 array),
+    restated exactly in integers: one rounding of the exact x * fl(1/p) +
+    1.5 2^23 to FP32, whose spacing there is 1."""
     f32 = np.float32
-    sign = np.where(neg, -1, 1).astype(np.int64)
-    x = np.zeros(mag.shape, np.int64)
-    for d in range(CHUNKS):
-        c = ((mag >> np.uint64(CHUNK_BITS * d)) & np.uint64((1 << CHUNK_BITS) - 1)).astype(np.int64)
-        x += sign * c * ((1 << (CHUNK_BITS * d)) % p)
-    assert np.abs(x).max() < 2 ** 24
     pinv = f32(1.0) / f32(p)
     mant, ex = np.frexp(np.float64(pinv))            # pinv = mant 2^ex, mant in [0.5, 1)
     M = int(mant * 2 ** 24)                         # pinv = M 2^(ex - 24), M < 2^24
     sh = 24 - int(ex)                               # x * pinv = x M 2^-sh
     S = x * M + (3 << (22 + sh))                    # (x pinv + 1.5 2^23) 2^sh, exact
-    unit = 1 << sh                                  # FP32 spacing 1 in [2^23, 2^24)
+    unit = 1 << sh
     low = S % unit
     rounded = S - low + np.where((low > unit // 2) | ((low == unit // 2) & ((S // unit) % 2 == 1)),
                                  unit, 0)
-    q = rounded // unit - (3 << 22)
-    r = x - q * p
-    half = (p - 1) // 2
-    r = np.where(r > half, r - p, r)
-    r = np.where(r < -half, r + p, r)
-    return r
+    return rounded // unit - (3 << 22)
+
+
+def _fp32_residues(mag, neg, p):
+    """The split kernel's FP32 residue of sign * mag (mag: non-negative t-bit
+    integers, uint64 array; neg: bool array) modulo p: x = sum_d c_d w_d with
+    signed 12-bit chunks c_d and w_d = 2^(12 d) mod p in the symmetric range
+    (every term and partial sum an exact integer below 2^22.33 in FP32), the
+    quotient fmaf(x, fl(1/p), 1.5 2^23) - 1.5 2^23 restated exactly in
+    integers (one rounding of the exact x * fl(1/p) + 1.5 2^23 to FP32, whose
+    spacing there is 1), and x - q p, with no correction step."""
+    sign = np.where(neg, -1, 1).astype(np.int64)
+    x = np.zeros(mag.shape, np.int64)
+    for d in range(CHUNKS):
+        c = ((mag >> np.uint64(CHUNK_BITS * d)) & np.uint64((1 << CHUNK_BITS) - 1)).astype(np.int64)
+        w = (1 << (CHUNK_BITS * d)) % p
+        w = w - p if w > p // 2 else w
+        x += sign * c * w
+    assert np.abs(x).max() < 2 ** 22.33
+    return x - _fp32_quotient(x, p) * p
 
 
 def test_fp32_residues_are_exact():
@@ -163,8 +187,28 @@ def test_fp32_residues_are_exact():
         assert np.abs(got).max() <= (p - 1) // 2
 
 
+def test_fp32_quotient_is_exact_next_to_half_integers():
+    """Every chunk sum the split can form (|x| < 5 * 4096 * 255) whose
+    quotient x / p lies closest to a half-integer (residue +-(p - 1)/2)."""
+    lim = CHUNKS * ((1 << CHUNK_BITS) - 1) * 255
+    for p in MODULI:
+        h = (p - 1) // 2
+        q = np.arange(-(lim // p) - 1, lim // p + 2, dtype=np.int64)
+        for r in (h, -h):
+            x = q * p + r
+            x = x[np.abs(x) <= lim]
+            assert np.array_equal(_fp32_quotient(x, p), (x - r) // p)
+
+
 def test_crt_reconstruction_recovers_the_product():
-    F, W = crt_table()
+    pairs = crt_table()
+    for i, pr in enumerate(pairs):                # each pair's residue is C' mod a b
+        for c in (0, 1, -1, 12345678901234567, -98765432109876543):
+            y_ref = c % (pr["a"] * pr["b"])
+            res = [c % p for p in MODULI]
+            u = ((res[2 * i + 1] + 2 * pr["b"] - res[2 * i]) * pr["inv"]) & 0xFFFFFFFF
+            t = u - ((u * pr["magic"]) >> 32) * pr["b"]
+            assert res[2 * i] + pr["a"] * t == y_ref
     rng = np.random.default_rng(12)
     for k in (64, 1000, 4096):
         t = mod_bits(k)
@@ -176,7 +220,7 @@ def test_crt_reconstruction_recovers_the_product():
         for c in vals:
             assert abs(c) <= lim
             residues = [c % p for p in MODULI]
-            assert reconstruct(residues, F, W) == c
+            assert reconstruct(residues, pairs) == c
 
 
 def test_epilogue_reduction_is_exact():
