@@ -279,7 +279,10 @@ int gb_get_sgemm_mode(void);
  * k: the K segment.)  Uniform and exponent-spread operands take the
  * modular scheme; digit slices (8) are left for columns whose error bound it
  * cannot meet, e.g. rows scaled far above the entries that meet the column.
- * The LU/Cholesky trailing updates always use 7 slices. */
+ * The LU/Cholesky trailing updates, panel solves and refinement residuals
+ * use the modular scheme on every tile when their depth k is 512 or more,
+ * and 7 digit slices otherwise (or when the calling thread has turned the
+ * modular scheme off). */
 int gb_set_ozaki_slices(int slices);
 /* Largest slice count chosen by the calling thread's last automatic-mode
  * emulated DGEMM for its digit-slice tiles (0 if none); synchronises the

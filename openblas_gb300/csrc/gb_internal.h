@@ -163,14 +163,19 @@ void launch_sgemm_fp32_tri(int ta, int tb, int64_t m, int64_t n, int64_t k, floa
 // Slice count argument meaning "choose per 256-column tile of C from the
 // operands and the accuracy target" (see ozaki.cu).
 constexpr int OZAKI_SLICES_AUTO = -1;
+// Slice count argument meaning "the modular scheme on every tile, with no
+// choice" (the internal default of the factorisations' updates).
+constexpr int OZAKI_MODULAR_FIXED = -2;
 // The count for a caller-facing emulated GEMM: the thread's fixed setting
 // (gb_set_ozaki_slices / GB_OZAKI_SLICES), or OZAKI_SLICES_AUTO when unset/0.
 int ozaki_caller_slices();
 // Whether the calling thread's automatic mode may take the modular scheme
 // (gb_set_ozaki_modular / GB_OZAKI_MODULAR).
 bool ozaki_modular_enabled();
-// Emulated-FP64 GEMM (Ozaki slices on the bf16 tensor cores).  slices = 0:
-// default count (7); OZAKI_SLICES_AUTO: chosen on the device.  tri = 1 (2): only C(i,j) with i >= j (i <= j) is written,
+// Emulated-FP64 GEMM (Ozaki schemes on the bf16 tensor cores).  slices = 0:
+// the default form (the modular scheme on every tile, or 7 digit slices
+// when the thread turned it off); 1-8: that many digit slices;
+// OZAKI_SLICES_AUTO: chosen per tile on the device.  tri = 1 (2): only C(i,j) with i >= j (i <= j) is written,
 // tiles wholly in the other triangle are skipped (SYRK-shaped updates).
 // skip: device flag; when nonzero at run time C is left unchanged.
 int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,

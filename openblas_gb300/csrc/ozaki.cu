@@ -1299,8 +1299,10 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
                      int64_t nb = 0, EmuBlockHooks *hooks = nullptr) {
   if (nb <= 0 || nb >= n) nb = n;
   const bool automatic = S == OZAKI_SLICES_AUTO;
-  const int Sa = automatic ? MAX_SLICES : S;  // slices allocated (and cut from op(A))
-  const bool modular = automatic && ozaki_modular_enabled();
+  const bool fixed_mod = S == OZAKI_MODULAR_FIXED;  // every tile modular, no choice
+  // slices allocated (and cut from op(A)); none in the fixed modular form
+  const int Sa = automatic ? MAX_SLICES : fixed_mod ? 0 : S;
+  const bool modular = fixed_mod || (automatic && ozaki_modular_enabled());
   const int64_t seg_len = modular ? MOD_K_SEGMENT : MAX_K_SEGMENT;
   const int64_t kseg = k < seg_len ? k : seg_len;
   const int64_t nseg = (k + seg_len - 1) / seg_len;
@@ -1462,7 +1464,7 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
   if (a_once) {
     if (hooks && (st = hooks->a_range(0, k))) return st;
     prep_a(0, 0, k);
-    if (a_early && (st = split_a(0, 0, k, nullptr))) return st;
+    if (a_early && Sa > 0 && (st = split_a(0, 0, k, nullptr))) return st;
     if (a_early && modular && (st = split_a_mod(0, 0, k, nullptr))) return st;
   }
   for (int64_t j0 = 0; j0 < n; j0 += nb) {
@@ -1480,7 +1482,7 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       if (!a_once && (!a_cache || j0 == 0)) {
         if (hooks && (st = hooks->a_range(k0, kk))) return st;
         prep_a(sg, k0, kk);
-        if (a_cache && (st = split_a(sg, k0, kk, nullptr))) return st;
+        if (a_cache && Sa > 0 && (st = split_a(sg, k0, kk, nullptr))) return st;
         if (a_cache && modular && (st = split_a_mod(sg, k0, kk, nullptr))) return st;
       }
       const ASeg a = aseg(sg);
@@ -1490,6 +1492,20 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       const dim3 g((unsigned)((m + BM - 1) / BM), (unsigned)((jn + BN - 1) / BN));
       const int m_tiles = (int)(m_pad / BM);
       const int64_t ps = m_pad * jn_pad;
+      if (fixed_mod) {
+        // every tile on the modular scheme: no statistics, no choice
+        if (!a_both && (st = split_a_mod(sg, k0, kk, nullptr))) return st;
+        operand_exponents(tb == 0, jn, kk, Bk, ldbj, jn_pad, mx + m_pad, eb, s);
+        launch_split_mod(tb == 0, jn, kk, Bk, ldbj, eb, jn_pad, kp, slb, nullptr, nullptr, tab, s);
+        if ((st = make_map(&mapBr, slb, (int64_t)MOD_COUNT * jn_pad, kp, BN))) return st;
+        if ((st = gemm(true, mapAr[a_cache ? sg : 0], mapBr, jn_pad, 0, kp, nullptr))) return st;
+        reconstruct_tile_kernel<<<g, 256, 0, s>>>(
+            m, jn, m_tiles, ps, reinterpret_cast<const uint16_t *>(planes), a.ea, eb, alpha, bseg,
+            Cj, ldcj, ta, tb, kk, Ak, lda, Bk, ldbj, tri, skip, nullptr, nullptr, tab);
+        count_launch();
+        if ((st = check_cuda(cudaGetLastError(), "emulated dgemm"))) return st;
+        continue;
+      }
       if (!automatic) {
         if (!a_both && (st = split_a(sg, k0, kk, nullptr))) return st;
         split_operand(tb == 0, jn, kk, Bk, ldbj, S, jn_pad, kp, mx + m_pad, eb, slb, s);
@@ -1553,35 +1569,43 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
 
 }  // namespace oz
 
-// Slice count used when the caller passes 0 (the LU and Cholesky trailing
-// updates and panel solves): 7 slices of 8-bit digits keep 56 bits,
-// FP64-level accuracy for operands whose rows/columns span a moderate
-// exponent range.
-int ozaki_default_slices() { return 7; }
+// Form used when the caller passes 0 (the LU and Cholesky trailing updates
+// and panel solves, the refinement residuals): for k >= MOD_MIN_K the
+// modular scheme on every tile (t >= 55 bits, nothing dropped: a tighter
+// bound than 7 digit slices with half the tensor-core work), otherwise (or
+// when the thread has turned the modular scheme off) 7 slices of 8-bit
+// digits.  Below k = 512 the CRT reconstruction per element of C costs more
+// than the 14 products it saves (measured: the emulated DPOTRF 32768 with
+// k = 256 updates took 789 ms on residues against 737 ms on digits).
+constexpr int64_t MOD_MIN_K = 512;
+static int ozaki_default_form(int64_t k) {
+  return ozaki_modular_enabled() && k >= MOD_MIN_K ? OZAKI_MODULAR_FIXED : 7;
+}
 
 // Resolves a requested slice count: > 0 fixed (at most MAX_SLICES), 0 the
 // default, OZAKI_SLICES_AUTO chosen per tile on the device (the records of
 // the largest count and of the moduli chosen are reset for the new call).
-static int resolve_slices(int slices, cudaStream_t s) {
+static int resolve_slices(int slices, int64_t k, cudaStream_t s) {
   if (slices == OZAKI_SLICES_AUTO) {
     static_assert(STATUS_LAST_MODULI == STATUS_LAST_SLICES + 1, "adjacent status words");
     cudaMemsetAsync(ctx().d_status + STATUS_LAST_SLICES, 0, 2 * sizeof(int), s);
     return OZAKI_SLICES_AUTO;
   }
-  int S = slices > 0 ? slices : ozaki_default_slices();
-  return S > oz::MAX_SLICES ? oz::MAX_SLICES : S;
+  if (slices <= 0) return ozaki_default_form(k);
+  return slices > oz::MAX_SLICES ? oz::MAX_SLICES : slices;
 }
 
 int64_t emulated_k_segment(int slices) {
-  return slices == OZAKI_SLICES_AUTO && ozaki_modular_enabled() ? oz::MOD_K_SEGMENT
-                                                                 : oz::MAX_K_SEGMENT;
+  const bool mod = (slices == OZAKI_SLICES_AUTO || slices == OZAKI_MODULAR_FIXED || slices == 0) &&
+                   ozaki_modular_enabled();
+  return mod ? oz::MOD_K_SEGMENT : oz::MAX_K_SEGMENT;
 }
 
 int dgemm_emulated_blocked(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha,
                            const double *A, int64_t lda, double beta, int slices, int64_t nb,
                            EmuBlockHooks *hooks, cudaStream_t s) {
   if (m <= 0 || n <= 0) return GB_SUCCESS;
-  const int S = resolve_slices(slices, s);
+  const int S = resolve_slices(slices, k, s);
   if (m > (int64_t)1 << 22 || n > (int64_t)1 << 22)
     return set_error(GB_ERR_UNSUPPORTED, "blocked emulated dgemm: dimension too large");
   nb = (nb + oz::BN - 1) / oz::BN * oz::BN;
@@ -1594,7 +1618,7 @@ int dgemm_emulated(int ta, int tb, int64_t m, int64_t n, int64_t k, double alpha
                    double *C, int64_t ldc, int slices, cudaStream_t s, int tri,
                    const int *skip) {
   if (m <= 0 || n <= 0) return GB_SUCCESS;
-  const int S = resolve_slices(slices, s);
+  const int S = resolve_slices(slices, k, s);
   if ((m > GEMM_BLOCK_EXTENT || n > GEMM_BLOCK_EXTENT) && tri == 0 && !skip)
     return gemm_over_blocks(ta, tb, m, n, A, lda, B, ldb, C, ldc, GEMM_BLOCK_EXTENT,
                             [&](int64_t mb, int64_t nb, const double *Ai, const double *Bj,
