@@ -1768,6 +1768,35 @@ __global__ void set_identity_kernel(int64_t n, double *__restrict__ W) {
 // skipped on the device (info), as in the native form.
 static int potrf_panel_solve(bool upper, int64_t rest, int64_t jb, const double *D,
                              int64_t lda, double *P, int *info, int gemm_mode, cudaStream_t s) {
+  if (gemm_mode == 1 && rest >= 256 && jb > POTRF_NB) {
+    // a block wider than 256: blocked substitution over its 256-wide block
+    // columns, each one's triangle inverted as below and the coupling with
+    // the block columns before it applied as one emulated GEMM (depth 256 i)
+    for (int64_t i0 = 0; i0 < jb; i0 += POTRF_NB) {
+      const int64_t ib = (jb - i0) < POTRF_NB ? (jb - i0) : POTRF_NB;
+      int st;
+      if (upper) {
+        double *Pi = P + i0;  // rows i0.. of the jb x rest panel
+        if (i0 > 0 &&
+            (st = dgemm_emulated(1, 0, ib, rest, i0, -1.0, D + i0 * lda, lda, P, lda, 1.0, Pi, lda,
+                                 0, s, 0, info)))
+          return st;
+        if ((st = potrf_panel_solve(true, rest, ib, D + i0 + i0 * lda, lda, Pi, info, gemm_mode,
+                                    s)))
+          return st;
+      } else {
+        double *Pi = P + i0 * lda;  // columns i0.. of the rest x jb panel
+        if (i0 > 0 &&
+            (st = dgemm_emulated(0, 1, rest, ib, i0, -1.0, P, lda, D + i0, lda, 1.0, Pi, lda, 0,
+                                 s, 0, info)))
+          return st;
+        if ((st = potrf_panel_solve(false, rest, ib, D + i0 + i0 * lda, lda, Pi, info, gemm_mode,
+                                    s)))
+          return st;
+      }
+    }
+    return GB_SUCCESS;
+  }
   if (!(gemm_mode == 1 && rest >= 256 && jb >= 64))
     return upper ? trsm_skip<double>(0, 0, 1, 1, jb, rest, D, lda, P, lda, s, info)
                  : trsm_skip<double>(1, 1, 1, 1, rest, jb, D, lda, P, lda, s, info);
@@ -1798,19 +1827,29 @@ static int potrf_panel_solve(bool upper, int64_t rest, int64_t jb, const float *
 // solved against the block's triangle (potrf_panel_solve), and the trailing
 // matrix gets one rank-256 SYRK (see potrf_trailing).  Every step after a non-positive pivot
 // is skipped on the device (info), so the matrix is left as it was at the
-// failing column.
+// failing column.  With emulated-FP64 updates (FP64, gemm_mode 1) the block
+// columns are POTRF_NB_EMULATED wide and each diagonal block is itself
+// factored by this routine with 256-wide blocks: every emulated panel solve
+// and trailing update then has depth k = 1024, which amortises the residue
+// planes' round trip through HBM over four times the work and takes the
+// modular scheme (k >= 512).  off: the global column of A(0,0) (for info).
+constexpr int64_t POTRF_NB_EMULATED = 1024;
 template <typename T>
-int potrf_device_t(int uplo, int64_t n, T *A, int64_t lda, int *info, int gemm_mode,
-                   cudaStream_t s) {
-  GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
+int potrf_blocked(int uplo, int64_t n, T *A, int64_t lda, int *info, int gemm_mode,
+                  cudaStream_t s, int64_t nb, int64_t off) {
   const bool upper = uplo == 0;
-  for (int64_t j0 = 0; j0 < n; j0 += POTRF_NB) {
-    const int64_t jb = (n - j0) < POTRF_NB ? (n - j0) : POTRF_NB;
+  for (int64_t j0 = 0; j0 < n; j0 += nb) {
+    const int64_t jb = (n - j0) < nb ? (n - j0) : nb;
     T *D = A + j0 + j0 * lda;
     int st;
     {
       ProfileScope prof("potrf_diag", s);
-      if ((st = potrf_diag_block<T>(upper, jb, D, lda, info, j0, s))) return st;
+      if (jb > POTRF_NB) {
+        if ((st = potrf_blocked<T>(uplo, jb, D, lda, info, gemm_mode, s, POTRF_NB, off + j0)))
+          return st;
+      } else if ((st = potrf_diag_block<T>(upper, jb, D, lda, info, off + j0, s))) {
+        return st;
+      }
     }
     const int64_t rest = n - j0 - jb;
     if (rest <= 0) continue;
@@ -1828,6 +1867,14 @@ int potrf_device_t(int uplo, int64_t n, T *A, int64_t lda, int *info, int gemm_m
     if (st) return st;
   }
   return check_cuda(cudaGetLastError(), "potrf");
+}
+
+template <typename T>
+int potrf_device_t(int uplo, int64_t n, T *A, int64_t lda, int *info, int gemm_mode,
+                   cudaStream_t s) {
+  GB_CUDA(cudaMemsetAsync(info, 0, sizeof(int), s));
+  const int64_t nb = (sizeof(T) == 8 && gemm_mode == 1) ? POTRF_NB_EMULATED : POTRF_NB;
+  return potrf_blocked<T>(uplo, n, A, lda, info, gemm_mode, s, nb, 0);
 }
 
 int potrf_device(int uplo, int64_t n, double *A, int64_t lda, int *info, int gemm_mode,

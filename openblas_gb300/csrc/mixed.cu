@@ -385,12 +385,14 @@ struct Mixed {
 // Restarted flexible GMRES for A d = r (one column), right preconditioner
 // M^-1 = the FP32 LU.  Returns iterations used; d is written to `d`.  A first
 // restart cycle whose 16th iteration has not reduced the residual tenfold,
-// or a cycle that does not reduce it a hundredfold, sets *hopeless: at that
-// rate the iteration budget cannot reach FP64 accuracy (measured on
-// U diag(logspace(0,-8)) V^T at n = 4096 and 8192, where the FP32 factors
-// leave a quarter of the spectrum unpreconditioned and GMRES reduces the
-// residual by less than 2x per 100 iterations, while a matrix with a few
-// tiny singular values converges within ~25 iterations).
+// 16 consecutive iterations that do not halve it, or a cycle that does not
+// reduce it a hundredfold, set *hopeless: at that rate the iteration budget
+// cannot reach FP64 accuracy (measured on U diag(logspace(0,-8)) V^T at
+// n = 4096 and 8192, where the FP32 factors leave a quarter of the spectrum
+// unpreconditioned: a first cycle drops the residual ~7000x and then
+// stalls, and the next cycle reduces it by less than 1%, while a matrix with
+// a few tiny singular values converges within ~25 iterations).  The residual
+// norm of each iterate is the Givens-rotated |g_j+1|, known on the host.
 int fgmres(Mixed &M, const double *r, double *d, int restart, int max_it, double rtol,
            int *iters, bool *hopeless) {
   *hopeless = false;
@@ -403,7 +405,8 @@ int fgmres(Mixed &M, const double *r, double *d, int restart, int max_it, double
   double *w = Z + n * restart;               // n
   double *hcol = w + n;                      // restart+1 (device)
   std::vector<double> H((restart + 1) * restart, 0.0), cs(restart), sn(restart), g(restart + 1);
-  std::vector<double> hh(restart + 1);
+  std::vector<double> hh(restart + 1), est(restart);
+  constexpr int STALL_WINDOW = 16;
   GB_CUDA(cudaMemsetAsync(d, 0, n * sizeof(double), s));
   // initial residual of the correction equation: r - A*0 = r
   double beta = 0.0, prev_beta = 0.0;
@@ -468,7 +471,10 @@ int fgmres(Mixed &M, const double *r, double *d, int restart, int max_it, double
       g[j + 1] = -sn[j] * g[j];
       g[j] = cs[j] * g[j];
       for (int i = 0; i <= j; ++i) H[i + j * (restart + 1)] = hh[i];
-      if (fabs(g[j + 1]) <= rtol || hnext == 0.0) {
+      est[j] = fabs(g[j + 1]);  // the residual norm of the cycle's iterate
+      if (config().verbose >= 3)
+        fprintf(stderr, "libgbblas fgmres: iteration %d  ||r|| ~ %.3e\n", total + 1, est[j]);
+      if (est[j] <= rtol || hnext == 0.0) {
         ++j;
         ++total;
         break;
@@ -476,7 +482,14 @@ int fgmres(Mixed &M, const double *r, double *d, int restart, int max_it, double
       // 16 iterations into the first cycle without a tenfold reduction: the
       // preconditioner leaves too much of the spectrum spread for GMRES to
       // finish (a few outlying directions are resolved by then)
-      if (outer == 0 && j + 1 == 16 && fabs(g[j + 1]) > 0.1 * beta) {
+      if (outer == 0 && j + 1 == 16 && est[j] > 0.1 * beta) {
+        *hopeless = true;
+        ++j;
+        ++total;
+        break;
+      }
+      // a stall: 16 iterations that did not halve the residual
+      if (j >= STALL_WINDOW && est[j] > 0.5 * est[j - STALL_WINDOW]) {
         *hopeless = true;
         ++j;
         ++total;
@@ -493,6 +506,7 @@ int fgmres(Mixed &M, const double *r, double *d, int restart, int max_it, double
     for (int i = 0; i < j; ++i)
       { scale_kernel<<<(unsigned)((n + 255) / 256), 256, 0, s>>>(n, y[i], Z + i * n, d, 1); count_launch(); }
     if (fabs(g[j]) <= rtol) break;
+    if (*hopeless) break;  // d keeps the cycle's best iterate; no further restart
     // new residual of the correction equation: w = r - A d
     M.gemv_dd(d, -1.0, r, 1.0, w);
   }
