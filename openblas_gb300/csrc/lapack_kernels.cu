@@ -446,6 +446,62 @@ __device__ __forceinline__ void st_async(uint32_t dst, int v, uint32_t mbar) {
   asm volatile("st.async.shared::cluster.mbarrier::complete_tx::bytes.b32 [%0], %1, [%2];"
                ::"r"(dst), "r"(v), "r"(mbar) : "memory");
 }
+
+// IAMAX of the cluster panel.  getf2_k.c's running maximum starts from
+// |a_jj| and only moves to a larger value, so a NaN never becomes the pivot.
+// FP32 compares the magnitudes as floats (-1: no candidate).  FP64 compares
+// ordered integer keys instead, 0 for NaN and for "no candidate",
+// bits(|x|) + 1 otherwise: GB300 has ~2 FP64 operations per clock per SM,
+// and the compares of the search and its warp reductions would otherwise
+// cost more than the column's rank-1 update.
+template <typename T>
+struct PivotOps;
+template <>
+struct PivotOps<float> {
+  using V = float;
+  __device__ static V none() { return -1.0f; }
+  __device__ static V mag(float x) { return x < 0.f ? -x : x; }
+  __device__ static bool better(V a, V best, long long row, long long bidx) {
+    return a > best || (a == best && row < bidx);
+  }
+  __device__ static void argmax(V &v, long long &i) { warp_argmax<float>(v, i); }
+  __device__ static float carry(V v) { return v; }
+  __device__ static V uncarry(float v) { return v; }
+  __device__ static bool is_nan(float x) { return x != x; }
+  __device__ static bool nonzero(float x) { return x != 0.f; }
+  __device__ static bool scaled(float x) { return x != 0.f && (x < 0.f ? -x : x) >= FLT_MIN; }
+};
+template <>
+struct PivotOps<double> {
+  using V = unsigned long long;
+  __device__ static V none() { return 0ull; }
+  __device__ static V mag(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+    return b > 0x7FF0000000000000ull ? 0ull : b + 1ull;
+  }
+  __device__ static bool better(V a, V best, long long row, long long bidx) {
+    return a > best || (a == best && a != 0ull && row < bidx);
+  }
+  // first maximum over the warp: the largest key, the smallest row among its
+  // holders (rows < 2^32 - 1); 0 / LLONG_MAX when no lane has a candidate
+  __device__ static void argmax(V &k, long long &i) {
+    const unsigned hi = (unsigned)(k >> 32), lo = (unsigned)k;
+    const unsigned hmax = __reduce_max_sync(0xffffffffu, hi);
+    const unsigned lmax = __reduce_max_sync(0xffffffffu, hi == hmax ? lo : 0u);
+    const unsigned long long kmax = ((unsigned long long)hmax << 32) | lmax;
+    const unsigned ik = (k == kmax && kmax != 0ull) ? (unsigned)i : 0xffffffffu;
+    const unsigned imin = __reduce_min_sync(0xffffffffu, ik);
+    k = kmax;
+    i = imin == 0xffffffffu ? LLONG_MAX : (long long)imin;
+  }
+  __device__ static double carry(V k) { return __longlong_as_double((long long)k); }  // bits
+  __device__ static V uncarry(double v) { return (unsigned long long)__double_as_longlong(v); }
+  __device__ static bool is_nan(double x) { return mag(x) == 0ull; }
+  // piv != 0 (NaN counts) and fabs(piv) >= DBL_MIN (NaN does not), on the key
+  __device__ static bool nonzero(double x) { return mag(x) != 1ull; }
+  __device__ static bool scaled(double x) { return mag(x) >= mag(DBL_MIN); }
+};
+
 __device__ __forceinline__ void cl_mbar_init(unsigned long long *bar, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;"
                ::"r"(static_cast<uint32_t>(__cvta_generic_to_shared(bar))), "r"(count)
@@ -577,21 +633,37 @@ getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__r
     if (j >= ncol) break;
     const int par = j & 1;
     // ---- local first maximum of |a_ij| over this thread's rows >= j
-    T best = T(-1);
+    using PO = PivotOps<T>;
+    using V = typename PO::V;
+    V best = PO::none();
     long long bidx = LLONG_MAX;
+    if constexpr (sizeof(T) == 4) {
 #pragma unroll
-    for (int q = 0; q < L; ++q) {
-      const int64_t row = g + q * nthr;
-      if (row < m && row >= j) {
-        T a = r[q][j];  // j is a compile-time index in the unrolled loop
-        a = a < T(0) ? -a : a;
-        if (a > best || (a == best && row < bidx)) {
-          best = a;
-          bidx = row;
+      for (int q = 0; q < L; ++q) {
+        const int64_t row = g + q * nthr;
+        if (row < m && row >= j) {
+          T a = r[q][j];  // j is a compile-time index in the unrolled loop
+          a = a < T(0) ? -a : a;
+          if (a > best || (a == best && row < bidx)) {
+            best = a;
+            bidx = row;
+          }
+        }
+      }
+    } else {
+#pragma unroll
+      for (int q = 0; q < L; ++q) {
+        const int64_t row = g + q * nthr;
+        if (row < m && row >= j) {
+          const V a = PO::mag(r[q][j]);
+          if (PO::better(a, best, row, bidx)) {
+            best = a;
+            bidx = row;
+          }
         }
       }
     }
-    warp_argmax<T>(best, bidx);
+    PO::argmax(best, bidx);
     // the lane holding the warp's best row stages it; the holder of row j too
     if (bidx != LLONG_MAX && (int)(bidx & 31) == lane) {
       const int qb = (int)(bidx >> lg_nthr);
@@ -600,7 +672,7 @@ getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__r
         if (q == qb) stage_row(w_row + (par * CPANEL_WARPS + warp) * PANEL_NB, r[q]);
     }
     if (lane == 0) {
-      red_val[par * CPANEL_WARPS + warp] = best;
+      red_val[par * CPANEL_WARPS + warp] = PO::carry(best);
       red_idx[par * CPANEL_WARPS + warp] = bidx;
     }
     const int jowner = (int)(((int64_t)j & nmask) / CPANEL_THREADS);
@@ -616,9 +688,9 @@ getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__r
       break;
     }
     // ---- every warp: the CTA's candidate; warp w sends it (and row j) to CTA w
-    T cb = lane < CPANEL_WARPS ? red_val[par * CPANEL_WARPS + lane] : T(-1);
+    V cb = lane < CPANEL_WARPS ? PO::uncarry(red_val[par * CPANEL_WARPS + lane]) : PO::none();
     long long ci = lane < CPANEL_WARPS ? red_idx[par * CPANEL_WARPS + lane] : LLONG_MAX;
-    warp_argmax<T>(cb, ci);
+    PO::argmax(cb, ci);
     if (warp < CS) {
       const int dst = warp;
       T rv = T(0);
@@ -631,7 +703,7 @@ getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__r
         st_async(cl_smem_addr(in_row + (par * CPANEL_MAX_CS + rank) * PANEL_NB + lane, dst), rv,
                  rb);
       if (lane == 0) {
-        st_async(cl_smem_addr(in_val + par * CPANEL_MAX_CS + rank, dst), cb, rb);
+        st_async(cl_smem_addr(in_val + par * CPANEL_MAX_CS + rank, dst), PO::carry(cb), rb);
         st_async(cl_smem_addr(in_idx + par * CPANEL_MAX_CS + rank, dst),
                  ci == LLONG_MAX ? -1 : (int)ci, rb);
       }
@@ -658,35 +730,46 @@ getf2_cluster_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__r
       armed_to = j + 3;
     }
     // ---- global pivot from the local inbox (identical in every CTA)
-    T gb = T(-1);
+    V gb = PO::none();
     long long gi = LLONG_MAX;
     if (lane < CS) {
       const int idx = in_idx[par * CPANEL_MAX_CS + lane];
       if (idx >= 0) {
-        gb = in_val[par * CPANEL_MAX_CS + lane];
+        gb = PO::uncarry(in_val[par * CPANEL_MAX_CS + lane]);
         gi = idx;
       }
     }
-    warp_argmax<T>(gb, gi);
+    PO::argmax(gb, gi);
     const T *rowj_v = in_rowj + par * PANEL_NB;
     // IAMAX starts from |a_jj| and only a larger value moves it: a NaN at row
     // j (or no comparable entry at all) keeps row j
     const T ajj = rowj_v[j];
-    const bool keep = gi == LLONG_MAX || ajj != ajj;
+    const bool keep = gi == LLONG_MAX || (sizeof(T) == 4 ? ajj != ajj : PO::is_nan(ajj));
     const int64_t p = keep ? (int64_t)j : gi;
     const T *u_v = keep ? rowj_v
                         : in_row + (par * CPANEL_MAX_CS + (int)((gi & nmask) / CPANEL_THREADS)) *
                                        PANEL_NB;
     const T piv = u_v[j];
+    // piv != 0 (NaN counts) and |piv| >= the smallest normal (NaN does not);
+    // FP32 keeps the float tests (the same results: the compiler then keeps
+    // more of the 16-column kernel's rows in registers)
     const T apiv = piv < T(0) ? -piv : piv;
-    const bool nonzero = piv != T(0);
-    const bool scaled = nonzero && apiv >= tiny_pivot<T>();  // getf2_k.c:103-116
+    const bool nonzero = sizeof(T) == 4 ? piv != T(0) : PO::nonzero(piv);
+    const bool scaled =
+        sizeof(T) == 4 ? (nonzero && apiv >= tiny_pivot<T>()) : PO::scaled(piv);  // getf2_k.c:103-116
     const bool swap = p != j;
     if (rank == 0 && tid == 0) {
       ipiv[j] = (int)(p + row_off + 1);
       if (!nonzero && *info == 0) *info = (int)(j + row_off + 1);
     }
-    const T rcp = scaled ? T(1) / piv : T(1);
+    // FP64: one division per warp, broadcast (a division is ~10 FP64 operations)
+    T rcp = T(1);
+    if (sizeof(T) == 8) {
+      if (lane == 0 && scaled) rcp = T(1) / piv;
+      rcp = __shfl_sync(0xffffffffu, rcp, 0);
+    } else if (scaled) {
+      rcp = T(1) / piv;
+    }
 #pragma unroll
     for (int q = 0; q < L; ++q) {
       const int64_t i = g + q * nthr;
@@ -755,7 +838,9 @@ struct ClusterPanel {
 };
 
 // Rows per thread held in registers: 32 columns x 2 rows (FP32) or 1 row
-// (FP64); for taller FP32 panels, 16 columns x 4 rows.
+// (FP64); for taller FP32 panels, 16 columns x 4 rows (FP64 panels taller
+// than one cluster holds take the grid-wide kernel: a 16-column FP64 form
+// measured slower, LU 16384 430 -> 455 ms).
 template <typename T>
 constexpr int cpanel_lmax() { return sizeof(T) == 4 ? 2 : 1; }
 template <typename T>
@@ -827,7 +912,11 @@ ClusterPanel<T> cluster_panel_caps() {
 }
 
 // Widest leaf (32 or 16 columns) whose cluster panel holds `rows` rows; 32
-// when neither does (the grid-wide kernel then takes 32 columns).
+// when neither does (the grid-wide kernel then takes 32 columns).  (16-column
+// leaves for every FP64 panel were tried: more leaves, each as slow -- the
+// per-column exchange, not the FP64 rank-1 updates, sets a leaf's time --
+// and the recursion's extra small updates: emulated-update LU 8192 147 ->
+// 175 ms.)
 template <typename T>
 int lu_leaf_width(int64_t rows) {
   const ClusterPanel<T> caps = cluster_panel_caps<T>();
