@@ -79,6 +79,78 @@ __device__ inline double tiny_pivot<double>() { return DBL_MIN; }
 template <>
 __device__ inline float tiny_pivot<float>() { return FLT_MIN; }
 
+// IAMAX of the panel kernels.  getf2_k.c's running maximum starts from
+// |a_jj| and only moves to a larger value, so a NaN never becomes the pivot.
+// FP32 compares the magnitudes as floats (-1: no candidate).  FP64 compares
+// ordered integer keys instead, 0 for NaN and for "no candidate",
+// bits(|x|) + 1 otherwise: GB300 has ~2 FP64 operations per clock per SM,
+// and the compares of the search and its warp reductions would otherwise
+// cost more than the column's rank-1 update.
+template <typename T>
+struct PivotOps;
+template <>
+struct PivotOps<float> {
+  using V = float;
+  __device__ static V none() { return -1.0f; }
+  __device__ static V mag(float x) { return x < 0.f ? -x : x; }
+  __device__ static bool better(V a, V best, long long row, long long bidx) {
+    return a > best || (a == best && row < bidx);
+  }
+  __device__ static void argmax(V &v, long long &i);  // warp_argmax<float>, below
+  __device__ static float carry(V v) { return v; }
+  __device__ static V uncarry(float v) { return v; }
+  __device__ static bool is_nan(float x) { return x != x; }
+  __device__ static bool nonzero(float x) { return x != 0.f; }
+  __device__ static bool scaled(float x) { return x != 0.f && (x < 0.f ? -x : x) >= FLT_MIN; }
+};
+template <>
+struct PivotOps<double> {
+  using V = unsigned long long;
+  __device__ static V none() { return 0ull; }
+  __device__ static V mag(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
+    return b > 0x7FF0000000000000ull ? 0ull : b + 1ull;
+  }
+  __device__ static bool better(V a, V best, long long row, long long bidx) {
+    return a > best || (a == best && a != 0ull && row < bidx);
+  }
+  // first maximum over the warp: the largest key, the smallest row among its
+  // holders (rows < 2^32 - 1); 0 / LLONG_MAX when no lane has a candidate
+  __device__ static void argmax(V &k, long long &i) {
+    const unsigned hi = (unsigned)(k >> 32), lo = (unsigned)k;
+    const unsigned hmax = __reduce_max_sync(0xffffffffu, hi);
+    const unsigned lmax = __reduce_max_sync(0xffffffffu, hi == hmax ? lo : 0u);
+    const unsigned long long kmax = ((unsigned long long)hmax << 32) | lmax;
+    const unsigned ik = (k == kmax && kmax != 0ull) ? (unsigned)i : 0xffffffffu;
+    const unsigned imin = __reduce_min_sync(0xffffffffu, ik);
+    k = kmax;
+    i = imin == 0xffffffffu ? LLONG_MAX : (long long)imin;
+  }
+  __device__ static double carry(V k) { return __longlong_as_double((long long)k); }  // bits
+  __device__ static V uncarry(double v) { return (unsigned long long)__double_as_longlong(v); }
+  __device__ static bool is_nan(double x) { return mag(x) == 0ull; }
+  // piv != 0 (NaN counts) and fabs(piv) >= DBL_MIN (NaN does not), on the key
+  __device__ static bool nonzero(double x) { return mag(x) != 1ull; }
+  __device__ static bool scaled(double x) { return mag(x) >= mag(DBL_MIN); }
+};
+
+// The grid-wide panel's candidate values: FP32 magnitudes (-1: none), FP64
+// PivotOps keys carried as the bits of a double (0: none).
+template <typename T>
+__device__ __forceinline__ T panel_none() {
+  if constexpr (sizeof(T) == 4) return T(-1);
+  else return PivotOps<double>::carry(PivotOps<double>::none());
+}
+template <typename T>
+__device__ __forceinline__ bool panel_better(T a, T b, int64_t ia, int64_t ib) {
+  if constexpr (sizeof(T) == 4) {
+    return a > b || (a == b && ia < ib);
+  } else {
+    const auto ka = PivotOps<double>::uncarry(a), kb = PivotOps<double>::uncarry(b);
+    return ka > kb || (ka == kb && ka != 0ull && ia < ib);
+  }
+}
+
 template <typename T, int R>
 __global__ void __launch_bounds__(PANEL_THREADS)
 getf2_panel_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__restrict__ ipiv,
@@ -113,31 +185,55 @@ getf2_panel_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__res
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int j = 0; j < nb && j < m; ++j) {
     const int par = j & 1;
-    // ---- 1. block-local first-max over rows >= j
+    // ---- 1. block-local first-max over rows >= j (FP64: on the integer
+    // keys of PivotOps, carried in the T-typed slots as their bits)
     T best = T(-1);
     int64_t bidx = INT64_MAX;
+    if constexpr (sizeof(T) == 4) {
 #pragma unroll
-    for (int r = 0; r < R; ++r) {
-      if (rows[r] < m && rows[r] >= j) {
-        T a = v[r][0];
+      for (int r = 0; r < R; ++r) {
+        if (rows[r] < m && rows[r] >= j) {
+          T a = v[r][0];
 #pragma unroll
-        for (int c = 1; c < PANEL_NB; ++c)
-          if (c == j) a = v[r][c];
-        a = a < T(0) ? -a : a;
-        if (a > best || (a == best && rows[r] < bidx)) {
-          best = a;
-          bidx = rows[r];
+          for (int c = 1; c < PANEL_NB; ++c)
+            if (c == j) a = v[r][c];
+          a = a < T(0) ? -a : a;
+          if (a > best || (a == best && rows[r] < bidx)) {
+            best = a;
+            bidx = rows[r];
+          }
         }
       }
-    }
 #pragma unroll
-    for (int off = 16; off > 0; off >>= 1) {
-      T ob = __shfl_down_sync(0xffffffffu, best, off);
-      int64_t oi = __shfl_down_sync(0xffffffffu, bidx, off);
-      if (ob > best || (ob == best && oi < bidx)) {
-        best = ob;
-        bidx = oi;
+      for (int off = 16; off > 0; off >>= 1) {
+        T ob = __shfl_down_sync(0xffffffffu, best, off);
+        int64_t oi = __shfl_down_sync(0xffffffffu, bidx, off);
+        if (ob > best || (ob == best && oi < bidx)) {
+          best = ob;
+          bidx = oi;
+        }
       }
+    } else {
+      using PO = PivotOps<double>;
+      PO::V key = PO::none();
+      long long kidx = LLONG_MAX;
+#pragma unroll
+      for (int r = 0; r < R; ++r) {
+        if (rows[r] < m && rows[r] >= j) {
+          T a = v[r][0];
+#pragma unroll
+          for (int c = 1; c < PANEL_NB; ++c)
+            if (c == j) a = v[r][c];
+          const PO::V k = PO::mag(a);
+          if (PO::better(k, key, rows[r], kidx)) {
+            key = k;
+            kidx = rows[r];
+          }
+        }
+      }
+      PO::argmax(key, kidx);
+      best = PO::carry(key);
+      bidx = kidx == LLONG_MAX ? INT64_MAX : kidx;
     }
     if (lane == 0) {
       s_val[warp] = best;
@@ -148,7 +244,7 @@ getf2_panel_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__res
       T bb = s_val[0];
       int64_t bi = s_idx[0];
       for (int w = 1; w < PANEL_THREADS / 32; ++w)
-        if (s_val[w] > bb || (s_val[w] == bb && s_idx[w] < bi)) {
+        if (panel_better<T>(s_val[w], bb, s_idx[w], bi)) {
           bb = s_val[w];
           bi = s_idx[w];
         }
@@ -176,13 +272,13 @@ getf2_panel_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__res
     if (!grid_barrier(bar, nblocks, status, 100 + j)) return;
     // ---- 3. global pivot (same in every block)
     if (threadIdx.x < 32) {
-      T bb = T(-1);
+      T bb = panel_none<T>();
       int64_t bi = INT64_MAX;
       for (unsigned b = lane; b < nblocks; b += 32) {
         const T *slot = cand + ((int64_t)par * nblocks + b) * W;
         T val = __ldcg(slot + PANEL_NB);
         int64_t idx = (int64_t)__ldcg(slot + PANEL_NB + 1);
-        if (idx >= 0 && (val > bb || (val == bb && idx < bi))) {
+        if (idx >= 0 && panel_better<T>(val, bb, idx, bi)) {
           bb = val;
           bi = idx;
         }
@@ -191,7 +287,7 @@ getf2_panel_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__res
       for (int off = 16; off > 0; off >>= 1) {
         T ob = __shfl_down_sync(0xffffffffu, bb, off);
         int64_t oi = __shfl_down_sync(0xffffffffu, bi, off);
-        if (ob > bb || (ob == bb && oi < bi)) {
+        if (panel_better<T>(ob, bb, oi, bi)) {
           bb = ob;
           bi = oi;
         }
@@ -229,7 +325,14 @@ getf2_panel_kernel(int64_t m, int nb, T *__restrict__ A, int64_t lda, int *__res
       ipiv[j] = (int)(p + row_off + 1);
       if (!nonzero && *info == 0) *info = (int)(j + row_off + 1);
     }
-    const T rcp = scaled ? T(1) / piv : T(1);
+    // FP64: one division per warp, broadcast (a division is ~10 FP64 operations)
+    T rcp = T(1);
+    if (sizeof(T) == 8) {
+      if (lane == 0 && scaled) rcp = T(1) / piv;
+      rcp = __shfl_sync(0xffffffffu, rcp, 0);
+    } else if (scaled) {
+      rcp = T(1) / piv;
+    }
     // ---- 4. interchange and update the rows this thread owns
 #pragma unroll
     for (int r = 0; r < R; ++r) {
@@ -424,6 +527,9 @@ __device__ __forceinline__ void warp_argmax<float>(float &v, long long &i) {
   v = kmax == 0u ? -1.f : __uint_as_float(kmax - 1u);
   i = imin == 0xffffffffu ? LLONG_MAX : (long long)imin;
 }
+__device__ __forceinline__ void PivotOps<float>::argmax(V &v, long long &i) {
+  warp_argmax<float>(v, i);
+}
 
 // Distributed-shared-memory messages of the cluster panel.  A value is stored
 // into another CTA's shared memory with st.async, which completes its bytes on
@@ -447,60 +553,6 @@ __device__ __forceinline__ void st_async(uint32_t dst, int v, uint32_t mbar) {
                ::"r"(dst), "r"(v), "r"(mbar) : "memory");
 }
 
-// IAMAX of the cluster panel.  getf2_k.c's running maximum starts from
-// |a_jj| and only moves to a larger value, so a NaN never becomes the pivot.
-// FP32 compares the magnitudes as floats (-1: no candidate).  FP64 compares
-// ordered integer keys instead, 0 for NaN and for "no candidate",
-// bits(|x|) + 1 otherwise: GB300 has ~2 FP64 operations per clock per SM,
-// and the compares of the search and its warp reductions would otherwise
-// cost more than the column's rank-1 update.
-template <typename T>
-struct PivotOps;
-template <>
-struct PivotOps<float> {
-  using V = float;
-  __device__ static V none() { return -1.0f; }
-  __device__ static V mag(float x) { return x < 0.f ? -x : x; }
-  __device__ static bool better(V a, V best, long long row, long long bidx) {
-    return a > best || (a == best && row < bidx);
-  }
-  __device__ static void argmax(V &v, long long &i) { warp_argmax<float>(v, i); }
-  __device__ static float carry(V v) { return v; }
-  __device__ static V uncarry(float v) { return v; }
-  __device__ static bool is_nan(float x) { return x != x; }
-  __device__ static bool nonzero(float x) { return x != 0.f; }
-  __device__ static bool scaled(float x) { return x != 0.f && (x < 0.f ? -x : x) >= FLT_MIN; }
-};
-template <>
-struct PivotOps<double> {
-  using V = unsigned long long;
-  __device__ static V none() { return 0ull; }
-  __device__ static V mag(double x) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x) & 0x7FFFFFFFFFFFFFFFull;
-    return b > 0x7FF0000000000000ull ? 0ull : b + 1ull;
-  }
-  __device__ static bool better(V a, V best, long long row, long long bidx) {
-    return a > best || (a == best && a != 0ull && row < bidx);
-  }
-  // first maximum over the warp: the largest key, the smallest row among its
-  // holders (rows < 2^32 - 1); 0 / LLONG_MAX when no lane has a candidate
-  __device__ static void argmax(V &k, long long &i) {
-    const unsigned hi = (unsigned)(k >> 32), lo = (unsigned)k;
-    const unsigned hmax = __reduce_max_sync(0xffffffffu, hi);
-    const unsigned lmax = __reduce_max_sync(0xffffffffu, hi == hmax ? lo : 0u);
-    const unsigned long long kmax = ((unsigned long long)hmax << 32) | lmax;
-    const unsigned ik = (k == kmax && kmax != 0ull) ? (unsigned)i : 0xffffffffu;
-    const unsigned imin = __reduce_min_sync(0xffffffffu, ik);
-    k = kmax;
-    i = imin == 0xffffffffu ? LLONG_MAX : (long long)imin;
-  }
-  __device__ static double carry(V k) { return __longlong_as_double((long long)k); }  // bits
-  __device__ static V uncarry(double v) { return (unsigned long long)__double_as_longlong(v); }
-  __device__ static bool is_nan(double x) { return mag(x) == 0ull; }
-  // piv != 0 (NaN counts) and fabs(piv) >= DBL_MIN (NaN does not), on the key
-  __device__ static bool nonzero(double x) { return mag(x) != 1ull; }
-  __device__ static bool scaled(double x) { return mag(x) >= mag(DBL_MIN); }
-};
 
 __device__ __forceinline__ void cl_mbar_init(unsigned long long *bar, unsigned count) {
   asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;"
