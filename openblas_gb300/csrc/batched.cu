@@ -385,6 +385,7 @@ __device__ int cta_getrf(int n, T *M, int ld, int *ipiv) {
   __shared__ int si[NT / 32];
   __shared__ T s_piv;
   __shared__ int s_p;
+  __shared__ T s_rcp;
   const T tiny = sizeof(T) == 8 ? (T)DBL_MIN : (T)FLT_MIN;
   int info = 0;
   for (int j = 0; j < n; ++j) {
@@ -401,10 +402,13 @@ __device__ int cta_getrf(int n, T *M, int ld, int *ipiv) {
     cta_argmax<T, NT>(best, bidx, sv, si, &s_piv, &s_p);
     const int p = s_p;
     const T piv = M[p + (int64_t)j * ld];
-    __syncthreads();  // every thread has the pivot before any row moves
     const T apiv = piv < T(0) ? -piv : piv;
     const bool nonzero = piv != T(0);
     const bool scaled = nonzero && apiv >= tiny;
+    // one division per CTA (FP64 divisions are ~10 operations on GB300's
+    // scarce FP64 units), shared after the barrier
+    if (threadIdx.x == 0) s_rcp = scaled ? T(1) / piv : T(1);
+    __syncthreads();  // every thread has the pivot before any row moves
     if (threadIdx.x == 0) ipiv[j] = p + 1;
     if (!nonzero && info == 0) info = j + 1;
     // interchange rows j and p: all columns when scaled, columns > j otherwise
@@ -417,7 +421,7 @@ __device__ int cta_getrf(int n, T *M, int ld, int *ipiv) {
         }
     __syncthreads();
     if (scaled) {
-      const T r = T(1) / piv;
+      const T r = s_rcp;
       for (int i = j + 1 + threadIdx.x; i < n; i += NT) M[i + (int64_t)j * ld] *= r;
     }
     __syncthreads();
@@ -446,6 +450,7 @@ __device__ int cta_getrf_blk(int n, T *M, int ld, int *ipiv, T *P) {
   __shared__ int si[NT / 32];
   __shared__ T s_piv;
   __shared__ int s_p;
+  __shared__ T s_rcp;
   const T tiny = sizeof(T) == 8 ? (T)DBL_MIN : (T)FLT_MIN;
   int info = 0;
   for (int j0 = 0; j0 < n; j0 += PANEL_B) {
@@ -471,10 +476,11 @@ __device__ int cta_getrf_blk(int n, T *M, int ld, int *ipiv, T *P) {
       cta_argmax<T, NT>(best, bidx, sv, si, &s_piv, &s_p);
       const int p = s_p;
       const T piv = P[p + j * rows];
-      __syncthreads();  // every thread has the pivot before any row moves
       const T apiv = piv < T(0) ? -piv : piv;
       const bool nonzero = piv != T(0);
       const bool scaled = nonzero && apiv >= tiny;
+      if (threadIdx.x == 0) s_rcp = scaled ? T(1) / piv : T(1);  // one division per CTA
+      __syncthreads();  // every thread has the pivot before any row moves
       if (threadIdx.x == 0) ipiv[j0 + j] = j0 + p + 1;
       if (!nonzero && info == 0) info = j0 + j + 1;
       if (p != j)
@@ -486,7 +492,7 @@ __device__ int cta_getrf_blk(int n, T *M, int ld, int *ipiv, T *P) {
           }
       __syncthreads();
       if (scaled) {
-        const T r = T(1) / piv;
+        const T r = s_rcp;
         for (int i = j + 1 + threadIdx.x; i < rows; i += NT) P[i + j * rows] *= r;
       }
       __syncthreads();
@@ -586,7 +592,7 @@ __device__ void cta_getrs(int n, int nrhs, const TM *LU, int ld, const int *ipiv
 // ---------------------------------------------------------------- POTRF
 template <int NT>
 __device__ int cta_potrf(int n, double *M, int ld, bool upper) {
-  __shared__ double s_d;
+  __shared__ double s_d, s_r;
   __shared__ int s_fail;
   auto at = [&](int i, int c) -> double & {  // element (i, c) of the lower view
     return upper ? M[c + (int64_t)i * ld] : M[i + (int64_t)c * ld];
@@ -601,10 +607,11 @@ __device__ int cta_potrf(int n, double *M, int ld, bool upper) {
         at(j, j) = sqrt(ajj);
       }
       s_d = at(j, j);
+      s_r = 1.0 / s_d;  // one division per CTA
     }
     __syncthreads();
     if (s_fail) return j + 1;
-    const double r = 1.0 / s_d;
+    const double r = s_r;
     for (int i = j + 1 + threadIdx.x; i < n; i += NT) at(i, j) *= r;
     __syncthreads();
     const int rows = n - j - 1;
@@ -624,7 +631,7 @@ __device__ int cta_potrf(int n, double *M, int ld, bool upper) {
 // carries exactly the updates of those columns, as in the unblocked form.
 template <int NT>
 __device__ int cta_potrf_blk(int n, double *M, int ld, bool upper, double *P) {
-  __shared__ double s_d;
+  __shared__ double s_d, s_r;
   __shared__ int s_fail;
   auto at = [&](int i, int c) -> double & {  // element (i, c) of the lower view
     return upper ? M[c + (int64_t)i * ld] : M[i + (int64_t)c * ld];
@@ -645,13 +652,14 @@ __device__ int cta_potrf_blk(int n, double *M, int ld, bool upper, double *P) {
         if (ajj <= 0.0) s_fail = 1;  // potf2_L.c:67-71: the pivot stays, info = j + 1
         else P[j + j * rows] = sqrt(ajj);
         s_d = P[j + j * rows];
+        s_r = 1.0 / s_d;  // one division per CTA
       }
       __syncthreads();
       if (s_fail) {
         done = j;
         break;
       }
-      const double r = 1.0 / s_d;
+      const double r = s_r;
       for (int i = j + 1 + threadIdx.x; i < rows; i += NT) P[i + j * rows] *= r;
       __syncthreads();
       const int pr = rows - j - 1, pc = jb - j - 1;
