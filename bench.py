@@ -57,6 +57,9 @@ def parse_args():
     ap.add_argument("--suite", action="store_true",
                     help="measure every configuration of the level-3/LAPACK sweep (one JSON "
                          "line each) instead of the headline step")
+    ap.add_argument("--suite-only", default="",
+                    help="with --suite: comma-separated sections to run (dgemm1024, dgemm_sweep, "
+                         "sgemm, dtrsm, dsyrk, emulated, complex, dgesv, illcond, dpotrf)")
     return ap.parse_args()
 
 
@@ -237,380 +240,452 @@ def run_suite(args):
         if st != 0:
             raise RuntimeError(gb.last_error(lib))
 
+    sections = set(args.suite_only.split(",")) if args.suite_only else None
+
+    def want(key):
+        return sections is None or key in sections
+
     def urand(shape, seed, dtype=torch.float64):
         g = torch.Generator(device="cuda")
         g.manual_seed(seed)
         return (torch.rand(shape, dtype=dtype, device="cuda", generator=g) * 2 - 1)
 
-    # ---- DGEMM 1024^3 NN alpha=1.5 beta=0.5 (native), DMMCH-style ratio
-    n = 1024
-    A, B, C0 = urand((n, n), 1), urand((n, n), 2), urand((n, n), 3)
-    Cd = C0.clone()
-    ms = _time_dev(torch, stream, lambda: check(lib.gb_dgemm_native_dev(
-        b"N", b"N", n, n, n, 1.5, A.data_ptr(), n, B.data_ptr(), n, 0.5, Cd.data_ptr(), n)))
-    Cd.copy_(C0)
-    check(lib.gb_dgemm_native_dev(b"N", b"N", n, n, n, 1.5, A.data_ptr(), n, B.data_ptr(), n, 0.5,
-                                  Cd.data_ptr(), n))
-    torch.cuda.synchronize()
-    # torch tensors hold the column-major matrices transposed: C^T = B^T A^T
-    Ah, Bh, Ch = A.cpu().numpy().T, B.cpu().numpy().T, C0.cpu().numpy().T
-    ref = 1.5 * (Ah @ Bh) + 0.5 * Ch
-    G = 1.5 * (np.abs(Ah) @ np.abs(Bh)) + 0.5 * np.abs(Ch)
-    ratio = float(np.max(np.abs(Cd.cpu().numpy().T - ref) / (eps * G)))
-    _emit({"suite": "dgemm_1024", "workload": "DGEMM NN 1024^3 alpha=1.5 beta=0.5, native FP64",
-           "value": 2 * n ** 3 / ms / 1e9, "unit": UNIT, "ms": ms,
-           "dmmch_ratio_eps": ratio, "dmmch_bound": 2 * (n + 2)})
-    del A, B, C0, Cd
+    if want("dgemm1024"):
+        # ---- DGEMM 1024^3 NN alpha=1.5 beta=0.5 (native), DMMCH-style ratio
+        n = 1024
+        A, B, C0 = urand((n, n), 1), urand((n, n), 2), urand((n, n), 3)
+        Cd = C0.clone()
+        ms = _time_dev(torch, stream, lambda: check(lib.gb_dgemm_native_dev(
+            b"N", b"N", n, n, n, 1.5, A.data_ptr(), n, B.data_ptr(), n, 0.5, Cd.data_ptr(), n)))
+        Cd.copy_(C0)
+        check(lib.gb_dgemm_native_dev(b"N", b"N", n, n, n, 1.5, A.data_ptr(), n, B.data_ptr(), n, 0.5,
+                                      Cd.data_ptr(), n))
+        torch.cuda.synchronize()
+        # torch tensors hold the column-major matrices transposed: C^T = B^T A^T
+        Ah, Bh, Ch = A.cpu().numpy().T, B.cpu().numpy().T, C0.cpu().numpy().T
+        ref = 1.5 * (Ah @ Bh) + 0.5 * Ch
+        G = 1.5 * (np.abs(Ah) @ np.abs(Bh)) + 0.5 * np.abs(Ch)
+        ratio = float(np.max(np.abs(Cd.cpu().numpy().T - ref) / (eps * G)))
+        _emit({"suite": "dgemm_1024", "workload": "DGEMM NN 1024^3 alpha=1.5 beta=0.5, native FP64",
+               "value": 2 * n ** 3 / ms / 1e9, "unit": UNIT, "ms": ms,
+               "dmmch_ratio_eps": ratio, "dmmch_bound": 2 * (n + 2)})
+        del A, B, C0, Cd
 
-    # ---- native DGEMM sweep, lda = M + 8, all four transposes
-    for n in (2048, 4096, 8192, 16384):
-        ld = n + 8
-        A, B, Cd = urand((n, ld), 10 + n), urand((n, ld), 11 + n), torch.zeros((n, ld), dtype=torch.float64, device="cuda")
-        for ta, tb in (("N", "N"), ("N", "T"), ("T", "N"), ("T", "T")):
-            if n == 16384 and (ta, tb) != ("N", "N"):
-                continue  # ~7 s per native call at 16384: one combination
-            reps = 1 if n == 16384 else 2
-            ms = _time_dev(torch, stream, lambda: check(lib.gb_dgemm_native_dev(
-                ta.encode(), tb.encode(), n, n, n, 1.0, A.data_ptr(), ld, B.data_ptr(), ld, 0.0,
-                Cd.data_ptr(), ld)), reps=reps, warm=0 if n == 16384 else 1)
-            _emit({"suite": f"dgemm_native_{n}_{ta}{tb}",
-                   "workload": f"DGEMM {ta}{tb} M=N=K={n}, lda=ldb=ldc={ld}, native FP64",
-                   "value": 2 * n ** 3 / ms / 1e9, "unit": UNIT, "ms": ms})
-        del A, B, Cd
+    if want("dgemm_sweep"):
+        # ---- native DGEMM sweep, lda = M + 8, all four transposes
+        for n in (2048, 4096, 8192, 16384):
+            ld = n + 8
+            A, B, Cd = urand((n, ld), 10 + n), urand((n, ld), 11 + n), torch.zeros((n, ld), dtype=torch.float64, device="cuda")
+            for ta, tb in (("N", "N"), ("N", "T"), ("T", "N"), ("T", "T")):
+                if n == 16384 and (ta, tb) != ("N", "N"):
+                    continue  # ~7 s per native call at 16384: one combination
+                reps = 1 if n == 16384 else 2
+                ms = _time_dev(torch, stream, lambda: check(lib.gb_dgemm_native_dev(
+                    ta.encode(), tb.encode(), n, n, n, 1.0, A.data_ptr(), ld, B.data_ptr(), ld, 0.0,
+                    Cd.data_ptr(), ld)), reps=reps, warm=0 if n == 16384 else 1)
+                _emit({"suite": f"dgemm_native_{n}_{ta}{tb}",
+                       "workload": f"DGEMM {ta}{tb} M=N=K={n}, lda=ldb=ldc={ld}, native FP64",
+                       "value": 2 * n ** 3 / ms / 1e9, "unit": UNIT, "ms": ms})
+            del A, B, Cd
 
-    # ---- SGEMM 16384^3 FP32: tensor-core (bf16x3) and SIMT forms
-    n = 16384
-    A, B = urand((n, n), 20, torch.float32), urand((n, n), 21, torch.float32)
-    Cs = torch.zeros((n, n), dtype=torch.float32, device="cuda")
-    res = {}
-    for mode, name in ((2, "tensor_bf16x3"), (1, "simt_fp32")):
-        lib.gb_set_sgemm_mode(mode)
-        res[name] = _time_dev(torch, stream, lambda: check(lib.gb_sgemm_dev(
-            b"N", b"N", n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.0, Cs.data_ptr(), n)),
-            reps=2)
-    lib.gb_set_sgemm_mode(0)
-    # accuracy of the tensor form on a 2048-row slab against FP64
-    lib.gb_set_sgemm_mode(2)
-    check(lib.gb_sgemm_dev(b"N", b"N", n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.0,
-                           Cs.data_ptr(), n))
-    lib.gb_set_sgemm_mode(0)
-    torch.cuda.synchronize()
-    rows = 256
-    a64 = A.double()
-    Cref = torch.empty((n, n), dtype=torch.float64, device="cuda")
-    b64 = B.double()
-    check(lib.gb_dgemm_native_dev(b"N", b"N", rows, n, n, 1.0, a64.data_ptr(), n, b64.data_ptr(),
-                                  n, 0.0, Cref.data_ptr(), n))
-    Gs = torch.empty_like(Cref)
-    aa, ba = a64.abs(), b64.abs()
-    check(lib.gb_dgemm_native_dev(b"N", b"N", rows, n, n, 1.0, aa.data_ptr(), n, ba.data_ptr(),
-                                  n, 0.0, Gs.data_ptr(), n))
-    torch.cuda.synchronize()
-    # column-major rows 0..rows-1 are the first `rows` entries of each torch row
-    diff = (Cs.double()[:, :rows] - Cref[:, :rows]).abs() / Gs[:, :rows]
-    feps = float(np.finfo(np.float32).eps)
-    _emit({"suite": "sgemm_16384", "workload": "SGEMM NN 16384^3 FP32",
-           "value": 2 * n ** 3 / res["tensor_bf16x3"] / 1e9, "unit": UNIT,
-           "ms": res["tensor_bf16x3"], "method": "bf16x3 split, six tcgen05 products, FP32 TMEM",
-           "simt_fp32": {"value": 2 * n ** 3 / res["simt_fp32"] / 1e9, "ms": res["simt_fp32"]},
-           "componentwise_err_fp32_eps_first_256_rows": float(diff.max()) / feps,
-           "bound_k_plus_2": n + 2})
-    del A, B, Cs, a64, b64, aa, ba, Cref, Gs, diff
+    if want("sgemm"):
+        # ---- SGEMM 16384^3 FP32: tensor-core (bf16x3) and SIMT forms
+        n = 16384
+        A, B = urand((n, n), 20, torch.float32), urand((n, n), 21, torch.float32)
+        Cs = torch.zeros((n, n), dtype=torch.float32, device="cuda")
+        res = {}
+        for mode, name in ((2, "tensor_bf16x3"), (1, "simt_fp32")):
+            lib.gb_set_sgemm_mode(mode)
+            res[name] = _time_dev(torch, stream, lambda: check(lib.gb_sgemm_dev(
+                b"N", b"N", n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.0, Cs.data_ptr(), n)),
+                reps=2)
+        lib.gb_set_sgemm_mode(0)
+        # accuracy of the tensor form on a 2048-row slab against FP64
+        lib.gb_set_sgemm_mode(2)
+        check(lib.gb_sgemm_dev(b"N", b"N", n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.0,
+                               Cs.data_ptr(), n))
+        lib.gb_set_sgemm_mode(0)
+        torch.cuda.synchronize()
+        rows = 256
+        a64 = A.double()
+        Cref = torch.empty((n, n), dtype=torch.float64, device="cuda")
+        b64 = B.double()
+        check(lib.gb_dgemm_native_dev(b"N", b"N", rows, n, n, 1.0, a64.data_ptr(), n, b64.data_ptr(),
+                                      n, 0.0, Cref.data_ptr(), n))
+        Gs = torch.empty_like(Cref)
+        aa, ba = a64.abs(), b64.abs()
+        check(lib.gb_dgemm_native_dev(b"N", b"N", rows, n, n, 1.0, aa.data_ptr(), n, ba.data_ptr(),
+                                      n, 0.0, Gs.data_ptr(), n))
+        torch.cuda.synchronize()
+        # column-major rows 0..rows-1 are the first `rows` entries of each torch row
+        diff = (Cs.double()[:, :rows] - Cref[:, :rows]).abs() / Gs[:, :rows]
+        feps = float(np.finfo(np.float32).eps)
+        _emit({"suite": "sgemm_16384", "workload": "SGEMM NN 16384^3 FP32",
+               "value": 2 * n ** 3 / res["tensor_bf16x3"] / 1e9, "unit": UNIT,
+               "ms": res["tensor_bf16x3"], "method": "bf16x3 split, six tcgen05 products, FP32 TMEM",
+               "simt_fp32": {"value": 2 * n ** 3 / res["simt_fp32"] / 1e9, "ms": res["simt_fp32"]},
+               "componentwise_err_fp32_eps_first_256_rows": float(diff.max()) / feps,
+               "bound_k_plus_2": n + 2})
+        del A, B, Cs, a64, b64, aa, ba, Cref, Gs, diff
 
-    # ---- DTRSM Left/Lower/NoTrans/NonUnit 8192^2, diagonal n + U(0,1)
-    n = 8192
-    L = urand((n, n), 30)
-    L = torch.tril(L.T, -1).T.contiguous()  # strictly lower in column-major
-    g = torch.Generator(device="cuda")
-    g.manual_seed(31)
-    L.view(-1)[:: n + 1] = n + torch.rand(n, dtype=torch.float64, device="cuda", generator=g)
-    B0 = urand((n, n), 32)
-    Bt = B0.clone()
-    ms = _time_dev(torch, stream, lambda: check(lib.gb_dtrsm_dev(
-        b"L", b"L", b"N", b"N", n, n, 1.0, L.data_ptr(), n, Bt.data_ptr(), n)), reps=2)
-    _emit({"suite": "dtrsm_8192", "workload": "DTRSM LLNN M=N=8192, native FP64",
-           "value": n ** 3 / ms / 1e9, "unit": UNIT, "ms": ms})
-    del L, B0, Bt
+    if want("dtrsm"):
+        # ---- DTRSM Left/Lower/NoTrans/NonUnit 8192^2, diagonal n + U(0,1)
+        n = 8192
+        L = urand((n, n), 30)
+        L = torch.tril(L.T, -1).T.contiguous()  # strictly lower in column-major
+        g = torch.Generator(device="cuda")
+        g.manual_seed(31)
+        L.view(-1)[:: n + 1] = n + torch.rand(n, dtype=torch.float64, device="cuda", generator=g)
+        B0 = urand((n, n), 32)
+        Bt = B0.clone()
+        Lnorm = float(L.abs().sum(dim=0).max())  # row sums of the column-major L
+        R = torch.empty((512, n), dtype=torch.float64, device="cuda")  # column-major n x 512
+        trsm = {}
+        for mode, name in ((0, "native"), (1, "emulated")):
+            lib.gb_set_dgemm_mode(mode)
+            ms = _time_dev(torch, stream, lambda: check(lib.gb_dtrsm_dev(
+                b"L", b"L", b"N", b"N", n, n, 1.0, L.data_ptr(), n, Bt.data_ptr(), n)), reps=2)
+            # residual of a fresh solve, first 512 right-hand sides:
+            # max_j |L x_j - b_j|_inf / (|L|_inf |x_j|_inf), in units of eps
+            Bt.copy_(B0)
+            check(lib.gb_dtrsm_dev(b"L", b"L", b"N", b"N", n, n, 1.0, L.data_ptr(), n,
+                                   Bt.data_ptr(), n))
+            lib.gb_set_dgemm_mode(0)
+            R.copy_(B0[:512])
+            check(lib.gb_dgemm_native_dev(b"N", b"N", n, 512, n, 1.0, L.data_ptr(), n, Bt.data_ptr(),
+                                          n, -1.0, R.data_ptr(), n))
+            torch.cuda.synchronize()
+            xn = Bt[:512].abs().amax(dim=1)
+            res = float((R.abs().amax(dim=1) / (Lnorm * xn)).max()) / eps
+            trsm[name] = {"value": n ** 3 / ms / 1e9, "ms": ms, "residual_eps": res}
+        _emit({"suite": "dtrsm_8192", "workload": "DTRSM LLNN M=N=8192, native FP64",
+               "value": trsm["native"]["value"], "unit": UNIT, "ms": trsm["native"]["ms"],
+               "residual_eps": trsm["native"]["residual_eps"]})
+        _emit({"suite": "dtrsm_8192_emulated",
+               "workload": "DTRSM LLNN M=N=8192, emulated FP64 (recursive, 256-wide native leaves, "
+                           "off-diagonal blocks on the emulated DGEMM, automatic choice)",
+               "unit": UNIT, **trsm["emulated"], "native_fp64_ms": trsm["native"]["ms"],
+               "speedup_over_native": trsm["native"]["ms"] / trsm["emulated"]["ms"]})
+        del L, B0, Bt, R
 
-    # ---- emulated DGEMM: 8-bit slices 5..8, exponent spread e in {0, 8, 16}
-    for n in (8192, 16384):
-        for e in (0, 8, 16):
-            gA, gB = torch.Generator(device="cuda"), torch.Generator(device="cuda")
-            gA.manual_seed(40 + e)
-            gB.manual_seed(50 + e)
-            A = urand((n, n), 60 + e)
-            B = urand((n, n), 70 + e)
-            if e:
-                A = torch.ldexp(A, torch.randint(-e, e + 1, (n, n), device="cuda", generator=gA))
-                B = torch.ldexp(B, torch.randint(-e, e + 1, (n, n), device="cuda", generator=gB))
-            Cn = None
-            if n == 8192 or e == 0:
-                Cn = torch.empty((n, n), dtype=torch.float64, device="cuda")
-                t0 = time.perf_counter()
-                check(lib.gb_dgemm_native_dev(b"N", b"N", n, n, n, 1.0, A.data_ptr(), n,
-                                              B.data_ptr(), n, 0.0, Cn.data_ptr(), n))
-                torch.cuda.synchronize()
-                native_ms = (time.perf_counter() - t0) * 1e3
-                Ga = torch.empty_like(Cn)
-                Aa, Ba = A.abs(), B.abs()
-                check(lib.gb_dgemm_native_dev(b"N", b"N", n, n, n, 1.0, Aa.data_ptr(), n,
-                                              Ba.data_ptr(), n, 0.0, Ga.data_ptr(), n))
-                del Aa, Ba
-            Ce = torch.empty((n, n), dtype=torch.float64, device="cuda")
-            # S = 0: the automatic choice (the library default: modular
-            # scheme or slice count per tile), "0s": automatic with digit
-            # slices only
-            variants = (0, "0s", 5, 6, 7, 8) if n == 8192 else (0, "0s", 7)
-            for S in variants:
-                modular = 0 if S == "0s" else 1
-                Sv = 0 if S == "0s" else S
-                lib.gb_set_ozaki_modular(modular)
-                ms = _time_dev(torch, stream, lambda: check(lib.gb_dgemm_emulated_dev(
-                    b"N", b"N", n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.0,
-                    Ce.data_ptr(), n, Sv)), reps=3 if n == 8192 else 2)
-                lib.gb_set_ozaki_modular(1)
-                tag = f"s{S}" if Sv else ("auto" if modular else "auto_slices")
-                chosen_m, chosen_s = lib.gb_last_ozaki_moduli(), lib.gb_last_ozaki_slices()
-                how = f"{Sv} slices" if Sv else \
-                    f"automatic choice ({chosen_m} moduli, {chosen_s} slices)"
-                d = {"suite": f"dgemm_emulated_{n}_e{e}_{tag}",
-                     "workload": f"emulated DGEMM NN {n}^3, A,B = U.*2^E, E in [-{e},{e}], {how}",
-                     "value": 2 * n ** 3 / ms / 1e9, "unit": UNIT, "ms": ms}
-                if not Sv:
-                    d["slices_chosen"] = chosen_s
-                    d["moduli_chosen"] = chosen_m
-                if Cn is not None:
+    if want("dsyrk"):
+        # ---- DSYRK Lower/NoTrans n = k = 8192: native FP64 and emulated FP64
+        n = 8192
+        A = urand((n, n), 33)
+        C0 = urand((n, n), 34)
+        syrk = {}
+        for mode, name in ((0, "native"), (1, "emulated")):
+            lib.gb_set_dgemm_mode(mode)
+            Cs = C0.clone()
+            ms = _time_dev(torch, stream, lambda: check(lib.gb_dsyrk_dev(
+                b"L", b"N", n, n, -1.0, A.data_ptr(), n, 1.0, Cs.data_ptr(), n)), reps=2)
+            Cs.copy_(C0)
+            check(lib.gb_dsyrk_dev(b"L", b"N", n, n, -1.0, A.data_ptr(), n, 1.0, Cs.data_ptr(), n))
+            syrk[name] = (ms, Cs)
+        lib.gb_set_dgemm_mode(0)
+        torch.cuda.synchronize()
+        # normwise difference on the stored (lower, column-major) triangle,
+        # relative to max(|A||A^T| + |C|) (its largest entries lie on the
+        # diagonal, sum_l A(i,l)^2, by Cauchy-Schwarz; |C| <= 1)
+        low = torch.triu(torch.ones(n, n, dtype=torch.bool, device="cuda"))  # lower of col-major
+        diff = float(((syrk["emulated"][1] - syrk["native"][1]).abs() * low).max())
+        gmax = float((A * A).sum(dim=0).max()) + 1.0
+        for name in ("native", "emulated"):
+            d = {"suite": "dsyrk_8192" + ("" if name == "native" else "_emulated"),
+                 "workload": f"DSYRK LN n=k=8192, {name} FP64", "unit": UNIT,
+                 "value": n ** 3 / syrk[name][0] / 1e9, "ms": syrk[name][0]}
+            if name == "emulated":
+                d["normwise_err_vs_native_eps"] = diff / gmax / eps
+                d["native_fp64_ms"] = syrk["native"][0]
+                d["speedup_over_native"] = syrk["native"][0] / syrk["emulated"][0]
+            _emit(d)
+        del A, C0, syrk, low
+        torch.cuda.empty_cache()
+
+    if want("emulated"):
+        # ---- emulated DGEMM: 8-bit slices 5..8, exponent spread e in {0, 8, 16}
+        for n in (8192, 16384):
+            for e in (0, 8, 16):
+                gA, gB = torch.Generator(device="cuda"), torch.Generator(device="cuda")
+                gA.manual_seed(40 + e)
+                gB.manual_seed(50 + e)
+                A = urand((n, n), 60 + e)
+                B = urand((n, n), 70 + e)
+                if e:
+                    A = torch.ldexp(A, torch.randint(-e, e + 1, (n, n), device="cuda", generator=gA))
+                    B = torch.ldexp(B, torch.randint(-e, e + 1, (n, n), device="cuda", generator=gB))
+                Cn = None
+                if n == 8192 or e == 0:
+                    Cn = torch.empty((n, n), dtype=torch.float64, device="cuda")
+                    t0 = time.perf_counter()
+                    check(lib.gb_dgemm_native_dev(b"N", b"N", n, n, n, 1.0, A.data_ptr(), n,
+                                                  B.data_ptr(), n, 0.0, Cn.data_ptr(), n))
                     torch.cuda.synchronize()
-                    diff = (Ce - Cn).abs()
-                    d["normwise_err_vs_native_eps"] = float(diff.max() / Ga.max()) / eps
-                    d["componentwise_err_vs_native_eps"] = float((diff / Ga).max()) / eps
-                    d["native_fp64_ms"] = native_ms
-                    d["speedup_over_native"] = native_ms / ms
-                _emit(d)
-            del A, B, Ce
-            if Cn is not None:
-                del Cn, Ga
+                    native_ms = (time.perf_counter() - t0) * 1e3
+                    Ga = torch.empty_like(Cn)
+                    Aa, Ba = A.abs(), B.abs()
+                    check(lib.gb_dgemm_native_dev(b"N", b"N", n, n, n, 1.0, Aa.data_ptr(), n,
+                                                  Ba.data_ptr(), n, 0.0, Ga.data_ptr(), n))
+                    del Aa, Ba
+                Ce = torch.empty((n, n), dtype=torch.float64, device="cuda")
+                # S = 0: the automatic choice (the library default: modular
+                # scheme or slice count per tile), "0s": automatic with digit
+                # slices only
+                variants = (0, "0s", 5, 6, 7, 8) if n == 8192 else (0, "0s", 7)
+                for S in variants:
+                    modular = 0 if S == "0s" else 1
+                    Sv = 0 if S == "0s" else S
+                    lib.gb_set_ozaki_modular(modular)
+                    ms = _time_dev(torch, stream, lambda: check(lib.gb_dgemm_emulated_dev(
+                        b"N", b"N", n, n, n, 1.0, A.data_ptr(), n, B.data_ptr(), n, 0.0,
+                        Ce.data_ptr(), n, Sv)), reps=3 if n == 8192 else 2)
+                    lib.gb_set_ozaki_modular(1)
+                    tag = f"s{S}" if Sv else ("auto" if modular else "auto_slices")
+                    chosen_m, chosen_s = lib.gb_last_ozaki_moduli(), lib.gb_last_ozaki_slices()
+                    how = f"{Sv} slices" if Sv else \
+                        f"automatic choice ({chosen_m} moduli, {chosen_s} slices)"
+                    d = {"suite": f"dgemm_emulated_{n}_e{e}_{tag}",
+                         "workload": f"emulated DGEMM NN {n}^3, A,B = U.*2^E, E in [-{e},{e}], {how}",
+                         "value": 2 * n ** 3 / ms / 1e9, "unit": UNIT, "ms": ms}
+                    if not Sv:
+                        d["slices_chosen"] = chosen_s
+                        d["moduli_chosen"] = chosen_m
+                    if Cn is not None:
+                        torch.cuda.synchronize()
+                        diff = (Ce - Cn).abs()
+                        d["normwise_err_vs_native_eps"] = float(diff.max() / Ga.max()) / eps
+                        d["componentwise_err_vs_native_eps"] = float((diff / Ga).max()) / eps
+                        d["native_fp64_ms"] = native_ms
+                        d["speedup_over_native"] = native_ms / ms
+                    _emit(d)
+                del A, B, Ce
+                if Cn is not None:
+                    del Cn, Ga
+                torch.cuda.empty_cache()
+
+    if want("complex"):
+        # ---- complex GEMM 8192^3 NN: ZGEMM (4M embedding) native and emulated,
+        # ZGEMM3M emulated, CGEMM / CGEMM3M on the tensor-core FP32 engine;
+        # rates count 8 n^3 real flops per complex GEMM (3M forms: effective rate)
+        n = 8192
+        one = np.array([1.0, 0.0])
+        zero = np.array([0.0, 0.0])
+        Az = torch.complex(urand((n, n), 80), urand((n, n), 81))
+        Bz = torch.complex(urand((n, n), 82), urand((n, n), 83))
+        Cn = torch.empty_like(Az)
+        Ce = torch.empty_like(Az)
+
+        def zcall(fn, Cout):
+            return lambda: check(getattr(lib, fn)(b"N", b"N", n, n, n, one.ctypes.data, Az.data_ptr(),
+                                                  n, Bz.data_ptr(), n, zero.ctypes.data,
+                                                  Cout.data_ptr(), n))
+        zres = {}
+        lib.gb_set_dgemm_mode(0)
+        zres["zgemm_native"] = _time_dev(torch, stream, zcall("gb_zgemm_dev", Cn), reps=1, warm=0)
+        lib.gb_set_dgemm_mode(1)
+        # error scale: max of |A||B| (complex moduli), the DMMCH denominator
+        Am, Bm = Az.abs().contiguous(), Bz.abs().contiguous()
+        Gz = torch.empty((n, n), dtype=torch.float64, device="cuda")
+        check(lib.gb_dgemm_native_dev(b"N", b"N", n, n, n, 1.0, Am.data_ptr(), n, Bm.data_ptr(), n,
+                                      0.0, Gz.data_ptr(), n))
+        torch.cuda.synchronize()
+        gmax = float(Gz.max())
+        del Am, Bm, Gz
+        zres["zgemm_emulated"] = _time_dev(torch, stream, zcall("gb_zgemm_dev", Ce), reps=3)
+        torch.cuda.synchronize()
+        zerr = float((Ce - Cn).abs().max()) / gmax / eps
+        zres["zgemm3m_emulated"] = _time_dev(torch, stream, zcall("gb_zgemm3m_dev", Ce), reps=3)
+        torch.cuda.synchronize()
+        z3err = float((Ce - Cn).abs().max()) / gmax / eps
+        lib.gb_set_dgemm_mode(0)
+        for key, err in (("zgemm_native", None), ("zgemm_emulated", zerr), ("zgemm3m_emulated", z3err)):
+            d = {"suite": f"{key}_{n}", "workload": f"{key.split('_')[0].upper()} NN {n}^3 complex128, "
+                 f"{key.split('_')[1]} FP64 engine", "value": 8 * n ** 3 / zres[key] / 1e9,
+                 "unit": UNIT, "ms": zres[key], "flops_counted": "8 n^3"}
+            if err is not None:
+                d["normwise_err_vs_native_zgemm_eps_of_max_AB"] = err
+                d["speedup_over_native_zgemm"] = zres["zgemm_native"] / zres[key]
+            _emit(d)
+        del Az, Bz, Cn, Ce
+        Ac = torch.complex(urand((n, n), 84, torch.float32), urand((n, n), 85, torch.float32))
+        Bc = torch.complex(urand((n, n), 86, torch.float32), urand((n, n), 87, torch.float32))
+        Cc = torch.empty_like(Ac)
+        onef, zerof = one.astype(np.float32), zero.astype(np.float32)
+        for fn in ("gb_cgemm_dev", "gb_cgemm3m_dev"):
+            ms = _time_dev(torch, stream, lambda: check(getattr(lib, fn)(
+                b"N", b"N", n, n, n, onef.ctypes.data, Ac.data_ptr(), n, Bc.data_ptr(), n,
+                zerof.ctypes.data, Cc.data_ptr(), n)), reps=3)
+            name = fn[3:-4]
+            _emit({"suite": f"{name}_{n}", "workload": f"{name.upper()} NN {n}^3 complex64, "
+                   "bf16x3 tensor-core FP32 engine", "value": 8 * n ** 3 / ms / 1e9, "unit": UNIT,
+                   "ms": ms, "flops_counted": "8 n^3"})
+        del Ac, Bc, Cc
+        torch.cuda.empty_cache()
+
+    if want("dgesv"):
+        # ---- DGESV N in {8192, 16384, 32768}, NRHS in {1, 64}: mixed vs native
+        for n in (8192, 16384, 32768):
+            A = urand((n, n), 80 + n)
+            ipiv = torch.zeros(n, dtype=torch.int32, device="cuda")
+            dinfo = torch.zeros(1, dtype=torch.int32, device="cuda")
+            Af = A.clone()
+            t0 = time.perf_counter()
+            check(lib.gb_dgetrf_dev(n, n, Af.data_ptr(), n, ipiv.data_ptr(), dinfo.data_ptr()))
+            torch.cuda.synchronize()
+            t_getrf = time.perf_counter() - t0
+            for nrhs in (1, 64):
+                Bm = urand((nrhs, n), 90 + nrhs)
+                Xn = Bm.clone()
+                t0 = time.perf_counter()
+                check(lib.gb_dgetrs_dev(b"N", n, nrhs, Af.data_ptr(), n, ipiv.data_ptr(),
+                                        Xn.data_ptr(), n))
+                torch.cuda.synchronize()
+                t_native = t_getrf + time.perf_counter() - t0
+                X = torch.zeros_like(Bm)
+                p2 = torch.zeros(n, dtype=torch.int32, device="cuda")
+                it, info = C.c_int(0), C.c_int(0)
+
+                Aw = A.clone()  # a fallback would overwrite its A with the FP64 LU
+
+                def mixed():
+                    check(lib.gb_dsgesv_dev(n, nrhs, Aw.data_ptr(), n, p2.data_ptr(), Bm.data_ptr(),
+                                            n, X.data_ptr(), n, C.byref(it), C.byref(info)))
+
+                mixed()
+                torch.cuda.synchronize()
+                ts = []
+                for _ in range(2 if n == 32768 else 3):
+                    t0 = time.perf_counter()
+                    mixed()
+                    torch.cuda.synchronize()
+                    ts.append(time.perf_counter() - t0)
+                t_mixed = statistics.median(ts)
+                R = Bm.clone()
+                check(lib.gb_dgemm_native_dev(b"N", b"N", n, nrhs, n, -1.0, A.data_ptr(), n,
+                                              X.data_ptr(), n, 1.0, R.data_ptr(), n))
+                torch.cuda.synchronize()
+                anorm = float(A.abs().sum(dim=0).max())
+                berr = float((R.abs().amax(dim=1) / (anorm * X.abs().amax(dim=1) + Bm.abs().amax(dim=1))).max())
+                flops = 2.0 / 3.0 * n ** 3 + 2.0 * n * n * nrhs
+                _emit({"suite": f"dgesv_{n}_{nrhs}", "workload": f"DGESV N={n} NRHS={nrhs}, uniform(-1,1)",
+                       "value": flops / t_mixed / 1e12, "unit": UNIT, "ms": t_mixed * 1e3,
+                       "iter": it.value, "info": info.value,
+                       "backward_error_eps_max_over_rhs": berr / eps, "bound_n_eps": n,
+                       "native_fp64": {"value": flops / t_native / 1e12, "ms": t_native * 1e3},
+                       "speedup_mixed_over_native": t_native / t_mixed})
+                del Bm, Xn, X, R, Aw
+            del A, Af
             torch.cuda.empty_cache()
 
-    # ---- complex GEMM 8192^3 NN: ZGEMM (4M embedding) native and emulated,
-    # ZGEMM3M emulated, CGEMM / CGEMM3M on the tensor-core FP32 engine;
-    # rates count 8 n^3 real flops per complex GEMM (3M forms: effective rate)
-    n = 8192
-    one = np.array([1.0, 0.0])
-    zero = np.array([0.0, 0.0])
-    Az = torch.complex(urand((n, n), 80), urand((n, n), 81))
-    Bz = torch.complex(urand((n, n), 82), urand((n, n), 83))
-    Cn = torch.empty_like(Az)
-    Ce = torch.empty_like(Az)
-
-    def zcall(fn, Cout):
-        return lambda: check(getattr(lib, fn)(b"N", b"N", n, n, n, one.ctypes.data, Az.data_ptr(),
-                                              n, Bz.data_ptr(), n, zero.ctypes.data,
-                                              Cout.data_ptr(), n))
-    zres = {}
-    lib.gb_set_dgemm_mode(0)
-    zres["zgemm_native"] = _time_dev(torch, stream, zcall("gb_zgemm_dev", Cn), reps=1, warm=0)
-    lib.gb_set_dgemm_mode(1)
-    # error scale: max of |A||B| (complex moduli), the DMMCH denominator
-    Am, Bm = Az.abs().contiguous(), Bz.abs().contiguous()
-    Gz = torch.empty((n, n), dtype=torch.float64, device="cuda")
-    check(lib.gb_dgemm_native_dev(b"N", b"N", n, n, n, 1.0, Am.data_ptr(), n, Bm.data_ptr(), n,
-                                  0.0, Gz.data_ptr(), n))
-    torch.cuda.synchronize()
-    gmax = float(Gz.max())
-    del Am, Bm, Gz
-    zres["zgemm_emulated"] = _time_dev(torch, stream, zcall("gb_zgemm_dev", Ce), reps=3)
-    torch.cuda.synchronize()
-    zerr = float((Ce - Cn).abs().max()) / gmax / eps
-    zres["zgemm3m_emulated"] = _time_dev(torch, stream, zcall("gb_zgemm3m_dev", Ce), reps=3)
-    torch.cuda.synchronize()
-    z3err = float((Ce - Cn).abs().max()) / gmax / eps
-    lib.gb_set_dgemm_mode(0)
-    for key, err in (("zgemm_native", None), ("zgemm_emulated", zerr), ("zgemm3m_emulated", z3err)):
-        d = {"suite": f"{key}_{n}", "workload": f"{key.split('_')[0].upper()} NN {n}^3 complex128, "
-             f"{key.split('_')[1]} FP64 engine", "value": 8 * n ** 3 / zres[key] / 1e9,
-             "unit": UNIT, "ms": zres[key], "flops_counted": "8 n^3"}
-        if err is not None:
-            d["normwise_err_vs_native_zgemm_eps_of_max_AB"] = err
-            d["speedup_over_native_zgemm"] = zres["zgemm_native"] / zres[key]
-        _emit(d)
-    del Az, Bz, Cn, Ce
-    Ac = torch.complex(urand((n, n), 84, torch.float32), urand((n, n), 85, torch.float32))
-    Bc = torch.complex(urand((n, n), 86, torch.float32), urand((n, n), 87, torch.float32))
-    Cc = torch.empty_like(Ac)
-    onef, zerof = one.astype(np.float32), zero.astype(np.float32)
-    for fn in ("gb_cgemm_dev", "gb_cgemm3m_dev"):
-        ms = _time_dev(torch, stream, lambda: check(getattr(lib, fn)(
-            b"N", b"N", n, n, n, onef.ctypes.data, Ac.data_ptr(), n, Bc.data_ptr(), n,
-            zerof.ctypes.data, Cc.data_ptr(), n)), reps=3)
-        name = fn[3:-4]
-        _emit({"suite": f"{name}_{n}", "workload": f"{name.upper()} NN {n}^3 complex64, "
-               "bf16x3 tensor-core FP32 engine", "value": 8 * n ** 3 / ms / 1e9, "unit": UNIT,
-               "ms": ms, "flops_counted": "8 n^3"})
-    del Ac, Bc, Cc
-    torch.cuda.empty_cache()
-
-    # ---- DGESV N in {8192, 16384, 32768}, NRHS in {1, 64}: mixed vs native
-    for n in (8192, 16384, 32768):
-        A = urand((n, n), 80 + n)
-        ipiv = torch.zeros(n, dtype=torch.int32, device="cuda")
-        dinfo = torch.zeros(1, dtype=torch.int32, device="cuda")
-        Af = A.clone()
-        t0 = time.perf_counter()
-        check(lib.gb_dgetrf_dev(n, n, Af.data_ptr(), n, ipiv.data_ptr(), dinfo.data_ptr()))
-        torch.cuda.synchronize()
-        t_getrf = time.perf_counter() - t0
-        for nrhs in (1, 64):
-            Bm = urand((nrhs, n), 90 + nrhs)
-            Xn = Bm.clone()
-            t0 = time.perf_counter()
-            check(lib.gb_dgetrs_dev(b"N", n, nrhs, Af.data_ptr(), n, ipiv.data_ptr(),
-                                    Xn.data_ptr(), n))
-            torch.cuda.synchronize()
-            t_native = t_getrf + time.perf_counter() - t0
+    if want("illcond"):
+        # ---- ill-conditioned DGESV (GMRES-IR): A = U diag(logspace(0,-kappa)) V^T
+        n = 4096
+        rng = np.random.default_rng(123)
+        U, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        V, _ = np.linalg.qr(rng.standard_normal((n, n)))
+        for kappa in (4, 8, 12):
+            sv = np.logspace(0, -kappa, n)
+            Ah = (U * sv) @ V.T                   # row-major numpy matrix
+            A = torch.from_numpy(np.ascontiguousarray(Ah.T)).cuda()  # column-major buffer
+            Aw = A.clone()  # the FP64 fallback overwrites its A with the LU factors
+            Bm = urand((1, n), 95)
             X = torch.zeros_like(Bm)
             p2 = torch.zeros(n, dtype=torch.int32, device="cuda")
             it, info = C.c_int(0), C.c_int(0)
-
-            Aw = A.clone()  # a fallback would overwrite its A with the FP64 LU
-
-            def mixed():
-                check(lib.gb_dsgesv_dev(n, nrhs, Aw.data_ptr(), n, p2.data_ptr(), Bm.data_ptr(),
-                                        n, X.data_ptr(), n, C.byref(it), C.byref(info)))
-
-            mixed()
             torch.cuda.synchronize()
-            ts = []
-            for _ in range(2 if n == 32768 else 3):
-                t0 = time.perf_counter()
-                mixed()
-                torch.cuda.synchronize()
-                ts.append(time.perf_counter() - t0)
-            t_mixed = statistics.median(ts)
+            t0 = time.perf_counter()
+            check(lib.gb_dsgesv_dev(n, 1, Aw.data_ptr(), n, p2.data_ptr(), Bm.data_ptr(), n,
+                                    X.data_ptr(), n, C.byref(it), C.byref(info)))
+            torch.cuda.synchronize()
+            t_mixed = time.perf_counter() - t0
             R = Bm.clone()
-            check(lib.gb_dgemm_native_dev(b"N", b"N", n, nrhs, n, -1.0, A.data_ptr(), n,
-                                          X.data_ptr(), n, 1.0, R.data_ptr(), n))
+            check(lib.gb_dgemm_native_dev(b"N", b"N", n, 1, n, -1.0, A.data_ptr(), n, X.data_ptr(), n,
+                                          1.0, R.data_ptr(), n))
             torch.cuda.synchronize()
             anorm = float(A.abs().sum(dim=0).max())
-            berr = float((R.abs().amax(dim=1) / (anorm * X.abs().amax(dim=1) + Bm.abs().amax(dim=1))).max())
-            flops = 2.0 / 3.0 * n ** 3 + 2.0 * n * n * nrhs
-            _emit({"suite": f"dgesv_{n}_{nrhs}", "workload": f"DGESV N={n} NRHS={nrhs}, uniform(-1,1)",
-                   "value": flops / t_mixed / 1e12, "unit": UNIT, "ms": t_mixed * 1e3,
-                   "iter": it.value, "info": info.value,
-                   "backward_error_eps_max_over_rhs": berr / eps, "bound_n_eps": n,
-                   "native_fp64": {"value": flops / t_native / 1e12, "ms": t_native * 1e3},
-                   "speedup_mixed_over_native": t_native / t_mixed})
-            del Bm, Xn, X, R, Aw
-        del A, Af
+            berr = float(R.abs().max() / (anorm * X.abs().max() + Bm.abs().max()))
+            _emit({"suite": f"dgesv_illcond_{n}_kappa1e{kappa}",
+                   "workload": f"DGESV N={n} NRHS=1, A = U diag(logspace(0,-{kappa})) V^T (seeded QR)",
+                   "ms": t_mixed * 1e3, "iter": it.value, "info": info.value,
+                   "backward_error_eps": berr / eps, "bound_n_eps": n,
+                   "path": "FP32 LU + IR" if 0 <= it.value <= 30 else
+                           ("GMRES-IR" if it.value >= 100 else "FP64-accurate fallback")})
+            del A, Aw, Bm, X, R
+        del U, V
+
+    if want("dpotrf"):
+        # ---- DPOTRF N=32768, A = B B^T / N + I (B uniform), native and emulated updates
+        n = 32768
+        Bm = urand((n, n), 99)
+        A0 = torch.empty((n, n), dtype=torch.float64, device="cuda")
+        check(lib.gb_dgemm_emulated_dev(b"N", b"T", n, n, n, 1.0 / n, Bm.data_ptr(), n, Bm.data_ptr(),
+                                        n, 0.0, A0.data_ptr(), n, 8))
+        A0.view(-1)[:: n + 1] += 1.0
+        del Bm
         torch.cuda.empty_cache()
-
-    # ---- ill-conditioned DGESV (GMRES-IR): A = U diag(logspace(0,-kappa)) V^T
-    n = 4096
-    rng = np.random.default_rng(123)
-    U, _ = np.linalg.qr(rng.standard_normal((n, n)))
-    V, _ = np.linalg.qr(rng.standard_normal((n, n)))
-    for kappa in (4, 8, 12):
-        sv = np.logspace(0, -kappa, n)
-        Ah = (U * sv) @ V.T                   # row-major numpy matrix
-        A = torch.from_numpy(np.ascontiguousarray(Ah.T)).cuda()  # column-major buffer
-        Aw = A.clone()  # the FP64 fallback overwrites its A with the LU factors
-        Bm = urand((1, n), 95)
+        A = torch.empty_like(A0)
+        dinfo = torch.zeros(1, dtype=torch.int32, device="cuda")
+        out = {}
+        for mode, name in ((1, "emulated_updates"), (0, "native_fp64")):
+            lib.gb_set_dgemm_mode(mode)
+            ts = []
+            for _ in range(2 if mode == 1 else 1):
+                A.copy_(A0)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                check(lib.gb_dpotrf_dev(b"L", n, A.data_ptr(), n, dinfo.data_ptr()))
+                torch.cuda.synchronize()
+                ts.append(time.perf_counter() - t0)
+            out[name] = (statistics.median(ts), int(dinfo.item()))
+            if mode == 1:
+                # scaled residual of a 2048-column slab: |A0 - L L^T| / (n eps |A0|)
+                cols = 2048
+                Lw = A.clone()
+                Lw.copy_(torch.triu(Lw))  # column-major lower = torch upper
+                R = A0[:cols].clone()
+                check(lib.gb_dgemm_emulated_dev(b"N", b"T", n, cols, n, -1.0, Lw.data_ptr(), n,
+                                                Lw.data_ptr(), n, 1.0, R.data_ptr(), n, 8))
+                torch.cuda.synchronize()
+                resid = float(R.abs().sum(dim=1).max() / (n * eps * A0.abs().sum(dim=1).max()))
+                del Lw, R
+        lib.gb_set_dgemm_mode(0)
+        # DSPOSV on the same matrix: FP32 Cholesky + FP64 refinement vs native
+        # FP64 DPOTRF + DPOTRS (the native factor time is the one just measured)
+        Bm = urand((1, n), 98)
         X = torch.zeros_like(Bm)
-        p2 = torch.zeros(n, dtype=torch.int32, device="cuda")
         it, info = C.c_int(0), C.c_int(0)
-        torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        check(lib.gb_dsgesv_dev(n, 1, Aw.data_ptr(), n, p2.data_ptr(), Bm.data_ptr(), n,
-                                X.data_ptr(), n, C.byref(it), C.byref(info)))
-        torch.cuda.synchronize()
-        t_mixed = time.perf_counter() - t0
-        R = Bm.clone()
-        check(lib.gb_dgemm_native_dev(b"N", b"N", n, 1, n, -1.0, A.data_ptr(), n, X.data_ptr(), n,
-                                      1.0, R.data_ptr(), n))
-        torch.cuda.synchronize()
-        anorm = float(A.abs().sum(dim=0).max())
-        berr = float(R.abs().max() / (anorm * X.abs().max() + Bm.abs().max()))
-        _emit({"suite": f"dgesv_illcond_{n}_kappa1e{kappa}",
-               "workload": f"DGESV N={n} NRHS=1, A = U diag(logspace(0,-{kappa})) V^T (seeded QR)",
-               "ms": t_mixed * 1e3, "iter": it.value, "info": info.value,
-               "backward_error_eps": berr / eps, "bound_n_eps": n,
-               "path": "FP32 LU + IR" if 0 <= it.value <= 30 else
-                       ("GMRES-IR" if it.value >= 100 else "FP64-accurate fallback")})
-        del A, Aw, Bm, X, R
-    del U, V
-
-    # ---- DPOTRF N=32768, A = B B^T / N + I (B uniform), native and emulated updates
-    n = 32768
-    Bm = urand((n, n), 99)
-    A0 = torch.empty((n, n), dtype=torch.float64, device="cuda")
-    check(lib.gb_dgemm_emulated_dev(b"N", b"T", n, n, n, 1.0 / n, Bm.data_ptr(), n, Bm.data_ptr(),
-                                    n, 0.0, A0.data_ptr(), n, 8))
-    A0.view(-1)[:: n + 1] += 1.0
-    del Bm
-    torch.cuda.empty_cache()
-    A = torch.empty_like(A0)
-    dinfo = torch.zeros(1, dtype=torch.int32, device="cuda")
-    out = {}
-    for mode, name in ((1, "emulated_updates"), (0, "native_fp64")):
-        lib.gb_set_dgemm_mode(mode)
+        A.copy_(A0)  # the mixed path leaves A alone unless it falls back
+        check(lib.gb_dsposv_dev(b"L", n, 1, A.data_ptr(), n, Bm.data_ptr(), n, X.data_ptr(), n,
+                                C.byref(it), C.byref(info)))
         ts = []
-        for _ in range(2 if mode == 1 else 1):
+        for _ in range(2):
             A.copy_(A0)
             torch.cuda.synchronize()
             t0 = time.perf_counter()
-            check(lib.gb_dpotrf_dev(b"L", n, A.data_ptr(), n, dinfo.data_ptr()))
+            check(lib.gb_dsposv_dev(b"L", n, 1, A.data_ptr(), n, Bm.data_ptr(), n, X.data_ptr(), n,
+                                    C.byref(it), C.byref(info)))
             torch.cuda.synchronize()
             ts.append(time.perf_counter() - t0)
-        out[name] = (statistics.median(ts), int(dinfo.item()))
-        if mode == 1:
-            # scaled residual of a 2048-column slab: |A0 - L L^T| / (n eps |A0|)
-            cols = 2048
-            Lw = A.clone()
-            Lw.copy_(torch.triu(Lw))  # column-major lower = torch upper
-            R = A0[:cols].clone()
-            check(lib.gb_dgemm_emulated_dev(b"N", b"T", n, cols, n, -1.0, Lw.data_ptr(), n,
-                                            Lw.data_ptr(), n, 1.0, R.data_ptr(), n, 8))
-            torch.cuda.synchronize()
-            resid = float(R.abs().sum(dim=1).max() / (n * eps * A0.abs().sum(dim=1).max()))
-            del Lw, R
-    lib.gb_set_dgemm_mode(0)
-    # DSPOSV on the same matrix: FP32 Cholesky + FP64 refinement vs native
-    # FP64 DPOTRF + DPOTRS (the native factor time is the one just measured)
-    Bm = urand((1, n), 98)
-    X = torch.zeros_like(Bm)
-    it, info = C.c_int(0), C.c_int(0)
-    A.copy_(A0)  # the mixed path leaves A alone unless it falls back
-    check(lib.gb_dsposv_dev(b"L", n, 1, A.data_ptr(), n, Bm.data_ptr(), n, X.data_ptr(), n,
-                            C.byref(it), C.byref(info)))
-    ts = []
-    for _ in range(2):
-        A.copy_(A0)
+        t_sposv = statistics.median(ts)
+        R = Bm.clone()
+        check(lib.gb_dgemm_native_dev(b"N", b"N", n, 1, n, -1.0, A0.data_ptr(), n, X.data_ptr(), n,
+                                      1.0, R.data_ptr(), n))
         torch.cuda.synchronize()
-        t0 = time.perf_counter()
-        check(lib.gb_dsposv_dev(b"L", n, 1, A.data_ptr(), n, Bm.data_ptr(), n, X.data_ptr(), n,
-                                C.byref(it), C.byref(info)))
-        torch.cuda.synchronize()
-        ts.append(time.perf_counter() - t0)
-    t_sposv = statistics.median(ts)
-    R = Bm.clone()
-    check(lib.gb_dgemm_native_dev(b"N", b"N", n, 1, n, -1.0, A0.data_ptr(), n, X.data_ptr(), n,
-                                  1.0, R.data_ptr(), n))
-    torch.cuda.synchronize()
-    anorm = float(A0.abs().sum(dim=0).max())
-    berr_sposv = float(R.abs().max() / (anorm * X.abs().max() + Bm.abs().max())) / eps
-    flops = n ** 3 / 3.0
-    _emit({"suite": "dsposv_32768_1", "workload": "DSPOSV L N=32768 NRHS=1, A = B B^T/N + I",
-           "value": (flops + 2.0 * n * n) / t_sposv / 1e12, "unit": UNIT, "ms": t_sposv * 1e3,
-           "iter": it.value, "info": info.value, "backward_error_eps": berr_sposv,
-           "bound_n_eps": n,
-           "speedup_over_native_dpotrf": out["native_fp64"][0] / t_sposv})
-    _emit({"suite": "dpotrf_32768", "workload": "DPOTRF L N=32768, A = B B^T/N + I",
-           "value": flops / out["emulated_updates"][0] / 1e12, "unit": UNIT,
-           "ms": out["emulated_updates"][0] * 1e3, "info": out["emulated_updates"][1],
-           "scaled_residual_first_2048_cols": resid, "bound": 10,
-           "native_fp64": {"value": flops / out["native_fp64"][0] / 1e12,
-                           "ms": out["native_fp64"][0] * 1e3, "info": out["native_fp64"][1]},
-           "speedup_emulated_over_native": out["native_fp64"][0] / out["emulated_updates"][0]})
+        anorm = float(A0.abs().sum(dim=0).max())
+        berr_sposv = float(R.abs().max() / (anorm * X.abs().max() + Bm.abs().max())) / eps
+        flops = n ** 3 / 3.0
+        _emit({"suite": "dsposv_32768_1", "workload": "DSPOSV L N=32768 NRHS=1, A = B B^T/N + I",
+               "value": (flops + 2.0 * n * n) / t_sposv / 1e12, "unit": UNIT, "ms": t_sposv * 1e3,
+               "iter": it.value, "info": info.value, "backward_error_eps": berr_sposv,
+               "bound_n_eps": n,
+               "speedup_over_native_dpotrf": out["native_fp64"][0] / t_sposv})
+        _emit({"suite": "dpotrf_32768", "workload": "DPOTRF L N=32768, A = B B^T/N + I",
+               "value": flops / out["emulated_updates"][0] / 1e12, "unit": UNIT,
+               "ms": out["emulated_updates"][0] * 1e3, "info": out["emulated_updates"][1],
+               "scaled_residual_first_2048_cols": resid, "bound": 10,
+               "native_fp64": {"value": flops / out["native_fp64"][0] / 1e12,
+                               "ms": out["native_fp64"][0] * 1e3, "info": out["native_fp64"][1]},
+               "speedup_emulated_over_native": out["native_fp64"][0] / out["emulated_updates"][0]})
 
 
 # --------------------------------------------------------------------------

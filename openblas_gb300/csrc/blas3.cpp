@@ -366,6 +366,8 @@ int dtrsm_device(int side, int uplo, int trans, int unit, int64_t m, int64_t n, 
                  const double *A, int64_t lda, double *B, int64_t ldb, cudaStream_t s);
 int dsyrk_device(int uplo, int trans, int64_t n, int64_t k, double alpha, const double *A,
                  int64_t lda, double beta, double *C, int64_t ldc, cudaStream_t s);
+int dtrsm_select(int side, int uplo, int trans, int unit, int64_t m, int64_t n, double alpha,
+                 const double *A, int64_t lda, double *B, int64_t ldb, cudaStream_t s);
 int gb_dgemm_batch_grouped(int order, const int *ta, const int *tb, const blasint *m,
                            const blasint *n, const blasint *k, const double *alpha,
                            const double **A, const blasint *lda, const double **B,
@@ -381,7 +383,7 @@ static void dtrsm_blocking(int side, int uplo, int trans, int unit, int64_t m, i
   Operand a(A, na, na, lda, 8), b(B, m, n, ldb, 8);
   if (alpha != 0.0 && a.bind(true, s)) return;
   if (b.bind(alpha != 0.0, s)) return;
-  if (dtrsm_device(side, uplo, trans, unit, m, n, alpha, a.d<double>(), a.dld, b.d<double>(),
+  if (dtrsm_select(side, uplo, trans, unit, m, n, alpha, a.d<double>(), a.dld, b.d<double>(),
                    b.dld, s))
     return;
   b.unbind(s);
@@ -1009,7 +1011,7 @@ int gb_dtrsm_dev(char side, char uplo, char transa, char diag, int64_t m, int64_
   int st = ensure_init();
   if (st) return st;
   if (m == 0 || n == 0) return GB_SUCCESS;
-  return dtrsm_device(is, iu, it, id, m, n, alpha, A, lda, B, ldb, stream());
+  return dtrsm_select(is, iu, it, id, m, n, alpha, A, lda, B, ldb, stream());
 }
 
 int gb_dsyrk_dev(char uplo, char trans, int64_t n, int64_t k, double alpha, const double *A,

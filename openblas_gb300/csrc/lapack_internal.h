@@ -86,5 +86,8 @@ int ssyrk_device_skip(int uplo, int trans, int64_t n, int64_t k, float alpha, co
                       const int *skip);
 int dsyrk_device(int uplo, int trans, int64_t n, int64_t k, double alpha, const double *A,
                  int64_t lda, double beta, double *C, int64_t ldc, cudaStream_t s);
+// DTRSM with the engine the DGEMM mode selects (the caller-facing entries).
+int dtrsm_select(int side, int uplo, int trans, int unit, int64_t m, int64_t n, double alpha,
+                 const double *A, int64_t lda, double *B, int64_t ldb, cudaStream_t s);
 
 }  // namespace gb

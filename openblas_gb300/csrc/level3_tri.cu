@@ -183,6 +183,68 @@ int dtrsm_device(int side, int uplo, int trans, int unit, int64_t m, int64_t n, 
   return trsm_device_t<double>(side, uplo, trans, unit, m, n, alpha, A, lda, B, ldb, s);
 }
 
+namespace {
+// Leaves of the recursive emulated-FP64 TRSM: solved by the native blocked
+// TRSM above.
+constexpr int64_t TRSM_EMU_LEAF = 256;
+
+// Solve for the triangular index range [i0, i0 + len) of op(A) (rows of B on
+// the left, columns on the right): halves in the order of the substitution,
+// the later half updated with the solved one by one FP64-accurate GEMM
+// (X1 = op(A11)^-1 B1, B2 -= op(A21) X1, X2 = op(A22)^-1 B2, as
+// driver/level3/trsm_L.c's blocked loop does with GEMM_P blocks).
+int trsm_rec_emulated(int side, int uplo, int trans, int unit_code, int64_t m, int64_t n,
+                      const double *A, int64_t lda, double *B, int64_t ldb, bool forward,
+                      int64_t i0, int64_t len, cudaStream_t s) {
+  const bool left = side == 0;
+  if (len <= TRSM_EMU_LEAF)
+    return trsm_device_t<double>(side, uplo, trans, unit_code, left ? len : m, left ? n : len,
+                                 1.0, A + i0 + i0 * lda, lda, left ? B + i0 : B + i0 * ldb, ldb,
+                                 s);
+  // first half, a multiple of 128 (and shorter than len: len > 256)
+  int64_t h = (len / 2 + 127) / 128 * 128;
+  if (h >= len) h = len / 2;
+  const int64_t f0 = forward ? i0 : i0 + len - h, fl = h;
+  const int64_t s0 = forward ? i0 + h : i0, sl = len - h;
+  auto opA = [&](int64_t r, int64_t c) { return trans ? A + c + r * lda : A + r + c * lda; };
+  int st = trsm_rec_emulated(side, uplo, trans, unit_code, m, n, A, lda, B, ldb, forward, f0, fl,
+                             s);
+  if (st) return st;
+  // the caller's slice setting, as for DGEMM (automatic: per-tile tolerance)
+  const int slices = ozaki_caller_slices();
+  if (left)
+    st = dgemm_emulated(trans, 0, sl, n, fl, -1.0, opA(s0, f0), lda, B + f0, ldb, 1.0, B + s0,
+                        ldb, slices, s);
+  else
+    st = dgemm_emulated(0, trans, m, sl, fl, -1.0, B + f0 * ldb, ldb, opA(f0, s0), lda, 1.0,
+                        B + s0 * ldb, ldb, slices, s);
+  if (st) return st;
+  return trsm_rec_emulated(side, uplo, trans, unit_code, m, n, A, lda, B, ldb, forward, s0, sl,
+                           s);
+}
+}  // namespace
+
+// The caller-facing DTRSM (dtrsm_, cblas_dtrsm, gb_dtrsm_dev): with the
+// emulated-FP64 DGEMM selected (or in auto mode for a large solve) and a
+// triangle wider than one leaf, the recursive form above moves all but the
+// leaves' 256-wide diagonal solves onto the tensor cores; otherwise the
+// native blocked TRSM.
+int dtrsm_select(int side, int uplo, int trans, int unit, int64_t m, int64_t n, double alpha,
+                 const double *A, int64_t lda, double *B, int64_t ldb, cudaStream_t s) {
+  const bool left = side == 0;
+  const int64_t na = left ? m : n, nvec = left ? n : m;
+  const int mode = gb_get_dgemm_mode();
+  const bool emulated =
+      mode == GB_DGEMM_EMULATED ||
+      (mode == GB_DGEMM_AUTO && (double)na * na * nvec >= 512.0 * 512.0 * 512.0);
+  if (!emulated || na <= TRSM_EMU_LEAF || m == 0 || n == 0 || alpha == 0.0)
+    return dtrsm_device(side, uplo, trans, unit, m, n, alpha, A, lda, B, ldb, s);
+  if (alpha != 1.0) launch_dgemm_beta(m, n, alpha, B, ldb, s);
+  const int lower_eff = (uplo == 1) ^ trans;  // triangle of op(A)
+  const bool forward = left ? lower_eff : !lower_eff;
+  return trsm_rec_emulated(side, uplo, trans, unit, m, n, A, lda, B, ldb, forward, 0, na, s);
+}
+
 int dtrsm_device_skip(int side, int uplo, int trans, int unit, int64_t m, int64_t n,
                       double alpha, const double *A, int64_t lda, double *B, int64_t ldb,
                       cudaStream_t s, const int *skip) {
@@ -220,17 +282,19 @@ int dsyrk_device_skip(int uplo, int trans, int64_t n, int64_t k, double alpha, c
   return check_cuda(cudaGetLastError(), "syrk launch");
 }
 
+// The caller-facing DSYRK: the stored triangle of alpha op(A) op(A)^T + beta C
+// with the FP64 GEMM the DGEMM mode selects (tiles outside the triangle
+// skipped).
 int dsyrk_device(int uplo, int trans, int64_t n, int64_t k, double alpha, const double *A,
                  int64_t lda, double beta, double *C, int64_t ldc, cudaStream_t s) {
   if (n == 0) return GB_SUCCESS;
   const int tri = uplo == 1 ? 1 : 2;
   if (k == 0 || alpha == 0.0) {
     launch_dbeta_tri(n, beta, C, ldc, tri, s);
-  } else {
-    launch_dgemm_fp64_tri(trans ? 1 : 0, trans ? 0 : 1, n, n, k, alpha, A, lda, A, lda, beta, C,
-                          ldc, tri, s);
+    return check_cuda(cudaGetLastError(), "syrk launch");
   }
-  return check_cuda(cudaGetLastError(), "syrk launch");
+  return dgemm_select(trans ? 1 : 0, trans ? 0 : 1, n, n, k, alpha, A, lda, A, lda, beta, C, ldc,
+                      tri, s);
 }
 
 }  // namespace gb

@@ -129,6 +129,11 @@ struct GemmParams {
   // s_tiles[nt] == 0 (all when null) take part.
   const int *s_tiles;
   const int *run_if;   // when non-null and *run_if == 0 the launch does nothing
+  // Work units: (tile, level group); a tile's levels are split into
+  // level_groups consecutive ranges of about equal product counts, each
+  // computed by its own CTA (more CTAs than tiles for small products: the
+  // levels write separate planes).
+  int level_groups;
   int mod_p[MOD_COUNT];          // moduli (modular scheme)
   uint32_t mod_magic[MOD_COUNT];  // ceil(2^40 / p_l): u / p_l = umulhi(u, magic) >> 8 for u < 2^31
 };
@@ -160,6 +165,24 @@ __device__ __forceinline__ void product_slices(int l, int s, int &sa, int &sb) {
   }
   sa = s - 1;
   sb = l + 1 - s;  // t - 1 with t = L - s, L = l + 2
+}
+
+// Levels [l0, l1) of level group g of a tile with nl levels: equal shares
+// of the moduli, or of the digit-slice products (level l has l + 1).
+template <bool MOD>
+__device__ __forceinline__ void group_levels(int nl, int g, int groups, int &l0, int &l1) {
+  if (MOD) {
+    l0 = g * nl / groups;
+    l1 = (g + 1) * nl / groups;
+    return;
+  }
+  const int total = nl * (nl + 1) / 2;
+  const int t0 = (g * total + groups / 2) / groups, t1 = ((g + 1) * total + groups / 2) / groups;
+  l0 = l1 = 0;
+  for (int l = 0, cum = 0; l < nl; cum += ++l) {  // cum: products of the levels before l
+    if (cum < t0) l0 = l + 1;
+    if (cum < t1) l1 = l + 1;
+  }
 }
 
 // Tile order: groups of group_m m-tiles, walked column by column inside a
@@ -226,7 +249,7 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
   tc_fence_after();
   const uint32_t tmem_base = *tmem_slot;
 
-  const int ntiles = p.m_tiles * p.n_tiles;
+  const int nunits = p.m_tiles * p.n_tiles * p.level_groups;
   const int nkc = (p.kblocks + KC_BLOCKS - 1) / KC_BLOCKS;
   auto fail = [&](int site) {
     *abort_flag = 1;
@@ -245,12 +268,13 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       bool issued[STAGES];
       for (int i = 0; i < STAGES; ++i) issued[i] = false;
       bool ok = true;
-      for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
-        int mt, nt;
-        tile_coords(tile, p, mt, nt);
+      for (int w = blockIdx.x; ok && w < nunits; w += gridDim.x) {
+        int mt, nt, l0, l1;
+        tile_coords(w / p.level_groups, p, mt, nt);
         if (!tile_active(mt, nt, p)) continue;
         const int nl = tile_levels<MOD>(nt, p);
-        for (int l = 0; ok && l < nl; ++l) {
+        group_levels<MOD>(nl, w % p.level_groups, p.level_groups, l0, l1);
+        for (int l = l0; ok && l < l1; ++l) {
           int s_lo, s_hi;
           level_products<MOD>(l, nl, s_lo, s_hi);
           for (int s = s_lo; ok && s <= s_hi; ++s) {
@@ -294,12 +318,13 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
       int acc = 0;
       uint32_t acc_phase = 0;
       bool ok = true;
-      for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
-        int mt, nt;
-        tile_coords(tile, p, mt, nt);
+      for (int w = blockIdx.x; ok && w < nunits; w += gridDim.x) {
+        int mt, nt, l0, l1;
+        tile_coords(w / p.level_groups, p, mt, nt);
         if (!tile_active(mt, nt, p)) continue;
         const int nl = tile_levels<MOD>(nt, p);
-        for (int l = 0; ok && l < nl; ++l) {
+        group_levels<MOD>(nl, w % p.level_groups, p.level_groups, l0, l1);
+        for (int l = l0; ok && l < l1; ++l) {
           int s_lo, s_hi;
           level_products<MOD>(l, nl, s_lo, s_hi);
           for (int s = s_lo; ok && s <= s_hi; ++s) {
@@ -355,13 +380,14 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
     uint32_t acc_phase = 0;
     bool ok = true;
     int32_t sum[128];
-    for (int tile = blockIdx.x; ok && tile < ntiles; tile += gridDim.x) {
-      int mt, nt;
-      tile_coords(tile, p, mt, nt);
+    for (int w = blockIdx.x; ok && w < nunits; w += gridDim.x) {
+      int mt, nt, l0, l1;
+      tile_coords(w / p.level_groups, p, mt, nt);
       if (!tile_active(mt, nt, p)) continue;
       const int nl = tile_levels<MOD>(nt, p);
+      group_levels<MOD>(nl, w % p.level_groups, p.level_groups, l0, l1);
       const int64_t plane_tile = (int64_t)nt * p.m_tiles + mt;
-      for (int l = 0; ok && l < nl; ++l) {
+      for (int l = l0; ok && l < l1; ++l) {
 #pragma unroll
         for (int c = 0; c < 128; ++c) sum[c] = 0;
         int s_lo, s_hi;
@@ -901,7 +927,9 @@ recombine_tile(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
   int e_i[4];
 #pragma unroll
   for (int r = 0; r < 4; ++r) e_i[r] = (i0 + il + r < m) ? ea[i0 + il + r] : 0;
-  for (int jl = jb; jl < BN; jl += 8) {
+  // grid z splits the tile's columns into chunks (more CTAs for small C)
+  const int chunk = BN / (int)gridDim.z, jz0 = (int)blockIdx.z * chunk;
+  for (int jl = jz0 + jb; jl < jz0 + chunk; jl += 8) {
     const int64_t j = j0 + jl;
     if (j >= n) break;
     const int fj = eb[j];
@@ -1013,15 +1041,19 @@ reconstruct_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
   int e_i[2];
 #pragma unroll
   for (int r = 0; r < 2; ++r) e_i[r] = (i0 + il + r < m) ? ea[i0 + il + r] : 0;
-  // the planes of the next column are loaded while this one is combined
-  const int jend = (n - j0) < BN ? (int)(n - j0) : BN;
+  // the planes of the next column are loaded while this one is combined;
+  // grid z splits the tile's columns into chunks (more CTAs for small C)
+  const int chunk = BN / (int)gridDim.z, jz0 = (int)blockIdx.z * chunk;
+  const int jn_tile = (n - j0) < BN ? (int)(n - j0) : BN;
+  const int jend = jn_tile < jz0 + chunk ? jn_tile : jz0 + chunk;
   uint32_t Pn[MOD_COUNT];
-  if (jb < jend) {
+  if (jz0 + jb < jend) {
 #pragma unroll
     for (int l = 0; l < MOD_COUNT; ++l)
-      Pn[l] = *reinterpret_cast<const uint32_t *>(pt + (int64_t)l * plane_stride + jb * BM + il);
+      Pn[l] = *reinterpret_cast<const uint32_t *>(pt + (int64_t)l * plane_stride +
+                                                  (jz0 + jb) * BM + il);
   }
-  for (int jl = jb; jl < jend; jl += 4) {
+  for (int jl = jz0 + jb; jl < jend; jl += 4) {
     const int64_t j = j0 + jl;
     const int fj = eb[j];
     uint32_t P[MOD_COUNT];
@@ -1218,8 +1250,11 @@ void operand_exponents(bool kcontig, int64_t R, int64_t K, const double *X, int6
   if (kcontig) {
     { rowmax_kcontig_kernel<<<(unsigned)((R + 7) / 8), 256, 0, s>>>(R, K, X, ld, mx); count_launch(); }
   } else {
-    const int64_t kspan = 256;
-    dim3 g((unsigned)((R + 255) / 256), (unsigned)((K + kspan - 1) / kspan));
+    // K spans of 16..256 columns: enough CTAs for a short op(A) too
+    const int64_t gx = (R + 255) / 256;
+    int64_t kspan = 256;
+    while (kspan > 16 && gx * ((K + kspan - 1) / kspan) < 2LL * persistent_ctas()) kspan /= 2;
+    dim3 g((unsigned)gx, (unsigned)((K + kspan - 1) / kspan));
     { rowmax_mcontig_kernel<<<g, 256, 0, s>>>(R, K, X, ld, kspan, mx); count_launch(); }
   }
   { exponent_kernel<<<(unsigned)((Rpad + 255) / 256), 256, 0, s>>>(Rpad, R, mx, expo, emax); count_launch(); }
@@ -1449,7 +1484,12 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       gp.mod_magic[l] = (uint32_t)(((1ull << 40) + MODULI[l] - 1) / MODULI[l]);
     }
     const int ntiles = gp.m_tiles * gp.n_tiles;
-    const int grid = ntiles < persistent_ctas() ? ntiles : persistent_ctas();
+    // fewer tiles than CTAs: split each tile's levels over idle CTAs
+    const int maxl = mod ? MOD_COUNT : Sa;
+    const int spare = persistent_ctas() / ntiles;
+    gp.level_groups = spare < 1 ? 1 : (spare > maxl ? maxl : spare);
+    const int nunits = ntiles * gp.level_groups;
+    const int grid = nunits < persistent_ctas() ? nunits : persistent_ctas();
     if (mod) {
       ProfileScope prof("residue_gemm", s);
       slice_gemm_kernel<true><<<grid, NUM_THREADS, SMEM_BYTES, s>>>(ma, mb, gp);
@@ -1489,7 +1529,10 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       const double *Ak = seg_a(k0);
       const double *Bk = tb ? Bj + k0 * ldbj : Bj + k0;
       const double bseg = sg == 0 ? beta : 1.0;  // later segments accumulate
-      const dim3 g((unsigned)((m + BM - 1) / BM), (unsigned)((jn + BN - 1) / BN));
+      // recombination grid: one CTA per tile and column chunk, the tiles
+      // split into up to 16 chunks until there are 4 CTAs per SM
+      dim3 g((unsigned)((m + BM - 1) / BM), (unsigned)((jn + BN - 1) / BN), 1);
+      while (g.z < 16 && (int64_t)g.x * g.y * g.z < 4LL * persistent_ctas()) g.z *= 2;
       const int m_tiles = (int)(m_pad / BM);
       const int64_t ps = m_pad * jn_pad;
       if (fixed_mod) {

@@ -327,6 +327,71 @@ def test_dtrsm_config_8192_rows_property(F, gb_clean):
     assert res <= 4 * m * EPS
 
 
+@pytest.fixture
+def emulated_mode(gblib, gb_clean):
+    gblib.gb_set_dgemm_mode(1)
+    try:
+        yield gblib
+    finally:
+        gblib.gb_set_dgemm_mode(0)
+
+
+@pytest.mark.parametrize("side,uplo,ta,diag", [
+    (s, u, t, d) for s in "LR" for u in "UL" for t in "NT" for d in "UN"])
+def test_dtrsm_emulated_recursive_vs_oracle(orc, F, emulated_mode, side, uplo, ta, diag):
+    """Emulated-FP64 DTRSM: triangles wider than the 256-wide native leaves
+    recurse, the off-diagonal blocks applied by the emulated DGEMM (automatic
+    per-tile choice); alpha != 1 and a padded ldb.  Same bound as the native
+    blocked solve."""
+    m, n = (1100, 300) if side == "L" else (300, 1100)
+    na = m if side == "L" else n
+    A = W.trsm_lower(71, na)
+    if uplo == "U":
+        A = np.asfortranarray(A.T)
+    if diag == "U":
+        A = np.asfortranarray(np.where(np.eye(na) == 1, A, A / na))
+    B = np.asfortranarray(W.uniform(72, (m + 5, n)))
+    Bo = B.copy(order="F")
+    F.dtrsm(side, uplo, ta, diag, m, n, -0.6, A, na, B, m + 5)
+    orc.dtrsm(side, uplo, ta, diag, m, n, -0.6, A, na, Bo, m + 5)
+    assert np.max(np.abs(B[:m] - Bo[:m])) <= 1e3 * na * EPS * max(1.0, np.abs(Bo[:m]).max())
+    assert np.array_equal(B[m:], Bo[m:])
+
+
+def test_dtrsm_emulated_residual(F, emulated_mode):
+    """Left/Lower/NoTrans/NonUnit, 2048 x 256 with an exponent-spread right-hand
+    side (columns scaled by 2^-40 .. 2^40): L X - B at rounding level column by
+    column, i.e. the automatic choice keeps each column's relative accuracy."""
+    m, n = 2048, 256
+    L = W.trsm_lower(57, m)
+    B = W.uniform(58, (m, n)) * np.exp2(np.linspace(-40, 40, n))[None, :]
+    X = np.asfortranarray(B.copy())
+    F.dtrsm("L", "L", "N", "N", m, n, 1.0, L, m, X, m)
+    res = np.abs(L @ X - B).max(axis=0) / (np.abs(L).sum(axis=1).max() * np.abs(X).max(axis=0))
+    assert res.max() <= 4 * m * EPS
+
+
+def test_dsyrk_emulated(orc, F, emulated_mode):
+    """Emulated-FP64 DSYRK: the stored triangle within the DMMCH bound, the
+    other triangle untouched."""
+    n, k = 700, 333
+    for uplo in "UL":
+        for tr in "NT":
+            ra, ca = (n, k) if tr == "N" else (k, n)
+            A = W.uniform(62, (ra, ca))
+            Cm = W.uniform(63, (n, n))
+            C0, Co = Cm.copy(order="F"), Cm.copy(order="F")
+            F.dsyrk(uplo, tr, n, k, -1.0, A, ra, 0.5, Cm, n)
+            orc.dsyrk(uplo, tr, n, k, -1.0, A, ra, 0.5, Co, n)
+            Aop = A if tr == "N" else A.T
+            G = np.abs(Aop) @ np.abs(Aop.T) + 0.5 * np.abs(C0)
+            tri = np.tril if uplo == "L" else np.triu
+            assert dmmch_ratio(tri(Cm), tri(Co), tri(G), k) <= 2 * (k + 2)
+            other = np.triu(C0, 1) if uplo == "L" else np.tril(C0, -1)
+            got_other = np.triu(Cm, 1) if uplo == "L" else np.tril(Cm, -1)
+            assert np.array_equal(other, got_other)
+
+
 def test_dsyrk_golden_cases(golden, F, gb_clean):
     idx = 0
     for (n, k) in GG.SYRK_SHAPES:
