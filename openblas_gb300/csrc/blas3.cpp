@@ -10,6 +10,7 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
 #include <chrono>
 #include <vector>
 
@@ -100,10 +101,73 @@ static int dgemm_dispatch(int ta, int tb, int64_t m, int64_t n, int64_t k, doubl
 // overlap with the GPU.
 namespace {
 constexpr int64_t PIPE_K_SEGMENT = EMU_K_SEGMENT;  // upload piece of op(A) and op(B) along K
+
+// Column blocks of the pipelined DGEMM, in 256-column tiles of C (block
+// starts, the last entry n; *nb the widest block).  The first block's
+// upload and the last block's download lie outside any overlap, so both
+// are at most one wave of the persistent GEMM's tiles (one 128 x 256 tile
+// per CTA); the two or three blocks between them are picked with a
+// timeline model: uploads run back to back from the start, block b's
+// compute starts when its upload and block b - 1 are done and takes whole
+// waves of tiles, its download follows it and the previous download.  The
+// model's constants are this part's measured rates: ~200 GB/s up and
+// ~190 GB/s down the host link, ~0.84 ms per wave of modular-scheme tiles
+// per 8192 of K, ~0.8 ms per 8192^2 of op(A) preparation and ~0.12 ms of
+// fixed work per block.  The plan changes only the overlap, never the
+// result.
+std::vector<int64_t> pipeline_blocks(int64_t m, int64_t n, int64_t k, int64_t *nb) {
+  const int64_t T = (n + 255) / 256, mt = (m + 127) / 128, P = persistent_ctas();
+  const double a_up = (double)m * k * 8 / 200e9 * 1e3;
+  const double a_prep = 0.8 * ((double)m * k / (8192.0 * 8192.0));
+  const double up_t = 256.0 * k * 8 / 200e9 * 1e3, dn_t = 256.0 * m * 8 / 190e9 * 1e3;
+  const double wave = 0.843 * k / 8192.0;
+  auto cost = [&](const std::vector<int64_t> &t) {
+    double up = a_up, comp = a_up + a_prep, dn = 0.0;
+    for (int64_t b : t) {
+      up += b * up_t;
+      comp = (comp > up ? comp : up) + (double)((mt * b + P - 1) / P) * wave + 0.12;
+      dn = (comp > dn ? comp : dn) + b * dn_t;
+    }
+    return dn;
+  };
+  // the even split into blocks of ~4096 columns, and the edge-block plans
+  int64_t nu = n / 4096;
+  nu = nu < 2 ? 2 : nu > 8 ? 8 : nu;
+  std::vector<int64_t> best;
+  for (int64_t i = 0; i < nu; ++i) best.push_back(T * (i + 1) / nu - T * i / nu);
+  double best_cost = cost(best);
+  int64_t e = P / mt;
+  e = e < 1 ? 1 : e;
+  const int64_t R = T - 2 * e;
+  auto consider = [&](const std::vector<int64_t> &t) {
+    const double c = cost(t);
+    if (c < best_cost - 1e-9) {
+      best_cost = c;
+      best = t;
+    }
+  };
+  for (int64_t x = 1; R >= 2 && x < R; ++x) {
+    consider({e, x, R - x, e});
+    for (int64_t y = 1; x + y < R; ++y) consider({e, x, y, R - x - y, e});
+  }
+  std::vector<int64_t> starts{0};
+  *nb = 0;
+  for (int64_t b : best) {
+    const int64_t j1 = starts.back() + b * 256 < n ? starts.back() + b * 256 : n;
+    *nb = j1 - starts.back() > *nb ? j1 - starts.back() : *nb;
+    starts.push_back(j1);
+  }
+  return starts;
+}
+
 struct PipelinedDgemm : EmuBlockHooks {
   cudaStream_t s = nullptr, cin = nullptr, cout = nullptr;
   int ta = 0, tb = 0;
-  int64_t m = 0, n = 0, k = 0, nb = 0, nseg = 1, lda = 0, ldb = 0, ldc = 0;
+  int64_t m = 0, n = 0, k = 0, nseg = 1, lda = 0, ldb = 0, ldc = 0;
+  std::vector<int64_t> bs;  // column blocks: block j is [bs[j], bs[j + 1])
+  int64_t block_of(int64_t j0) const {
+    return (int64_t)(std::upper_bound(bs.begin(), bs.end(), j0) - bs.begin()) - 1;
+  }
   const double *A = nullptr, *B = nullptr;
   double *C = nullptr;
   bool load_c = false;
@@ -164,7 +228,7 @@ struct PipelinedDgemm : EmuBlockHooks {
   }
   // segment sg of block j of op(B) (and C's block with the first segment)
   int upload(int64_t j, int64_t sg) {
-    const int64_t j0 = j * nb, jn = (n - j0) < nb ? (n - j0) : nb;
+    const int64_t j0 = bs[j], jn = bs[j + 1] - bs[j];
     const int64_t k0 = sg * PIPE_K_SEGMENT, kk = seg_len(sg);
     if (tb)  // op(B) = B^T: rows j0.. and columns k0.. of the n x k matrix B
       GB_CUDA(cudaMemcpy2DAsync(dB + j0 + k0 * dldb, dldb * 8, B + j0 + k0 * ldb, ldb * 8, jn * 8,
@@ -188,7 +252,7 @@ struct PipelinedDgemm : EmuBlockHooks {
     return GB_SUCCESS;
   }
   int download(int64_t j) {
-    const int64_t j0 = j * nb, jn = (n - j0) < nb ? (n - j0) : nb;
+    const int64_t j0 = bs[j], jn = bs[j + 1] - bs[j];
     GB_CUDA(cudaStreamWaitEvent(cout, done[j], 0));
     const int st = stage_out(C + j0 * ldc, dC + j0 * m, ldc, m, jn, 8, cout);
     mark(cout, "C block downloaded", j);
@@ -206,7 +270,7 @@ struct PipelinedDgemm : EmuBlockHooks {
   int segment(int64_t j0, int64_t, int64_t k0, int64_t kk) override {
     for (int64_t sg = k0 / PIPE_K_SEGMENT; sg * PIPE_K_SEGMENT < k0 + kk; ++sg) {
       GB_CUDA(cudaStreamWaitEvent(s, a_up[sg], 0));
-      GB_CUDA(cudaStreamWaitEvent(s, up[(j0 / nb) * nseg + sg], 0));
+      GB_CUDA(cudaStreamWaitEvent(s, up[block_of(j0) * nseg + sg], 0));
     }
     return GB_SUCCESS;
   }
@@ -215,8 +279,12 @@ struct PipelinedDgemm : EmuBlockHooks {
       GB_CUDA(cudaStreamWaitEvent(s, a_up[sg], 0));
     return GB_SUCCESS;
   }
+  int64_t block_cols(int64_t j0, int64_t) override {
+    const int64_t j = block_of(j0);
+    return bs[j + 1] - bs[j];
+  }
   int after(int64_t j0, int64_t) override {
-    const int64_t j = j0 / nb, nblk = (int64_t)done.size();
+    const int64_t j = block_of(j0), nblk = (int64_t)done.size();
     GB_CUDA(cudaEventRecord(done[j], s));
     mark(s, "C block computed", j);
     int st = GB_SUCCESS;
@@ -241,10 +309,9 @@ static int dgemm_host_pipelined(int ta, int tb, int64_t m, int64_t n, int64_t k,
   p.h0 = std::chrono::steady_clock::now();
   p.s = stream();
   if (copy_streams(&p.cin, &p.cout)) return 1;
-  int64_t nblk = n / 4096;
-  nblk = nblk < 2 ? 2 : nblk > 8 ? 8 : nblk;
-  p.nb = ((n + nblk - 1) / nblk + 255) / 256 * 256;
-  nblk = (n + p.nb - 1) / p.nb;
+  int64_t nb = 0;
+  p.bs = pipeline_blocks(m, n, k, &nb);
+  const int64_t nblk = (int64_t)p.bs.size() - 1;
   p.ta = ta;
   p.tb = tb;
   p.m = m;
@@ -296,7 +363,7 @@ static int dgemm_host_pipelined(int ta, int tb, int64_t m, int64_t n, int64_t k,
         if ((st = p.upload(0, sg))) return st;
     }
     st = dgemm_emulated_blocked(ta, tb, m, n, k, alpha, dA, ra, beta,
-                                ozaki_caller_slices(), p.nb, &p, p.s);
+                                ozaki_caller_slices(), nb, &p, p.s);
     // the staging buffer is released on the compute stream after the last download
     GB_CUDA(cudaEventRecord(out_done, p.cout));
     GB_CUDA(cudaStreamWaitEvent(p.s, out_done, 0));

@@ -195,11 +195,14 @@ constexpr int64_t EMU_K_SEGMENT = 4096;
 // hooks->segment(j0, jn, k0, kk) runs before the K range [k0, k0 + kk) of
 // the block is used (e.g. to wait for that range of op(A) and op(B)), and
 // hooks->a_range(k0, kk) before op(A)'s columns [k0, k0 + kk) are first read.
+// hooks->block_cols(j0, nb) gives the width of the block starting at column
+// j0 (a multiple of 256, at most nb; the default: nb).
 struct EmuBlockHooks {
   virtual int before(int64_t j0, int64_t jn, const double **Bj, int64_t *ldb, double **Cj,
                      int64_t *ldc) = 0;
   virtual int segment(int64_t, int64_t, int64_t, int64_t) { return GB_SUCCESS; }
   virtual int a_range(int64_t, int64_t) { return GB_SUCCESS; }
+  virtual int64_t block_cols(int64_t, int64_t nb) { return nb; }
   virtual int after(int64_t j0, int64_t jn) = 0;
   virtual ~EmuBlockHooks() = default;
 };

@@ -1121,6 +1121,15 @@ reconstruct_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
   }
 }
 
+// Automatic mode over several column blocks: op(A)'s digit split runs once,
+// for the first block with digit-slice tiles (run = count > 0 and not yet
+// done).
+__global__ void latch_kernel(const int *__restrict__ count, int *__restrict__ latch) {
+  const int run = *count > 0 && latch[0] == 0;
+  latch[1] = run;
+  if (run) latch[0] = 1;
+}
+
 // ------------------------------------------------------------------ host
 // The modular scheme's moduli: the 14 largest odd numbers <= 511 that are
 // pairwise coprime (511 = 7 * 73, 507 = 3 * 13^2, 505 = 5 * 101,
@@ -1318,7 +1327,9 @@ void choose_b(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld, i
 // accumulating into C (beta = 1).  The columns of op(B) and C are taken in blocks of `nb`
 // (a multiple of BN), all segments of a block before the next block, with
 // the hooks (when given) making block j of op(B) and C available on the
-// device first and told when C's block is final.  op(A) is split once when K
+// device first, setting the blocks' widths (multiples of 256 columns, so the
+// 256-column tiles of the automatic choice are those of the single-block
+// form) and told when C's block is final.  op(A) is split once when K
 // is one segment and per segment and block otherwise.  Every C(i,j) depends
 // only on row i of op(A) and column j of op(B) (and their own exponents), so
 // the blocked result equals the single-block one bit for bit.
@@ -1356,6 +1367,10 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
   const bool a_cache = !a_once && nb < n;
   const bool a_early = a_once && (!automatic || nb < n);
   const bool a_both = a_early || a_cache;  // both forms split unpredicated
+  // automatic, one segment, several blocks: op(A)'s digit slices are cut for
+  // the first block whose choice has digit-slice tiles (none when every
+  // tile takes the modular scheme)
+  const bool a_dig_lazy = a_early && automatic;
   const int64_t a_copies = a_cache ? nseg : 1;
   const int b_planes = modular && MOD_COUNT > Sa ? MOD_COUNT : Sa;
   const size_t seg_sa = align256((size_t)Sa * m_pad * ks_pad * 2);
@@ -1369,10 +1384,10 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
   const size_t plane_bytes = (size_t)Sa * 4 > (size_t)MOD_COUNT * 2 || !modular
                                  ? (size_t)Sa * 4 : (size_t)MOD_COUNT * 2;
   const size_t bytes_pl = align256(plane_bytes * m_pad * nb_pad);
-  // automatic mode, op(B) side: its column sums, the per-tile choices and
-  // the two pass counts
+  // automatic mode, op(B) side: its column sums, the per-tile choices, the
+  // two pass counts and the latch of op(A)'s digit split
   const size_t bytes_auto =
-      automatic ? align256((size_t)(2 * nb_pad) * 4 + (size_t)(nb_pad / BN + 2) * 4) : 0;
+      automatic ? align256((size_t)(2 * nb_pad) * 4 + (size_t)(nb_pad / BN + 4) * 4) : 0;
   Scratch ws((seg_sa + seg_ra + seg_ea + seg_st) * a_copies + bytes_sb + bytes_mx + bytes_eb +
                  bytes_pl + bytes_auto, s);
   if (!ws.p) return GB_ERR_ALLOC;
@@ -1388,13 +1403,14 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
   int *planes = reinterpret_cast<int *>(base);
   base += bytes_pl;
   float *st_s1 = nullptr, *st_s2 = nullptr;
-  int *s_tiles = nullptr, *pass = nullptr;
+  int *s_tiles = nullptr, *pass = nullptr, *latch = nullptr;
   double budget_mod = 0.0, budget_dig = 0.0;
   if (automatic) {
     st_s1 = reinterpret_cast<float *>(base);
     st_s2 = st_s1 + nb_pad;
     s_tiles = reinterpret_cast<int *>(st_s2 + nb_pad);
     pass = s_tiles + nb_pad / BN;  // [0] modular tiles, [1] digit-slice tiles
+    latch = pass + 2;              // [0] op(A)'s digits split, [1] split them now
     // the tolerance in units of 2^-52 less the roundings of the recombine
     // (one conversion, the alpha/beta step) and of the accumulation over
     // the segments (modular tiles) or the digit passes' sub-segments
@@ -1504,11 +1520,14 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
   if (a_once) {
     if (hooks && (st = hooks->a_range(0, k))) return st;
     prep_a(0, 0, k);
-    if (a_early && Sa > 0 && (st = split_a(0, 0, k, nullptr))) return st;
+    if (a_dig_lazy) cudaMemsetAsync(latch, 0, 2 * sizeof(int), s);
+    if (a_early && Sa > 0 && !a_dig_lazy && (st = split_a(0, 0, k, nullptr))) return st;
     if (a_early && modular && (st = split_a_mod(0, 0, k, nullptr))) return st;
   }
-  for (int64_t j0 = 0; j0 < n; j0 += nb) {
-    const int64_t jn = (n - j0) < nb ? (n - j0) : nb;
+  for (int64_t j0 = 0, jn = 0; j0 < n; j0 += jn) {
+    jn = hooks ? hooks->block_cols(j0, nb) : nb;
+    if (jn > nb || jn <= 0) jn = nb;
+    if (jn > n - j0) jn = n - j0;
     const int64_t jn_pad = round_up(jn, BN);
     const double *Bj = tb ? B + j0 : B + j0 * ldb;
     double *Cj = C + j0 * ldc;
@@ -1587,7 +1606,12 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       // ---- digit-slice pass (tiles with s_tiles = S > 0), over sub-segments
       // of at most MAX_K_SEGMENT (each level sum exact in int32), each
       // recombined into C in turn
-      if (!a_both && (st = split_a(sg, k0, kk, pass + 1))) return st;
+      if (a_dig_lazy) {
+        { latch_kernel<<<1, 1, 0, s>>>(pass + 1, latch); count_launch(); }
+        if ((st = split_a(sg, k0, kk, latch + 1))) return st;
+      } else if (!a_both && (st = split_a(sg, k0, kk, pass + 1))) {
+        return st;
+      }
       launch_split(tb == 0, jn, kk, Bk, ldbj, eb, MAX_SLICES, jn_pad, kp, slb, s_tiles, pass + 1,
                    s);
       if ((st = make_map(&mapB, slb, (int64_t)Sa * jn_pad, kp, BN))) return st;

@@ -225,6 +225,27 @@ def test_host_pipelined_several_k_segments(F, emulated, gblib):
     assert np.array_equal(C, ref)
 
 
+@pytest.mark.parametrize("hard", [False, True])
+def test_host_pipelined_planned_blocks(F, emulated, gblib, hard):
+    """A shape whose block plan is uneven (one-wave edge blocks of 4 tiles
+    at m = 4096, two or three wider blocks between them, a ragged last
+    one): still bit-identical to the single device call.  With `hard`, 200
+    columns of op(B) in a late block meet a tiny column of op(A) (the
+    construction of the per-tile test below), so that block alone needs
+    digit slices: op(A)'s digit split then runs for it only."""
+    m, n, k = 4096, 8292, 700
+    A, B, C = W.gemm_operands(93, m, n, k, "N", "T", pad=1)
+    if hard:
+        A[:, 0] *= 2.0 ** -30
+        B[6000:6200, :k] = np.ldexp(W.uniform(94, (200, k)), -40)
+        B[6000:6200, 0] = 1.0
+    ref = _device_emulated(gblib, "N", "T", m, n, k, 0.75, A, B, -1.5, C)
+    F.dgemm("N", "T", m, n, k, 0.75, A, A.shape[0], B, B.shape[0], -1.5, C, C.shape[0])
+    assert np.array_equal(C, ref)
+    if hard:
+        assert (gblib.gb_last_ozaki_moduli(), gblib.gb_last_ozaki_slices()) == (MOD_COUNT, 8)
+
+
 def test_host_pipelined_pinned_buffers(emulated, gblib):
     """The same through cblas_dgemm on pinned (page-locked) host buffers."""
     torch = pytest.importorskip("torch")
