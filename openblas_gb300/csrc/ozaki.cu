@@ -1031,8 +1031,8 @@ reconstruct_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
   if (tri == 1 && i0 + BM - 1 < j0) return;
   if (tri == 2 && i0 > j0 + BN - 1) return;
   // a thread takes two consecutive rows of a column (one 4-byte load per
-  // plane), 64 threads a column; few registers per thread keep enough warps
-  // resident to hide the integer multiply chains
+  // plane), 64 threads a column; grid z splits the tile's columns into
+  // chunks (more CTAs, and short last waves, for any size of C)
   const int tid = threadIdx.x;
   const int il = (tid & 63) * 2, jb = tid >> 6;
   // FP64 compares run on the FP64 pipe: decide alpha = 1 and beta = 0 once
@@ -1041,30 +1041,17 @@ reconstruct_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
   int e_i[2];
 #pragma unroll
   for (int r = 0; r < 2; ++r) e_i[r] = (i0 + il + r < m) ? ea[i0 + il + r] : 0;
-  // the planes of the next column are loaded while this one is combined;
-  // grid z splits the tile's columns into chunks (more CTAs for small C)
   const int chunk = BN / (int)gridDim.z, jz0 = (int)blockIdx.z * chunk;
   const int jn_tile = (n - j0) < BN ? (int)(n - j0) : BN;
   const int jend = jn_tile < jz0 + chunk ? jn_tile : jz0 + chunk;
-  uint32_t Pn[MOD_COUNT];
-  if (jz0 + jb < jend) {
-#pragma unroll
-    for (int l = 0; l < MOD_COUNT; ++l)
-      Pn[l] = *reinterpret_cast<const uint32_t *>(pt + (int64_t)l * plane_stride +
-                                                  (jz0 + jb) * BM + il);
-  }
   for (int jl = jz0 + jb; jl < jend; jl += 4) {
     const int64_t j = j0 + jl;
     const int fj = eb[j];
     uint32_t P[MOD_COUNT];
 #pragma unroll
-    for (int l = 0; l < MOD_COUNT; ++l) P[l] = Pn[l];
-    if (jl + 4 < jend) {
-#pragma unroll
-      for (int l = 0; l < MOD_COUNT; ++l)
-        Pn[l] = *reinterpret_cast<const uint32_t *>(pt + (int64_t)l * plane_stride +
-                                                    (jl + 4) * BM + il);
-    }
+    for (int l = 0; l < MOD_COUNT; ++l)
+      P[l] = __ldg(reinterpret_cast<const unsigned int *>(pt + (int64_t)l * plane_stride +
+                                                          jl * BM + il));
 #pragma unroll
     for (int r = 0; r < 2; ++r) {
       const int64_t i = i0 + il + r;
@@ -1080,8 +1067,9 @@ reconstruct_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
         }
         v = alpha * sum;
       } else {
-        unsigned long long qa = 0;
-        long long a0 = 0, a1 = 0, a2 = 0, a3 = 0;
+        // X = sum_i y_i W_i in four 32-bit limbs (each limb sum below 2^53)
+        // and the quotient estimate sum_i y_i F_i (fraction of 2^32)
+        unsigned long long qa = 0, x0 = 0, x1 = 0, x2 = 0, x3 = 0;
 #pragma unroll
         for (int i2 = 0; i2 < MOD_PAIRS; ++i2) {
           const uint32_t ra = r ? (P[2 * i2] >> 16) : (P[2 * i2] & 0xFFFFu);
@@ -1091,27 +1079,30 @@ reconstruct_tile_kernel(int64_t m, int64_t n, int m_tiles, int64_t plane_stride,
           // the product below 2^20, its quotient by b exact from the magic
           const uint32_t u = (rb + 2 * b - ra) * tab.pinv_ab[i2];
           const uint32_t tq = u - __umulhi(u, tab.pmagic[i2]) * b;
-          const unsigned long long y = ra + tab.pa[i2] * tq;  // C' mod a b
-          qa += y * tab.F[i2];
-          a0 += (long long)(y * tab.W[i2][0]);
-          a1 += (long long)(y * tab.W[i2][1]);
-          a2 += (long long)(y * tab.W[i2][2]);
-          a3 += (long long)(y * tab.W[i2][3]);
+          const uint32_t y = ra + tab.pa[i2] * tq;  // C' mod a b, below 2^18
+          qa += (unsigned long long)y * tab.F[i2];
+          x0 += (unsigned long long)y * tab.W[i2][0];
+          x1 += (unsigned long long)y * tab.W[i2][1];
+          x2 += (unsigned long long)y * tab.W[i2][2];
+          x3 += (unsigned long long)y * tab.W[i2][3];
         }
-        const long long q = (long long)((qa + 0x80000000ull) >> 32);
-        a0 -= q * (long long)tab.M[0];
-        a1 -= q * (long long)tab.M[1];
-        a2 -= q * (long long)tab.M[2];
-        a3 -= q * (long long)tab.M[3];
-        const unsigned __int128 u = (unsigned __int128)(__int128)a0 +
-                                    ((unsigned __int128)(__int128)a1 << 32) +
-                                    ((unsigned __int128)(__int128)a2 << 64) +
-                                    ((unsigned __int128)(__int128)a3 << 96);
-        const int x0 = e_i[r] + fj - 2 * tab.bits;
+        // C' = X - q M modulo 2^128: signed limb differences (|d| < 2^54),
+        // then one carry pass into two 64-bit words
+        const unsigned long long q = (qa + 0x80000000ull) >> 32;
+        long long d = (long long)x0 - (long long)(q * tab.M[0]);
+        const unsigned long long c0 = (unsigned long long)d & 0xFFFFFFFFull;
+        d = ((long long)x1 - (long long)(q * tab.M[1])) + (d >> 32);
+        const unsigned long long c1 = (unsigned long long)d & 0xFFFFFFFFull;
+        d = ((long long)x2 - (long long)(q * tab.M[2])) + (d >> 32);
+        const unsigned long long c2 = (unsigned long long)d & 0xFFFFFFFFull;
+        d = ((long long)x3 - (long long)(q * tab.M[3])) + (d >> 32);
+        const unsigned long long lo = c0 | (c1 << 32);
+        const unsigned long long hi = c2 | ((unsigned long long)d << 32);
+        const int xs = e_i[r] + fj - 2 * tab.bits;
         bool ok;
-        v = ozd::int_scaled((__int128)u, x0, ok);
+        v = ozd::i128_scaled(hi, lo, xs, ok);
         if (!ok)
-          v = ozd::scaled_value((__int128)u, x0, alpha);
+          v = ozd::scaled_value((__int128)(((unsigned __int128)hi << 64) | lo), xs, alpha);
         else if (!alpha_one)
           v *= alpha;
       }
@@ -1549,9 +1540,10 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       const double *Bk = tb ? Bj + k0 * ldbj : Bj + k0;
       const double bseg = sg == 0 ? beta : 1.0;  // later segments accumulate
       // recombination grid: one CTA per tile and column chunk, the tiles
-      // split into up to 16 chunks until there are 4 CTAs per SM
+      // split into up to 16 chunks until there are 16 CTAs per SM (about
+      // four waves: a short last wave costs little)
       dim3 g((unsigned)((m + BM - 1) / BM), (unsigned)((jn + BN - 1) / BN), 1);
-      while (g.z < 16 && (int64_t)g.x * g.y * g.z < 4LL * persistent_ctas()) g.z *= 2;
+      while (g.z < 16 && (int64_t)g.x * g.y * g.z < 16LL * persistent_ctas()) g.z *= 2;
       const int m_tiles = (int)(m_pad / BM);
       const int64_t ps = m_pad * jn_pad;
       if (fixed_mod) {

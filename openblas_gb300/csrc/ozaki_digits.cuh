@@ -14,6 +14,7 @@
 
 #include <math.h>
 #include <stdint.h>
+#include <string.h>
 
 namespace gb {
 namespace ozd {
@@ -94,30 +95,60 @@ __device__ __forceinline__ double scaled_value(__int128 acc, int x0, double alph
   return scale_out_of_range(neg ? -t : t, alpha, x);
 }
 
-// acc * 2^x0 rounded to nearest (ties to even) with integer operations only,
-// when the result is a normal number (ok = true); FP64 arithmetic is the
-// scarcest unit on this part.  Equal to scaled_value(acc, x0, 1.0) whenever
-// ok is set.
-__device__ __forceinline__ double int_scaled(__int128 acc, int x0, bool &ok) {
+// Leading zeros and bit casts on both sides, so the rounding below also
+// compiles as host code (tested against exact integer rounding on the CPU).
+__host__ __device__ __forceinline__ int clz64(unsigned long long x) {
+#ifdef __CUDA_ARCH__
+  return __clzll((long long)x);
+#else
+  return __builtin_clzll(x);
+#endif
+}
+__host__ __device__ __forceinline__ double bits_double(unsigned long long b) {
+#ifdef __CUDA_ARCH__
+  return __longlong_as_double((long long)b);
+#else
+  double d;
+  memcpy(&d, &b, sizeof d);
+  return d;
+#endif
+}
+
+// v * 2^x0 for the two's-complement 128-bit integer v = hi:lo, rounded to
+// nearest (ties to even) with integer operations only, when the result is a
+// normal number (ok = true; FP64 arithmetic is the scarcest unit on this
+// part).  The magnitude is normalised to its leading 64 bits; the 11 bits
+// below the 53-bit significand and a sticky bit for everything under them
+// decide the rounding.
+__host__ __device__ __forceinline__ double i128_scaled(unsigned long long hi, unsigned long long lo,
+                                                       int x0, bool &ok) {
   ok = true;
-  if (acc == 0) return 0.0;
-  const bool neg = acc < 0;
-  const unsigned __int128 u = neg ? (unsigned __int128)(-acc) : (unsigned __int128)acc;
-  const unsigned long long hi = (unsigned long long)(u >> 64);
-  int msb = hi ? 127 - __clzll((long long)hi) : 63 - __clzll((long long)(unsigned long long)u);
-  unsigned long long mant;  // 53 significant bits
-  const int sh = msb - 52;
-  if (sh <= 0) {
-    mant = (unsigned long long)u << (-sh);
+  const bool neg = (long long)hi < 0;
+  if (neg) {  // |v|
+    lo = ~lo + 1ull;
+    hi = ~hi + (lo == 0 ? 1ull : 0ull);
+  }
+  if ((hi | lo) == 0) return 0.0;
+  int msb;
+  unsigned long long top;
+  bool sticky;
+  if (hi != 0) {
+    const int lz = clz64(hi);
+    msb = 127 - lz;
+    top = lz ? (hi << lz) | (lo >> (64 - lz)) : hi;
+    sticky = (lz ? lo << lz : lo) != 0;
   } else {
-    mant = (unsigned long long)(u >> sh);
-    const unsigned __int128 rem = u & (((unsigned __int128)1 << sh) - 1);
-    const unsigned __int128 half = (unsigned __int128)1 << (sh - 1);
-    if (rem > half || (rem == half && (mant & 1ull))) {
-      if (++mant >> 53) {  // rounded up to the next power of two
-        mant >>= 1;
-        ++msb;
-      }
+    const int lz = clz64(lo);
+    msb = 63 - lz;
+    top = lo << lz;
+    sticky = false;
+  }
+  unsigned long long mant = top >> 11;  // 53 bits, the leading one at bit 52
+  const unsigned rem = (unsigned)(top & 0x7FFu), half = 0x400u;
+  if (rem > half || (rem == half && (sticky || (mant & 1ull)))) {
+    if (++mant >> 53) {  // rounded up to the next power of two
+      mant >>= 1;
+      ++msb;
     }
   }
   const int E = msb + x0 + 1023;  // biased exponent of mant * 2^(msb - 52 + x0)
@@ -125,9 +156,8 @@ __device__ __forceinline__ double int_scaled(__int128 acc, int x0, bool &ok) {
     ok = false;
     return 0.0;
   }
-  const unsigned long long bits = ((unsigned long long)neg << 63) |
-                                  ((unsigned long long)E << 52) | (mant & 0xFFFFFFFFFFFFFull);
-  return __longlong_as_double((long long)bits);
+  return bits_double(((unsigned long long)neg << 63) | ((unsigned long long)E << 52) |
+                     (mant & 0xFFFFFFFFFFFFFull));
 }
 
 // alpha * 2^(ei + fj - 8(S+1)) * acc: one element of C from its level sum.
