@@ -613,11 +613,19 @@ a_totals_kernel(int64_t R, int64_t K, const int *__restrict__ expo,
   }
 }
 
-// op(B)'s R x K view (R = columns of op(B)), a warp per column: the column
-// maximum and exponent f_j, then (a second read, from L2) the column sums
+// op(B)'s R x K view (R = columns of op(B)), a warp per column, one read:
+// the column maximum and exponent f_j, and the column sums
 // s1_j 2^-f_j = sum_k |b_kj| 2^-f_j and s2_j 2^-(f_j + E_A) =
-// sum_k (alpha_k 2^-E_A)(|b_kj| 2^-f_j) in FP32.  Rows R..Rpad-1 get
+// sum_k (alpha_k 2^-E_A)(|b_kj| 2^-f_j) in FP32.  Each lane scales by the
+// exponent of its own running maximum and rescales its partial sums by a
+// power of two when that grows, and by 2^(f_lane - f_j) at the end; FP32
+// rounding commutes with power-of-two scaling, so the sums are those of
+// scaling by f_j throughout except for terms below 2^-126 of the maximum
+// (counted as dropped in the error bound either way).  Rows R..Rpad-1 get
 // exponent 0 and zero sums.
+__device__ __forceinline__ float pow2f(int d) {  // 2^d for d <= 0; 0 below FP32's normal range
+  return d < -126 ? 0.0f : __int_as_float((127 + d) << 23);
+}
 __global__ void col_stats_kcontig_kernel(int64_t R, int64_t Rpad, int64_t K,
                                          const double *__restrict__ X, int64_t ld,
                                          const float *__restrict__ alpha,
@@ -637,34 +645,50 @@ __global__ void col_stats_kcontig_kernel(int64_t R, int64_t Rpad, int64_t K,
   }
   const double *x = X + r * ld;
   unsigned long long best = 0;
+  int fl = 0;  // exponent of this lane's running maximum (while best != 0)
+  float a1 = 0.0f, a2 = 0.0f;
 #pragma unroll 4
   for (int64_t pp = lane; pp < K; pp += 32) {
-    const unsigned long long b = (unsigned long long)__double_as_longlong(x[pp]) &
+    const double xv = x[pp];
+    const unsigned long long b = (unsigned long long)__double_as_longlong(xv) &
                                  0x7FFFFFFFFFFFFFFFull;
-    best = b > best ? b : best;
-  }
-#pragma unroll
-  for (int off = 16; off > 0; off >>= 1) {
-    const unsigned long long o = __shfl_xor_sync(0xffffffffu, best, off);
-    best = o > best ? o : best;
-  }
-  const int f = ozd::exponent_of_max(best);
-  float a1 = 0.0f, a2 = 0.0f;
-  if (best != 0 && f != NONFINITE) {
-#pragma unroll 4
-    for (int64_t pp = lane; pp < K; pp += 32) {
-      const float v = scaled_abs(x[pp], f);
+    if (b > best) {
+      const int fn = ozd::exponent_of_max(b);
+      if (best != 0 && fn != NONFINITE && fl != NONFINITE && fn != fl) {
+        const float sc = pow2f(fl - fn);
+        a1 *= sc;
+        a2 *= sc;
+      }
+      best = b;
+      fl = fn;
+    }
+    if (fl != NONFINITE) {
+      const float v = scaled_abs(xv, fl);
       a1 += v;
       a2 = fmaf(alpha[pp], v, a2);
     }
+  }
+  unsigned long long wbest = best;
+#pragma unroll
+  for (int off = 16; off > 0; off >>= 1) {
+    const unsigned long long o = __shfl_xor_sync(0xffffffffu, wbest, off);
+    wbest = o > wbest ? o : wbest;
+  }
+  const int f = ozd::exponent_of_max(wbest);
+  if (wbest != 0 && f != NONFINITE) {
+    const float sc = best != 0 ? pow2f(fl - f) : 0.0f;  // fl <= f
+    a1 *= sc;
+    a2 *= sc;
 #pragma unroll
     for (int off = 16; off > 0; off >>= 1) {
       a1 += __shfl_down_sync(0xffffffffu, a1, off);
       a2 += __shfl_down_sync(0xffffffffu, a2, off);
     }
+  } else {
+    a1 = a2 = 0.0f;
   }
   if (lane == 0) {
-    out[r] = best;
+    out[r] = wbest;
     expo[r] = f;
     s1[r] = a1;
     s2[r] = a2;
@@ -1250,10 +1274,11 @@ void operand_exponents(bool kcontig, int64_t R, int64_t K, const double *X, int6
   if (kcontig) {
     { rowmax_kcontig_kernel<<<(unsigned)((R + 7) / 8), 256, 0, s>>>(R, K, X, ld, mx); count_launch(); }
   } else {
-    // K spans of 16..256 columns: enough CTAs for a short op(A) too
+    // K spans of 16..256 columns: 8 CTAs per SM (HBM needs them), a short
+    // op(A) too
     const int64_t gx = (R + 255) / 256;
     int64_t kspan = 256;
-    while (kspan > 16 && gx * ((K + kspan - 1) / kspan) < 2LL * persistent_ctas()) kspan /= 2;
+    while (kspan > 16 && gx * ((K + kspan - 1) / kspan) < 8LL * persistent_ctas()) kspan /= 2;
     dim3 g((unsigned)gx, (unsigned)((K + kspan - 1) / kspan));
     { rowmax_mcontig_kernel<<<g, 256, 0, s>>>(R, K, X, ld, kspan, mx); count_launch(); }
   }
@@ -1274,7 +1299,10 @@ void a_side_stats(bool kcontig, int64_t R, int64_t K, const double *X, int64_t l
                   const int *expo, const unsigned long long *mx, const int *emax, float *alpha,
                   double *totals, cudaStream_t s) {
   cudaMemsetAsync(alpha, 0, sizeof(float) * K, s);
-  const int64_t rspan = kcontig ? 256 : 1024;  // at most 256 rows summed by one thread
+  // at most 256 rows summed by one thread: a thread per k over 256 rows, or
+  // a block of 256 threads per k over up to 65536 rows (one block per
+  // column of op(A) up to that height)
+  const int64_t rspan = kcontig ? 256 : 65536;
   if (kcontig) {
     dim3 g((unsigned)((K + 255) / 256), (unsigned)((R + rspan - 1) / rspan));
     { abs_colsum_kernel<true><<<g, 256, 0, s>>>(R, K, X, ld, expo, emax, rspan, alpha); count_launch(); }
