@@ -203,9 +203,15 @@ void launch_dgemm_fp64_tri(int ta, int tb, int64_t m, int64_t n, int64_t k, doub
     dim3 grid((unsigned)((m + 63) / 64), (unsigned)((n + 63) / 64));
     { gemm_simt_kernel<double, 64, 64, 16, 4, 4><<<grid, 256, 0, s>>>(
         ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, skip); count_launch(); }
-  } else {
+  } else if (((m + 31) / 32) * ((n + 31) / 32) >= (int64_t)sm_count()) {
     dim3 grid((unsigned)((m + 31) / 32), (unsigned)((n + 31) / 32));
     { gemm_simt_kernel<double, 32, 32, 16, 2, 2><<<grid, 256, 0, s>>>(
+        ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, skip); count_launch(); }
+  } else {
+    // fewer 32 x 32 tiles than SMs (the Cholesky's in-block updates): 16 x 16
+    // tiles spread the FP64 work, which one SM does at ~2 FMA per clock
+    dim3 grid((unsigned)((m + 15) / 16), (unsigned)((n + 15) / 16));
+    { gemm_simt_kernel<double, 16, 16, 16, 1, 1><<<grid, 256, 0, s>>>(
         ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, tri, skip); count_launch(); }
   }
 }

@@ -427,10 +427,16 @@ __global__ void permute_rows_kernel(int64_t n, int64_t ncol, const int *__restri
 }
 
 // Unblocked Cholesky of an nb x nb diagonal block (nb <= PANEL_NB) in
-// shared memory, lapack/potf2/potf2_L.c:50-97 (upper: potf2_U.c, handled by
-// transposing into the lower form).  On the first pivot <= 0 the pivot value
-// is written back and info = row_off + j + 1; later calls see info != 0 and
-// return at once.
+// shared memory: lapack/potf2/potf2_L.c:50-97's algorithm (upper: potf2_U.c,
+// handled by transposing into the lower form), right-looking: column j's
+// pivot is a_jj less the updates already applied, its square root and one
+// reciprocal come from one thread, the column is scaled by it and every
+// thread takes a share of the rank-1 update of the trailing triangle.  (The
+// dot-product form ran one serial chain of up to nb FP64 FMAs per row in a
+// single warp, and a division in every thread, on the FP64 pipe that this
+// part has least of: 70 us per 32 x 32 block.)  On the first pivot <= 0 the
+// pivot value is written back and info = row_off + j + 1; later calls see
+// info != 0 and return at once.
 template <typename T>
 __global__ void __launch_bounds__(256)
 potf2_kernel(int upper, int nb, T *__restrict__ A, int64_t lda, int *__restrict__ info,
@@ -438,6 +444,7 @@ potf2_kernel(int upper, int nb, T *__restrict__ A, int64_t lda, int *__restrict_
   if (*info) return;
   __shared__ T S[PANEL_NB][PANEL_NB + 1];  // lower-triangular working copy
   __shared__ int s_fail;
+  __shared__ T s_rcp;
   const int tid = threadIdx.x;
   for (int e = tid; e < nb * nb; e += blockDim.x) {
     int r = e % nb, c = e / nb;
@@ -446,28 +453,28 @@ potf2_kernel(int upper, int nb, T *__restrict__ A, int64_t lda, int *__restrict_
   if (tid == 0) s_fail = -1;
   __syncthreads();
   for (int j = 0; j < nb; ++j) {
-    if (tid < 32) {
-      T acc = T(0);
-      for (int p = tid; p < j; p += 32) acc = fma(S[j][p], S[j][p], acc);
-#pragma unroll
-      for (int off = 16; off > 0; off >>= 1) acc += __shfl_down_sync(0xffffffffu, acc, off);
-      if (tid == 0) {
-        T ajj = S[j][j] - acc;
-        if (ajj <= T(0)) {
-          S[j][j] = ajj;
-          s_fail = j;
-        } else {
-          S[j][j] = sqrt(ajj);
-        }
+    if (tid == 0) {
+      const T ajj = S[j][j];
+      if (ajj <= T(0)) {
+        s_fail = j;
+      } else {
+        const T d = sqrt(ajj);
+        S[j][j] = d;
+        s_rcp = T(1) / d;
       }
     }
     __syncthreads();
     if (s_fail >= 0) break;
-    const T r = T(1) / S[j][j];
-    for (int i = j + 1 + tid; i < nb; i += blockDim.x) {
-      T t = T(0);
-      for (int p = 0; p < j; ++p) t = fma(S[i][p], S[j][p], t);
-      S[i][j] = (S[i][j] - t) * r;
+    const T r = s_rcp;
+    for (int i = j + 1 + tid; i < nb; i += blockDim.x) S[i][j] *= r;
+    __syncthreads();
+    // S[i][k] -= l_ij l_kj for j < k <= i < nb
+    const int m = nb - j - 1;
+    for (int e = tid; e < m * m; e += blockDim.x) {
+      const int ii = e % m, kk = e / m;
+      if (kk > ii) continue;
+      const int i = j + 1 + ii, k = j + 1 + kk;
+      S[i][k] = fma(-S[i][j], S[k][j], S[i][k]);
     }
     __syncthreads();
   }

@@ -88,10 +88,65 @@ trsm_diag_kernel(int trans, int unit, int ib, int64_t nvec, const T *__restrict_
     if (t < ib) base[t * stride] = x[t];
 }
 
+// The same solves with one warp per vector, lane t holding element t: for
+// few vectors (the Cholesky's in-block panels), where one thread per vector
+// leaves most SMs idle and runs each vector's ~NB^2/2 FP64 FMAs in series.
+// Step c finalises element c (times 1/T_cc) and broadcasts it; the lanes it
+// still affects apply their FMA.  Every element sees the same FMAs in the
+// same order as in the thread-per-vector kernel (Left: x_r -= T_rc x_c in
+// solve order; Right forward: x_c = (b_c - sum_p x_p T_pc) / T_cc with p
+// ascending), so the results are the same bit for bit.  Right backward sums
+// its dot products with p ascending against a descending solve, so it keeps
+// the thread-per-vector kernel.
+template <typename T, bool LEFT, bool FORWARD>
+__global__ void __launch_bounds__(128)
+trsm_diag_warp_kernel(int trans, int unit, int ib, int64_t nvec, const T *__restrict__ A,
+                      int64_t lda, T *__restrict__ B, int64_t ldb, const int *__restrict__ skip) {
+  if (skip && *skip) return;
+  __shared__ T Ts[TRSM_NB][TRSM_NB + 1];  // Ts[r][c] = op(Ablk)[r][c]
+  __shared__ T inv[TRSM_NB];
+  for (int e = threadIdx.x; e < TRSM_NB * TRSM_NB; e += blockDim.x) {
+    int r = e % TRSM_NB, c = e / TRSM_NB;
+    T v = T(0);
+    if (r < ib && c < ib) v = trans ? A[c + (int64_t)r * lda] : A[r + (int64_t)c * lda];
+    if (r >= ib && r == c) v = T(1);
+    Ts[r][c] = v;
+  }
+  __syncthreads();
+  for (int r = threadIdx.x; r < TRSM_NB; r += blockDim.x)
+    inv[r] = (unit && r < ib) ? T(1) : T(1) / Ts[r][r];
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int64_t v = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  if (v >= nvec) return;  // whole warps leave together
+  T *base = LEFT ? B + v * ldb : B + v;
+  const int64_t stride = LEFT ? 1 : ldb;
+  T x = lane < ib ? base[lane * stride] : T(0);
+#pragma unroll
+  for (int cc = 0; cc < TRSM_NB; ++cc) {
+    const int c = FORWARD ? cc : TRSM_NB - 1 - cc;
+    if (lane == c) x *= inv[c];
+    const T xc = __shfl_sync(0xffffffffu, x, c);
+    const bool later = FORWARD ? lane > c : lane < c;
+    if (later) x = LEFT ? fma(-Ts[lane][c], xc, x) : fma(-xc, Ts[c][lane], x);
+  }
+  if (lane < ib) base[lane * stride] = x;
+}
+
 template <typename T>
 void launch_trsm_diag(bool left, bool forward, int trans, int unit, int ib, int64_t nvec,
                       const T *A, int64_t lda, T *B, int64_t ldb, cudaStream_t s,
                       const int *skip) {
+  if (nvec < 4096 && (left || forward)) {
+    const unsigned wgrid = (unsigned)((nvec + 3) / 4);  // four vectors (warps) per block
+    if (left && forward)
+      { trsm_diag_warp_kernel<T, true, true><<<wgrid, 128, 0, s>>>(trans, unit, ib, nvec, A, lda, B, ldb, skip); count_launch(); }
+    else if (left)
+      { trsm_diag_warp_kernel<T, true, false><<<wgrid, 128, 0, s>>>(trans, unit, ib, nvec, A, lda, B, ldb, skip); count_launch(); }
+    else
+      { trsm_diag_warp_kernel<T, false, true><<<wgrid, 128, 0, s>>>(trans, unit, ib, nvec, A, lda, B, ldb, skip); count_launch(); }
+    return;
+  }
   const unsigned grid = (unsigned)((nvec + 127) / 128);
   if (left && forward)
     { trsm_diag_kernel<T, true, true><<<grid, 128, 0, s>>>(trans, unit, ib, nvec, A, lda, B, ldb, skip); count_launch(); }
