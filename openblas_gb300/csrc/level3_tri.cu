@@ -241,7 +241,7 @@ int dtrsm_device(int side, int uplo, int trans, int unit, int64_t m, int64_t n, 
 namespace {
 // Leaves of the recursive emulated-FP64 TRSM: solved by the native blocked
 // TRSM above.
-constexpr int64_t TRSM_EMU_LEAF = 256;
+constexpr int64_t TRSM_EMU_LEAF = 128;
 
 // Solve for the triangular index range [i0, i0 + len) of op(A) (rows of B on
 // the left, columns on the right): halves in the order of the substitution,
@@ -282,7 +282,7 @@ int trsm_rec_emulated(int side, int uplo, int trans, int unit_code, int64_t m, i
 // The caller-facing DTRSM (dtrsm_, cblas_dtrsm, gb_dtrsm_dev): with the
 // emulated-FP64 DGEMM selected (or in auto mode for a large solve) and a
 // triangle wider than one leaf, the recursive form above moves all but the
-// leaves' 256-wide diagonal solves onto the tensor cores; otherwise the
+// leaves' 128-wide diagonal solves onto the tensor cores; otherwise the
 // native blocked TRSM.
 int dtrsm_select(int side, int uplo, int trans, int unit, int64_t m, int64_t n, double alpha,
                  const double *A, int64_t lda, double *B, int64_t ldb, cudaStream_t s) {

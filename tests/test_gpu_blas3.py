@@ -339,7 +339,7 @@ def emulated_mode(gblib, gb_clean):
 @pytest.mark.parametrize("side,uplo,ta,diag", [
     (s, u, t, d) for s in "LR" for u in "UL" for t in "NT" for d in "UN"])
 def test_dtrsm_emulated_recursive_vs_oracle(orc, F, emulated_mode, side, uplo, ta, diag):
-    """Emulated-FP64 DTRSM: triangles wider than the 256-wide native leaves
+    """Emulated-FP64 DTRSM: triangles wider than the 128-wide native leaves
     recurse, the off-diagonal blocks applied by the emulated DGEMM (automatic
     per-tile choice); alpha != 1 and a padded ldb.  Same bound as the native
     blocked solve."""
