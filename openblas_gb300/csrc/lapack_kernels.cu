@@ -1395,6 +1395,30 @@ int lu_update<float>(LuCtx<float> &c, int64_t m, int64_t n, int64_t k, const flo
   return check_cuda(cudaGetLastError(), "sgemm launch");
 }
 
+// L11^-1 A12 of a blocked LU step.  With the emulated-FP64 updates and a
+// block wider than 128 the triangle is solved in two halves on the FP64 pipe
+// (lu_trsm) coupled by one emulated GEMM, B2 -= L21 X1, which halves the FP64
+// work (the single-launch solve ran at ~1/4 of the FP64 pipe over the whole
+// factorisation).  The form does not depend on the number of columns, and
+// the coupling's default form (digit slices at this depth) gives every
+// element from its own row and column only.
+template <typename T>
+int lu_trsm_block(const LuCtx<T> &c, int64_t n1, int64_t w, const T *L, int64_t ldl, T *B,
+                  int64_t ldb, cudaStream_t s) {
+  if constexpr (sizeof(T) == 8) {
+    if (c.gemm_mode == 1 && n1 > 128 && w > 0) {
+      const int64_t h = n1 / 2;
+      int st;
+      if ((st = lu_trsm<T>(h, w, L, ldl, B, ldb, s))) return st;
+      if ((st = dgemm_emulated(0, 0, n1 - h, w, h, -1.0, L + h, ldl, B, ldb, 1.0, B + h, ldb, 0,
+                               s)))
+        return st;
+      return lu_trsm<T>(n1 - h, w, L + h + h * ldl, ldl, B + h, ldb, s);
+    }
+  }
+  return lu_trsm<T>(n1, w, L, ldl, B, ldb, s);
+}
+
 template <typename T>
 int lu_panel_factor(LuCtx<T> &c, int64_t r0, int64_t m, int n) {
   ProfileScope prof("lu_panel", c.s);
@@ -1511,7 +1535,7 @@ int lu_blocked(LuCtx<T> &c, int64_t m, int64_t mn, int64_t n) {
       T *A12 = c.A + j0 + (j0 + jb) * lda;
       {
         ProfileScope prof("lu_trsm", c.s);
-        if ((st = lu_trsm<T>(jb, n - j0 - jb, L11, lda, A12, lda, c.s))) return st;
+        if ((st = lu_trsm_block<T>(c, jb, n - j0 - jb, L11, lda, A12, lda, c.s))) return st;
       }
       if (j0 + jb < m) {
         ProfileScope prof("lu_gemm", c.s);
