@@ -802,9 +802,13 @@ split_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
              const int *__restrict__ run_if) {
   __shared__ double tile[32][65];
   if (run_if && *run_if == 0) return;
-  const int64_t r0 = (int64_t)blockIdx.y * 32, p0 = (int64_t)blockIdx.x * 64;
-  if (s_tiles) S = s_tiles[r0 / BN];  // the slice count of this 256-row tile (automatic mode)
-  if (S == 0) return;                 // a modular tile
+  // a grid-stride loop over the tiles (see split_grid)
+  const int64_t tiles_x = Kpad / 64, ntiles = tiles_x * (Rpad / 32);
+  for (int64_t tid_t = blockIdx.x; tid_t < ntiles; tid_t += gridDim.x) {
+  const int64_t r0 = (tid_t / tiles_x) * 32, p0 = (tid_t % tiles_x) * 64;
+  // the slice count of this 256-row tile (automatic mode); 0: a modular tile
+  const int St = s_tiles ? s_tiles[r0 / BN] : S;
+  if (St == 0) continue;
   const int tid = threadIdx.x;
   // all eight loads of a thread in flight before the shared-memory stores
   double vin[8];
@@ -832,9 +836,9 @@ split_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
   unsigned long long mag[8];
   bool neg[8];
 #pragma unroll
-  for (int j = 0; j < 8; ++j) mag[j] = ozd::digit_magnitude(tile[rr][pc + j], e, S, neg[j]);
-  for (int s = 1; s <= S; ++s) {
-    const int sh = DIGIT_BITS * (S - s);
+  for (int j = 0; j < 8; ++j) mag[j] = ozd::digit_magnitude(tile[rr][pc + j], e, St, neg[j]);
+  for (int s = 1; s <= St; ++s) {
+    const int sh = DIGIT_BITS * (St - s);
     __align__(16) __nv_bfloat16 out[8];
 #pragma unroll
     for (int j = 0; j < 8; ++j) {
@@ -843,6 +847,8 @@ split_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld,
     }
     __nv_bfloat16 *dst = slices + ((int64_t)(s - 1) * Rpad + r) * Kpad + p0 + pc;
     *reinterpret_cast<uint4 *>(dst) = *reinterpret_cast<const uint4 *>(out);
+  }
+  __syncthreads();  // the tile buffer is refilled by the next iteration
   }
 }
 
@@ -1237,10 +1243,19 @@ int make_map(CUtensorMap *map, void *base, int64_t rows, int64_t kpad, int box_r
 inline int64_t round_up(int64_t x, int64_t a) { return (x + a - 1) / a * a; }
 inline size_t align256(size_t x) { return (x + 255) & ~size_t(255); }
 
+// Blocks of the digit split's grid-stride loop over 32 x 64 tiles: one per
+// tile, or, for a launch predicated on the device (the automatic mode's
+// digit pass, off unless some tile needs digits), eight per SM, so that a
+// launch with nothing to do costs a few CTAs.
+static unsigned split_grid(int64_t Rpad, int64_t Kpad, bool predicated) {
+  const int64_t ntiles = (Kpad / 64) * (Rpad / 32), cap = 8LL * sm_count();
+  return (unsigned)(predicated && ntiles > cap ? cap : ntiles);
+}
+
 void launch_split(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld,
                   const int *expo, int S, int64_t Rpad, int64_t Kpad, __nv_bfloat16 *slices,
                   const int *s_tiles, const int *run_if, cudaStream_t s) {
-  dim3 g2((unsigned)(Kpad / 64), (unsigned)(Rpad / 32));
+  const unsigned g2 = split_grid(Rpad, Kpad, run_if != nullptr);
   if (kcontig)
     split_kernel<true><<<g2, 256, 0, s>>>(R, K, X, ld, expo, S, Rpad, Kpad, slices, s_tiles,
                                           run_if);
