@@ -87,13 +87,13 @@ static int dgemm_dispatch(int ta, int tb, int64_t m, int64_t n, int64_t k, doubl
   return dgemm_native(ta, tb, m, n, k, alpha, A, lda, B, ldb, beta, C, ldc, s);
 }
 
-// Host-pointer emulated DGEMM pipelined over column blocks of op(B) and C
-// and over the 4096-deep K segments the emulated engine works in.  op(A) and
-// every block of op(B) go up segment by segment, so the first slice GEMM
-// starts once the first segment of op(A) and of block 0 are on the device,
-// while the rest is still on its way; block j+1 uploads on the copy-in
-// stream while block j computes, and C's block j comes down on the copy-out
-// stream while later blocks compute.  The result is the one of the
+// Host-pointer emulated DGEMM pipelined over column blocks of op(B) and C.
+// With one engine K segment and op(A) = A^T, op(A) goes up in row blocks,
+// each prepared (row maxima, exponents, residues) while the next uploads;
+// otherwise op(A) and every block of op(B) go up in 4096-deep K pieces, so
+// the first slice GEMM starts once the first segment is on the device.  Block j+1 uploads on
+// the copy-in stream while block j computes, and C's block j comes down on
+// the copy-out stream while later blocks compute.  The result is the one of the
 // single-call emulated GEMM bit for bit (each C(i,j) sees only row i of
 // op(A) and column j of op(B)).  The upload of block j+1 and the download of
 // block j-1 are issued after block j's kernels, so that pageable host
@@ -174,6 +174,9 @@ struct PipelinedDgemm : EmuBlockHooks {
   double *dA = nullptr, *dB = nullptr, *dC = nullptr;
   int64_t dlda = 0, dldb = 0;
   std::vector<cudaEvent_t> a_up, up, done;  // a_up[seg], up[block * nseg + seg], done[block]
+  // op(A) in row blocks of arb rows (0: in K pieces), ar_up[row block]
+  int64_t arb = 0;
+  std::vector<cudaEvent_t> ar_up;
   // GB_VERBOSE >= 3: a timeline of the copies and blocks (timing events)
   struct Mark {
     cudaEvent_t e;
@@ -226,6 +229,24 @@ struct PipelinedDgemm : EmuBlockHooks {
     mark(cin, "op(A) segment uploaded", sg);
     return GB_SUCCESS;
   }
+  // rows [b arb, b arb + arb) of op(A): rows of A (ta = 0) or columns of A
+  int upload_a_rows(int64_t b) {
+    const int64_t i0 = b * arb, rb = (m - i0) < arb ? (m - i0) : arb;
+    if (ta)
+      GB_CUDA(cudaMemcpy2DAsync(dA + i0 * dlda, dlda * 8, A + i0 * lda, lda * 8, k * 8, rb,
+                                cudaMemcpyHostToDevice, cin));
+    else
+      GB_CUDA(cudaMemcpy2DAsync(dA + i0, dlda * 8, A + i0, lda * 8, rb * 8, k,
+                                cudaMemcpyHostToDevice, cin));
+    GB_CUDA(cudaEventRecord(ar_up[b], cin));
+    mark(cin, "op(A) row block uploaded", b);
+    return GB_SUCCESS;
+  }
+  int64_t a_row_block() override { return arb; }
+  int a_rows(int64_t i0, int64_t) override {
+    GB_CUDA(cudaStreamWaitEvent(s, ar_up[i0 / arb], 0));
+    return GB_SUCCESS;
+  }
   // segment sg of block j of op(B) (and C's block with the first segment)
   int upload(int64_t j, int64_t sg) {
     const int64_t j0 = bs[j], jn = bs[j + 1] - bs[j];
@@ -267,18 +288,24 @@ struct PipelinedDgemm : EmuBlockHooks {
     return GB_SUCCESS;
   }
   // every upload piece overlapping [k0, k0 + kk)
-  int segment(int64_t j0, int64_t, int64_t k0, int64_t kk) override {
-    for (int64_t sg = k0 / PIPE_K_SEGMENT; sg * PIPE_K_SEGMENT < k0 + kk; ++sg) {
-      GB_CUDA(cudaStreamWaitEvent(s, a_up[sg], 0));
-      GB_CUDA(cudaStreamWaitEvent(s, up[block_of(j0) * nseg + sg], 0));
+  // op(A) is complete on the device: its last row block, or its K pieces
+  int wait_a(int64_t k0, int64_t kk) {
+    if (arb > 0) {
+      GB_CUDA(cudaStreamWaitEvent(s, ar_up.back(), 0));
+      return GB_SUCCESS;
     }
-    return GB_SUCCESS;
-  }
-  int a_range(int64_t k0, int64_t kk) override {
     for (int64_t sg = k0 / PIPE_K_SEGMENT; sg * PIPE_K_SEGMENT < k0 + kk; ++sg)
       GB_CUDA(cudaStreamWaitEvent(s, a_up[sg], 0));
     return GB_SUCCESS;
   }
+  int segment(int64_t j0, int64_t, int64_t k0, int64_t kk) override {
+    int st = wait_a(k0, kk);
+    if (st) return st;
+    for (int64_t sg = k0 / PIPE_K_SEGMENT; sg * PIPE_K_SEGMENT < k0 + kk; ++sg)
+      GB_CUDA(cudaStreamWaitEvent(s, up[block_of(j0) * nseg + sg], 0));
+    return GB_SUCCESS;
+  }
+  int a_range(int64_t k0, int64_t kk) override { return wait_a(k0, kk); }
   int64_t block_cols(int64_t j0, int64_t) override {
     const int64_t j = block_of(j0);
     return bs[j + 1] - bs[j];
@@ -340,9 +367,20 @@ static int dgemm_host_pipelined(int ta, int tb, int64_t m, int64_t n, int64_t k,
   p.a_up.assign(p.nseg, nullptr);
   p.up.assign(nblk * p.nseg, nullptr);
   p.done.assign(nblk, nullptr);
+  // one K segment in the engine and op(A) = A^T (its rows are A's contiguous
+  // columns): op(A) goes up in eight row blocks (at least 512 rows each),
+  // each prepared while the next uploads.  With op(A) = A the rows are
+  // strided on the host, and the 2D copies of 8-16 KB rows ran at 107-175
+  // instead of ~210 GB/s, more than the overlap saved: K pieces then.
+  if (ta && emulated_k_segment(ozaki_caller_slices()) >= k) {
+    const int64_t rb = ((m + 7) / 8 + 127) / 128 * 128;
+    p.arb = rb < 512 ? 512 : rb;
+    if (p.arb >= m) p.arb = 0;
+  }
+  p.ar_up.assign(p.arb > 0 ? (m + p.arb - 1) / p.arb : 0, nullptr);
   cudaEvent_t ready = nullptr, out_done = nullptr;
   auto run = [&]() -> int {
-    for (auto *v : {&p.a_up, &p.up, &p.done})
+    for (auto *v : {&p.a_up, &p.up, &p.done, &p.ar_up})
       for (cudaEvent_t &e : *v) GB_CUDA(cudaEventCreateWithFlags(&e, cudaEventDisableTiming));
     GB_CUDA(cudaEventCreateWithFlags(&ready, cudaEventDisableTiming));
     GB_CUDA(cudaEventCreateWithFlags(&out_done, cudaEventDisableTiming));
@@ -354,8 +392,14 @@ static int dgemm_host_pipelined(int ta, int tb, int64_t m, int64_t n, int64_t k,
     // op(A)'s pieces of a segment first (its preparation needs the whole
     // segment and overlaps block 0's upload), then block 0's
     int st;
+    if (p.arb > 0) {  // op(A) by row blocks, then block 0 of op(B)
+      for (int64_t b = 0; b < (int64_t)p.ar_up.size(); ++b)
+        if ((st = p.upload_a_rows(b))) return st;
+      for (int64_t sg = 0; sg < p.nseg; ++sg)
+        if ((st = p.upload(0, sg))) return st;
+    }
     const int64_t eseg = emulated_k_segment(ozaki_caller_slices()) / PIPE_K_SEGMENT;
-    for (int64_t g0 = 0; g0 < p.nseg; g0 += eseg) {
+    for (int64_t g0 = 0; p.arb == 0 && g0 < p.nseg; g0 += eseg) {
       const int64_t g1 = g0 + eseg < p.nseg ? g0 + eseg : p.nseg;
       for (int64_t sg = g0; sg < g1; ++sg)
         if ((st = p.upload_a(sg))) return st;
@@ -378,7 +422,7 @@ static int dgemm_host_pipelined(int ta, int tb, int64_t m, int64_t n, int64_t k,
   p.report();
   if (!st) finish_blocking(p.s);
   else cudaStreamSynchronize(p.s);
-  for (auto *v : {&p.a_up, &p.up, &p.done})
+  for (auto *v : {&p.a_up, &p.up, &p.done, &p.ar_up})
     for (cudaEvent_t e : *v)
       if (e) cudaEventDestroy(e);
   if (ready) cudaEventDestroy(ready);

@@ -196,13 +196,19 @@ constexpr int64_t EMU_K_SEGMENT = 4096;
 // the block is used (e.g. to wait for that range of op(A) and op(B)), and
 // hooks->a_range(k0, kk) before op(A)'s columns [k0, k0 + kk) are first read.
 // hooks->block_cols(j0, nb) gives the width of the block starting at column
-// j0 (a multiple of 256, at most nb; the default: nb).
+// j0 (a multiple of 256, at most nb; the default: nb).  When
+// hooks->a_row_block() is positive (a multiple of 128), op(A) arrives in
+// blocks of that many rows, and with a single K segment each block's row
+// maxima, exponents and residues are prepared as it arrives;
+// hooks->a_rows(i0, rb) runs before rows [i0, i0 + rb) of op(A) are read.
 struct EmuBlockHooks {
   virtual int before(int64_t j0, int64_t jn, const double **Bj, int64_t *ldb, double **Cj,
                      int64_t *ldc) = 0;
   virtual int segment(int64_t, int64_t, int64_t, int64_t) { return GB_SUCCESS; }
   virtual int a_range(int64_t, int64_t) { return GB_SUCCESS; }
   virtual int64_t block_cols(int64_t, int64_t nb) { return nb; }
+  virtual int64_t a_row_block() { return 0; }
+  virtual int a_rows(int64_t, int64_t) { return GB_SUCCESS; }
   virtual int after(int64_t j0, int64_t jn) = 0;
   virtual ~EmuBlockHooks() = default;
 };

@@ -1265,11 +1265,13 @@ void launch_split(bool kcontig, int64_t R, int64_t K, const double *X, int64_t l
   count_launch();
 }
 
+// Rpad: the planes' row stride; Rgrid (default Rpad): the rows written, a
+// multiple of 32 (less than Rpad for a block of rows at res + i0 Kpad).
 void launch_split_mod(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld,
                       const int *expo, int64_t Rpad, int64_t Kpad, __nv_bfloat16 *res,
                       const int *s_tiles, const int *run_if, const ModTable &tab,
-                      cudaStream_t s) {
-  dim3 g2((unsigned)(Kpad / 64), (unsigned)(Rpad / 32));
+                      cudaStream_t s, int64_t Rgrid = 0) {
+  dim3 g2((unsigned)(Kpad / 64), (unsigned)((Rgrid > 0 ? Rgrid : Rpad) / 32));
   if (kcontig)
     split_mod_kernel<true><<<g2, 256, 0, s>>>(R, K, X, ld, expo, Rpad, Kpad, res, s_tiles,
                                               run_if, tab);
@@ -1283,9 +1285,9 @@ void launch_split_mod(bool kcontig, int64_t R, int64_t K, const double *X, int64
 // maximum over the non-zero finite rows as well).
 void operand_exponents(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld,
                        int64_t Rpad, unsigned long long *mx, int *expo, cudaStream_t s,
-                       int *emax = nullptr) {
+                       int *emax = nullptr, bool init_emax = true) {
   cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * Rpad, s);
-  if (emax) cudaMemsetAsync(emax, 0x80, sizeof(int), s);  // a large negative value
+  if (emax && init_emax) cudaMemsetAsync(emax, 0x80, sizeof(int), s);  // a large negative value
   if (kcontig) {
     { rowmax_kcontig_kernel<<<(unsigned)((R + 7) / 8), 256, 0, s>>>(R, K, X, ld, mx); count_launch(); }
   } else {
@@ -1551,7 +1553,31 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
     GB_CUDA(cudaGetLastError());
     return GB_SUCCESS;
   };
-  if (a_once) {
+  const int64_t arb = a_early && hooks ? hooks->a_row_block() : 0;
+  if (a_once && arb > 0 && arb < m) {
+    // op(A) arrives in row blocks: each block's row maxima and exponents
+    // (and, with the modular scheme, residues) while the next one uploads;
+    // the choice statistics need every row and follow the last block.  Every
+    // value is the one of the whole-operand preparation (all per row).
+    const ASeg a = aseg(0);
+    const int64_t kp = round_up(k, BK);
+    if (a.emax) cudaMemsetAsync(a.emax, 0x80, sizeof(int), s);
+    for (int64_t i0 = 0; i0 < m; i0 += arb) {
+      const int64_t rb = (m - i0) < arb ? (m - i0) : arb;
+      const int64_t rb_pad = i0 + rb < m ? rb : m_pad - i0;  // the last block pads to m_pad
+      if ((st = hooks->a_rows(i0, rb))) return st;
+      const double *Xi = ta ? A + i0 * lda : A + i0;
+      operand_exponents(ta != 0, rb, k, Xi, lda, rb_pad, mx + i0, a.ea + i0, s, a.emax, false);
+      if (modular)
+        launch_split_mod(ta != 0, rb, k, Xi, lda, a.ea + i0, m_pad, kp, a.res + i0 * kp, nullptr,
+                         nullptr, tab, s, rb_pad);
+    }
+    if (automatic) a_side_stats(ta != 0, m, k, A, lda, a.ea, mx, a.emax, a.alpha, a.tot, s);
+    if (a_dig_lazy) cudaMemsetAsync(latch, 0, 2 * sizeof(int), s);
+    if (modular && (st = make_map(&mapAr[0], a.res, (int64_t)MOD_COUNT * m_pad, kp, BM)))
+      return st;
+    if (Sa > 0 && !a_dig_lazy && (st = split_a(0, 0, k, nullptr))) return st;
+  } else if (a_once) {
     if (hooks && (st = hooks->a_range(0, k))) return st;
     prep_a(0, 0, k);
     if (a_dig_lazy) cudaMemsetAsync(latch, 0, 2 * sizeof(int), s);

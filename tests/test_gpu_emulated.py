@@ -229,21 +229,34 @@ def test_host_pipelined_several_k_segments(F, emulated, gblib):
 def test_host_pipelined_planned_blocks(F, emulated, gblib, hard):
     """A shape whose block plan is uneven (one-wave edge blocks of 4 tiles
     at m = 4096, two or three wider blocks between them, a ragged last
-    one): still bit-identical to the single device call.  With `hard`, 200
+    one), op(A) = A^T arriving in eight row blocks prepared one by one:
+    still bit-identical to the single device call.  With `hard`, 200
     columns of op(B) in a late block meet a tiny column of op(A) (the
     construction of the per-tile test below), so that block alone needs
     digit slices: op(A)'s digit split then runs for it only."""
     m, n, k = 4096, 8292, 700
-    A, B, C = W.gemm_operands(93, m, n, k, "N", "T", pad=1)
+    A, B, C = W.gemm_operands(93, m, n, k, "T", "T", pad=1)  # op(A) = A^T: row blocks
     if hard:
-        A[:, 0] *= 2.0 ** -30
+        A[0, :] *= 2.0 ** -30
         B[6000:6200, :k] = np.ldexp(W.uniform(94, (200, k)), -40)
         B[6000:6200, 0] = 1.0
-    ref = _device_emulated(gblib, "N", "T", m, n, k, 0.75, A, B, -1.5, C)
-    F.dgemm("N", "T", m, n, k, 0.75, A, A.shape[0], B, B.shape[0], -1.5, C, C.shape[0])
+    ref = _device_emulated(gblib, "T", "T", m, n, k, 0.75, A, B, -1.5, C)
+    F.dgemm("T", "T", m, n, k, 0.75, A, A.shape[0], B, B.shape[0], -1.5, C, C.shape[0])
     assert np.array_equal(C, ref)
     if hard:
         assert (gblib.gb_last_ozaki_moduli(), gblib.gb_last_ozaki_slices()) == (MOD_COUNT, 8)
+
+
+def test_host_pipelined_two_engine_segments(F, emulated, gblib):
+    """K beyond one 8192-deep engine segment with op(A) = A^T: op(A) goes up
+    in K pieces (row blocks need a single segment) and is prepared per
+    segment inside the first column block; still bit-identical to the single
+    device call."""
+    m, n, k = 2048, 6400, 9000
+    A, B, C = W.gemm_operands(95, m, n, k, "T", "N")
+    ref = _device_emulated(gblib, "T", "N", m, n, k, 1.0, A, B, 0.0, C)
+    F.dgemm("T", "N", m, n, k, 1.0, A, A.shape[0], B, B.shape[0], 0.0, C, C.shape[0])
+    assert np.array_equal(C, ref)
 
 
 def test_host_pipelined_pinned_buffers(emulated, gblib):
