@@ -232,7 +232,7 @@ int xerbla_(const char *name, const blasint *info, blasint len);
 
 /* DGEMM precision modes */
 #define GB_DGEMM_NATIVE 0   /* FP64 FMA units */
-#define GB_DGEMM_EMULATED 1 /* Ozaki split into 8-bit slices on bf16 tensor cores */
+#define GB_DGEMM_EMULATED 1 /* Ozaki schemes (residues or 8-bit slices) on bf16 tensor cores */
 #define GB_DGEMM_AUTO 2     /* emulated when the shape is large enough to win */
 
 /* Stream used by every entry point of the calling thread (NULL = the
@@ -248,8 +248,10 @@ void gb_clear_error(void);
 /* Last argument error seen by xerbla on this thread: routine name (up to 8
  * chars + NUL) and parameter position; returns that position or 0. */
 int gb_last_xerbla(char *name, int len);
-/* Precision of the FP64 GEMM behind cblas_dgemm/dgemm_ and the LAPACK
- * trailing updates' caller-facing DGEMM (default from GB_DGEMM_MODE). */
+/* Precision of the FP64 GEMM behind cblas_dgemm/dgemm_, the GEMMs inside
+ * dsyrk_/dtrmm_/dsyr2k_/dgemmt_/zgemm_, the LU and Cholesky trailing updates,
+ * and the form of dtrsm_ (emulated: recursive, 128-wide triangles solved in
+ * FP64, the rest on the emulated GEMM); default from GB_DGEMM_MODE. */
 int gb_set_dgemm_mode(int mode);
 int gb_get_dgemm_mode(void);
 /* FP32 GEMM behind sgemm_/cblas_sgemm and the FP32 LU of the mixed solver

@@ -81,8 +81,9 @@ def test_worst_case_digits_exact(F, emulated, gblib, scheme):
 
 def test_multi_digit_exact(F, emulated):
     """Operands with several nonzero 8-bit digits (integers below 2^41 with a
-    common row scale) are represented exactly by the default 7 slices
-    (56 bits)."""
+    common row scale) are represented exactly by the default automatic form
+    (a 55-bit cut for the modular scheme, or up to 8 digit slices), so the
+    product is exact up to its final rounding."""
     m, n, k = 96, 96, 300
     A = _int_matrix(3, (m, k), -(2 ** 20), 2 ** 20)
     B = _int_matrix(4, (k, n), -(2 ** 20), 2 ** 20)
