@@ -121,6 +121,7 @@ struct GemmParams {
   int kblocks;
   int kblock0;  // first K block of the operands' tensor maps this launch reads
   int m_pad, n_pad;
+  int b_rows;  // rows of one slice (residue) plane of the op(B) operand
   int64_t plane_stride;
   int *planes;
   int *status;
@@ -281,7 +282,7 @@ slice_gemm_kernel(const __grid_constant__ CUtensorMap tmA, const __grid_constant
             int sa, sb;
             product_slices<MOD>(l, s, sa, sb);
             const int rowA = sa * p.m_pad + mt * BM;
-            const int rowB = sb * p.n_pad + nt * BN;
+            const int rowB = sb * p.b_rows + nt * BN;
             for (int kc = 0; ok && kc < nkc; ++kc) {
               const int kb1 = min(p.kblocks, (kc + 1) * KC_BLOCKS);
               for (int kb = kc * KC_BLOCKS; kb < kb1; ++kb) {
@@ -1513,7 +1514,7 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
     return make_map(&mapAr[a_cache ? sg : 0], a.res, (int64_t)MOD_COUNT * m_pad, kp, BM);
   };
   auto gemm = [&](bool mod, const CUtensorMap &ma, const CUtensorMap &mb, int64_t jn_pad,
-                  int64_t kb0, int64_t kp, const int *run_if) -> int {
+                  int64_t kb0, int64_t kp, const int *run_if, int64_t b_rows) -> int {
     GemmParams gp{};
     gp.S = Sa;
     gp.m_tiles = (int)(m_pad / BM);
@@ -1526,6 +1527,7 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
     gp.kblock0 = (int)kb0;
     gp.m_pad = (int)m_pad;
     gp.n_pad = (int)jn_pad;
+    gp.b_rows = (int)b_rows;
     gp.plane_stride = m_pad * jn_pad;
     gp.planes = planes;
     gp.status = ctx().d_status;
@@ -1589,6 +1591,13 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
     if (jn > nb || jn <= 0) jn = nb;
     if (jn > n - j0) jn = n - j0;
     const int64_t jn_pad = round_up(jn, BN);
+    // op(B) = op(A)^T (SYRK-shaped products: the same matrix, one block):
+    // op(B)'s residues and digits are op(A)'s rows, split with the same
+    // exponents, so the B operand reads op(A)'s planes (whose plane stride
+    // is m_pad rows; tiles past n read the next plane or TMA's zero fill,
+    // only for columns that are never stored)
+    const bool b_from_a = B != nullptr && B == A && ldb == lda && ta != tb && m == n && jn == n;
+    const int64_t b_rows = b_from_a ? m_pad : jn_pad;
     const double *Bj = tb ? B + j0 : B + j0 * ldb;
     double *Cj = C + j0 * ldc;
     int64_t ldbj = ldb, ldcj = ldc;
@@ -1618,25 +1627,37 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       if (fixed_mod) {
         // every tile on the modular scheme: no statistics, no choice
         if (!a_both && (st = split_a_mod(sg, k0, kk, nullptr))) return st;
-        operand_exponents(tb == 0, jn, kk, Bk, ldbj, jn_pad, mx + m_pad, eb, s);
-        launch_split_mod(tb == 0, jn, kk, Bk, ldbj, eb, jn_pad, kp, slb, nullptr, nullptr, tab, s);
-        if ((st = make_map(&mapBr, slb, (int64_t)MOD_COUNT * jn_pad, kp, BN))) return st;
-        if ((st = gemm(true, mapAr[a_cache ? sg : 0], mapBr, jn_pad, 0, kp, nullptr))) return st;
+        if (b_from_a) {
+          if ((st = make_map(&mapBr, a.res, (int64_t)MOD_COUNT * m_pad, kp, BN))) return st;
+        } else {
+          operand_exponents(tb == 0, jn, kk, Bk, ldbj, jn_pad, mx + m_pad, eb, s);
+          launch_split_mod(tb == 0, jn, kk, Bk, ldbj, eb, jn_pad, kp, slb, nullptr, nullptr, tab, s);
+          if ((st = make_map(&mapBr, slb, (int64_t)MOD_COUNT * jn_pad, kp, BN))) return st;
+        }
+        if ((st = gemm(true, mapAr[a_cache ? sg : 0], mapBr, jn_pad, 0, kp, nullptr, b_rows)))
+          return st;
         reconstruct_tile_kernel<<<g, 256, 0, s>>>(
-            m, jn, m_tiles, ps, reinterpret_cast<const uint16_t *>(planes), a.ea, eb, alpha, bseg,
-            Cj, ldcj, ta, tb, kk, Ak, lda, Bk, ldbj, tri, skip, nullptr, nullptr, tab);
+            m, jn, m_tiles, ps, reinterpret_cast<const uint16_t *>(planes), a.ea,
+            b_from_a ? a.ea : eb, alpha, bseg, Cj, ldcj, ta, tb, kk, Ak, lda, Bk, ldbj, tri, skip,
+            nullptr, nullptr, tab);
         count_launch();
         if ((st = check_cuda(cudaGetLastError(), "emulated dgemm"))) return st;
         continue;
       }
       if (!automatic) {
         if (!a_both && (st = split_a(sg, k0, kk, nullptr))) return st;
-        split_operand(tb == 0, jn, kk, Bk, ldbj, S, jn_pad, kp, mx + m_pad, eb, slb, s);
-        if ((st = make_map(&mapB, slb, (int64_t)Sa * jn_pad, kp, BN))) return st;
-        if ((st = gemm(false, mapA[a_cache ? sg : 0], mapB, jn_pad, 0, kp, nullptr))) return st;
+        if (b_from_a) {
+          if ((st = make_map(&mapB, a.dig, (int64_t)Sa * m_pad, kp, BN))) return st;
+        } else {
+          split_operand(tb == 0, jn, kk, Bk, ldbj, S, jn_pad, kp, mx + m_pad, eb, slb, s);
+          if ((st = make_map(&mapB, slb, (int64_t)Sa * jn_pad, kp, BN))) return st;
+        }
+        if ((st = gemm(false, mapA[a_cache ? sg : 0], mapB, jn_pad, 0, kp, nullptr, b_rows)))
+          return st;
+        const int *ebk = b_from_a ? a.ea : eb;
 #define GB_RECOMBINE(SS)                                                                        \
   case SS:                                                                                      \
-    recombine_tile_kernel<SS><<<g, 256, 0, s>>>(m, jn, m_tiles, ps, planes, a.ea, eb, alpha,    \
+    recombine_tile_kernel<SS><<<g, 256, 0, s>>>(m, jn, m_tiles, ps, planes, a.ea, ebk, alpha,   \
                                                 bseg, Cj, ldcj, ta, tb, kk, Ak, lda, Bk, ldbj,  \
                                                 tri, skip);                                     \
     break;
@@ -1655,9 +1676,14 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       if (modular) {
         // ---- modular pass (tiles with s_tiles = 0)
         if (!a_both && (st = split_a_mod(sg, k0, kk, pass))) return st;
-        launch_split_mod(tb == 0, jn, kk, Bk, ldbj, eb, jn_pad, kp, slb, s_tiles, pass, tab, s);
-        if ((st = make_map(&mapBr, slb, (int64_t)MOD_COUNT * jn_pad, kp, BN))) return st;
-        if ((st = gemm(true, mapAr[a_cache ? sg : 0], mapBr, jn_pad, 0, kp, pass))) return st;
+        if (b_from_a) {
+          if ((st = make_map(&mapBr, a.res, (int64_t)MOD_COUNT * m_pad, kp, BN))) return st;
+        } else {
+          launch_split_mod(tb == 0, jn, kk, Bk, ldbj, eb, jn_pad, kp, slb, s_tiles, pass, tab, s);
+          if ((st = make_map(&mapBr, slb, (int64_t)MOD_COUNT * jn_pad, kp, BN))) return st;
+        }
+        if ((st = gemm(true, mapAr[a_cache ? sg : 0], mapBr, jn_pad, 0, kp, pass, b_rows)))
+          return st;
         reconstruct_tile_kernel<<<g, 256, 0, s>>>(
             m, jn, m_tiles, ps, reinterpret_cast<const uint16_t *>(planes), a.ea, eb, alpha, bseg,
             Cj, ldcj, ta, tb, kk, Ak, lda, Bk, ldbj, tri, skip, s_tiles, pass, tab);
@@ -1673,13 +1699,17 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       } else if (!a_both && (st = split_a(sg, k0, kk, pass + 1))) {
         return st;
       }
-      launch_split(tb == 0, jn, kk, Bk, ldbj, eb, MAX_SLICES, jn_pad, kp, slb, s_tiles, pass + 1,
-                   s);
-      if ((st = make_map(&mapB, slb, (int64_t)Sa * jn_pad, kp, BN))) return st;
+      if (b_from_a) {
+        if ((st = make_map(&mapB, a.dig, (int64_t)Sa * m_pad, kp, BN))) return st;
+      } else {
+        launch_split(tb == 0, jn, kk, Bk, ldbj, eb, MAX_SLICES, jn_pad, kp, slb, s_tiles,
+                     pass + 1, s);
+        if ((st = make_map(&mapB, slb, (int64_t)Sa * jn_pad, kp, BN))) return st;
+      }
       for (int64_t u0 = 0; u0 < kk; u0 += MAX_K_SEGMENT) {
         const int64_t uk = (kk - u0) < MAX_K_SEGMENT ? (kk - u0) : MAX_K_SEGMENT;
         if ((st = gemm(false, mapA[a_cache ? sg : 0], mapB, jn_pad, u0 / BK, round_up(uk, BK),
-                       pass + 1)))
+                       pass + 1, b_rows)))
           return st;
         const double *Au = ta ? Ak + u0 : Ak + u0 * lda;
         const double *Bu = tb ? Bk + u0 * ldbj : Bk + u0;

@@ -260,6 +260,41 @@ def test_host_pipelined_two_engine_segments(F, emulated, gblib):
     assert np.array_equal(C, ref)
 
 
+@pytest.mark.parametrize("ta,slices,hard", [("N", 0, False), ("T", 0, False), ("N", 0, True),
+                                             ("T", 7, False)])
+def test_syrk_shaped_reuses_op_a(gblib, ta, slices, hard):
+    """C = op(A) op(A)^T with op(B) the same matrix: op(B)'s residues and
+    digits are op(A)'s rows, which the engine reuses.  The result must equal
+    the product with op(B) a separate copy of the same values (split on its
+    own) bit for bit -- n = 600 makes op(A)'s plane stride (640 rows) differ
+    from op(B)'s (768); `hard` gives some tiles digit slices."""
+    torch = pytest.importorskip("torch")
+    n, k = 600, 300
+    tb = "T" if ta == "N" else "N"
+    A = W.uniform(96, (n, k) if ta == "N" else (k, n))
+    if hard:  # one tiny column of op(A) against columns of op(B) led by a large entry
+        if ta == "N":
+            A[:, 0] *= 2.0 ** -30
+            A[300:500, 1:] *= 2.0 ** -40
+        else:
+            A[0, :] *= 2.0 ** -30
+            A[1:, 300:500] *= 2.0 ** -40
+    A = np.asfortranarray(A)
+    ld = A.shape[0]
+    dA = torch.from_numpy(A.T.copy()).cuda()
+    dB = dA.clone()
+    out = []
+    for B in (dA, dB):
+        dC = torch.zeros((n, n), dtype=torch.float64, device="cuda")
+        assert gblib.gb_dgemm_emulated_dev(ta.encode(), tb.encode(), n, n, k, 1.0, dA.data_ptr(), ld,
+                                           B.data_ptr(), ld, 0.0, dC.data_ptr(), n, slices) == 0
+        assert gblib.gb_synchronize() == 0
+        out.append(dC.cpu().numpy())
+    assert np.array_equal(out[0], out[1])
+    opA = A if ta == "N" else A.T
+    assert np.allclose(out[0].T, opA @ opA.T, rtol=0, atol=1e-12 * k)
+
+
 def test_host_pipelined_pinned_buffers(emulated, gblib):
     """The same through cblas_dgemm on pinned (page-locked) host buffers."""
     torch = pytest.importorskip("torch")
