@@ -2001,11 +2001,13 @@ static int potrf_panel_solve(bool upper, int64_t rest, int64_t jb, const float *
 // is skipped on the device (info), so the matrix is left as it was at the
 // failing column.  With emulated-FP64 updates (FP64, gemm_mode 1) the block
 // columns are POTRF_NB_EMULATED wide and each diagonal block is itself
-// factored by this routine with 256-wide blocks: every emulated panel solve
-// and trailing update then has depth k = 1024, which amortises the residue
-// planes' round trip through HBM over four times the work and takes the
-// modular scheme (k >= 512).  off: the global column of A(0,0) (for info).
-constexpr int64_t POTRF_NB_EMULATED = 1024;
+// factored by this routine with 256-wide blocks: every outer emulated panel
+// solve and trailing update then has depth k = 2048, which amortises the
+// residue planes' round trip through HBM over eight times the work and takes
+// the modular scheme (k >= 512); measured at 32768: 1024-wide 359 ms,
+// 2048-wide 332 ms, 4096-wide with 1024-wide inner blocks 350 ms.
+// off: the global column of A(0,0) (for info).
+constexpr int64_t POTRF_NB_EMULATED = 2048;
 template <typename T>
 int potrf_blocked(int uplo, int64_t n, T *A, int64_t lda, int *info, int gemm_mode,
                   cudaStream_t s, int64_t nb, int64_t off) {
