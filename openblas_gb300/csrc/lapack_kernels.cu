@@ -1209,7 +1209,7 @@ int lu_trsm(int64_t n1, int64_t w, const T *L, int64_t ldl, T *B, int64_t ldb, c
 // result equals applying the interchanges one after another
 // (lapack/laswp/generic/laswp_k_1.c), at the cost of two memory round trips
 // instead of one per interchange.
-constexpr int LASWP_FUSED_MAX = 256;
+constexpr int LASWP_FUSED_MAX = 512;
 constexpr int LASWP_FUSED_ELEMS = 4096;
 
 template <typename T>
@@ -1502,7 +1502,18 @@ int lu_rec(LuCtx<T> &c, int64_t r0, int64_t m, int64_t n) {
 // min(mn/2, GEMM_Q), recursive call on the panel, LASWP + TRSM + GEMM on the
 // trailing columns, later interchanges applied to the columns on the left).
 constexpr int64_t LU_OUTER_NB = 256;
-static_assert(LU_OUTER_NB <= LASWP_FUSED_MAX, "a block's interchanges fit one fused LASWP");
+// With the emulated-FP64 updates and min(m, n) >= 16384 the block columns
+// are twice as wide: the trailing updates then have depth 512 and take the
+// modular scheme (14 residue products instead of 28 digit-slice products at
+// depth 256, and half as many round trips of their planes through HBM).
+// Measured: 16384^2 340 -> 319 ms; at 8192^2 the wider panels' inner solves
+// cost more than that saves (94.6 -> 97.7 ms), so smaller matrices keep 256.
+constexpr int64_t LU_OUTER_NB_EMULATED = 512;
+static_assert(LU_OUTER_NB_EMULATED <= LASWP_FUSED_MAX, "a block's interchanges fit one fused LASWP");
+template <typename T>
+int64_t lu_outer_nb(const LuCtx<T> &c, int64_t mn) {
+  return sizeof(T) == 8 && c.gemm_mode == 1 && mn >= 16384 ? LU_OUTER_NB_EMULATED : LU_OUTER_NB;
+}
 
 template <typename T>
 int lu_blocked(LuCtx<T> &c, int64_t m, int64_t mn, int64_t n) {
@@ -1511,12 +1522,13 @@ int lu_blocked(LuCtx<T> &c, int64_t m, int64_t mn, int64_t n) {
   // measured on GB300 (FP32 LU): per-panel interchanges over the whole
   // width win at 8192^2 (268 MB), lose from 16384^2 (1 GB) on
   const bool whole = (double)c.nrows * (double)c.ncols * sizeof(T) <= 512.0 * 1024 * 1024;
-  for (int64_t j0 = 0; j0 < mn; j0 += LU_OUTER_NB) {
-    const int64_t jb = (mn - j0) < LU_OUTER_NB ? (mn - j0) : LU_OUTER_NB;
+  const int64_t onb = lu_outer_nb<T>(c, mn);
+  for (int64_t j0 = 0; j0 < mn; j0 += onb) {
+    const int64_t jb = (mn - j0) < onb ? (mn - j0) : onb;
     c.blk0 = whole ? 0 : j0;
     c.blk1 = whole ? c.ncols : j0 + jb;
     if ((st = lu_rec<T>(c, j0, m - j0, jb))) return st;
-    // the block's interchanges (at most LU_OUTER_NB <= LASWP_FUSED_MAX) on the
+    // the block's interchanges (at most LASWP_FUSED_MAX) on the
     // trailing columns, then on the finished columns to the left
     const int64_t npiv = (m - j0) < jb ? (m - j0) : jb;
     if (!whole && j0 + jb < n) {
