@@ -233,7 +233,7 @@ int xerbla_(const char *name, const blasint *info, blasint len);
 /* DGEMM precision modes */
 #define GB_DGEMM_NATIVE 0   /* FP64 FMA units */
 #define GB_DGEMM_EMULATED 1 /* Ozaki schemes (residues or 8-bit slices) on bf16 tensor cores */
-#define GB_DGEMM_AUTO 2     /* emulated when the shape is large enough to win */
+#define GB_DGEMM_AUTO 2     /* emulated from m*n*k >= 384^3 (k >= 64), native below */
 
 /* Stream used by every entry point of the calling thread (NULL = the
  * library's own non-blocking stream).  The handle is a cudaStream_t. */

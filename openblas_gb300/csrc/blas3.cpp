@@ -71,9 +71,7 @@ static int dgemm_native(int ta, int tb, int64_t m, int64_t n, int64_t k, double 
 
 
 static bool dgemm_wants_emulated(int64_t m, int64_t n, int64_t k) {
-  const int mode = gb_get_dgemm_mode();
-  return mode == GB_DGEMM_EMULATED ||
-         (mode == GB_DGEMM_AUTO && (double)m * n * k >= 256.0 * 256.0 * 256.0 && k >= 64);
+  return dgemm_mode_emulated(m, n, k);
 }
 
 // Selected by the DGEMM mode: emulated when requested, or in auto mode when

@@ -172,6 +172,9 @@ int ozaki_caller_slices();
 // Whether the calling thread's automatic mode may take the modular scheme
 // (gb_set_ozaki_modular / GB_OZAKI_MODULAR).
 bool ozaki_modular_enabled();
+// Whether the thread's DGEMM mode selects the emulated GEMM for an m x n x k
+// product (auto mode: from 384^3 on, with k >= 64).
+bool dgemm_mode_emulated(int64_t m, int64_t n, int64_t k);
 // Emulated-FP64 GEMM (Ozaki schemes on the bf16 tensor cores).  slices = 0:
 // the default form (the modular scheme on every tile, or 7 digit slices
 // when the thread turned it off); 1-8: that many digit slices;

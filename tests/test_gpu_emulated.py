@@ -295,6 +295,35 @@ def test_syrk_shaped_reuses_op_a(gblib, ta, slices, hard):
     assert np.allclose(out[0].T, opA @ opA.T, rtol=0, atol=1e-12 * k)
 
 
+@pytest.mark.parametrize("m,n,k,engine", [(256, 256, 256, "native"), (512, 512, 512, "emulated"),
+                                           (2048, 2048, 32, "native"), (384, 384, 384, "emulated")])
+def test_auto_mode_picks_the_faster_engine(gblib, gb_clean, m, n, k, engine):
+    """GB_DGEMM_MODE=auto: the emulated GEMM from m n k >= 384^3 with k >= 64
+    (the measured crossover), the native one below; the result equals that
+    engine's own entry bit for bit."""
+    torch = pytest.importorskip("torch")
+    g = torch.Generator(device="cuda")
+    g.manual_seed(m + k)
+    A = torch.rand((k, m), dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    B = torch.rand((n, k), dtype=torch.float64, device="cuda", generator=g) * 2 - 1
+    C1 = torch.empty((n, m), dtype=torch.float64, device="cuda")
+    C2 = torch.empty_like(C1)
+    gblib.gb_set_dgemm_mode(2)
+    try:
+        assert gblib.gb_dgemm_dev(b"N", b"N", m, n, k, 1.0, A.data_ptr(), m, B.data_ptr(), k, 0.0,
+                                  C1.data_ptr(), m) == 0
+    finally:
+        gblib.gb_set_dgemm_mode(0)
+    if engine == "native":
+        st = gblib.gb_dgemm_native_dev(b"N", b"N", m, n, k, 1.0, A.data_ptr(), m, B.data_ptr(), k,
+                                       0.0, C2.data_ptr(), m)
+    else:
+        st = gblib.gb_dgemm_emulated_dev(b"N", b"N", m, n, k, 1.0, A.data_ptr(), m, B.data_ptr(),
+                                         k, 0.0, C2.data_ptr(), m, 0)
+    assert st == 0 and gblib.gb_synchronize() == 0
+    assert torch.equal(C1, C2)
+
+
 def test_host_pipelined_pinned_buffers(emulated, gblib):
     """The same through cblas_dgemm on pinned (page-locked) host buffers."""
     torch = pytest.importorskip("torch")
