@@ -362,8 +362,9 @@ def run_suite(args):
                "value": trsm["native"]["value"], "unit": UNIT, "ms": trsm["native"]["ms"],
                "residual_eps": trsm["native"]["residual_eps"]})
         _emit({"suite": "dtrsm_8192_emulated",
-               "workload": "DTRSM LLNN M=N=8192, emulated FP64 (recursive, 128-wide native leaves, "
-                           "off-diagonal blocks on the emulated DGEMM, automatic choice)",
+               "workload": "DTRSM LLNN M=N=8192, emulated FP64 (recursive, 128-wide FP64 leaves in "
+                           "one fused launch each, off-diagonal blocks on the emulated DGEMM, "
+                           "automatic choice)",
                "unit": UNIT, **trsm["emulated"], "native_fp64_ms": trsm["native"]["ms"],
                "speedup_over_native": trsm["native"]["ms"] / trsm["emulated"]["ms"]})
         del L, B0, Bt, R

@@ -239,9 +239,174 @@ int dtrsm_device(int side, int uplo, int trans, int unit, int64_t m, int64_t n, 
 }
 
 namespace {
-// Leaves of the recursive emulated-FP64 TRSM: solved by the native blocked
-// TRSM above.
+// Leaves of the recursive emulated-FP64 TRSM: triangles of at most 128.
 constexpr int64_t TRSM_EMU_LEAF = 128;
+
+// One leaf in one launch: a whole triangle of nb <= 128 columns against 32
+// right-hand-side vectors per CTA.  The blocked path above spends four
+// diagonal-block launches (64 CTAs of 128 vectors at 8192 vectors) and three
+// FP64 GEMMs of depth 32 on it, which keeps the FP64 pipe, the scarcest unit
+// on this part, about half busy.  The solve is the column sweep of the
+// substitution, walked in 32-wide blocks as driver/level3/trsm_L.c walks its
+// GEMM_P blocks: element c takes x_c *= 1/T_cc, then every later element r
+// takes x_r -= T_rc x_c, c ascending.  The 32 vectors (columns of B on the
+// left, rows on the right) sit in shared memory, 128 x 32 doubles with an
+// XOR swizzle, so the coalesced loads along a vector and the one-thread-per-
+// vector accesses both meet the two-wavefront minimum; the triangle is
+// staged 32 columns at a time and read by broadcast.  The four warps share
+// each diagonal block's solve (rows dealt round robin, one barrier per
+// column) and then update the later rows in groups of four (four
+// independent FMA chains per thread).  Each SM sub-partition's FP64 unit
+// takes about 64 clocks per warp-wide DFMA, so all four warps must carry
+// FP64 work at every phase.
+//
+// Working order: element i of the working vector is element o(i) of the
+// stored one, o(i) = i (FORWARD) or nb - 1 - i, so the working triangle
+// L'[i][j] = Leff[o(i)][o(j)] is lower.  Leff = op(A) on the left and
+// op(A)^T on the right (x op(A) = b is op(A)^T x^T = b^T); with
+// eff_t = trans ^ right, Leff[r][c] = A[r + c lda] (eff_t 0) or A[c + r lda].
+constexpr int LEAF_V = 32;        // vectors per CTA, one per lane
+constexpr int LEAF_THREADS = 128;
+constexpr int LEAF_PLD = 33;      // row pitch of the staged panel (doubles)
+constexpr size_t LEAF_SMEM =
+    sizeof(double) * ((size_t)TRSM_EMU_LEAF * LEAF_V + (size_t)TRSM_EMU_LEAF * LEAF_PLD + 32);
+
+template <bool FORWARD>
+__global__ void __launch_bounds__(LEAF_THREADS)
+trsm_leaf_kernel(int right, int eff_t, int unit, int nb, int64_t nvec,
+                 const double *__restrict__ A, int64_t lda, double *__restrict__ B,
+                 int64_t ldb) {
+  constexpr int NBMAX = (int)TRSM_EMU_LEAF;
+  extern __shared__ double leaf_smem[];
+  double *Xs = leaf_smem;                // [NBMAX][LEAF_V], swizzled columns
+  double *Ps = Xs + NBMAX * LEAF_V;      // [NBMAX][LEAF_PLD]: rows j0.. of the panel
+  double *inv = Ps + NBMAX * LEAF_PLD;   // [32]
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  const int64_t v0 = (int64_t)blockIdx.x * LEAF_V;
+  const int nv = (int)(nvec - v0 < LEAF_V ? nvec - v0 : LEAF_V);
+  auto xs = [&](int i, int v) -> double & { return Xs[i * LEAF_V + (v ^ (i & 31))]; };
+  auto o = [&](int i) { return FORWARD ? i : nb - 1 - i; };
+
+  // the vectors, element o(i) at working row i (zero beyond nb and nv)
+  if (!right) {
+#pragma unroll 4
+    for (int v = warp; v < LEAF_V; v += 4)
+      for (int i = lane; i < NBMAX; i += 32)
+        xs(i, v) = (v < nv && i < nb) ? B[o(i) + (v0 + v) * ldb] : 0.0;
+  } else {
+#pragma unroll 4
+    for (int i = warp; i < NBMAX; i += 4)
+      xs(i, lane) = (lane < nv && i < nb) ? B[v0 + lane + (int64_t)o(i) * ldb] : 0.0;
+  }
+
+  for (int j0 = 0; j0 < nb; j0 += 32) {
+    const int cb = nb - j0 < 32 ? nb - j0 : 32;
+    __syncthreads();  // the previous block's panel reads and row updates are done
+    // panel: Ps[(i - j0) * LEAF_PLD + jj] = L'[i][j0 + jj], i in [j0, nb), jj < cb
+    if (eff_t == 0) {
+      for (int jj = warp; jj < cb; jj += 4) {
+        const double *col = A + (int64_t)o(j0 + jj) * lda;
+        for (int i = j0 + lane; i < nb; i += 32) Ps[(i - j0) * LEAF_PLD + jj] = col[o(i)];
+      }
+    } else {
+      for (int i = j0 + warp; i < nb; i += 4)
+        if (lane < cb) Ps[(i - j0) * LEAF_PLD + lane] = A[o(j0 + lane) + (int64_t)o(i) * lda];
+    }
+    if (tid < cb) {
+      const int64_t d = o(j0 + tid);
+      inv[tid] = unit ? 1.0 : 1.0 / A[d + d * lda];
+    }
+    __syncthreads();
+    {
+      // diagonal block over the four warps (one warp alone would leave three
+      // of the SM's four FP64 units idle): warp w owns rows w + 4t; at step
+      // c the owner of row c scales it by 1/T_cc and publishes it in Xs, and
+      // after the barrier every warp applies it to its later rows
+      double xr[8];
+#pragma unroll
+      for (int t = 0; t < 8; ++t) {
+        const int r = warp + 4 * t;
+        xr[t] = r < cb ? xs(j0 + r, lane) : 0.0;
+      }
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+        if (c < cb) {
+          if (warp == (c & 3)) {
+            xr[c >> 2] *= inv[c];
+            xs(j0 + c, lane) = xr[c >> 2];
+          }
+          __syncthreads();
+          const double xc = xs(j0 + c, lane);
+#pragma unroll
+          for (int t = 0; t < 8; ++t) {
+            const int r = warp + 4 * t;
+            if (r > c && r < cb) xr[t] = fma(-Ps[r * LEAF_PLD + c], xc, xr[t]);
+          }
+        }
+      }
+    }
+    const int r0 = j0 + 32;
+    if (r0 >= nb) break;  // the last block (the only one with cb < 32): no later rows
+    // every row of the block was published before one of the barriers above
+    double x[32];
+#pragma unroll
+    for (int c = 0; c < 32; ++c) x[c] = xs(j0 + c, lane);
+    // rows r0.. in groups of four, the k-th group to warp k % 4; the lanes of
+    // a short last group repeat row g and do not store it
+    for (int g = r0 + 4 * warp; g < nb; g += 16) {
+      const int nr = nb - g < 4 ? nb - g : 4;
+      double acc[4];
+      const double *prow[4];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int i = q < nr ? g + q : g;
+        acc[q] = xs(i, lane);
+        prow[q] = Ps + (i - j0) * LEAF_PLD;
+      }
+#pragma unroll
+      for (int c = 0; c < 32; ++c) {
+#pragma unroll
+        for (int q = 0; q < 4; ++q) acc[q] = fma(-prow[q][c], x[c], acc[q]);
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q)
+        if (q < nr) xs(g + q, lane) = acc[q];
+    }
+  }
+  __syncthreads();
+  if (!right) {
+#pragma unroll 4
+    for (int v = warp; v < LEAF_V; v += 4)
+      for (int i = lane; i < NBMAX; i += 32)
+        if (v < nv && i < nb) B[o(i) + (v0 + v) * ldb] = xs(i, v);
+  } else {
+#pragma unroll 4
+    for (int i = warp; i < NBMAX; i += 4)
+      if (lane < nv && i < nb) B[v0 + lane + (int64_t)o(i) * ldb] = xs(i, lane);
+  }
+}
+
+// The leaf solve op(A) X = B (left, nb = m) or X op(A) = B (right, nb = n),
+// nb <= 128, alpha already applied; forward as in trsm_device_t.
+int trsm_leaf(bool left, bool forward, int trans, int unit_code, int64_t nb, int64_t nvec,
+              const double *A, int64_t lda, double *B, int64_t ldb, cudaStream_t s) {
+  static PerDeviceOnce attr_once;
+  const int ast = attr_once.run(current_device(), [] {
+    GB_CUDA(cudaFuncSetAttribute(trsm_leaf_kernel<true>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LEAF_SMEM));
+    GB_CUDA(cudaFuncSetAttribute(trsm_leaf_kernel<false>,
+                                 cudaFuncAttributeMaxDynamicSharedMemorySize, (int)LEAF_SMEM));
+    return GB_SUCCESS;
+  });
+  if (ast) return ast;
+  const int right = left ? 0 : 1, eff_t = trans ^ right, unit = unit_code == 0;
+  const unsigned grid = (unsigned)((nvec + LEAF_V - 1) / LEAF_V);
+  if (forward)
+    { trsm_leaf_kernel<true><<<grid, LEAF_THREADS, LEAF_SMEM, s>>>(right, eff_t, unit, (int)nb, nvec, A, lda, B, ldb); count_launch(); }
+  else
+    { trsm_leaf_kernel<false><<<grid, LEAF_THREADS, LEAF_SMEM, s>>>(right, eff_t, unit, (int)nb, nvec, A, lda, B, ldb); count_launch(); }
+  return check_cuda(cudaGetLastError(), "trsm leaf");
+}
 
 // Solve for the triangular index range [i0, i0 + len) of op(A) (rows of B on
 // the left, columns on the right): halves in the order of the substitution,
@@ -252,10 +417,11 @@ int trsm_rec_emulated(int side, int uplo, int trans, int unit_code, int64_t m, i
                       const double *A, int64_t lda, double *B, int64_t ldb, bool forward,
                       int64_t i0, int64_t len, cudaStream_t s) {
   const bool left = side == 0;
-  if (len <= TRSM_EMU_LEAF)
-    return trsm_device_t<double>(side, uplo, trans, unit_code, left ? len : m, left ? n : len,
-                                 1.0, A + i0 + i0 * lda, lda, left ? B + i0 : B + i0 * ldb, ldb,
-                                 s);
+  if (len <= TRSM_EMU_LEAF) {
+    ProfileScope prof("trsm_leaf", s);
+    return trsm_leaf(left, forward, trans, unit_code, len, left ? n : m, A + i0 + i0 * lda, lda,
+                     left ? B + i0 : B + i0 * ldb, ldb, s);
+  }
   // first half, a multiple of 128 (and shorter than len: len > 256)
   int64_t h = (len / 2 + 127) / 128 * 128;
   if (h >= len) h = len / 2;
@@ -267,12 +433,15 @@ int trsm_rec_emulated(int side, int uplo, int trans, int unit_code, int64_t m, i
   if (st) return st;
   // the caller's slice setting, as for DGEMM (automatic: per-tile tolerance)
   const int slices = ozaki_caller_slices();
-  if (left)
-    st = dgemm_emulated(trans, 0, sl, n, fl, -1.0, opA(s0, f0), lda, B + f0, ldb, 1.0, B + s0,
-                        ldb, slices, s);
-  else
-    st = dgemm_emulated(0, trans, m, sl, fl, -1.0, B + f0 * ldb, ldb, opA(f0, s0), lda, 1.0,
-                        B + s0 * ldb, ldb, slices, s);
+  {
+    ProfileScope prof("trsm_emu_gemm", s);
+    if (left)
+      st = dgemm_emulated(trans, 0, sl, n, fl, -1.0, opA(s0, f0), lda, B + f0, ldb, 1.0, B + s0,
+                          ldb, slices, s);
+    else
+      st = dgemm_emulated(0, trans, m, sl, fl, -1.0, B + f0 * ldb, ldb, opA(f0, s0), lda, 1.0,
+                          B + s0 * ldb, ldb, slices, s);
+  }
   if (st) return st;
   return trsm_rec_emulated(side, uplo, trans, unit_code, m, n, A, lda, B, ldb, forward, s0, sl,
                            s);

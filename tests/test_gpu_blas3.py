@@ -358,6 +358,24 @@ def test_dtrsm_emulated_recursive_vs_oracle(orc, F, emulated_mode, side, uplo, t
     assert np.array_equal(B[m:], Bo[m:])
 
 
+@pytest.mark.parametrize("side,ta", [(s, t) for s in "LR" for t in "NT"])
+def test_dtrsm_emulated_leaf_many_vectors(orc, F, emulated_mode, side, ta):
+    """The fused FP64 leaves of the emulated DTRSM with many vectors: a 200-wide
+    upper triangle (leaves of 128 and 72, forward and backward working orders
+    as side and trans vary) against 5000 vectors, the last CTA's 8 lanes idle;
+    padded lda and ldb."""
+    na, nv = 200, 5000
+    m, n = (na, nv) if side == "L" else (nv, na)
+    A = np.asfortranarray(np.zeros((na + 3, na)))
+    A[:na] = W.trsm_lower(73, na).T
+    B = np.asfortranarray(W.uniform(74, (m + 2, n)))
+    Bo = B.copy(order="F")
+    F.dtrsm(side, "U", ta, "N", m, n, 1.5, A, na + 3, B, m + 2)
+    orc.dtrsm(side, "U", ta, "N", m, n, 1.5, A, na + 3, Bo, m + 2)
+    assert np.max(np.abs(B[:m] - Bo[:m])) <= 1e3 * na * EPS * max(1.0, np.abs(Bo[:m]).max())
+    assert np.array_equal(B[m:], Bo[m:])
+
+
 def test_dtrsm_emulated_residual(F, emulated_mode):
     """Left/Lower/NoTrans/NonUnit, 2048 x 256 with an exponent-spread right-hand
     side (columns scaled by 2^-40 .. 2^40): L X - B at rounding level column by
