@@ -1961,19 +1961,23 @@ static int potrf_panel_solve(bool upper, int64_t rest, int64_t jb, const double 
       int st;
       if (upper) {
         double *Pi = P + i0;  // rows i0.. of the jb x rest panel
-        if (i0 > 0 &&
-            (st = dgemm_emulated(1, 0, ib, rest, i0, -1.0, D + i0 * lda, lda, P, lda, 1.0, Pi, lda,
-                                 0, s, 0, info)))
-          return st;
+        if (i0 > 0) {
+          ProfileScope prof("potrf_couple", s);
+          if ((st = dgemm_emulated(1, 0, ib, rest, i0, -1.0, D + i0 * lda, lda, P, lda, 1.0, Pi,
+                                   lda, 0, s, 0, info)))
+            return st;
+        }
         if ((st = potrf_panel_solve(true, rest, ib, D + i0 + i0 * lda, lda, Pi, info, gemm_mode,
                                     s)))
           return st;
       } else {
         double *Pi = P + i0 * lda;  // columns i0.. of the rest x jb panel
-        if (i0 > 0 &&
-            (st = dgemm_emulated(0, 1, rest, ib, i0, -1.0, P, lda, D + i0, lda, 1.0, Pi, lda, 0,
-                                 s, 0, info)))
-          return st;
+        if (i0 > 0) {
+          ProfileScope prof("potrf_couple", s);
+          if ((st = dgemm_emulated(0, 1, rest, ib, i0, -1.0, P, lda, D + i0, lda, 1.0, Pi, lda, 0,
+                                   s, 0, info)))
+            return st;
+        }
         if ((st = potrf_panel_solve(false, rest, ib, D + i0 + i0 * lda, lda, Pi, info, gemm_mode,
                                     s)))
           return st;
@@ -1987,10 +1991,15 @@ static int potrf_panel_solve(bool upper, int64_t rest, int64_t jb, const double 
   Scratch ws((size_t)(jb * jb + rest * jb) * sizeof(double), s);
   if (!ws.p) return GB_ERR_ALLOC;
   double *W = ws.as<double>(), *T = W + jb * jb;
-  { set_identity_kernel<<<(unsigned)((jb * jb + 255) / 256), 256, 0, s>>>(jb, W); count_launch(); }
-  // W := tri(D)^-1 (the block's lower or upper triangle, non-unit)
-  int st = dtrsm_device_skip(0, upper ? 0 : 1, 0, 1, jb, jb, 1.0, D, lda, W, jb, s, info);
+  int st;
+  {
+    ProfileScope prof("potrf_inv", s);
+    { set_identity_kernel<<<(unsigned)((jb * jb + 255) / 256), 256, 0, s>>>(jb, W); count_launch(); }
+    // W := tri(D)^-1 (the block's lower or upper triangle, non-unit)
+    st = dtrsm_device_skip(0, upper ? 0 : 1, 0, 1, jb, jb, 1.0, D, lda, W, jb, s, info);
+  }
   if (st) return st;
+  ProfileScope prof("potrf_apply", s);
   if (upper) {  // P (jb x rest) := W^T P
     GB_CUDA(cudaMemcpy2DAsync(T, jb * 8, P, lda * 8, jb * 8, rest, cudaMemcpyDeviceToDevice, s));
     return dgemm_emulated(1, 0, jb, rest, jb, 1.0, W, jb, T, jb, 0.0, P, lda, 0, s, 0, info);
