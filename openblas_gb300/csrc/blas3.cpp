@@ -368,11 +368,18 @@ static int dgemm_host_pipelined(int ta, int tb, int64_t m, int64_t n, int64_t k,
   // one K segment in the engine and op(A) = A^T (its rows are A's contiguous
   // columns): op(A) goes up in eight row blocks (at least 512 rows each),
   // each prepared while the next uploads.  With op(A) = A the rows are
-  // strided on the host, and the 2D copies of 8-16 KB rows ran at 107-175
-  // instead of ~210 GB/s, more than the overlap saved: K pieces then.
-  if (ta && emulated_k_segment(ozaki_caller_slices()) >= k) {
-    const int64_t rb = ((m + 7) / 8 + 127) / 128 * 128;
-    p.arb = rb < 512 ? 512 : rb;
+  // strided on the host: a block's 2D copy moves runs of 8 x rows bytes, at
+  // 96, 107, 180 and 210 GB/s for 4, 8, 16 and 32 KB runs, so such blocks
+  // are at least 4096 rows (up to eight of them), and smaller operands go
+  // up in K pieces.
+  if (emulated_k_segment(ozaki_caller_slices()) >= k) {
+    if (ta) {
+      const int64_t rb = ((m + 7) / 8 + 127) / 128 * 128;
+      p.arb = rb < 512 ? 512 : rb;
+    } else if (m >= 2 * 4096) {
+      const int64_t nbk = m / 4096 < 8 ? m / 4096 : 8;
+      p.arb = ((m + nbk - 1) / nbk + 127) / 128 * 128;
+    }
     if (p.arb >= m) p.arb = 0;
   }
   p.ar_up.assign(p.arb > 0 ? (m + p.arb - 1) / p.arb : 0, nullptr);

@@ -248,6 +248,19 @@ def test_host_pipelined_planned_blocks(F, emulated, gblib, hard):
         assert (gblib.gb_last_ozaki_moduli(), gblib.gb_last_ozaki_slices()) == (MOD_COUNT, 8)
 
 
+def test_host_pipelined_nn_row_blocks(F, emulated, gblib):
+    """op(A) = A with at least 8192 rows goes up in row blocks of at least 4096
+    rows (strided 2D copies of 32 KB runs), each block's exponents and
+    residues prepared while the next uploads: here blocks of 4224 and 4076
+    rows with a padded lda and beta != 0, bit-identical to the single device
+    call."""
+    m, n, k = 8300, 6200, 300
+    A, B, C = W.gemm_operands(95, m, n, k, "N", "N", pad=3)
+    ref = _device_emulated(gblib, "N", "N", m, n, k, -1.25, A, B, 0.5, C)
+    F.dgemm("N", "N", m, n, k, -1.25, A, A.shape[0], B, B.shape[0], 0.5, C, C.shape[0])
+    assert np.array_equal(C, ref)
+
+
 def test_host_pipelined_two_engine_segments(F, emulated, gblib):
     """K beyond one 8192-deep engine segment with op(A) = A^T: op(A) goes up
     in K pieces (row blocks need a single segment) and is prepared per
