@@ -1936,17 +1936,116 @@ static int potrf_trailing(bool upper, int64_t rest, int64_t jb, const float *P, 
   return syrk_skip<float>(upper ? 0 : 1, upper ? 1 : 0, rest, jb, P, lda, C, lda, s, info);
 }
 
-__global__ void set_identity_kernel(int64_t n, double *__restrict__ W) {
-  const int64_t total = n * n;
-  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < total;
-       e += (int64_t)gridDim.x * blockDim.x)
-    W[e] = (e % n == e / n) ? 1.0 : 0.0;
+// Inverse of a lower triangle of at most 256 rows, by recursive doubling:
+// the same identity as lapack/trtri/trtri_L_single.c:87-107 (whose block
+// step forms W21 = -W22 L21 L11^-1 with TRMM and TRSM), evaluated as
+// W21 = -W22 (L21 W11) over pairs of blocks of 32, 64 and 128.  Each level is
+// one launch for every pair's T = L21 W11 and one for W21 = -W22 T, so the
+// 256-wide inverse takes eight small launches; the native blocked TRSM on
+// the identity took about fifteen (0.15 ms, launch- and latency-bound: the
+// FP64 work is ~3 MFLOP).  L is the lower triangle of op(D) padded with the
+// identity to npad (32 times a power of two): Lp(i, j) below.
+__device__ __forceinline__ double trtri_lp(int jb, const double *__restrict__ D, int64_t lda,
+                                           int tr, int i, int j) {
+  if (i < jb && j < jb) return tr ? D[j + (int64_t)i * lda] : D[i + (int64_t)j * lda];
+  return i == j ? 1.0 : 0.0;
+}
+
+// The 32 x 32 diagonal blocks of W = Lp^-1 (W zeroed beforehand): one warp
+// per block, lane j the column j solve of Lp_bb w = e_j by the column sweep
+// (w_c *= 1/l_cc, then w_r -= l_rc w_c for r > c).  The block is read column
+// by column, a lane per row.
+__global__ void __launch_bounds__(32)
+trtri_diag32_kernel(int jb, const double *__restrict__ D, int64_t lda, int tr,
+                    double *__restrict__ W, int64_t npad, const int *__restrict__ skip) {
+  if (skip && *skip) return;
+  __shared__ double Ls[32][33];
+  __shared__ double invd[32];
+  const int lane = threadIdx.x, b0 = blockIdx.x * 32;
+  double v[32];
+#pragma unroll
+  for (int c = 0; c < 32; ++c) v[c] = lane >= c ? trtri_lp(jb, D, lda, tr, b0 + lane, b0 + c) : 0.0;
+#pragma unroll
+  for (int c = 0; c < 32; ++c) Ls[lane][c] = v[c];
+  __syncwarp();
+  invd[lane] = 1.0 / Ls[lane][lane];
+  __syncwarp();
+  double x[32];
+#pragma unroll
+  for (int r = 0; r < 32; ++r) x[r] = r == lane ? 1.0 : 0.0;
+#pragma unroll
+  for (int c = 0; c < 32; ++c) {
+    x[c] *= invd[c];
+#pragma unroll
+    for (int r = c + 1; r < 32; ++r) x[r] = fma(-Ls[r][c], x[c], x[r]);
+  }
+#pragma unroll
+  for (int r = 0; r < 32; ++r) W[(b0 + r) + (int64_t)(b0 + lane) * npad] = x[r];
+}
+
+// One doubling level for block size sz <= 128: pair p covers rows/columns
+// [2 sz p, 2 sz p + 2 sz).  FIRST: T_p = Lp21 W11; second: W21 = -W22 T_p.
+// A CTA computes a 16 x 16 tile from its 16 rows of the left factor and 16
+// columns of the right one, staged in shared memory by one coalesced round
+// of loads; the sums run over all sz terms (the triangles' other entries
+// are exact zeros), in four partial sums.
+template <bool FIRST>
+__global__ void __launch_bounds__(256)
+trtri_level_kernel(int jb, const double *__restrict__ D, int64_t lda, int tr,
+                   double *__restrict__ W, int64_t npad, int sz, double *__restrict__ T,
+                   const int *__restrict__ skip) {
+  if (skip && *skip) return;
+  __shared__ double Xs[128][17];  // Xs[k][rr]: left factor, rows r0 + rr
+  __shared__ double Ys[128][17];  // Ys[k][cc]: right factor, columns c0 + cc
+  const int tid = threadIdx.x + 16 * threadIdx.y;
+  const int r0 = blockIdx.x * 16, c0 = blockIdx.y * 16;
+  const int o = 2 * sz * blockIdx.z;
+  double *Tp = T + (int64_t)blockIdx.z * sz * sz;
+  for (int e = tid; e < 16 * sz; e += 256) {
+    const int rr = e & 15, k = e >> 4;  // 16 consecutive rows (or k) per group
+    Xs[k][rr] = FIRST ? trtri_lp(jb, D, lda, tr, o + sz + r0 + rr, o + k)
+                      : W[(o + sz + r0 + rr) + (int64_t)(o + sz + k) * npad];
+  }
+  for (int e = tid; e < 16 * sz; e += 256) {
+    const int k = e % sz, cc = e / sz;
+    Ys[k][cc] = FIRST ? W[(o + k) + (int64_t)(o + c0 + cc) * npad] : Tp[k + (int64_t)(c0 + cc) * sz];
+  }
+  __syncthreads();
+  const int rr = threadIdx.x, cc = threadIdx.y;
+  double a0 = 0.0, a1 = 0.0, a2 = 0.0, a3 = 0.0;
+  for (int k = 0; k < sz; k += 4) {  // sz is a multiple of 32
+    a0 = fma(Xs[k][rr], Ys[k][cc], a0);
+    a1 = fma(Xs[k + 1][rr], Ys[k + 1][cc], a1);
+    a2 = fma(Xs[k + 2][rr], Ys[k + 2][cc], a2);
+    a3 = fma(Xs[k + 3][rr], Ys[k + 3][cc], a3);
+  }
+  const double sum = (a0 + a1) + (a2 + a3);
+  if (FIRST)
+    Tp[(r0 + rr) + (int64_t)(c0 + cc) * sz] = sum;
+  else
+    W[(o + sz + r0 + rr) + (int64_t)(o + c0 + cc) * npad] = -sum;
+}
+
+// W (npad x npad, leading dimension npad) := the inverse of the lower
+// triangle of op(D) (jb <= npad rows; op(D) = D, or D^T when tr), the
+// identity beyond jb.  T: npad^2 / 4 doubles of scratch.
+static int trtri_lower_fp64(int64_t jb, const double *D, int64_t lda, int tr, double *W,
+                            int64_t npad, double *T, cudaStream_t s, const int *skip) {
+  if (npad > 256) return set_error(GB_ERR_UNSUPPORTED, "trtri: triangle wider than 256");
+  GB_CUDA(cudaMemsetAsync(W, 0, (size_t)npad * npad * sizeof(double), s));
+  { trtri_diag32_kernel<<<(unsigned)(npad / 32), 32, 0, s>>>((int)jb, D, lda, tr, W, npad, skip); count_launch(); }
+  for (int64_t sz = 32; sz < npad; sz *= 2) {
+    const dim3 g((unsigned)(sz / 16), (unsigned)(sz / 16), (unsigned)(npad / (2 * sz)));
+    { trtri_level_kernel<true><<<g, dim3(16, 16), 0, s>>>((int)jb, D, lda, tr, W, npad, (int)sz, T, skip); count_launch(); }
+    { trtri_level_kernel<false><<<g, dim3(16, 16), 0, s>>>((int)jb, D, lda, tr, W, npad, (int)sz, T, skip); count_launch(); }
+  }
+  return check_cuda(cudaGetLastError(), "trtri");
 }
 
 // The panel solve of a 256-wide step: L21 = A21 L11^-T (lower) or
 // U12 = U11^-T A12 (upper).  Native: one FP64 TRSM.  In the emulated-FP64
-// mode the block's triangle is inverted once by substitution on the identity
-// (native FP64, jb^3/3 flops) and the panel becomes one FP64-accurate GEMM on
+// mode the block's triangle is inverted once (native FP64, jb^3/3 flops, by
+// trtri_lower_fp64) and the panel becomes one FP64-accurate GEMM on
 // the tensor cores -- the native TRSM over the whole panel ran at the FP64
 // pipe's rate (152 of 884 ms at n = 32768).  Steps after a failed pivot are
 // skipped on the device (info), as in the native form.
@@ -1988,25 +2087,27 @@ static int potrf_panel_solve(bool upper, int64_t rest, int64_t jb, const double 
   if (!(gemm_mode == 1 && rest >= 256 && jb >= 64))
     return upper ? trsm_skip<double>(0, 0, 1, 1, jb, rest, D, lda, P, lda, s, info)
                  : trsm_skip<double>(1, 1, 1, 1, rest, jb, D, lda, P, lda, s, info);
-  Scratch ws((size_t)(jb * jb + rest * jb) * sizeof(double), s);
+  int64_t npad = 32;
+  while (npad < jb) npad *= 2;
+  Scratch ws((size_t)(npad * npad + npad * npad / 4 + rest * jb) * sizeof(double), s);
   if (!ws.p) return GB_ERR_ALLOC;
-  double *W = ws.as<double>(), *T = W + jb * jb;
+  double *W = ws.as<double>(), *Tl = W + npad * npad, *T = Tl + npad * npad / 4;
   int st;
   {
+    // W := the inverse of the block's lower triangle (L), or of the lower
+    // triangle of D^T (U^T, whose inverse is U^-T): non-unit
     ProfileScope prof("potrf_inv", s);
-    { set_identity_kernel<<<(unsigned)((jb * jb + 255) / 256), 256, 0, s>>>(jb, W); count_launch(); }
-    // W := tri(D)^-1 (the block's lower or upper triangle, non-unit)
-    st = dtrsm_device_skip(0, upper ? 0 : 1, 0, 1, jb, jb, 1.0, D, lda, W, jb, s, info);
+    st = trtri_lower_fp64(jb, D, lda, upper ? 1 : 0, W, npad, Tl, s, info);
   }
   if (st) return st;
   ProfileScope prof("potrf_apply", s);
-  if (upper) {  // P (jb x rest) := W^T P
+  if (upper) {  // P (jb x rest) := U^-T P = W P
     GB_CUDA(cudaMemcpy2DAsync(T, jb * 8, P, lda * 8, jb * 8, rest, cudaMemcpyDeviceToDevice, s));
-    return dgemm_emulated(1, 0, jb, rest, jb, 1.0, W, jb, T, jb, 0.0, P, lda, 0, s, 0, info);
+    return dgemm_emulated(0, 0, jb, rest, jb, 1.0, W, npad, T, jb, 0.0, P, lda, 0, s, 0, info);
   }
-  // P (rest x jb) := P W^T
+  // P (rest x jb) := P L^-T = P W^T
   GB_CUDA(cudaMemcpy2DAsync(T, rest * 8, P, lda * 8, rest * 8, jb, cudaMemcpyDeviceToDevice, s));
-  return dgemm_emulated(0, 1, rest, jb, jb, 1.0, T, rest, W, jb, 0.0, P, lda, 0, s, 0, info);
+  return dgemm_emulated(0, 1, rest, jb, jb, 1.0, T, rest, W, npad, 0.0, P, lda, 0, s, 0, info);
 }
 static int potrf_panel_solve(bool upper, int64_t rest, int64_t jb, const float *D, int64_t lda,
                              float *P, int *info, int, cudaStream_t s) {
