@@ -585,6 +585,15 @@ abs_colsum_kernel(int64_t R, int64_t K, const double *__restrict__ X, int64_t ld
   }
 }
 
+// x 2^n, equal to ldexp(x, n): when 2^n is a normal double, one multiply by
+// it (the exact product rounded once, as ldexp rounds it, overflow to Inf
+// included); otherwise ldexp.  The statistics and choice kernels run short
+// chains of these, where ldexp's general path was most of their latency.
+__device__ __forceinline__ double scale2(double x, int n) {
+  if (n >= -1022 && n <= 1023) return x * __longlong_as_double((long long)(n + 1023) << 52);
+  return ldexp(x, n);
+}
+
 // totals[0] = T_e = sum of 2^e_r over the non-zero finite rows of op(A),
 // totals[1] = T_1 = sum_k alpha_k, totals[2] = E_A (the scale of the FP32
 // alpha_k).  One block.
@@ -594,7 +603,7 @@ a_totals_kernel(int64_t R, int64_t K, const int *__restrict__ expo,
                 const int *__restrict__ emax, double *__restrict__ totals) {
   double te = 0.0, t1 = 0.0;
   for (int64_t r = threadIdx.x; r < R; r += blockDim.x)
-    if (mx[r] != 0 && expo[r] != NONFINITE) te += ldexp(1.0, expo[r]);
+    if (mx[r] != 0 && expo[r] != NONFINITE) te += scale2(1.0, expo[r]);
   for (int64_t kk = threadIdx.x; kk < K; kk += blockDim.x) t1 += (double)alpha[kk];
   __shared__ double pe[256], p1[256];
   pe[threadIdx.x] = te;
@@ -609,7 +618,7 @@ a_totals_kernel(int64_t R, int64_t K, const int *__restrict__ expo,
   }
   if (threadIdx.x == 0) {
     totals[0] = pe[0];
-    totals[1] = ldexp(p1[0], *emax);
+    totals[1] = scale2(p1[0], *emax);
     totals[2] = (double)*emax;
   }
 }
@@ -743,9 +752,9 @@ choose_slices_kernel(int64_t R, const int *__restrict__ expo,
   if (j < R && mx[j] != 0 && expo[j] != NONFINITE && s2f[j] > 0.0f) {
     const double te = totals[0], t1 = totals[1];
     const int fj = expo[j], ea = (int)totals[2];
-    const double s1 = ldexp((double)s1f[j], fj), s2 = ldexp((double)s2f[j], fj + ea);
-    rho = RHO_SLACK * (te * s1 + ldexp(t1 + DROP_C * (double)k * te, fj)) / s2;
-    rho2 = RHO_SLACK * (te * s1 + ldexp(t1 + ldexp((double)k * te, -mod_t), fj)) / s2;
+    const double s1 = scale2((double)s1f[j], fj), s2 = scale2((double)s2f[j], fj + ea);
+    rho = RHO_SLACK * (te * s1 + scale2(t1 + DROP_C * (double)k * te, fj)) / s2;
+    rho2 = RHO_SLACK * (te * s1 + scale2(t1 + scale2((double)k * te, -mod_t), fj)) / s2;
     if (!(rho <= 1e300)) rho = 1e300;  // Inf or NaN: the largest count
     if (!(rho2 <= 1e300)) rho2 = 1e300;
   } else if (j < R && mx[j] != 0 && expo[j] != NONFINITE) {
@@ -763,7 +772,7 @@ choose_slices_kernel(int64_t R, const int *__restrict__ expo,
     __syncthreads();
   }
   if (threadIdx.x == 0) {
-    if (mod_t > 0 && ldexp(red2[0], -mod_t) <= budget_mod) {
+    if (mod_t > 0 && scale2(red2[0], -mod_t) <= budget_mod) {
       s_tiles[blockIdx.x] = 0;
       atomicAdd(pass, 1);
       atomicMax(last_moduli, MOD_COUNT);
@@ -771,7 +780,7 @@ choose_slices_kernel(int64_t R, const int *__restrict__ expo,
     }
     int S = MAX_SLICES;
     for (int c = 1; c < MAX_SLICES; ++c)
-      if (ldexp(red[0], -DIGIT_BITS * c) <= budget_dig) {
+      if (scale2(red[0], -DIGIT_BITS * c) <= budget_dig) {
         S = c;
         break;
       }
