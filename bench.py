@@ -579,40 +579,42 @@ def run_suite(args):
             torch.cuda.empty_cache()
 
     if want("illcond"):
-        # ---- ill-conditioned DGESV (GMRES-IR): A = U diag(logspace(0,-kappa)) V^T
-        n = 4096
-        rng = np.random.default_rng(123)
-        U, _ = np.linalg.qr(rng.standard_normal((n, n)))
-        V, _ = np.linalg.qr(rng.standard_normal((n, n)))
-        for kappa in (4, 8, 12):
-            sv = np.logspace(0, -kappa, n)
-            Ah = (U * sv) @ V.T                   # row-major numpy matrix
-            A = torch.from_numpy(np.ascontiguousarray(Ah.T)).cuda()  # column-major buffer
-            Aw = A.clone()  # the FP64 fallback overwrites its A with the LU factors
-            Bm = urand((1, n), 95)
-            X = torch.zeros_like(Bm)
-            p2 = torch.zeros(n, dtype=torch.int32, device="cuda")
-            it, info = C.c_int(0), C.c_int(0)
-            torch.cuda.synchronize()
-            t0 = time.perf_counter()
-            check(lib.gb_dsgesv_dev(n, 1, Aw.data_ptr(), n, p2.data_ptr(), Bm.data_ptr(), n,
-                                    X.data_ptr(), n, C.byref(it), C.byref(info)))
-            torch.cuda.synchronize()
-            t_mixed = time.perf_counter() - t0
-            R = Bm.clone()
-            check(lib.gb_dgemm_native_dev(b"N", b"N", n, 1, n, -1.0, A.data_ptr(), n, X.data_ptr(), n,
-                                          1.0, R.data_ptr(), n))
-            torch.cuda.synchronize()
-            anorm = float(A.abs().sum(dim=0).max())
-            berr = float(R.abs().max() / (anorm * X.abs().max() + Bm.abs().max()))
-            _emit({"suite": f"dgesv_illcond_{n}_kappa1e{kappa}",
-                   "workload": f"DGESV N={n} NRHS=1, A = U diag(logspace(0,-{kappa})) V^T (seeded QR)",
-                   "ms": t_mixed * 1e3, "iter": it.value, "info": info.value,
-                   "backward_error_eps": berr / eps, "bound_n_eps": n,
-                   "path": "FP32 LU + IR" if 0 <= it.value <= 30 else
-                           ("GMRES-IR" if it.value >= 100 else "FP64-accurate fallback")})
-            del A, Aw, Bm, X, R
-        del U, V
+        # ---- ill-conditioned DGESV (GMRES-IR): A = U diag(logspace(0,-kappa)) V^T, U and
+        # V the Q factors of seeded uniform matrices (QR on the device); N = 32768 is left
+        # out, as its two FP64 QRs alone would take minutes
+        for n in (4096, 8192, 16384):
+            U, _ = torch.linalg.qr(urand((n, n), 121))
+            V, _ = torch.linalg.qr(urand((n, n), 122))
+            for kappa in (4, 8, 12):
+                sv = torch.logspace(0.0, -float(kappa), n, dtype=torch.float64, device="cuda")
+                A = ((U * sv) @ V.T).T.contiguous()  # column-major buffer of A
+                Aw = A.clone()  # the FP64 fallback overwrites its A with the LU factors
+                Bm = urand((1, n), 95)
+                X = torch.zeros_like(Bm)
+                p2 = torch.zeros(n, dtype=torch.int32, device="cuda")
+                it, info = C.c_int(0), C.c_int(0)
+                torch.cuda.synchronize()
+                t0 = time.perf_counter()
+                check(lib.gb_dsgesv_dev(n, 1, Aw.data_ptr(), n, p2.data_ptr(), Bm.data_ptr(), n,
+                                        X.data_ptr(), n, C.byref(it), C.byref(info)))
+                torch.cuda.synchronize()
+                t_mixed = time.perf_counter() - t0
+                R = Bm.clone()
+                check(lib.gb_dgemm_native_dev(b"N", b"N", n, 1, n, -1.0, A.data_ptr(), n,
+                                              X.data_ptr(), n, 1.0, R.data_ptr(), n))
+                torch.cuda.synchronize()
+                anorm = float(A.abs().sum(dim=0).max())
+                berr = float(R.abs().max() / (anorm * X.abs().max() + Bm.abs().max()))
+                _emit({"suite": f"dgesv_illcond_{n}_kappa1e{kappa}",
+                       "workload": f"DGESV N={n} NRHS=1, A = U diag(logspace(0,-{kappa})) V^T "
+                                   "(U, V: Q factors of seeded uniform matrices)",
+                       "ms": t_mixed * 1e3, "iter": it.value, "info": info.value,
+                       "backward_error_eps": berr / eps, "bound_n_eps": n,
+                       "path": "FP32 LU + IR" if 0 <= it.value <= 30 else
+                               ("GMRES-IR" if it.value >= 100 else "FP64-accurate fallback")})
+                del A, Aw, Bm, X, R
+            del U, V
+            torch.cuda.empty_cache()
 
     if want("dpotrf"):
         # ---- DPOTRF N=32768, A = B B^T / N + I (B uniform), native and emulated updates
