@@ -1341,17 +1341,29 @@ void a_side_stats(bool kcontig, int64_t R, int64_t K, const double *X, int64_t l
 }
 
 // Automatic choice, op(B) side: exponents and FP32 column statistics of
-// op(B), then the scheme (and slice count) of every 256-column tile.
+// op(B), then the scheme (and slice count) of every 256-column tile.  With
+// mx_a / ea_a (op(B) = op(A)^T over the same K segment, R rows of op(A)):
+// op(B)'s column maxima and exponents are op(A)'s row ones, copied instead
+// of read again from the operand.
 void choose_b(bool kcontig, int64_t R, int64_t K, const double *X, int64_t ld, int64_t Rpad,
               unsigned long long *mx, int *expo, const float *alpha, const double *totals,
               float *s1, float *s2, double budget_mod, double budget_dig, int mod_t,
-              int *s_tiles, int *pass, cudaStream_t s) {
+              int *s_tiles, int *pass, cudaStream_t s,
+              const unsigned long long *mx_a = nullptr, const int *ea_a = nullptr) {
   cudaMemsetAsync(pass, 0, 2 * sizeof(int), s);
   if (kcontig) {
     { col_stats_kcontig_kernel<<<(unsigned)((Rpad + 7) / 8), 256, 0, s>>>(R, Rpad, K, X, ld, alpha,
                                                                           mx, expo, s1, s2); count_launch(); }
   } else {
-    operand_exponents(false, R, K, X, ld, Rpad, mx, expo, s);
+    if (mx_a) {
+      // the values operand_exponents gives: zero maxima and exponents past R
+      cudaMemsetAsync(mx, 0, sizeof(unsigned long long) * Rpad, s);
+      cudaMemsetAsync(expo, 0, sizeof(int) * Rpad, s);
+      cudaMemcpyAsync(mx, mx_a, sizeof(unsigned long long) * R, cudaMemcpyDeviceToDevice, s);
+      cudaMemcpyAsync(expo, ea_a, sizeof(int) * R, cudaMemcpyDeviceToDevice, s);
+    } else {
+      operand_exponents(false, R, K, X, ld, Rpad, mx, expo, s);
+    }
     cudaMemsetAsync(s1, 0, sizeof(float) * Rpad, s);
     cudaMemsetAsync(s2, 0, sizeof(float) * Rpad, s);
     const int64_t kspan = 256;
@@ -1681,7 +1693,8 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
         continue;
       }
       choose_b(tb == 0, jn, kk, Bk, ldbj, jn_pad, mx + m_pad, eb, a.alpha, a.tot, st_s1, st_s2,
-               budget_mod, budget_dig, mod_t, s_tiles, pass, s);
+               budget_mod, budget_dig, mod_t, s_tiles, pass, s, b_from_a ? mx : nullptr,
+               b_from_a ? a.ea : nullptr);
       if (modular) {
         // ---- modular pass (tiles with s_tiles = 0)
         if (!a_both && (st = split_a_mod(sg, k0, kk, pass))) return st;
