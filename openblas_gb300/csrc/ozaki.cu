@@ -1639,10 +1639,11 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       const double *Bk = tb ? Bj + k0 * ldbj : Bj + k0;
       const double bseg = sg == 0 ? beta : 1.0;  // later segments accumulate
       // recombination grid: one CTA per tile and column chunk, the tiles
-      // split into up to 16 chunks until there are 16 CTAs per SM (about
-      // four waves: a short last wave costs little)
+      // split into up to 64 chunks (of 4 columns) until there are 16 CTAs
+      // per SM (about four waves: a short last wave costs little); a small C
+      // then gets a column per thread instead of a chain of several
       dim3 g((unsigned)((m + BM - 1) / BM), (unsigned)((jn + BN - 1) / BN), 1);
-      while (g.z < 16 && (int64_t)g.x * g.y * g.z < 16LL * persistent_ctas()) g.z *= 2;
+      while (g.z < 64 && (int64_t)g.x * g.y * g.z < 16LL * persistent_ctas()) g.z *= 2;
       const int m_tiles = (int)(m_pad / BM);
       const int64_t ps = m_pad * jn_pad;
       if (fixed_mod) {
