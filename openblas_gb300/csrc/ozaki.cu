@@ -1559,12 +1559,30 @@ int emulated_product(int ta, int tb, int64_t m, int64_t n, int64_t k, double alp
       gp.mod_magic[l] = (uint32_t)(((1ull << 40) + MODULI[l] - 1) / MODULI[l]);
     }
     const int ntiles = gp.m_tiles * gp.n_tiles;
-    // fewer tiles than CTAs: split each tile's levels over idle CTAs
+    // fewer tiles than CTAs: split each tile's levels over idle CTAs.  Digit
+    // slices: as many groups as there are idle CTAs per tile.  Modular (14
+    // equal levels): the group count with the fewest levels per CTA, units
+    // beyond one wave included (32 tiles: 14 groups, 3 levels per CTA, where
+    // one wave of 4 groups left 4); ties keep fewer groups.
     const int maxl = mod ? MOD_COUNT : Sa;
-    const int spare = persistent_ctas() / ntiles;
-    gp.level_groups = spare < 1 ? 1 : (spare > maxl ? maxl : spare);
+    const int pc = persistent_ctas();
+    gp.level_groups = 1;
+    if (ntiles < pc && mod) {
+      int64_t best = INT64_MAX;
+      for (int gc = 1; gc <= maxl; ++gc) {
+        const int64_t units = (int64_t)ntiles * gc;
+        const int64_t per_cta = ((units + pc - 1) / pc) * ((maxl + gc - 1) / gc);
+        if (per_cta < best) {
+          best = per_cta;
+          gp.level_groups = gc;
+        }
+      }
+    } else if (ntiles < pc) {
+      const int spare = pc / ntiles;
+      gp.level_groups = spare > maxl ? maxl : spare;
+    }
     const int nunits = ntiles * gp.level_groups;
-    const int grid = nunits < persistent_ctas() ? nunits : persistent_ctas();
+    const int grid = nunits < pc ? nunits : pc;
     if (mod) {
       ProfileScope prof("residue_gemm", s);
       slice_gemm_kernel<true><<<grid, NUM_THREADS, SMEM_BYTES, s>>>(ma, mb, gp);
